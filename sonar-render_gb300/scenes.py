@@ -1,0 +1,210 @@
+"""Synthetic scenes for the discrete Kirchhoff path (numpy only).
+
+Triangle arrays are float32 of shape (n, 9): v1, v2, v3 per triangle, the
+layout ``load_geometry`` takes (python_interface.cpp:26-41).  The winding sets
+the scattering side: the reference's normal is unit((v2-v1) x (v3-v1))
+(Facet.cpp:95-109).
+
+The workloads below are the benchmark configurations of this path, restated
+as seeded synthetic inputs of the same shapes and sizes:
+
+* ``plate_config``      1.0 x 0.5 m plate, 10 kHz, one source, 64 x 64 field grid
+* ``sphere_config``     r = 1 m icosphere (subdivision 4), 20 kHz, source at 10 m,
+                        field plane through the centre
+* ``trihedral_config``  orthogonal trihedral, 1 m legs, 3 bounces at 40 kHz
+                        (60 kHz, 2 bounces for the compression workload)
+
+Mesh helpers mirror the reference's run_scripts/modules/geo.py builders
+(make_rectangle, halve_facets, make_cube, generate_field_points) without
+numpy-stl / trimesh, and ``read_stl`` reads binary STL files.
+"""
+from __future__ import annotations
+
+import math
+import struct
+
+import numpy as np
+
+CP_WATER = 1480.0
+
+
+def delta_for(frequency, cp=CP_WATER, per_wavelength=7.5):
+    """Fragment side of lambda / 7.5, the convention of the reference scripts."""
+    return (cp / frequency) / per_wavelength
+
+
+# ---------------------------------------------------------------- meshes
+def plate_1x05():
+    """The 1.0 x 0.5 m plate in z = 0, normal +z (two triangles)."""
+    return np.array([[-0.5, -0.25, 0.0, 0.5, -0.25, 0.0, 0.5, 0.25, 0.0],
+                     [-0.5, -0.25, 0.0, 0.5, 0.25, 0.0, -0.5, 0.25, 0.0]], np.float32)
+
+
+def rectangle(width, height, z=0.0, normal_up=True):
+    """Axis-aligned rectangle centred at the origin in the plane z (two triangles)."""
+    w, h = width / 2.0, height / 2.0
+    a, b, c, d = (-w, -h, z), (w, -h, z), (w, h, z), (-w, h, z)
+    if normal_up:
+        t = [a + b + c, a + c + d]
+    else:
+        t = [a + c + b, a + d + c]
+    return np.array(t, np.float32)
+
+
+def halve_facets(tris):
+    """Split every triangle into four through its edge midpoints (geo.py:158-196)."""
+    t = np.asarray(tris, np.float64).reshape(-1, 3, 3)
+    a, b, c = t[:, 0], t[:, 1], t[:, 2]
+    ab, bc, ca = (a + b) / 2, (b + c) / 2, (c + a) / 2
+    out = np.stack([np.stack([a, ab, ca], 1), np.stack([ab, b, bc], 1),
+                    np.stack([ca, bc, c], 1), np.stack([ab, bc, ca], 1)], 1)
+    return out.reshape(-1, 9).astype(np.float32)
+
+
+def box(sx, sy, sz, center=(0.0, 0.0, 0.0)):
+    """Closed box with outward normals (12 triangles)."""
+    x0, y0, z0 = (np.asarray(center) - np.array([sx, sy, sz]) / 2).tolist()
+    x1, y1, z1 = x0 + sx, y0 + sy, z0 + sz
+    v = np.array([[x0, y0, z0], [x1, y0, z0], [x1, y1, z0], [x0, y1, z0],
+                  [x0, y0, z1], [x1, y0, z1], [x1, y1, z1], [x0, y1, z1]])
+    quads = [(0, 3, 2, 1), (4, 5, 6, 7), (0, 1, 5, 4), (2, 3, 7, 6), (1, 2, 6, 5), (3, 0, 4, 7)]
+    tris = []
+    for q in quads:
+        tris.append(np.concatenate([v[q[0]], v[q[1]], v[q[2]]]))
+        tris.append(np.concatenate([v[q[0]], v[q[2]], v[q[3]]]))
+    return np.array(tris, np.float32)
+
+
+def icosphere(subdivisions=4, radius=1.0, center=(0.0, 0.0, 0.0)):
+    """Icosphere with outward normals: 20 * 4**subdivisions triangles."""
+    p = (1.0 + 5 ** 0.5) / 2
+    verts = [(-1, p, 0), (1, p, 0), (-1, -p, 0), (1, -p, 0), (0, -1, p), (0, 1, p),
+             (0, -1, -p), (0, 1, -p), (p, 0, -1), (p, 0, 1), (-p, 0, -1), (-p, 0, 1)]
+    verts = [np.array(v, np.float64) / np.linalg.norm(v) for v in verts]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+             (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8),
+             (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdivisions):
+        cache = {}
+
+        def mid(i, j):
+            key = (min(i, j), max(i, j))
+            if key not in cache:
+                m = verts[i] + verts[j]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    V = np.array(verts) * radius + np.asarray(center, np.float64)
+    F = np.array(faces)
+    tris = np.concatenate([V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]], axis=1)
+    # orient outward: (v2-v1) x (v3-v1) along the centroid direction
+    t = tris.reshape(-1, 3, 3)
+    n = np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0])
+    outward = np.einsum("ij,ij->i", n, t.mean(1) - np.asarray(center)) > 0
+    t[~outward] = t[~outward][:, [0, 2, 1]]
+    return t.reshape(-1, 9).astype(np.float32)
+
+
+def trihedral(leg=1.0):
+    """Orthogonal trihedral corner reflector: three right triangles with legs
+    ``leg`` along +x, +y, +z from the origin corner; normals point into the
+    octant (the reflecting side)."""
+    L = float(leg)
+    return np.array([[0, 0, 0, L, 0, 0, 0, L, 0],     # z = 0, normal +z
+                     [0, 0, 0, 0, L, 0, 0, 0, L],     # x = 0, normal +x
+                     [0, 0, 0, 0, 0, L, L, 0, 0]],    # y = 0, normal +y
+                    np.float32)
+
+
+def read_stl(path):
+    """Binary STL -> (n, 9) float32 triangles (normals in the file are ignored)."""
+    with open(path, "rb") as fh:
+        data = fh.read()
+    n = struct.unpack_from("<I", data, 80)[0]
+    rec = np.frombuffer(data, dtype=np.uint8, count=n * 50, offset=84).reshape(n, 50)
+    return np.ascontiguousarray(rec[:, 12:48]).view("<f4").reshape(n, 9).astype(np.float32)
+
+
+def translate(tris, offset):
+    t = np.asarray(tris, np.float32).reshape(-1, 3, 3) + np.asarray(offset, np.float32)
+    return t.reshape(-1, 9)
+
+
+def rotate(tris, axis, degrees):
+    """Rotate about a coordinate axis through the origin (geo.py:414-446)."""
+    a = math.radians(degrees)
+    c, s = math.cos(a), math.sin(a)
+    R = {"x": [[1, 0, 0], [0, c, -s], [0, s, c]],
+         "y": [[c, 0, s], [0, 1, 0], [-s, 0, c]],
+         "z": [[c, -s, 0], [s, c, 0], [0, 0, 1]]}[axis]
+    t = np.asarray(tris, np.float64).reshape(-1, 3, 3) @ np.array(R).T
+    return t.reshape(-1, 9).astype(np.float32)
+
+
+# ---------------------------------------------------------------- points
+def grid_xy(n, half, z):
+    """n x n points on [-half, half]^2 in the plane z (row-major in y then x)."""
+    g = np.linspace(-half, half, n)
+    X, Y = np.meshgrid(g, g)
+    return np.stack([X.ravel(), Y.ravel(), np.full(X.size, z)], 1).astype(np.float32)
+
+
+def arc_xz(radius, angles_deg):
+    """Points on an arc in the xz-plane (geo.py:64-73 generate_field_points)."""
+    a = np.radians(np.asarray(angles_deg, np.float64))
+    return np.stack([radius * np.sin(a), np.zeros_like(a), radius * np.cos(a)], 1).astype(np.float32)
+
+
+def hemisphere(n_theta, n_phi, radius, axis=(1.0, 1.0, 1.0), center=(0.0, 0.0, 0.0)):
+    """n_theta x n_phi points on the hemisphere of given radius around ``axis``."""
+    ax = np.asarray(axis, np.float64)
+    ax = ax / np.linalg.norm(ax)
+    tmp = np.array([1.0, 0.0, 0.0]) if abs(ax[0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+    u = np.cross(ax, tmp)
+    u /= np.linalg.norm(u)
+    w = np.cross(ax, u)
+    th = (np.arange(n_theta) + 0.5) / n_theta * (math.pi / 2)
+    ph = np.arange(n_phi) / n_phi * 2 * math.pi
+    T, P = np.meshgrid(th, ph, indexing="ij")
+    d = (np.cos(T)[..., None] * ax + np.sin(T)[..., None] * (np.cos(P)[..., None] * u + np.sin(P)[..., None] * w))
+    return (np.asarray(center) + radius * d.reshape(-1, 3)).astype(np.float32)
+
+
+# ---------------------------------------------------------------- workloads
+def plate_config():
+    """Plate, 10 kHz, source at (0, 0, 5), 64 x 64 field points at z = 3."""
+    f = 10e3
+    return dict(name="plate_1x0.5m_10kHz", frequency=f, cp=CP_WATER, attenuation=0.0,
+                targets=[(plate_1x05(), delta_for(f))], fields=[],
+                sources=np.array([[0.0, 0.0, 5.0]], np.float32),
+                field_points=grid_xy(64, 1.0, 3.0), bounces=0)
+
+
+def sphere_config(field_points_side=512, field_surface=True):
+    """Icosphere (r = 1 m, 5,120 triangles), 20 kHz, source at 10 m on +z;
+    readout onto the 4 x 4 m field plane x = 0 through the centre."""
+    f = 20e3
+    plane = np.array([[0, -2, -2, 0, 2, -2, 0, 2, 2], [0, -2, -2, 0, 2, 2, 0, -2, 2]], np.float32)
+    fields = [(plane, 4.0 / field_points_side)] if field_surface else []
+    g = np.linspace(-2, 2, field_points_side)
+    Y, Z = np.meshgrid(g, g)
+    fp = np.stack([np.zeros(Y.size), Y.ravel(), Z.ravel()], 1).astype(np.float32)
+    return dict(name="icosphere_r1m_20kHz", frequency=f, cp=CP_WATER, attenuation=0.0,
+                targets=[(icosphere(4, 1.0), delta_for(f))], fields=fields,
+                sources=np.array([[0.0, 0.0, 10.0]], np.float32),
+                field_points=None if field_surface else fp, bounces=0)
+
+
+def trihedral_config(frequency=40e3, bounces=3, n_theta=256, n_phi=256):
+    """Trihedral (1 m legs), source at 20 m on the (1,1,1) diagonal, bounces,
+    readout to an n_theta x n_phi hemisphere of radius 2 m."""
+    src = (20.0 / math.sqrt(3.0)) * np.ones((1, 3), np.float32)
+    return dict(name="trihedral_1m_%dkHz_%db" % (int(frequency / 1e3), bounces), frequency=frequency,
+                cp=CP_WATER, attenuation=0.0, targets=[(trihedral(1.0), delta_for(frequency))], fields=[],
+                sources=src, field_points=hemisphere(n_theta, n_phi, 2.0), bounces=bounces)
