@@ -1,0 +1,152 @@
+/*
+ * sonar_render.h -- C ABI of the GB300 discrete Kirchhoff library
+ * (libsonar_gb300.so, also shipped as build/libcuda_project.so).
+ *
+ * The first block keeps the reference's python_interface symbols and
+ * signatures so existing ctypes callers (run_scripts/modules/api.py:4-111)
+ * load this library unchanged.  Each declaration cites the reference entry
+ * point it replaces (src/python_interface.cpp).  Like the reference they
+ * return void; unlike the reference they never throw across the boundary:
+ * an error is recorded (sonar_status / sonar_last_error) and the call, and
+ * every later projection until TearDownCuda, does nothing.
+ *
+ * The second block is additive: status, headless surface-pressure read-back
+ * (the reference only exposes surfaces through GL textures,
+ * src/FacetCuda.cu:74-85), fragment layout, statistics, options and the
+ * interaction mask (test/diagnostic use).
+ *
+ * Pointers are plain host pointers; sizes are element counts.  The library
+ * owns all device memory (freed by TearDownCuda).  Calls are synchronous and
+ * not thread-safe, as in the reference (one process-global model,
+ * src/python_interface.cpp:11).
+ */
+#ifndef SONAR_RENDER_H
+#define SONAR_RENDER_H
+
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Complex pressure, two doubles (src/dcomplex.h:12-15). */
+typedef struct DCOMPLEX {
+    double r, i;
+} dcomplex;
+
+/* ---- reference entry points (src/python_interface.cpp) ------------------ */
+
+/* :21-24 -- k = (float)(2*pi*f) / cp, attenuation is the imaginary part of k
+ * in Np/m (src/Model.cpp:44-54); density is stored and unused. */
+void set_initial_conditions(float cp, float frequency, float attenuation, float density);
+
+/* :26-41 -- num_vertices counts TRIANGLES (9 floats each: v1 v2 v3);
+ * objectType 0 target, 1 source (stored, unused), 2 field surface;
+ * resolution is the fragment side delta in metres. */
+void load_geometry(float *v1, int num_vertices, int objectType, float resolution);
+
+/* :43-50 -- xyz triples; field point pressures start at 0 and accumulate. */
+void load_field_points(float *v1, int num_feild_points);
+
+/* :52-59 -- xyz triples; every source has pressure 1 + 0i (src/Model.cpp:16-19). */
+void load_source_points(float *v1, int num_source_points);
+
+/* :61-65 -- fragment every target and field facet (src/Facet.cpp:111-339),
+ * build the occluder BVH over all target triangles (replaces the OptiX GAS,
+ * src/OptiX.cpp:264-350) and upload the scene.  No projection runs here. */
+void render_cuda(void);
+
+/* :67-70 -- source points -> every target object (and every field object when
+ * projectFieldObjects), src/ModelCuda.cpp:242-278, src/OptiX.cu:35-110. */
+void ProjectSrcPointsToObjects(bool projectFieldObjects);
+
+/* :72-75 -- target objects -> field objects (FACET_NO_RESP),
+ * src/ModelCuda.cpp:280-301, src/OptiX.cu:192-406. */
+void ProjectTargetToFieldObjects(void);
+
+/* :77-80 -- target objects -> field points, src/ModelCuda.cpp:302-321,
+ * src/OptiX.cu:112-190. */
+void ProjectTargetToFieldPoints(void);
+
+/* :82-85 -- number_reflections fragment -> fragment bounces per target object
+ * (FACET_SELF with reciprocity), src/ModelCuda.cpp:323-356. */
+void ProjectTargetToTargetObjects(int number_reflections);
+
+/* :87-90 -- copy the field point pressures (load order).  The reference copies
+ * every loaded point whatever NumPoints says (src/ModelCuda.cpp:203-208); this
+ * copies min(NumPoints, loaded) and records an error when NumPoints is short. */
+void GetFieldPointPressures(dcomplex *field_points_pressure, int NumPoints);
+
+/* :92-96 -- GL/EGL rendering is not available (no graphics stack): records the
+ * reason in sonar_last_error (without making it a pending error) and returns.
+ * Surface pressures are read with sonar_get_object_pressures. */
+void RenderOpenGL(int width, int height, char *filename, float viewSettings[9]);
+
+/* :98-101 -- free all device memory, drop target/field objects and points
+ * (src/Model.cpp:115-129, src/ModelCuda.cpp:124-181) and clear the error. */
+void TearDownCuda(void);
+
+/* :103-107 -- store the dB window and phase flags used by surface colouring. */
+void SoundVisualisationInit(float maxDbValue, float minDbValue, bool renderPhaseTarget, bool renderPhaseField);
+
+/* ---- additive entry points ---------------------------------------------- */
+
+/* 0 when no error is pending, else a negative code. */
+int sonar_status(void);
+/* Message of the pending error ("" when none). */
+const char *sonar_last_error(void);
+/* Clear a pending error (loads and projections run again). */
+void sonar_clear_error(void);
+
+/* Number of loaded objects of a type (0 target, 1 source, 2 field). */
+int sonar_get_object_count(int objectType);
+/* Cells of an object after render_cuda: sum over facets of numXpnts*numYpnts. */
+long long sonar_get_object_cells(int objectType, int objIdx);
+/* Total pressure P of every cell of a target or field object: facet-major,
+ * each facet row-major y*numXpnts + x (src/OptiX.cu:49).  n is the capacity
+ * in dcomplex; returns the number written or a negative code. */
+int sonar_get_object_pressures(int objectType, int objIdx, dcomplex *out, long long n);
+/* Fragment layout of an object: 3 ints per facet (numXpnts, numYpnts,
+ * numXpntsNegative, src/Facet.cpp:124-127) and the FP32 cell areas in the
+ * same order as the pressures.  Returns the number of facets or < 0. */
+int sonar_get_fragment_layout(int objectType, int objIdx, int *nx_ny_neg, int nfacets_cap, float *areas,
+                              long long ncells_cap);
+/* JSON statistics of the last projection calls (pairs, kernel ms, grazing). */
+int sonar_get_stats(char *json, int cap);
+/* Options: "split" (source splits of the sum kernels, 0 = automatic),
+ * "verbose" (0/1), "reset_stats", "reset_pressures" (zero every surface and
+ * field-point pressure), "drop_masks" (free the cached interaction masks; the
+ * next projection rebuilds them).  Returns 0, or < 0 for an unknown key or a
+ * failed action. */
+int sonar_set_option(const char *key, double value);
+/* The library's CUDA stream (a cudaStream_t; NULL before render_cuda), for
+ * callers that time or order work against it. */
+void *sonar_get_stream(void);
+/* Throughput probe of the current device for roofline denominators:
+ * which = 0 FP32 fused multiply-add rate in FLOP/s, which = 1 MUFU (sine)
+ * rate in op/s.  Runs for a few milliseconds; < 0 on failure. */
+double sonar_measure_peak(int which);
+/* Interaction mask of one hop, for diagnostics: one byte per (destination,
+ * source) pair, destination-major, 1 when the pair passes the area, cosine
+ * and visibility gates.  hop 0 sources -> cells of object dstIdx of type
+ * srcIdx (0 target, 2 field); hop 1 active cells of target srcIdx -> field
+ * points; hop 2 active cells of target srcIdx -> themselves; hop 3 active
+ * cells of target srcIdx -> active cells of field object dstIdx.  Returns
+ * the number of bytes (ndst*nsrc), or < 0.  The mask is built if needed. */
+long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, long long cap);
+
+/* Host only (no GPU needed): frame and clipped area grid of one triangle
+ * (src/Facet.cpp:6-339).  nx_ny_neg gets numXpnts, numYpnts,
+ * numXpntsNegative; frame17 gets normal(3) base point(3) xAxis(3) yAxis(3)
+ * BaseLength Height BaseLengthNeg BaseLengthPos Area; areas (row-major
+ * y*numXpnts + x) is written when cap holds every cell.  Returns the cell
+ * count, or < 0 for invalid arguments. */
+long long sonar_fragment_triangle(const float *tri9, float delta, int *nx_ny_neg, float *frame17, float *areas,
+                                  long long cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

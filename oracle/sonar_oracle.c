@@ -515,9 +515,14 @@ static void build_occluders(scene_t *s)
 }
 
 /* Tolerances of the visibility classification; see the header comment. */
-#define VIS_TOL_D_REL 1e-6   /* plane distances */
-#define VIS_TOL_T_REL 2e-6   /* crossing distance vs tmax */
-#define VIS_TOL_E_REL 2e-6   /* crossing point vs triangle edges */
+/* The tolerances bound the error of an FP32 evaluation of the same quantities
+ * at coordinate scale sc: a plane distance n.x - c from FP32 n, c and x has an
+ * error of a few units in the last place of sc (~2e-7 sc); the crossing
+ * distance and the edge distances of the crossing point add one rounding of
+ * the segment parameter. */
+#define VIS_TOL_D_REL 4e-7   /* plane distances */
+#define VIS_TOL_T_REL 1e-6   /* crossing distance vs tmax */
+#define VIS_TOL_E_REL 1e-6   /* crossing point vs triangle edges */
 #define VIS_EPS_PLANE_REL 1e-4 /* origin-plane exclusion */
 
 static int seg_box(const double o[3], const double d[3], const double lo[3], const double hi[3])
@@ -560,10 +565,11 @@ static int tri_verdict(const otri_t *t, const double o[3], const double e[3], do
         const double den = ad0 + ad1;
         const double sp = den > 0.0 ? ad0 / den : 0.0;
         const double tc = r * sp;
-        /* bounds of the crossing distance when d0, d1 move by tol_d */
-        const double t_lo = (ad0 > tol_d) ? r * (ad0 - tol_d) / (den + 2.0 * tol_d) : 0.0;
-        const double den_hi = den - 2.0 * tol_d;
-        const double t_hi = (den_hi > ad0 + tol_d) ? r * (ad0 + tol_d) / den_hi : r;
+        /* bounds of the crossing distance t = r a0 / (a0 + a1) when |d0|, |d1|
+         * move by tol_d (t grows with a0 and shrinks with a1) */
+        const double t_lo = (ad0 > tol_d) ? r * (ad0 - tol_d) / den : 0.0;
+        const double a1_lo = ad1 > tol_d ? ad1 - tol_d : 0.0;
+        const double t_hi = r * (ad0 + tol_d) / (ad0 + tol_d + a1_lo);
         double X[3], gmin = 1e300;
         for (int k = 0; k < 3; k++) X[k] = o[k] + (e[k] - o[k]) * sp;
         for (int q = 0; q < 3; q++) {

@@ -1,0 +1,265 @@
+// geometry.cpp -- facet frames, fragment grids and the occluder BVH.
+//
+// The frame and the area grid must reproduce the reference's FP32 results bit
+// for bit (src/Facet.cpp:6-339, src/GeoMath.h:19-106), so every expression
+// keeps the reference's operation order; build with -ffp-contract=off.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "host.h"
+
+namespace sonar {
+namespace {
+
+inline Vec3 sub(Vec3 a, Vec3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline float dot3(Vec3 a, Vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline float len3(Vec3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+inline Vec3 unit3(Vec3 a)
+{
+    const float L = len3(a);
+    return {a.x / L, a.y / L, a.z / L};
+}
+inline Vec3 cross3(Vec3 a, Vec3 b)
+{
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+}  // namespace
+
+FacetFrame make_frame(Vec3 v1, Vec3 v2, Vec3 v3, float delta)
+{
+    FacetFrame f;
+    f.v1 = v1;
+    f.v2 = v2;
+    f.v3 = v3;
+    f.delta = delta;
+    // normal = unit((v1 - v2) x (v1 - v3)) == unit((v2 - v1) x (v3 - v1))
+    f.normal = unit3(cross3(sub(v1, v2), sub(v1, v3)));
+
+    // the longest edge (first maximum wins) is the base, running origin -> end;
+    // the remaining vertex is the apex
+    const float e[3] = {len3(sub(v1, v2)), len3(sub(v1, v3)), len3(sub(v2, v3))};
+    int m = 0;
+    if (e[1] > e[m]) m = 1;
+    if (e[2] > e[m]) m = 2;
+    const Vec3 origin = (m == 2) ? v2 : v1;
+    const Vec3 end = (m == 0) ? v2 : v3;
+    const Vec3 apex = (m == 0) ? v3 : (m == 1) ? v2 : v1;
+
+    const Vec3 along = sub(end, origin);
+    const Vec3 u = unit3(along);
+    const float proj = dot3(u, sub(apex, origin));
+    f.base = {origin.x + u.x * proj, origin.y + u.y * proj, origin.z + u.z * proj};
+    const Vec3 alt = sub(apex, f.base);
+
+    f.baseLen = e[m];
+    f.height = len3(alt);
+    f.baseNeg = len3(sub(origin, f.base));
+    f.basePos = len3(sub(f.base, end));
+    f.xAxis = u;
+    f.yAxis = unit3(alt);
+    f.area = (f.baseLen * f.height) / 2.0f;
+
+    const float cn = std::ceil(std::fabs(f.baseNeg) / delta);
+    const float cp = std::ceil(std::fabs(f.basePos) / delta);
+    const float cy = std::ceil(f.height / delta);
+    // a triangle whose frame is not finite (coincident vertices) gets no cells;
+    // a zero-height one gets numYpnts = 0 as in the reference
+    if (!std::isfinite(cn) || !std::isfinite(cp) || !std::isfinite(cy)) {
+        f.nx = f.ny = f.neg = 0;
+    } else {
+        f.neg = (int)cn;
+        f.nx = f.neg + (int)cp;
+        f.ny = (int)cy;
+    }
+    return f;
+}
+
+void fragment_areas(const FacetFrame &f, float *area)
+{
+    const int nx = f.nx, ny = f.ny, neg = f.neg;
+    const float d = f.delta, H = f.height, h = d / 2;
+    std::fill(area, area + (size_t)nx * ny, 0.0f);
+    // slopes of the two sloping sides: x > 0 is the positive-base side
+    const float mPos = H / (-f.basePos);
+    const float mNeg = H / (f.baseNeg);
+    std::vector<unsigned char> inL(ny + 1), inR(ny + 1);
+
+    for (int i = 0; i < nx; i++) {
+        const float xc = ((float)(i - neg) * d) + h;  // column centre
+        const float xL = xc - h, xR = xc + h;
+        const bool pos = xc > 0;
+        const float m = pos ? mPos : mNeg;
+        const float yL = m * xL + H;  // side line at the column's left and right edges
+        const float yR = m * xR + H;
+        for (int j = 0; j <= ny; j++) {
+            inL[j] = d * (float)j <= yL;
+            inR[j] = d * (float)j <= yR;
+        }
+        for (int j = 0; j < ny; j++) {
+            const bool lb = inL[j], rb = inR[j], lt = inL[j + 1], rt = inR[j + 1];
+            float *A = area + (size_t)j * nx + i;
+            if (!lb && !rb && !lt && !rt) break;  // above the triangle: rest of column empty
+            if (lb && rb && lt && rt) {
+                *A = d * d;
+                continue;
+            }
+            const float yB = d * (float)j;
+            if (pos) {
+                const float yT = d * (float)(j + 1);
+                if (lb && rb && lt && !rt) {
+                    const float xTop = (yT - H) / mPos;
+                    *A = d * d - (yT - yR) * (xR - xTop) / 2;
+                } else if (lb && rb && !lt && !rt) {
+                    *A = ((yL - yR) * d / 2) + (yR - yB) * d;
+                } else if (lb && !rb && lt && !rt) {
+                    const float xTop = ((yT - H) / mPos) - xL;
+                    const float xBot = ((yB - H) / mPos) - xL;
+                    *A = (xTop * d) + (xBot - xTop) * d / 2;
+                } else if (lb && !rb && !lt && !rt) {
+                    *A = (yL - yB) * (((yB - H) / mPos) - xL) / 2;
+                }
+            } else {
+                const float yc = ((float)j * d) + h;  // row centre
+                if (lb && rb && !lt && rt) {
+                    *A = d * d - (yc + h - yL) * (-(xL - ((yc + h - H) / mNeg)) / 2);
+                } else if (lb && rb && !lt && !rt) {
+                    *A = (yR - yL) * d / 2 + ((yL - (yc - h)) * d);
+                } else if (!lb && rb && !lt && rt) {
+                    *A = -((yc - h - H) / mNeg - (yc + h - H) / mNeg) * d / 2 - (((yc + h - H) / mNeg) - xR) * d;
+                } else if (!lb && rb && !lt && !rt) {
+                    *A = (yR - (yc - h)) * (-((((yc - h) - H) / mNeg) - xR)) / 2;
+                }
+            }
+        }
+    }
+}
+
+Vec3 fragment_centroid(const FacetFrame &f, int x, int y, bool source_hop)
+{
+    const float d = f.delta;
+    float xo = d * (float)(x - f.neg);
+    if (source_hop) xo = xo + d / 2;
+    const float yo = d * (float)y + d / 2;
+    const Vec3 xa = {f.xAxis.x * xo, f.xAxis.y * xo, f.xAxis.z * xo};
+    const Vec3 ya = {f.yAxis.x * yo, f.yAxis.y * yo, f.yAxis.z * yo};
+    return {(f.base.x + xa.x) + ya.x, (f.base.y + xa.y) + ya.y, (f.base.z + xa.z) + ya.z};
+}
+
+// ---------------------------------------------------------------- BVH
+namespace {
+
+struct TriBox {
+    double lo[3], hi[3], c[3];
+};
+
+struct Builder {
+    const std::vector<TriBox> &box;
+    std::vector<int> &order;
+    std::vector<BvhNode> &nodes;
+    double pad;
+    int depth = 0;
+
+    int build(int t0, int tn, int level)
+    {
+        depth = std::max(depth, level);
+        const int id = (int)nodes.size();
+        nodes.push_back(BvhNode{});
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        double clo[3] = {1e300, 1e300, 1e300}, chi[3] = {-1e300, -1e300, -1e300};
+        for (int i = t0; i < t0 + tn; i++) {
+            const TriBox &b = box[order[i]];
+            for (int k = 0; k < 3; k++) {
+                lo[k] = std::min(lo[k], b.lo[k]);
+                hi[k] = std::max(hi[k], b.hi[k]);
+                clo[k] = std::min(clo[k], b.c[k]);
+                chi[k] = std::max(chi[k], b.c[k]);
+            }
+        }
+        BvhNode n{};
+        for (int k = 0; k < 3; k++) {
+            n.lo[k] = (float)(lo[k] - pad);
+            n.hi[k] = (float)(hi[k] + pad);
+        }
+        if (tn <= 4 || level >= 48) {
+            n.left = -(t0 + 1);
+            n.right = tn;
+            nodes[id] = n;
+            return id;
+        }
+        int ax = 0;
+        for (int k = 1; k < 3; k++)
+            if (chi[k] - clo[k] > chi[ax] - clo[ax]) ax = k;
+        const int half = tn / 2;
+        std::nth_element(order.begin() + t0, order.begin() + t0 + half, order.begin() + t0 + tn,
+                         [&](int a, int b) { return box[a].c[ax] < box[b].c[ax]; });
+        const int l = build(t0, half, level + 1);
+        const int r = build(t0 + half, tn - half, level + 1);
+        n.left = l;
+        n.right = r;
+        nodes[id] = n;
+        return id;
+    }
+};
+
+}  // namespace
+
+BvhHost build_bvh(const std::vector<std::array<float, 9>> &tris, double pad)
+{
+    BvhHost out;
+    const int n = (int)tris.size();
+    std::vector<TriBox> box(n);
+    for (int i = 0; i < n; i++) {
+        for (int k = 0; k < 3; k++) {
+            const double a = tris[i][k], b = tris[i][3 + k], c = tris[i][6 + k];
+            box[i].lo[k] = std::min(a, std::min(b, c));
+            box[i].hi[k] = std::max(a, std::max(b, c));
+            box[i].c[k] = 0.5 * (box[i].lo[k] + box[i].hi[k]);
+        }
+    }
+    std::vector<int> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    if (n > 0) {
+        Builder b{box, order, out.nodes, pad};
+        b.build(0, n, 0);
+        out.depth = b.depth;
+    }
+    // triangle records in leaf order: plane (n, c) and the three inward edge
+    // planes (m_k, c_k), computed in double from the FP32 vertices
+    out.tris.resize((size_t)4 * n);
+    for (int q = 0; q < n; q++) {
+        const auto &t = tris[order[q]];
+        const double v[3][3] = {{t[0], t[1], t[2]}, {t[3], t[4], t[5]}, {t[6], t[7], t[8]}};
+        double e1[3], e2[3], nn[3];
+        for (int k = 0; k < 3; k++) {
+            e1[k] = v[1][k] - v[0][k];
+            e2[k] = v[2][k] - v[0][k];
+        }
+        nn[0] = e1[1] * e2[2] - e1[2] * e2[1];
+        nn[1] = e1[2] * e2[0] - e1[0] * e2[2];
+        nn[2] = e1[0] * e2[1] - e1[1] * e2[0];
+        const double L = std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        float4 *rec = &out.tris[(size_t)4 * q];
+        if (!(L > 0.0)) {
+            // degenerate: a plane no segment can cross strictly (d0 = d1 = 0)
+            for (int k = 0; k < 4; k++) rec[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            continue;
+        }
+        for (double &x : nn) x /= L;
+        const double c = nn[0] * v[0][0] + nn[1] * v[0][1] + nn[2] * v[0][2];
+        rec[0] = make_float4((float)nn[0], (float)nn[1], (float)nn[2], (float)c);
+        for (int e = 0; e < 3; e++) {
+            const double *p = v[e], *qv = v[(e + 1) % 3];
+            const double dd[3] = {qv[0] - p[0], qv[1] - p[1], qv[2] - p[2]};
+            double m[3] = {nn[1] * dd[2] - nn[2] * dd[1], nn[2] * dd[0] - nn[0] * dd[2], nn[0] * dd[1] - nn[1] * dd[0]};
+            const double ml = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+            for (double &x : m) x /= ml;
+            const double cm = m[0] * p[0] + m[1] * p[1] + m[2] * p[2];
+            rec[1 + e] = make_float4((float)m[0], (float)m[1], (float)m[2], (float)cm);
+        }
+    }
+    return out;
+}
+
+}  // namespace sonar

@@ -1,0 +1,46 @@
+// host.h -- host-side geometry of the GB300 library: facet frames and
+// fragment grids (bit-identical to the reference's FP32 arithmetic) and the
+// occluder BVH.
+#pragma once
+#include <array>
+#include <vector>
+
+#include "sonar_internal.h"
+
+namespace sonar {
+
+struct Vec3 {
+    float x, y, z;
+};
+
+// Frame of one facet (src/Facet.cpp:6-109): unit normal, the longest edge as
+// the x axis, the foot of the altitude from the opposite vertex as the base
+// point, the unit altitude as the y axis; fragment grid sizes
+// (numXpnts, numYpnts, numXpntsNegative) from src/Facet.cpp:124-127.
+struct FacetFrame {
+    Vec3 v1, v2, v3;
+    Vec3 normal, xAxis, yAxis, base;
+    float baseLen = 0, height = 0, baseNeg = 0, basePos = 0, area = 0, delta = 0;
+    int nx = 0, ny = 0, neg = 0;
+};
+
+FacetFrame make_frame(Vec3 v1, Vec3 v2, Vec3 v3, float delta);
+
+// Clipped fragment areas, row-major y*nx + x (src/Facet.cpp:111-339).
+void fragment_areas(const FacetFrame &f, float *area);
+
+// Fragment centroid of cell (x, y) as the kernels use it: with the +delta/2 x
+// shift for the source hop (src/OptiX.cu:51), without it for the others
+// (src/OptiX.cu:129, :210, :273).
+Vec3 fragment_centroid(const FacetFrame &f, int x, int y, bool source_hop);
+
+struct BvhHost {
+    std::vector<BvhNode> nodes;
+    std::vector<float4> tris;  // 4 per triangle
+    int depth = 0;
+};
+
+// Median-split BVH over triangles (9 floats each), boxes padded by pad.
+BvhHost build_bvh(const std::vector<std::array<float, 9>> &tris, double pad);
+
+}  // namespace sonar

@@ -1,0 +1,891 @@
+// model.cpp -- the process-global scene and the C ABI (include/sonar_render.h).
+//
+// Mirrors the reference's one global Model (src/python_interface.cpp:11) and
+// its call sequence: load_* and set_initial_conditions collect the scene,
+// render_cuda fragments it and uploads it, the Project* calls run the hops
+// synchronously, TearDownCuda frees everything.  Differences by design:
+//   - device memory is structure-of-arrays per object (sonar_internal.h), and
+//     a hop is two kernels (interaction mask + sum) instead of one OptiX launch
+//     per facet;
+//   - masks depend only on geometry, so they are built once per (hop, source,
+//     destination) after render_cuda and reused by later calls (bounces,
+//     frequency changes through set_initial_conditions);
+//   - nothing throws across the ABI: errors set a status and a message, and
+//     calls are skipped until TearDownCuda or sonar_clear_error;
+//   - all work runs on one library stream; each entry point returns after the
+//     stream is idle, as the reference's DoProjection does (OptiX.cpp:163).
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sonar_render.h"
+#include "host.h"
+
+namespace sonar {
+namespace {
+
+constexpr int OBJ_TARGET = 0, OBJ_SOURCE = 1, OBJ_FIELD = 2;
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    throw Error(code, buf);
+}
+
+#define CK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) fail(-10, "%s failed: %s", #call, cudaGetErrorString(e_));          \
+    } while (0)
+
+template <class T>
+T *dalloc(size_t n)
+{
+    void *p = nullptr;
+    if (n == 0) n = 1;
+    CK(cudaMalloc(&p, n * sizeof(T)));
+    return (T *)p;
+}
+
+template <class T>
+void dfree(T *&p)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+struct Object {
+    int type = 0;
+    float delta = 0.0f;
+    std::vector<FacetFrame> facets;
+    // after render
+    std::vector<long long> cell0;
+    long long ncells = 0;
+    std::vector<float> area;
+    std::vector<int> act_cell;
+    std::vector<int> facet_act_end;  // active index one past facet f's last active cell
+    std::vector<long long> facet_nact;
+    // device
+    float4 *d_cell_pos = nullptr;
+    int *d_cell_facet = nullptr;
+    float4 *d_facet_n = nullptr;
+    double2 *d_P = nullptr, *d_Pin = nullptr, *d_Pout = nullptr;
+    float4 *d_act_pos = nullptr;
+    int *d_act_facet = nullptr, *d_act_cell = nullptr, *d_facet_end = nullptr;
+
+    int nact() const { return (int)act_cell.size(); }
+    void free_device()
+    {
+        dfree(d_cell_pos); dfree(d_cell_facet); dfree(d_facet_n); dfree(d_P); dfree(d_Pin); dfree(d_Pout);
+        dfree(d_act_pos); dfree(d_act_facet); dfree(d_act_cell); dfree(d_facet_end);
+    }
+};
+
+struct MaskEntry {
+    int hop, a, b;
+    int nsrc, ndst;
+    MaskView view{};
+    float mask_ms = 0.0f;
+};
+
+struct HopRecord {
+    int hop;
+    long long pairs;
+    float mask_ms;   // interaction mask kernel (0 when the cached mask was reused)
+    float sum_ms;    // sum kernel alone
+    float total_ms;  // pack + sum + finalize
+    int nsplit;
+    int launches;    // kernels launched by this hop, mask included
+};
+
+struct Model {
+    std::vector<std::unique_ptr<Object>> obj[3];
+    std::vector<Vec3> src, fp;
+    float cp = 1480.0f, freq = 0.0f, att = 0.0f, density = 0.0f;
+    double kr = 0.0, ki = 0.0;
+    float max_db = 0.0f, min_db = -100.0f;
+    bool phase_target = false, phase_field = false;
+    bool rendered = false;
+    int status = 0;
+    std::string err;
+    // device
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+    float4 *d_src_pos = nullptr, *d_fp_pos = nullptr;
+    double2 *d_src_P = nullptr, *d_fp_P = nullptr;
+    float4 *d_nodes = nullptr, *d_tris = nullptr;
+    int nnodes = 0, ntri = 0;
+    std::vector<MaskEntry> masks;
+    float4 *d_packA = nullptr, *d_packB = nullptr;
+    size_t pack_cap = 0;
+    double2 *d_partial = nullptr;
+    size_t partial_cap = 0;
+    int *d_limit = nullptr;
+    size_t limit_cap = 0;
+    // options and statistics
+    int opt_split = 0;
+    int verbose = 0;
+    std::vector<HopRecord> log;
+    long long launches = 0, h2d_bytes = 0, d2h_bytes = 0;
+
+    void free_device()
+    {
+        for (int t = 0; t < 3; t++)
+            for (auto &o : obj[t]) o->free_device();
+        dfree(d_src_pos); dfree(d_fp_pos); dfree(d_src_P); dfree(d_fp_P);
+        dfree(d_nodes); dfree(d_tris);
+        for (auto &m : masks) {
+            dfree(m.view.bits);
+            dfree(m.view.flags);
+        }
+        masks.clear();
+        dfree(d_packA); dfree(d_packB); dfree(d_partial); dfree(d_limit);
+        pack_cap = partial_cap = limit_cap = 0;
+        for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3})
+            if (*e) {
+                cudaEventDestroy(*e);
+                *e = nullptr;
+            }
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+        nnodes = ntri = 0;
+    }
+};
+
+Model g;
+
+// ---------------------------------------------------------------- render
+void render_object(Object &o)
+{
+    const int nf = (int)o.facets.size();
+    o.cell0.assign(nf + 1, 0);
+    for (int f = 0; f < nf; f++) o.cell0[f + 1] = o.cell0[f] + (long long)o.facets[f].nx * o.facets[f].ny;
+    o.ncells = o.cell0[nf];
+    if (o.ncells > (1LL << 31) - 1) fail(-3, "object has %lld cells (limit 2^31-1)", o.ncells);
+    o.area.assign((size_t)o.ncells, 0.0f);
+    std::vector<float4> cell_pos((size_t)o.ncells);
+    std::vector<int> cell_facet((size_t)o.ncells);
+    std::vector<float4> facet_n(std::max(nf, 1));
+    std::vector<float4> act_pos;
+    std::vector<int> act_facet;
+    o.act_cell.clear();
+    o.facet_act_end.assign(std::max(nf, 1), 0);
+    o.facet_nact.assign(std::max(nf, 1), 0);
+    for (int f = 0; f < nf; f++) {
+        const FacetFrame &F = o.facets[f];
+        float *A = o.area.data() + o.cell0[f];
+        fragment_areas(F, A);
+        facet_n[f] = make_float4(F.normal.x, F.normal.y, F.normal.z, 0.0f);
+        for (int y = 0; y < F.ny; y++)
+            for (int x = 0; x < F.nx; x++) {
+                const long long c = o.cell0[f] + (long long)y * F.nx + x;
+                const Vec3 ps = fragment_centroid(F, x, y, true);
+                cell_pos[c] = make_float4(ps.x, ps.y, ps.z, A[(long long)y * F.nx + x]);
+                cell_facet[c] = f;
+                if (A[(long long)y * F.nx + x] > 1e-6f) {
+                    const Vec3 pa = fragment_centroid(F, x, y, false);
+                    act_pos.push_back(make_float4(pa.x, pa.y, pa.z, A[(long long)y * F.nx + x]));
+                    act_facet.push_back(f);
+                    o.act_cell.push_back((int)c);
+                    o.facet_nact[f]++;
+                }
+            }
+        o.facet_act_end[f] = (int)o.act_cell.size();
+    }
+    const size_t nc = (size_t)o.ncells, na = o.act_cell.size();
+    o.d_cell_pos = dalloc<float4>(nc);
+    o.d_cell_facet = dalloc<int>(nc);
+    o.d_facet_n = dalloc<float4>(facet_n.size());
+    o.d_P = dalloc<double2>(nc);
+    o.d_act_pos = dalloc<float4>(na);
+    o.d_act_facet = dalloc<int>(na);
+    o.d_act_cell = dalloc<int>(na);
+    o.d_facet_end = dalloc<int>(o.facet_act_end.size());
+    cudaStream_t s = g.stream;
+    CK(cudaMemcpyAsync(o.d_cell_pos, cell_pos.data(), nc * sizeof(float4), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(o.d_cell_facet, cell_facet.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(o.d_facet_n, facet_n.data(), facet_n.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(o.d_P, 0, std::max<size_t>(nc, 1) * sizeof(double2), s));
+    if (na) {
+        CK(cudaMemcpyAsync(o.d_act_pos, act_pos.data(), na * sizeof(float4), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(o.d_act_facet, act_facet.data(), na * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(o.d_act_cell, o.act_cell.data(), na * sizeof(int), cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemcpyAsync(o.d_facet_end, o.facet_act_end.data(), o.facet_act_end.size() * sizeof(int),
+                       cudaMemcpyHostToDevice, s));
+    g.h2d_bytes += (long long)(nc * (sizeof(float4) + sizeof(int)) + facet_n.size() * sizeof(float4) +
+                               na * (sizeof(float4) + 2 * sizeof(int)) + o.facet_act_end.size() * sizeof(int));
+    if (o.type == OBJ_TARGET) {
+        o.d_Pin = dalloc<double2>(nc);
+        o.d_Pout = dalloc<double2>(nc);
+        CK(cudaMemsetAsync(o.d_Pin, 0, std::max<size_t>(nc, 1) * sizeof(double2), s));
+        CK(cudaMemsetAsync(o.d_Pout, 0, std::max<size_t>(nc, 1) * sizeof(double2), s));
+    }
+    // the pageable host vectors above are read by the copies before they go
+    CK(cudaStreamSynchronize(s));
+}
+
+void upload_points(const std::vector<Vec3> &pts, float4 *&d_pos, double2 *&d_P, double value)
+{
+    std::vector<float4> pos(pts.size());
+    std::vector<double2> P(pts.size(), make_double2(value, 0.0));
+    for (size_t i = 0; i < pts.size(); i++) pos[i] = make_float4(pts[i].x, pts[i].y, pts[i].z, 0.0f);
+    d_pos = dalloc<float4>(pts.size());
+    d_P = dalloc<double2>(pts.size());
+    if (!pts.empty()) {
+        CK(cudaMemcpyAsync(d_pos, pos.data(), pos.size() * sizeof(float4), cudaMemcpyHostToDevice, g.stream));
+        CK(cudaMemcpyAsync(d_P, P.data(), P.size() * sizeof(double2), cudaMemcpyHostToDevice, g.stream));
+        g.h2d_bytes += (long long)(pos.size() * sizeof(float4) + P.size() * sizeof(double2));
+    }
+    CK(cudaStreamSynchronize(g.stream));
+}
+
+void render()
+{
+    if (g.rendered) fail(-2, "render_cuda called twice without TearDownCuda");
+    CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+    for (cudaEvent_t *e : {&g.ev0, &g.ev1, &g.ev2, &g.ev3}) CK(cudaEventCreate(e));
+    for (int t : {OBJ_TARGET, OBJ_FIELD})
+        for (auto &o : g.obj[t]) render_object(*o);
+    // occluders: every triangle of every target object (OptiX.cpp:264-296)
+    std::vector<std::array<float, 9>> tris;
+    double maxc = 0.0;
+    for (auto &o : g.obj[OBJ_TARGET])
+        for (auto &F : o->facets) {
+            std::array<float, 9> t = {F.v1.x, F.v1.y, F.v1.z, F.v2.x, F.v2.y, F.v2.z, F.v3.x, F.v3.y, F.v3.z};
+            for (float v : t) maxc = std::max(maxc, (double)std::fabs(v));
+            tris.push_back(t);
+        }
+    for (auto &p : g.src) maxc = std::max({maxc, (double)std::fabs(p.x), (double)std::fabs(p.y), (double)std::fabs(p.z)});
+    for (auto &p : g.fp) maxc = std::max({maxc, (double)std::fabs(p.x), (double)std::fabs(p.y), (double)std::fabs(p.z)});
+    BvhHost bvh = build_bvh(tris, 1e-3 * (1.0 + maxc));
+    g.ntri = (int)tris.size();
+    g.nnodes = (int)bvh.nodes.size();
+    g.d_nodes = dalloc<float4>(2 * bvh.nodes.size());
+    g.d_tris = dalloc<float4>(bvh.tris.size());
+    if (g.ntri) {
+        CK(cudaMemcpyAsync(g.d_nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(BvhNode), cudaMemcpyHostToDevice,
+                           g.stream));
+        CK(cudaMemcpyAsync(g.d_tris, bvh.tris.data(), bvh.tris.size() * sizeof(float4), cudaMemcpyHostToDevice,
+                           g.stream));
+        g.h2d_bytes += (long long)(bvh.nodes.size() * sizeof(BvhNode) + bvh.tris.size() * sizeof(float4));
+    }
+    upload_points(g.src, g.d_src_pos, g.d_src_P, 1.0);  // unit source pressure (Model.cpp:16-19)
+    upload_points(g.fp, g.d_fp_pos, g.d_fp_P, 0.0);
+    g.rendered = true;
+}
+
+// ---------------------------------------------------------------- hops
+Object &get(int type, int idx)
+{
+    if (type < 0 || type > 2 || idx < 0 || idx >= (int)g.obj[type].size())
+        fail(-4, "no object %d of type %d", idx, type);
+    return *g.obj[type][idx];
+}
+
+struct HopSets {
+    MaskArgs m{};
+    int nsrc = 0, ndst = 0;
+};
+
+HopSets hop_sets(int hop, int a, int b)
+{
+    HopSets h;
+    MaskArgs &m = h.m;
+    m.hop = hop;
+    m.bvh = BvhView{g.d_nodes, g.d_tris, g.nnodes, g.ntri};
+    if (hop == HOP_SRC) {
+        Object &B = get(a, b);  // a = object type (target or field), b = index
+        m.nsrc = (int)g.src.size();
+        m.src_pos = g.d_src_pos;
+        m.ndst = (int)B.ncells;
+        m.dst_pos = B.d_cell_pos;
+        m.dst_facet = B.d_cell_facet;
+        m.dst_facet_n = B.d_facet_n;
+        m.dst_is_field = B.type == OBJ_FIELD;
+    } else if (hop == HOP_FP) {
+        Object &A = get(OBJ_TARGET, a);
+        m.nsrc = A.nact();
+        m.src_pos = A.d_act_pos;
+        m.src_facet = A.d_act_facet;
+        m.src_facet_n = A.d_facet_n;
+        m.ndst = (int)g.fp.size();
+        m.dst_pos = g.d_fp_pos;
+    } else if (hop == HOP_F2F) {
+        Object &A = get(OBJ_TARGET, a);
+        m.nsrc = m.ndst = A.nact();
+        m.src_pos = m.dst_pos = A.d_act_pos;
+        m.src_facet = m.dst_facet = A.d_act_facet;
+        m.src_facet_n = m.dst_facet_n = A.d_facet_n;
+    } else {
+        Object &A = get(OBJ_TARGET, a);
+        Object &B = get(OBJ_FIELD, b);
+        m.nsrc = A.nact();
+        m.src_pos = A.d_act_pos;
+        m.src_facet = A.d_act_facet;
+        m.src_facet_n = A.d_facet_n;
+        m.ndst = B.nact();
+        m.dst_pos = B.d_act_pos;
+        m.dst_facet = B.d_act_facet;
+        m.dst_facet_n = B.d_facet_n;
+        m.dst_is_field = 1;
+    }
+    h.nsrc = m.nsrc;
+    h.ndst = m.ndst;
+    return h;
+}
+
+MaskEntry &get_mask(int hop, int a, int b)
+{
+    for (auto &e : g.masks)
+        if (e.hop == hop && e.a == a && e.b == b) return e;
+    HopSets hs = hop_sets(hop, a, b);
+    MaskEntry e{};
+    e.hop = hop;
+    e.a = a;
+    e.b = b;
+    e.nsrc = hs.nsrc;
+    e.ndst = hs.ndst;
+    MaskView &v = e.view;
+    v.nwords = (hs.nsrc + 31) / 32;
+    v.ntiles = (hs.nsrc + kTile - 1) / kTile;
+    v.ndstblocks = (hs.ndst + kTile - 1) / kTile;
+    v.pitch = ((long long)hs.ndst + 31) / 32 * 32;
+    if (v.ntiles > 65535) fail(-3, "hop %d has %d sources (limit %d)", hop, hs.nsrc, 65535 * kTile);
+    const size_t words = (size_t)v.ntiles * kWordsPerTile * (size_t)v.pitch;
+    const size_t nflags = (size_t)v.ntiles * v.ndstblocks;
+    v.bits = dalloc<uint32_t>(words);
+    v.flags = dalloc<uint8_t>(nflags);
+    CK(cudaMemsetAsync(v.bits, 0, std::max<size_t>(words, 1) * sizeof(uint32_t), g.stream));
+    CK(cudaMemsetAsync(v.flags, 0, std::max<size_t>(nflags, 1), g.stream));
+    hs.m.mask = v;
+    CK(cudaEventRecord(g.ev0, g.stream));
+    launch_mask(hs.m, g.stream);
+    CK(cudaGetLastError());
+    g.launches += (hs.nsrc > 0 && hs.ndst > 0) ? 1 : 0;
+    CK(cudaEventRecord(g.ev1, g.stream));
+    CK(cudaEventSynchronize(g.ev1));
+    CK(cudaEventElapsedTime(&e.mask_ms, g.ev0, g.ev1));
+    g.masks.push_back(e);
+    return g.masks.back();
+}
+
+void ensure_scratch(int nsrc, int ndst, int nsplit)
+{
+    if ((size_t)nsrc > g.pack_cap) {
+        dfree(g.d_packA);
+        dfree(g.d_packB);
+        g.d_packA = dalloc<float4>(nsrc);
+        g.d_packB = dalloc<float4>(nsrc);
+        g.pack_cap = nsrc;
+    }
+    const size_t np = (size_t)ndst * nsplit;
+    if (np > g.partial_cap) {
+        dfree(g.d_partial);
+        g.d_partial = dalloc<double2>(np);
+        g.partial_cap = np;
+    }
+    if ((size_t)ndst > g.limit_cap) {
+        dfree(g.d_limit);
+        g.d_limit = dalloc<int>(ndst);
+        g.limit_cap = ndst;
+    }
+}
+
+int choose_split(int ntiles, int ndstblocks)
+{
+    if (g.opt_split > 0) return std::min(g.opt_split, std::max(ntiles, 1));
+    // aim for ~16 resident-CTA waves' worth of CTAs on 152 SMs, at least 2 tiles per split
+    const int want = (2432 + ndstblocks - 1) / std::max(ndstblocks, 1);
+    return std::max(1, std::min(want, std::max(1, ntiles / 2)));
+}
+
+long long pair_count(int hop, int a, int b)
+{
+    if (hop == HOP_SRC) return (long long)g.src.size() * get(a, b).ncells;
+    if (hop == HOP_FP) return (long long)get(OBJ_TARGET, a).nact() * (long long)g.fp.size();
+    if (hop == HOP_F2F) {
+        Object &A = get(OBJ_TARGET, a);
+        long long tot = A.nact(), sq = 0;
+        for (long long n : A.facet_nact) sq += n * n;
+        return tot * tot - sq;
+    }
+    return (long long)get(OBJ_TARGET, a).nact() * get(OBJ_FIELD, b).nact();
+}
+
+// The sum kernel bracketed by its own events (per-launch duration of the
+// dominant kernel).
+void timed_sum(const SumArgs &s, cudaStream_t st)
+{
+    CK(cudaEventRecord(g.ev2, st));
+    launch_sum(s, st);
+    CK(cudaEventRecord(g.ev3, st));
+}
+
+// One hop: mask (cached), pack the source weights, sum, finalize.
+void run_hop(int hop, int a, int b)
+{
+    MaskEntry &M = get_mask(hop, a, b);
+    if (M.nsrc == 0 || M.ndst == 0) return;
+    HopSets hs = hop_sets(hop, a, b);
+    SumArgs s{};
+    s.hop = hop;
+    s.nsrc = M.nsrc;
+    s.ndst = M.ndst;
+    s.dst_pos = hs.m.dst_pos;
+    s.dst_facet = hs.m.dst_facet;
+    s.dst_facet_n = hs.m.dst_facet_n;
+    s.dst_is_field = hs.m.dst_is_field;
+    s.mask = M.view;
+    s.kr = (float)g.kr;
+    s.ka = (float)g.ki;
+    const double k2 = g.kr / (2.0 * M_PI);
+    s.k2hi = (float)k2;
+    s.k2lo = (float)(k2 - (double)s.k2hi);
+    s.nsplit = choose_split(M.view.ntiles, M.view.ndstblocks);
+    s.tiles_per_split = (M.view.ntiles + s.nsplit - 1) / s.nsplit;
+    s.nsplit = (M.view.ntiles + s.tiles_per_split - 1) / s.tiles_per_split;
+    ensure_scratch(M.nsrc, M.ndst, s.nsplit);
+    s.srcA = g.d_packA;
+    s.srcB = g.d_packB;
+    s.partial = g.d_partial;
+    s.dst_limit = g.d_limit;
+    cudaStream_t st = g.stream;
+
+    CK(cudaEventRecord(g.ev0, st));
+    if (hop == HOP_SRC) {
+        launch_pack_points(g.d_src_pos, g.d_src_P, M.nsrc, g.d_packA, g.d_packB, st);
+        timed_sum(s, st);
+        launch_finalize_add(g.d_partial, s.nsplit, M.ndst, nullptr, get(a, b).d_P, st);
+    } else if (hop == HOP_FP) {
+        Object &A = get(OBJ_TARGET, a);
+        launch_pack_frags(A.d_act_pos, A.d_act_facet, A.d_act_cell, A.d_facet_n, A.d_P, 1.0f, M.nsrc, g.d_packA,
+                          g.d_packB, st);
+        timed_sum(s, st);
+        launch_finalize_add(g.d_partial, s.nsplit, M.ndst, nullptr, g.d_fp_P, st);
+    } else if (hop == HOP_F2F) {
+        Object &A = get(OBJ_TARGET, a);
+        s.rmin = A.delta;
+        launch_f2f_limits(A.d_act_facet, A.d_act_cell, A.d_facet_end, A.d_Pin, M.ndst, M.nsrc, g.d_limit, st);
+        launch_pack_frags(A.d_act_pos, A.d_act_facet, A.d_act_cell, A.d_facet_n, A.d_Pin, 0.9f, M.nsrc, g.d_packA,
+                          g.d_packB, st);
+        timed_sum(s, st);
+        launch_finalize_f2f(g.d_partial, s.nsplit, M.ndst, A.d_act_cell, A.d_Pout, A.d_P, st);
+    } else {
+        Object &A = get(OBJ_TARGET, a);
+        Object &B = get(OBJ_FIELD, b);
+        s.rmin = A.delta;
+        launch_pack_frags(A.d_act_pos, A.d_act_facet, A.d_act_cell, A.d_facet_n, A.d_P, 0.9f, M.nsrc, g.d_packA,
+                          g.d_packB, st);
+        timed_sum(s, st);
+        launch_finalize_add(g.d_partial, s.nsplit, M.ndst, B.d_act_cell, B.d_P, st);
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(g.ev1, st));
+    CK(cudaEventSynchronize(g.ev1));
+    float ms = 0.0f, sum_ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
+    CK(cudaEventElapsedTime(&sum_ms, g.ev2, g.ev3));
+    const int nl = (hop == HOP_F2F ? 4 : 3) + (M.mask_ms > 0.0f ? 1 : 0);
+    g.launches += hop == HOP_F2F ? 4 : 3;
+    g.log.push_back(HopRecord{hop, pair_count(hop, a, b), M.mask_ms, sum_ms, ms, s.nsplit, nl});
+    M.mask_ms = 0.0f;  // reported once, with the first use
+}
+
+void need_render()
+{
+    if (!g.rendered) fail(-5, "render_cuda has not been called");
+}
+
+// ---------------------------------------------------------------- ABI glue
+template <class F>
+int guarded(F &&f)
+{
+    if (g.status != 0) return g.status;
+    try {
+        f();
+        return 0;
+    } catch (const Error &e) {
+        g.status = e.code;
+        g.err = e.what();
+    } catch (const std::exception &e) {
+        g.status = -1;
+        g.err = e.what();
+    } catch (...) {
+        g.status = -1;
+        g.err = "unknown error";
+    }
+    if (g.verbose) fprintf(stderr, "sonar: %s\n", g.err.c_str());
+    return g.status;
+}
+
+bool finite3(const float *p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+}  // namespace
+}  // namespace sonar
+
+using namespace sonar;
+
+extern "C" {
+
+void set_initial_conditions(float cp, float frequency, float attenuation, float density)
+{
+    guarded([&] {
+        // src/Model.cpp:44-54: omega and k are FP32
+        const float omega = (float)(2 * M_PI * (double)frequency);
+        const float k = omega / cp;
+        g.cp = cp;
+        g.freq = frequency;
+        g.att = attenuation;
+        g.density = density;
+        g.kr = (double)k;
+        g.ki = (double)attenuation;
+    });
+}
+
+void load_geometry(float *v1, int num_vertices, int objectType, float resolution)
+{
+    guarded([&] {
+        if (objectType < OBJ_TARGET || objectType > OBJ_FIELD) fail(-6, "invalid objectType %d", objectType);
+        if (num_vertices < 0 || (num_vertices > 0 && !v1)) fail(-6, "invalid triangle buffer");
+        if (!(resolution > 0.0f) || !std::isfinite(resolution)) fail(-6, "invalid resolution %g", (double)resolution);
+        auto o = std::make_unique<Object>();
+        o->type = objectType;
+        o->delta = resolution;
+        o->facets.reserve(num_vertices);
+        for (int i = 0; i < num_vertices; i++) {
+            const float *t = v1 + 9L * i;
+            if (!finite3(t) || !finite3(t + 3) || !finite3(t + 6)) fail(-6, "triangle %d has a non-finite vertex", i);
+            o->facets.push_back(make_frame({t[0], t[1], t[2]}, {t[3], t[4], t[5]}, {t[6], t[7], t[8]}, resolution));
+        }
+        g.obj[objectType].push_back(std::move(o));
+    });
+}
+
+void load_field_points(float *v1, int num_feild_points)
+{
+    guarded([&] {
+        if (num_feild_points < 0 || (num_feild_points > 0 && !v1)) fail(-6, "invalid field point buffer");
+        if (g.rendered) fail(-7, "load_field_points after render_cuda");
+        for (int i = 0; i < num_feild_points; i++) {
+            if (!finite3(v1 + 3L * i)) fail(-6, "field point %d is not finite", i);
+            g.fp.push_back({v1[3L * i], v1[3L * i + 1], v1[3L * i + 2]});
+        }
+    });
+}
+
+void load_source_points(float *v1, int num_source_points)
+{
+    guarded([&] {
+        if (num_source_points < 0 || (num_source_points > 0 && !v1)) fail(-6, "invalid source point buffer");
+        if (g.rendered) fail(-7, "load_source_points after render_cuda");
+        for (int i = 0; i < num_source_points; i++) {
+            if (!finite3(v1 + 3L * i)) fail(-6, "source point %d is not finite", i);
+            g.src.push_back({v1[3L * i], v1[3L * i + 1], v1[3L * i + 2]});
+        }
+    });
+}
+
+void render_cuda(void)
+{
+    guarded([] { render(); });
+}
+
+void ProjectSrcPointsToObjects(bool projectFieldObjects)
+{
+    guarded([&] {
+        need_render();
+        for (int i = 0; i < (int)g.obj[OBJ_TARGET].size(); i++) run_hop(HOP_SRC, OBJ_TARGET, i);
+        if (projectFieldObjects)
+            for (int i = 0; i < (int)g.obj[OBJ_FIELD].size(); i++) run_hop(HOP_SRC, OBJ_FIELD, i);
+    });
+}
+
+void ProjectTargetToFieldObjects(void)
+{
+    guarded([] {
+        need_render();
+        for (int t = 0; t < (int)g.obj[OBJ_TARGET].size(); t++)
+            for (int f = 0; f < (int)g.obj[OBJ_FIELD].size(); f++) run_hop(HOP_NORESP, t, f);
+    });
+}
+
+void ProjectTargetToFieldPoints(void)
+{
+    guarded([] {
+        need_render();
+        for (int t = 0; t < (int)g.obj[OBJ_TARGET].size(); t++) run_hop(HOP_FP, t, 0);
+    });
+}
+
+void ProjectTargetToTargetObjects(int number_reflections)
+{
+    guarded([&] {
+        need_render();
+        // src/ModelCuda.cpp:323-356: prime P_out <- P; per bounce P_in <- P_out,
+        // P_out <- 0, project, P += P_out.  Objects never interact, so each
+        // object runs its bounces in turn; P_in/P_out swap by pointer.
+        for (int t = 0; t < (int)g.obj[OBJ_TARGET].size(); t++) {
+            Object &A = *g.obj[OBJ_TARGET][t];
+            const size_t bytes = std::max<size_t>((size_t)A.ncells, 1) * sizeof(double2);
+            CK(cudaMemcpyAsync(A.d_Pout, A.d_P, bytes, cudaMemcpyDeviceToDevice, g.stream));
+            for (int b = 0; b < number_reflections; b++) {
+                std::swap(A.d_Pin, A.d_Pout);
+                CK(cudaMemsetAsync(A.d_Pout, 0, bytes, g.stream));
+                run_hop(HOP_F2F, t, 0);
+            }
+        }
+        CK(cudaStreamSynchronize(g.stream));
+    });
+}
+
+void GetFieldPointPressures(dcomplex *field_points_pressure, int NumPoints)
+{
+    guarded([&] {
+        need_render();
+        const size_t n = std::min<size_t>(NumPoints < 0 ? 0 : (size_t)NumPoints, g.fp.size());
+        if (n && !field_points_pressure) fail(-6, "null output buffer");
+        if (n) {
+            CK(cudaMemcpyAsync(field_points_pressure, g.d_fp_P, n * sizeof(double2), cudaMemcpyDeviceToHost, g.stream));
+            CK(cudaStreamSynchronize(g.stream));
+            g.d2h_bytes += (long long)(n * sizeof(double2));
+        }
+        if ((size_t)std::max(NumPoints, 0) < g.fp.size())
+            fail(-8, "GetFieldPointPressures: buffer holds %d of %zu field points", NumPoints, g.fp.size());
+    });
+}
+
+void RenderOpenGL(int width, int height, char *filename, float viewSettings[9])
+{
+    (void)width; (void)height; (void)filename; (void)viewSettings;
+    // not sticky: the scene stays usable (run_scripts call this before TearDownCuda)
+    g.err = "RenderOpenGL: no graphics stack; read surfaces with sonar_get_object_pressures";
+    if (g.verbose) fprintf(stderr, "sonar: %s\n", g.err.c_str());
+}
+
+void TearDownCuda(void)
+{
+    // src/Model.cpp:115-129, src/ModelCuda.cpp:124-181: points, target and
+    // field objects are dropped; source objects are kept, as in the reference
+    try {
+        if (g.stream) cudaStreamSynchronize(g.stream);
+        g.free_device();
+    } catch (...) {
+    }
+    g.obj[OBJ_TARGET].clear();
+    g.obj[OBJ_FIELD].clear();
+    g.src.clear();
+    g.fp.clear();
+    g.rendered = false;
+    g.status = 0;
+    g.err.clear();
+    g.log.clear();
+}
+
+void SoundVisualisationInit(float maxDbValue, float minDbValue, bool renderPhaseTarget, bool renderPhaseField)
+{
+    g.max_db = maxDbValue;
+    g.min_db = minDbValue;
+    g.phase_target = renderPhaseTarget;
+    g.phase_field = renderPhaseField;
+}
+
+int sonar_status(void) { return g.status; }
+
+const char *sonar_last_error(void) { return g.err.c_str(); }
+
+void sonar_clear_error(void)
+{
+    g.status = 0;
+    g.err.clear();
+}
+
+int sonar_get_object_count(int objectType)
+{
+    return (objectType >= 0 && objectType <= 2) ? (int)g.obj[objectType].size() : -1;
+}
+
+long long sonar_get_object_cells(int objectType, int objIdx)
+{
+    if (objectType < 0 || objectType > 2 || objIdx < 0 || objIdx >= (int)g.obj[objectType].size()) return -1;
+    const Object &o = *g.obj[objectType][objIdx];
+    if (!g.rendered) {
+        long long n = 0;
+        for (auto &F : o.facets) n += (long long)F.nx * F.ny;
+        return n;
+    }
+    return o.ncells;
+}
+
+int sonar_get_object_pressures(int objectType, int objIdx, dcomplex *out, long long n)
+{
+    int written = 0;
+    int st = guarded([&] {
+        need_render();
+        Object &o = get(objectType, objIdx);
+        if (o.type == OBJ_SOURCE || !o.d_P) fail(-4, "object has no pressures");
+        if (n < o.ncells) fail(-8, "buffer holds %lld of %lld cells", n, o.ncells);
+        if (o.ncells) {
+            CK(cudaMemcpyAsync(out, o.d_P, (size_t)o.ncells * sizeof(double2), cudaMemcpyDeviceToHost, g.stream));
+            CK(cudaStreamSynchronize(g.stream));
+            g.d2h_bytes += o.ncells * (long long)sizeof(double2);
+        }
+        written = (int)o.ncells;
+    });
+    return st != 0 ? st : written;
+}
+
+int sonar_get_fragment_layout(int objectType, int objIdx, int *nx_ny_neg, int nfacets_cap, float *areas,
+                              long long ncells_cap)
+{
+    int nf = 0;
+    int st = guarded([&] {
+        Object &o = get(objectType, objIdx);
+        nf = (int)o.facets.size();
+        if (nx_ny_neg) {
+            if (nfacets_cap < nf) fail(-8, "layout buffer holds %d of %d facets", nfacets_cap, nf);
+            for (int f = 0; f < nf; f++) {
+                nx_ny_neg[3 * f] = o.facets[f].nx;
+                nx_ny_neg[3 * f + 1] = o.facets[f].ny;
+                nx_ny_neg[3 * f + 2] = o.facets[f].neg;
+            }
+        }
+        if (areas) {
+            long long total = 0;
+            for (auto &F : o.facets) total += (long long)F.nx * F.ny;
+            if (ncells_cap < total) fail(-8, "area buffer holds %lld of %lld cells", ncells_cap, total);
+            long long off = 0;
+            for (auto &F : o.facets) {
+                fragment_areas(F, areas + off);
+                off += (long long)F.nx * F.ny;
+            }
+        }
+    });
+    return st != 0 ? st : nf;
+}
+
+int sonar_get_stats(char *json, int cap)
+{
+    std::string s = "{\"hops\": [";
+    char buf[256];
+    for (size_t i = 0; i < g.log.size(); i++) {
+        const HopRecord &r = g.log[i];
+        snprintf(buf, sizeof(buf),
+                 "%s{\"hop\": %d, \"pairs\": %lld, \"mask_ms\": %.6f, \"sum_ms\": %.6f, \"total_ms\": %.6f, "
+                 "\"nsplit\": %d, \"launches\": %d}",
+                 i ? ", " : "", r.hop, r.pairs, r.mask_ms, r.sum_ms, r.total_ms, r.nsplit, r.launches);
+        s += buf;
+    }
+    snprintf(buf, sizeof(buf),
+             "], \"ntri\": %d, \"nnodes\": %d, \"masks\": %zu, \"launches\": %lld, \"h2d_bytes\": %lld, "
+             "\"d2h_bytes\": %lld}",
+             g.ntri, g.nnodes, g.masks.size(), g.launches, g.h2d_bytes, g.d2h_bytes);
+    s += buf;
+    if (json && cap > 0) {
+        const size_t n = std::min<size_t>(s.size(), (size_t)cap - 1);
+        memcpy(json, s.data(), n);
+        json[n] = 0;
+    }
+    return (int)s.size();
+}
+
+int sonar_set_option(const char *key, double value)
+{
+    if (!key) return -1;
+    if (!strcmp(key, "split")) { g.opt_split = (int)value; return 0; }
+    if (!strcmp(key, "verbose")) { g.verbose = (int)value; return 0; }
+    if (!strcmp(key, "reset_stats")) {
+        g.log.clear();
+        g.launches = g.h2d_bytes = g.d2h_bytes = 0;
+        return 0;
+    }
+    if (!strcmp(key, "reset_pressures")) {
+        // zero every surface and field-point pressure (benchmark steps start clean)
+        return guarded([] {
+            need_render();
+            for (int t : {OBJ_TARGET, OBJ_FIELD})
+                for (auto &o : g.obj[t]) {
+                    const size_t b = std::max<size_t>((size_t)o->ncells, 1) * sizeof(double2);
+                    CK(cudaMemsetAsync(o->d_P, 0, b, g.stream));
+                    if (o->d_Pin) CK(cudaMemsetAsync(o->d_Pin, 0, b, g.stream));
+                    if (o->d_Pout) CK(cudaMemsetAsync(o->d_Pout, 0, b, g.stream));
+                }
+            if (!g.fp.empty()) CK(cudaMemsetAsync(g.d_fp_P, 0, g.fp.size() * sizeof(double2), g.stream));
+            CK(cudaStreamSynchronize(g.stream));
+        });
+    }
+    if (!strcmp(key, "drop_masks")) {
+        for (auto &m : g.masks) { dfree(m.view.bits); dfree(m.view.flags); }
+        g.masks.clear();
+        return 0;
+    }
+    return -1;
+}
+
+long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, long long cap)
+{
+    long long nbytes = 0;
+    int st = guarded([&] {
+        need_render();
+        if (hop < HOP_SRC || hop > HOP_NORESP) fail(-6, "invalid hop %d", hop);
+        MaskEntry &M = get_mask(hop, srcIdx, dstIdx);
+        nbytes = (long long)M.nsrc * M.ndst;
+        if (!out) return;
+        if (cap < nbytes) fail(-8, "mask buffer holds %lld of %lld bytes", cap, nbytes);
+        if (nbytes == 0) return;
+        uint8_t *d = dalloc<uint8_t>((size_t)nbytes);
+        launch_mask_export(M.view, M.nsrc, M.ndst, d, g.stream);
+        CK(cudaGetLastError());
+        cudaError_t e = cudaMemcpyAsync(out, d, (size_t)nbytes, cudaMemcpyDeviceToHost, g.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
+        cudaFree(d);
+        if (e != cudaSuccess) fail(-10, "mask export failed: %s", cudaGetErrorString(e));
+    });
+    return st != 0 ? st : nbytes;
+}
+
+void *sonar_get_stream(void) { return (void *)g.stream; }
+
+double sonar_measure_peak(int which) { return measure_peak(which); }
+
+/* Host-only: frame and area grid of one triangle (no GPU needed). */
+long long sonar_fragment_triangle(const float *tri9, float delta, int *nx_ny_neg, float *frame17, float *areas,
+                                  long long cap)
+{
+    if (!tri9 || !(delta > 0.0f)) return -6;
+    FacetFrame F = make_frame({tri9[0], tri9[1], tri9[2]}, {tri9[3], tri9[4], tri9[5]}, {tri9[6], tri9[7], tri9[8]}, delta);
+    if (nx_ny_neg) {
+        nx_ny_neg[0] = F.nx;
+        nx_ny_neg[1] = F.ny;
+        nx_ny_neg[2] = F.neg;
+    }
+    if (frame17) {
+        const float v[17] = {F.normal.x, F.normal.y, F.normal.z, F.base.x, F.base.y, F.base.z, F.xAxis.x, F.xAxis.y,
+                             F.xAxis.z, F.yAxis.x, F.yAxis.y, F.yAxis.z, F.baseLen, F.height, F.baseNeg, F.basePos,
+                             F.area};
+        memcpy(frame17, v, sizeof(v));
+    }
+    const long long n = (long long)F.nx * F.ny;
+    if (areas && cap >= n) fragment_areas(F, areas);
+    return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,104 @@
+// sonar_internal.h -- structures shared by the host model (model.cpp) and the
+// CUDA kernels (kernels.cu).  All device buffers are structure-of-arrays.
+//
+// Device layout of one object (HBM):
+//   cells      every fragment cell of every facet, facet-major, row-major
+//              y*numXpnts + x inside a facet (the reference's P layout,
+//              src/OptiX.cu:49).  cell_pos (float4 x,y,z,area) holds the
+//              source-hop centroid (x offset + delta/2, src/OptiX.cu:51);
+//              cell_facet the facet index; P/Pin/Pout are double2.
+//   active     cells with area > 1e-6 (the area gates of src/OptiX.cu:138,
+//              :219, :286), in cell order: act_pos (float4 x,y,z,area) with
+//              the centroid WITHOUT the delta/2 x shift (src/OptiX.cu:129,
+//              :210, :273), act_facet, act_cell.
+//   facet_n    unit normal per facet (float4).
+// Interaction masks: uint32 words [src_word][dst_pitch] -- bit b of word
+// (w, j) is the pair (source 32w+b, destination j) -- plus one flag byte per
+// (source tile of 256, destination block of 256) telling whether any bit is set.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sonar {
+
+enum Hop : int { HOP_SRC = 0, HOP_FP = 1, HOP_F2F = 2, HOP_NORESP = 3 };
+
+constexpr int kTile = 256;          // sources per tile, destinations per block
+constexpr int kWordsPerTile = kTile / 32;
+
+struct BvhNode {                    // 32 bytes
+    float lo[3];
+    int left;                       // >= 0 inner child, < 0 leaf: first triangle = -left-1
+    float hi[3];
+    int right;                      // inner: right child; leaf: triangle count
+};
+
+struct BvhView {
+    const float4 *nodes;            // BvhNode as 2 float4
+    const float4 *tris;             // 4 float4 per triangle: (n,c) (m0,c0) (m1,c1) (m2,c2)
+    int nnodes;
+    int ntri;
+};
+
+struct MaskView {
+    uint32_t *bits;
+    uint8_t *flags;
+    long long pitch;                // words per source-word row (>= ndst, multiple of 32)
+    int nwords;                     // ceil(nsrc / 32)
+    int ntiles;                     // ceil(nsrc / 256)
+    int ndstblocks;                 // ceil(ndst / 256)
+};
+
+struct MaskArgs {
+    int hop;
+    int nsrc, ndst;
+    const float4 *src_pos;          // x, y, z, area
+    const int *src_facet;           // may be null (points)
+    const float4 *src_facet_n;
+    const float4 *dst_pos;
+    const int *dst_facet;           // may be null (points)
+    const float4 *dst_facet_n;
+    int dst_is_field;               // cos_inc forced to 1 (src/OptiX.cu:67-72, :308-312)
+    BvhView bvh;
+    MaskView mask;
+};
+
+struct SumArgs {
+    int hop;
+    int nsrc, ndst;
+    const float4 *srcA;             // x, y, z, Re(weight)
+    const float4 *srcB;             // nx, ny, nz, Im(weight)
+    const float4 *dst_pos;
+    const int *dst_facet;
+    const float4 *dst_facet_n;
+    const int *dst_limit;           // FACET_SELF: sources at or past this index are dropped
+    int dst_is_field;
+    MaskView mask;
+    float kr, ka;                   // Re k, Im k (FP32 values of the reference's k_wave)
+    float k2hi, k2lo;               // Re k / (2 pi) split in two floats
+    float rmin;                     // regularisation radius (source object delta)
+    double2 *partial;               // [nsplit][ndst]
+    int nsplit;
+    int tiles_per_split;
+};
+
+// kernels.cu
+void launch_mask(const MaskArgs &a, cudaStream_t s);
+void launch_sum(const SumArgs &a, cudaStream_t s);
+void launch_pack_points(const float4 *pts, const double2 *P, int n, float4 *A, float4 *B, cudaStream_t s);
+void launch_pack_frags(const float4 *act_pos, const int *act_facet, const int *act_cell, const float4 *facet_n,
+                       const double2 *P, float scale, int n, float4 *A, float4 *B, cudaStream_t s);
+void launch_f2f_limits(const int *act_facet, const int *act_cell, const int *facet_end, const double2 *Pin, int n,
+                       int nsrc, int *limit, cudaStream_t s);
+// out[cell[j]] += sum over splits (cell == nullptr: out[j])
+void launch_finalize_add(const double2 *partial, int nsplit, int ndst, const int *cell, double2 *out,
+                         cudaStream_t s);
+// Pout[cell[j]] = sum, P[cell[j]] += sum
+void launch_finalize_f2f(const double2 *partial, int nsplit, int ndst, const int *cell, double2 *Pout,
+                         double2 *P, cudaStream_t s);
+void launch_mask_export(const MaskView &m, int nsrc, int ndst, uint8_t *out, cudaStream_t s);
+// FP32 FMA rate in FLOP/s (which = 0) or MUFU sine rate in op/s (which = 1)
+// on the current device; < 0 on failure.
+double measure_peak(int which);
+
+}  // namespace sonar
