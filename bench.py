@@ -178,6 +178,16 @@ def run_gb300(args):
     for _ in range(args.warmup):
         one_step()
     torch.cuda.synchronize()
+    if args.profile_only:
+        # device work only, for profiler captures: no e2e, no CPU legs, no JSON line
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            one_step()
+        torch.cuda.synchronize()
+        print("profile-only: %d steps of %s done" % (args.steps, cfg["name"]))
+        api.TearDownCuda()
+        return
     if world > 1:
         dist.barrier()
     api.set_option("reset_stats", 1)
@@ -411,6 +421,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="trihedral60")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run warm-up and steps of device work only (for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
