@@ -146,6 +146,41 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
 long long sonar_fragment_triangle(const float *tri9, float delta, int *nx_ny_neg, float *frame17, float *areas,
                                   long long cap);
 
+/* Fragment -> field-point readout that allocates no memory.  No counterpart in
+ * the reference: it exists for callers that cannot call cudaMalloc while they
+ * run (a host framework that owns all device memory through its own pool, a
+ * real-time host that allocates only at start-up, code that must avoid the
+ * synchronisation an allocation can cause).
+ *
+ * Computes, for every field point j, out[j] += sum over fragments i with
+ * area > 1e-6 and cos_scat >= 1e-6 of area_i cos_scat P_i G(r) -- the
+ * FIELD_POINTS sum of ProjectTargetToFieldPoints -- without shadowing (no
+ * occlusion test), on caller-owned DEVICE buffers:
+ *   frag_pos       n_frag x 4 floats: centroid x, y, z and area
+ *   frag_normal    n_frag x 4 floats: unit normal x, y, z (4th unused)
+ *   frag_pressure  n_frag x 2 doubles: complex pressure
+ *   points         n_points x 4 floats: field point x, y, z (4th unused)
+ *   out            n_points x 2 doubles: complex pressure, accumulated (+=)
+ * k_re, k_im: the wave number as set_initial_conditions computes it
+ * ((float)(2 pi f) / c and the attenuation).  The work is queued on `stream`
+ * (a cudaStream_t, NULL for the default stream); the call does not wait.
+ *
+ * Its only working memory is a fixed 8 MiB device array inside this library
+ * (held by every GPU that loads it, until the process exits), so n_points is
+ * limited to SONAR_NOALLOC_MAX_POINTS.  The array's address is looked up on
+ * the first call made on each device; make that first call before any stream
+ * capture begins.  All calls share the array: calls whose work overlaps on the
+ * GPU (e.g. on two streams at once) race and give wrong results.
+ * Returns 0, SONAR_NOALLOC_EINVAL (bad size or null pointer),
+ * SONAR_NOALLOC_ETOOBIG (n_points above the maximum) or SONAR_NOALLOC_ECUDA
+ * (device lookup or launch failed; a line goes to stderr). */
+#define SONAR_NOALLOC_MAX_POINTS 524288
+#define SONAR_NOALLOC_EINVAL (-1)
+#define SONAR_NOALLOC_ETOOBIG (-2)
+#define SONAR_NOALLOC_ECUDA (-3)
+int sonar_readout_noalloc(const float *frag_pos, const float *frag_normal, const double *frag_pressure, int n_frag,
+                          const float *points, int n_points, float k_re, float k_im, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
