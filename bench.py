@@ -230,18 +230,24 @@ def run_gb300(args):
     f2f = [h for h in stats["hops"] if h["hop"] == 2]
     fp32_peak = api.measure_peak(0)
     mufu_peak = api.measure_peak(1)
-    roof_pairs = min(fp32_peak / FLOP_PER_PAIR, mufu_peak / SFU_PER_PAIR) if fp32_peak > 0 and mufu_peak > 0 else None
     roofline = None
-    if f2f and roof_pairs:
+    if f2f and fp32_peak > 0 and mufu_peak > 0:
+        # the bounce sum evaluates one Green's function per unordered pair and
+        # applies it in both directions: per ordered pair 20 flop (half of the
+        # 40-flop evaluation incl. one complex MAC) + 4 (the second MAC) and 1.5
+        # MUFU ops; roofline pairs/s = min(FP32 / 24, MUFU / 1.5)
+        flop_pp, sfu_pp = 24.0, 1.5
+        roof = min(fp32_peak / flop_pp, mufu_peak / sfu_pp)
         launch_ms = sum(h["sum_ms"] for h in f2f) / len(f2f)
         pairs_launch = f2f[0]["pairs"]
-        achieved = pairs_launch * FLOP_PER_PAIR / (launch_ms * 1e-3) / 1e12
-        peak = roof_pairs * FLOP_PER_PAIR / 1e12
-        roofline = {"kernel": "k_sum<F2F> (bounce sum)", "bound": "fp32+sfu", "achieved": round(achieved, 3),
-                    "peak": round(peak, 3), "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
-                    "traffic": None, "pairs_per_launch": pairs_launch, "launch_ms": round(launch_ms, 4),
+        achieved = pairs_launch * flop_pp / (launch_ms * 1e-3) / 1e12
+        peak = roof * flop_pp / 1e12
+        roofline = {"kernel": "k_sum_f2f_sym (bounce sum, reciprocity)", "bound": "fp32+sfu",
+                    "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
+                    "frac": round(achieved / peak, 4), "traffic": None, "pairs_per_launch": pairs_launch,
+                    "pairs_per_s": round(pairs_launch / (launch_ms * 1e-3), 1), "launch_ms": round(launch_ms, 4),
                     "peak_source": "measured now by sonar_measure_peak: FP32 %.1f TFLOP/s, MUFU %.2f Top/s; "
-                                   "roofline = min(FP32/40, MUFU/3) pairs/s x 40 flop"
+                                   "roofline = min(FP32/24, MUFU/1.5) ordered pairs/s x 24 flop"
                                    % (fp32_peak / 1e12, mufu_peak / 1e12)}
     mask_f2f = [h for h in stats["hops"] if h["hop"] == 2 and h["mask_ms"] > 0]
     mask_info = None
@@ -331,17 +337,26 @@ def check_error(api, cfg):
         out["fragments"] = int(len(act))
         rng = np.random.default_rng(2024)
         q = np.sort(rng.choice(len(act), min(32, len(act)), replace=False))
-        v1, m1 = o.hop_subset(2, 0, 0, q, pin=P0)
+        nact = len(act)
+        v1, m1 = o.hop_subset(2, 0, 0, q, pin=P0, want_mask=True, nsrc=nact)
         c1 = o.counters()
-        e = {"bounce1": float(np.linalg.norm((P1 - P0)[act[q]] - v1) / np.linalg.norm(v1))}
+        g1 = (m1 & 2).any(axis=1)
+        d1 = (P1 - P0)[act[q]]
+        e = {"bounce1": float(np.linalg.norm(d1 - v1) / np.linalg.norm(v1))}
+        if (~g1).any():
+            e["bounce1_nongrazing_dst"] = float(np.linalg.norm((d1 - v1)[~g1]) / np.linalg.norm(v1[~g1]))
         graze = {"bounce_pairs_checked": c1["pairs"], "bounce_grazing": c1["grazing"]}
         if npts:
             o.set_pressures(0, 0, P1)
             jj = np.sort(rng.choice(npts, min(32, npts), replace=False))
-            vf, _ = o.hop_subset(1, 0, 0, jj)
+            vf, mf = o.hop_subset(1, 0, 0, jj, want_mask=True, nsrc=nact)
             c2 = o.counters()
+            gf = (mf & 2).any(axis=1)
             e["readout"] = float(np.linalg.norm(fp[jj] - vf) / np.linalg.norm(vf))
-            graze.update({"readout_pairs_checked": c2["pairs"], "readout_grazing": c2["grazing"]})
+            if (~gf).any():
+                e["readout_nongrazing_dst"] = float(np.linalg.norm((fp[jj] - vf)[~gf]) / np.linalg.norm(vf[~gf]))
+            graze.update({"readout_pairs_checked": c2["pairs"], "readout_grazing": c2["grazing"],
+                          "readout_dst_with_grazing": int(gf.sum())})
         out["errors"] = e
         out["grazing"] = graze
     except Exception as ex:  # the error check must not hide the timing

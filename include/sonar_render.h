@@ -116,10 +116,13 @@ int sonar_get_fragment_layout(int objectType, int objIdx, int *nx_ny_neg, int nf
 /* JSON statistics of the last projection calls (pairs, kernel ms, grazing). */
 int sonar_get_stats(char *json, int cap);
 /* Options: "split" (source splits of the sum kernels, 0 = automatic),
+ * "f2f_symmetric" (1, default: bounce sums evaluate each unordered pair once
+ * and feed both directions, as the reference's reciprocity does; 0: every
+ * ordered pair separately),
  * "verbose" (0/1), "reset_stats", "reset_pressures" (zero every surface and
- * field-point pressure), "drop_masks" (free the cached interaction masks; the
- * next projection rebuilds them).  Returns 0, or < 0 for an unknown key or a
- * failed action. */
+ * field-point pressure), "drop_masks" (rebuild the cached interaction masks,
+ * in place, at their next use), "free_masks" (free them).  Returns 0, or < 0
+ * for an unknown key or a failed action. */
 int sonar_set_option(const char *key, double value);
 /* The library's CUDA stream (a cudaStream_t; NULL before render_cuda), for
  * callers that time or order work against it. */

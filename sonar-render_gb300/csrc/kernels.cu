@@ -80,6 +80,25 @@ __device__ __forceinline__ bool tri_blocks(const float4 *__restrict__ T, float3 
     return true;
 }
 
+// The same test on triangle records already in registers (shared-memory
+// candidate lists).
+__device__ __forceinline__ bool tri_blocks_v(float4 P, float4 M1, float4 M2, float4 M3, float3 o, float3 e, float3 d,
+                                             float r, float tmax, float eps)
+{
+    const float d0 = fmaf(P.x, o.x, fmaf(P.y, o.y, P.z * o.z)) - P.w;
+    if (fabsf(d0) <= eps) return false;
+    const float d1 = fmaf(P.x, e.x, fmaf(P.y, e.y, P.z * e.z)) - P.w;
+    if (!((d0 > 0.0f && d1 < 0.0f) || (d0 < 0.0f && d1 > 0.0f))) return false;
+    const float ad0 = fabsf(d0), den = ad0 + fabsf(d1);
+    if (r * ad0 > tmax * den) return false;
+    const float s = ad0 / den;
+    const float Xx = fmaf(d.x, s, o.x), Xy = fmaf(d.y, s, o.y), Xz = fmaf(d.z, s, o.z);
+    if (fmaf(M1.x, Xx, fmaf(M1.y, Xy, M1.z * Xz)) < M1.w) return false;
+    if (fmaf(M2.x, Xx, fmaf(M2.y, Xy, M2.z * Xz)) < M2.w) return false;
+    if (fmaf(M3.x, Xx, fmaf(M3.y, Xy, M3.z * Xz)) < M3.w) return false;
+    return true;
+}
+
 constexpr int kStack = 64;
 
 __device__ bool occluded(const BvhView &B, float3 o, float3 e, float r, float tmax)
@@ -119,58 +138,118 @@ __device__ bool occluded(const BvhView &B, float3 o, float3 e, float r, float tm
 }
 
 // ---------------------------------------------------------------- gates
-// Returns whether pair (source s, destination t) interacts.  s/t: positions
-// (w = area); ns/nt: facet normals (w of ns = source facet index bits).
-template <int HOP>
-__device__ __forceinline__ bool pair_pass(const MaskArgs &a, float4 s, float4 ns, float4 t, float4 nt, int ft)
+// Cosine gates.  The reference's decision is "cos < 1e-6 -> skip" with
+// cos = dot(v * (1/r), n) in FP32 without contraction (exact_cos below).  A
+// cheaper estimate dot(v, n) * rsqrt(v.v) differs from it by less than 7e-7
+// (both are within a few ulp of the true cosine, |cos| <= 1), so outside the
+// band [0, 2e-6] the estimate decides the same way; inside it the exact
+// expression is evaluated.
+__device__ __forceinline__ float exact_cos(float vx, float vy, float vz, float sign, float nx, float ny, float nz)
 {
-    if (HOP == HOP_SRC) {
-        // OptiX.cu:59-98: v = p_j - p_i, uv = v * (1/r), cos_inc = dot(-uv, n_B)
-        const float vx = __fsub_rn(t.x, s.x), vy = __fsub_rn(t.y, s.y), vz = __fsub_rn(t.z, s.z);
-        const float r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
-        const float inv = __frcp_rn(r);
-        const float ux = __fmul_rn(vx, inv), uy = __fmul_rn(vy, inv), uz = __fmul_rn(vz, inv);
-        float ci = dot_rn(-ux, -uy, -uz, nt.x, nt.y, nt.z);
-        if (a.dst_is_field) ci = 1.0f;
-        if (ci < 1e-6f) return false;
-        return !occluded(a.bvh, make_float3(s.x, s.y, s.z), make_float3(t.x, t.y, t.z), r, __fsub_rn(r, 1e-3f));
-    } else if (HOP == HOP_FP) {
-        // OptiX.cu:147-180: v = p_i - p_j, cos_scat = dot(-uv, n_A), ray from the field point
-        const float vx = __fsub_rn(s.x, t.x), vy = __fsub_rn(s.y, t.y), vz = __fsub_rn(s.z, t.z);
-        const float r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
-        const float inv = __frcp_rn(r);
-        const float ux = __fmul_rn(vx, inv), uy = __fmul_rn(vy, inv), uz = __fmul_rn(vz, inv);
-        const float cs = dot_rn(-ux, -uy, -uz, ns.x, ns.y, ns.z);
-        if (cs < 1e-6f) return false;
-        return !occluded(a.bvh, make_float3(t.x, t.y, t.z), make_float3(s.x, s.y, s.z), r, __fsub_rn(r, 1e-3f));
-    } else if (HOP == HOP_F2F) {
-        // OptiX.cu:247-338 in the enumeration orientation: the lower facet
-        // index is the "A" side and the ray starts there
-        const int fs = __float_as_int(ns.w);
-        if (fs == ft) return false;
-        const bool fwd = fs < ft;
-        const float4 pA = fwd ? s : t, pB = fwd ? t : s;
-        const float4 nA = fwd ? ns : nt, nB = fwd ? nt : ns;
-        const float vx = __fsub_rn(pB.x, pA.x), vy = __fsub_rn(pB.y, pA.y), vz = __fsub_rn(pB.z, pA.z);
-        const float r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
-        const float inv = __frcp_rn(r);
-        const float ux = __fmul_rn(vx, inv), uy = __fmul_rn(vy, inv), uz = __fmul_rn(vz, inv);
-        const float cs = dot_rn(ux, uy, uz, nA.x, nA.y, nA.z);
-        if (cs < 1e-6f) return false;
-        const float ci = dot_rn(-ux, -uy, -uz, nB.x, nB.y, nB.z);
-        if (ci < 1e-6f) return false;
-        return !occluded(a.bvh, make_float3(pA.x, pA.y, pA.z), make_float3(pB.x, pB.y, pB.z), r,
-                         __fsub_rn(r, 1e-3f));
-    } else {
-        // FACET_NO_RESP, OptiX.cu:281-338 with cos_inc = 1 (field destination)
-        const float vx = __fsub_rn(t.x, s.x), vy = __fsub_rn(t.y, s.y), vz = __fsub_rn(t.z, s.z);
-        const float r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
-        const float inv = __frcp_rn(r);
-        const float ux = __fmul_rn(vx, inv), uy = __fmul_rn(vy, inv), uz = __fmul_rn(vz, inv);
-        const float cs = dot_rn(ux, uy, uz, ns.x, ns.y, ns.z);
-        if (cs < 1e-6f) return false;
-        return !occluded(a.bvh, make_float3(s.x, s.y, s.z), make_float3(t.x, t.y, t.z), r, __fsub_rn(r, 1e-3f));
+    const float r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
+    const float inv = __frcp_rn(r);
+    const float ux = __fmul_rn(vx, inv), uy = __fmul_rn(vy, inv), uz = __fmul_rn(vz, inv);
+    return dot_rn(sign * ux, sign * uy, sign * uz, nx, ny, nz);
+}
+
+// true when cos(sign * v, n) passes the reference's ">= 1e-6" gate
+__device__ __forceinline__ bool cos_gate(float vx, float vy, float vz, float rinv, float sign, float nx, float ny,
+                                         float nz)
+{
+    const float est = sign * fmaf(vx, nx, fmaf(vy, ny, vz * nz)) * rinv;
+    if (est > 2e-6f) return true;
+    if (est < 0.0f) return false;
+    return !(exact_cos(vx, vy, vz, sign, nx, ny, nz) < 1e-6f);
+}
+
+// Gates of one pair (the reference's discrete decisions).  For FACET_SELF
+// the two cosines are the same pair of numbers whichever fragment is the
+// enumeration's "A" side (u and -u give exactly negated dot products), so
+// they are evaluated with v = p_dst - p_src and no orientation select.
+template <int HOP>
+__device__ __forceinline__ bool pair_gates(const MaskArgs &a, float4 s, float4 ns, float4 t, float4 nt, int ft)
+{
+    const float vx = __fsub_rn(t.x, s.x), vy = __fsub_rn(t.y, s.y), vz = __fsub_rn(t.z, s.z);
+    if (HOP == HOP_SRC && a.dst_is_field) return true;  // cos_inc = 1 (OptiX.cu:67-72)
+    if (HOP == HOP_F2F && __float_as_int(ns.w) == ft) return false;  // same facet (OptiX.cu:247-262)
+    const float rinv = rsqrtf(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+    if (HOP == HOP_SRC) return cos_gate(vx, vy, vz, rinv, -1.0f, nt.x, nt.y, nt.z);   // cos_inc = dot(-uv, n_B)
+    if (HOP == HOP_FP) return cos_gate(vx, vy, vz, rinv, 1.0f, ns.x, ns.y, ns.z);     // cos_scat = dot(-uv_ji, n_A)
+    if (HOP == HOP_NORESP) return cos_gate(vx, vy, vz, rinv, 1.0f, ns.x, ns.y, ns.z); // cos_scat = dot(uv, n_A)
+    return cos_gate(vx, vy, vz, rinv, 1.0f, ns.x, ns.y, ns.z) && cos_gate(vx, vy, vz, rinv, -1.0f, nt.x, nt.y, nt.z);
+}
+
+// The shadow ray of a pair: origin and end point (OptiX.cu:81-93, 163-175, 321-333).
+template <int HOP>
+__device__ __forceinline__ void pair_ray(float4 s, float4 ns, float4 t, int ft, float3 &o, float3 &e)
+{
+    bool src_first = true;  // source point, target fragment (NO_RESP), lower facet (SELF)
+    if (HOP == HOP_FP) src_first = false;  // from the field point
+    if (HOP == HOP_F2F) src_first = __float_as_int(ns.w) < ft;
+    o = src_first ? make_float3(s.x, s.y, s.z) : make_float3(t.x, t.y, t.z);
+    e = src_first ? make_float3(t.x, t.y, t.z) : make_float3(s.x, s.y, s.z);
+}
+
+// Occlusion by the block's candidate triangles held in shared memory.
+__device__ __forceinline__ bool occluded_list(const float4 *sT, int n, float3 o, float3 e)
+{
+    const float vx = __fsub_rn(e.x, o.x), vy = __fsub_rn(e.y, o.y), vz = __fsub_rn(e.z, o.z);
+    const float r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
+    const float tmax = __fsub_rn(r, 1e-3f);
+    const float sc = 1.0f + fmaxf(fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fmaxf(fabsf(o.z), fabsf(e.x))),
+                                  fmaxf(fabsf(e.y), fabsf(e.z)));
+    const float eps = 1e-4f * sc;
+    const float3 d = make_float3(e.x - o.x, e.y - o.y, e.z - o.z);
+    for (int k = 0; k < n; ++k)
+        if (tri_blocks_v(sT[4 * k], sT[4 * k + 1], sT[4 * k + 2], sT[4 * k + 3], o, e, d, r, tmax, eps)) return true;
+    return false;
+}
+
+__device__ __forceinline__ bool occluded_full(const BvhView &B, float3 o, float3 e)
+{
+    const float vx = __fsub_rn(e.x, o.x), vy = __fsub_rn(e.y, o.y), vz = __fsub_rn(e.z, o.z);
+    const float r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
+    return occluded(B, o, e, r, __fsub_rn(r, 1e-3f));
+}
+
+// ---- block-level occluder culling
+constexpr int kMaxCand = 32;  // candidate triangles tested per block in shared memory
+
+// order-preserving float <-> int map for shared-memory atomic min / max
+__device__ __forceinline__ int f2o(float f)
+{
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float o2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+__device__ __forceinline__ float plane_dist(const float4 P, float x, float y, float z)
+{
+    // the same expression as tri_blocks, so verdicts derived from it agree
+    return fmaf(P.x, x, fmaf(P.y, y, P.z * z)) - P.w;
+}
+
+// Can a triangle with signed-distance ranges [o_lo, o_hi] over the ray
+// origins and [e_lo, e_hi] over the endpoints occlude any ray of the block?
+// rmax bounds every ray's length.  false only when provably not:
+//  (a) all origins and endpoints on one closed side: no strict crossing;
+//  (b) every origin within 1e-4 of the plane: the origin-plane exclusion
+//      (eps = 1e-4 * scale >= 1e-4) removes it from every ray;
+//  (c) origins at distance >= o0 > 0 on one side and endpoints within e1 of
+//      the plane: any crossing lies within rmax*e1/o0 of the endpoint, beyond
+//      tmax = r - 1e-3 when o0 * 0.8e-3 > 1.1 * rmax * e1 (the margins cover
+//      the rounding of tmax and of the FP32 comparison in tri_blocks).
+__device__ __forceinline__ bool may_occlude(float o_lo, float o_hi, float e_lo, float e_hi, float rmax)
+{
+    if (fminf(o_lo, e_lo) >= 0.0f || fmaxf(o_hi, e_hi) <= 0.0f) return false;
+    if (fmaxf(fabsf(o_lo), fabsf(o_hi)) <= 1e-4f) return false;
+    const bool one_side = o_lo > 0.0f || o_hi < 0.0f;
+    if (one_side) {
+        const float o0 = fminf(fabsf(o_lo), fabsf(o_hi));
+        const float e1 = fmaxf(fabsf(e_lo), fabsf(e_hi));
+        if (o0 * 0.8e-3f > rmax * e1 * 1.1f + 1e-30f) return false;
     }
+    return true;
 }
 
 template <int HOP>
@@ -178,26 +257,43 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
 {
     __shared__ float4 sP[kTile];
     __shared__ float4 sN[kTile];
+    __shared__ float4 sTri[4 * kMaxCand];
+    __shared__ int sCand[kMaxCand];
+    __shared__ int sRed[kMaxCand][4];  // ordered-int min/max of distances: src lo, src hi, dst lo, dst hi
+    __shared__ int sBox[6];            // ordered-int union box of all points: lo xyz, hi xyz
+    __shared__ int sFac[4];            // src facet lo/hi, dst facet lo/hi
+    __shared__ int sNc, sKeep, sOverflow;
     const int tid = threadIdx.x;
     const int tile = blockIdx.y;
     const int i0 = tile * kTile;
     const int j = blockIdx.x * kTile + tid;
-    {
-        const int i = i0 + tid;
-        float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        float4 n = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
-        if (i < a.nsrc) {
-            p = a.src_pos[i];
-            if (a.src_facet) {
-                const int f = a.src_facet[i];
-                const float4 fn = a.src_facet_n[f];
-                n = make_float4(fn.x, fn.y, fn.z, __int_as_float(f));
-            }
-        }
-        sP[tid] = p;
-        sN[tid] = n;
-    }
+    const bool src_ok = i0 + tid < a.nsrc;
     const bool live = j < a.ndst;
+    const long long fidx = (long long)tile * a.mask.ndstblocks + blockIdx.x;
+    if (HOP == HOP_F2F && a.upper_only && tile > (int)blockIdx.x) {
+        // the symmetric bounce sum reads each unordered block once, from its upper side
+        if (tid == 0) a.mask.flags[fidx] = kFlagNone;
+        return;
+    }
+    if (tid < 6) sBox[tid] = tid < 3 ? f2o(3.0e38f) : f2o(-3.0e38f);
+    if (tid < 4) sFac[tid] = (tid & 1) ? -2147483647 : 2147483647;
+    if (tid == 0) {
+        sNc = 0;
+        sKeep = 0;
+        sOverflow = 0;
+    }
+    float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 n = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+    if (src_ok) {
+        p = a.src_pos[i0 + tid];
+        if (a.src_facet) {
+            const int f = a.src_facet[i0 + tid];
+            const float4 fn = a.src_facet_n[f];
+            n = make_float4(fn.x, fn.y, fn.z, __int_as_float(f));
+        }
+    }
+    sP[tid] = p;
+    sN[tid] = n;
     float4 t = make_float4(0.0f, 0.0f, 0.0f, 0.0f), nt = t;
     int ft = -2;
     if (live) {
@@ -207,7 +303,219 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
             nt = a.dst_facet_n[ft];
         }
     }
+    // union box of the block's points and the facet ranges of both sides
+    {
+        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        if (src_ok) {
+            lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
+            hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
+        }
+        if (live) {
+            lo[0] = fminf(lo[0], t.x); lo[1] = fminf(lo[1], t.y); lo[2] = fminf(lo[2], t.z);
+            hi[0] = fmaxf(hi[0], t.x); hi[1] = fmaxf(hi[1], t.y); hi[2] = fmaxf(hi[2], t.z);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            for (int off = 16; off > 0; off >>= 1) {
+                lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], off));
+                hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], off));
+            }
+        }
+        int fs_lo = src_ok ? __float_as_int(n.w) : 2147483647, fs_hi = src_ok ? __float_as_int(n.w) : -2147483647;
+        int fd_lo = live ? ft : 2147483647, fd_hi = live ? ft : -2147483647;
+        for (int off = 16; off > 0; off >>= 1) {
+            fs_lo = min(fs_lo, __shfl_xor_sync(0xffffffffu, fs_lo, off));
+            fs_hi = max(fs_hi, __shfl_xor_sync(0xffffffffu, fs_hi, off));
+            fd_lo = min(fd_lo, __shfl_xor_sync(0xffffffffu, fd_lo, off));
+            fd_hi = max(fd_hi, __shfl_xor_sync(0xffffffffu, fd_hi, off));
+        }
+        __syncthreads();  // shared-memory initialisation above is complete
+        if ((tid & 31) == 0) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(&sBox[k], f2o(lo[k]));
+                atomicMax(&sBox[3 + k], f2o(hi[k]));
+            }
+            atomicMin(&sFac[0], fs_lo);
+            atomicMax(&sFac[1], fs_hi);
+            atomicMin(&sFac[2], fd_lo);
+            atomicMax(&sFac[3], fd_hi);
+        }
+    }
     __syncthreads();
+
+    // ---- FACET_SELF blocks whose fragments all share one facet interact nowhere
+    if (HOP == HOP_F2F && sFac[0] == sFac[1] && sFac[2] == sFac[3] && sFac[0] == sFac[2]) {
+        if (tid == 0) a.mask.flags[fidx] = kFlagNone;
+        return;
+    }
+
+    // ---- block culling of occluders
+    const bool have_tris = a.bvh.ntri > 0;
+    if (have_tris) {
+        // candidate triangles: all of them in small scenes, else the BVH leaves
+        // whose boxes overlap the block's union box
+        if (tid == 0) {
+            if (a.bvh.ntri <= kMaxCand) {
+                for (int q = 0; q < a.bvh.ntri; ++q) sCand[q] = q;
+                sNc = a.bvh.ntri;
+            } else {
+                const float bl[3] = {o2f(sBox[0]), o2f(sBox[1]), o2f(sBox[2])};
+                const float bh[3] = {o2f(sBox[3]), o2f(sBox[4]), o2f(sBox[5])};
+                int stack[kStack];
+                int sp = 0, node = 0, nc = 0;
+                bool over = false;
+                for (int guard = 0; guard < a.bvh.nnodes && !over; ++guard) {
+                    const float4 na = __ldg(a.bvh.nodes + 2 * node), nb = __ldg(a.bvh.nodes + 2 * node + 1);
+                    bool descend = false;
+                    if (na.x <= bh[0] && nb.x >= bl[0] && na.y <= bh[1] && nb.y >= bl[1] && na.z <= bh[2] &&
+                        nb.z >= bl[2]) {
+                        const int left = __float_as_int(na.w), right = __float_as_int(nb.w);
+                        if (left < 0) {
+                            for (int q = -left - 1; q < -left - 1 + right; ++q) {
+                                if (nc >= kMaxCand) {
+                                    over = true;
+                                    break;
+                                }
+                                sCand[nc++] = q;
+                            }
+                        } else {
+                            if (sp < kStack) stack[sp++] = right;
+                            node = left;
+                            descend = true;
+                        }
+                    }
+                    if (!descend) {
+                        if (sp == 0) break;
+                        node = stack[--sp];
+                    }
+                }
+                sNc = nc;
+                sOverflow = over ? 1 : 0;
+            }
+        }
+        __syncthreads();
+        const int nc = sNc;
+        if (!sOverflow && nc > 0) {
+            // signed-distance ranges of every candidate over the block's points
+            for (int c = tid; c < nc * 4; c += kTile) sRed[c >> 2][c & 3] = (c & 1) ? f2o(-3.0e38f) : f2o(3.0e38f);
+            __syncthreads();
+            for (int c = 0; c < nc; ++c) {
+                const float4 P = __ldg(a.bvh.tris + 4 * sCand[c]);
+                float sl = 3.0e38f, sh = -3.0e38f, dl = 3.0e38f, dh = -3.0e38f;
+                if (src_ok) sl = sh = plane_dist(P, p.x, p.y, p.z);
+                if (live) dl = dh = plane_dist(P, t.x, t.y, t.z);
+                for (int off = 16; off > 0; off >>= 1) {
+                    sl = fminf(sl, __shfl_xor_sync(0xffffffffu, sl, off));
+                    sh = fmaxf(sh, __shfl_xor_sync(0xffffffffu, sh, off));
+                    dl = fminf(dl, __shfl_xor_sync(0xffffffffu, dl, off));
+                    dh = fmaxf(dh, __shfl_xor_sync(0xffffffffu, dh, off));
+                }
+                if ((tid & 31) == 0) {
+                    atomicMin(&sRed[c][0], f2o(sl));
+                    atomicMax(&sRed[c][1], f2o(sh));
+                    atomicMin(&sRed[c][2], f2o(dl));
+                    atomicMax(&sRed[c][3], f2o(dh));
+                }
+            }
+            __syncthreads();
+            if (tid == 0) {
+                const float dx = o2f(sBox[3]) - o2f(sBox[0]), dy = o2f(sBox[4]) - o2f(sBox[1]),
+                            dz = o2f(sBox[5]) - o2f(sBox[2]);
+                const float rmax = sqrtf(dx * dx + dy * dy + dz * dz) * 1.0001f;
+                // which side holds the ray origins
+                bool src_origin = (HOP == HOP_SRC || HOP == HOP_NORESP);
+                bool dst_origin = (HOP == HOP_FP);
+                if (HOP == HOP_F2F) {
+                    src_origin = sFac[0] < sFac[3];  // some source facet below some destination facet
+                    dst_origin = sFac[2] < sFac[1];
+                }
+                int keep = 0;
+                for (int c = 0; c < nc; ++c) {
+                    const float sl = o2f(sRed[c][0]), sh = o2f(sRed[c][1]), dl = o2f(sRed[c][2]), dh = o2f(sRed[c][3]);
+                    bool m = false;
+                    if (src_origin) m = m || may_occlude(sl, sh, dl, dh, rmax);
+                    if (dst_origin) m = m || may_occlude(dl, dh, sl, sh, rmax);
+                    if (m) {
+                        const float4 *T = a.bvh.tris + 4 * sCand[c];
+                        sTri[4 * keep] = T[0];
+                        sTri[4 * keep + 1] = T[1];
+                        sTri[4 * keep + 2] = T[2];
+                        sTri[4 * keep + 3] = T[3];
+                        ++keep;
+                    }
+                }
+                sKeep = keep;
+            }
+            __syncthreads();
+        }
+    }
+    const int nkeep = sKeep;
+    const bool overflow = have_tris && sOverflow;
+
+    // ---- block class.  CLEAR: no triangle can occlude any pair, so the sum
+    // kernel evaluates the gates inline and no bits are stored (unless the full
+    // mask is requested).  FACET_SELF blocks whose sides share a facet range
+    // keep per-pair bits: the inline gates do not see the source facet.
+    bool clear = !overflow && nkeep == 0;
+    if (HOP == HOP_F2F) clear = clear && (sFac[1] < sFac[2] || sFac[3] < sFac[0]);
+    if (clear && !a.full) {
+        // ALL: every pair passes its cosine gates with margin.  With one source
+        // facet normal n_s and one destination facet normal n_d per block, the
+        // gate values are dot(+-v, n) / |v| with v = p_dst - p_src; their minima
+        // are bounded below by plane-distance ranges over the block divided by
+        // the longest pair distance.  When the bound clears 1e-5 (the per-pair
+        // estimates are within 1e-6 of the exact values, so the exact gates
+        // pass), no pair needs a gate.
+        const bool need_s = HOP != HOP_SRC, need_d = (HOP == HOP_SRC && !a.dst_is_field) || HOP == HOP_F2F;
+        const bool uni = (!need_s || sFac[0] == sFac[1]) && (!need_d || sFac[2] == sFac[3]);
+        bool all = false;
+        if (uni) {
+            const float4 ns = sN[0];
+            float4 nd = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (need_d) nd = a.dst_facet_n[a.dst_facet[blockIdx.x * kTile]];
+            // ranges of p.n_s and p.n_d over sources and destinations
+            float s_s = -3.0e38f, s_d = 3.0e38f, d_s = 3.0e38f, d_d = -3.0e38f;
+            if (src_ok) {
+                s_s = fmaf(p.x, ns.x, fmaf(p.y, ns.y, p.z * ns.z));
+                s_d = fmaf(p.x, nd.x, fmaf(p.y, nd.y, p.z * nd.z));
+            }
+            if (live) {
+                d_s = fmaf(t.x, ns.x, fmaf(t.y, ns.y, t.z * ns.z));
+                d_d = fmaf(t.x, nd.x, fmaf(t.y, nd.y, t.z * nd.z));
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+                s_s = fmaxf(s_s, __shfl_xor_sync(0xffffffffu, s_s, off));
+                s_d = fminf(s_d, __shfl_xor_sync(0xffffffffu, s_d, off));
+                d_s = fminf(d_s, __shfl_xor_sync(0xffffffffu, d_s, off));
+                d_d = fmaxf(d_d, __shfl_xor_sync(0xffffffffu, d_d, off));
+            }
+            if (tid < kMaxCand && tid < 4) sRed[0][tid] = (tid == 0 || tid == 3) ? f2o(-3.0e38f) : f2o(3.0e38f);
+            __syncthreads();
+            if ((tid & 31) == 0) {
+                atomicMax(&sRed[0][0], f2o(s_s));
+                atomicMin(&sRed[0][1], f2o(s_d));
+                atomicMin(&sRed[0][2], f2o(d_s));
+                atomicMax(&sRed[0][3], f2o(d_d));
+            }
+            __syncthreads();
+            const float dx = o2f(sBox[3]) - o2f(sBox[0]), dy = o2f(sBox[4]) - o2f(sBox[1]),
+                        dz = o2f(sBox[5]) - o2f(sBox[2]);
+            const float rmax = sqrtf(dx * dx + dy * dy + dz * dz) * 1.0001f;
+            float S = 1.0f;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) S = fmaxf(S, 1.0f + fabsf(o2f(sBox[k])));
+            const float thr = rmax * 1e-5f + S * 1e-6f;
+            // source-side gate: dot(v, n_s) >= d_s - s_s ; destination side: -dot(v, n_d) >= s_d - d_d
+            const bool ok_s = !need_s || (o2f(sRed[0][2]) - o2f(sRed[0][0]) > thr);
+            const bool ok_d = !need_d || (o2f(sRed[0][1]) - o2f(sRed[0][3]) > thr);
+            all = ok_s && ok_d;
+        }
+        if (tid == 0) a.mask.flags[fidx] = all ? kFlagAll : kFlagClear;
+        return;
+    }
+
+    // ---- pairs
     const int ntile = min(kTile, a.nsrc - i0);
     const int nw = (ntile + 31) >> 5;
     uint32_t any = 0;
@@ -217,14 +525,25 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
             const int bmax = min(32, ntile - w * 32);
             for (int b = 0; b < bmax; ++b) {
                 const int q = w * 32 + b;
-                if (pair_pass<HOP>(a, sP[q], sN[q], t, nt, ft)) word |= 1u << b;
+                const float4 sq = sP[q], nq = sN[q];
+                if (!pair_gates<HOP>(a, sq, nq, t, nt, ft)) continue;
+                bool vis = true;
+                if (!clear) {
+                    float3 o, e;
+                    pair_ray<HOP>(sq, nq, t, ft, o, e);
+                    if (overflow)
+                        vis = !occluded_full(a.bvh, o, e);
+                    else if (nkeep > 0)
+                        vis = !occluded_list(sTri, nkeep, o, e);
+                }
+                if (vis) word |= 1u << b;
             }
             a.mask.bits[(long long)(tile * kWordsPerTile + w) * a.mask.pitch + j] = word;
         }
         any |= word;
     }
     const int blk = __syncthreads_or(any != 0u);
-    if (tid == 0) a.mask.flags[(long long)tile * a.mask.ndstblocks + blockIdx.x] = blk ? 1 : 0;
+    if (tid == 0) a.mask.flags[fidx] = clear ? kFlagClear : (blk ? kFlagBits : kFlagNone);
 }
 
 // ---------------------------------------------------------------- sums
@@ -233,15 +552,30 @@ struct Dst {
     float nx, ny, nz;
 };
 
-template <int HOP>
-__device__ __forceinline__ void pair_term(const SumArgs &a, const float4 A, const float4 B, const Dst &d, float &tr,
-                                          float &ti)
+// Gate from an estimate already at hand (same band rule as cos_gate): the
+// decision always equals the reference's exact FP32 one.
+__device__ __forceinline__ bool gate_from(float est, float vx, float vy, float vz, float sign, float nx, float ny,
+                                          float nz)
 {
-    // v = p_dst - p_src; |v| with the reference's rounding (its r feeds the phase)
+    if (est > 2e-6f) return true;
+    if (est < 0.0f) return false;
+    return !(exact_cos(vx, vy, vz, sign, nx, ny, nz) < 1e-6f);
+}
+
+// One pair's term.  GATE: also evaluate the pair's cosine gates inline (CLEAR
+// blocks) and return them in ok.
+template <int HOP, bool ATT, bool GATE>
+__device__ __forceinline__ void pair_term(const SumArgs &a, const float4 A, const float4 B, const Dst &d, float &tr,
+                                          float &ti, bool &ok)
+{
+    // v = p_dst - p_src; |v|^2 with the reference's rounding (its r feeds the phase)
     const float vx = __fsub_rn(d.px, A.x), vy = __fsub_rn(d.py, A.y), vz = __fsub_rn(d.pz, A.z);
     const float r2 = dot_rn(vx, vy, vz, vx, vy, vz);
-    const float r = __fsqrt_rn(r2);
+    // r: one Newton step on the reciprocal square root, r = r0 + (r2 - r0^2) / (2 r0)
+    // with r0 = r2 * rsqrt(r2); within an ulp of the correctly rounded root
     const float rinv = rsqrtf(r2);
+    const float r0 = r2 * rinv;
+    const float r = fmaf(fmaf(-r0, r0, r2), 0.5f * rinv, r0);
     // phase k r in turns: r * (k / 2 pi) as an exact two-float product plus the
     // low part of k / 2 pi, the integer part removed exactly
     const float th = __fmul_rn(r, a.k2hi);
@@ -249,32 +583,51 @@ __device__ __forceinline__ void pair_term(const SumArgs &a, const float4 A, cons
     const float frac = (th - rintf(th)) + tl;
     float sn, cs;
     __sincosf(frac * kTwoPi, &sn, &cs);
-    float damp = 1.0f;
-    if (a.ka != 0.0f) damp = __expf(-a.ka * r);
+    const float damp = ATT ? __expf(-a.ka * r) : 1.0f;
+    ok = true;
     if (HOP == HOP_SRC) {
         // cos_inc P e^{ikr} / r
         float ci = -(vx * d.nx + vy * d.ny + vz * d.nz) * rinv;
-        if (a.dst_is_field) ci = 1.0f;
-        const float amp = ci * rinv * damp;
+        if (a.dst_is_field)
+            ci = 1.0f;
+        else if (GATE)
+            ok = gate_from(ci, vx, vy, vz, -1.0f, d.nx, d.ny, d.nz);
+        const float amp = ATT ? ci * rinv * damp : ci * rinv;
         const float er = amp * cs, ei = amp * sn;
         tr = er * A.w - ei * B.w;
         ti = er * B.w + ei * A.w;
     } else {
-        const float amp = rinv * kInv4Pi * damp;
         // -e^{ikr}/(4 pi) * (ik/r) + 1/r^2
-        float gr = fmaf(amp, fmaf(a.ka, cs, a.kr * sn), rinv * rinv);
-        float gi = amp * fmaf(a.ka, sn, -a.kr * cs);
-        float wgt;
-        if (HOP == HOP_FP) {
-            wgt = (vx * B.x + vy * B.y + vz * B.z) * rinv;                     // cos_scat
-        } else if (HOP == HOP_F2F) {
-            wgt = -(vx * B.x + vy * B.y + vz * B.z) * (vx * d.nx + vy * d.ny + vz * d.nz) * (rinv * rinv);
+        const float rinv2 = rinv * rinv;
+        float gr, gi;
+        if (ATT) {
+            const float amp = rinv * kInv4Pi * damp;
+            gr = fmaf(amp, fmaf(a.ka, cs, a.kr * sn), rinv2);
+            gi = amp * fmaf(a.ka, sn, -a.kr * cs);
         } else {
-            wgt = (vx * B.x + vy * B.y + vz * B.z) * rinv;                     // cos_scat, cos_inc = 1
+            const float ampk = rinv * (kInv4Pi * a.kr);
+            gr = fmaf(ampk, sn, rinv2);
+            gi = -ampk * cs;
         }
-        if (HOP != HOP_FP && r < a.rmin) {
-            gr = -a.ka * kInv4Pi;
-            gi = a.kr * kInv4Pi;
+        const float c1 = (vx * B.x + vy * B.y + vz * B.z) * rinv;  // cos_scat (source side)
+        float wgt;
+        if (HOP == HOP_F2F) {
+            const float c2 = -(vx * d.nx + vy * d.ny + vz * d.nz) * rinv;  // cos_inc (destination side)
+            wgt = c1 * c2;
+            if (GATE) ok = gate_from(c1, vx, vy, vz, 1.0f, B.x, B.y, B.z) && gate_from(c2, vx, vy, vz, -1.0f, d.nx, d.ny, d.nz);
+        } else {
+            wgt = c1;
+            if (GATE) ok = gate_from(c1, vx, vy, vz, 1.0f, B.x, B.y, B.z);
+        }
+        if (HOP != HOP_FP) {
+            // regularised G below r_min = delta_src (OptiX.cu:340-346); near the
+            // threshold the branch uses the correctly rounded r, as the reference
+            float rr = r;
+            if (fabsf(r - a.rmin) <= a.rmin * 4e-7f) rr = __fsqrt_rn(r2);
+            if (rr < a.rmin) {
+                gr = -a.ka * kInv4Pi;
+                gi = a.kr * kInv4Pi;
+            }
         }
         gr *= wgt;
         gi *= wgt;
@@ -283,7 +636,7 @@ __device__ __forceinline__ void pair_term(const SumArgs &a, const float4 A, cons
     }
 }
 
-template <int HOP>
+template <int HOP, bool ATT>
 __global__ void __launch_bounds__(kTile) k_sum(SumArgs a)
 {
     __shared__ float4 sA[kTile];
@@ -306,7 +659,8 @@ __global__ void __launch_bounds__(kTile) k_sum(SumArgs a)
     const int t0 = blockIdx.y * a.tiles_per_split;
     const int t1 = min(t0 + a.tiles_per_split, a.mask.ntiles);
     for (int t = t0; t < t1; ++t) {
-        if (!a.mask.flags[(long long)t * a.mask.ndstblocks + blockIdx.x]) continue;  // uniform per CTA
+        const uint8_t fl = a.mask.flags[(long long)t * a.mask.ndstblocks + blockIdx.x];  // uniform per CTA
+        if (fl == kFlagNone) continue;
         __syncthreads();
         {
             const int i = t * kTile + tid;
@@ -319,7 +673,13 @@ __global__ void __launch_bounds__(kTile) k_sum(SumArgs a)
         const int nw = (ntile + 31) >> 5;
         float fr = 0.0f, fi = 0.0f;
         for (int w = 0; w < nw; ++w) {
-            uint32_t m = live ? a.mask.bits[(long long)(t * kWordsPerTile + w) * a.mask.pitch + j] : 0u;
+            uint32_t m;
+            if (fl == kFlagBits) {
+                m = live ? a.mask.bits[(long long)(t * kWordsPerTile + w) * a.mask.pitch + j] : 0u;
+            } else {
+                const int nb = ntile - w * 32;  // CLEAR / ALL: every valid source
+                m = !live ? 0u : (nb >= 32 ? 0xffffffffu : ((1u << nb) - 1u));
+            }
             if (HOP == HOP_F2F) {
                 // FACET_SELF zero-input rule: when this destination's input is 0
                 // the sources of higher facets (its reciprocal partners) drop out
@@ -327,21 +687,248 @@ __global__ void __launch_bounds__(kTile) k_sum(SumArgs a)
                 m &= keep >= 32 ? 0xffffffffu : (keep <= 0 ? 0u : ((1u << keep) - 1u));
             }
             if (!__any_sync(0xffffffffu, m != 0u)) continue;
+            if (fl != kFlagClear) {
 #pragma unroll 8
-            for (int b = 0; b < 32; ++b) {
-                const float4 A = sA[w * 32 + b];
-                const float4 B = sB[w * 32 + b];
-                float tr, ti;
-                pair_term<HOP>(a, A, B, d, tr, ti);
-                const bool on = (m >> b) & 1u;
-                fr += on ? tr : 0.0f;
-                fi += on ? ti : 0.0f;
+                for (int b = 0; b < 32; ++b) {
+                    const float4 A = sA[w * 32 + b];
+                    const float4 B = sB[w * 32 + b];
+                    float tr, ti;
+                    bool ok;
+                    pair_term<HOP, ATT, false>(a, A, B, d, tr, ti, ok);
+                    const bool on = (m >> b) & 1u;
+                    fr += on ? tr : 0.0f;
+                    fi += on ? ti : 0.0f;
+                }
+            } else {
+#pragma unroll 8
+                for (int b = 0; b < 32; ++b) {
+                    const float4 A = sA[w * 32 + b];
+                    const float4 B = sB[w * 32 + b];
+                    float tr, ti;
+                    bool ok;
+                    pair_term<HOP, ATT, true>(a, A, B, d, tr, ti, ok);
+                    const bool on = ((m >> b) & 1u) && ok;
+                    fr += on ? tr : 0.0f;
+                    fi += on ? ti : 0.0f;
+                }
             }
         }
         accr += (double)fr;
         acci += (double)fi;
     }
     if (live) a.partial[(long long)blockIdx.y * a.ndst + j] = make_double2(accr, acci);
+}
+
+// ---------------------------------------------------------------- symmetric bounce sum
+// FACET_SELF with reciprocity evaluated once per unordered pair, as the
+// reference does (OptiX.cu:367-390): for source tile I < destination tile J
+// the CTA computes T_ij = 0.9-free G(r_ij) cos_scat cos_inc once per pair and
+// adds T_ij w_i into its destination row j (registers) and T_ij w_j into the
+// column of i (warp reductions, per-warp shared sums, one write per (I, J)).
+// Tiles are in facet order, so every interacting pair of such a block has
+// facet(i) < facet(j): the row term is the forward term and the column term
+// the reciprocal one, dropped in the final reduction when P_in[i] == 0.
+// The diagonal tile (I == J) runs the destination-owned loop.  Column sums of
+// (I, J) land at colpart[256 J (J-1) / 2 + i]; k_finalize_f2f_sym adds them in
+// a fixed order (deterministic results).
+template <bool ATT, bool GATE>
+__device__ __forceinline__ void sym_pair(const SumArgs &a, const float4 A, const float4 B, const Dst &d, float &Tr,
+                                         float &Ti, bool &ok)
+{
+    const float vx = __fsub_rn(d.px, A.x), vy = __fsub_rn(d.py, A.y), vz = __fsub_rn(d.pz, A.z);
+    const float r2 = dot_rn(vx, vy, vz, vx, vy, vz);
+    const float rinv = rsqrtf(r2);
+    const float r0 = r2 * rinv;
+    const float r = fmaf(fmaf(-r0, r0, r2), 0.5f * rinv, r0);
+    const float th = __fmul_rn(r, a.k2hi);
+    const float tl = fmaf(r, a.k2lo, fmaf(r, a.k2hi, -th));
+    const float frac = (th - rintf(th)) + tl;
+    float sn, cs;
+    __sincosf(frac * kTwoPi, &sn, &cs);
+    const float rinv2 = rinv * rinv;
+    float gr, gi;
+    if (ATT) {
+        const float amp = rinv * kInv4Pi * __expf(-a.ka * r);
+        gr = fmaf(amp, fmaf(a.ka, cs, a.kr * sn), rinv2);
+        gi = amp * fmaf(a.ka, sn, -a.kr * cs);
+    } else {
+        const float ampk = rinv * (kInv4Pi * a.kr);
+        gr = fmaf(ampk, sn, rinv2);
+        gi = -ampk * cs;
+    }
+    const float c1 = (vx * B.x + vy * B.y + vz * B.z) * rinv;
+    const float c2 = -(vx * d.nx + vy * d.ny + vz * d.nz) * rinv;
+    ok = true;
+    if (GATE) ok = gate_from(c1, vx, vy, vz, 1.0f, B.x, B.y, B.z) && gate_from(c2, vx, vy, vz, -1.0f, d.nx, d.ny, d.nz);
+    float rr = r;
+    if (fabsf(r - a.rmin) <= a.rmin * 4e-7f) rr = __fsqrt_rn(r2);
+    if (rr < a.rmin) {
+        gr = -a.ka * kInv4Pi;
+        gi = a.kr * kInv4Pi;
+    }
+    const float wgt = c1 * c2;
+    Tr = gr * wgt;
+    Ti = gi * wgt;
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+template <bool ATT>
+__global__ void __launch_bounds__(kTile) k_sum_f2f_sym(SumArgs a, double2 *colpart)
+{
+    __shared__ float4 sA[kTile];
+    __shared__ float4 sB[kTile];
+    __shared__ float2 sCol[kTile / 32][kTile];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int J = blockIdx.x;
+    const int j = J * kTile + tid;
+    const bool live = j < a.ndst;
+    Dst d{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    int limit = a.nsrc;
+    float wjr = 0.0f, wji = 0.0f;  // this destination's own source weight (the reciprocal input)
+    if (live) {
+        const float4 p = a.dst_pos[j];
+        d.px = p.x; d.py = p.y; d.pz = p.z;
+        const float4 n = a.dst_facet_n[a.dst_facet[j]];
+        d.nx = n.x; d.ny = n.y; d.nz = n.z;
+        limit = a.dst_limit[j];
+        wjr = a.srcA[j].w;
+        wji = a.srcB[j].w;
+    }
+    const long long cbase = (long long)kTile * J * (J - 1) / 2;  // this J's column region
+    double accr = 0.0, acci = 0.0;
+    const int t0 = blockIdx.y * a.tiles_per_split;
+    const int t1 = min(t0 + a.tiles_per_split, J + 1);
+    for (int t = t0; t < t1; ++t) {
+        const uint8_t fl = a.mask.flags[(long long)t * a.mask.ndstblocks + J];
+        const int i0 = t * kTile;
+        if (fl == kFlagNone) {
+            if (t < J) colpart[cbase + i0 + tid] = make_double2(0.0, 0.0);
+            continue;
+        }
+        __syncthreads();
+        {
+            const int i = i0 + tid;
+            const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            sA[tid] = i < a.nsrc ? a.srcA[i] : z;
+            sB[tid] = i < a.nsrc ? a.srcB[i] : z;
+        }
+        __syncthreads();
+        const int ntile = min(kTile, a.nsrc - i0);
+        const int nw = (ntile + 31) >> 5;
+        float fr = 0.0f, fi = 0.0f;
+        if (t == J) {
+            // diagonal tile: destination-owned, with the zero-input source limit
+            for (int w = 0; w < nw; ++w) {
+                uint32_t m;
+                if (fl == kFlagBits) {
+                    m = live ? a.mask.bits[(long long)(t * kWordsPerTile + w) * a.mask.pitch + j] : 0u;
+                } else {
+                    const int nb = ntile - w * 32;
+                    m = !live ? 0u : (nb >= 32 ? 0xffffffffu : ((1u << nb) - 1u));
+                }
+                const int keep = limit - (i0 + w * 32);
+                m &= keep >= 32 ? 0xffffffffu : (keep <= 0 ? 0u : ((1u << keep) - 1u));
+                if (!__any_sync(0xffffffffu, m != 0u)) continue;
+                for (int b = 0; b < 32; ++b) {
+                    const float4 A = sA[w * 32 + b], B = sB[w * 32 + b];
+                    float Tr, Ti;
+                    bool ok;
+                    if (fl != kFlagClear)
+                        sym_pair<ATT, false>(a, A, B, d, Tr, Ti, ok);
+                    else
+                        sym_pair<ATT, true>(a, A, B, d, Tr, Ti, ok);
+                    const bool on = ((m >> b) & 1u) && ok;
+                    fr += on ? Tr * A.w - Ti * B.w : 0.0f;
+                    fi += on ? Tr * B.w + Ti * A.w : 0.0f;
+                }
+            }
+        } else {
+            for (int w = 0; w < nw; ++w) {
+                uint32_t m;
+                if (fl == kFlagBits) {
+                    m = live ? a.mask.bits[(long long)(t * kWordsPerTile + w) * a.mask.pitch + j] : 0u;
+                } else {
+                    const int nb = ntile - w * 32;
+                    m = !live ? 0u : (nb >= 32 ? 0xffffffffu : ((1u << nb) - 1u));
+                }
+                if (!__any_sync(0xffffffffu, m != 0u)) {
+                    if (lane == 0)
+                        for (int b = 0; b < 32; ++b) sCol[warp][w * 32 + b] = make_float2(0.0f, 0.0f);
+                    continue;
+                }
+#pragma unroll 4
+                for (int b = 0; b < 32; ++b) {
+                    const float4 A = sA[w * 32 + b], B = sB[w * 32 + b];
+                    float Tr, Ti;
+                    bool ok;
+                    if (fl != kFlagClear)
+                        sym_pair<ATT, false>(a, A, B, d, Tr, Ti, ok);
+                    else
+                        sym_pair<ATT, true>(a, A, B, d, Tr, Ti, ok);
+                    const bool on = ((m >> b) & 1u) && ok;
+                    // row: forward term into this destination
+                    fr += on ? Tr * A.w - Ti * B.w : 0.0f;
+                    fi += on ? Tr * B.w + Ti * A.w : 0.0f;
+                    // column: reciprocal term into source i, summed over the warp
+                    const float cr = warp_sum(on ? Tr * wjr - Ti * wji : 0.0f);
+                    const float ci = warp_sum(on ? Tr * wji + Ti * wjr : 0.0f);
+                    if (lane == 0) sCol[warp][w * 32 + b] = make_float2(cr, ci);
+                }
+            }
+            for (int w = nw; w < kWordsPerTile; ++w)
+                if (lane == 0)
+                    for (int b = 0; b < 32; ++b) sCol[warp][w * 32 + b] = make_float2(0.0f, 0.0f);
+            __syncthreads();
+            double sr = 0.0, si = 0.0;
+#pragma unroll
+            for (int k = 0; k < kTile / 32; ++k) {
+                const float2 v = sCol[k][tid];
+                sr += (double)v.x;
+                si += (double)v.y;
+            }
+            colpart[cbase + i0 + tid] = make_double2(sr, si);
+        }
+        accr += (double)fr;
+        acci += (double)fi;
+    }
+    if (live) a.partial[(long long)blockIdx.y * a.ndst + j] = make_double2(accr, acci);
+}
+
+// P_out[cell] = rows + (P_in[i] != 0 ? columns : 0); P[cell] += P_out[cell]
+__global__ void k_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,
+                                   const int *cell, const double2 *Pin, double2 *Pout, double2 *P)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= ndst) return;
+    double sr = 0.0, si = 0.0;
+    for (int k = 0; k < nsplit; ++k) {
+        const double2 v = partial[(long long)k * ndst + q];
+        sr += v.x;
+        si += v.y;
+    }
+    const int c = cell[q];
+    const double2 pin = Pin[c];
+    if (pin.x != 0.0 || pin.y != 0.0) {
+        double cr = 0.0, ci = 0.0;
+        for (int J = q / kTile + 1; J < ntiles; ++J) {
+            const double2 v = colpart[(long long)kTile * J * (J - 1) / 2 + q];
+            cr += v.x;
+            ci += v.y;
+        }
+        sr += cr;
+        si += ci;
+    }
+    Pout[c] = make_double2(sr, si);
+    double2 o = P[c];
+    o.x += sr;
+    o.y += si;
+    P[c] = o;
 }
 
 // ---------------------------------------------------------------- helpers
@@ -514,12 +1101,43 @@ void launch_sum(const SumArgs &a, cudaStream_t s)
 {
     if (a.nsrc <= 0 || a.ndst <= 0) return;
     dim3 grid(a.mask.ndstblocks, a.nsplit);
+    const bool att = a.ka != 0.0f;
     switch (a.hop) {
-    case HOP_SRC: k_sum<HOP_SRC><<<grid, kTile, 0, s>>>(a); break;
-    case HOP_FP: k_sum<HOP_FP><<<grid, kTile, 0, s>>>(a); break;
-    case HOP_F2F: k_sum<HOP_F2F><<<grid, kTile, 0, s>>>(a); break;
-    default: k_sum<HOP_NORESP><<<grid, kTile, 0, s>>>(a); break;
+    case HOP_SRC:
+        if (att) k_sum<HOP_SRC, true><<<grid, kTile, 0, s>>>(a);
+        else k_sum<HOP_SRC, false><<<grid, kTile, 0, s>>>(a);
+        break;
+    case HOP_FP:
+        if (att) k_sum<HOP_FP, true><<<grid, kTile, 0, s>>>(a);
+        else k_sum<HOP_FP, false><<<grid, kTile, 0, s>>>(a);
+        break;
+    case HOP_F2F:
+        if (att) k_sum<HOP_F2F, true><<<grid, kTile, 0, s>>>(a);
+        else k_sum<HOP_F2F, false><<<grid, kTile, 0, s>>>(a);
+        break;
+    default:
+        if (att) k_sum<HOP_NORESP, true><<<grid, kTile, 0, s>>>(a);
+        else k_sum<HOP_NORESP, false><<<grid, kTile, 0, s>>>(a);
+        break;
     }
+}
+
+void launch_sum_f2f_sym(const SumArgs &a, double2 *colpart, cudaStream_t s)
+{
+    if (a.nsrc <= 0 || a.ndst <= 0) return;
+    dim3 grid(a.mask.ndstblocks, a.nsplit);
+    if (a.ka != 0.0f)
+        k_sum_f2f_sym<true><<<grid, kTile, 0, s>>>(a, colpart);
+    else
+        k_sum_f2f_sym<false><<<grid, kTile, 0, s>>>(a, colpart);
+}
+
+void launch_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,
+                             const int *cell, const double2 *Pin, double2 *Pout, double2 *P, cudaStream_t s)
+{
+    if (ndst > 0)
+        k_finalize_f2f_sym<<<blocks_for(ndst, 256), 256, 0, s>>>(partial, nsplit, ndst, colpart, ntiles, cell, Pin,
+                                                                 Pout, P);
 }
 
 void launch_pack_points(const float4 *pts, const double2 *P, int n, float4 *A, float4 *B, cudaStream_t s)

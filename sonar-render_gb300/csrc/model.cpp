@@ -34,6 +34,7 @@ namespace sonar {
 namespace {
 
 constexpr int OBJ_TARGET = 0, OBJ_SOURCE = 1, OBJ_FIELD = 2;
+constexpr int kPatch = 16;  // side, in cells, of the patches that order active fragments
 
 struct Error : std::runtime_error {
     int code;
@@ -101,9 +102,11 @@ struct Object {
 
 struct MaskEntry {
     int hop, a, b;
+    int upper_only = 0;
     int nsrc, ndst;
     MaskView view{};
     float mask_ms = 0.0f;
+    bool stale = false;  // rebuild into the same buffers before the next use
 };
 
 struct HopRecord {
@@ -140,9 +143,12 @@ struct Model {
     size_t partial_cap = 0;
     int *d_limit = nullptr;
     size_t limit_cap = 0;
+    double2 *d_colpart = nullptr;
+    size_t colpart_cap = 0;
     // options and statistics
     int opt_split = 0;
     int verbose = 0;
+    int opt_f2f_sym = 1;
     std::vector<HopRecord> log;
     long long launches = 0, h2d_bytes = 0, d2h_bytes = 0;
 
@@ -157,8 +163,8 @@ struct Model {
             dfree(m.view.flags);
         }
         masks.clear();
-        dfree(d_packA); dfree(d_packB); dfree(d_partial); dfree(d_limit);
-        pack_cap = partial_cap = limit_cap = 0;
+        dfree(d_packA); dfree(d_packB); dfree(d_partial); dfree(d_limit); dfree(d_colpart);
+        pack_cap = partial_cap = limit_cap = colpart_cap = 0;
         for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3})
             if (*e) {
                 cudaEventDestroy(*e);
@@ -200,14 +206,23 @@ void render_object(Object &o)
                 const Vec3 ps = fragment_centroid(F, x, y, true);
                 cell_pos[c] = make_float4(ps.x, ps.y, ps.z, A[(long long)y * F.nx + x]);
                 cell_facet[c] = f;
-                if (A[(long long)y * F.nx + x] > 1e-6f) {
-                    const Vec3 pa = fragment_centroid(F, x, y, false);
-                    act_pos.push_back(make_float4(pa.x, pa.y, pa.z, A[(long long)y * F.nx + x]));
-                    act_facet.push_back(f);
-                    o.act_cell.push_back((int)c);
-                    o.facet_nact[f]++;
-                }
             }
+        // active cells of the facet in compact 16 x 16-cell patches (patch row,
+        // patch column, then row-major inside the patch), so that 256
+        // consecutive fragments -- one source tile or destination block of the
+        // kernels -- cover a small area
+        for (int py = 0; py < F.ny; py += kPatch)
+            for (int px = 0; px < F.nx; px += kPatch)
+                for (int y = py; y < std::min(F.ny, py + kPatch); y++)
+                    for (int x = px; x < std::min(F.nx, px + kPatch); x++) {
+                        const float a = A[(long long)y * F.nx + x];
+                        if (!(a > 1e-6f)) continue;
+                        const Vec3 pa = fragment_centroid(F, x, y, false);
+                        act_pos.push_back(make_float4(pa.x, pa.y, pa.z, a));
+                        act_facet.push_back(f);
+                        o.act_cell.push_back((int)(o.cell0[f] + (long long)y * F.nx + x));
+                        o.facet_nact[f]++;
+                    }
         o.facet_act_end[f] = (int)o.act_cell.size();
     }
     const size_t nc = (size_t)o.ncells, na = o.act_cell.size();
@@ -353,15 +368,17 @@ HopSets hop_sets(int hop, int a, int b)
     return h;
 }
 
-MaskEntry &get_mask(int hop, int a, int b)
+// Build one interaction mask.  full = 0: CLEAR blocks store no bits (the sum
+// kernels evaluate their gates inline); full = 1: every block stores its bits
+// (diagnostic export).
+MaskEntry build_mask(int hop, int a, int b, int full, const MaskEntry *reuse = nullptr)
 {
-    for (auto &e : g.masks)
-        if (e.hop == hop && e.a == a && e.b == b) return e;
     HopSets hs = hop_sets(hop, a, b);
     MaskEntry e{};
     e.hop = hop;
     e.a = a;
     e.b = b;
+    e.upper_only = (hop == HOP_F2F && !full && g.opt_f2f_sym) ? 1 : 0;
     e.nsrc = hs.nsrc;
     e.ndst = hs.ndst;
     MaskView &v = e.view;
@@ -372,11 +389,19 @@ MaskEntry &get_mask(int hop, int a, int b)
     if (v.ntiles > 65535) fail(-3, "hop %d has %d sources (limit %d)", hop, hs.nsrc, 65535 * kTile);
     const size_t words = (size_t)v.ntiles * kWordsPerTile * (size_t)v.pitch;
     const size_t nflags = (size_t)v.ntiles * v.ndstblocks;
-    v.bits = dalloc<uint32_t>(words);
-    v.flags = dalloc<uint8_t>(nflags);
-    CK(cudaMemsetAsync(v.bits, 0, std::max<size_t>(words, 1) * sizeof(uint32_t), g.stream));
-    CK(cudaMemsetAsync(v.flags, 0, std::max<size_t>(nflags, 1), g.stream));
+    if (reuse) {
+        v.bits = reuse->view.bits;
+        v.flags = reuse->view.flags;
+    } else {
+        v.bits = dalloc<uint32_t>(words);
+        v.flags = dalloc<uint8_t>(nflags);
+    }
+    // every block writes its flag, and the sums read bits only of blocks that
+    // stored them; the full export also reads blocks that store none
+    if (full) CK(cudaMemsetAsync(v.bits, 0, std::max<size_t>(words, 1) * sizeof(uint32_t), g.stream));
     hs.m.mask = v;
+    hs.m.full = full;
+    hs.m.upper_only = (hop == HOP_F2F && !full && g.opt_f2f_sym) ? 1 : 0;
     CK(cudaEventRecord(g.ev0, g.stream));
     launch_mask(hs.m, g.stream);
     CK(cudaGetLastError());
@@ -384,7 +409,18 @@ MaskEntry &get_mask(int hop, int a, int b)
     CK(cudaEventRecord(g.ev1, g.stream));
     CK(cudaEventSynchronize(g.ev1));
     CK(cudaEventElapsedTime(&e.mask_ms, g.ev0, g.ev1));
-    g.masks.push_back(e);
+    return e;
+}
+
+MaskEntry &get_mask(int hop, int a, int b)
+{
+    const int upper = (hop == HOP_F2F && g.opt_f2f_sym) ? 1 : 0;
+    for (auto &e : g.masks)
+        if (e.hop == hop && e.a == a && e.b == b) {
+            if (e.stale || e.upper_only != upper) e = build_mask(hop, a, b, 0, &e);
+            return e;
+        }
+    g.masks.push_back(build_mask(hop, a, b, 0));
     return g.masks.back();
 }
 
@@ -407,6 +443,16 @@ void ensure_scratch(int nsrc, int ndst, int nsplit)
         dfree(g.d_limit);
         g.d_limit = dalloc<int>(ndst);
         g.limit_cap = ndst;
+    }
+}
+
+void ensure_colpart(int ntiles)
+{
+    const size_t n = (size_t)kTile * ntiles * (ntiles > 0 ? ntiles - 1 : 0) / 2;
+    if (n > g.colpart_cap) {
+        dfree(g.d_colpart);
+        g.d_colpart = dalloc<double2>(n);
+        g.colpart_cap = n;
     }
 }
 
@@ -487,8 +533,17 @@ void run_hop(int hop, int a, int b)
         launch_f2f_limits(A.d_act_facet, A.d_act_cell, A.d_facet_end, A.d_Pin, M.ndst, M.nsrc, g.d_limit, st);
         launch_pack_frags(A.d_act_pos, A.d_act_facet, A.d_act_cell, A.d_facet_n, A.d_Pin, 0.9f, M.nsrc, g.d_packA,
                           g.d_packB, st);
-        timed_sum(s, st);
-        launch_finalize_f2f(g.d_partial, s.nsplit, M.ndst, A.d_act_cell, A.d_Pout, A.d_P, st);
+        if (g.opt_f2f_sym) {
+            ensure_colpart(M.view.ntiles);
+            CK(cudaEventRecord(g.ev2, st));
+            launch_sum_f2f_sym(s, g.d_colpart, st);
+            CK(cudaEventRecord(g.ev3, st));
+            launch_finalize_f2f_sym(g.d_partial, s.nsplit, M.ndst, g.d_colpart, M.view.ntiles, A.d_act_cell, A.d_Pin,
+                                    A.d_Pout, A.d_P, st);
+        } else {
+            timed_sum(s, st);
+            launch_finalize_f2f(g.d_partial, s.nsplit, M.ndst, A.d_act_cell, A.d_Pout, A.d_P, st);
+        }
     } else {
         Object &A = get(OBJ_TARGET, a);
         Object &B = get(OBJ_FIELD, b);
@@ -811,6 +866,7 @@ int sonar_set_option(const char *key, double value)
 {
     if (!key) return -1;
     if (!strcmp(key, "split")) { g.opt_split = (int)value; return 0; }
+    if (!strcmp(key, "f2f_symmetric")) { g.opt_f2f_sym = value != 0.0; return 0; }
     if (!strcmp(key, "verbose")) { g.verbose = (int)value; return 0; }
     if (!strcmp(key, "reset_stats")) {
         g.log.clear();
@@ -833,6 +889,11 @@ int sonar_set_option(const char *key, double value)
         });
     }
     if (!strcmp(key, "drop_masks")) {
+        // rebuild every mask (same buffers) at its next use
+        for (auto &m : g.masks) m.stale = true;
+        return 0;
+    }
+    if (!strcmp(key, "free_masks")) {
         for (auto &m : g.masks) { dfree(m.view.bits); dfree(m.view.flags); }
         g.masks.clear();
         return 0;
@@ -846,18 +907,47 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
     int st = guarded([&] {
         need_render();
         if (hop < HOP_SRC || hop > HOP_NORESP) fail(-6, "invalid hop %d", hop);
-        MaskEntry &M = get_mask(hop, srcIdx, dstIdx);
-        nbytes = (long long)M.nsrc * M.ndst;
+        HopSets hs = hop_sets(hop, srcIdx, dstIdx);
+        nbytes = (long long)hs.nsrc * hs.ndst;
         if (!out) return;
         if (cap < nbytes) fail(-8, "mask buffer holds %lld of %lld bytes", cap, nbytes);
         if (nbytes == 0) return;
-        uint8_t *d = dalloc<uint8_t>((size_t)nbytes);
-        launch_mask_export(M.view, M.nsrc, M.ndst, d, g.stream);
-        CK(cudaGetLastError());
-        cudaError_t e = cudaMemcpyAsync(out, d, (size_t)nbytes, cudaMemcpyDeviceToHost, g.stream);
+        // a full mask (bits in every block), built for the export and freed
+        MaskEntry M = build_mask(hop, srcIdx, dstIdx, 1);
+        uint8_t *d = nullptr;
+        cudaError_t e = cudaMalloc(&d, (size_t)nbytes);
+        if (e == cudaSuccess) {
+            launch_mask_export(M.view, M.nsrc, M.ndst, d, g.stream);
+            e = cudaGetLastError();
+        }
+        std::vector<uint8_t> tmp((size_t)nbytes);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(tmp.data(), d, (size_t)nbytes, cudaMemcpyDeviceToHost, g.stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
-        cudaFree(d);
+        if (d) cudaFree(d);
+        dfree(M.view.bits);
+        dfree(M.view.flags);
         if (e != cudaSuccess) fail(-10, "mask export failed: %s", cudaGetErrorString(e));
+        // active fragments are stored in patch order; report them in cell order
+        auto canon = [](const Object &o) {
+            std::vector<int> idx(o.act_cell.size()), rank(o.act_cell.size());
+            for (size_t q = 0; q < idx.size(); q++) idx[q] = (int)q;
+            std::sort(idx.begin(), idx.end(), [&](int x, int y) { return o.act_cell[x] < o.act_cell[y]; });
+            for (size_t k = 0; k < idx.size(); k++) rank[idx[k]] = (int)k;
+            return rank;
+        };
+        std::vector<int> rs, rd;  // internal index -> canonical index (empty: identity)
+        if (hop == HOP_FP || hop == HOP_F2F || hop == HOP_NORESP) rs = canon(get(OBJ_TARGET, srcIdx));
+        if (hop == HOP_F2F) rd = rs;
+        if (hop == HOP_NORESP) rd = canon(get(OBJ_FIELD, dstIdx));
+        for (long long jd = 0; jd < M.ndst; jd++) {
+            const long long cd = rd.empty() ? jd : rd[jd];
+            const uint8_t *row = tmp.data() + jd * M.nsrc;
+            uint8_t *orow = out + cd * M.nsrc;
+            if (rs.empty())
+                memcpy(orow, row, (size_t)M.nsrc);
+            else
+                for (long long js = 0; js < M.nsrc; js++) orow[rs[js]] = row[js];
+        }
     });
     return st != 0 ? st : nbytes;
 }

@@ -12,9 +12,11 @@
 //              the centroid WITHOUT the delta/2 x shift (src/OptiX.cu:129,
 //              :210, :273), act_facet, act_cell.
 //   facet_n    unit normal per facet (float4).
-// Interaction masks: uint32 words [src_word][dst_pitch] -- bit b of word
-// (w, j) is the pair (source 32w+b, destination j) -- plus one flag byte per
-// (source tile of 256, destination block of 256) telling whether any bit is set.
+// Interaction masks: one flag byte per (source tile of 256, destination block
+// of 256): nothing interacts, per-pair bits stored, or CLEAR (no triangle can
+// occlude any pair; the sum kernel evaluates the cosine gates inline).  Bits
+// are uint32 words [src_word][dst_pitch] -- bit b of word (w, j) is the pair
+// (source 32w+b, destination j).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -25,6 +27,11 @@ enum Hop : int { HOP_SRC = 0, HOP_FP = 1, HOP_F2F = 2, HOP_NORESP = 3 };
 
 constexpr int kTile = 256;          // sources per tile, destinations per block
 constexpr int kWordsPerTile = kTile / 32;
+
+// Per-block mask flags: no pair interacts / per-pair bits stored / no triangle
+// can occlude any pair of the block, gates are evaluated inline by the sums /
+// every pair of the block interacts (no occluder, every cosine gate passes).
+constexpr uint8_t kFlagNone = 0, kFlagBits = 1, kFlagClear = 2, kFlagAll = 3;
 
 struct BvhNode {                    // 32 bytes
     float lo[3];
@@ -59,6 +66,8 @@ struct MaskArgs {
     const int *dst_facet;           // may be null (points)
     const float4 *dst_facet_n;
     int dst_is_field;               // cos_inc forced to 1 (src/OptiX.cu:67-72, :308-312)
+    int full;                       // store per-pair bits for CLEAR blocks too (diagnostic export)
+    int upper_only;                 // FACET_SELF: only blocks with source tile <= destination block
     BvhView bvh;
     MaskView mask;
 };
@@ -97,6 +106,11 @@ void launch_finalize_add(const double2 *partial, int nsplit, int ndst, const int
 void launch_finalize_f2f(const double2 *partial, int nsplit, int ndst, const int *cell, double2 *Pout,
                          double2 *P, cudaStream_t s);
 void launch_mask_export(const MaskView &m, int nsrc, int ndst, uint8_t *out, cudaStream_t s);
+// FACET_SELF with reciprocity: one Green's function per unordered pair.
+// colpart holds 256 * ntiles * (ntiles - 1) / 2 double2.
+void launch_sum_f2f_sym(const SumArgs &a, double2 *colpart, cudaStream_t s);
+void launch_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,
+                             const int *cell, const double2 *Pin, double2 *Pout, double2 *P, cudaStream_t s);
 // FP32 FMA rate in FLOP/s (which = 0) or MUFU sine rate in op/s (which = 1)
 // on the current device; < 0 on failure.
 double measure_peak(int which);
