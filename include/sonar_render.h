@@ -113,6 +113,12 @@ int sonar_get_object_pressures(int objectType, int objIdx, dcomplex *out, long l
  * same order as the pressures.  Returns the number of facets or < 0. */
 int sonar_get_fragment_layout(int objectType, int objIdx, int *nx_ny_neg, int nfacets_cap, float *areas,
                               long long ncells_cap);
+/* Surface colours of a target or field object: 4 floats (RGBA in [0, 1]) per
+ * cell in the pressure layout, the texel values the reference writes into its
+ * GL textures (MakeSurface, src/FacetCuda.cu:43-72) with the dB window and
+ * phase flags of SoundVisualisationInit.  Returns the number of cells written
+ * or < 0. */
+int sonar_get_surface_colours(int objectType, int objIdx, float *rgba, long long ncells);
 /* JSON statistics of the last projection calls (pairs, kernel ms, grazing). */
 int sonar_get_stats(char *json, int cap);
 /* Options: "split" (source splits of the sum kernels, 0 = automatic),

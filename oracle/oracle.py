@@ -105,6 +105,17 @@ def lib():
     return _lib
 
 
+def colour_map(P, min_db, max_db, phase):
+    """Reference surface colours (RGBA float32, (n, 4)) of complex pressures."""
+    L = lib()
+    P = np.asarray(P, dtype=np.complex128)
+    buf = np.ascontiguousarray(np.stack([P.real, P.imag], axis=1))
+    out = np.zeros((len(P), 4), np.float32)
+    L.orc_colour_map.argtypes = [_d, C.c_long, C.c_float, C.c_float, C.c_int, _f]
+    L.orc_colour_map(_dp(buf), len(P), C.c_float(min_db), C.c_float(max_db), int(phase), _fp(out))
+    return out
+
+
 def num_threads() -> int:
     return int(lib().orc_num_threads())
 

@@ -1212,6 +1212,42 @@ int orc_segment(void *h, const double *o, const double *e, double tmax, int *fla
     return hit;
 }
 
+/* Surface colour map of src/FacetCuda.cu:10-72 (hsv2rgb, MakeSurface) with the
+ * reference's float/double promotions: P (2 doubles per cell) -> RGBA floats. */
+static void hsv2rgb_ref(float h, float s, float v, float *o)
+{
+    float c = v * s;
+    float x = c * (1.0 - fabs(fmod(h * 6.0, 2.0) - 1.0));
+    float m = v - c;
+    float alpha = 1;
+    float r, g, b;
+    if (h < 1.0 / 6.0) { r = c + m; g = x + m; b = 0.0 + m; }
+    else if (h < 2.0 / 6.0) { r = x + m; g = c + m; b = 0.0 + m; }
+    else if (h < 3.0 / 6.0) { r = 0.0 + m; g = c + m; b = x + m; }
+    else if (h < 4.0 / 6.0) { r = 0.0 + m; g = x + m; b = c + m; }
+    else if (h < 5.0 / 6.0) { r = x + m; g = 0.0 + m; b = c + m; }
+    else { r = c + m; g = 0.0 + m; b = x + m; }
+    o[0] = r; o[1] = g; o[2] = b; o[3] = alpha;
+}
+
+void orc_colour_map(const double *P, long n, float min_db, float max_db, int phase, float *rgba)
+{
+    for (long i = 0; i < n; i++) {
+        float pr = (float)P[2 * i], pi = (float)P[2 * i + 1];
+        const float saturation = 0.8f;
+        float dB = 20.0f * log10f(hypotf(pr, pi) + 1e-8f);
+        float mag = (dB - min_db) / (max_db - min_db);
+        mag = fminf(fmaxf(mag, 0.0f), 1.0f);
+        float *o = rgba + 4 * i;
+        o[0] = o[1] = o[2] = saturation * mag;
+        o[3] = 1.0f;
+        if (phase) {
+            float h = (atan2f(pi, pr) + M_PI) / (2.0f * M_PI);
+            hsv2rgb_ref(h, 0.8f, mag, o);
+        }
+    }
+}
+
 int orc_num_threads(void)
 {
 #ifdef _OPENMP

@@ -82,6 +82,7 @@ def load_library(path: str | None = None, build: bool = False):
     L.sonar_get_mask.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_ubyte), C.c_longlong]
     L.sonar_get_mask.restype = C.c_longlong
     L.sonar_get_stream.restype = C.c_void_p
+    L.sonar_get_surface_colours.argtypes = [C.c_int, C.c_int, _f, C.c_longlong]
     L.sonar_measure_peak.argtypes = [C.c_int]
     L.sonar_measure_peak.restype = C.c_double
     L.sonar_fragment_triangle.argtypes = [_f, C.c_float, _i, _f, _f, C.c_longlong]
@@ -209,6 +210,17 @@ def get_object_pressures(object_type, idx=0):
     if r < 0:
         raise SonarError("sonar_get_object_pressures failed (%d)" % r)
     return out[:, 0] + 1j * out[:, 1]
+
+
+def get_surface_colours(object_type, idx=0):
+    """RGBA colours (float32, (ncells, 4)) of an object's surface cells."""
+    n = object_cells(object_type, idx)
+    out = np.zeros((max(n, 0), 4), dtype=np.float32)
+    r = lib().sonar_get_surface_colours(int(object_type), int(idx), out.ctypes.data_as(_f), n)
+    _check()
+    if r < 0:
+        raise SonarError("sonar_get_surface_colours failed (%d)" % r)
+    return out
 
 
 def get_field_point_pressures(n):

@@ -260,7 +260,8 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
     __shared__ float4 sTri[4 * kMaxCand];
     __shared__ int sCand[kMaxCand];
     __shared__ int sRed[kMaxCand][4];  // ordered-int min/max of distances: src lo, src hi, dst lo, dst hi
-    __shared__ int sBox[6];            // ordered-int union box of all points: lo xyz, hi xyz
+    __shared__ int sBox[18];           // ordered-int boxes (lo xyz, hi xyz): union, sources, destinations
+    __shared__ int sAllOcc;
     __shared__ int sFac[4];            // src facet lo/hi, dst facet lo/hi
     __shared__ int sNc, sKeep, sOverflow;
     const int tid = threadIdx.x;
@@ -275,12 +276,13 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
         if (tid == 0) a.mask.flags[fidx] = kFlagNone;
         return;
     }
-    if (tid < 6) sBox[tid] = tid < 3 ? f2o(3.0e38f) : f2o(-3.0e38f);
+    if (tid < 18) sBox[tid] = (tid % 6) < 3 ? f2o(3.0e38f) : f2o(-3.0e38f);
     if (tid < 4) sFac[tid] = (tid & 1) ? -2147483647 : 2147483647;
     if (tid == 0) {
         sNc = 0;
         sKeep = 0;
         sOverflow = 0;
+        sAllOcc = 0;
     }
     float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     float4 n = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
@@ -303,23 +305,30 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
             nt = a.dst_facet_n[ft];
         }
     }
-    // union box of the block's points and the facet ranges of both sides
+    // boxes of the block's sources and destinations and the facet ranges of both sides
     {
-        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        float slo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, shi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        float dlo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, dhi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
         if (src_ok) {
-            lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
-            hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
+            slo[0] = shi[0] = p.x; slo[1] = shi[1] = p.y; slo[2] = shi[2] = p.z;
         }
         if (live) {
-            lo[0] = fminf(lo[0], t.x); lo[1] = fminf(lo[1], t.y); lo[2] = fminf(lo[2], t.z);
-            hi[0] = fmaxf(hi[0], t.x); hi[1] = fmaxf(hi[1], t.y); hi[2] = fmaxf(hi[2], t.z);
+            dlo[0] = dhi[0] = t.x; dlo[1] = dhi[1] = t.y; dlo[2] = dhi[2] = t.z;
         }
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             for (int off = 16; off > 0; off >>= 1) {
-                lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], off));
-                hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], off));
+                slo[k] = fminf(slo[k], __shfl_xor_sync(0xffffffffu, slo[k], off));
+                shi[k] = fmaxf(shi[k], __shfl_xor_sync(0xffffffffu, shi[k], off));
+                dlo[k] = fminf(dlo[k], __shfl_xor_sync(0xffffffffu, dlo[k], off));
+                dhi[k] = fmaxf(dhi[k], __shfl_xor_sync(0xffffffffu, dhi[k], off));
             }
+        }
+        float lo[3], hi[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(slo[k], dlo[k]);
+            hi[k] = fmaxf(shi[k], dhi[k]);
         }
         int fs_lo = src_ok ? __float_as_int(n.w) : 2147483647, fs_hi = src_ok ? __float_as_int(n.w) : -2147483647;
         int fd_lo = live ? ft : 2147483647, fd_hi = live ? ft : -2147483647;
@@ -335,6 +344,10 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
             for (int k = 0; k < 3; ++k) {
                 atomicMin(&sBox[k], f2o(lo[k]));
                 atomicMax(&sBox[3 + k], f2o(hi[k]));
+                atomicMin(&sBox[6 + k], f2o(slo[k]));
+                atomicMax(&sBox[9 + k], f2o(shi[k]));
+                atomicMin(&sBox[12 + k], f2o(dlo[k]));
+                atomicMax(&sBox[15 + k], f2o(dhi[k]));
             }
             atomicMin(&sFac[0], fs_lo);
             atomicMax(&sFac[1], fs_hi);
@@ -448,7 +461,81 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
                 sKeep = keep;
             }
             __syncthreads();
+            // ALL OCCLUDED: one kept triangle that every ray of the block crosses,
+            // inside, before tmax (ray origins on one side: sources for the
+            // source hop and NO_RESP, destinations for the field-point readout)
+            if (HOP != HOP_F2F && sKeep > 0) {
+                const int ob = (HOP == HOP_FP) ? 12 : 6, eb = (HOP == HOP_FP) ? 6 : 12;
+                const float ol[3] = {o2f(sBox[ob]), o2f(sBox[ob + 1]), o2f(sBox[ob + 2])};
+                const float oh[3] = {o2f(sBox[ob + 3]), o2f(sBox[ob + 4]), o2f(sBox[ob + 5])};
+                const float el[3] = {o2f(sBox[eb]), o2f(sBox[eb + 1]), o2f(sBox[eb + 2])};
+                const float eh[3] = {o2f(sBox[eb + 3]), o2f(sBox[eb + 4]), o2f(sBox[eb + 5])};
+                float S = 1.0f;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) S = fmaxf(S, 1.0f + fmaxf(fmaxf(fabsf(ol[k]), fabsf(oh[k])),
+                                                                    fmaxf(fabsf(el[k]), fabsf(eh[k]))));
+                const float tol = 1e-5f * S;
+                // shortest possible ray of the block (box gap)
+                float g2 = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float gk = fmaxf(0.0f, fmaxf(ol[k] - eh[k], el[k] - oh[k]));
+                    g2 = fmaf(gk, gk, g2);
+                }
+                const float rmin_pair = sqrtf(g2);
+                for (int c = 0; c < sKeep; ++c) {
+                    const float4 P = sTri[4 * c];
+                    // plane distances over the two boxes (exact ranges of an affine function)
+                    float o_lo = -P.w, o_hi = -P.w, e_lo = -P.w, e_hi = -P.w;
+                    const float nv[3] = {P.x, P.y, P.z};
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        o_lo += fminf(nv[k] * ol[k], nv[k] * oh[k]);
+                        o_hi += fmaxf(nv[k] * ol[k], nv[k] * oh[k]);
+                        e_lo += fminf(nv[k] * el[k], nv[k] * eh[k]);
+                        e_hi += fmaxf(nv[k] * el[k], nv[k] * eh[k]);
+                    }
+                    const bool split = (o_lo > 1.2e-4f * S && e_hi < -tol) || (o_hi < -1.2e-4f * S && e_lo > tol);
+                    if (!split) continue;  // uniform per block
+                    const float a0 = fminf(fabsf(o_lo), fabsf(o_hi)), a0max = fmaxf(fabsf(o_lo), fabsf(o_hi));
+                    const float a1 = fminf(fabsf(e_lo), fabsf(e_hi)), a1max = fmaxf(fabsf(e_lo), fabsf(e_hi));
+                    // every crossing at least rmin_pair * a1 / (a0max + a1max) before the end point
+                    if (!(rmin_pair * a1 > 1.2e-3f * (a0max + a1max) + tol)) continue;
+                    // the 64 corner-to-corner crossings must lie inside the triangle
+                    bool inside = true;
+                    if (tid < 64) {
+                        const int oc = tid & 7, ec = tid >> 3;
+                        const float ox = (oc & 1) ? oh[0] : ol[0], oy = (oc & 2) ? oh[1] : ol[1],
+                                    oz = (oc & 4) ? oh[2] : ol[2];
+                        const float ex = (ec & 1) ? eh[0] : el[0], ey = (ec & 2) ? eh[1] : el[1],
+                                    ez = (ec & 4) ? eh[2] : el[2];
+                        const float d0 = plane_dist(P, ox, oy, oz), d1 = plane_dist(P, ex, ey, ez);
+                        const float sp = d0 / (d0 - d1);
+                        const float X = fmaf(ex - ox, sp, ox), Y = fmaf(ey - oy, sp, oy), Z = fmaf(ez - oz, sp, oz);
+#pragma unroll
+                        for (int q = 1; q <= 3; ++q) {
+                            const float4 M = sTri[4 * c + q];
+                            if (!(fmaf(M.x, X, fmaf(M.y, Y, M.z * Z)) - M.w > tol)) inside = false;
+                        }
+                    }
+                    if (__syncthreads_and(inside)) {
+                        if (tid == 0) sAllOcc = 1;
+                        break;
+                    }
+                }
+                __syncthreads();
+            }
         }
+    }
+    if (sAllOcc) {
+        if (tid == 0) a.mask.flags[fidx] = kFlagNone;
+        if (a.full) {
+            const int ntile = min(kTile, a.nsrc - i0);
+            const int nw = (ntile + 31) >> 5;
+            if (live)
+                for (int w = 0; w < nw; ++w) a.mask.bits[(long long)(tile * kWordsPerTile + w) * a.mask.pitch + j] = 0u;
+        }
+        return;
     }
     const int nkeep = sKeep;
     const bool overflow = have_tris && sOverflow;
@@ -731,12 +818,15 @@ __global__ void __launch_bounds__(kTile) k_sum(SumArgs a)
 // The diagonal tile (I == J) runs the destination-owned loop.  Column sums of
 // (I, J) land at colpart[256 J (J-1) / 2 + i]; k_finalize_f2f_sym adds them in
 // a fixed order (deterministic results).
-template <bool ATT, bool GATE>
+template <bool ATT, bool GATE, bool REG>
 __device__ __forceinline__ void sym_pair(const SumArgs &a, const float4 A, const float4 B, const Dst &d, float &Tr,
                                          float &Ti, bool &ok)
 {
     const float vx = __fsub_rn(d.px, A.x), vy = __fsub_rn(d.py, A.y), vz = __fsub_rn(d.pz, A.z);
-    const float r2 = dot_rn(vx, vy, vz, vx, vy, vz);
+    // |v|^2 with fused multiply-adds; r from one Newton step on rsqrt (within an
+    // ulp or two of the reference's FP32 r; the regularisation branch below
+    // recomputes the reference's r exactly where it decides)
+    const float r2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
     const float rinv = rsqrtf(r2);
     const float r0 = r2 * rinv;
     const float r = fmaf(fmaf(-r0, r0, r2), 0.5f * rinv, r0);
@@ -745,30 +835,34 @@ __device__ __forceinline__ void sym_pair(const SumArgs &a, const float4 A, const
     const float frac = (th - rintf(th)) + tl;
     float sn, cs;
     __sincosf(frac * kTwoPi, &sn, &cs);
+    const float d1 = vx * B.x + vy * B.y + vz * B.z;    // r cos_scat (source side)
+    const float d2 = vx * d.nx + vy * d.ny + vz * d.nz;  // -r cos_inc (destination side)
+    ok = true;
+    if (GATE)
+        ok = gate_from(d1 * rinv, vx, vy, vz, 1.0f, B.x, B.y, B.z) &&
+             gate_from(-d2 * rinv, vx, vy, vz, -1.0f, d.nx, d.ny, d.nz);
+    // T = cos_scat cos_inc G,  G = -e^{ikr}/(4 pi) (ik/r) + 1/r^2
     const float rinv2 = rinv * rinv;
-    float gr, gi;
+    const float u = (d1 * d2) * (-rinv2);  // cos_scat cos_inc
     if (ATT) {
         const float amp = rinv * kInv4Pi * __expf(-a.ka * r);
-        gr = fmaf(amp, fmaf(a.ka, cs, a.kr * sn), rinv2);
-        gi = amp * fmaf(a.ka, sn, -a.kr * cs);
+        Tr = u * fmaf(amp, fmaf(a.ka, cs, a.kr * sn), rinv2);
+        Ti = u * (amp * fmaf(a.ka, sn, -a.kr * cs));
     } else {
-        const float ampk = rinv * (kInv4Pi * a.kr);
-        gr = fmaf(ampk, sn, rinv2);
-        gi = -ampk * cs;
+        const float ua = (u * rinv) * a.kr4pi;
+        Tr = fmaf(ua, sn, u * rinv2);
+        Ti = -ua * cs;
     }
-    const float c1 = (vx * B.x + vy * B.y + vz * B.z) * rinv;
-    const float c2 = -(vx * d.nx + vy * d.ny + vz * d.nz) * rinv;
-    ok = true;
-    if (GATE) ok = gate_from(c1, vx, vy, vz, 1.0f, B.x, B.y, B.z) && gate_from(c2, vx, vy, vz, -1.0f, d.nx, d.ny, d.nz);
-    float rr = r;
-    if (fabsf(r - a.rmin) <= a.rmin * 4e-7f) rr = __fsqrt_rn(r2);
-    if (rr < a.rmin) {
-        gr = -a.ka * kInv4Pi;
-        gi = a.kr * kInv4Pi;
+    if (REG) {
+        // regularised G below r_min = delta_src (OptiX.cu:340-346), decided with
+        // the reference's r where it is close to the threshold
+        float rr = r;
+        if (fabsf(r - a.rmin) <= a.rmin * 1e-6f) rr = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
+        if (rr < a.rmin) {
+            Tr = u * (-a.ka * kInv4Pi);
+            Ti = u * (a.kr * kInv4Pi);
+        }
     }
-    const float wgt = c1 * c2;
-    Tr = gr * wgt;
-    Ti = gi * wgt;
 }
 
 __device__ __forceinline__ float warp_sum(float v)
@@ -778,12 +872,93 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
-template <bool ATT>
-__global__ void __launch_bounds__(kTile) k_sum_f2f_sym(SumArgs a, double2 *colpart)
+// minimum distance between two axis-aligned boxes
+__device__ __forceinline__ float box_gap(const float *lo1, const float *hi1, const float *lo2, const float *hi2)
 {
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float g = fmaxf(0.0f, fmaxf(lo1[k] - hi2[k], lo2[k] - hi1[k]));
+        s = fmaf(g, g, s);
+    }
+    return sqrtf(s);
+}
+
+// Shared-memory transpose of one warp's column terms, 16 sources at a time:
+// row = lane (destination), column = source; pitch 17 keeps the row-wise
+// writes and the column-wise reads free of bank conflicts.
+constexpr int kTrPitch = 17;
+constexpr size_t kSymDynSmem = sizeof(float2) * (kTile / 32) * 32 * kTrPitch;
+
+// one 32-source word of an off-diagonal block: row terms into the thread's
+// destination, column terms summed over the warp into colw[word].  FULL:
+// every pair of the word interacts (no per-pair mask or gate).
+template <bool ATT, bool GATE, bool REG, bool FULL>
+__device__ __forceinline__ void sym_word(const SumArgs &a, const float4 *sA, const float4 *sB, int w, uint32_t m,
+                                         const Dst &d, float wjr, float wji, float &fr, float &fi, float2 *colw,
+                                         float2 *tr, int lane)
+{
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+#pragma unroll 4
+        for (int b = 0; b < 16; ++b) {
+            const int q = w * 32 + h * 16 + b;
+            const float4 A = sA[q], B = sB[q];
+            float Tr, Ti;
+            bool ok;
+            sym_pair<ATT, GATE, REG>(a, A, B, d, Tr, Ti, ok);
+            if (!FULL) {
+                const bool on = ((m >> (h * 16 + b)) & 1u) && ok;
+                Tr = on ? Tr : 0.0f;
+                Ti = on ? Ti : 0.0f;
+            }
+            fr = fmaf(Tr, A.w, fmaf(-Ti, B.w, fr));  // forward term into this destination
+            fi = fmaf(Tr, B.w, fmaf(Ti, A.w, fi));
+            tr[lane * kTrPitch + b] = make_float2(Tr * wjr - Ti * wji, Tr * wji + Ti * wjr);  // reciprocal term
+        }
+        __syncwarp();
+        // lane l sums column (l & 15) over rows 16 (l >> 4) .. +15; the two halves combine
+        const int c = lane & 15, r0 = (lane >> 4) * 16;
+        float sr = 0.0f, si = 0.0f;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const float2 v = tr[(r0 + r) * kTrPitch + c];
+            sr += v.x;
+            si += v.y;
+        }
+        sr += __shfl_xor_sync(0xffffffffu, sr, 16);
+        si += __shfl_xor_sync(0xffffffffu, si, 16);
+        if (lane < 16) colw[w * 32 + h * 16 + lane] = make_float2(sr, si);
+        __syncwarp();
+    }
+}
+
+template <bool ATT, bool GATE, bool REG>
+__device__ __forceinline__ void diag_word(const SumArgs &a, const float4 *sA, const float4 *sB, int w, uint32_t m,
+                                          const Dst &d, float &fr, float &fi)
+{
+#pragma unroll 4
+    for (int b = 0; b < 32; ++b) {
+        const float4 A = sA[w * 32 + b], B = sB[w * 32 + b];
+        float Tr, Ti;
+        bool ok;
+        sym_pair<ATT, GATE, REG>(a, A, B, d, Tr, Ti, ok);
+        const bool on = ((m >> b) & 1u) && ok;
+        Tr = on ? Tr : 0.0f;
+        Ti = on ? Ti : 0.0f;
+        fr = fmaf(Tr, A.w, fmaf(-Ti, B.w, fr));
+        fi = fmaf(Tr, B.w, fmaf(Ti, A.w, fi));
+    }
+}
+
+template <bool ATT>
+__global__ void __launch_bounds__(kTile, 3) k_sum_f2f_sym(SumArgs a, double2 *colpart)
+{
+    extern __shared__ float2 sTr[];  // kSymDynSmem bytes: per-warp transpose tiles
     __shared__ float4 sA[kTile];
     __shared__ float4 sB[kTile];
     __shared__ float2 sCol[kTile / 32][kTile];
+    __shared__ float sTb[6];  // source tile box
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int J = blockIdx.x;
     const int j = J * kTile + tid;
@@ -791,6 +966,7 @@ __global__ void __launch_bounds__(kTile) k_sum_f2f_sym(SumArgs a, double2 *colpa
     Dst d{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     int limit = a.nsrc;
     float wjr = 0.0f, wji = 0.0f;  // this destination's own source weight (the reciprocal input)
+    float dlo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, dhi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
     if (live) {
         const float4 p = a.dst_pos[j];
         d.px = p.x; d.py = p.y; d.pz = p.z;
@@ -799,7 +975,32 @@ __global__ void __launch_bounds__(kTile) k_sum_f2f_sym(SumArgs a, double2 *colpa
         limit = a.dst_limit[j];
         wjr = a.srcA[j].w;
         wji = a.srcB[j].w;
+        dlo[0] = dhi[0] = p.x; dlo[1] = dhi[1] = p.y; dlo[2] = dhi[2] = p.z;
     }
+    // destination block box (for the regularisation test)
+    __shared__ int sDb[6];
+    if (tid < 6) sDb[tid] = tid < 3 ? f2o(3.0e38f) : f2o(-3.0e38f);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        for (int off = 16; off > 0; off >>= 1) {
+            dlo[k] = fminf(dlo[k], __shfl_xor_sync(0xffffffffu, dlo[k], off));
+            dhi[k] = fmaxf(dhi[k], __shfl_xor_sync(0xffffffffu, dhi[k], off));
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(&sDb[k], f2o(dlo[k]));
+            atomicMax(&sDb[3 + k], f2o(dhi[k]));
+        }
+    __syncthreads();
+    float blo[3], bhi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        blo[k] = o2f(sDb[k]);
+        bhi[k] = o2f(sDb[3 + k]);
+    }
+
     const long long cbase = (long long)kTile * J * (J - 1) / 2;  // this J's column region
     double accr = 0.0, acci = 0.0;
     const int t0 = blockIdx.y * a.tiles_per_split;
@@ -815,75 +1016,86 @@ __global__ void __launch_bounds__(kTile) k_sum_f2f_sym(SumArgs a, double2 *colpa
         {
             const int i = i0 + tid;
             const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            sA[tid] = i < a.nsrc ? a.srcA[i] : z;
+            const float4 A = i < a.nsrc ? a.srcA[i] : z;
+            sA[tid] = A;
             sB[tid] = i < a.nsrc ? a.srcB[i] : z;
+            // source tile box
+            float lo[3] = {A.x, A.y, A.z}, hi[3] = {A.x, A.y, A.z};
+            if (i >= a.nsrc) {
+                lo[0] = lo[1] = lo[2] = 3.0e38f;
+                hi[0] = hi[1] = hi[2] = -3.0e38f;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                for (int off = 16; off > 0; off >>= 1) {
+                    lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], off));
+                    hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], off));
+                }
+            if (lane == 0) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    sCol[warp][k] = make_float2(lo[k], hi[k]);
+                }
+            }
         }
         __syncthreads();
+        if (tid == 0) {
+            float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+            for (int q = 0; q < kTile / 32; ++q)
+                for (int k = 0; k < 3; ++k) {
+                    lo[k] = fminf(lo[k], sCol[q][k].x);
+                    hi[k] = fmaxf(hi[k], sCol[q][k].y);
+                }
+            for (int k = 0; k < 3; ++k) {
+                sTb[k] = lo[k];
+                sTb[3 + k] = hi[k];
+            }
+        }
+        __syncthreads();
+        // no pair of this block can be closer than r_min: skip the regularisation code
+        const float tlo[3] = {sTb[0], sTb[1], sTb[2]}, thi[3] = {sTb[3], sTb[4], sTb[5]};
+        const bool reg = box_gap(tlo, thi, blo, bhi) <= a.rmin * 1.001f;
         const int ntile = min(kTile, a.nsrc - i0);
         const int nw = (ntile + 31) >> 5;
         float fr = 0.0f, fi = 0.0f;
-        if (t == J) {
-            // diagonal tile: destination-owned, with the zero-input source limit
-            for (int w = 0; w < nw; ++w) {
-                uint32_t m;
-                if (fl == kFlagBits) {
-                    m = live ? a.mask.bits[(long long)(t * kWordsPerTile + w) * a.mask.pitch + j] : 0u;
-                } else {
-                    const int nb = ntile - w * 32;
-                    m = !live ? 0u : (nb >= 32 ? 0xffffffffu : ((1u << nb) - 1u));
-                }
+        const bool gate = fl == kFlagClear;
+        for (int w = 0; w < nw; ++w) {
+            uint32_t m;
+            if (fl == kFlagBits) {
+                m = live ? a.mask.bits[(long long)(t * kWordsPerTile + w) * a.mask.pitch + j] : 0u;
+            } else {
+                const int nb = ntile - w * 32;
+                m = !live ? 0u : (nb >= 32 ? 0xffffffffu : ((1u << nb) - 1u));
+            }
+            if (t == J) {
+                // diagonal tile: destination-owned, with the zero-input source limit
                 const int keep = limit - (i0 + w * 32);
                 m &= keep >= 32 ? 0xffffffffu : (keep <= 0 ? 0u : ((1u << keep) - 1u));
                 if (!__any_sync(0xffffffffu, m != 0u)) continue;
-                for (int b = 0; b < 32; ++b) {
-                    const float4 A = sA[w * 32 + b], B = sB[w * 32 + b];
-                    float Tr, Ti;
-                    bool ok;
-                    if (fl != kFlagClear)
-                        sym_pair<ATT, false>(a, A, B, d, Tr, Ti, ok);
-                    else
-                        sym_pair<ATT, true>(a, A, B, d, Tr, Ti, ok);
-                    const bool on = ((m >> b) & 1u) && ok;
-                    fr += on ? Tr * A.w - Ti * B.w : 0.0f;
-                    fi += on ? Tr * B.w + Ti * A.w : 0.0f;
-                }
-            }
-        } else {
-            for (int w = 0; w < nw; ++w) {
-                uint32_t m;
-                if (fl == kFlagBits) {
-                    m = live ? a.mask.bits[(long long)(t * kWordsPerTile + w) * a.mask.pitch + j] : 0u;
-                } else {
-                    const int nb = ntile - w * 32;
-                    m = !live ? 0u : (nb >= 32 ? 0xffffffffu : ((1u << nb) - 1u));
-                }
+                if (gate) diag_word<ATT, true, true>(a, sA, sB, w, m, d, fr, fi);
+                else diag_word<ATT, false, true>(a, sA, sB, w, m, d, fr, fi);
+            } else {
                 if (!__any_sync(0xffffffffu, m != 0u)) {
-                    if (lane == 0)
-                        for (int b = 0; b < 32; ++b) sCol[warp][w * 32 + b] = make_float2(0.0f, 0.0f);
+                    sCol[warp][w * 32 + lane] = make_float2(0.0f, 0.0f);
                     continue;
                 }
-#pragma unroll 4
-                for (int b = 0; b < 32; ++b) {
-                    const float4 A = sA[w * 32 + b], B = sB[w * 32 + b];
-                    float Tr, Ti;
-                    bool ok;
-                    if (fl != kFlagClear)
-                        sym_pair<ATT, false>(a, A, B, d, Tr, Ti, ok);
-                    else
-                        sym_pair<ATT, true>(a, A, B, d, Tr, Ti, ok);
-                    const bool on = ((m >> b) & 1u) && ok;
-                    // row: forward term into this destination
-                    fr += on ? Tr * A.w - Ti * B.w : 0.0f;
-                    fi += on ? Tr * B.w + Ti * A.w : 0.0f;
-                    // column: reciprocal term into source i, summed over the warp
-                    const float cr = warp_sum(on ? Tr * wjr - Ti * wji : 0.0f);
-                    const float ci = warp_sum(on ? Tr * wji + Ti * wjr : 0.0f);
-                    if (lane == 0) sCol[warp][w * 32 + b] = make_float2(cr, ci);
+                float2 *colw = &sCol[warp][0];
+                float2 *trw = sTr + warp * 32 * kTrPitch;
+                const bool full = !gate && __all_sync(0xffffffffu, m == 0xffffffffu);
+                if (gate) {
+                    if (reg) sym_word<ATT, true, true, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
+                    else sym_word<ATT, true, false, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
+                } else if (full) {
+                    if (reg) sym_word<ATT, false, true, true>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
+                    else sym_word<ATT, false, false, true>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
+                } else {
+                    if (reg) sym_word<ATT, false, true, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
+                    else sym_word<ATT, false, false, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
                 }
             }
-            for (int w = nw; w < kWordsPerTile; ++w)
-                if (lane == 0)
-                    for (int b = 0; b < 32; ++b) sCol[warp][w * 32 + b] = make_float2(0.0f, 0.0f);
+        }
+        if (t < J) {
+            for (int w = nw; w < kWordsPerTile; ++w) sCol[warp][w * 32 + lane] = make_float2(0.0f, 0.0f);
             __syncthreads();
             double sr = 0.0, si = 0.0;
 #pragma unroll
@@ -1126,10 +1338,16 @@ void launch_sum_f2f_sym(const SumArgs &a, double2 *colpart, cudaStream_t s)
 {
     if (a.nsrc <= 0 || a.ndst <= 0) return;
     dim3 grid(a.mask.ndstblocks, a.nsplit);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_sum_f2f_sym<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymDynSmem);
+        cudaFuncSetAttribute(k_sum_f2f_sym<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymDynSmem);
+        attr_set = true;
+    }
     if (a.ka != 0.0f)
-        k_sum_f2f_sym<true><<<grid, kTile, 0, s>>>(a, colpart);
+        k_sum_f2f_sym<true><<<grid, kTile, kSymDynSmem, s>>>(a, colpart);
     else
-        k_sum_f2f_sym<false><<<grid, kTile, 0, s>>>(a, colpart);
+        k_sum_f2f_sym<false><<<grid, kTile, kSymDynSmem, s>>>(a, colpart);
 }
 
 void launch_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,

@@ -134,6 +134,11 @@ struct Model {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
     float4 *d_src_pos = nullptr, *d_fp_pos = nullptr;
     double2 *d_src_P = nullptr, *d_fp_P = nullptr;
+    // field points are kept in Morton (spatial) order on the device so that a
+    // block of 256 destinations covers a small region; fp_order[k] is the load
+    // index of the k-th stored point
+    std::vector<int> fp_order;
+    int *d_fp_order = nullptr;
     float4 *d_nodes = nullptr, *d_tris = nullptr;
     int nnodes = 0, ntri = 0;
     std::vector<MaskEntry> masks;
@@ -156,7 +161,7 @@ struct Model {
     {
         for (int t = 0; t < 3; t++)
             for (auto &o : obj[t]) o->free_device();
-        dfree(d_src_pos); dfree(d_fp_pos); dfree(d_src_P); dfree(d_fp_P);
+        dfree(d_src_pos); dfree(d_fp_pos); dfree(d_src_P); dfree(d_fp_P); dfree(d_fp_order);
         dfree(d_nodes); dfree(d_tris);
         for (auto &m : masks) {
             dfree(m.view.bits);
@@ -273,6 +278,44 @@ void upload_points(const std::vector<Vec3> &pts, float4 *&d_pos, double2 *&d_P, 
     CK(cudaStreamSynchronize(g.stream));
 }
 
+// Order of points along a Morton (Z-order) curve of their bounding box.
+std::vector<int> morton_order(const std::vector<Vec3> &pts)
+{
+    std::vector<int> order(pts.size());
+    for (size_t k = 0; k < pts.size(); k++) order[k] = (int)k;
+    if (pts.size() < 2) return order;
+    float lo[3] = {pts[0].x, pts[0].y, pts[0].z}, hi[3] = {lo[0], lo[1], lo[2]};
+    for (auto &p : pts) {
+        const float c[3] = {p.x, p.y, p.z};
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::min(lo[k], c[k]);
+            hi[k] = std::max(hi[k], c[k]);
+        }
+    }
+    auto spread = [](uint64_t v) {  // 21 bits -> every third bit
+        v &= 0x1fffff;
+        v = (v | v << 32) & 0x1f00000000ffffULL;
+        v = (v | v << 16) & 0x1f0000ff0000ffULL;
+        v = (v | v << 8) & 0x100f00f00f00f00fULL;
+        v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+        v = (v | v << 2) & 0x1249249249249249ULL;
+        return v;
+    };
+    std::vector<uint64_t> code(pts.size());
+    for (size_t i = 0; i < pts.size(); i++) {
+        const float c[3] = {pts[i].x, pts[i].y, pts[i].z};
+        uint64_t q[3];
+        for (int k = 0; k < 3; k++) {
+            const double ext = (double)hi[k] - (double)lo[k];
+            const double u = ext > 0 ? ((double)c[k] - (double)lo[k]) / ext : 0.0;
+            q[k] = (uint64_t)std::min(2097151.0, std::max(0.0, u * 2097151.0));
+        }
+        code[i] = spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return code[a] < code[b]; });
+    return order;
+}
+
 void render()
 {
     if (g.rendered) fail(-2, "render_cuda called twice without TearDownCuda");
@@ -304,7 +347,16 @@ void render()
         g.h2d_bytes += (long long)(bvh.nodes.size() * sizeof(BvhNode) + bvh.tris.size() * sizeof(float4));
     }
     upload_points(g.src, g.d_src_pos, g.d_src_P, 1.0);  // unit source pressure (Model.cpp:16-19)
-    upload_points(g.fp, g.d_fp_pos, g.d_fp_P, 0.0);
+    g.fp_order = morton_order(g.fp);
+    std::vector<Vec3> fp_sorted(g.fp.size());
+    for (size_t k = 0; k < g.fp.size(); k++) fp_sorted[k] = g.fp[g.fp_order[k]];
+    upload_points(fp_sorted, g.d_fp_pos, g.d_fp_P, 0.0);
+    g.d_fp_order = dalloc<int>(g.fp_order.size());
+    if (!g.fp_order.empty()) {
+        CK(cudaMemcpyAsync(g.d_fp_order, g.fp_order.data(), g.fp_order.size() * sizeof(int), cudaMemcpyHostToDevice,
+                           g.stream));
+        CK(cudaStreamSynchronize(g.stream));
+    }
     g.rendered = true;
 }
 
@@ -506,6 +558,7 @@ void run_hop(int hop, int a, int b)
     const double k2 = g.kr / (2.0 * M_PI);
     s.k2hi = (float)k2;
     s.k2lo = (float)(k2 - (double)s.k2hi);
+    s.kr4pi = (float)(g.kr / (4.0 * M_PI));
     s.nsplit = choose_split(M.view.ntiles, M.view.ndstblocks);
     s.tiles_per_split = (M.view.ntiles + s.nsplit - 1) / s.nsplit;
     s.nsplit = (M.view.ntiles + s.tiles_per_split - 1) / s.tiles_per_split;
@@ -526,7 +579,7 @@ void run_hop(int hop, int a, int b)
         launch_pack_frags(A.d_act_pos, A.d_act_facet, A.d_act_cell, A.d_facet_n, A.d_P, 1.0f, M.nsrc, g.d_packA,
                           g.d_packB, st);
         timed_sum(s, st);
-        launch_finalize_add(g.d_partial, s.nsplit, M.ndst, nullptr, g.d_fp_P, st);
+        launch_finalize_add(g.d_partial, s.nsplit, M.ndst, g.d_fp_order, g.d_fp_P, st);
     } else if (hop == HOP_F2F) {
         Object &A = get(OBJ_TARGET, a);
         s.rmin = A.delta;
@@ -938,6 +991,7 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
         std::vector<int> rs, rd;  // internal index -> canonical index (empty: identity)
         if (hop == HOP_FP || hop == HOP_F2F || hop == HOP_NORESP) rs = canon(get(OBJ_TARGET, srcIdx));
         if (hop == HOP_F2F) rd = rs;
+        if (hop == HOP_FP) rd = g.fp_order;  // stored field point k is load index fp_order[k]
         if (hop == HOP_NORESP) rd = canon(get(OBJ_FIELD, dstIdx));
         for (long long jd = 0; jd < M.ndst; jd++) {
             const long long cd = rd.empty() ? jd : rd[jd];
@@ -950,6 +1004,29 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
         }
     });
     return st != 0 ? st : nbytes;
+}
+
+int sonar_get_surface_colours(int objectType, int objIdx, float *rgba, long long ncells)
+{
+    int written = 0;
+    int st = guarded([&] {
+        need_render();
+        Object &o = get(objectType, objIdx);
+        if (o.type == OBJ_SOURCE || !o.d_P) fail(-4, "object has no pressures");
+        if (ncells < o.ncells) fail(-8, "colour buffer holds %lld of %lld cells", ncells, o.ncells);
+        if (o.ncells == 0) return;
+        float4 *d = dalloc<float4>((size_t)o.ncells);
+        const int phase = o.type == OBJ_FIELD ? g.phase_field : g.phase_target;
+        launch_colour_map(o.d_P, o.ncells, g.min_db, g.max_db, phase, d, g.stream);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(rgba, d, (size_t)o.ncells * sizeof(float4), cudaMemcpyDeviceToHost, g.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
+        cudaFree(d);
+        if (e != cudaSuccess) fail(-10, "colour map failed: %s", cudaGetErrorString(e));
+        written = (int)o.ncells;
+    });
+    return st != 0 ? st : written;
 }
 
 void *sonar_get_stream(void) { return (void *)g.stream; }

@@ -86,6 +86,7 @@ struct SumArgs {
     float kr, ka;                   // Re k, Im k (FP32 values of the reference's k_wave)
     float k2hi, k2lo;               // Re k / (2 pi) split in two floats
     float rmin;                     // regularisation radius (source object delta)
+    float kr4pi;                    // Re k / (4 pi)
     double2 *partial;               // [nsplit][ndst]
     int nsplit;
     int tiles_per_split;
@@ -111,6 +112,9 @@ void launch_mask_export(const MaskView &m, int nsrc, int ndst, uint8_t *out, cud
 void launch_sum_f2f_sym(const SumArgs &a, double2 *colpart, cudaStream_t s);
 void launch_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,
                              const int *cell, const double2 *Pin, double2 *Pout, double2 *P, cudaStream_t s);
+// surface.cu: pressure -> RGBA colour map of the reference's surface textures
+void launch_colour_map(const double2 *P, long long n, float min_db, float max_db, int phase, float4 *out,
+                       cudaStream_t s);
 // FP32 FMA rate in FLOP/s (which = 0) or MUFU sine rate in op/s (which = 1)
 // on the current device; < 0 on failure.
 double measure_peak(int which);
