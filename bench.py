@@ -166,6 +166,7 @@ def run_gb300(args):
     cfg = workload(args.workload)
 
     # ---- device-timed steps on the resident scene
+    api.set_option("compress", args.compress)
     load_scene(api, cfg)
     ext = torch.cuda.ExternalStream(api.stream_handle())
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
@@ -186,6 +187,7 @@ def run_gb300(args):
             one_step()
         torch.cuda.synchronize()
         print("profile-only: %d steps of %s done" % (args.steps, cfg["name"]))
+        print(json.dumps(api.stats()["hops"][-4:]))
         api.TearDownCuda()
         return
     if world > 1:
@@ -257,6 +259,15 @@ def run_gb300(args):
         mask_info = {"kernel": "k_mask<F2F>", "launch_ms": round(ms, 4),
                      "mask_bytes_written": None, "note": "1 bit per ordered pair"}
 
+    # block classes of the interaction masks (an untimed extra step)
+    api.set_option("class_stats", 1)
+    api.set_option("drop_masks", 1)
+    api.set_option("reset_pressures", 1)
+    api.set_option("reset_stats", 1)
+    projections(api, cfg)
+    mask_classes = api.stats().get("mask_classes")
+    api.set_option("class_stats", 0)
+
     # ---- end to end through the C ABI from host buffers
     api.TearDownCuda()
     e2e_times = []
@@ -297,7 +308,7 @@ def run_gb300(args):
                    "field_points": npts, "pairs_per_step": e2e_pairs, "l2": "flushed between steps (256 MB write)",
                    "path": "plain FP32 sums + interaction masks (rebuilt every step)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": roofline, "mask_kernel": mask_info, "kernel_share": share,
+        "roofline": roofline, "mask_kernel": mask_info, "kernel_share": share, "mask_block_classes": mask_classes,
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
         "rel_err_vs_fp64": extra.get("errors"), "grazing": extra.get("grazing"),
     }
@@ -438,6 +449,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
+    ap.add_argument("--compress", type=int, default=0, help="compress admissible bounce blocks (low rank)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

@@ -162,6 +162,39 @@ __device__ __forceinline__ bool cos_gate(float vx, float vy, float vz, float rin
     return !(exact_cos(vx, vy, vz, sign, nx, ny, nz) < 1e-6f);
 }
 
+// Branch-free form of cos_gate for the mask kernel's pair loop: the estimate
+// decides outside the band; lanes inside it (rare) are settled by the exact
+// expression under a warp vote, so the common path carries no divergent
+// branch.
+__device__ __forceinline__ bool cos_gate_vote(float vx, float vy, float vz, float rinv, float sign, float nx,
+                                              float ny, float nz, bool active)
+{
+    const float est = sign * fmaf(vx, nx, fmaf(vy, ny, vz * nz)) * rinv;
+    bool pass = est > 2e-6f;
+    const bool unsure = active && !pass && !(est < 0.0f);
+    if (__any_sync(0xffffffffu, unsure)) {
+        if (unsure) pass = !(exact_cos(vx, vy, vz, sign, nx, ny, nz) < 1e-6f);
+    }
+    return pass;
+}
+
+template <int HOP>
+__device__ __forceinline__ bool pair_gates_vote(const MaskArgs &a, float4 s, float4 ns, float4 t, float4 nt, int ft,
+                                                bool active)
+{
+    const float vx = __fsub_rn(t.x, s.x), vy = __fsub_rn(t.y, s.y), vz = __fsub_rn(t.z, s.z);
+    const float rinv = rsqrtf(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+    if (HOP == HOP_SRC) {
+        if (a.dst_is_field) return true;
+        return cos_gate_vote(vx, vy, vz, rinv, -1.0f, nt.x, nt.y, nt.z, active);
+    }
+    if (HOP == HOP_FP || HOP == HOP_NORESP) return cos_gate_vote(vx, vy, vz, rinv, 1.0f, ns.x, ns.y, ns.z, active);
+    const bool other = __float_as_int(ns.w) != ft;
+    const bool g1 = cos_gate_vote(vx, vy, vz, rinv, 1.0f, ns.x, ns.y, ns.z, active && other);
+    const bool g2 = cos_gate_vote(vx, vy, vz, rinv, -1.0f, nt.x, nt.y, nt.z, active && other);
+    return other && g1 && g2;
+}
+
 // Gates of one pair (the reference's discrete decisions).  For FACET_SELF
 // the two cosines are the same pair of numbers whichever fragment is the
 // enumeration's "A" side (u and -u give exactly negated dot products), so
@@ -602,31 +635,30 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
         return;
     }
 
-    // ---- pairs
+    // ---- pairs (every lane runs the loop: the gates vote across the warp)
     const int ntile = min(kTile, a.nsrc - i0);
     const int nw = (ntile + 31) >> 5;
     uint32_t any = 0;
     for (int w = 0; w < nw; ++w) {
         uint32_t word = 0;
-        if (live) {
-            const int bmax = min(32, ntile - w * 32);
-            for (int b = 0; b < bmax; ++b) {
-                const int q = w * 32 + b;
-                const float4 sq = sP[q], nq = sN[q];
-                if (!pair_gates<HOP>(a, sq, nq, t, nt, ft)) continue;
-                bool vis = true;
-                if (!clear) {
-                    float3 o, e;
-                    pair_ray<HOP>(sq, nq, t, ft, o, e);
-                    if (overflow)
-                        vis = !occluded_full(a.bvh, o, e);
-                    else if (nkeep > 0)
-                        vis = !occluded_list(sTri, nkeep, o, e);
-                }
-                if (vis) word |= 1u << b;
+        const int bmax = min(32, ntile - w * 32);
+#pragma unroll 4
+        for (int b = 0; b < 32; ++b) {
+            const int q = w * 32 + b;
+            const bool act = live && b < bmax;
+            const float4 sq = sP[q], nq = sN[q];
+            bool pass = pair_gates_vote<HOP>(a, sq, nq, t, nt, ft, act) && act;
+            if (!clear && pass) {
+                float3 o, e;
+                pair_ray<HOP>(sq, nq, t, ft, o, e);
+                if (overflow)
+                    pass = !occluded_full(a.bvh, o, e);
+                else if (nkeep > 0)
+                    pass = !occluded_list(sTri, nkeep, o, e);
             }
-            a.mask.bits[(long long)(tile * kWordsPerTile + w) * a.mask.pitch + j] = word;
+            word |= pass ? (1u << b) : 0u;
         }
+        if (live) a.mask.bits[(long long)(tile * kWordsPerTile + w) * a.mask.pitch + j] = word;
         any |= word;
     }
     const int blk = __syncthreads_or(any != 0u);
@@ -1113,8 +1145,10 @@ __global__ void __launch_bounds__(kTile, 3) k_sum_f2f_sym(SumArgs a, double2 *co
 }
 
 // P_out[cell] = rows + (P_in[i] != 0 ? columns : 0); P[cell] += P_out[cell]
+// (yrow / ycol: compressed-block rows and columns, may be null)
 __global__ void k_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,
-                                   const int *cell, const double2 *Pin, double2 *Pout, double2 *P)
+                                   const int *cell, const double2 *Pin, double2 *Pout, double2 *P,
+                                   const double2 *yrow, const double2 *ycol)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= ndst) return;
@@ -1126,12 +1160,20 @@ __global__ void k_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst,
     }
     const int c = cell[q];
     const double2 pin = Pin[c];
+    if (yrow) {
+        sr += yrow[q].x;
+        si += yrow[q].y;
+    }
     if (pin.x != 0.0 || pin.y != 0.0) {
         double cr = 0.0, ci = 0.0;
         for (int J = q / kTile + 1; J < ntiles; ++J) {
             const double2 v = colpart[(long long)kTile * J * (J - 1) / 2 + q];
             cr += v.x;
             ci += v.y;
+        }
+        if (ycol) {
+            cr += ycol[q].x;
+            ci += ycol[q].y;
         }
         sr += cr;
         si += ci;
@@ -1141,6 +1183,278 @@ __global__ void k_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst,
     o.x += sr;
     o.y += si;
     P[c] = o;
+}
+
+// ---------------------------------------------------------------- low-rank blocks
+// Compressed FACET_SELF blocks.  For a block of source tile I and destination
+// tile J (I < J, every pair interacting: mask class ALL) the interaction matrix
+// T_ji = cos_scat cos_inc G(r_ji) (weights excluded) is approximated by
+// U V^T with U: 256 x k over the rows j of J and V: 256 x k over the columns i
+// of I, built by adaptive cross approximation with partial pivoting: each
+// step takes the residual row at a pivot row, its largest entry as pivot
+// column, the residual column there, and stops when |u_k| |v_k| falls below
+// tol times the running Frobenius estimate.  The forward terms are then
+// U (V^T w_I) into J and the reciprocal ones V (U^T w_J) into I.
+
+__device__ __forceinline__ void block_argmax(float v, int idx, float *sv, int *si, float &best, int &bi)
+{
+    // block-wide argmax of v (ties: lowest index); all threads get the result
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int off = 16; off > 0; off >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, v, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, idx, off);
+        if (ov > v || (ov == v && oi < idx)) {
+            v = ov;
+            idx = oi;
+        }
+    }
+    __syncthreads();
+    if (lane == 0) {
+        sv[warp] = v;
+        si[warp] = idx;
+    }
+    __syncthreads();
+    best = sv[0];
+    bi = si[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+        if (sv[w] > best || (sv[w] == best && si[w] < bi)) {
+            best = sv[w];
+            bi = si[w];
+        }
+}
+
+__device__ __forceinline__ float block_sum(float v, float *sv)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    __syncthreads();
+    if (lane == 0) sv[warp] = v;
+    __syncthreads();
+    float t = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sv[w];
+    return t;
+}
+
+// T(j, i) of one pair from staged fragments (pos.xyz, normal.xyz)
+template <bool ATT>
+__device__ __forceinline__ float2 t_entry(const SumArgs &a, float4 pi, float4 ni, float4 pj, float4 nj)
+{
+    Dst d{pj.x, pj.y, pj.z, nj.x, nj.y, nj.z};
+    float Tr, Ti;
+    bool ok;
+    sym_pair<ATT, false, true>(a, pi, ni, d, Tr, Ti, ok);
+    return make_float2(Tr, Ti);
+}
+
+template <bool ATT>
+__global__ void __launch_bounds__(kTile) k_aca(SumArgs a, const int2 *blocks, int nblocks, int rmax, float tol,
+                                               float2 *U, float2 *V, int *rank, float *fro)
+{
+    __shared__ float4 sPI[kTile], sNI[kTile], sPJ[kTile], sNJ[kTile];
+    __shared__ float sv[kTile / 32];
+    __shared__ int si[kTile / 32];
+    __shared__ unsigned char used[kTile];
+    const int b = blockIdx.x;
+    if (b >= nblocks) return;
+    const int I = blocks[b].x, J = blocks[b].y, t = threadIdx.x;
+    const int i = I * kTile + t, j = J * kTile + t;
+    const bool vi = i < a.nsrc, vj = j < a.nsrc;
+    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    sPI[t] = vi ? a.srcA[i] : z;
+    sNI[t] = vi ? a.srcB[i] : z;
+    sPJ[t] = vj ? a.srcA[j] : z;
+    sNJ[t] = vj ? a.srcB[j] : z;
+    used[t] = vj ? 0 : 1;
+    __syncthreads();
+    float2 *Ub = U + (size_t)b * rmax * kTile, *Vb = V + (size_t)b * rmax * kTile;
+    int r = 0;  // first pivot row
+    float norm2 = 0.0f;
+    int k = 0;
+    for (int l = 0; l < rmax; ++l) {
+        // residual row r over the columns (thread t = column i)
+        float2 val = vi ? t_entry<ATT>(a, sPI[t], sNI[t], sPJ[r], sNJ[r]) : make_float2(0.0f, 0.0f);
+        for (int m = 0; m < l; ++m) {
+            const float2 u = Ub[m * kTile + r], v = Vb[m * kTile + t];
+            val.x -= u.x * v.x - u.y * v.y;
+            val.y -= u.x * v.y + u.y * v.x;
+        }
+        float best;
+        int c;
+        block_argmax(vi ? val.x * val.x + val.y * val.y : -1.0f, t, sv, si, best, c);
+        if (!(best > 1e-30f)) break;  // the residual row vanished
+        // pivot value, broadcast through shared memory
+        __shared__ float2 piv;
+        if (t == c) piv = val;
+        __syncthreads();
+        const float2 dl = piv;
+        const float inv = 1.0f / (dl.x * dl.x + dl.y * dl.y);
+        const float2 vv = make_float2((val.x * dl.x + val.y * dl.y) * inv, (val.y * dl.x - val.x * dl.y) * inv);
+        Vb[l * kTile + t] = vv;
+        // residual column c over the rows (thread t = row j)
+        float2 u = vj ? t_entry<ATT>(a, sPI[c], sNI[c], sPJ[t], sNJ[t]) : make_float2(0.0f, 0.0f);
+        __syncthreads();  // Vb[l] complete before it is read below
+        for (int m = 0; m < l; ++m) {
+            const float2 um = Ub[m * kTile + t], vm = Vb[m * kTile + c];
+            u.x -= um.x * vm.x - um.y * vm.y;
+            u.y -= um.x * vm.y + um.y * vm.x;
+        }
+        Ub[l * kTile + t] = u;
+        const float nu2 = block_sum(u.x * u.x + u.y * u.y, sv);
+        const float nv2 = block_sum(vv.x * vv.x + vv.y * vv.y, sv);
+        norm2 += nu2 * nv2;
+        k = l + 1;
+        if (nu2 * nv2 <= tol * tol * norm2) break;
+        if (t == r) used[r] = 1;
+        __syncthreads();
+        block_argmax((vj && !used[t]) ? u.x * u.x + u.y * u.y : -1.0f, t, sv, si, best, r);
+        if (best < 0.0f) break;  // every row used
+        __syncthreads();
+    }
+    if (t == 0) {
+        rank[b] = k;
+        fro[b] = sqrtf(norm2);
+    }
+}
+
+// The exact tile judges its approximation: 64 sampled entries per block,
+// relative RMS error against the block's RMS entry; blocks above the limit
+// (or not converged) get rank -1 and stay dense.
+template <bool ATT>
+__global__ void __launch_bounds__(64) k_aca_judge(SumArgs a, const int2 *blocks, int nblocks, int rmax, float limit,
+                                                  const float2 *U, const float2 *V, int *rank, const float *fro,
+                                                  float *err_out)
+{
+    __shared__ float sv[2];
+    const int b = blockIdx.x;
+    if (b >= nblocks) return;
+    const int k = rank[b];
+    const int I = blocks[b].x, J = blocks[b].y, t = threadIdx.x;
+    // deterministic sample: rows and columns from a hash of (block, sample)
+    unsigned h = (unsigned)b * 2654435761u + (unsigned)t * 40503u + 12345u;
+    h ^= h >> 13; h *= 0x5bd1e995u; h ^= h >> 15;
+    int ci = (int)(h & 255u), rj = (int)((h >> 8) & 255u);
+    const int i = I * kTile + ci, j = J * kTile + rj;
+    float e2 = 0.0f;
+    if (k > 0 && i < a.nsrc && j < a.nsrc) {
+        const float2 ex = t_entry<ATT>(a, a.srcA[i], a.srcB[i], a.srcA[j], a.srcB[j]);
+        float ar = 0.0f, ai = 0.0f;
+        const float2 *Ub = U + (size_t)b * rmax * kTile, *Vb = V + (size_t)b * rmax * kTile;
+        for (int m = 0; m < k; ++m) {
+            const float2 u = Ub[m * kTile + rj], v = Vb[m * kTile + ci];
+            ar += u.x * v.x - u.y * v.y;
+            ai += u.x * v.y + u.y * v.x;
+        }
+        e2 = (ex.x - ar) * (ex.x - ar) + (ex.y - ai) * (ex.y - ai);
+    }
+    float s = e2;
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if ((t & 31) == 0) sv[t >> 5] = s;
+    __syncthreads();
+    if (t == 0) {
+        const float rms_err = sqrtf((sv[0] + sv[1]) / 64.0f);
+        const float rms_ent = fro[b] / (float)kTile;
+        err_out[b] = rms_ent > 0.0f ? rms_err / rms_ent : 0.0f;
+        if (k <= 0 || k >= rmax || !(rms_err <= limit * rms_ent)) rank[b] = -1;
+    }
+}
+
+// Stage 1 of the compressed bounce: per block, tv = V^T w_I and su = U^T w_J
+// (k complex values each).
+__global__ void __launch_bounds__(kTile) k_lr_project(SumArgs a, const int2 *blocks, const int *bidx, int nb,
+                                                      int rmax, const float2 *U, const float2 *V, const int *rank,
+                                                      float2 *tv, float2 *su)
+{
+    __shared__ float sv[kTile / 32];
+    const int q = blockIdx.x;
+    if (q >= nb) return;
+    const int b = bidx[q];
+    const int k = rank[b];
+    const int I = blocks[b].x, J = blocks[b].y, t = threadIdx.x;
+    const int i = I * kTile + t, j = J * kTile + t;
+    const float wir = i < a.nsrc ? a.srcA[i].w : 0.0f, wii = i < a.nsrc ? a.srcB[i].w : 0.0f;
+    const float wjr = j < a.nsrc ? a.srcA[j].w : 0.0f, wji = j < a.nsrc ? a.srcB[j].w : 0.0f;
+    const float2 *Ub = U + (size_t)b * rmax * kTile, *Vb = V + (size_t)b * rmax * kTile;
+    for (int m = 0; m < k; ++m) {
+        const float2 v = Vb[m * kTile + t], u = Ub[m * kTile + t];
+        const float tr = block_sum(v.x * wir - v.y * wii, sv);
+        const float ti = block_sum(v.x * wii + v.y * wir, sv);
+        const float sr = block_sum(u.x * wjr - u.y * wji, sv);
+        const float sim = block_sum(u.x * wji + u.y * wjr, sv);
+        if (t == 0) {
+            tv[(size_t)b * rmax + m] = make_float2(tr, ti);
+            su[(size_t)b * rmax + m] = make_float2(sr, sim);
+        }
+    }
+}
+
+// Stage 2: per owner tile X, rows of every block with J = X (forward) and
+// columns of every block with I = X (reciprocal), in list order
+// (deterministic).  Results in FP64 per fragment.
+__global__ void __launch_bounds__(kTile) k_lr_expand(int n, int rmax, const float2 *U, const float2 *V, const int *rank,
+                                                     const float2 *tv, const float2 *su, const int *byJ_off,
+                                                     const int *byJ, const int *byI_off, const int *byI,
+                                                     double2 *yrow, double2 *ycol)
+{
+    const int X = blockIdx.x, t = threadIdx.x;
+    const int q = X * kTile + t;
+    double fr = 0.0, fi = 0.0, cr = 0.0, ci = 0.0;
+    for (int p = byJ_off[X]; p < byJ_off[X + 1]; ++p) {
+        const int b = byJ[p];
+        const int k = rank[b];
+        const float2 *Ub = U + (size_t)b * rmax * kTile;
+        float ar = 0.0f, ai = 0.0f;
+        for (int m = 0; m < k; ++m) {
+            const float2 u = Ub[m * kTile + t], c = tv[(size_t)b * rmax + m];
+            ar += u.x * c.x - u.y * c.y;
+            ai += u.x * c.y + u.y * c.x;
+        }
+        fr += ar;
+        fi += ai;
+    }
+    for (int p = byI_off[X]; p < byI_off[X + 1]; ++p) {
+        const int b = byI[p];
+        const int k = rank[b];
+        const float2 *Vb = V + (size_t)b * rmax * kTile;
+        float ar = 0.0f, ai = 0.0f;
+        for (int m = 0; m < k; ++m) {
+            const float2 v = Vb[m * kTile + t], c = su[(size_t)b * rmax + m];
+            ar += v.x * c.x - v.y * c.y;
+            ai += v.x * c.y + v.y * c.x;
+        }
+        cr += ar;
+        ci += ai;
+    }
+    if (q < n) {
+        yrow[q] = make_double2(fr, fi);
+        ycol[q] = make_double2(cr, ci);
+    }
+}
+
+// Per-tile geometry for block descriptors: centroid, radius, mean normal.
+__global__ void __launch_bounds__(kTile) k_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen,
+                                                      float4 *nmean)
+{
+    __shared__ float sv[kTile / 32];
+    const int T = blockIdx.x, t = threadIdx.x, i = T * kTile + t;
+    const bool v = i < n;
+    const float4 p = v ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 q = v ? nrm[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float cnt = block_sum(v ? 1.0f : 0.0f, sv);
+    const float cx = block_sum(p.x, sv) / cnt, cy = block_sum(p.y, sv) / cnt, cz = block_sum(p.z, sv) / cnt;
+    const float nx = block_sum(q.x, sv), ny = block_sum(q.y, sv), nz = block_sum(q.z, sv);
+    const float dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
+    float r = v ? sqrtf(dx * dx + dy * dy + dz * dz) : 0.0f;
+    for (int off = 16; off > 0; off >>= 1) r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, off));
+    __syncthreads();
+    if ((t & 31) == 0) sv[t >> 5] = r;
+    __syncthreads();
+    if (t == 0) {
+        float rm = 0.0f;
+        for (int w = 0; w < kTile / 32; ++w) rm = fmaxf(rm, sv[w]);
+        const float nl = sqrtf(nx * nx + ny * ny + nz * nz);
+        cen[T] = make_float4(cx, cy, cz, rm);
+        nmean[T] = nl > 0.0f ? make_float4(nx / nl, ny / nl, nz / nl, 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
 }
 
 // ---------------------------------------------------------------- helpers
@@ -1351,11 +1665,40 @@ void launch_sum_f2f_sym(const SumArgs &a, double2 *colpart, cudaStream_t s)
 }
 
 void launch_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,
-                             const int *cell, const double2 *Pin, double2 *Pout, double2 *P, cudaStream_t s)
+                             const int *cell, const double2 *Pin, double2 *Pout, double2 *P, cudaStream_t s,
+                             const double2 *yrow, const double2 *ycol)
 {
     if (ndst > 0)
         k_finalize_f2f_sym<<<blocks_for(ndst, 256), 256, 0, s>>>(partial, nsplit, ndst, colpart, ntiles, cell, Pin,
-                                                                 Pout, P);
+                                                                 Pout, P, yrow, ycol);
+}
+
+void launch_aca(const SumArgs &a, const int2 *blocks, int nblocks, int rmax, float tol, float2 *U, float2 *V,
+                int *rank, float *fro, float limit, float *err, cudaStream_t s)
+{
+    if (nblocks <= 0) return;
+    if (a.ka != 0.0f) {
+        k_aca<true><<<nblocks, kTile, 0, s>>>(a, blocks, nblocks, rmax, tol, U, V, rank, fro);
+        k_aca_judge<true><<<nblocks, 64, 0, s>>>(a, blocks, nblocks, rmax, limit, U, V, rank, fro, err);
+    } else {
+        k_aca<false><<<nblocks, kTile, 0, s>>>(a, blocks, nblocks, rmax, tol, U, V, rank, fro);
+        k_aca_judge<false><<<nblocks, 64, 0, s>>>(a, blocks, nblocks, rmax, limit, U, V, rank, fro, err);
+    }
+}
+
+void launch_lr_apply(const SumArgs &a, const int2 *blocks, const int *bidx, int nb, int rmax, const float2 *U,
+                     const float2 *V, const int *rank, float2 *tv, float2 *su, int ntiles, const int *byJ_off,
+                     const int *byJ, const int *byI_off, const int *byI, double2 *yrow, double2 *ycol, cudaStream_t s)
+{
+    if (nb > 0) k_lr_project<<<nb, kTile, 0, s>>>(a, blocks, bidx, nb, rmax, U, V, rank, tv, su);
+    if (ntiles > 0)
+        k_lr_expand<<<ntiles, kTile, 0, s>>>(a.nsrc, rmax, U, V, rank, tv, su, byJ_off, byJ, byI_off, byI, yrow,
+                                             ycol);
+}
+
+void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s)
+{
+    if (n > 0) k_tile_stats<<<(n + kTile - 1) / kTile, kTile, 0, s>>>(pos, nrm, n, cen, nmean);
 }
 
 void launch_pack_points(const float4 *pts, const double2 *P, int n, float4 *A, float4 *B, cudaStream_t s)

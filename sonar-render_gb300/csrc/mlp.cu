@@ -1,0 +1,402 @@
+// mlp.cu -- the learned admissibility model: a 4-layer, width-128 perceptron
+// trained and evaluated by this library's own CUDA kernels.
+//
+// It maps the descriptors of a fragment-cluster pair (separation and radii in
+// wavelengths, normal angles, visibility fraction) to the predicted log2 of
+// the rank adaptive cross approximation needs for that block.  Blocks whose
+// predicted rank is above the cut stay dense without an approximation
+// attempt; the others are approximated with a rank cap derived from the
+// prediction, and the exact tile still judges every approximation.
+//
+// Layers: 8 -> 128 -> 128 -> 128 -> 1, ReLU between, FP32 weights, activations
+// and gradients.  Training: mean-squared error on log2(rank), Adam.
+// Kernels: a shared-memory tiled dense layer (forward, input gradient, weight
+// gradient), bias/ReLU epilogues, the loss gradient and the Adam update.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "sonar_internal.h"
+
+namespace sonar {
+namespace {
+
+constexpr int kIn = 8, kWidth = 128, kLayers = 4;
+constexpr int kDims[kLayers + 1] = {kIn, kWidth, kWidth, kWidth, 1};
+constexpr int kT = 16;  // tile of the dense-layer kernels
+
+// Y[b, o] = sum_i X[b, i] W[o, i] + bias[o]  (optionally ReLU)
+__global__ void k_dense_fwd(const float *X, const float *W, const float *bias, float *Y, int B, int in, int out,
+                            int relu)
+{
+    __shared__ float sX[kT][kT + 1], sW[kT][kT + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int b = blockIdx.y * kT + ty, o = blockIdx.x * kT + tx;
+    float acc = 0.0f;
+    for (int k0 = 0; k0 < in; k0 += kT) {
+        sX[ty][tx] = (b < B && k0 + tx < in) ? X[(size_t)b * in + k0 + tx] : 0.0f;
+        const int ow = blockIdx.x * kT + ty;
+        sW[ty][tx] = (ow < out && k0 + tx < in) ? W[(size_t)ow * in + k0 + tx] : 0.0f;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kT; ++k) acc = fmaf(sX[ty][k], sW[tx][k], acc);
+        __syncthreads();
+    }
+    if (b < B && o < out) {
+        float v = acc + bias[o];
+        if (relu) v = fmaxf(v, 0.0f);
+        Y[(size_t)b * out + o] = v;
+    }
+}
+
+// dX[b, i] = sum_o dY[b, o] W[o, i]   (then masked by the ReLU of X's layer)
+__global__ void k_dense_bwd_x(const float *dY, const float *W, const float *Xact, float *dX, int B, int in, int out,
+                              int relu_mask)
+{
+    __shared__ float sD[kT][kT + 1], sW[kT][kT + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int b = blockIdx.y * kT + ty, i = blockIdx.x * kT + tx;
+    float acc = 0.0f;
+    for (int o0 = 0; o0 < out; o0 += kT) {
+        sD[ty][tx] = (b < B && o0 + tx < out) ? dY[(size_t)b * out + o0 + tx] : 0.0f;
+        const int iw = blockIdx.x * kT + tx;
+        sW[ty][tx] = (o0 + ty < out && iw < in) ? W[(size_t)(o0 + ty) * in + iw] : 0.0f;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kT; ++k) acc = fmaf(sD[ty][k], sW[k][tx], acc);
+        __syncthreads();
+    }
+    if (b < B && i < in) {
+        if (relu_mask && !(Xact[(size_t)b * in + i] > 0.0f)) acc = 0.0f;
+        dX[(size_t)b * in + i] = acc;
+    }
+}
+
+// dW[o, i] = sum_b dY[b, o] X[b, i]
+__global__ void k_dense_bwd_w(const float *dY, const float *X, float *dW, int B, int in, int out)
+{
+    __shared__ float sD[kT][kT + 1], sX[kT][kT + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int o = blockIdx.y * kT + ty, i = blockIdx.x * kT + tx;
+    float acc = 0.0f;
+    for (int b0 = 0; b0 < B; b0 += kT) {
+        const int ob = blockIdx.y * kT + tx;
+        sD[ty][tx] = (b0 + ty < B && ob < out) ? dY[(size_t)(b0 + ty) * out + ob] : 0.0f;
+        sX[ty][tx] = (b0 + ty < B && i < in) ? X[(size_t)(b0 + ty) * in + i] : 0.0f;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kT; ++k) acc = fmaf(sD[k][ty], sX[k][tx], acc);
+        __syncthreads();
+    }
+    if (o < out && i < in) dW[(size_t)o * in + i] = acc;
+}
+
+// db[o] = sum_b dY[b, o]
+__global__ void k_bias_grad(const float *dY, float *db, int B, int out)
+{
+    const int o = blockIdx.x;
+    float acc = 0.0f;
+    for (int b = threadIdx.x; b < B; b += blockDim.x) acc += dY[(size_t)b * out + o];
+    __shared__ float sv[8];
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) sv[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.0f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sv[w];
+        db[o] = t;
+    }
+}
+
+// mean-squared error: dY = 2 (y_hat - y) / B; per-sample squared error out
+__global__ void k_mse(const float *yhat, const float *y, float *dY, float *se, int B)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const float d = yhat[b] - y[b];
+    dY[b] = 2.0f * d / (float)B;
+    se[b] = d * d;
+}
+
+__global__ void k_adam(float *p, const float *g, float *m, float *v, int n, float lr, float b1, float b2, float eps,
+                       float c1, float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+__global__ void k_gather(const float *X, const float *y, const int *idx, int B, float *Xb, float *yb)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const int i = idx[b];
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) Xb[(size_t)b * kIn + k] = X[(size_t)i * kIn + k];
+    yb[b] = y[i];
+}
+
+inline dim3 tiles(int cols, int rows) { return dim3((cols + kT - 1) / kT, (rows + kT - 1) / kT); }
+
+}  // namespace
+
+// ---------------------------------------------------------------- host model
+struct Mlp {
+    // flat parameter vector: for each layer W (out x in) then b (out)
+    std::vector<size_t> woff, boff;
+    size_t nparam = 0;
+    float *d_p = nullptr, *d_g = nullptr, *d_m = nullptr, *d_v = nullptr;
+    int adam_t = 0;
+    bool ready = false;
+
+    void layout()
+    {
+        woff.assign(kLayers, 0);
+        boff.assign(kLayers, 0);
+        size_t o = 0;
+        for (int l = 0; l < kLayers; ++l) {
+            woff[l] = o;
+            o += (size_t)kDims[l + 1] * kDims[l];
+            boff[l] = o;
+            o += kDims[l + 1];
+        }
+        nparam = o;
+    }
+};
+
+static Mlp g_mlp;
+
+static cudaError_t mlp_alloc()
+{
+    if (g_mlp.d_p) return cudaSuccess;
+    g_mlp.layout();
+    cudaError_t e = cudaMalloc(&g_mlp.d_p, g_mlp.nparam * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&g_mlp.d_g, g_mlp.nparam * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&g_mlp.d_m, g_mlp.nparam * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&g_mlp.d_v, g_mlp.nparam * sizeof(float));
+    return e;
+}
+
+size_t mlp_param_count()
+{
+    g_mlp.layout();
+    return g_mlp.nparam;
+}
+
+// He-uniform initialisation from a seed (host), zero Adam state.
+cudaError_t mlp_init(unsigned seed)
+{
+    cudaError_t e = mlp_alloc();
+    if (e != cudaSuccess) return e;
+    std::vector<float> p(g_mlp.nparam, 0.0f);
+    std::mt19937 rng(seed);
+    for (int l = 0; l < kLayers; ++l) {
+        const float lim = std::sqrt(6.0f / (float)kDims[l]);
+        std::uniform_real_distribution<float> u(-lim, lim);
+        for (size_t k = 0; k < (size_t)kDims[l + 1] * kDims[l]; ++k) p[g_mlp.woff[l] + k] = u(rng);
+    }
+    e = cudaMemcpy(g_mlp.d_p, p.data(), p.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(g_mlp.d_m, 0, g_mlp.nparam * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(g_mlp.d_v, 0, g_mlp.nparam * sizeof(float));
+    g_mlp.adam_t = 0;
+    g_mlp.ready = e == cudaSuccess;
+    return e;
+}
+
+cudaError_t mlp_set_params(const float *p, size_t n)
+{
+    cudaError_t e = mlp_alloc();
+    if (e != cudaSuccess) return e;
+    if (n != g_mlp.nparam) return cudaErrorInvalidValue;
+    e = cudaMemcpy(g_mlp.d_p, p, n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(g_mlp.d_m, 0, n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(g_mlp.d_v, 0, n * sizeof(float));
+    g_mlp.adam_t = 0;
+    g_mlp.ready = e == cudaSuccess;
+    return e;
+}
+
+cudaError_t mlp_get_params(float *p, size_t n)
+{
+    if (!g_mlp.ready || n != g_mlp.nparam) return cudaErrorInvalidValue;
+    return cudaMemcpy(p, g_mlp.d_p, n * sizeof(float), cudaMemcpyDeviceToHost);
+}
+
+bool mlp_ready() { return g_mlp.ready; }
+
+// Activations of a batch: A[0] = X (B x 8), A[l] (B x dims[l]), A[4] = y_hat.
+struct Acts {
+    float *a[kLayers + 1] = {nullptr};
+    float *d[kLayers + 1] = {nullptr};
+    int B = 0;
+    cudaError_t alloc(int b)
+    {
+        release();
+        B = b;
+        for (int l = 0; l <= kLayers; ++l) {
+            cudaError_t e = cudaMalloc(&a[l], (size_t)b * kDims[l] * sizeof(float));
+            if (e == cudaSuccess) e = cudaMalloc(&d[l], (size_t)b * kDims[l] * sizeof(float));
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    void release()
+    {
+        for (int l = 0; l <= kLayers; ++l) {
+            if (a[l]) cudaFree(a[l]);
+            if (d[l]) cudaFree(d[l]);
+            a[l] = d[l] = nullptr;
+        }
+    }
+};
+
+static void forward(Acts &A, int B, cudaStream_t s)
+{
+    for (int l = 0; l < kLayers; ++l) {
+        const int in = kDims[l], out = kDims[l + 1];
+        k_dense_fwd<<<tiles(out, B), dim3(kT, kT), 0, s>>>(A.a[l], g_mlp.d_p + g_mlp.woff[l], g_mlp.d_p + g_mlp.boff[l],
+                                                            A.a[l + 1], B, in, out, l + 1 < kLayers);
+    }
+}
+
+// gradient of the mean squared error of one batch into d_g; per-sample
+// squared errors into se (device, B floats)
+static void backward(Acts &A, const float *y, float *se, int B, cudaStream_t s)
+{
+    k_mse<<<(B + 255) / 256, 256, 0, s>>>(A.a[kLayers], y, A.d[kLayers], se, B);
+    for (int l = kLayers - 1; l >= 0; --l) {
+        const int in = kDims[l], out = kDims[l + 1];
+        k_dense_bwd_w<<<tiles(in, out), dim3(kT, kT), 0, s>>>(A.d[l + 1], A.a[l], g_mlp.d_g + g_mlp.woff[l], B, in,
+                                                              out);
+        k_bias_grad<<<out, 256, 0, s>>>(A.d[l + 1], g_mlp.d_g + g_mlp.boff[l], B, out);
+        if (l > 0)
+            k_dense_bwd_x<<<tiles(in, B), dim3(kT, kT), 0, s>>>(A.d[l + 1], g_mlp.d_p + g_mlp.woff[l], A.a[l],
+                                                                A.d[l], B, in, out, 1);
+    }
+}
+
+// One forward/backward pass; gradient and loss to the host (gradient checks).
+cudaError_t mlp_grad(const float *X, const float *y, int B, float *grad, float *loss)
+{
+    if (!g_mlp.ready || B <= 0) return cudaErrorInvalidValue;
+    Acts A;
+    float *d_y = nullptr, *d_se = nullptr;
+    cudaError_t e = A.alloc(B);
+    if (e == cudaSuccess) e = cudaMalloc(&d_y, B * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_se, B * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(A.a[0], X, (size_t)B * kIn * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_y, y, B * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        forward(A, B, 0);
+        backward(A, d_y, d_se, B, 0);
+        e = cudaGetLastError();
+    }
+    std::vector<float> se(B);
+    if (e == cudaSuccess) e = cudaMemcpy(grad, g_mlp.d_g, g_mlp.nparam * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(se.data(), d_se, B * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) {
+        double t = 0.0;
+        for (float v : se) t += v;
+        *loss = (float)(t / B);
+    }
+    A.release();
+    if (d_y) cudaFree(d_y);
+    if (d_se) cudaFree(d_se);
+    return e;
+}
+
+// Adam training on device arrays (n rows of 8 descriptors, n labels):
+// mini-batches in a seeded shuffled order, gathered on the device.  Returns
+// the mean squared error of the last epoch.
+cudaError_t mlp_train_dev(const float *d_X, const float *d_y, int n, int epochs, int batch, float lr, unsigned seed,
+                          float *last_loss, cudaStream_t s)
+{
+    if (!g_mlp.ready || n <= 0 || epochs < 0) return cudaErrorInvalidValue;
+    batch = std::max(1, std::min(batch, n));
+    const int nb = n / batch;
+    float *d_by = nullptr, *d_se = nullptr;
+    int *d_idx = nullptr;
+    Acts A;
+    cudaError_t e = cudaMalloc(&d_se, (size_t)nb * batch * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_by, (size_t)batch * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_idx, (size_t)n * sizeof(int));
+    if (e == cudaSuccess) e = A.alloc(batch);
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::mt19937 rng(seed);
+    std::vector<float> se((size_t)nb * batch);
+    double epoch_loss = 0.0;
+    for (int ep = 0; ep < epochs && e == cudaSuccess; ++ep) {
+        std::shuffle(order.begin(), order.end(), rng);
+        e = cudaMemcpyAsync(d_idx, order.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s);
+        for (int k = 0; k < nb && e == cudaSuccess; ++k) {
+            k_gather<<<(batch + 255) / 256, 256, 0, s>>>(d_X, d_y, d_idx + (size_t)k * batch, batch, A.a[0], d_by);
+            forward(A, batch, s);
+            backward(A, d_by, d_se + (size_t)k * batch, batch, s);
+            ++g_mlp.adam_t;
+            const float b1 = 0.9f, b2 = 0.999f;
+            const float c1 = 1.0f - std::pow(b1, (float)g_mlp.adam_t), c2 = 1.0f - std::pow(b2, (float)g_mlp.adam_t);
+            k_adam<<<(unsigned)((g_mlp.nparam + 255) / 256), 256, 0, s>>>(
+                g_mlp.d_p, g_mlp.d_g, g_mlp.d_m, g_mlp.d_v, (int)g_mlp.nparam, lr, b1, b2, 1e-8f, c1, c2);
+        }
+        // the order vector must stay unchanged until its upload has completed
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    if (e == cudaSuccess && epochs > 0 && nb > 0) {
+        e = cudaMemcpy(se.data(), d_se, se.size() * sizeof(float), cudaMemcpyDeviceToHost);
+        for (float v : se) epoch_loss += v;
+        epoch_loss /= (double)se.size();
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (last_loss) *last_loss = (float)epoch_loss;
+    A.release();
+    if (d_se) cudaFree(d_se);
+    if (d_by) cudaFree(d_by);
+    if (d_idx) cudaFree(d_idx);
+    return e;
+}
+
+// The same from host arrays.
+cudaError_t mlp_train(const float *X, const float *y, int n, int epochs, int batch, float lr, unsigned seed,
+                      float *last_loss)
+{
+    if (!g_mlp.ready || n <= 0) return cudaErrorInvalidValue;
+    float *d_X = nullptr, *d_y = nullptr;
+    cudaError_t e = cudaMalloc(&d_X, (size_t)n * kIn * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_y, (size_t)n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(d_X, X, (size_t)n * kIn * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_y, y, (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = mlp_train_dev(d_X, d_y, n, epochs, batch, lr, seed, last_loss, 0);
+    if (d_X) cudaFree(d_X);
+    if (d_y) cudaFree(d_y);
+    return e;
+}
+
+// Predicted log2(rank) of n descriptor rows (device arrays), on stream s.
+cudaError_t mlp_predict_dev(const float *dX, int n, float *dY, cudaStream_t s)
+{
+    if (!g_mlp.ready) return cudaErrorInvalidValue;
+    if (n <= 0) return cudaSuccess;
+    Acts A;
+    cudaError_t e = A.alloc(n);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(A.a[0], dX, (size_t)n * kIn * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) {
+        forward(A, n, s);
+        e = cudaMemcpyAsync(dY, A.a[kLayers], (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    A.release();
+    return e;
+}
+
+}  // namespace sonar

@@ -103,10 +103,36 @@ struct Object {
 struct MaskEntry {
     int hop, a, b;
     int upper_only = 0;
+    long long classes[4] = {0, 0, 0, 0};  // blocks per flag: none, bits, clear, all
     int nsrc, ndst;
     MaskView view{};
     float mask_ms = 0.0f;
     bool stale = false;  // rebuild into the same buffers before the next use
+};
+
+// Low-rank compression of the FACET_SELF blocks of one object (built with its
+// mask, rebuilt when the mask or k changes).
+struct Compression {
+    bool valid = false;
+    int obj = -1;
+    double kr = 0.0, ki = 0.0;
+    int nblocks = 0, naccepted = 0, rmax = 0;
+    double mean_rank = 0.0, max_err = 0.0;
+    float build_ms = 0.0f;
+    int2 *d_blocks = nullptr;
+    float2 *d_U = nullptr, *d_V = nullptr, *d_tv = nullptr, *d_su = nullptr;
+    int *d_rank = nullptr, *d_bidx = nullptr;
+    float *d_fro = nullptr, *d_err = nullptr;
+    int *d_byJ_off = nullptr, *d_byJ = nullptr, *d_byI_off = nullptr, *d_byI = nullptr;
+    uint8_t *d_flags = nullptr;  // the mask flags with accepted blocks removed (dense kernel)
+    double2 *d_yrow = nullptr, *d_ycol = nullptr;
+    void release()
+    {
+        dfree(d_blocks); dfree(d_U); dfree(d_V); dfree(d_tv); dfree(d_su); dfree(d_rank); dfree(d_bidx);
+        dfree(d_fro); dfree(d_err); dfree(d_byJ_off); dfree(d_byJ); dfree(d_byI_off); dfree(d_byI);
+        dfree(d_flags); dfree(d_yrow); dfree(d_ycol);
+        valid = false;
+    }
 };
 
 struct HopRecord {
@@ -117,6 +143,10 @@ struct HopRecord {
     float total_ms;  // pack + sum + finalize
     int nsplit;
     int launches;    // kernels launched by this hop, mask included
+    // compressed bounce blocks (FACET_SELF with compression on)
+    int cmp_blocks = 0, cmp_accepted = 0;
+    double cmp_mean_rank = 0.0, cmp_max_err = 0.0;
+    float cmp_build_ms = 0.0f, lr_ms = 0.0f;
 };
 
 struct Model {
@@ -131,7 +161,7 @@ struct Model {
     std::string err;
     // device
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr, ev4 = nullptr, ev5 = nullptr;
     float4 *d_src_pos = nullptr, *d_fp_pos = nullptr;
     double2 *d_src_P = nullptr, *d_fp_P = nullptr;
     // field points are kept in Morton (spatial) order on the device so that a
@@ -154,6 +184,12 @@ struct Model {
     int opt_split = 0;
     int verbose = 0;
     int opt_f2f_sym = 1;
+    int opt_class_stats = 0;
+    // compression of the bounce blocks
+    int opt_compress = 0;
+    float opt_cmp_tol = 1e-4f, opt_cmp_judge = 3e-4f, opt_cmp_eta = 1.0f;
+    int opt_cmp_rmax = 32;
+    Compression cmp;
     std::vector<HopRecord> log;
     long long launches = 0, h2d_bytes = 0, d2h_bytes = 0;
 
@@ -168,9 +204,10 @@ struct Model {
             dfree(m.view.flags);
         }
         masks.clear();
+        cmp.release();
         dfree(d_packA); dfree(d_packB); dfree(d_partial); dfree(d_limit); dfree(d_colpart);
         pack_cap = partial_cap = limit_cap = colpart_cap = 0;
-        for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3})
+        for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3, &ev4, &ev5})
             if (*e) {
                 cudaEventDestroy(*e);
                 *e = nullptr;
@@ -320,7 +357,7 @@ void render()
 {
     if (g.rendered) fail(-2, "render_cuda called twice without TearDownCuda");
     CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
-    for (cudaEvent_t *e : {&g.ev0, &g.ev1, &g.ev2, &g.ev3}) CK(cudaEventCreate(e));
+    for (cudaEvent_t *e : {&g.ev0, &g.ev1, &g.ev2, &g.ev3, &g.ev4, &g.ev5}) CK(cudaEventCreate(e));
     for (int t : {OBJ_TARGET, OBJ_FIELD})
         for (auto &o : g.obj[t]) render_object(*o);
     // occluders: every triangle of every target object (OptiX.cpp:264-296)
@@ -461,6 +498,11 @@ MaskEntry build_mask(int hop, int a, int b, int full, const MaskEntry *reuse = n
     CK(cudaEventRecord(g.ev1, g.stream));
     CK(cudaEventSynchronize(g.ev1));
     CK(cudaEventElapsedTime(&e.mask_ms, g.ev0, g.ev1));
+    if (g.opt_class_stats && nflags > 0) {
+        std::vector<uint8_t> fl(nflags);
+        CK(cudaMemcpy(fl.data(), v.flags, nflags, cudaMemcpyDeviceToHost));
+        for (uint8_t f : fl) e.classes[f & 3]++;
+    }
     return e;
 }
 
@@ -508,6 +550,110 @@ void ensure_colpart(int ntiles)
     }
 }
 
+// Choose and compress the admissible blocks of a FACET_SELF hop: upper
+// blocks (I < J) whose every pair interacts (mask class ALL) and whose tile
+// centroids are farther apart than eta (r_I + r_J).  Every candidate is
+// compressed by adaptive cross approximation (rank cap rmax, tolerance tol)
+// and judged on sampled exact entries; accepted blocks leave the dense
+// kernel's flags.
+void build_compression(int a, MaskEntry &M, const SumArgs &s)
+{
+    Compression &C = g.cmp;
+    C.release();
+    Object &A = get(OBJ_TARGET, a);
+    const int nt = M.view.ntiles, nb = M.view.ndstblocks;
+    cudaStream_t st = g.stream;
+    CK(cudaEventRecord(g.ev2, st));
+    // tile geometry
+    float4 *d_cen = dalloc<float4>(nt), *d_nm = dalloc<float4>(nt);
+    launch_tile_stats(g.d_packA, g.d_packB, M.nsrc, d_cen, d_nm, st);
+    std::vector<float4> cen(nt), nm(nt);
+    std::vector<uint8_t> flags((size_t)nt * nb);
+    CK(cudaMemcpyAsync(cen.data(), d_cen, nt * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(nm.data(), d_nm, nt * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(flags.data(), M.view.flags, flags.size(), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    dfree(d_cen);
+    dfree(d_nm);
+    std::vector<int2> blocks;
+    for (int J = 0; J < nb; J++)
+        for (int I = 0; I < std::min(J, nt); I++) {
+            if (flags[(size_t)I * nb + J] != kFlagAll) continue;
+            const float dx = cen[I].x - cen[J].x, dy = cen[I].y - cen[J].y, dz = cen[I].z - cen[J].z;
+            const float sep = std::sqrt(dx * dx + dy * dy + dz * dz);
+            if (sep > g.opt_cmp_eta * (cen[I].w + cen[J].w)) blocks.push_back(make_int2(I, J));
+        }
+    C.nblocks = (int)blocks.size();
+    C.rmax = g.opt_cmp_rmax;
+    C.obj = a;
+    C.kr = g.kr;
+    C.ki = g.ki;
+    C.d_flags = dalloc<uint8_t>(flags.size());
+    C.d_yrow = dalloc<double2>(M.nsrc);
+    C.d_ycol = dalloc<double2>(M.nsrc);
+    std::vector<int> rank(C.nblocks);
+    std::vector<float> err(C.nblocks);
+    if (C.nblocks > 0) {
+        C.d_blocks = dalloc<int2>(C.nblocks);
+        const size_t per = (size_t)C.rmax * kTile;
+        C.d_U = dalloc<float2>(per * C.nblocks);
+        C.d_V = dalloc<float2>(per * C.nblocks);
+        C.d_tv = dalloc<float2>((size_t)C.rmax * C.nblocks);
+        C.d_su = dalloc<float2>((size_t)C.rmax * C.nblocks);
+        C.d_rank = dalloc<int>(C.nblocks);
+        C.d_fro = dalloc<float>(C.nblocks);
+        C.d_err = dalloc<float>(C.nblocks);
+        CK(cudaMemcpyAsync(C.d_blocks, blocks.data(), blocks.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+        launch_aca(s, C.d_blocks, C.nblocks, C.rmax, g.opt_cmp_tol, C.d_U, C.d_V, C.d_rank, C.d_fro,
+                   g.opt_cmp_judge, C.d_err, st);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(rank.data(), C.d_rank, C.nblocks * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(err.data(), C.d_err, C.nblocks * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    // accepted blocks: dense flags off, owner lists
+    std::vector<int> bidx;
+    std::vector<std::vector<int>> byJ(nb), byI(nt);
+    double rsum = 0.0, emax = 0.0;
+    for (int b = 0; b < C.nblocks; b++) {
+        if (rank[b] <= 0) continue;
+        bidx.push_back(b);
+        flags[(size_t)blocks[b].x * nb + blocks[b].y] = kFlagNone;
+        byJ[blocks[b].y].push_back(b);
+        byI[blocks[b].x].push_back(b);
+        rsum += rank[b];
+        emax = std::max(emax, (double)err[b]);
+    }
+    C.naccepted = (int)bidx.size();
+    C.mean_rank = C.naccepted ? rsum / C.naccepted : 0.0;
+    C.max_err = emax;
+    auto csr = [&](const std::vector<std::vector<int>> &lists, int *&d_off, int *&d_idx) {
+        std::vector<int> off(lists.size() + 1, 0), idx;
+        for (size_t x = 0; x < lists.size(); x++) {
+            off[x + 1] = off[x] + (int)lists[x].size();
+            idx.insert(idx.end(), lists[x].begin(), lists[x].end());
+        }
+        d_off = dalloc<int>(off.size());
+        d_idx = dalloc<int>(std::max<size_t>(idx.size(), 1));
+        CK(cudaMemcpyAsync(d_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        if (!idx.empty()) CK(cudaMemcpyAsync(d_idx, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    };
+    // the expansion runs per tile X covering both roles (J = X rows, I = X columns)
+    byI.resize(nb);
+    byJ.resize(nb);
+    csr(byJ, C.d_byJ_off, C.d_byJ);
+    csr(byI, C.d_byI_off, C.d_byI);
+    C.d_bidx = dalloc<int>(std::max<size_t>(bidx.size(), 1));
+    if (!bidx.empty())
+        CK(cudaMemcpyAsync(C.d_bidx, bidx.data(), bidx.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(C.d_flags, flags.data(), flags.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(g.ev3, st));
+    CK(cudaEventSynchronize(g.ev3));
+    CK(cudaEventElapsedTime(&C.build_ms, g.ev2, g.ev3));
+    C.valid = true;
+    (void)A;
+}
+
 int choose_split(int ntiles, int ndstblocks)
 {
     if (g.opt_split > 0) return std::min(g.opt_split, std::max(ntiles, 1));
@@ -542,6 +688,9 @@ void timed_sum(const SumArgs &s, cudaStream_t st)
 void run_hop(int hop, int a, int b)
 {
     MaskEntry &M = get_mask(hop, a, b);
+    const bool mask_rebuilt = M.mask_ms > 0.0f;  // built for this call (reported once)
+    float rec_cmp_build = 0.0f;
+    bool rec_cmp = false;
     if (M.nsrc == 0 || M.ndst == 0) return;
     HopSets hs = hop_sets(hop, a, b);
     SumArgs s{};
@@ -588,11 +737,27 @@ void run_hop(int hop, int a, int b)
                           g.d_packB, st);
         if (g.opt_f2f_sym) {
             ensure_colpart(M.view.ntiles);
+            const double2 *yrow = nullptr, *ycol = nullptr;
+            if (g.opt_compress) {
+                Compression &C = g.cmp;
+                if (!C.valid || C.obj != a || C.kr != g.kr || C.ki != g.ki || mask_rebuilt) {
+                    build_compression(a, M, s);
+                    rec_cmp_build = C.build_ms;
+                }
+                s.mask.flags = C.d_flags;  // accepted blocks are left to the low-rank path
+                CK(cudaEventRecord(g.ev4, st));
+                launch_lr_apply(s, C.d_blocks, C.d_bidx, C.naccepted, C.rmax, C.d_U, C.d_V, C.d_rank, C.d_tv, C.d_su,
+                                M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, st);
+                CK(cudaEventRecord(g.ev5, st));
+                yrow = C.d_yrow;
+                ycol = C.d_ycol;
+                rec_cmp = true;
+            }
             CK(cudaEventRecord(g.ev2, st));
             launch_sum_f2f_sym(s, g.d_colpart, st);
             CK(cudaEventRecord(g.ev3, st));
             launch_finalize_f2f_sym(g.d_partial, s.nsplit, M.ndst, g.d_colpart, M.view.ntiles, A.d_act_cell, A.d_Pin,
-                                    A.d_Pout, A.d_P, st);
+                                    A.d_Pout, A.d_P, st, yrow, ycol);
         } else {
             timed_sum(s, st);
             launch_finalize_f2f(g.d_partial, s.nsplit, M.ndst, A.d_act_cell, A.d_Pout, A.d_P, st);
@@ -612,9 +777,18 @@ void run_hop(int hop, int a, int b)
     float ms = 0.0f, sum_ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
     CK(cudaEventElapsedTime(&sum_ms, g.ev2, g.ev3));
-    const int nl = (hop == HOP_F2F ? 4 : 3) + (M.mask_ms > 0.0f ? 1 : 0);
-    g.launches += hop == HOP_F2F ? 4 : 3;
-    g.log.push_back(HopRecord{hop, pair_count(hop, a, b), M.mask_ms, sum_ms, ms, s.nsplit, nl});
+    const int nl = (hop == HOP_F2F ? 4 : 3) + (M.mask_ms > 0.0f ? 1 : 0) + (rec_cmp ? 2 : 0);
+    g.launches += (hop == HOP_F2F ? 4 : 3) + (rec_cmp ? 2 : 0) + (rec_cmp_build > 0.0f ? 3 : 0);
+    HopRecord rec{hop, pair_count(hop, a, b), M.mask_ms, sum_ms, ms, s.nsplit, nl};
+    if (rec_cmp) {
+        rec.cmp_blocks = g.cmp.nblocks;
+        rec.cmp_accepted = g.cmp.naccepted;
+        rec.cmp_mean_rank = g.cmp.mean_rank;
+        rec.cmp_max_err = g.cmp.max_err;
+        rec.cmp_build_ms = rec_cmp_build;
+        CK(cudaEventElapsedTime(&rec.lr_ms, g.ev4, g.ev5));
+    }
+    g.log.push_back(rec);
     M.mask_ms = 0.0f;  // reported once, with the first use
 }
 
@@ -893,20 +1067,29 @@ int sonar_get_fragment_layout(int objectType, int objIdx, int *nx_ny_neg, int nf
 int sonar_get_stats(char *json, int cap)
 {
     std::string s = "{\"hops\": [";
-    char buf[256];
+    char buf[512];
     for (size_t i = 0; i < g.log.size(); i++) {
         const HopRecord &r = g.log[i];
         snprintf(buf, sizeof(buf),
                  "%s{\"hop\": %d, \"pairs\": %lld, \"mask_ms\": %.6f, \"sum_ms\": %.6f, \"total_ms\": %.6f, "
-                 "\"nsplit\": %d, \"launches\": %d}",
-                 i ? ", " : "", r.hop, r.pairs, r.mask_ms, r.sum_ms, r.total_ms, r.nsplit, r.launches);
+                 "\"nsplit\": %d, \"launches\": %d, \"cmp_blocks\": %d, \"cmp_accepted\": %d, "
+                 "\"cmp_mean_rank\": %.3f, \"cmp_max_err\": %.3e, \"cmp_build_ms\": %.6f, \"lr_ms\": %.6f}",
+                 i ? ", " : "", r.hop, r.pairs, r.mask_ms, r.sum_ms, r.total_ms, r.nsplit, r.launches, r.cmp_blocks,
+                 r.cmp_accepted, r.cmp_mean_rank, r.cmp_max_err, r.cmp_build_ms, r.lr_ms);
         s += buf;
     }
     snprintf(buf, sizeof(buf),
              "], \"ntri\": %d, \"nnodes\": %d, \"masks\": %zu, \"launches\": %lld, \"h2d_bytes\": %lld, "
-             "\"d2h_bytes\": %lld}",
+             "\"d2h_bytes\": %lld, \"mask_classes\": [",
              g.ntri, g.nnodes, g.masks.size(), g.launches, g.h2d_bytes, g.d2h_bytes);
     s += buf;
+    for (size_t i = 0; i < g.masks.size(); i++) {
+        const MaskEntry &m = g.masks[i];
+        snprintf(buf, sizeof(buf), "%s{\"hop\": %d, \"none\": %lld, \"bits\": %lld, \"clear\": %lld, \"all\": %lld}",
+                 i ? ", " : "", m.hop, m.classes[0], m.classes[1], m.classes[2], m.classes[3]);
+        s += buf;
+    }
+    s += "]}";
     if (json && cap > 0) {
         const size_t n = std::min<size_t>(s.size(), (size_t)cap - 1);
         memcpy(json, s.data(), n);
@@ -920,6 +1103,16 @@ int sonar_set_option(const char *key, double value)
     if (!key) return -1;
     if (!strcmp(key, "split")) { g.opt_split = (int)value; return 0; }
     if (!strcmp(key, "f2f_symmetric")) { g.opt_f2f_sym = value != 0.0; return 0; }
+    if (!strcmp(key, "class_stats")) { g.opt_class_stats = value != 0.0; return 0; }
+    if (!strcmp(key, "compress")) { g.opt_compress = value != 0.0; g.cmp.release(); return 0; }
+    if (!strcmp(key, "compress_tol")) { g.opt_cmp_tol = (float)value; g.cmp.release(); return 0; }
+    if (!strcmp(key, "compress_judge")) { g.opt_cmp_judge = (float)value; g.cmp.release(); return 0; }
+    if (!strcmp(key, "compress_eta")) { g.opt_cmp_eta = (float)value; g.cmp.release(); return 0; }
+    if (!strcmp(key, "compress_rmax")) {
+        g.opt_cmp_rmax = std::max(1, std::min(256, (int)value));
+        g.cmp.release();
+        return 0;
+    }
     if (!strcmp(key, "verbose")) { g.verbose = (int)value; return 0; }
     if (!strcmp(key, "reset_stats")) {
         g.log.clear();

@@ -111,7 +111,16 @@ void launch_mask_export(const MaskView &m, int nsrc, int ndst, uint8_t *out, cud
 // colpart holds 256 * ntiles * (ntiles - 1) / 2 double2.
 void launch_sum_f2f_sym(const SumArgs &a, double2 *colpart, cudaStream_t s);
 void launch_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,
-                             const int *cell, const double2 *Pin, double2 *Pout, double2 *P, cudaStream_t s);
+                             const int *cell, const double2 *Pin, double2 *Pout, double2 *P, cudaStream_t s,
+                             const double2 *yrow = nullptr, const double2 *ycol = nullptr);
+// Low-rank FACET_SELF blocks (adaptive cross approximation, judged on sampled
+// entries; rank -1 = keep dense) and their application in a bounce.
+void launch_aca(const SumArgs &a, const int2 *blocks, int nblocks, int rmax, float tol, float2 *U, float2 *V,
+                int *rank, float *fro, float limit, float *err, cudaStream_t s);
+void launch_lr_apply(const SumArgs &a, const int2 *blocks, const int *bidx, int nb, int rmax, const float2 *U,
+                     const float2 *V, const int *rank, float2 *tv, float2 *su, int ntiles, const int *byJ_off,
+                     const int *byJ, const int *byI_off, const int *byI, double2 *yrow, double2 *ycol, cudaStream_t s);
+void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s);
 // surface.cu: pressure -> RGBA colour map of the reference's surface textures
 void launch_colour_map(const double2 *P, long long n, float min_db, float max_db, int phase, float4 *out,
                        cudaStream_t s);
