@@ -165,8 +165,21 @@ def run_gb300(args):
     api.load_library()
     cfg = workload(args.workload)
 
+    train_info = None
+    if args.compress and args.select == 2:
+        # the admissibility network learns from the exact method's blocks of
+        # the same trihedral at other frequencies (untimed set-up)
+        from sonar_render_gb300 import admissibility, scenes
+        t0 = time.time()
+        train_cfgs = [scenes.trihedral_config(f, bounces=1, n_theta=4, n_phi=4) for f in (40e3, 50e3)]
+        X, y, loss = admissibility.train_on_scenes(train_cfgs, epochs=args.train_epochs, batch=256, lr=1e-3, seed=0)
+        train_info = {"samples": int(len(y)), "scenes": ["trihedral_1m_40kHz", "trihedral_1m_50kHz"],
+                      "epochs": args.train_epochs, "final_mse": loss, "seconds": round(time.time() - t0, 2)}
+        print("network trained: %s" % json.dumps(train_info), file=sys.stderr)
+
     # ---- device-timed steps on the resident scene
     api.set_option("compress", args.compress)
+    api.set_option("compress_select", args.select)
     load_scene(api, cfg)
     ext = torch.cuda.ExternalStream(api.stream_handle())
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
@@ -450,6 +463,9 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
     ap.add_argument("--compress", type=int, default=0, help="compress admissible bounce blocks (low rank)")
+    ap.add_argument("--select", type=int, default=0,
+                    help="compressed blocks: 0 separation rule, 1 every interacting block, 2 the trained network")
+    ap.add_argument("--train-epochs", type=int, default=40)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

@@ -127,8 +127,18 @@ int sonar_get_stats(char *json, int cap);
  * ordered pair separately),
  * "verbose" (0/1), "reset_stats", "reset_pressures" (zero every surface and
  * field-point pressure), "drop_masks" (rebuild the cached interaction masks,
- * in place, at their next use), "free_masks" (free them).  Returns 0, or < 0
- * for an unknown key or a failed action. */
+ * in place, at their next use), "free_masks" (free them), "class_stats"
+ * (count the mask's block classes).
+ * Low-rank bounce blocks (no counterpart in the reference, which evaluates
+ * every pair): "compress" (0/1), "compress_tol" (cross-approximation stopping
+ * tolerance, 1e-4), "compress_judge" (largest accepted relative RMS error of
+ * a block on its sampled exact entries, 3e-4), "compress_rmax" (rank cap,
+ * 32, at most 64), "compress_select" (which blocks are approximated: 0 those
+ * whose every pair interacts and whose tiles are farther apart than
+ * "compress_eta" (1.0) times the sum of their radii; 1 every interacting
+ * block; 2 the blocks the admissibility network proposes), "compress_rcut"
+ * (the network proposes blocks with predicted rank below this, 24).
+ * Returns 0, or < 0 for an unknown key or a failed action. */
 int sonar_set_option(const char *key, double value);
 /* The library's CUDA stream (a cudaStream_t; NULL before render_cuda), for
  * callers that time or order work against it. */
@@ -154,6 +164,31 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
  * count, or < 0 for invalid arguments. */
 long long sonar_fragment_triangle(const float *tri9, float delta, int *nx_ny_neg, float *frame17, float *areas,
                                   long long cap);
+
+/* Admissibility network for the low-rank bounce blocks (no counterpart in the
+ * reference): a perceptron 8 -> 128 -> 128 -> 128 -> 1 with ReLU, FP32,
+ * trained and run by the library's own CUDA kernels.  Input: 8 descriptors
+ * of a block (log2(1 + separation / lambda), log2(1 + radius / lambda) of the
+ * source and destination tiles, cosines of both mean normals with the
+ * separation direction and with each other, (r_I + r_J) / separation capped
+ * at 4, fraction of interacting pairs); output: predicted log2(1 + rank).
+ * Parameters: per layer the weights (out x in, row-major) then the biases.
+ * Every call returns 0 or a negative code (sonar_last_error). */
+int sonar_mlp_param_count(void);
+int sonar_mlp_init(unsigned seed); /* He-uniform weights, zero biases */
+int sonar_mlp_set_params(const float *params, long long n);
+int sonar_mlp_get_params(float *params, long long n);
+/* Mean squared error of (X: n x 8, y: n) and its gradient (param_count floats). */
+int sonar_mlp_grad(const float *X, const float *y, int n, float *grad, float *loss);
+/* Adam (beta 0.9, 0.999, eps 1e-8) over seeded shuffled mini-batches; loss
+ * gets the mean squared error of the last epoch. */
+int sonar_mlp_train(const float *X, const float *y, int n, int epochs, int batch, float lr, unsigned seed,
+                    float *loss);
+int sonar_mlp_predict(const float *X, int n, float *out);
+/* Descriptors (n x 8) and rank labels (n; log2(1 + rank), or log2(1 + 2 cap)
+ * for blocks the judge rejected) of the blocks approximated by the last
+ * compressed bounce.  Returns n; copies when cap >= n. */
+long long sonar_get_block_samples(float *X, float *y, long long cap);
 
 /* Fragment -> field-point readout that allocates no memory.  No counterpart in
  * the reference: it exists for callers that cannot call cudaMalloc while they

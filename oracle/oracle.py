@@ -38,12 +38,12 @@ _vp = C.c_void_p
 
 def build(force: bool = False) -> str:
     """Compile the oracle library with gcc (no fused multiply-add, OpenMP)."""
-    src = os.path.join(HERE, "sonar_oracle.c")
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, "sonar_oracle.c"), os.path.join(HERE, "mlp_oracle.c")]
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(s) for s in srcs):
         os.makedirs(os.path.dirname(LIB), exist_ok=True)
         tmp = LIB + ".tmp%d" % os.getpid()
         subprocess.check_call(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off",
-                               "-fopenmp", "-o", tmp, src, "-lm"])
+                               "-fopenmp", "-o", tmp] + srcs + ["-lm"])
         os.replace(tmp, LIB)
     return LIB
 
@@ -101,6 +101,8 @@ def lib():
         L.orc_fragment_triangle.argtypes = [_f, C.c_float, _i, _f, _f, C.c_long]
         L.orc_fragment_triangle.restype = C.c_long
         L.orc_segment.argtypes = [_vp, _d, _d, C.c_double, _i]
+        L.orc_mlp_forward.argtypes = [_f, _f, C.c_int, _d]
+        L.orc_mlp_grad.argtypes = [_f, _f, _f, C.c_int, _d, _d]
         _lib = L
     return _lib
 
@@ -131,6 +133,30 @@ def fragment_triangle(tri9, delta):
     L.orc_fragment_triangle(_fp(t), C.c_float(delta), ints.ctypes.data_as(_i), _fp(fl), _fp(areas), n)
     nx, ny, neg = (int(v) for v in ints)
     return (nx, ny, neg), fl, areas[:n].reshape(ny, nx)
+
+
+def mlp_param_count() -> int:
+    return int(lib().orc_mlp_param_count())
+
+
+def mlp_forward(params, X):
+    """FP64 predictions of the admissibility network (n x 8 inputs)."""
+    p = np.ascontiguousarray(params, np.float32)
+    X = np.ascontiguousarray(X, np.float32).reshape(-1, 8)
+    out = np.zeros(len(X), np.float64)
+    lib().orc_mlp_forward(_fp(p), _fp(X), C.c_int(len(X)), out.ctypes.data_as(_d))
+    return out
+
+
+def mlp_grad(params, X, y):
+    """FP64 mean squared error and its gradient."""
+    p = np.ascontiguousarray(params, np.float32)
+    X = np.ascontiguousarray(X, np.float32).reshape(-1, 8)
+    y = np.ascontiguousarray(y, np.float32)
+    g = np.zeros(mlp_param_count(), np.float64)
+    loss = C.c_double(0.0)
+    lib().orc_mlp_grad(_fp(p), _fp(X), _fp(y), C.c_int(len(X)), g.ctypes.data_as(_d), C.byref(loss))
+    return loss.value, g
 
 
 class Oracle:

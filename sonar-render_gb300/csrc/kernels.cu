@@ -1187,41 +1187,17 @@ __global__ void k_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst,
 
 // ---------------------------------------------------------------- low-rank blocks
 // Compressed FACET_SELF blocks.  For a block of source tile I and destination
-// tile J (I < J, every pair interacting: mask class ALL) the interaction matrix
-// T_ji = cos_scat cos_inc G(r_ji) (weights excluded) is approximated by
-// U V^T with U: 256 x k over the rows j of J and V: 256 x k over the columns i
-// of I, built by adaptive cross approximation with partial pivoting: each
-// step takes the residual row at a pivot row, its largest entry as pivot
-// column, the residual column there, and stops when |u_k| |v_k| falls below
-// tol times the running Frobenius estimate.  The forward terms are then
-// U (V^T w_I) into J and the reciprocal ones V (U^T w_J) into I.
-
-__device__ __forceinline__ void block_argmax(float v, int idx, float *sv, int *si, float &best, int &bi)
-{
-    // block-wide argmax of v (ties: lowest index); all threads get the result
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int off = 16; off > 0; off >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, v, off);
-        const int oi = __shfl_xor_sync(0xffffffffu, idx, off);
-        if (ov > v || (ov == v && oi < idx)) {
-            v = ov;
-            idx = oi;
-        }
-    }
-    __syncthreads();
-    if (lane == 0) {
-        sv[warp] = v;
-        si[warp] = idx;
-    }
-    __syncthreads();
-    best = sv[0];
-    bi = si[0];
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
-        if (sv[w] > best || (sv[w] == best && si[w] < bi)) {
-            best = sv[w];
-            bi = si[w];
-        }
-}
+// tile J (I < J) the interaction matrix T_ji = m_ji cos_scat cos_inc G(r_ji)
+// (weights excluded; m_ji = 1 for class ALL, the inline cosine gates for
+// CLEAR, the stored mask bit for BITS) is approximated by U V^T, U: 256 x k
+// over the rows j of J, V: 256 x k over the columns i of I, by adaptive cross
+// approximation with partial pivoting: each step takes the residual row at a
+// pivot row, its largest entry as pivot column, the residual column there,
+// and stops when |u_k| |v_k| falls below tol times the running Frobenius
+// estimate.  Residual rows that vanish (rows the mask zeroes) are skipped.
+// The forward terms are then U (V^T w_I) into J and the reciprocal ones
+// V (U^T w_J) into I.  Factors of block b start at column off[b] (in 256-entry
+// columns) of the U and V arrays; cap[b] columns are reserved.
 
 __device__ __forceinline__ float block_sum(float v, float *sv)
 {
@@ -1235,198 +1211,429 @@ __device__ __forceinline__ float block_sum(float v, float *sv)
     return t;
 }
 
-// T(j, i) of one pair from staged fragments (pos.xyz, normal.xyz)
+// T(j, i) of one pair of a block of class cls (bit: the pair's mask bit for BITS)
 template <bool ATT>
-__device__ __forceinline__ float2 t_entry(const SumArgs &a, float4 pi, float4 ni, float4 pj, float4 nj)
+__device__ __forceinline__ float2 lr_entry(const SumArgs &a, int cls, bool bit, float4 pi, float4 ni, float4 pj,
+                                           float4 nj)
 {
-    Dst d{pj.x, pj.y, pj.z, nj.x, nj.y, nj.z};
+    const Dst d{pj.x, pj.y, pj.z, nj.x, nj.y, nj.z};
     float Tr, Ti;
     bool ok;
-    sym_pair<ATT, false, true>(a, pi, ni, d, Tr, Ti, ok);
-    return make_float2(Tr, Ti);
+    if (cls == kFlagClear) {
+        sym_pair<ATT, true, true>(a, pi, ni, d, Tr, Ti, ok);
+    } else {
+        sym_pair<ATT, false, true>(a, pi, ni, d, Tr, Ti, ok);
+        ok = cls == kFlagAll || bit;
+    }
+    return ok ? make_float2(Tr, Ti) : make_float2(0.0f, 0.0f);
 }
 
-template <bool ATT>
-__global__ void __launch_bounds__(kTile) k_aca(SumArgs a, const int2 *blocks, int nblocks, int rmax, float tol,
-                                               float2 *U, float2 *V, int *rank, float *fro)
+__device__ __forceinline__ float2 cmul(float2 x, float2 y)
 {
-    __shared__ float4 sPI[kTile], sNI[kTile], sPJ[kTile], sNJ[kTile];
-    __shared__ float sv[kTile / 32];
-    __shared__ int si[kTile / 32];
-    __shared__ unsigned char used[kTile];
-    const int b = blockIdx.x;
-    if (b >= nblocks) return;
-    const int I = blocks[b].x, J = blocks[b].y, t = threadIdx.x;
-    const int i = I * kTile + t, j = J * kTile + t;
-    const bool vi = i < a.nsrc, vj = j < a.nsrc;
-    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    sPI[t] = vi ? a.srcA[i] : z;
-    sNI[t] = vi ? a.srcB[i] : z;
-    sPJ[t] = vj ? a.srcA[j] : z;
-    sNJ[t] = vj ? a.srcB[j] : z;
-    used[t] = vj ? 0 : 1;
-    __syncthreads();
-    float2 *Ub = U + (size_t)b * rmax * kTile, *Vb = V + (size_t)b * rmax * kTile;
-    int r = 0;  // first pivot row
-    float norm2 = 0.0f;
-    int k = 0;
-    for (int l = 0; l < rmax; ++l) {
-        // residual row r over the columns (thread t = column i)
-        float2 val = vi ? t_entry<ATT>(a, sPI[t], sNI[t], sPJ[r], sNJ[r]) : make_float2(0.0f, 0.0f);
-        for (int m = 0; m < l; ++m) {
-            const float2 u = Ub[m * kTile + r], v = Vb[m * kTile + t];
-            val.x -= u.x * v.x - u.y * v.y;
-            val.y -= u.x * v.y + u.y * v.x;
+    return make_float2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
+}
+
+// warp-wide argmax of v (ties: lowest index)
+__device__ __forceinline__ void warp_argmax(float &v, int &idx)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, v, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, idx, off);
+        if (ov > v || (ov == v && oi < idx)) {
+            v = ov;
+            idx = oi;
         }
-        float best;
-        int c;
-        block_argmax(vi ? val.x * val.x + val.y * val.y : -1.0f, t, sv, si, best, c);
-        if (!(best > 1e-30f)) break;  // the residual row vanished
-        // pivot value, broadcast through shared memory
-        __shared__ float2 piv;
-        if (t == c) piv = val;
-        __syncthreads();
-        const float2 dl = piv;
-        const float inv = 1.0f / (dl.x * dl.x + dl.y * dl.y);
-        const float2 vv = make_float2((val.x * dl.x + val.y * dl.y) * inv, (val.y * dl.x - val.x * dl.y) * inv);
-        Vb[l * kTile + t] = vv;
-        // residual column c over the rows (thread t = row j)
-        float2 u = vj ? t_entry<ATT>(a, sPI[c], sNI[c], sPJ[t], sNJ[t]) : make_float2(0.0f, 0.0f);
-        __syncthreads();  // Vb[l] complete before it is read below
-        for (int m = 0; m < l; ++m) {
-            const float2 um = Ub[m * kTile + t], vm = Vb[m * kTile + c];
-            u.x -= um.x * vm.x - um.y * vm.y;
-            u.y -= um.x * vm.y + um.y * vm.x;
-        }
-        Ub[l * kTile + t] = u;
-        const float nu2 = block_sum(u.x * u.x + u.y * u.y, sv);
-        const float nv2 = block_sum(vv.x * vv.x + vv.y * vv.y, sv);
-        norm2 += nu2 * nv2;
-        k = l + 1;
-        if (nu2 * nv2 <= tol * tol * norm2) break;
-        if (t == r) used[r] = 1;
-        __syncthreads();
-        block_argmax((vj && !used[t]) ? u.x * u.x + u.y * u.y : -1.0f, t, sv, si, best, r);
-        if (best < 0.0f) break;  // every row used
-        __syncthreads();
     }
-    if (t == 0) {
+}
+
+constexpr int kAcaWarps = 4;
+constexpr size_t kAcaSmem = sizeof(float4) * 4 * kTile * kAcaWarps;
+constexpr int kAcaMaxZeroRows = 48;
+
+// One warp per block; lane l owns columns (and rows) l + 32 q, q = 0..7.
+template <bool ATT>
+__global__ void __launch_bounds__(32 * kAcaWarps) k_aca(SumArgs a, const int2 *blocks, const uint8_t *cls,
+                                                        const int *cap, const long long *off, int nblocks, float tol,
+                                                        float2 *U, float2 *V, int *rank, float *fro)
+{
+    extern __shared__ float4 sAca[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.x * kAcaWarps + warp;
+    if (b >= nblocks) return;  // warp-uniform; no CTA barrier follows
+    float4 *PI = sAca + warp * 4 * kTile, *NI = PI + kTile, *PJ = NI + kTile, *NJ = PJ + kTile;
+    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = cap[b];
+    const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
+    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int t = lane + 32 * q;
+        PI[t] = t < ni ? a.srcA[I * kTile + t] : z;
+        NI[t] = t < ni ? a.srcB[I * kTile + t] : z;
+        PJ[t] = t < nj ? a.srcA[J * kTile + t] : z;
+        NJ[t] = t < nj ? a.srcB[J * kTile + t] : z;
+    }
+    __syncwarp();
+    float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
+    // mask word w of destination row j: bw[w * pitch + j]
+    const uint32_t *bw = a.mask.bits + (long long)I * kWordsPerTile * a.mask.pitch + (long long)J * kTile;
+    unsigned used = 0u;  // bit q: row lane + 32 q taken (or absent)
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        if (lane + 32 * q >= nj) used |= 1u << q;
+    int r = 0, k = 0, zero_rows = 0;
+    float norm2 = 0.0f;
+    while (k < K) {
+        // ---- residual row r over the columns
+        float2 val[8];
+        const float4 pr = PJ[r], nr = NJ[r];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int i = lane + 32 * q;
+            const bool bit =
+                bc == kFlagBits && i < ni ? ((bw[(long long)q * a.mask.pitch + r] >> lane) & 1u) : true;
+            val[q] = i < ni ? lr_entry<ATT>(a, bc, bit, PI[i], NI[i], pr, nr) : make_float2(0.0f, 0.0f);
+        }
+        for (int m = 0; m < k; ++m) {
+            const float2 u = Ub[m * kTile + r];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float2 v = Vb[m * kTile + lane + 32 * q];
+                val[q].x -= u.x * v.x - u.y * v.y;
+                val[q].y -= u.x * v.y + u.y * v.x;
+            }
+        }
+        float best = -1.0f;
+        int c = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int i = lane + 32 * q;
+            const float m2 = i < ni ? val[q].x * val[q].x + val[q].y * val[q].y : -1.0f;
+            if (m2 > best) {
+                best = m2;
+                c = i;
+            }
+        }
+        warp_argmax(best, c);
+        if (!(best > 1e-30f)) {
+            // the residual row vanished: take the next unused row instead
+            if ((r & 31) == lane) used |= 1u << (r >> 5);
+            if (++zero_rows > kAcaMaxZeroRows) break;
+            int nr_ = 1 << 30;
+#pragma unroll
+            for (int q = 7; q >= 0; --q)
+                if (!((used >> q) & 1u)) nr_ = lane + 32 * q;
+#pragma unroll
+            for (int off2 = 16; off2 > 0; off2 >>= 1) nr_ = min(nr_, __shfl_xor_sync(0xffffffffu, nr_, off2));
+            if (nr_ >= kTile) break;
+            r = nr_;
+            continue;
+        }
+        // pivot value from the owner lane of column c
+        float2 pv = val[0];
+#pragma unroll
+        for (int q = 1; q < 8; ++q)
+            if ((c >> 5) == q) pv = val[q];
+        pv.x = __shfl_sync(0xffffffffu, pv.x, c & 31);
+        pv.y = __shfl_sync(0xffffffffu, pv.y, c & 31);
+        const float inv = 1.0f / (pv.x * pv.x + pv.y * pv.y);
+        float nv2 = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float2 vv = make_float2((val[q].x * pv.x + val[q].y * pv.y) * inv,
+                                          (val[q].y * pv.x - val[q].x * pv.y) * inv);
+            Vb[k * kTile + lane + 32 * q] = vv;
+            nv2 += vv.x * vv.x + vv.y * vv.y;
+        }
+        // ---- residual column c over the rows
+        const float4 pc = PI[c], nc = NI[c];
+        const uint32_t *cw = bw + (long long)(c >> 5) * a.mask.pitch;
+        float2 uu[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int j = lane + 32 * q;
+            const bool bit = bc == kFlagBits && j < nj ? ((cw[j] >> (c & 31)) & 1u) : true;
+            uu[q] = j < nj ? lr_entry<ATT>(a, bc, bit, pc, nc, PJ[j], NJ[j]) : make_float2(0.0f, 0.0f);
+        }
+        for (int m = 0; m < k; ++m) {
+            const float2 vc = Vb[m * kTile + c];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float2 um = Ub[m * kTile + lane + 32 * q];
+                uu[q].x -= um.x * vc.x - um.y * vc.y;
+                uu[q].y -= um.x * vc.y + um.y * vc.x;
+            }
+        }
+        float nu2 = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            Ub[k * kTile + lane + 32 * q] = uu[q];
+            nu2 += uu[q].x * uu[q].x + uu[q].y * uu[q].y;
+        }
+        nu2 = warp_sum(nu2);
+        nv2 = warp_sum(nv2);
+        norm2 += nu2 * nv2;
+        ++k;
+        __syncwarp();  // U and V column k-1 visible to every lane
+        if (nu2 * nv2 <= tol * tol * norm2) break;
+        if ((r & 31) == lane) used |= 1u << (r >> 5);
+        // next pivot row: largest residual-column entry among unused rows
+        best = -1.0f;
+        int nr_ = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float m2 = ((used >> q) & 1u) ? -1.0f : uu[q].x * uu[q].x + uu[q].y * uu[q].y;
+            if (m2 > best) {
+                best = m2;
+                nr_ = lane + 32 * q;
+            }
+        }
+        warp_argmax(best, nr_);
+        if (best < 0.0f) break;  // every row taken
+        r = nr_;
+    }
+    if (lane == 0) {
         rank[b] = k;
         fro[b] = sqrtf(norm2);
     }
 }
 
-// The exact tile judges its approximation: 64 sampled entries per block,
-// relative RMS error against the block's RMS entry; blocks above the limit
-// (or not converged) get rank -1 and stay dense.
+// The exact entries judge each approximation: 512 sampled entries per block
+// (every row once at a hashed column, every column once at a hashed row),
+// relative RMS error against the sampled entries' RMS; blocks above the
+// limit, not converged within their cap, or of rank 0 get rank -1 and stay
+// dense.
 template <bool ATT>
-__global__ void __launch_bounds__(64) k_aca_judge(SumArgs a, const int2 *blocks, int nblocks, int rmax, float limit,
-                                                  const float2 *U, const float2 *V, int *rank, const float *fro,
-                                                  float *err_out)
+__global__ void __launch_bounds__(kTile) k_aca_judge(SumArgs a, const int2 *blocks, const uint8_t *cls,
+                                                     const int *cap, const long long *off, int nblocks, float limit,
+                                                     const float2 *U, const float2 *V, int *rank, float *err_out)
 {
-    __shared__ float sv[2];
+    __shared__ float sv[kTile / 32];
     const int b = blockIdx.x;
     if (b >= nblocks) return;
     const int k = rank[b];
-    const int I = blocks[b].x, J = blocks[b].y, t = threadIdx.x;
-    // deterministic sample: rows and columns from a hash of (block, sample)
-    unsigned h = (unsigned)b * 2654435761u + (unsigned)t * 40503u + 12345u;
-    h ^= h >> 13; h *= 0x5bd1e995u; h ^= h >> 15;
-    int ci = (int)(h & 255u), rj = (int)((h >> 8) & 255u);
-    const int i = I * kTile + ci, j = J * kTile + rj;
-    float e2 = 0.0f;
-    if (k > 0 && i < a.nsrc && j < a.nsrc) {
-        const float2 ex = t_entry<ATT>(a, a.srcA[i], a.srcB[i], a.srcA[j], a.srcB[j]);
-        float ar = 0.0f, ai = 0.0f;
-        const float2 *Ub = U + (size_t)b * rmax * kTile, *Vb = V + (size_t)b * rmax * kTile;
-        for (int m = 0; m < k; ++m) {
-            const float2 u = Ub[m * kTile + rj], v = Vb[m * kTile + ci];
-            ar += u.x * v.x - u.y * v.y;
-            ai += u.x * v.y + u.y * v.x;
+    if (k <= 0 || k >= cap[b]) {  // block-uniform
+        if (threadIdx.x == 0) {
+            rank[b] = -1;
+            err_out[b] = -1.0f;
         }
-        e2 = (ex.x - ar) * (ex.x - ar) + (ex.y - ai) * (ex.y - ai);
+        return;
     }
-    float s = e2;
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-    if ((t & 31) == 0) sv[t >> 5] = s;
-    __syncthreads();
+    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], t = threadIdx.x;
+    const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
+    const float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
+    const uint32_t *bw = a.mask.bits + (long long)I * kWordsPerTile * a.mask.pitch + (long long)J * kTile;
+    float e2 = 0.0f, x2 = 0.0f;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        unsigned h = (unsigned)b * 2654435761u + (unsigned)(t + 256 * s) * 40503u + 12345u;
+        h ^= h >> 13;
+        h *= 0x5bd1e995u;
+        h ^= h >> 15;
+        const int jj = s == 0 ? t : (int)(h & 255u), ii = s == 0 ? (int)(h & 255u) : t;
+        if (ii < ni && jj < nj) {
+            const bool bit = bc == kFlagBits ? ((bw[(long long)(ii >> 5) * a.mask.pitch + jj] >> (ii & 31)) & 1u) : true;
+            const float2 ex = lr_entry<ATT>(a, bc, bit, a.srcA[I * kTile + ii], a.srcB[I * kTile + ii],
+                                            a.srcA[J * kTile + jj], a.srcB[J * kTile + jj]);
+            float ar = 0.0f, ai = 0.0f;
+            for (int m = 0; m < k; ++m) {
+                const float2 u = Ub[m * kTile + jj], v = Vb[m * kTile + ii];
+                ar += u.x * v.x - u.y * v.y;
+                ai += u.x * v.y + u.y * v.x;
+            }
+            e2 += (ex.x - ar) * (ex.x - ar) + (ex.y - ai) * (ex.y - ai);
+            x2 += ex.x * ex.x + ex.y * ex.y;
+        }
+    }
+    const float se = block_sum(e2, sv);
+    const float sx = block_sum(x2, sv);
     if (t == 0) {
-        const float rms_err = sqrtf((sv[0] + sv[1]) / 64.0f);
-        const float rms_ent = fro[b] / (float)kTile;
-        err_out[b] = rms_ent > 0.0f ? rms_err / rms_ent : 0.0f;
-        if (k <= 0 || k >= rmax || !(rms_err <= limit * rms_ent)) rank[b] = -1;
+        const float rel = sx > 0.0f ? sqrtf(se / sx) : (se > 0.0f ? 1.0f : 0.0f);
+        err_out[b] = rel;
+        if (!(rel <= limit)) rank[b] = -1;
     }
 }
 
-// Stage 1 of the compressed bounce: per block, tv = V^T w_I and su = U^T w_J
-// (k complex values each).
-__global__ void __launch_bounds__(kTile) k_lr_project(SumArgs a, const int2 *blocks, const int *bidx, int nb,
-                                                      int rmax, const float2 *U, const float2 *V, const int *rank,
-                                                      float2 *tv, float2 *su)
+// Block descriptors of the admissibility network, one warp per block:
+// log2(1 + separation / lambda), log2(1 + radius / lambda) of both tiles, the
+// cosines of both mean normals with the separation direction and with each
+// other, (r_I + r_J) / separation (at most 4) and the fraction of the block's
+// pairs that interact (1 for ALL, the stored bits for BITS, 256 sampled gate
+// pairs for CLEAR).
+__global__ void __launch_bounds__(128) k_block_desc(SumArgs a, const int2 *blocks, const uint8_t *cls, int nblocks,
+                                                    const float4 *cen, const float4 *nm, float inv_lambda, float *X)
 {
-    __shared__ float sv[kTile / 32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.x * 4 + warp;
+    if (b >= nblocks) return;
+    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b];
+    const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
+    float vis = 1.0f;
+    if (bc == kFlagBits) {
+        const uint32_t *bw = a.mask.bits + (long long)I * kWordsPerTile * a.mask.pitch + (long long)J * kTile;
+        const int nw = (ni + 31) >> 5;
+        int cnt = 0;
+        for (int w = 0; w < nw; ++w)
+            for (int j = lane; j < nj; j += 32) cnt += __popc(bw[(long long)w * a.mask.pitch + j]);
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        vis = (float)cnt / (float)(ni * nj);
+    } else if (bc == kFlagClear) {
+        int cnt = 0;
+        for (int q = 0; q < 8; ++q) {
+            const int s = lane + 32 * q;
+            unsigned h = (unsigned)b * 2654435761u + (unsigned)s * 40503u + 777u;
+            h ^= h >> 13;
+            h *= 0x5bd1e995u;
+            h ^= h >> 15;
+            const int ii = (int)(h & 255u) % ni, jj = (int)((h >> 8) & 255u) % nj;
+            const float4 pi = a.srcA[I * kTile + ii], qi = a.srcB[I * kTile + ii];
+            const float4 pj = a.srcA[J * kTile + jj], qj = a.srcB[J * kTile + jj];
+            const Dst d{pj.x, pj.y, pj.z, qj.x, qj.y, qj.z};
+            float Tr, Ti;
+            bool ok;
+            sym_pair<false, true, false>(a, pi, qi, d, Tr, Ti, ok);
+            cnt += ok ? 1 : 0;
+        }
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        vis = (float)cnt / 256.0f;
+    }
+    if (lane == 0) {
+        const float4 cI = cen[I], cJ = cen[J], nI = nm[I], nJ = nm[J];
+        const float sx = cJ.x - cI.x, sy = cJ.y - cI.y, sz = cJ.z - cI.z;
+        const float sep = sqrtf(sx * sx + sy * sy + sz * sz);
+        const float is = sep > 0.0f ? 1.0f / sep : 0.0f;
+        float *x = X + (size_t)b * 8;
+        x[0] = log2f(1.0f + sep * inv_lambda);
+        x[1] = log2f(1.0f + cI.w * inv_lambda);
+        x[2] = log2f(1.0f + cJ.w * inv_lambda);
+        x[3] = (nI.x * sx + nI.y * sy + nI.z * sz) * is;
+        x[4] = (nJ.x * sx + nJ.y * sy + nJ.z * sz) * is;
+        x[5] = nI.x * nJ.x + nI.y * nJ.y + nI.z * nJ.z;
+        x[6] = sep > 0.0f ? fminf((cI.w + cJ.w) * is, 4.0f) : 4.0f;
+        x[7] = vis;
+    }
+}
+
+constexpr int kLrMaxRank = 64;
+
+// Stage 1 of the compressed bounce: per block, tv = V^T w_I and su = U^T w_J
+// (k complex values each); warp partial sums, one barrier.
+__global__ void __launch_bounds__(kTile) k_lr_project(SumArgs a, const int2 *blocks, const long long *off,
+                                                      const int *bidx, int nb, const float2 *U, const float2 *V,
+                                                      const int *rank, float2 *tv, float2 *su)
+{
+    __shared__ float4 sRed[kTile / 32][kLrMaxRank];
     const int q = blockIdx.x;
     if (q >= nb) return;
     const int b = bidx[q];
     const int k = rank[b];
-    const int I = blocks[b].x, J = blocks[b].y, t = threadIdx.x;
+    const int I = blocks[b].x, J = blocks[b].y, t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int i = I * kTile + t, j = J * kTile + t;
     const float wir = i < a.nsrc ? a.srcA[i].w : 0.0f, wii = i < a.nsrc ? a.srcB[i].w : 0.0f;
     const float wjr = j < a.nsrc ? a.srcA[j].w : 0.0f, wji = j < a.nsrc ? a.srcB[j].w : 0.0f;
-    const float2 *Ub = U + (size_t)b * rmax * kTile, *Vb = V + (size_t)b * rmax * kTile;
+    const float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
     for (int m = 0; m < k; ++m) {
         const float2 v = Vb[m * kTile + t], u = Ub[m * kTile + t];
-        const float tr = block_sum(v.x * wir - v.y * wii, sv);
-        const float ti = block_sum(v.x * wii + v.y * wir, sv);
-        const float sr = block_sum(u.x * wjr - u.y * wji, sv);
-        const float sim = block_sum(u.x * wji + u.y * wjr, sv);
-        if (t == 0) {
-            tv[(size_t)b * rmax + m] = make_float2(tr, ti);
-            su[(size_t)b * rmax + m] = make_float2(sr, sim);
+        float4 p = make_float4(v.x * wir - v.y * wii, v.x * wii + v.y * wir, u.x * wjr - u.y * wji,
+                               u.x * wji + u.y * wjr);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            p.x += __shfl_xor_sync(0xffffffffu, p.x, o);
+            p.y += __shfl_xor_sync(0xffffffffu, p.y, o);
+            p.z += __shfl_xor_sync(0xffffffffu, p.z, o);
+            p.w += __shfl_xor_sync(0xffffffffu, p.w, o);
         }
+        if (lane == 0) sRed[warp][m] = p;
+    }
+    __syncthreads();
+    if (t < k) {
+        float4 s = sRed[0][t];
+#pragma unroll
+        for (int w = 1; w < kTile / 32; ++w) {
+            const float4 p = sRed[w][t];
+            s.x += p.x;
+            s.y += p.y;
+            s.z += p.z;
+            s.w += p.w;
+        }
+        tv[off[b] + t] = make_float2(s.x, s.y);
+        su[off[b] + t] = make_float2(s.z, s.w);
     }
 }
 
 // Stage 2: per owner tile X, rows of every block with J = X (forward) and
-// columns of every block with I = X (reciprocal), in list order
-// (deterministic).  Results in FP64 per fragment.
-__global__ void __launch_bounds__(kTile) k_lr_expand(int n, int rmax, const float2 *U, const float2 *V, const int *rank,
-                                                     const float2 *tv, const float2 *su, const int *byJ_off,
-                                                     const int *byJ, const int *byI_off, const int *byI,
-                                                     double2 *yrow, double2 *ycol)
+// columns of every block with I = X (reciprocal).  Four groups of 256 threads
+// take the owner's blocks round-robin; the group sums combine in a fixed
+// order (deterministic).  Results in FP64 per fragment.
+constexpr int kLrGroups = 4;
+__global__ void __launch_bounds__(kTile * kLrGroups) k_lr_expand(int n, const long long *off, const float2 *U,
+                                                                 const float2 *V, const int *rank, const float2 *tv,
+                                                                 const float2 *su, const int *byJ_off, const int *byJ,
+                                                                 const int *byI_off, const int *byI, double2 *yrow,
+                                                                 double2 *ycol)
 {
-    const int X = blockIdx.x, t = threadIdx.x;
+    __shared__ double2 sR[kLrGroups][kTile], sC[kLrGroups][kTile];
+    const int X = blockIdx.x, g = threadIdx.x / kTile, t = threadIdx.x % kTile;
     const int q = X * kTile + t;
     double fr = 0.0, fi = 0.0, cr = 0.0, ci = 0.0;
-    for (int p = byJ_off[X]; p < byJ_off[X + 1]; ++p) {
+    for (int p = byJ_off[X] + g; p < byJ_off[X + 1]; p += kLrGroups) {
         const int b = byJ[p];
         const int k = rank[b];
-        const float2 *Ub = U + (size_t)b * rmax * kTile;
-        float ar = 0.0f, ai = 0.0f;
-        for (int m = 0; m < k; ++m) {
-            const float2 u = Ub[m * kTile + t], c = tv[(size_t)b * rmax + m];
-            ar += u.x * c.x - u.y * c.y;
-            ai += u.x * c.y + u.y * c.x;
+        const float2 *Ub = U + off[b] * kTile + t;
+        const float2 *c = tv + off[b];
+        float ar = 0.0f, ai = 0.0f, br = 0.0f, bi = 0.0f;
+        int m = 0;
+        for (; m + 1 < k; m += 2) {
+            const float2 u0 = Ub[m * kTile], u1 = Ub[(m + 1) * kTile], c0 = c[m], c1 = c[m + 1];
+            ar += u0.x * c0.x - u0.y * c0.y;
+            ai += u0.x * c0.y + u0.y * c0.x;
+            br += u1.x * c1.x - u1.y * c1.y;
+            bi += u1.x * c1.y + u1.y * c1.x;
         }
-        fr += ar;
-        fi += ai;
+        if (m < k) {
+            const float2 u0 = Ub[m * kTile], c0 = c[m];
+            ar += u0.x * c0.x - u0.y * c0.y;
+            ai += u0.x * c0.y + u0.y * c0.x;
+        }
+        fr += (double)(ar + br);
+        fi += (double)(ai + bi);
     }
-    for (int p = byI_off[X]; p < byI_off[X + 1]; ++p) {
+    for (int p = byI_off[X] + g; p < byI_off[X + 1]; p += kLrGroups) {
         const int b = byI[p];
         const int k = rank[b];
-        const float2 *Vb = V + (size_t)b * rmax * kTile;
-        float ar = 0.0f, ai = 0.0f;
-        for (int m = 0; m < k; ++m) {
-            const float2 v = Vb[m * kTile + t], c = su[(size_t)b * rmax + m];
-            ar += v.x * c.x - v.y * c.y;
-            ai += v.x * c.y + v.y * c.x;
+        const float2 *Vb = V + off[b] * kTile + t;
+        const float2 *c = su + off[b];
+        float ar = 0.0f, ai = 0.0f, br = 0.0f, bi = 0.0f;
+        int m = 0;
+        for (; m + 1 < k; m += 2) {
+            const float2 v0 = Vb[m * kTile], v1 = Vb[(m + 1) * kTile], c0 = c[m], c1 = c[m + 1];
+            ar += v0.x * c0.x - v0.y * c0.y;
+            ai += v0.x * c0.y + v0.y * c0.x;
+            br += v1.x * c1.x - v1.y * c1.y;
+            bi += v1.x * c1.y + v1.y * c1.x;
         }
-        cr += ar;
-        ci += ai;
+        if (m < k) {
+            const float2 v0 = Vb[m * kTile], c0 = c[m];
+            ar += v0.x * c0.x - v0.y * c0.y;
+            ai += v0.x * c0.y + v0.y * c0.x;
+        }
+        cr += (double)(ar + br);
+        ci += (double)(ai + bi);
     }
-    if (q < n) {
-        yrow[q] = make_double2(fr, fi);
-        ycol[q] = make_double2(cr, ci);
+    sR[g][t] = make_double2(fr, fi);
+    sC[g][t] = make_double2(cr, ci);
+    __syncthreads();
+    if (g == 0 && q < n) {
+        double2 R = sR[0][t], Cc = sC[0][t];
+#pragma unroll
+        for (int h = 1; h < kLrGroups; ++h) {
+            R.x += sR[h][t].x;
+            R.y += sR[h][t].y;
+            Cc.x += sC[h][t].x;
+            Cc.y += sC[h][t].y;
+        }
+        yrow[q] = R;
+        ycol[q] = Cc;
     }
 }
 
@@ -1673,27 +1880,43 @@ void launch_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const
                                                                  Pout, P, yrow, ycol);
 }
 
-void launch_aca(const SumArgs &a, const int2 *blocks, int nblocks, int rmax, float tol, float2 *U, float2 *V,
-                int *rank, float *fro, float limit, float *err, cudaStream_t s)
+void launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
+                int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
+                cudaStream_t s)
 {
     if (nblocks <= 0) return;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_aca<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAcaSmem);
+        cudaFuncSetAttribute(k_aca<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAcaSmem);
+        attr = true;
+    }
+    const unsigned grid = (unsigned)((nblocks + kAcaWarps - 1) / kAcaWarps);
     if (a.ka != 0.0f) {
-        k_aca<true><<<nblocks, kTile, 0, s>>>(a, blocks, nblocks, rmax, tol, U, V, rank, fro);
-        k_aca_judge<true><<<nblocks, 64, 0, s>>>(a, blocks, nblocks, rmax, limit, U, V, rank, fro, err);
+        k_aca<true><<<grid, 32 * kAcaWarps, kAcaSmem, s>>>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro);
+        k_aca_judge<true><<<nblocks, kTile, 0, s>>>(a, blocks, cls, cap, off, nblocks, limit, U, V, rank, err);
     } else {
-        k_aca<false><<<nblocks, kTile, 0, s>>>(a, blocks, nblocks, rmax, tol, U, V, rank, fro);
-        k_aca_judge<false><<<nblocks, 64, 0, s>>>(a, blocks, nblocks, rmax, limit, U, V, rank, fro, err);
+        k_aca<false><<<grid, 32 * kAcaWarps, kAcaSmem, s>>>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro);
+        k_aca_judge<false><<<nblocks, kTile, 0, s>>>(a, blocks, cls, cap, off, nblocks, limit, U, V, rank, err);
     }
 }
 
-void launch_lr_apply(const SumArgs &a, const int2 *blocks, const int *bidx, int nb, int rmax, const float2 *U,
-                     const float2 *V, const int *rank, float2 *tv, float2 *su, int ntiles, const int *byJ_off,
-                     const int *byJ, const int *byI_off, const int *byI, double2 *yrow, double2 *ycol, cudaStream_t s)
+void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
+                       const float4 *nm, float inv_lambda, float *X, cudaStream_t s)
 {
-    if (nb > 0) k_lr_project<<<nb, kTile, 0, s>>>(a, blocks, bidx, nb, rmax, U, V, rank, tv, su);
+    if (nblocks > 0)
+        k_block_desc<<<(nblocks + 3) / 4, 128, 0, s>>>(a, blocks, cls, nblocks, cen, nm, inv_lambda, X);
+}
+
+void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
+                     const float2 *U, const float2 *V, const int *rank, float2 *tv, float2 *su, int ntiles,
+                     const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
+                     double2 *ycol, cudaStream_t s)
+{
+    if (nb > 0) k_lr_project<<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, tv, su);
     if (ntiles > 0)
-        k_lr_expand<<<ntiles, kTile, 0, s>>>(a.nsrc, rmax, U, V, rank, tv, su, byJ_off, byJ, byI_off, byI, yrow,
-                                             ycol);
+        k_lr_expand<<<ntiles, kTile * kLrGroups, 0, s>>>(a.nsrc, off, U, V, rank, tv, su, byJ_off, byJ, byI_off, byI,
+                                                         yrow, ycol);
 }
 
 void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s)

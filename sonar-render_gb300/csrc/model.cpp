@@ -116,19 +116,31 @@ struct Compression {
     bool valid = false;
     int obj = -1;
     double kr = 0.0, ki = 0.0;
-    int nblocks = 0, naccepted = 0, rmax = 0;
+    int select = 0;             // 0 rule, 1 exhaustive, 2 network
+    int rmax = 0;
+    int ncand = 0;              // candidate blocks before selection
+    int nblocks = 0;            // blocks approximated (after selection)
+    int naccepted = 0;
     double mean_rank = 0.0, max_err = 0.0;
-    float build_ms = 0.0f;
+    double pairs_cmp = 0.0;     // ordered pairs of the accepted blocks
+    float build_ms = 0.0f, select_ms = 0.0f, aca_ms = 0.0f;
+    long long ncols = 0;        // factor columns reserved (sum of caps)
     int2 *d_blocks = nullptr;
+    uint8_t *d_cls = nullptr;
+    int *d_cap = nullptr;
+    long long *d_off = nullptr;
     float2 *d_U = nullptr, *d_V = nullptr, *d_tv = nullptr, *d_su = nullptr;
     int *d_rank = nullptr, *d_bidx = nullptr;
     float *d_fro = nullptr, *d_err = nullptr;
     int *d_byJ_off = nullptr, *d_byJ = nullptr, *d_byI_off = nullptr, *d_byI = nullptr;
     uint8_t *d_flags = nullptr;  // the mask flags with accepted blocks removed (dense kernel)
     double2 *d_yrow = nullptr, *d_ycol = nullptr;
+    // descriptors and rank labels of the approximated blocks (network training)
+    std::vector<float> desc, label;
     void release()
     {
-        dfree(d_blocks); dfree(d_U); dfree(d_V); dfree(d_tv); dfree(d_su); dfree(d_rank); dfree(d_bidx);
+        dfree(d_blocks); dfree(d_cls); dfree(d_cap); dfree(d_off);
+        dfree(d_U); dfree(d_V); dfree(d_tv); dfree(d_su); dfree(d_rank); dfree(d_bidx);
         dfree(d_fro); dfree(d_err); dfree(d_byJ_off); dfree(d_byJ); dfree(d_byI_off); dfree(d_byI);
         dfree(d_flags); dfree(d_yrow); dfree(d_ycol);
         valid = false;
@@ -144,9 +156,9 @@ struct HopRecord {
     int nsplit;
     int launches;    // kernels launched by this hop, mask included
     // compressed bounce blocks (FACET_SELF with compression on)
-    int cmp_blocks = 0, cmp_accepted = 0;
-    double cmp_mean_rank = 0.0, cmp_max_err = 0.0;
-    float cmp_build_ms = 0.0f, lr_ms = 0.0f;
+    int cmp_cand = 0, cmp_blocks = 0, cmp_accepted = 0, cmp_select = 0;
+    double cmp_mean_rank = 0.0, cmp_max_err = 0.0, cmp_pairs = 0.0;
+    float cmp_build_ms = 0.0f, cmp_select_ms = 0.0f, cmp_aca_ms = 0.0f, lr_ms = 0.0f;
 };
 
 struct Model {
@@ -162,6 +174,7 @@ struct Model {
     // device
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr, ev4 = nullptr, ev5 = nullptr;
+    cudaEvent_t ev6 = nullptr, ev7 = nullptr, ev8 = nullptr;
     float4 *d_src_pos = nullptr, *d_fp_pos = nullptr;
     double2 *d_src_P = nullptr, *d_fp_P = nullptr;
     // field points are kept in Morton (spatial) order on the device so that a
@@ -189,6 +202,8 @@ struct Model {
     int opt_compress = 0;
     float opt_cmp_tol = 1e-4f, opt_cmp_judge = 3e-4f, opt_cmp_eta = 1.0f;
     int opt_cmp_rmax = 32;
+    int opt_cmp_select = 0;     // 0 rule (class ALL, eta-separated), 1 every interacting block, 2 the network
+    float opt_cmp_rcut = 24.0f; // network: propose blocks whose predicted rank is below this
     Compression cmp;
     std::vector<HopRecord> log;
     long long launches = 0, h2d_bytes = 0, d2h_bytes = 0;
@@ -207,7 +222,7 @@ struct Model {
         cmp.release();
         dfree(d_packA); dfree(d_packB); dfree(d_partial); dfree(d_limit); dfree(d_colpart);
         pack_cap = partial_cap = limit_cap = colpart_cap = 0;
-        for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3, &ev4, &ev5})
+        for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3, &ev4, &ev5, &ev6, &ev7, &ev8})
             if (*e) {
                 cudaEventDestroy(*e);
                 *e = nullptr;
@@ -357,7 +372,7 @@ void render()
 {
     if (g.rendered) fail(-2, "render_cuda called twice without TearDownCuda");
     CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
-    for (cudaEvent_t *e : {&g.ev0, &g.ev1, &g.ev2, &g.ev3, &g.ev4, &g.ev5}) CK(cudaEventCreate(e));
+    for (cudaEvent_t *e : {&g.ev0, &g.ev1, &g.ev2, &g.ev3, &g.ev4, &g.ev5, &g.ev6, &g.ev7, &g.ev8}) CK(cudaEventCreate(e));
     for (int t : {OBJ_TARGET, OBJ_FIELD})
         for (auto &o : g.obj[t]) render_object(*o);
     // occluders: every triangle of every target object (OptiX.cpp:264-296)
@@ -550,97 +565,181 @@ void ensure_colpart(int ntiles)
     }
 }
 
-// Choose and compress the admissible blocks of a FACET_SELF hop: upper
-// blocks (I < J) whose every pair interacts (mask class ALL) and whose tile
-// centroids are farther apart than eta (r_I + r_J).  Every candidate is
-// compressed by adaptive cross approximation (rank cap rmax, tolerance tol)
-// and judged on sampled exact entries; accepted blocks leave the dense
-// kernel's flags.
+// Choose and compress blocks of a FACET_SELF hop (upper blocks I < J).
+// Candidates: with the rule (select 0), blocks whose every pair interacts
+// (mask class ALL) and whose tile centroids are farther apart than
+// eta (r_I + r_J); otherwise every interacting off-diagonal block.  With the
+// network (select 2) each candidate's descriptors go through the
+// admissibility network, which predicts log2(1 + rank): blocks predicted
+// below the rank cut are approximated with a rank cap from the prediction,
+// the rest stay dense without an attempt.  Every approximated block is
+// built by adaptive cross approximation and judged on sampled exact entries;
+// accepted blocks leave the dense kernel's flags.  Rank labels of the
+// approximated blocks (log2(1 + rank), log2(1 + 2 cap) when rejected) are
+// kept with their descriptors for training the network.
 void build_compression(int a, MaskEntry &M, const SumArgs &s)
 {
     Compression &C = g.cmp;
     C.release();
-    Object &A = get(OBJ_TARGET, a);
     const int nt = M.view.ntiles, nb = M.view.ndstblocks;
+    const int rmax = std::min(g.opt_cmp_rmax, kLrRankLimit);
+    const int select = g.opt_cmp_select;
+    if (select == 2 && !mlp_ready())
+        fail(-2, "compress_select 2 needs the admissibility network's parameters (train or load them first)");
     cudaStream_t st = g.stream;
     CK(cudaEventRecord(g.ev2, st));
     // tile geometry
     float4 *d_cen = dalloc<float4>(nt), *d_nm = dalloc<float4>(nt);
     launch_tile_stats(g.d_packA, g.d_packB, M.nsrc, d_cen, d_nm, st);
-    std::vector<float4> cen(nt), nm(nt);
+    std::vector<float4> cen(nt);
     std::vector<uint8_t> flags((size_t)nt * nb);
     CK(cudaMemcpyAsync(cen.data(), d_cen, nt * sizeof(float4), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(nm.data(), d_nm, nt * sizeof(float4), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(flags.data(), M.view.flags, flags.size(), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    dfree(d_cen);
-    dfree(d_nm);
     std::vector<int2> blocks;
+    std::vector<uint8_t> cls;
     for (int J = 0; J < nb; J++)
         for (int I = 0; I < std::min(J, nt); I++) {
-            if (flags[(size_t)I * nb + J] != kFlagAll) continue;
-            const float dx = cen[I].x - cen[J].x, dy = cen[I].y - cen[J].y, dz = cen[I].z - cen[J].z;
-            const float sep = std::sqrt(dx * dx + dy * dy + dz * dz);
-            if (sep > g.opt_cmp_eta * (cen[I].w + cen[J].w)) blocks.push_back(make_int2(I, J));
+            const uint8_t f = flags[(size_t)I * nb + J];
+            if (f == kFlagNone) continue;
+            if (select == 0) {
+                if (f != kFlagAll) continue;
+                const float dx = cen[I].x - cen[J].x, dy = cen[I].y - cen[J].y, dz = cen[I].z - cen[J].z;
+                const float sep = std::sqrt(dx * dx + dy * dy + dz * dz);
+                if (!(sep > g.opt_cmp_eta * (cen[I].w + cen[J].w))) continue;
+            }
+            blocks.push_back(make_int2(I, J));
+            cls.push_back(f);
         }
-    C.nblocks = (int)blocks.size();
-    C.rmax = g.opt_cmp_rmax;
+    C.select = select;
+    C.ncand = (int)blocks.size();
     C.obj = a;
     C.kr = g.kr;
     C.ki = g.ki;
+    // descriptors of every candidate
+    const int nc = C.ncand;
+    int2 *d_cblocks = dalloc<int2>(nc);
+    uint8_t *d_ccls = dalloc<uint8_t>(nc);
+    float *d_desc = dalloc<float>((size_t)nc * 8);
+    if (nc > 0) {
+        CK(cudaMemcpyAsync(d_cblocks, blocks.data(), nc * sizeof(int2), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d_ccls, cls.data(), nc, cudaMemcpyHostToDevice, st));
+        const float inv_lambda = (float)(g.kr / (2.0 * M_PI));
+        launch_block_desc(s, d_cblocks, d_ccls, nc, d_cen, d_nm, inv_lambda, d_desc, st);
+    }
+    std::vector<float> desc((size_t)nc * 8);
+    std::vector<int> cap(nc, rmax);
+    std::vector<int> keep;  // candidates that are approximated
+    if (nc > 0) CK(cudaMemcpyAsync(desc.data(), d_desc, desc.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (select == 2 && nc > 0) {
+        float *d_pred = dalloc<float>(nc);
+        CK(mlp_predict_dev(d_desc, nc, d_pred, st));
+        std::vector<float> pred(nc);
+        CK(cudaMemcpyAsync(pred.data(), d_pred, nc * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        dfree(d_pred);
+        const float cut = std::log2(1.0f + g.opt_cmp_rcut);
+        for (int q = 0; q < nc; q++) {
+            if (!(pred[q] < cut)) continue;
+            const float r = std::exp2(pred[q]) - 1.0f;
+            cap[q] = std::max(4, std::min(rmax, (int)std::ceil(1.5f * r) + 4));
+            keep.push_back(q);
+        }
+    } else {
+        CK(cudaStreamSynchronize(st));
+        for (int q = 0; q < nc; q++) keep.push_back(q);
+    }
+    dfree(d_cblocks);
+    dfree(d_ccls);
+    dfree(d_desc);
+    dfree(d_cen);
+    dfree(d_nm);
+    CK(cudaEventRecord(g.ev6, st));
+    // approximated blocks, their caps and factor offsets
+    const int n = (int)keep.size();
+    std::vector<int2> ab(n);
+    std::vector<uint8_t> acls(n);
+    std::vector<int> acap(n);
+    std::vector<long long> off(n);
+    long long cols = 0;
+    for (int q = 0; q < n; q++) {
+        ab[q] = blocks[keep[q]];
+        acls[q] = cls[keep[q]];
+        acap[q] = cap[keep[q]];
+        off[q] = cols;
+        cols += acap[q];
+    }
+    C.nblocks = n;
+    C.ncols = cols;
+    C.rmax = rmax;
     C.d_flags = dalloc<uint8_t>(flags.size());
     C.d_yrow = dalloc<double2>(M.nsrc);
     C.d_ycol = dalloc<double2>(M.nsrc);
-    std::vector<int> rank(C.nblocks);
-    std::vector<float> err(C.nblocks);
-    if (C.nblocks > 0) {
-        C.d_blocks = dalloc<int2>(C.nblocks);
-        const size_t per = (size_t)C.rmax * kTile;
-        C.d_U = dalloc<float2>(per * C.nblocks);
-        C.d_V = dalloc<float2>(per * C.nblocks);
-        C.d_tv = dalloc<float2>((size_t)C.rmax * C.nblocks);
-        C.d_su = dalloc<float2>((size_t)C.rmax * C.nblocks);
-        C.d_rank = dalloc<int>(C.nblocks);
-        C.d_fro = dalloc<float>(C.nblocks);
-        C.d_err = dalloc<float>(C.nblocks);
-        CK(cudaMemcpyAsync(C.d_blocks, blocks.data(), blocks.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
-        launch_aca(s, C.d_blocks, C.nblocks, C.rmax, g.opt_cmp_tol, C.d_U, C.d_V, C.d_rank, C.d_fro,
+    std::vector<int> rank(n);
+    std::vector<float> err(n);
+    if (n > 0) {
+        C.d_blocks = dalloc<int2>(n);
+        C.d_cls = dalloc<uint8_t>(n);
+        C.d_cap = dalloc<int>(n);
+        C.d_off = dalloc<long long>(n);
+        C.d_U = dalloc<float2>((size_t)cols * kTile);
+        C.d_V = dalloc<float2>((size_t)cols * kTile);
+        C.d_tv = dalloc<float2>((size_t)cols);
+        C.d_su = dalloc<float2>((size_t)cols);
+        C.d_rank = dalloc<int>(n);
+        C.d_fro = dalloc<float>(n);
+        C.d_err = dalloc<float>(n);
+        CK(cudaMemcpyAsync(C.d_blocks, ab.data(), n * sizeof(int2), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(C.d_cls, acls.data(), n, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(C.d_cap, acap.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(C.d_off, off.data(), n * sizeof(long long), cudaMemcpyHostToDevice, st));
+        CK(cudaEventRecord(g.ev7, st));
+        launch_aca(s, C.d_blocks, C.d_cls, C.d_cap, C.d_off, n, g.opt_cmp_tol, C.d_U, C.d_V, C.d_rank, C.d_fro,
                    g.opt_cmp_judge, C.d_err, st);
         CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(rank.data(), C.d_rank, C.nblocks * sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(err.data(), C.d_err, C.nblocks * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CK(cudaEventRecord(g.ev8, st));
+        CK(cudaMemcpyAsync(rank.data(), C.d_rank, n * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(err.data(), C.d_err, n * sizeof(float), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        CK(cudaEventElapsedTime(&C.aca_ms, g.ev7, g.ev8));
+    } else {
+        C.aca_ms = 0.0f;
     }
-    // accepted blocks: dense flags off, owner lists
+    // accepted blocks: dense flags off, owner lists; training samples
     std::vector<int> bidx;
-    std::vector<std::vector<int>> byJ(nb), byI(nt);
-    double rsum = 0.0, emax = 0.0;
-    for (int b = 0; b < C.nblocks; b++) {
+    std::vector<std::vector<int>> byJ(nb), byI(nb);
+    double rsum = 0.0, emax = 0.0, pairs = 0.0;
+    C.desc.assign((size_t)n * 8, 0.0f);
+    C.label.assign(n, 0.0f);
+    for (int b = 0; b < n; b++) {
+        std::copy(desc.begin() + (size_t)keep[b] * 8, desc.begin() + (size_t)keep[b] * 8 + 8, C.desc.begin() + (size_t)b * 8);
+        C.label[b] = rank[b] > 0 ? std::log2(1.0f + (float)rank[b]) : std::log2(1.0f + 2.0f * (float)acap[b]);
         if (rank[b] <= 0) continue;
         bidx.push_back(b);
-        flags[(size_t)blocks[b].x * nb + blocks[b].y] = kFlagNone;
-        byJ[blocks[b].y].push_back(b);
-        byI[blocks[b].x].push_back(b);
+        flags[(size_t)ab[b].x * nb + ab[b].y] = kFlagNone;
+        byJ[ab[b].y].push_back(b);
+        byI[ab[b].x].push_back(b);
         rsum += rank[b];
         emax = std::max(emax, (double)err[b]);
+        const double ni = std::min(kTile, M.nsrc - ab[b].x * kTile), nj = std::min(kTile, M.nsrc - ab[b].y * kTile);
+        pairs += 2.0 * ni * nj;
     }
     C.naccepted = (int)bidx.size();
     C.mean_rank = C.naccepted ? rsum / C.naccepted : 0.0;
     C.max_err = emax;
-    auto csr = [&](const std::vector<std::vector<int>> &lists, int *&d_off, int *&d_idx) {
-        std::vector<int> off(lists.size() + 1, 0), idx;
+    C.pairs_cmp = pairs;
+    auto csr = [&](const std::vector<std::vector<int>> &lists, int *&d_o, int *&d_i) {
+        std::vector<int> o(lists.size() + 1, 0), idx;
         for (size_t x = 0; x < lists.size(); x++) {
-            off[x + 1] = off[x] + (int)lists[x].size();
+            o[x + 1] = o[x] + (int)lists[x].size();
             idx.insert(idx.end(), lists[x].begin(), lists[x].end());
         }
-        d_off = dalloc<int>(off.size());
-        d_idx = dalloc<int>(std::max<size_t>(idx.size(), 1));
-        CK(cudaMemcpyAsync(d_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-        if (!idx.empty()) CK(cudaMemcpyAsync(d_idx, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        d_o = dalloc<int>(o.size());
+        d_i = dalloc<int>(std::max<size_t>(idx.size(), 1));
+        CK(cudaMemcpyAsync(d_o, o.data(), o.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        if (!idx.empty()) CK(cudaMemcpyAsync(d_i, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     };
     // the expansion runs per tile X covering both roles (J = X rows, I = X columns)
-    byI.resize(nb);
-    byJ.resize(nb);
     csr(byJ, C.d_byJ_off, C.d_byJ);
     csr(byI, C.d_byI_off, C.d_byI);
     C.d_bidx = dalloc<int>(std::max<size_t>(bidx.size(), 1));
@@ -650,8 +749,8 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     CK(cudaEventRecord(g.ev3, st));
     CK(cudaEventSynchronize(g.ev3));
     CK(cudaEventElapsedTime(&C.build_ms, g.ev2, g.ev3));
+    CK(cudaEventElapsedTime(&C.select_ms, g.ev2, g.ev6));
     C.valid = true;
-    (void)A;
 }
 
 int choose_split(int ntiles, int ndstblocks)
@@ -746,7 +845,7 @@ void run_hop(int hop, int a, int b)
                 }
                 s.mask.flags = C.d_flags;  // accepted blocks are left to the low-rank path
                 CK(cudaEventRecord(g.ev4, st));
-                launch_lr_apply(s, C.d_blocks, C.d_bidx, C.naccepted, C.rmax, C.d_U, C.d_V, C.d_rank, C.d_tv, C.d_su,
+                launch_lr_apply(s, C.d_blocks, C.d_off, C.d_bidx, C.naccepted, C.d_U, C.d_V, C.d_rank, C.d_tv, C.d_su,
                                 M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, st);
                 CK(cudaEventRecord(g.ev5, st));
                 yrow = C.d_yrow;
@@ -781,11 +880,18 @@ void run_hop(int hop, int a, int b)
     g.launches += (hop == HOP_F2F ? 4 : 3) + (rec_cmp ? 2 : 0) + (rec_cmp_build > 0.0f ? 3 : 0);
     HopRecord rec{hop, pair_count(hop, a, b), M.mask_ms, sum_ms, ms, s.nsplit, nl};
     if (rec_cmp) {
+        rec.cmp_cand = g.cmp.ncand;
         rec.cmp_blocks = g.cmp.nblocks;
         rec.cmp_accepted = g.cmp.naccepted;
+        rec.cmp_select = g.cmp.select;
         rec.cmp_mean_rank = g.cmp.mean_rank;
         rec.cmp_max_err = g.cmp.max_err;
+        rec.cmp_pairs = g.cmp.pairs_cmp;
         rec.cmp_build_ms = rec_cmp_build;
+        if (rec_cmp_build > 0.0f) {
+            rec.cmp_select_ms = g.cmp.select_ms;
+            rec.cmp_aca_ms = g.cmp.aca_ms;
+        }
         CK(cudaEventElapsedTime(&rec.lr_ms, g.ev4, g.ev5));
     }
     g.log.push_back(rec);
@@ -1067,15 +1173,17 @@ int sonar_get_fragment_layout(int objectType, int objIdx, int *nx_ny_neg, int nf
 int sonar_get_stats(char *json, int cap)
 {
     std::string s = "{\"hops\": [";
-    char buf[512];
+    char buf[1024];
     for (size_t i = 0; i < g.log.size(); i++) {
         const HopRecord &r = g.log[i];
         snprintf(buf, sizeof(buf),
                  "%s{\"hop\": %d, \"pairs\": %lld, \"mask_ms\": %.6f, \"sum_ms\": %.6f, \"total_ms\": %.6f, "
-                 "\"nsplit\": %d, \"launches\": %d, \"cmp_blocks\": %d, \"cmp_accepted\": %d, "
-                 "\"cmp_mean_rank\": %.3f, \"cmp_max_err\": %.3e, \"cmp_build_ms\": %.6f, \"lr_ms\": %.6f}",
-                 i ? ", " : "", r.hop, r.pairs, r.mask_ms, r.sum_ms, r.total_ms, r.nsplit, r.launches, r.cmp_blocks,
-                 r.cmp_accepted, r.cmp_mean_rank, r.cmp_max_err, r.cmp_build_ms, r.lr_ms);
+                 "\"nsplit\": %d, \"launches\": %d, \"cmp_select\": %d, \"cmp_cand\": %d, \"cmp_blocks\": %d, "
+                 "\"cmp_accepted\": %d, \"cmp_pairs\": %.0f, \"cmp_mean_rank\": %.3f, \"cmp_max_err\": %.3e, "
+                 "\"cmp_build_ms\": %.6f, \"cmp_select_ms\": %.6f, \"cmp_aca_ms\": %.6f, \"lr_ms\": %.6f}",
+                 i ? ", " : "", r.hop, r.pairs, r.mask_ms, r.sum_ms, r.total_ms, r.nsplit, r.launches, r.cmp_select,
+                 r.cmp_cand, r.cmp_blocks, r.cmp_accepted, r.cmp_pairs, r.cmp_mean_rank, r.cmp_max_err,
+                 r.cmp_build_ms, r.cmp_select_ms, r.cmp_aca_ms, r.lr_ms);
         s += buf;
     }
     snprintf(buf, sizeof(buf),
@@ -1108,8 +1216,14 @@ int sonar_set_option(const char *key, double value)
     if (!strcmp(key, "compress_tol")) { g.opt_cmp_tol = (float)value; g.cmp.release(); return 0; }
     if (!strcmp(key, "compress_judge")) { g.opt_cmp_judge = (float)value; g.cmp.release(); return 0; }
     if (!strcmp(key, "compress_eta")) { g.opt_cmp_eta = (float)value; g.cmp.release(); return 0; }
+    if (!strcmp(key, "compress_select")) {
+        g.opt_cmp_select = std::max(0, std::min(2, (int)value));
+        g.cmp.release();
+        return 0;
+    }
+    if (!strcmp(key, "compress_rcut")) { g.opt_cmp_rcut = (float)value; g.cmp.release(); return 0; }
     if (!strcmp(key, "compress_rmax")) {
-        g.opt_cmp_rmax = std::max(1, std::min(256, (int)value));
+        g.opt_cmp_rmax = std::max(2, std::min(kLrRankLimit, (int)value));
         g.cmp.release();
         return 0;
     }
@@ -1245,6 +1359,88 @@ long long sonar_fragment_triangle(const float *tri9, float delta, int *nx_ny_neg
     }
     const long long n = (long long)F.nx * F.ny;
     if (areas && cap >= n) fragment_areas(F, areas);
+    return n;
+}
+
+// ---- admissibility network
+int sonar_mlp_param_count(void) { return (int)mlp_param_count(); }
+
+int sonar_mlp_init(unsigned seed)
+{
+    return guarded([&] {
+        cudaError_t e = mlp_init(seed);
+        if (e != cudaSuccess) fail(-10, "network init failed: %s", cudaGetErrorString(e));
+    });
+}
+
+int sonar_mlp_set_params(const float *params, long long n)
+{
+    return guarded([&] {
+        if (!params || n != (long long)mlp_param_count())
+            fail(-6, "the network has %zu parameters, %lld given", mlp_param_count(), n);
+        cudaError_t e = mlp_set_params(params, (size_t)n);
+        if (e != cudaSuccess) fail(-10, "network parameter upload failed: %s", cudaGetErrorString(e));
+        g.cmp.release();
+    });
+}
+
+int sonar_mlp_get_params(float *params, long long n)
+{
+    return guarded([&] {
+        if (!params || n != (long long)mlp_param_count())
+            fail(-6, "the network has %zu parameters, %lld requested", mlp_param_count(), n);
+        if (!mlp_ready()) fail(-2, "the network has no parameters");
+        cudaError_t e = mlp_get_params(params, (size_t)n);
+        if (e != cudaSuccess) fail(-10, "network parameter read failed: %s", cudaGetErrorString(e));
+    });
+}
+
+int sonar_mlp_grad(const float *X, const float *y, int n, float *grad, float *loss)
+{
+    return guarded([&] {
+        if (!X || !y || !grad || !loss || n <= 0) fail(-6, "sonar_mlp_grad: bad arguments");
+        if (!mlp_ready()) fail(-2, "the network has no parameters");
+        cudaError_t e = mlp_grad(X, y, n, grad, loss);
+        if (e != cudaSuccess) fail(-10, "network gradient failed: %s", cudaGetErrorString(e));
+    });
+}
+
+int sonar_mlp_train(const float *X, const float *y, int n, int epochs, int batch, float lr, unsigned seed,
+                    float *loss)
+{
+    return guarded([&] {
+        if (!X || !y || n <= 0 || epochs < 0 || batch <= 0 || !(lr > 0.0f)) fail(-6, "sonar_mlp_train: bad arguments");
+        if (!mlp_ready()) fail(-2, "the network has no parameters");
+        cudaError_t e = mlp_train(X, y, n, epochs, batch, lr, seed, loss);
+        if (e != cudaSuccess) fail(-10, "network training failed: %s", cudaGetErrorString(e));
+        g.cmp.release();
+    });
+}
+
+int sonar_mlp_predict(const float *X, int n, float *out)
+{
+    return guarded([&] {
+        if (!X || !out || n < 0) fail(-6, "sonar_mlp_predict: bad arguments");
+        if (!mlp_ready()) fail(-2, "the network has no parameters");
+        if (n == 0) return;
+        float *dX = dalloc<float>((size_t)n * 8), *dY = dalloc<float>(n);
+        cudaError_t e = cudaMemcpy(dX, X, (size_t)n * 8 * sizeof(float), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = mlp_predict_dev(dX, n, dY, 0);
+        if (e == cudaSuccess) e = cudaMemcpy(out, dY, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+        dfree(dX);
+        dfree(dY);
+        if (e != cudaSuccess) fail(-10, "network inference failed: %s", cudaGetErrorString(e));
+    });
+}
+
+long long sonar_get_block_samples(float *X, float *y, long long cap)
+{
+    const Compression &C = g.cmp;
+    const long long n = C.valid ? (long long)C.label.size() : 0;
+    if (X && y && cap >= n && n > 0) {
+        memcpy(X, C.desc.data(), (size_t)n * 8 * sizeof(float));
+        memcpy(y, C.label.data(), (size_t)n * sizeof(float));
+    }
     return n;
 }
 

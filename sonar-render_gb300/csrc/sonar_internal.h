@@ -113,14 +113,31 @@ void launch_sum_f2f_sym(const SumArgs &a, double2 *colpart, cudaStream_t s);
 void launch_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,
                              const int *cell, const double2 *Pin, double2 *Pout, double2 *P, cudaStream_t s,
                              const double2 *yrow = nullptr, const double2 *ycol = nullptr);
-// Low-rank FACET_SELF blocks (adaptive cross approximation, judged on sampled
-// entries; rank -1 = keep dense) and their application in a bounce.
-void launch_aca(const SumArgs &a, const int2 *blocks, int nblocks, int rmax, float tol, float2 *U, float2 *V,
-                int *rank, float *fro, float limit, float *err, cudaStream_t s);
-void launch_lr_apply(const SumArgs &a, const int2 *blocks, const int *bidx, int nb, int rmax, const float2 *U,
-                     const float2 *V, const int *rank, float2 *tv, float2 *su, int ntiles, const int *byJ_off,
-                     const int *byJ, const int *byI_off, const int *byI, double2 *yrow, double2 *ycol, cudaStream_t s);
+// Low-rank FACET_SELF blocks (adaptive cross approximation of blocks of any
+// interacting class, judged on sampled exact entries; rank -1 = keep dense),
+// the admissibility network's block descriptors, and the application of the
+// accepted blocks in a bounce.  Block b's factors start at column off[b].
+constexpr int kLrRankLimit = 64;
+void launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
+                int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
+                cudaStream_t s);
+void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
+                       const float4 *nm, float inv_lambda, float *X, cudaStream_t s);
+void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
+                     const float2 *U, const float2 *V, const int *rank, float2 *tv, float2 *su, int ntiles,
+                     const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
+                     double2 *ycol, cudaStream_t s);
 void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s);
+// mlp.cu: the admissibility network (8 -> 128 -> 128 -> 128 -> 1, ReLU, FP32)
+size_t mlp_param_count();
+bool mlp_ready();
+cudaError_t mlp_init(unsigned seed);
+cudaError_t mlp_set_params(const float *p, size_t n);
+cudaError_t mlp_get_params(float *p, size_t n);
+cudaError_t mlp_grad(const float *X, const float *y, int B, float *grad, float *loss);
+cudaError_t mlp_train(const float *X, const float *y, int n, int epochs, int batch, float lr, unsigned seed,
+                      float *last_loss);
+cudaError_t mlp_predict_dev(const float *dX, int n, float *dY, cudaStream_t s);
 // surface.cu: pressure -> RGBA colour map of the reference's surface textures
 void launch_colour_map(const double2 *P, long long n, float min_db, float max_db, int phase, float4 *out,
                        cudaStream_t s);

@@ -69,3 +69,43 @@ def test_compressed_deterministic(api, scenes):
     _, a, _ = _bounces(api, sc, 1)
     _, b, _ = _bounces(api, sc, 1)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("select", [1])
+def test_every_interacting_block_compressed_matches_plain_and_oracle(api, oracle_mod, scenes, select):
+    """Blocks of every class (per-pair mask bits, inline gates, all pairs
+    interacting) approximated with their interactions in the entries: the
+    bounce stays within 1e-3 of the plain path and of the FP64 oracle."""
+    sc = _trihedral(scenes, 30e3)
+    _, P_plain, _ = _bounces(api, sc, 0)
+    api.set_option("compress_select", select)
+    P0, P_cmp, st = _bounces(api, sc, 1)
+    api.set_option("compress_select", 0)
+    hop = [h for h in st["hops"] if h["hop"] == 2][0]
+    print("select %d: candidates %d approximated %d accepted %d pairs %.3e of %.3e, mean rank %.1f, "
+          "build %.2f ms (aca %.2f)" % (select, hop["cmp_cand"], hop["cmp_blocks"], hop["cmp_accepted"],
+                                        hop["cmp_pairs"], hop["pairs"], hop["cmp_mean_rank"], hop["cmp_build_ms"],
+                                        hop["cmp_aca_ms"]))
+    err = rel_l2(P_cmp - P0, P_plain - P0)
+    print("select %d compressed vs plain: rel L2 %.3e" % (select, err))
+    assert err < 1e-3
+    assert hop["cmp_pairs"] > 0.5 * hop["pairs"]
+    # one bounce against the oracle on seeded destinations
+    api.set_option("compress", 1)
+    api.set_option("compress_select", select)
+    load_scene(api, sc)
+    api.project_source_points_to_objects(False)
+    Q0 = api.get_object_pressures(api.TARGET, 0)
+    api.project_target_to_target_objects(1)
+    Q1 = api.get_object_pressures(api.TARGET, 0)
+    api.set_option("compress", 0)
+    api.set_option("compress_select", 0)
+    api.TearDownCuda()
+    o = oracle_scene(oracle_mod, sc)
+    act = o.active(0, 0)
+    rng = np.random.default_rng(78)
+    q = np.sort(rng.choice(len(act), 64, replace=False))
+    v1, _ = o.hop_subset(2, 0, 0, q, pin=Q0)
+    e1 = rel_l2((Q1 - Q0)[act[q]], v1)
+    print("select %d one bounce vs FP64 oracle: rel L2 %.3e" % (select, e1))
+    assert e1 < 1e-3
