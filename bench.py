@@ -1,25 +1,36 @@
 """Benchmark of the discrete Kirchhoff hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload trihedral60|trihedral40|sphere|plate]
+                    [--workload trihedral60|trihedral40|sphere|plate] [--mode both|plain|compressed]
 
 Metric: fragment-pair interactions per second (the reference loops' candidate
 pairs after the area gates, before the cosine and visibility gates): source
-hop S * N_cells, bounces sum_{a != b} n_a n_b, readout N_active * M.
+hop S * N_cells, bounces sum_{a != b} n_a n_b, readout N_active * M.  A
+compressed bounce performs the same interactions through low-rank factors, so
+its rate is those pairs over its time.
 
-Workload (default): the learned-compression configuration's scene, run with
-the plain FP32 path -- orthogonal trihedral with 1 m legs at 60 kHz
-(delta = lambda / 7.5 = 3.29 mm, ~138.7k fragments), one source at 20 m on the
-(1,1,1) diagonal, 2 fragment -> fragment bounces, readout to a 256 x 256
-hemisphere of radius 2 m.  Synthetic, seeded inputs; nothing is read from disk.
+Workload (default, trihedral60): the learned-compression configuration --
+orthogonal trihedral with 1 m legs at 60 kHz (delta = lambda / 7.5 =
+3.29 mm, ~139k fragments), one source at 20 m on the (1,1,1) diagonal, source
+hop then 2 fragment -> fragment bounces.  Synthetic, seeded inputs; nothing is
+read from disk.  Two paths run on it:
+  plain       every pair on the fly in FP32 (hand-written sums), masks rebuilt
+              every step;
+  compressed  the admissibility network proposes blocks and rank caps, cross
+              approximation builds them and the exact entries judge them, the
+              rest stays on the plain kernel -- masks, descriptors, network
+              inference and approximation rebuilt every step.
+``value`` is the compressed path's rate, ``plain`` the plain one's; both are
+checked against each other over every fragment and against the FP64 oracle
+on seeded destinations of each bounce.  The network is trained before the
+timed region on the same trihedral at 40 and 50 kHz (never on the 60 kHz
+blocks it is evaluated on).
 
-A step is one full pass of the path on the resident scene: interaction masks
-rebuilt (visibility included), source hop, 2 bounces, readout.  Each step is
-bracketed by CUDA events on the library's own stream; the L2 is flushed
-between steps (a 256 MB write) outside the events.  ``e2e`` runs the same
-work through the public C ABI from host buffers each step: load the
+Each step is bracketed by CUDA events on the library's own stream; the L2 is
+flushed between steps (a 256 MB write) outside the events.  ``e2e`` runs the
+same work through the public C ABI from host buffers each step: load the
 triangles and points, set_initial_conditions, render_cuda (fragmentation,
-upload), the projections and GetFieldPointPressures (device -> host).
+upload), the projections and the read-back of the surface pressures.
 
 N > 1 runs N independent replicas (the path runs on one GPU; there is no
 data-path collective): value = pairs of all ranks / max-over-ranks time.
@@ -54,9 +65,11 @@ def workload(name):
     ge.load_package()
     from sonar_render_gb300 import scenes
     if name == "trihedral60":
-        cfg = scenes.trihedral_config(60e3, bounces=2, n_theta=256, n_phi=256)
+        cfg = scenes.trihedral_config(60e3, bounces=2, n_theta=0, n_phi=0)
     elif name == "trihedral40":
         cfg = scenes.trihedral_config(40e3, bounces=3, n_theta=256, n_phi=256)
+    elif name == "trihedral40_2b":
+        cfg = scenes.trihedral_config(40e3, bounces=2, n_theta=0, n_phi=0)
     elif name == "sphere":
         cfg = scenes.sphere_config(512, field_surface=True)
     elif name == "plate":
@@ -151,38 +164,18 @@ def step_pairs(stats):
     return sum(h["pairs"] for h in stats["hops"])
 
 
-def run_gb300(args):
+def set_path(api, compressed, select):
+    api.set_option("compress", 1 if compressed else 0)
+    api.set_option("compress_select", select if compressed else 0)
+
+
+def time_path(api, cfg, args, flush, local, world):
+    """Warm-up and K timed steps of the current path on the loaded scene;
+    returns (times ms, stats, clocks).  Events are recorded on the library's
+    stream of this scene (load_scene recreates it)."""
     import torch
     import torch.distributed as dist
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    import __graft_entry__ as ge
-    ge.load_package()
-    from sonar_render_gb300 import api, build
-    build.build()
-    api.load_library()
-    cfg = workload(args.workload)
-
-    train_info = None
-    if args.compress and args.select == 2:
-        # the admissibility network learns from the exact method's blocks of
-        # the same trihedral at other frequencies (untimed set-up)
-        from sonar_render_gb300 import admissibility, scenes
-        t0 = time.time()
-        train_cfgs = [scenes.trihedral_config(f, bounces=1, n_theta=4, n_phi=4) for f in (40e3, 50e3)]
-        X, y, loss = admissibility.train_on_scenes(train_cfgs, epochs=args.train_epochs, batch=256, lr=1e-3, seed=0)
-        train_info = {"samples": int(len(y)), "scenes": ["trihedral_1m_40kHz", "trihedral_1m_50kHz"],
-                      "epochs": args.train_epochs, "final_mse": loss, "seconds": round(time.time() - t0, 2)}
-        print("network trained: %s" % json.dumps(train_info), file=sys.stderr)
-
-    # ---- device-timed steps on the resident scene
-    api.set_option("compress", args.compress)
-    api.set_option("compress_select", args.select)
-    load_scene(api, cfg)
     ext = torch.cuda.ExternalStream(api.stream_handle())
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
     def one_step():
         api.set_option("drop_masks", 1)
@@ -192,17 +185,6 @@ def run_gb300(args):
     for _ in range(args.warmup):
         one_step()
     torch.cuda.synchronize()
-    if args.profile_only:
-        # device work only, for profiler captures: no e2e, no CPU legs, no JSON line
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            one_step()
-        torch.cuda.synchronize()
-        print("profile-only: %d steps of %s done" % (args.steps, cfg["name"]))
-        print(json.dumps(api.stats()["hops"][-4:]))
-        api.TearDownCuda()
-        return
     if world > 1:
         dist.barrier()
     api.set_option("reset_stats", 1)
@@ -223,65 +205,93 @@ def run_gb300(args):
     clk = clocks.stop()
     if world > 1:
         dist.barrier()
-    stats = api.stats()
-    total_ms = float(sum(times))
-    pairs_rank = step_pairs(stats)  # all timed steps
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    return times, api.stats(), clk
+
+
+def max_over_ranks(ms, world):
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    max_ms = float(t.item())
-    value = pairs_rank * world / (max_ms * 1e-3)
-    per_step = stats["hops"][: len(stats["hops"]) // max(args.steps, 1)]
+    return float(t.item())
 
-    # ---- kernel breakdown and roofline of the dominant kernel
-    kern = {}
+
+def kernel_times(stats, steps):
+    """Per-step device time of each kernel group from the library's records."""
+    k = {}
     for h in stats["hops"]:
         name = {0: "source", 1: "field_points", 2: "bounce", 3: "field_object"}[h["hop"]]
-        kern.setdefault("mask_" + name, 0.0)
-        kern.setdefault("sum_" + name, 0.0)
-        kern["mask_" + name] += h["mask_ms"]
-        kern["sum_" + name] += h["sum_ms"]
-    share = {k: round(v / total_ms, 4) for k, v in kern.items() if v > 0}
-    f2f = [h for h in stats["hops"] if h["hop"] == 2]
+        k["mask_" + name] = k.get("mask_" + name, 0.0) + h["mask_ms"]
+        k["sum_" + name] = k.get("sum_" + name, 0.0) + h["sum_ms"]
+        if h.get("lr_ms"):
+            k["lowrank_apply"] = k.get("lowrank_apply", 0.0) + h["lr_ms"]
+        if h.get("cmp_build_ms"):
+            k["select_blocks"] = k.get("select_blocks", 0.0) + h["cmp_select_ms"]
+            k["cross_approx"] = k.get("cross_approx", 0.0) + h["cmp_aca_ms"]
+            k["build_other"] = k.get("build_other", 0.0) + h["cmp_build_ms"] - h["cmp_select_ms"] - h["cmp_aca_ms"]
+    return {n: v / max(steps, 1) for n, v in k.items() if v > 0}
+
+
+def sym_roofline(api, f2f):
     fp32_peak = api.measure_peak(0)
     mufu_peak = api.measure_peak(1)
-    roofline = None
-    if f2f and fp32_peak > 0 and mufu_peak > 0:
-        # the bounce sum evaluates one Green's function per unordered pair and
-        # applies it in both directions: per ordered pair 20 flop (half of the
-        # 40-flop evaluation incl. one complex MAC) + 4 (the second MAC) and 1.5
-        # MUFU ops; roofline pairs/s = min(FP32 / 24, MUFU / 1.5)
-        flop_pp, sfu_pp = 24.0, 1.5
-        roof = min(fp32_peak / flop_pp, mufu_peak / sfu_pp)
-        launch_ms = sum(h["sum_ms"] for h in f2f) / len(f2f)
-        pairs_launch = f2f[0]["pairs"]
-        achieved = pairs_launch * flop_pp / (launch_ms * 1e-3) / 1e12
-        peak = roof * flop_pp / 1e12
-        roofline = {"kernel": "k_sum_f2f_sym (bounce sum, reciprocity)", "bound": "fp32+sfu",
-                    "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
-                    "frac": round(achieved / peak, 4), "traffic": None, "pairs_per_launch": pairs_launch,
-                    "pairs_per_s": round(pairs_launch / (launch_ms * 1e-3), 1), "launch_ms": round(launch_ms, 4),
-                    "peak_source": "measured now by sonar_measure_peak: FP32 %.1f TFLOP/s, MUFU %.2f Top/s; "
-                                   "roofline = min(FP32/24, MUFU/1.5) ordered pairs/s x 24 flop"
-                                   % (fp32_peak / 1e12, mufu_peak / 1e12)}
-    mask_f2f = [h for h in stats["hops"] if h["hop"] == 2 and h["mask_ms"] > 0]
-    mask_info = None
-    if mask_f2f:
-        ms = sum(h["mask_ms"] for h in mask_f2f) / len(mask_f2f)
-        nact = int(round(math.sqrt(max(f2f[0]["pairs"], 1))))
-        mask_info = {"kernel": "k_mask<F2F>", "launch_ms": round(ms, 4),
-                     "mask_bytes_written": None, "note": "1 bit per ordered pair"}
+    if not f2f or not (fp32_peak > 0 and mufu_peak > 0):
+        return None, fp32_peak
+    # the bounce sum evaluates one Green's function per unordered pair and
+    # applies it in both directions: per ordered pair 20 flop (half of the
+    # 40-flop evaluation incl. one complex MAC) + 4 (the second MAC) and 1.5
+    # MUFU ops; roofline pairs/s = min(FP32 / 24, MUFU / 1.5)
+    flop_pp, sfu_pp = 24.0, 1.5
+    roof = min(fp32_peak / flop_pp, mufu_peak / sfu_pp)
+    launch_ms = sum(h["sum_ms"] for h in f2f) / len(f2f)
+    pairs_launch = f2f[0]["pairs"]
+    achieved = pairs_launch * flop_pp / (launch_ms * 1e-3) / 1e12
+    peak = roof * flop_pp / 1e12
+    return {"kernel": "k_sum_f2f_sym (bounce sum, reciprocity)", "bound": "fp32+sfu",
+            "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
+            "frac": round(achieved / peak, 4), "traffic": None, "pairs_per_launch": pairs_launch,
+            "pairs_per_s": round(pairs_launch / (launch_ms * 1e-3), 1), "launch_ms": round(launch_ms, 4),
+            "peak_source": "measured now by sonar_measure_peak: FP32 %.1f TFLOP/s, MUFU %.2f Top/s; "
+                           "roofline = min(FP32/24, MUFU/1.5) ordered pairs/s x 24 flop"
+                           % (fp32_peak / 1e12, mufu_peak / 1e12)}, fp32_peak
 
-    # block classes of the interaction masks (an untimed extra step)
-    api.set_option("class_stats", 1)
-    api.set_option("drop_masks", 1)
-    api.set_option("reset_pressures", 1)
-    api.set_option("reset_stats", 1)
-    projections(api, cfg)
-    mask_classes = api.stats().get("mask_classes")
-    api.set_option("class_stats", 0)
 
-    # ---- end to end through the C ABI from host buffers
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        for k in ("hbm_gbs", "hbm_GBs", "hbm"):
+            if k in d:
+                v = d[k]
+                return float(v if not isinstance(v, dict) else v.get("value")), "MEASURED_PEAKS.json hbm_gbs"
+    except Exception:
+        pass
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def lowrank_roofline(stats):
+    """The low-rank apply (k_lr_block + k_lr_gather) is HBM-bound: per
+    accepted block the factors U, V (rank x 256 complex FP32 each) are read
+    once and 2 x 256 complex FP32 outputs written and read back; the gather
+    writes 2 x 16 bytes per fragment."""
+    hops = [h for h in stats["hops"] if h["hop"] == 2 and h.get("lr_ms")]
+    if not hops:
+        return None
+    h = hops[0]
+    nacc = h["cmp_accepted"]
+    bytes_launch = nacc * (h["cmp_mean_rank"] * 256 * 8 * 2 + 256 * 8 * 2 * 2)
+    ms = sum(x["lr_ms"] for x in hops) / len(hops)
+    peak, src = hbm_peak()
+    ach = bytes_launch / (ms * 1e-3) / 1e9
+    return {"kernel": "k_lr_block + k_lr_gather (low-rank apply)", "bound": "hbm", "achieved": round(ach, 1),
+            "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": None,
+            "bytes_per_launch": int(bytes_launch), "launch_ms": round(ms, 4), "peak_source": src,
+            "blocks": nacc, "mean_rank": h["cmp_mean_rank"]}
+
+
+def e2e_path(api, cfg, args, world, pairs_step):
+    import torch
     api.TearDownCuda()
     e2e_times = []
     h2d = d2h = 0
@@ -291,7 +301,7 @@ def run_gb300(args):
         t0 = time.perf_counter()
         load_scene(api, cfg)
         projections(api, cfg)
-        res = api.GetFieldPoints(npts) if npts else api.get_object_pressures(api.TARGET, 0)
+        api.GetFieldPoints(npts) if npts else api.get_object_pressures(api.TARGET, 0)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         st = api.stats()
@@ -300,31 +310,148 @@ def run_gb300(args):
             h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
         api.TearDownCuda()
     e2e_s = statistics.median(e2e_times)
-    e2e_pairs = pairs_rank / max(args.steps, 1)
-    e2e = {"value": e2e_pairs * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h), "s_per_step": round(e2e_s, 4)}
+    return {"value": pairs_step * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "s_per_step": round(e2e_s, 4)}
 
-    # ---- error vs FP64 on a seeded subset (bounce 1) and CPU baseline, rank 0
-    extra = {}
-    cpu = None
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__ as ge
+    ge.load_package()
+    from sonar_render_gb300 import api, build
+    build.build()
+    api.load_library()
+    cfg = workload(args.workload)
+    modes = ["plain", "compressed"] if args.mode == "both" else [args.mode]
+    select = args.select
+
+    train_info = None
+    if "compressed" in modes and select == 2:
+        # the admissibility network learns from the exact method's blocks of
+        # the same trihedral at other frequencies (untimed set-up)
+        from sonar_render_gb300 import admissibility, scenes
+        t0 = time.time()
+        train_cfgs = [scenes.trihedral_config(f, bounces=1, n_theta=0, n_phi=0) for f in (40e3, 50e3)]
+        X, y, loss = admissibility.train_on_scenes(train_cfgs, epochs=args.train_epochs, batch=256, lr=1e-3, seed=0)
+        train_info = {"samples": int(len(y)), "scenes": ["trihedral_1m_40kHz", "trihedral_1m_50kHz"],
+                      "epochs": args.train_epochs, "final_mse_log2rank": round(loss, 5),
+                      "seconds": round(time.time() - t0, 2)}
+
+    load_scene(api, cfg)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    if args.profile_only:
+        # device work only, for profiler captures: no e2e, no CPU legs, no JSON line
+        for m in modes:
+            set_path(api, m == "compressed", select)
+            for _ in range(args.warmup + args.steps):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                api.set_option("drop_masks", 1)
+                api.set_option("reset_pressures", 1)
+                projections(api, cfg)
+            torch.cuda.synchronize()
+            print("profile-only: %d steps of %s (%s) done" % (args.warmup + args.steps, cfg["name"], m))
+            print(json.dumps(api.stats()["hops"][-3:]))
+        api.TearDownCuda()
+        return
+
+    res = {}
+    for m in modes:
+        set_path(api, m == "compressed", select)
+        load_scene(api, cfg)
+        times, stats, clk = time_path(api, cfg, args, flush, local, world)
+        total_ms = max_over_ranks(float(sum(times)), world)
+        pairs_step = step_pairs(stats) / max(args.steps, 1)
+        res[m] = {"times": times, "stats": stats, "clocks": clk, "ms_per_step": total_ms / args.steps,
+                  "value": pairs_step * args.steps * world / (total_ms * 1e-3), "pairs_step": pairs_step,
+                  "kernels_ms_per_step": {k: round(v, 4) for k, v in kernel_times(stats, args.steps).items()},
+                  "launches_per_step": stats["launches"] / max(args.steps, 1)}
+    f2f_plain = [h for h in res.get("plain", res[modes[0]])["stats"]["hops"] if h["hop"] == 2]
+    roof_sym, _ = sym_roofline(api, f2f_plain)
+
+    # block classes of the interaction masks (an untimed extra step)
+    set_path(api, False, 0)
+    api.set_option("class_stats", 1)
+    api.set_option("drop_masks", 1)
+    api.set_option("reset_pressures", 1)
+    api.set_option("reset_stats", 1)
+    projections(api, cfg)
+    mask_classes = api.stats().get("mask_classes")
+    api.set_option("class_stats", 0)
+
+    # ---- end to end through the C ABI from host buffers
+    for m in modes:
+        set_path(api, m == "compressed", select)
+        res[m]["e2e"] = e2e_path(api, cfg, args, world, res[m]["pairs_step"])
+
+    # ---- errors (vs FP64 on seeded destinations, compressed vs plain) and CPU baseline, rank 0
+    errs, cpu, frag = {}, None, None
     if rank == 0:
-        extra = check_error(api, cfg)
+        outs = {}
+        for m in modes:
+            set_path(api, m == "compressed", select)
+            e = check_error(api, cfg)
+            errs[m] = e.get("errors")
+            frag = e.get("fragments", frag)
+            outs[m] = e.get("out")
+            if m == "plain":
+                errs["grazing"] = e.get("grazing")
+        if "plain" in outs and "compressed" in outs and outs["plain"] is not None and outs["compressed"] is not None:
+            a, b = outs["compressed"], outs["plain"]
+            errs["compressed_vs_plain_all_fragments"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
         cpu = cpu_baseline(cfg, args.cpu_seconds)
-    launches = stats["launches"]
+    set_path(api, False, 0)
+
+    head = "compressed" if "compressed" in modes else modes[0]
+    H = res[head]
+    st = H["stats"]
+    cmp_hops = [h for h in st["hops"] if h["hop"] == 2 and h.get("cmp_build_ms")]
+    compression = None
+    if cmp_hops:
+        h = cmp_hops[0]
+        compression = {"select": {0: "separation rule", 1: "every interacting block", 2: "admissibility network"}
+                       [h["cmp_select"]], "candidate_blocks": h["cmp_cand"], "approximated": h["cmp_blocks"],
+                       "accepted": h["cmp_accepted"], "pair_fraction_compressed": round(h["cmp_pairs"] / h["pairs"], 4),
+                       "mean_rank": h["cmp_mean_rank"], "max_judged_block_err": h["cmp_max_err"],
+                       "tolerance": 1e-4, "judge_limit": 3e-4, "network_training": train_info}
+    kms = H["kernels_ms_per_step"]
+    kshare = {k: round(v / H["ms_per_step"], 4) for k, v in kms.items()}
+    roof_lr = lowrank_roofline(st) if head == "compressed" else None
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": H["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": H["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-        "data": "synthetic (seeded trihedral mesh and points, generated in-process)",
-        "config": {"workload": cfg["name"] + "_plain_fp32", "fragments": extra.get("fragments"),
-                   "bounces": cfg.get("bounces", 0), "sources": int(len(cfg["sources"])),
-                   "field_points": npts, "pairs_per_step": e2e_pairs, "l2": "flushed between steps (256 MB write)",
-                   "path": "plain FP32 sums + interaction masks (rebuilt every step)",
+        "data": "synthetic (seeded trihedral mesh and source, generated in-process)",
+        "config": {"workload": cfg["name"] + ("_compressed" if head == "compressed" else "_plain"),
+                   "fragments": frag, "bounces": cfg.get("bounces", 0), "sources": int(len(cfg["sources"])),
+                   "field_points": 0 if cfg.get("field_points") is None else len(cfg["field_points"]),
+                   "pairs_per_step": H["pairs_step"], "l2": "flushed between steps (256 MB write)",
+                   "path": ("network-proposed low-rank blocks + plain FP32 sums for the rest; masks, network "
+                            "inference and approximation rebuilt every step") if head == "compressed" else
+                           "plain FP32 sums + interaction masks (rebuilt every step)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": roofline, "mask_kernel": mask_info, "kernel_share": share, "mask_block_classes": mask_classes,
-        "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
-        "rel_err_vs_fp64": extra.get("errors"), "grazing": extra.get("grazing"),
+        "roofline": roof_sym, "roofline_lowrank": roof_lr,
+        "kernel_ms_per_step": kms, "kernel_share": kshare,
+        "compression": compression,
+        "mask_block_classes": mask_classes,
+        "cpu_baseline": cpu, "e2e": H["e2e"], "clocks": H["clocks"], "gpu_launches": int(H["launches_per_step"] * args.steps),
+        "rel_err_vs_fp64": errs.get(head), "grazing": errs.get("grazing"),
     }
+    if head == "compressed":
+        line["rel_err_compressed_vs_plain"] = errs.get("compressed_vs_plain_all_fragments")
+    if "plain" in res and head != "plain":
+        P = res["plain"]
+        line["plain"] = {"value": P["value"], "ms_per_step": P["ms_per_step"], "e2e": P["e2e"],
+                         "kernel_ms_per_step": P["kernels_ms_per_step"], "clocks": P["clocks"],
+                         "rel_err_vs_fp64": errs.get("plain"), "gpu_launches": int(P["launches_per_step"] * args.steps)}
+        line["compressed_over_plain"] = round(H["value"] / P["value"], 3)
+        line["compressed_over_plain_e2e"] = round(H["e2e"]["value"] / P["e2e"]["value"], 3)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -332,23 +459,27 @@ def run_gb300(args):
 
 
 def check_error(api, cfg):
-    """Bounce-1 and readout relative L2 error vs the FP64 oracle on seeded
-    destinations, given the GPU's own inputs."""
+    """Per-bounce relative L2 error vs the FP64 oracle on seeded destinations,
+    each bounce given the GPU's own input, and the readout's when the
+    workload has field points.  Also returns the GPU's bounce output."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     out = {}
     try:
+        nb = int(cfg.get("bounces", 0))
         load_scene(api, cfg)
         api.project_source_points_to_objects(False)
-        P0 = api.get_object_pressures(api.TARGET, 0)
-        api.project_target_to_target_objects(1)
-        P1 = api.get_object_pressures(api.TARGET, 0)
+        Ps = [api.get_object_pressures(api.TARGET, 0)]
+        for _ in range(nb):
+            api.project_target_to_target_objects(1)
+            Ps.append(api.get_object_pressures(api.TARGET, 0))
         npts = len(cfg["field_points"]) if cfg.get("field_points") is not None else 0
         if npts:
             api.project_target_to_field_points()
             fp = api.GetFieldPoints(npts)
             fp = fp[:, 0] + 1j * fp[:, 1]
         api.TearDownCuda()
+        out["out"] = Ps[-1] - Ps[0]
         o = O.Oracle()
         o.set_initial_conditions(cfg["cp"], cfg["frequency"], cfg.get("attenuation", 0.0))
         for tris, d in cfg["targets"]:
@@ -360,18 +491,23 @@ def check_error(api, cfg):
         act = o.active(0, 0)
         out["fragments"] = int(len(act))
         rng = np.random.default_rng(2024)
-        q = np.sort(rng.choice(len(act), min(32, len(act)), replace=False))
         nact = len(act)
-        v1, m1 = o.hop_subset(2, 0, 0, q, pin=P0, want_mask=True, nsrc=nact)
-        c1 = o.counters()
-        g1 = (m1 & 2).any(axis=1)
-        d1 = (P1 - P0)[act[q]]
-        e = {"bounce1": float(np.linalg.norm(d1 - v1) / np.linalg.norm(v1))}
-        if (~g1).any():
-            e["bounce1_nongrazing_dst"] = float(np.linalg.norm((d1 - v1)[~g1]) / np.linalg.norm(v1[~g1]))
-        graze = {"bounce_pairs_checked": c1["pairs"], "bounce_grazing": c1["grazing"]}
+        e = {}
+        graze = {}
+        for k in range(nb):
+            q = np.sort(rng.choice(nact, min(32, nact), replace=False))
+            # bounce k+1 input: the pressure after bounce k (P_out <- P)
+            v, m = o.hop_subset(2, 0, 0, q, pin=Ps[k], want_mask=(k == 0), nsrc=nact)
+            c = o.counters()
+            d = (Ps[k + 1] - Ps[k])[act[q]]
+            e["bounce%d" % (k + 1)] = float(np.linalg.norm(d - v) / np.linalg.norm(v))
+            if k == 0:
+                g1 = (m & 2).any(axis=1)
+                if (~g1).any():
+                    e["bounce1_nongrazing_dst"] = float(np.linalg.norm((d - v)[~g1]) / np.linalg.norm(v[~g1]))
+                graze = {"bounce_pairs_checked": c["pairs"], "bounce_grazing": c["grazing"]}
         if npts:
-            o.set_pressures(0, 0, P1)
+            o.set_pressures(0, 0, Ps[-1])
             jj = np.sort(rng.choice(npts, min(32, npts), replace=False))
             vf, mf = o.hop_subset(1, 0, 0, jj, want_mask=True, nsrc=nact)
             c2 = o.counters()
@@ -445,7 +581,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": cfg["name"] + "_plain_fp32", "sample": "bounce destinations on host cores"},
+            "config": {"workload": cfg["name"] + "_compressed", "sample": "bounce destinations on host cores"},
             "cpu_baseline": cpu,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference's own hot path is OptiX GPU code; its CPU restatement (the oracle) runs here"}
@@ -462,8 +598,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
-    ap.add_argument("--compress", type=int, default=0, help="compress admissible bounce blocks (low rank)")
-    ap.add_argument("--select", type=int, default=0,
+    ap.add_argument("--mode", default="both", choices=["both", "plain", "compressed"])
+    ap.add_argument("--select", type=int, default=2,
                     help="compressed blocks: 0 separation rule, 1 every interacting block, 2 the trained network")
     ap.add_argument("--train-epochs", type=int, default=40)
     args = ap.parse_args()

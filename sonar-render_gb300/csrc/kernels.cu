@@ -983,178 +983,257 @@ __device__ __forceinline__ void diag_word(const SumArgs &a, const float4 *sA, co
     }
 }
 
+// Work list of the symmetric bounce sum: the non-empty blocks of destination
+// row J (source tiles t <= J whose flag is not NONE) in tile order,
+// blist[J * ntiles + k], and their count.
+__global__ void __launch_bounds__(kTile) k_sym_rows(const uint8_t *flags, int ntiles, int nb, int *blist,
+                                                   int *rowcnt)
+{
+    __shared__ int sWarp[kTile / 32];
+    const int J = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tmax = min(J, ntiles - 1);
+    int base = 0;
+    for (int t0 = 0; t0 <= tmax; t0 += kTile) {
+        const int t = t0 + tid;
+        const bool on = t <= tmax && flags[(long long)t * nb + J] != kFlagNone;
+        const unsigned bal = __ballot_sync(0xffffffffu, on);
+        if (lane == 0) sWarp[warp] = __popc(bal);
+        __syncthreads();
+        int woff = 0, tot = 0;
+#pragma unroll
+        for (int w = 0; w < kTile / 32; ++w) {
+            woff += w < warp ? sWarp[w] : 0;
+            tot += sWarp[w];
+        }
+        if (on) blist[(long long)J * ntiles + base + woff + __popc(bal & ((1u << lane) - 1u))] = t;
+        base += tot;
+        __syncthreads();
+    }
+    if (tid == 0) rowcnt[J] = base;
+}
+
+// Chunks of at most `per` blocks of one row: chunks[c] = (J, k0, k1),
+// chunk_off[J] .. chunk_off[J + 1] the chunks of row J, *nchunks the total.
+// One CTA of 1024 threads scans the rows in segments.
+__global__ void __launch_bounds__(1024) k_sym_chunks(const int *rowcnt, int nb, int per, int *chunk_off, int4 *chunks,
+                                                     int *nchunks)
+{
+    __shared__ int sW[32];
+    __shared__ int sCarry;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) sCarry = 0;
+    __syncthreads();
+    for (int J0 = 0; J0 < nb; J0 += 1024) {
+        const int J = J0 + tid;
+        const int cnt = J < nb ? rowcnt[J] : 0;
+        const int n = (cnt + per - 1) / per;
+        int v = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        if (lane == 31) sW[warp] = v;
+        __syncthreads();
+        if (warp == 0) {
+            int x = sW[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            sW[lane] = x;
+        }
+        __syncthreads();
+        const int excl = sCarry + (warp > 0 ? sW[warp - 1] : 0) + v - n;
+        if (J < nb) {
+            chunk_off[J] = excl;
+            for (int k = 0; k < n; ++k) chunks[excl + k] = make_int4(J, k * per, min(cnt, (k + 1) * per), 0);
+        }
+        __syncthreads();
+        if (tid == 1023) sCarry = excl + n;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        chunk_off[nb] = sCarry;
+        *nchunks = sCarry;
+    }
+}
+
+// Persistent CTAs take the chunks round-robin (a fixed assignment: results
+// do not depend on timing).  Per chunk: the row terms of its blocks into
+// rowpart[chunk] (FP64), the column terms of block (t, J), t < J, into
+// colpart[256 J (J-1) / 2 + i].
 template <bool ATT>
-__global__ void __launch_bounds__(kTile, 3) k_sum_f2f_sym(SumArgs a, double2 *colpart)
+__global__ void __launch_bounds__(kTile, 3) k_sum_f2f_sym(SumArgs a, SymWork wl, double2 *colpart, double2 *rowpart)
 {
     extern __shared__ float2 sTr[];  // kSymDynSmem bytes: per-warp transpose tiles
     __shared__ float4 sA[kTile];
     __shared__ float4 sB[kTile];
     __shared__ float2 sCol[kTile / 32][kTile];
     __shared__ float sTb[6];  // source tile box
+    __shared__ int sDb[6];    // destination block box
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int J = blockIdx.x;
-    const int j = J * kTile + tid;
-    const bool live = j < a.ndst;
-    Dst d{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    int limit = a.nsrc;
-    float wjr = 0.0f, wji = 0.0f;  // this destination's own source weight (the reciprocal input)
-    float dlo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, dhi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
-    if (live) {
-        const float4 p = a.dst_pos[j];
-        d.px = p.x; d.py = p.y; d.pz = p.z;
-        const float4 n = a.dst_facet_n[a.dst_facet[j]];
-        d.nx = n.x; d.ny = n.y; d.nz = n.z;
-        limit = a.dst_limit[j];
-        wjr = a.srcA[j].w;
-        wji = a.srcB[j].w;
-        dlo[0] = dhi[0] = p.x; dlo[1] = dhi[1] = p.y; dlo[2] = dhi[2] = p.z;
-    }
-    // destination block box (for the regularisation test)
-    __shared__ int sDb[6];
-    if (tid < 6) sDb[tid] = tid < 3 ? f2o(3.0e38f) : f2o(-3.0e38f);
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-        for (int off = 16; off > 0; off >>= 1) {
-            dlo[k] = fminf(dlo[k], __shfl_xor_sync(0xffffffffu, dlo[k], off));
-            dhi[k] = fmaxf(dhi[k], __shfl_xor_sync(0xffffffffu, dhi[k], off));
+    const int nch = *wl.nchunks;
+    for (int ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+        const int4 cw = wl.chunks[ch];
+        const int J = cw.x;
+        const int j = J * kTile + tid;
+        const bool live = j < a.ndst;
+        Dst d{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        int limit = a.nsrc;
+        float wjr = 0.0f, wji = 0.0f;  // this destination's own source weight (the reciprocal input)
+        float dlo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, dhi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        if (live) {
+            const float4 p = a.dst_pos[j];
+            d.px = p.x; d.py = p.y; d.pz = p.z;
+            const float4 n = a.dst_facet_n[a.dst_facet[j]];
+            d.nx = n.x; d.ny = n.y; d.nz = n.z;
+            limit = a.dst_limit[j];
+            wjr = a.srcA[j].w;
+            wji = a.srcB[j].w;
+            dlo[0] = dhi[0] = p.x; dlo[1] = dhi[1] = p.y; dlo[2] = dhi[2] = p.z;
         }
-    if (lane == 0)
+        __syncthreads();  // the previous chunk is done with the shared arrays
+        if (tid < 6) sDb[tid] = tid < 3 ? f2o(3.0e38f) : f2o(-3.0e38f);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            for (int off = 16; off > 0; off >>= 1) {
+                dlo[k] = fminf(dlo[k], __shfl_xor_sync(0xffffffffu, dlo[k], off));
+                dhi[k] = fmaxf(dhi[k], __shfl_xor_sync(0xffffffffu, dhi[k], off));
+            }
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(&sDb[k], f2o(dlo[k]));
+                atomicMax(&sDb[3 + k], f2o(dhi[k]));
+            }
+        __syncthreads();
+        float blo[3], bhi[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            atomicMin(&sDb[k], f2o(dlo[k]));
-            atomicMax(&sDb[3 + k], f2o(dhi[k]));
+            blo[k] = o2f(sDb[k]);
+            bhi[k] = o2f(sDb[3 + k]);
         }
-    __syncthreads();
-    float blo[3], bhi[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        blo[k] = o2f(sDb[k]);
-        bhi[k] = o2f(sDb[3 + k]);
-    }
-
-    const long long cbase = (long long)kTile * J * (J - 1) / 2;  // this J's column region
-    double accr = 0.0, acci = 0.0;
-    const int t0 = blockIdx.y * a.tiles_per_split;
-    const int t1 = min(t0 + a.tiles_per_split, J + 1);
-    for (int t = t0; t < t1; ++t) {
-        const uint8_t fl = a.mask.flags[(long long)t * a.mask.ndstblocks + J];
-        const int i0 = t * kTile;
-        if (fl == kFlagNone) {
-            if (t < J) colpart[cbase + i0 + tid] = make_double2(0.0, 0.0);
-            continue;
-        }
-        __syncthreads();
-        {
-            const int i = i0 + tid;
-            const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            const float4 A = i < a.nsrc ? a.srcA[i] : z;
-            sA[tid] = A;
-            sB[tid] = i < a.nsrc ? a.srcB[i] : z;
-            // source tile box
-            float lo[3] = {A.x, A.y, A.z}, hi[3] = {A.x, A.y, A.z};
-            if (i >= a.nsrc) {
-                lo[0] = lo[1] = lo[2] = 3.0e38f;
-                hi[0] = hi[1] = hi[2] = -3.0e38f;
-            }
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-                for (int off = 16; off > 0; off >>= 1) {
-                    lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], off));
-                    hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], off));
-                }
-            if (lane == 0) {
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    sCol[warp][k] = make_float2(lo[k], hi[k]);
-                }
-            }
-        }
-        __syncthreads();
-        if (tid == 0) {
-            float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
-            for (int q = 0; q < kTile / 32; ++q)
-                for (int k = 0; k < 3; ++k) {
-                    lo[k] = fminf(lo[k], sCol[q][k].x);
-                    hi[k] = fmaxf(hi[k], sCol[q][k].y);
-                }
-            for (int k = 0; k < 3; ++k) {
-                sTb[k] = lo[k];
-                sTb[3 + k] = hi[k];
-            }
-        }
-        __syncthreads();
-        // no pair of this block can be closer than r_min: skip the regularisation code
-        const float tlo[3] = {sTb[0], sTb[1], sTb[2]}, thi[3] = {sTb[3], sTb[4], sTb[5]};
-        const bool reg = box_gap(tlo, thi, blo, bhi) <= a.rmin * 1.001f;
-        const int ntile = min(kTile, a.nsrc - i0);
-        const int nw = (ntile + 31) >> 5;
-        float fr = 0.0f, fi = 0.0f;
-        const bool gate = fl == kFlagClear;
-        for (int w = 0; w < nw; ++w) {
-            uint32_t m;
-            if (fl == kFlagBits) {
-                m = live ? a.mask.bits[(long long)(t * kWordsPerTile + w) * a.mask.pitch + j] : 0u;
-            } else {
-                const int nb = ntile - w * 32;
-                m = !live ? 0u : (nb >= 32 ? 0xffffffffu : ((1u << nb) - 1u));
-            }
-            if (t == J) {
-                // diagonal tile: destination-owned, with the zero-input source limit
-                const int keep = limit - (i0 + w * 32);
-                m &= keep >= 32 ? 0xffffffffu : (keep <= 0 ? 0u : ((1u << keep) - 1u));
-                if (!__any_sync(0xffffffffu, m != 0u)) continue;
-                if (gate) diag_word<ATT, true, true>(a, sA, sB, w, m, d, fr, fi);
-                else diag_word<ATT, false, true>(a, sA, sB, w, m, d, fr, fi);
-            } else {
-                if (!__any_sync(0xffffffffu, m != 0u)) {
-                    sCol[warp][w * 32 + lane] = make_float2(0.0f, 0.0f);
-                    continue;
-                }
-                float2 *colw = &sCol[warp][0];
-                float2 *trw = sTr + warp * 32 * kTrPitch;
-                const bool full = !gate && __all_sync(0xffffffffu, m == 0xffffffffu);
-                if (gate) {
-                    if (reg) sym_word<ATT, true, true, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
-                    else sym_word<ATT, true, false, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
-                } else if (full) {
-                    if (reg) sym_word<ATT, false, true, true>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
-                    else sym_word<ATT, false, false, true>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
-                } else {
-                    if (reg) sym_word<ATT, false, true, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
-                    else sym_word<ATT, false, false, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
-                }
-            }
-        }
-        if (t < J) {
-            for (int w = nw; w < kWordsPerTile; ++w) sCol[warp][w * 32 + lane] = make_float2(0.0f, 0.0f);
+        const long long cbase = (long long)kTile * J * (J - 1) / 2;  // this J's column region
+        double accr = 0.0, acci = 0.0;
+        for (int kk = cw.y; kk < cw.z; ++kk) {
+            const int t = wl.blist[(long long)J * wl.ntiles + kk];
+            const uint8_t fl = a.mask.flags[(long long)t * a.mask.ndstblocks + J];
+            const int i0 = t * kTile;
             __syncthreads();
-            double sr = 0.0, si = 0.0;
+            {
+                const int i = i0 + tid;
+                const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                const float4 A = i < a.nsrc ? a.srcA[i] : z;
+                sA[tid] = A;
+                sB[tid] = i < a.nsrc ? a.srcB[i] : z;
+                float lo[3] = {A.x, A.y, A.z}, hi[3] = {A.x, A.y, A.z};
+                if (i >= a.nsrc) {
+                    lo[0] = lo[1] = lo[2] = 3.0e38f;
+                    hi[0] = hi[1] = hi[2] = -3.0e38f;
+                }
 #pragma unroll
-            for (int k = 0; k < kTile / 32; ++k) {
-                const float2 v = sCol[k][tid];
-                sr += (double)v.x;
-                si += (double)v.y;
+                for (int k = 0; k < 3; ++k)
+                    for (int off = 16; off > 0; off >>= 1) {
+                        lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], off));
+                        hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], off));
+                    }
+                if (lane == 0) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) sCol[warp][k] = make_float2(lo[k], hi[k]);
+                }
             }
-            colpart[cbase + i0 + tid] = make_double2(sr, si);
+            __syncthreads();
+            if (tid == 0) {
+                float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+                for (int q = 0; q < kTile / 32; ++q)
+                    for (int k = 0; k < 3; ++k) {
+                        lo[k] = fminf(lo[k], sCol[q][k].x);
+                        hi[k] = fmaxf(hi[k], sCol[q][k].y);
+                    }
+                for (int k = 0; k < 3; ++k) {
+                    sTb[k] = lo[k];
+                    sTb[3 + k] = hi[k];
+                }
+            }
+            __syncthreads();
+            // no pair of this block can be closer than r_min: skip the regularisation code
+            const float tlo[3] = {sTb[0], sTb[1], sTb[2]}, thi[3] = {sTb[3], sTb[4], sTb[5]};
+            const bool reg = box_gap(tlo, thi, blo, bhi) <= a.rmin * 1.001f;
+            const int ntile = min(kTile, a.nsrc - i0);
+            const int nw = (ntile + 31) >> 5;
+            float fr = 0.0f, fi = 0.0f;
+            const bool gate = fl == kFlagClear;
+            for (int w = 0; w < nw; ++w) {
+                uint32_t m;
+                if (fl == kFlagBits) {
+                    m = live ? a.mask.bits[(long long)(t * kWordsPerTile + w) * a.mask.pitch + j] : 0u;
+                } else {
+                    const int nb = ntile - w * 32;
+                    m = !live ? 0u : (nb >= 32 ? 0xffffffffu : ((1u << nb) - 1u));
+                }
+                if (t == J) {
+                    // diagonal tile: destination-owned, with the zero-input source limit
+                    const int keep = limit - (i0 + w * 32);
+                    m &= keep >= 32 ? 0xffffffffu : (keep <= 0 ? 0u : ((1u << keep) - 1u));
+                    if (!__any_sync(0xffffffffu, m != 0u)) continue;
+                    if (gate) diag_word<ATT, true, true>(a, sA, sB, w, m, d, fr, fi);
+                    else diag_word<ATT, false, true>(a, sA, sB, w, m, d, fr, fi);
+                } else {
+                    if (!__any_sync(0xffffffffu, m != 0u)) {
+                        sCol[warp][w * 32 + lane] = make_float2(0.0f, 0.0f);
+                        continue;
+                    }
+                    float2 *colw = &sCol[warp][0];
+                    float2 *trw = sTr + warp * 32 * kTrPitch;
+                    const bool full = !gate && __all_sync(0xffffffffu, m == 0xffffffffu);
+                    if (gate) {
+                        if (reg) sym_word<ATT, true, true, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
+                        else sym_word<ATT, true, false, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
+                    } else if (full) {
+                        if (reg) sym_word<ATT, false, true, true>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
+                        else sym_word<ATT, false, false, true>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
+                    } else {
+                        if (reg) sym_word<ATT, false, true, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
+                        else sym_word<ATT, false, false, false>(a, sA, sB, w, m, d, wjr, wji, fr, fi, colw, trw, lane);
+                    }
+                }
+            }
+            if (t < J) {
+                for (int w = nw; w < kWordsPerTile; ++w) sCol[warp][w * 32 + lane] = make_float2(0.0f, 0.0f);
+                __syncthreads();
+                double sr = 0.0, si = 0.0;
+#pragma unroll
+                for (int k = 0; k < kTile / 32; ++k) {
+                    const float2 v = sCol[k][tid];
+                    sr += (double)v.x;
+                    si += (double)v.y;
+                }
+                colpart[cbase + i0 + tid] = make_double2(sr, si);
+            }
+            accr += (double)fr;
+            acci += (double)fi;
         }
-        accr += (double)fr;
-        acci += (double)fi;
+        if (live) rowpart[(long long)ch * kTile + tid] = make_double2(accr, acci);
     }
-    if (live) a.partial[(long long)blockIdx.y * a.ndst + j] = make_double2(accr, acci);
 }
 
-// P_out[cell] = rows + (P_in[i] != 0 ? columns : 0); P[cell] += P_out[cell]
-// (yrow / ycol: compressed-block rows and columns, may be null)
-__global__ void k_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,
-                                   const int *cell, const double2 *Pin, double2 *Pout, double2 *P,
-                                   const double2 *yrow, const double2 *ycol)
+// P_out[cell] = rows + (P_in[i] != 0 ? columns : 0); P[cell] += P_out[cell].
+// Rows: the chunks of the fragment's row in chunk order; columns: every
+// non-empty block (I, J > I) of its tile I in J order (deterministic).
+// yrow / ycol: compressed-block rows and columns, may be null.
+__global__ void k_finalize_f2f_sym(const double2 *rowpart, const int *chunk_off, int ndst, const double2 *colpart,
+                                   const uint8_t *flags, int ntiles, const int *cell, const double2 *Pin,
+                                   double2 *Pout, double2 *P, const double2 *yrow, const double2 *ycol)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= ndst) return;
+    const int I = q / kTile;
     double sr = 0.0, si = 0.0;
-    for (int k = 0; k < nsplit; ++k) {
-        const double2 v = partial[(long long)k * ndst + q];
+    for (int c = chunk_off[I]; c < chunk_off[I + 1]; ++c) {
+        const double2 v = rowpart[(long long)c * kTile + (q & (kTile - 1))];
         sr += v.x;
         si += v.y;
     }
@@ -1166,7 +1245,8 @@ __global__ void k_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst,
     }
     if (pin.x != 0.0 || pin.y != 0.0) {
         double cr = 0.0, ci = 0.0;
-        for (int J = q / kTile + 1; J < ntiles; ++J) {
+        for (int J = I + 1; J < ntiles; ++J) {
+            if (flags[(long long)I * ntiles + J] == kFlagNone) continue;
             const double2 v = colpart[(long long)kTile * J * (J - 1) / 2 + q];
             cr += v.x;
             ci += v.y;
@@ -1248,32 +1328,23 @@ __device__ __forceinline__ void warp_argmax(float &v, int &idx)
 }
 
 constexpr int kAcaWarps = 4;
-constexpr size_t kAcaSmem = sizeof(float4) * 4 * kTile * kAcaWarps;
 constexpr int kAcaMaxZeroRows = 48;
 
 // One warp per block; lane l owns columns (and rows) l + 32 q, q = 0..7.
+// Fragment data is read through the L1 cache (no shared staging, so that
+// occupancy is set by registers alone).
 template <bool ATT>
 __global__ void __launch_bounds__(32 * kAcaWarps) k_aca(SumArgs a, const int2 *blocks, const uint8_t *cls,
                                                         const int *cap, const long long *off, int nblocks, float tol,
-                                                        float2 *U, float2 *V, int *rank, float *fro)
+                                                        float limit, float2 *U, float2 *V, int *rank, float *fro,
+                                                        float *err)
 {
-    extern __shared__ float4 sAca[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int b = blockIdx.x * kAcaWarps + warp;
     if (b >= nblocks) return;  // warp-uniform; no CTA barrier follows
-    float4 *PI = sAca + warp * 4 * kTile, *NI = PI + kTile, *PJ = NI + kTile, *NJ = PJ + kTile;
     const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = cap[b];
     const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
-    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const int t = lane + 32 * q;
-        PI[t] = t < ni ? a.srcA[I * kTile + t] : z;
-        NI[t] = t < ni ? a.srcB[I * kTile + t] : z;
-        PJ[t] = t < nj ? a.srcA[J * kTile + t] : z;
-        NJ[t] = t < nj ? a.srcB[J * kTile + t] : z;
-    }
-    __syncwarp();
+    const float4 *PI = a.srcA + I * kTile, *NI = a.srcB + I * kTile, *PJ = a.srcA + J * kTile, *NJ = a.srcB + J * kTile;
     float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
     // mask word w of destination row j: bw[w * pitch + j]
     const uint32_t *bw = a.mask.bits + (long long)I * kWordsPerTile * a.mask.pitch + (long long)J * kTile;
@@ -1286,14 +1357,15 @@ __global__ void __launch_bounds__(32 * kAcaWarps) k_aca(SumArgs a, const int2 *b
     while (k < K) {
         // ---- residual row r over the columns
         float2 val[8];
-        const float4 pr = PJ[r], nr = NJ[r];
+        const float4 pr = __ldg(PJ + r), nr = __ldg(NJ + r);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int i = lane + 32 * q;
             const bool bit =
                 bc == kFlagBits && i < ni ? ((bw[(long long)q * a.mask.pitch + r] >> lane) & 1u) : true;
-            val[q] = i < ni ? lr_entry<ATT>(a, bc, bit, PI[i], NI[i], pr, nr) : make_float2(0.0f, 0.0f);
+            val[q] = i < ni ? lr_entry<ATT>(a, bc, bit, __ldg(PI + i), __ldg(NI + i), pr, nr) : make_float2(0.0f, 0.0f);
         }
+#pragma unroll 4
         for (int m = 0; m < k; ++m) {
             const float2 u = Ub[m * kTile + r];
 #pragma unroll
@@ -1346,15 +1418,16 @@ __global__ void __launch_bounds__(32 * kAcaWarps) k_aca(SumArgs a, const int2 *b
             nv2 += vv.x * vv.x + vv.y * vv.y;
         }
         // ---- residual column c over the rows
-        const float4 pc = PI[c], nc = NI[c];
+        const float4 pc = __ldg(PI + c), nc = __ldg(NI + c);
         const uint32_t *cw = bw + (long long)(c >> 5) * a.mask.pitch;
         float2 uu[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int j = lane + 32 * q;
             const bool bit = bc == kFlagBits && j < nj ? ((cw[j] >> (c & 31)) & 1u) : true;
-            uu[q] = j < nj ? lr_entry<ATT>(a, bc, bit, pc, nc, PJ[j], NJ[j]) : make_float2(0.0f, 0.0f);
+            uu[q] = j < nj ? lr_entry<ATT>(a, bc, bit, pc, nc, __ldg(PJ + j), __ldg(NJ + j)) : make_float2(0.0f, 0.0f);
         }
+#pragma unroll 4
         for (int m = 0; m < k; ++m) {
             const float2 vc = Vb[m * kTile + c];
 #pragma unroll
@@ -1392,65 +1465,45 @@ __global__ void __launch_bounds__(32 * kAcaWarps) k_aca(SumArgs a, const int2 *b
         if (best < 0.0f) break;  // every row taken
         r = nr_;
     }
-    if (lane == 0) {
-        rank[b] = k;
-        fro[b] = sqrtf(norm2);
-    }
-}
-
-// The exact entries judge each approximation: 512 sampled entries per block
-// (every row once at a hashed column, every column once at a hashed row),
-// relative RMS error against the sampled entries' RMS; blocks above the
-// limit, not converged within their cap, or of rank 0 get rank -1 and stay
-// dense.
-template <bool ATT>
-__global__ void __launch_bounds__(kTile) k_aca_judge(SumArgs a, const int2 *blocks, const uint8_t *cls,
-                                                     const int *cap, const long long *off, int nblocks, float limit,
-                                                     const float2 *U, const float2 *V, int *rank, float *err_out)
-{
-    __shared__ float sv[kTile / 32];
-    const int b = blockIdx.x;
-    if (b >= nblocks) return;
-    const int k = rank[b];
-    if (k <= 0 || k >= cap[b]) {  // block-uniform
-        if (threadIdx.x == 0) {
-            rank[b] = -1;
-            err_out[b] = -1.0f;
-        }
-        return;
-    }
-    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], t = threadIdx.x;
-    const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
-    const float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
-    const uint32_t *bw = a.mask.bits + (long long)I * kWordsPerTile * a.mask.pitch + (long long)J * kTile;
+    // ---- the exact entries judge the approximation (same warp, factors still
+    // in L1/L2): every row once at a hashed column, every column once at a
+    // hashed row; relative RMS error against the sampled entries' RMS
     float e2 = 0.0f, x2 = 0.0f;
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        unsigned h = (unsigned)b * 2654435761u + (unsigned)(t + 256 * s) * 40503u + 12345u;
-        h ^= h >> 13;
-        h *= 0x5bd1e995u;
-        h ^= h >> 15;
-        const int jj = s == 0 ? t : (int)(h & 255u), ii = s == 0 ? (int)(h & 255u) : t;
-        if (ii < ni && jj < nj) {
-            const bool bit = bc == kFlagBits ? ((bw[(long long)(ii >> 5) * a.mask.pitch + jj] >> (ii & 31)) & 1u) : true;
-            const float2 ex = lr_entry<ATT>(a, bc, bit, a.srcA[I * kTile + ii], a.srcB[I * kTile + ii],
-                                            a.srcA[J * kTile + jj], a.srcB[J * kTile + jj]);
-            float ar = 0.0f, ai = 0.0f;
-            for (int m = 0; m < k; ++m) {
-                const float2 u = Ub[m * kTile + jj], v = Vb[m * kTile + ii];
-                ar += u.x * v.x - u.y * v.y;
-                ai += u.x * v.y + u.y * v.x;
+    const bool converged = k > 0 && k < K;
+    if (converged) {
+        __syncwarp();
+#pragma unroll 1
+        for (int q = 0; q < 16; ++q) {
+            const int s = lane + 32 * q;  // sample 0..511
+            unsigned h = (unsigned)b * 2654435761u + (unsigned)s * 40503u + 12345u;
+            h ^= h >> 13;
+            h *= 0x5bd1e995u;
+            h ^= h >> 15;
+            const int jj = s < kTile ? s : (int)(h & 255u), ii = s < kTile ? (int)(h & 255u) : s - kTile;
+            if (ii < ni && jj < nj) {
+                const bool bit =
+                    bc == kFlagBits ? ((bw[(long long)(ii >> 5) * a.mask.pitch + jj] >> (ii & 31)) & 1u) : true;
+                const float2 ex = lr_entry<ATT>(a, bc, bit, __ldg(PI + ii), __ldg(NI + ii), __ldg(PJ + jj),
+                                                __ldg(NJ + jj));
+                float ar = 0.0f, ai = 0.0f;
+#pragma unroll 4
+                for (int m = 0; m < k; ++m) {
+                    const float2 u = Ub[m * kTile + jj], v = Vb[m * kTile + ii];
+                    ar += u.x * v.x - u.y * v.y;
+                    ai += u.x * v.y + u.y * v.x;
+                }
+                e2 += (ex.x - ar) * (ex.x - ar) + (ex.y - ai) * (ex.y - ai);
+                x2 += ex.x * ex.x + ex.y * ex.y;
             }
-            e2 += (ex.x - ar) * (ex.x - ar) + (ex.y - ai) * (ex.y - ai);
-            x2 += ex.x * ex.x + ex.y * ex.y;
         }
+        e2 = warp_sum(e2);
+        x2 = warp_sum(x2);
     }
-    const float se = block_sum(e2, sv);
-    const float sx = block_sum(x2, sv);
-    if (t == 0) {
-        const float rel = sx > 0.0f ? sqrtf(se / sx) : (se > 0.0f ? 1.0f : 0.0f);
-        err_out[b] = rel;
-        if (!(rel <= limit)) rank[b] = -1;
+    if (lane == 0) {
+        const float rel = x2 > 0.0f ? sqrtf(e2 / x2) : (e2 > 0.0f ? 1.0f : 0.0f);
+        rank[b] = converged && rel <= limit ? k : -1;
+        fro[b] = sqrtf(norm2);
+        err[b] = converged ? rel : -1.0f;
     }
 }
 
@@ -1516,13 +1569,17 @@ __global__ void __launch_bounds__(128) k_block_desc(SumArgs a, const int2 *block
 
 constexpr int kLrMaxRank = 64;
 
-// Stage 1 of the compressed bounce: per block, tv = V^T w_I and su = U^T w_J
-// (k complex values each); warp partial sums, one barrier.
-__global__ void __launch_bounds__(kTile) k_lr_project(SumArgs a, const int2 *blocks, const long long *off,
-                                                      const int *bidx, int nb, const float2 *U, const float2 *V,
-                                                      const int *rank, float2 *tv, float2 *su)
+// Compressed bounce, one CTA per accepted block: tv = V^T w_I and
+// su = U^T w_J (warp partial sums, one barrier), then the block's forward
+// terms U tv (rows of J) and reciprocal terms V su (columns of I) into the
+// block's own output slots (FP32).  The factors are read from HBM once; the
+// second pass over them hits L2.
+__global__ void __launch_bounds__(kTile) k_lr_block(SumArgs a, const int2 *blocks, const long long *off,
+                                                    const int *bidx, int nb, const float2 *U, const float2 *V,
+                                                    const int *rank, float2 *brow, float2 *bcol)
 {
     __shared__ float4 sRed[kTile / 32][kLrMaxRank];
+    __shared__ float2 sTv[kLrMaxRank], sSu[kLrMaxRank];
     const int q = blockIdx.x;
     if (q >= nb) return;
     const int b = bidx[q];
@@ -1531,9 +1588,9 @@ __global__ void __launch_bounds__(kTile) k_lr_project(SumArgs a, const int2 *blo
     const int i = I * kTile + t, j = J * kTile + t;
     const float wir = i < a.nsrc ? a.srcA[i].w : 0.0f, wii = i < a.nsrc ? a.srcB[i].w : 0.0f;
     const float wjr = j < a.nsrc ? a.srcA[j].w : 0.0f, wji = j < a.nsrc ? a.srcB[j].w : 0.0f;
-    const float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
+    const float2 *Ub = U + off[b] * kTile + t, *Vb = V + off[b] * kTile + t;
     for (int m = 0; m < k; ++m) {
-        const float2 v = Vb[m * kTile + t], u = Ub[m * kTile + t];
+        const float2 v = Vb[m * kTile], u = Ub[m * kTile];
         float4 p = make_float4(v.x * wir - v.y * wii, v.x * wii + v.y * wir, u.x * wjr - u.y * wji,
                                u.x * wji + u.y * wjr);
 #pragma unroll
@@ -1547,93 +1604,54 @@ __global__ void __launch_bounds__(kTile) k_lr_project(SumArgs a, const int2 *blo
     }
     __syncthreads();
     if (t < k) {
-        float4 s = sRed[0][t];
+        float4 s4 = sRed[0][t];
 #pragma unroll
         for (int w = 1; w < kTile / 32; ++w) {
             const float4 p = sRed[w][t];
-            s.x += p.x;
-            s.y += p.y;
-            s.z += p.z;
-            s.w += p.w;
+            s4.x += p.x;
+            s4.y += p.y;
+            s4.z += p.z;
+            s4.w += p.w;
         }
-        tv[off[b] + t] = make_float2(s.x, s.y);
-        su[off[b] + t] = make_float2(s.z, s.w);
+        sTv[t] = make_float2(s4.x, s4.y);
+        sSu[t] = make_float2(s4.z, s4.w);
     }
+    __syncthreads();
+    float rr = 0.0f, ri = 0.0f, cr = 0.0f, ci = 0.0f;
+    for (int m = 0; m < k; ++m) {
+        const float2 u = Ub[m * kTile], v = Vb[m * kTile], c = sTv[m], e = sSu[m];
+        rr += u.x * c.x - u.y * c.y;
+        ri += u.x * c.y + u.y * c.x;
+        cr += v.x * e.x - v.y * e.y;
+        ci += v.x * e.y + v.y * e.x;
+    }
+    brow[(size_t)q * kTile + t] = make_float2(rr, ri);
+    bcol[(size_t)q * kTile + t] = make_float2(cr, ci);
 }
 
-// Stage 2: per owner tile X, rows of every block with J = X (forward) and
-// columns of every block with I = X (reciprocal).  Four groups of 256 threads
-// take the owner's blocks round-robin; the group sums combine in a fixed
-// order (deterministic).  Results in FP64 per fragment.
-constexpr int kLrGroups = 4;
-__global__ void __launch_bounds__(kTile * kLrGroups) k_lr_expand(int n, const long long *off, const float2 *U,
-                                                                 const float2 *V, const int *rank, const float2 *tv,
-                                                                 const float2 *su, const int *byJ_off, const int *byJ,
-                                                                 const int *byI_off, const int *byI, double2 *yrow,
-                                                                 double2 *ycol)
+// Per owner tile X: rows of every accepted block with J = X and columns of
+// every accepted block with I = X, in list order, summed in FP64
+// (deterministic).  The lists hold accepted-block positions q.
+__global__ void __launch_bounds__(kTile) k_lr_gather(int n, const float2 *brow, const float2 *bcol,
+                                                     const int *byJ_off, const int *byJ, const int *byI_off,
+                                                     const int *byI, double2 *yrow, double2 *ycol)
 {
-    __shared__ double2 sR[kLrGroups][kTile], sC[kLrGroups][kTile];
-    const int X = blockIdx.x, g = threadIdx.x / kTile, t = threadIdx.x % kTile;
+    const int X = blockIdx.x, t = threadIdx.x;
     const int q = X * kTile + t;
     double fr = 0.0, fi = 0.0, cr = 0.0, ci = 0.0;
-    for (int p = byJ_off[X] + g; p < byJ_off[X + 1]; p += kLrGroups) {
-        const int b = byJ[p];
-        const int k = rank[b];
-        const float2 *Ub = U + off[b] * kTile + t;
-        const float2 *c = tv + off[b];
-        float ar = 0.0f, ai = 0.0f, br = 0.0f, bi = 0.0f;
-        int m = 0;
-        for (; m + 1 < k; m += 2) {
-            const float2 u0 = Ub[m * kTile], u1 = Ub[(m + 1) * kTile], c0 = c[m], c1 = c[m + 1];
-            ar += u0.x * c0.x - u0.y * c0.y;
-            ai += u0.x * c0.y + u0.y * c0.x;
-            br += u1.x * c1.x - u1.y * c1.y;
-            bi += u1.x * c1.y + u1.y * c1.x;
-        }
-        if (m < k) {
-            const float2 u0 = Ub[m * kTile], c0 = c[m];
-            ar += u0.x * c0.x - u0.y * c0.y;
-            ai += u0.x * c0.y + u0.y * c0.x;
-        }
-        fr += (double)(ar + br);
-        fi += (double)(ai + bi);
+    for (int p = byJ_off[X]; p < byJ_off[X + 1]; ++p) {
+        const float2 v = brow[(size_t)byJ[p] * kTile + t];
+        fr += (double)v.x;
+        fi += (double)v.y;
     }
-    for (int p = byI_off[X] + g; p < byI_off[X + 1]; p += kLrGroups) {
-        const int b = byI[p];
-        const int k = rank[b];
-        const float2 *Vb = V + off[b] * kTile + t;
-        const float2 *c = su + off[b];
-        float ar = 0.0f, ai = 0.0f, br = 0.0f, bi = 0.0f;
-        int m = 0;
-        for (; m + 1 < k; m += 2) {
-            const float2 v0 = Vb[m * kTile], v1 = Vb[(m + 1) * kTile], c0 = c[m], c1 = c[m + 1];
-            ar += v0.x * c0.x - v0.y * c0.y;
-            ai += v0.x * c0.y + v0.y * c0.x;
-            br += v1.x * c1.x - v1.y * c1.y;
-            bi += v1.x * c1.y + v1.y * c1.x;
-        }
-        if (m < k) {
-            const float2 v0 = Vb[m * kTile], c0 = c[m];
-            ar += v0.x * c0.x - v0.y * c0.y;
-            ai += v0.x * c0.y + v0.y * c0.x;
-        }
-        cr += (double)(ar + br);
-        ci += (double)(ai + bi);
+    for (int p = byI_off[X]; p < byI_off[X + 1]; ++p) {
+        const float2 v = bcol[(size_t)byI[p] * kTile + t];
+        cr += (double)v.x;
+        ci += (double)v.y;
     }
-    sR[g][t] = make_double2(fr, fi);
-    sC[g][t] = make_double2(cr, ci);
-    __syncthreads();
-    if (g == 0 && q < n) {
-        double2 R = sR[0][t], Cc = sC[0][t];
-#pragma unroll
-        for (int h = 1; h < kLrGroups; ++h) {
-            R.x += sR[h][t].x;
-            R.y += sR[h][t].y;
-            Cc.x += sC[h][t].x;
-            Cc.y += sC[h][t].y;
-        }
-        yrow[q] = R;
-        ycol[q] = Cc;
+    if (q < n) {
+        yrow[q] = make_double2(fr, fi);
+        ycol[q] = make_double2(cr, ci);
     }
 }
 
@@ -1855,10 +1873,18 @@ void launch_sum(const SumArgs &a, cudaStream_t s)
     }
 }
 
-void launch_sum_f2f_sym(const SumArgs &a, double2 *colpart, cudaStream_t s)
+void launch_sym_worklist(const uint8_t *flags, int ntiles, int nb, int per, int *blist, int *rowcnt, int *chunk_off,
+                         int4 *chunks, int *nchunks, cudaStream_t s)
 {
-    if (a.nsrc <= 0 || a.ndst <= 0) return;
-    dim3 grid(a.mask.ndstblocks, a.nsplit);
+    if (nb <= 0) return;
+    k_sym_rows<<<nb, kTile, 0, s>>>(flags, ntiles, nb, blist, rowcnt);
+    k_sym_chunks<<<1, 1024, 0, s>>>(rowcnt, nb, per, chunk_off, chunks, nchunks);
+}
+
+void launch_sum_f2f_sym(const SumArgs &a, const SymWork &wl, int grid, double2 *colpart, double2 *rowpart,
+                        cudaStream_t s)
+{
+    if (a.nsrc <= 0 || a.ndst <= 0 || grid <= 0) return;
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_sum_f2f_sym<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymDynSmem);
@@ -1866,18 +1892,18 @@ void launch_sum_f2f_sym(const SumArgs &a, double2 *colpart, cudaStream_t s)
         attr_set = true;
     }
     if (a.ka != 0.0f)
-        k_sum_f2f_sym<true><<<grid, kTile, kSymDynSmem, s>>>(a, colpart);
+        k_sum_f2f_sym<true><<<grid, kTile, kSymDynSmem, s>>>(a, wl, colpart, rowpart);
     else
-        k_sum_f2f_sym<false><<<grid, kTile, kSymDynSmem, s>>>(a, colpart);
+        k_sum_f2f_sym<false><<<grid, kTile, kSymDynSmem, s>>>(a, wl, colpart, rowpart);
 }
 
-void launch_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,
-                             const int *cell, const double2 *Pin, double2 *Pout, double2 *P, cudaStream_t s,
-                             const double2 *yrow, const double2 *ycol)
+void launch_finalize_f2f_sym(const double2 *rowpart, const int *chunk_off, int ndst, const double2 *colpart,
+                             const uint8_t *flags, int ntiles, const int *cell, const double2 *Pin, double2 *Pout,
+                             double2 *P, cudaStream_t s, const double2 *yrow, const double2 *ycol)
 {
     if (ndst > 0)
-        k_finalize_f2f_sym<<<blocks_for(ndst, 256), 256, 0, s>>>(partial, nsplit, ndst, colpart, ntiles, cell, Pin,
-                                                                 Pout, P, yrow, ycol);
+        k_finalize_f2f_sym<<<blocks_for(ndst, 256), 256, 0, s>>>(rowpart, chunk_off, ndst, colpart, flags, ntiles,
+                                                                 cell, Pin, Pout, P, yrow, ycol);
 }
 
 void launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
@@ -1885,19 +1911,13 @@ void launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const 
                 cudaStream_t s)
 {
     if (nblocks <= 0) return;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_aca<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAcaSmem);
-        cudaFuncSetAttribute(k_aca<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAcaSmem);
-        attr = true;
-    }
     const unsigned grid = (unsigned)((nblocks + kAcaWarps - 1) / kAcaWarps);
     if (a.ka != 0.0f) {
-        k_aca<true><<<grid, 32 * kAcaWarps, kAcaSmem, s>>>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro);
-        k_aca_judge<true><<<nblocks, kTile, 0, s>>>(a, blocks, cls, cap, off, nblocks, limit, U, V, rank, err);
+        k_aca<true><<<grid, 32 * kAcaWarps, 0, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro,
+                                                     err);
     } else {
-        k_aca<false><<<grid, 32 * kAcaWarps, kAcaSmem, s>>>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro);
-        k_aca_judge<false><<<nblocks, kTile, 0, s>>>(a, blocks, cls, cap, off, nblocks, limit, U, V, rank, err);
+        k_aca<false><<<grid, 32 * kAcaWarps, 0, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro,
+                                                      err);
     }
 }
 
@@ -1909,14 +1929,12 @@ void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls,
 }
 
 void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
-                     const float2 *U, const float2 *V, const int *rank, float2 *tv, float2 *su, int ntiles,
+                     const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
                      double2 *ycol, cudaStream_t s)
 {
-    if (nb > 0) k_lr_project<<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, tv, su);
-    if (ntiles > 0)
-        k_lr_expand<<<ntiles, kTile * kLrGroups, 0, s>>>(a.nsrc, off, U, V, rank, tv, su, byJ_off, byJ, byI_off, byI,
-                                                         yrow, ycol);
+    if (nb > 0) k_lr_block<<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol);
+    if (ntiles > 0) k_lr_gather<<<ntiles, kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, yrow, ycol);
 }
 
 void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s)

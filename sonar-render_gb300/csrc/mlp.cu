@@ -382,20 +382,26 @@ cudaError_t mlp_train(const float *X, const float *y, int n, int epochs, int bat
 }
 
 // Predicted log2(rank) of n descriptor rows (device arrays), on stream s.
+// The activations live in a grow-only buffer kept between calls.
+static Acts g_pred;
 cudaError_t mlp_predict_dev(const float *dX, int n, float *dY, cudaStream_t s)
 {
     if (!g_mlp.ready) return cudaErrorInvalidValue;
     if (n <= 0) return cudaSuccess;
-    Acts A;
-    cudaError_t e = A.alloc(n);
-    if (e != cudaSuccess) return e;
-    e = cudaMemcpyAsync(A.a[0], dX, (size_t)n * kIn * sizeof(float), cudaMemcpyDeviceToDevice, s);
-    if (e == cudaSuccess) {
-        forward(A, n, s);
-        e = cudaMemcpyAsync(dY, A.a[kLayers], (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (n > g_pred.B) {
+        cudaError_t e = g_pred.alloc(n);
+        if (e != cudaSuccess) {
+            g_pred.release();
+            g_pred.B = 0;
+            return e;
+        }
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    A.release();
+    cudaError_t e = cudaMemcpyAsync(g_pred.a[0], dX, (size_t)n * kIn * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) {
+        forward(g_pred, n, s);
+        e = cudaMemcpyAsync(dY, g_pred.a[kLayers], (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
     return e;
 }
 

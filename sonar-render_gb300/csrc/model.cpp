@@ -112,6 +112,39 @@ struct MaskEntry {
 
 // Low-rank compression of the FACET_SELF blocks of one object (built with its
 // mask, rebuilt when the mask or k changes).
+// Grow-only device arena: a build carves its arrays from it in order and the
+// next build starts over (no cudaMalloc / cudaFree per build).
+struct Arena {
+    char *base = nullptr;
+    size_t cap = 0, used = 0;
+    void reserve(size_t bytes)
+    {
+        used = 0;
+        if (bytes <= cap) return;
+        if (base) cudaFree(base);
+        base = nullptr;
+        cap = 0;
+        CK(cudaMalloc((void **)&base, bytes));
+        cap = bytes;
+    }
+    template <class T>
+    T *take(size_t n)
+    {
+        const size_t bytes = (std::max<size_t>(n, 1) * sizeof(T) + 255) / 256 * 256;
+        if (used + bytes > cap) fail(-10, "internal: arena overflow (%zu + %zu > %zu)", used, bytes, cap);
+        T *p = (T *)(base + used);
+        used += bytes;
+        return p;
+    }
+    void release()
+    {
+        if (base) cudaFree(base);
+        base = nullptr;
+        cap = used = 0;
+    }
+    static size_t bytes_of(size_t n, size_t elem) { return (std::max<size_t>(n, 1) * elem + 255) / 256 * 256; }
+};
+
 struct Compression {
     bool valid = false;
     int obj = -1;
@@ -129,7 +162,7 @@ struct Compression {
     uint8_t *d_cls = nullptr;
     int *d_cap = nullptr;
     long long *d_off = nullptr;
-    float2 *d_U = nullptr, *d_V = nullptr, *d_tv = nullptr, *d_su = nullptr;
+    float2 *d_U = nullptr, *d_V = nullptr, *d_brow = nullptr, *d_bcol = nullptr;
     int *d_rank = nullptr, *d_bidx = nullptr;
     float *d_fro = nullptr, *d_err = nullptr;
     int *d_byJ_off = nullptr, *d_byJ = nullptr, *d_byI_off = nullptr, *d_byI = nullptr;
@@ -137,12 +170,13 @@ struct Compression {
     double2 *d_yrow = nullptr, *d_ycol = nullptr;
     // descriptors and rank labels of the approximated blocks (network training)
     std::vector<float> desc, label;
-    void release()
+    Arena arena;    // the candidate- and block-level arrays above
+    Arena factors;  // U, V and the per-block outputs (sized after the selection)
+    void release() { valid = false; }
+    void free_all()
     {
-        dfree(d_blocks); dfree(d_cls); dfree(d_cap); dfree(d_off);
-        dfree(d_U); dfree(d_V); dfree(d_tv); dfree(d_su); dfree(d_rank); dfree(d_bidx);
-        dfree(d_fro); dfree(d_err); dfree(d_byJ_off); dfree(d_byJ); dfree(d_byI_off); dfree(d_byI);
-        dfree(d_flags); dfree(d_yrow); dfree(d_ycol);
+        arena.release();
+        factors.release();
         valid = false;
     }
 };
@@ -193,6 +227,12 @@ struct Model {
     size_t limit_cap = 0;
     double2 *d_colpart = nullptr;
     size_t colpart_cap = 0;
+    // work list of the symmetric bounce sum
+    int *d_blist = nullptr, *d_rowcnt = nullptr, *d_chunk_off = nullptr, *d_nchunks = nullptr;
+    int4 *d_chunks = nullptr;
+    double2 *d_rowpart = nullptr;
+    int sym_tiles = 0;
+    int nsm = 0;
     // options and statistics
     int opt_split = 0;
     int verbose = 0;
@@ -219,9 +259,11 @@ struct Model {
             dfree(m.view.flags);
         }
         masks.clear();
-        cmp.release();
+        cmp.free_all();
         dfree(d_packA); dfree(d_packB); dfree(d_partial); dfree(d_limit); dfree(d_colpart);
+        dfree(d_blist); dfree(d_rowcnt); dfree(d_chunk_off); dfree(d_nchunks); dfree(d_chunks); dfree(d_rowpart);
         pack_cap = partial_cap = limit_cap = colpart_cap = 0;
+        sym_tiles = 0;
         for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3, &ev4, &ev5, &ev6, &ev7, &ev8})
             if (*e) {
                 cudaEventDestroy(*e);
@@ -555,6 +597,32 @@ void ensure_scratch(int nsrc, int ndst, int nsplit)
     }
 }
 
+// Blocks per chunk of the symmetric bounce sum's work list.
+constexpr int kSymChunk = 2;
+
+// Work-list buffers for ntiles x ntiles blocks: at most ceil((J + 1) / per)
+// chunks in row J.
+void ensure_symwork(int ntiles)
+{
+    if (ntiles <= g.sym_tiles) return;
+    dfree(g.d_blist); dfree(g.d_rowcnt); dfree(g.d_chunk_off); dfree(g.d_nchunks); dfree(g.d_chunks);
+    dfree(g.d_rowpart);
+    size_t maxch = 0;
+    for (int J = 0; J < ntiles; J++) maxch += (size_t)(J + kSymChunk) / kSymChunk;
+    g.d_blist = dalloc<int>((size_t)ntiles * ntiles);
+    g.d_rowcnt = dalloc<int>(ntiles);
+    g.d_chunk_off = dalloc<int>(ntiles + 1);
+    g.d_nchunks = dalloc<int>(1);
+    g.d_chunks = dalloc<int4>(maxch);
+    g.d_rowpart = dalloc<double2>(maxch * kTile);
+    g.sym_tiles = ntiles;
+    if (g.nsm == 0) {
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&g.nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+}
+
 void ensure_colpart(int ntiles)
 {
     const size_t n = (size_t)kTile * ntiles * (ntiles > 0 ? ntiles - 1 : 0) / 2;
@@ -588,8 +656,23 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
         fail(-2, "compress_select 2 needs the admissibility network's parameters (train or load them first)");
     cudaStream_t st = g.stream;
     CK(cudaEventRecord(g.ev2, st));
+    // one arena for the whole build, sized for the worst case (every
+    // upper block approximated at the full rank cap)
+    const size_t nmax = (size_t)nt * (nt + 1) / 2;
+    {
+        size_t bytes = 2 * Arena::bytes_of(nt, sizeof(float4)) + Arena::bytes_of(nmax, sizeof(int2)) +
+                       Arena::bytes_of(nmax, 1) + Arena::bytes_of(nmax * 8, sizeof(float)) +
+                       Arena::bytes_of(nmax, sizeof(float)) + Arena::bytes_of((size_t)nt * nb, 1) +
+                       2 * Arena::bytes_of(M.nsrc, sizeof(double2)) + Arena::bytes_of(nmax, sizeof(int2)) +
+                       Arena::bytes_of(nmax, 1) + Arena::bytes_of(nmax, sizeof(int)) +
+                       Arena::bytes_of(nmax, sizeof(long long)) + 3 * Arena::bytes_of(nmax, sizeof(int)) +
+                       2 * Arena::bytes_of(nmax, sizeof(float)) + 4 * Arena::bytes_of(nb + 1, sizeof(int)) +
+                       2 * Arena::bytes_of(nmax, sizeof(int)) + 4096;
+        C.arena.reserve(bytes);
+    }
+    Arena &ar = C.arena;
     // tile geometry
-    float4 *d_cen = dalloc<float4>(nt), *d_nm = dalloc<float4>(nt);
+    float4 *d_cen = ar.take<float4>(nt), *d_nm = ar.take<float4>(nt);
     launch_tile_stats(g.d_packA, g.d_packB, M.nsrc, d_cen, d_nm, st);
     std::vector<float4> cen(nt);
     std::vector<uint8_t> flags((size_t)nt * nb);
@@ -618,26 +701,26 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     C.ki = g.ki;
     // descriptors of every candidate
     const int nc = C.ncand;
-    int2 *d_cblocks = dalloc<int2>(nc);
-    uint8_t *d_ccls = dalloc<uint8_t>(nc);
-    float *d_desc = dalloc<float>((size_t)nc * 8);
+    int2 *d_cblocks = ar.take<int2>(nc);
+    uint8_t *d_ccls = ar.take<uint8_t>(nc);
+    float *d_desc = ar.take<float>((size_t)nc * 8);
     if (nc > 0) {
         CK(cudaMemcpyAsync(d_cblocks, blocks.data(), nc * sizeof(int2), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(d_ccls, cls.data(), nc, cudaMemcpyHostToDevice, st));
         const float inv_lambda = (float)(g.kr / (2.0 * M_PI));
         launch_block_desc(s, d_cblocks, d_ccls, nc, d_cen, d_nm, inv_lambda, d_desc, st);
     }
-    std::vector<float> desc((size_t)nc * 8);
+    // descriptors come back to the host only when the build labels training samples
+    std::vector<float> desc(select == 1 ? (size_t)nc * 8 : 0);
     std::vector<int> cap(nc, rmax);
     std::vector<int> keep;  // candidates that are approximated
-    if (nc > 0) CK(cudaMemcpyAsync(desc.data(), d_desc, desc.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (!desc.empty()) CK(cudaMemcpyAsync(desc.data(), d_desc, desc.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
     if (select == 2 && nc > 0) {
-        float *d_pred = dalloc<float>(nc);
+        float *d_pred = ar.take<float>(nc);
         CK(mlp_predict_dev(d_desc, nc, d_pred, st));
         std::vector<float> pred(nc);
         CK(cudaMemcpyAsync(pred.data(), d_pred, nc * sizeof(float), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        dfree(d_pred);
         const float cut = std::log2(1.0f + g.opt_cmp_rcut);
         for (int q = 0; q < nc; q++) {
             if (!(pred[q] < cut)) continue;
@@ -649,11 +732,6 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
         CK(cudaStreamSynchronize(st));
         for (int q = 0; q < nc; q++) keep.push_back(q);
     }
-    dfree(d_cblocks);
-    dfree(d_ccls);
-    dfree(d_desc);
-    dfree(d_cen);
-    dfree(d_nm);
     CK(cudaEventRecord(g.ev6, st));
     // approximated blocks, their caps and factor offsets
     const int n = (int)keep.size();
@@ -672,23 +750,23 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     C.nblocks = n;
     C.ncols = cols;
     C.rmax = rmax;
-    C.d_flags = dalloc<uint8_t>(flags.size());
-    C.d_yrow = dalloc<double2>(M.nsrc);
-    C.d_ycol = dalloc<double2>(M.nsrc);
+    C.d_flags = ar.take<uint8_t>(flags.size());
+    C.d_yrow = ar.take<double2>(M.nsrc);
+    C.d_ycol = ar.take<double2>(M.nsrc);
     std::vector<int> rank(n);
     std::vector<float> err(n);
     if (n > 0) {
-        C.d_blocks = dalloc<int2>(n);
-        C.d_cls = dalloc<uint8_t>(n);
-        C.d_cap = dalloc<int>(n);
-        C.d_off = dalloc<long long>(n);
-        C.d_U = dalloc<float2>((size_t)cols * kTile);
-        C.d_V = dalloc<float2>((size_t)cols * kTile);
-        C.d_tv = dalloc<float2>((size_t)cols);
-        C.d_su = dalloc<float2>((size_t)cols);
-        C.d_rank = dalloc<int>(n);
-        C.d_fro = dalloc<float>(n);
-        C.d_err = dalloc<float>(n);
+        C.d_blocks = ar.take<int2>(n);
+        C.d_cls = ar.take<uint8_t>(n);
+        C.d_cap = ar.take<int>(n);
+        C.d_off = ar.take<long long>(n);
+        C.factors.reserve(2 * Arena::bytes_of((size_t)cols * kTile, sizeof(float2)) +
+                          2 * Arena::bytes_of((size_t)n * kTile, sizeof(float2)));
+        C.d_U = C.factors.take<float2>((size_t)cols * kTile);
+        C.d_V = C.factors.take<float2>((size_t)cols * kTile);
+        C.d_rank = ar.take<int>(n);
+        C.d_fro = ar.take<float>(n);
+        C.d_err = ar.take<float>(n);
         CK(cudaMemcpyAsync(C.d_blocks, ab.data(), n * sizeof(int2), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(C.d_cls, acls.data(), n, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(C.d_cap, acap.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -709,16 +787,20 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     std::vector<int> bidx;
     std::vector<std::vector<int>> byJ(nb), byI(nb);
     double rsum = 0.0, emax = 0.0, pairs = 0.0;
-    C.desc.assign((size_t)n * 8, 0.0f);
-    C.label.assign(n, 0.0f);
+    C.desc.assign(desc.empty() ? 0 : (size_t)n * 8, 0.0f);
+    C.label.assign(desc.empty() ? 0 : n, 0.0f);
     for (int b = 0; b < n; b++) {
-        std::copy(desc.begin() + (size_t)keep[b] * 8, desc.begin() + (size_t)keep[b] * 8 + 8, C.desc.begin() + (size_t)b * 8);
-        C.label[b] = rank[b] > 0 ? std::log2(1.0f + (float)rank[b]) : std::log2(1.0f + 2.0f * (float)acap[b]);
+        if (!desc.empty()) {
+            std::copy(desc.begin() + (size_t)keep[b] * 8, desc.begin() + (size_t)keep[b] * 8 + 8,
+                      C.desc.begin() + (size_t)b * 8);
+            C.label[b] = rank[b] > 0 ? std::log2(1.0f + (float)rank[b]) : std::log2(1.0f + 2.0f * (float)acap[b]);
+        }
         if (rank[b] <= 0) continue;
+        const int q = (int)bidx.size();  // accepted position: the block's output slots
         bidx.push_back(b);
         flags[(size_t)ab[b].x * nb + ab[b].y] = kFlagNone;
-        byJ[ab[b].y].push_back(b);
-        byI[ab[b].x].push_back(b);
+        byJ[ab[b].y].push_back(q);
+        byI[ab[b].x].push_back(q);
         rsum += rank[b];
         emax = std::max(emax, (double)err[b]);
         const double ni = std::min(kTile, M.nsrc - ab[b].x * kTile), nj = std::min(kTile, M.nsrc - ab[b].y * kTile);
@@ -734,15 +816,18 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
             o[x + 1] = o[x] + (int)lists[x].size();
             idx.insert(idx.end(), lists[x].begin(), lists[x].end());
         }
-        d_o = dalloc<int>(o.size());
-        d_i = dalloc<int>(std::max<size_t>(idx.size(), 1));
+        d_o = ar.take<int>(o.size());
+        d_i = ar.take<int>(std::max<size_t>(idx.size(), 1));
         CK(cudaMemcpyAsync(d_o, o.data(), o.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         if (!idx.empty()) CK(cudaMemcpyAsync(d_i, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     };
     // the expansion runs per tile X covering both roles (J = X rows, I = X columns)
     csr(byJ, C.d_byJ_off, C.d_byJ);
     csr(byI, C.d_byI_off, C.d_byI);
-    C.d_bidx = dalloc<int>(std::max<size_t>(bidx.size(), 1));
+    C.d_bidx = ar.take<int>(std::max<size_t>(bidx.size(), 1));
+    if (n == 0) C.factors.reserve(2 * Arena::bytes_of(kTile, sizeof(float2)));
+    C.d_brow = C.factors.take<float2>(std::max<size_t>(bidx.size(), 1) * kTile);
+    C.d_bcol = C.factors.take<float2>(std::max<size_t>(bidx.size(), 1) * kTile);
     if (!bidx.empty())
         CK(cudaMemcpyAsync(C.d_bidx, bidx.data(), bidx.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(C.d_flags, flags.data(), flags.size(), cudaMemcpyHostToDevice, st));
@@ -845,18 +930,23 @@ void run_hop(int hop, int a, int b)
                 }
                 s.mask.flags = C.d_flags;  // accepted blocks are left to the low-rank path
                 CK(cudaEventRecord(g.ev4, st));
-                launch_lr_apply(s, C.d_blocks, C.d_off, C.d_bidx, C.naccepted, C.d_U, C.d_V, C.d_rank, C.d_tv, C.d_su,
+                launch_lr_apply(s, C.d_blocks, C.d_off, C.d_bidx, C.naccepted, C.d_U, C.d_V, C.d_rank, C.d_brow, C.d_bcol,
                                 M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, st);
                 CK(cudaEventRecord(g.ev5, st));
                 yrow = C.d_yrow;
                 ycol = C.d_ycol;
                 rec_cmp = true;
             }
+            // work list of the non-empty blocks (the dense kernel's flags)
+            ensure_symwork(M.view.ntiles);
+            launch_sym_worklist(s.mask.flags, M.view.ntiles, M.view.ndstblocks, kSymChunk, g.d_blist, g.d_rowcnt,
+                                g.d_chunk_off, g.d_chunks, g.d_nchunks, st);
+            const SymWork wl{g.d_blist, g.d_chunks, g.d_nchunks, M.view.ntiles};
             CK(cudaEventRecord(g.ev2, st));
-            launch_sum_f2f_sym(s, g.d_colpart, st);
+            launch_sum_f2f_sym(s, wl, 3 * g.nsm, g.d_colpart, g.d_rowpart, st);
             CK(cudaEventRecord(g.ev3, st));
-            launch_finalize_f2f_sym(g.d_partial, s.nsplit, M.ndst, g.d_colpart, M.view.ntiles, A.d_act_cell, A.d_Pin,
-                                    A.d_Pout, A.d_P, st, yrow, ycol);
+            launch_finalize_f2f_sym(g.d_rowpart, g.d_chunk_off, M.ndst, g.d_colpart, s.mask.flags, M.view.ntiles,
+                                    A.d_act_cell, A.d_Pin, A.d_Pout, A.d_P, st, yrow, ycol);
         } else {
             timed_sum(s, st);
             launch_finalize_f2f(g.d_partial, s.nsplit, M.ndst, A.d_act_cell, A.d_Pout, A.d_P, st);
@@ -876,8 +966,8 @@ void run_hop(int hop, int a, int b)
     float ms = 0.0f, sum_ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
     CK(cudaEventElapsedTime(&sum_ms, g.ev2, g.ev3));
-    const int nl = (hop == HOP_F2F ? 4 : 3) + (M.mask_ms > 0.0f ? 1 : 0) + (rec_cmp ? 2 : 0);
-    g.launches += (hop == HOP_F2F ? 4 : 3) + (rec_cmp ? 2 : 0) + (rec_cmp_build > 0.0f ? 3 : 0);
+    const int nl = (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + (M.mask_ms > 0.0f ? 1 : 0) + (rec_cmp ? 2 : 0);
+    g.launches += (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + (rec_cmp ? 2 : 0) + (rec_cmp_build > 0.0f ? 4 : 0);
     HopRecord rec{hop, pair_count(hop, a, b), M.mask_ms, sum_ms, ms, s.nsplit, nl};
     if (rec_cmp) {
         rec.cmp_cand = g.cmp.ncand;

@@ -107,12 +107,24 @@ void launch_finalize_add(const double2 *partial, int nsplit, int ndst, const int
 void launch_finalize_f2f(const double2 *partial, int nsplit, int ndst, const int *cell, double2 *Pout,
                          double2 *P, cudaStream_t s);
 void launch_mask_export(const MaskView &m, int nsrc, int ndst, uint8_t *out, cudaStream_t s);
-// FACET_SELF with reciprocity: one Green's function per unordered pair.
-// colpart holds 256 * ntiles * (ntiles - 1) / 2 double2.
-void launch_sum_f2f_sym(const SumArgs &a, double2 *colpart, cudaStream_t s);
-void launch_finalize_f2f_sym(const double2 *partial, int nsplit, int ndst, const double2 *colpart, int ntiles,
-                             const int *cell, const double2 *Pin, double2 *Pout, double2 *P, cudaStream_t s,
-                             const double2 *yrow = nullptr, const double2 *ycol = nullptr);
+// FACET_SELF with reciprocity: one Green's function per unordered pair, over
+// a work list of the non-empty upper blocks cut into chunks of `per` blocks
+// of one destination row.  colpart holds 256 * ntiles * (ntiles - 1) / 2
+// double2, rowpart 256 per chunk.
+struct SymWork {
+    const int *blist;      // [nb][ntiles]: row J's non-empty source tiles
+    const int4 *chunks;    // (J, k0, k1)
+    const int *nchunks;    // device count
+    int ntiles;
+};
+void launch_sym_worklist(const uint8_t *flags, int ntiles, int nb, int per, int *blist, int *rowcnt, int *chunk_off,
+                         int4 *chunks, int *nchunks, cudaStream_t s);
+void launch_sum_f2f_sym(const SumArgs &a, const SymWork &wl, int grid, double2 *colpart, double2 *rowpart,
+                        cudaStream_t s);
+void launch_finalize_f2f_sym(const double2 *rowpart, const int *chunk_off, int ndst, const double2 *colpart,
+                             const uint8_t *flags, int ntiles, const int *cell, const double2 *Pin, double2 *Pout,
+                             double2 *P, cudaStream_t s, const double2 *yrow = nullptr,
+                             const double2 *ycol = nullptr);
 // Low-rank FACET_SELF blocks (adaptive cross approximation of blocks of any
 // interacting class, judged on sampled exact entries; rank -1 = keep dense),
 // the admissibility network's block descriptors, and the application of the
@@ -124,7 +136,7 @@ void launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const 
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
                        const float4 *nm, float inv_lambda, float *X, cudaStream_t s);
 void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
-                     const float2 *U, const float2 *V, const int *rank, float2 *tv, float2 *su, int ntiles,
+                     const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
                      double2 *ycol, cudaStream_t s);
 void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s);

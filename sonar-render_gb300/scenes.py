@@ -203,8 +203,10 @@ def sphere_config(field_points_side=512, field_surface=True):
 
 def trihedral_config(frequency=40e3, bounces=3, n_theta=256, n_phi=256):
     """Trihedral (1 m legs), source at 20 m on the (1,1,1) diagonal, bounces,
-    readout to an n_theta x n_phi hemisphere of radius 2 m."""
+    readout to an n_theta x n_phi hemisphere of radius 2 m (none when either
+    count is 0)."""
     src = (20.0 / math.sqrt(3.0)) * np.ones((1, 3), np.float32)
+    fp = hemisphere(n_theta, n_phi, 2.0) if n_theta and n_phi else None
     return dict(name="trihedral_1m_%dkHz_%db" % (int(frequency / 1e3), bounces), frequency=frequency,
                 cp=CP_WATER, attenuation=0.0, targets=[(trihedral(1.0), delta_for(frequency))], fields=[],
-                sources=src, field_points=hemisphere(n_theta, n_phi, 2.0), bounces=bounces)
+                sources=src, field_points=fp, bounces=bounces)
