@@ -1327,179 +1327,242 @@ __device__ __forceinline__ void warp_argmax(float &v, int &idx)
     }
 }
 
-constexpr int kAcaWarps = 4;
 constexpr int kAcaMaxZeroRows = 48;
+constexpr int kAcaRegRanks = 16;  // factor entries a thread keeps in registers; higher ranks are re-read from global
+constexpr int kAcaWarps = kTile / 32;
 
-// One warp per block; lane l owns columns (and rows) l + 32 q, q = 0..7.
-// Fragment data is read through the L1 cache (no shared staging, so that
-// occupancy is set by registers alone).
-template <bool ATT>
-__global__ void __launch_bounds__(32 * kAcaWarps) k_aca(SumArgs a, const int2 *blocks, const uint8_t *cls,
-                                                        const int *cap, const long long *off, int nblocks, float tol,
-                                                        float limit, float2 *U, float2 *V, int *rank, float *fro,
-                                                        float *err)
+// Block-wide argmax of v (ties: lowest index) and, with SUMS, the block-wide
+// sums of s0 and s1.  Every thread receives the result.  One barrier;
+// callers alternate between two slot arrays so that a slot array is never
+// rewritten while a thread may still read it.
+template <bool SUMS>
+__device__ __forceinline__ void cta_argmax(float &v, int &idx, float &s0, float &s1, float4 *slots)
 {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int b = blockIdx.x * kAcaWarps + warp;
-    if (b >= nblocks) return;  // warp-uniform; no CTA barrier follows
-    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = cap[b];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (SUMS) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        }
+        if (ov > v || (ov == v && oi < idx)) {
+            v = ov;
+            idx = oi;
+        }
+    }
+    if (lane == 0) slots[warp] = make_float4(v, __int_as_float(idx), s0, s1);
+    __syncthreads();
+    float bv = -3.0e38f, t0 = 0.0f, t1 = 0.0f;
+    int bi = 0x7fffffff;
+#pragma unroll
+    for (int q = 0; q < kAcaWarps; ++q) {
+        if (SUMS) {
+            const float4 o = slots[q];
+            t0 += o.z;
+            t1 += o.w;
+            if (o.x > bv || (o.x == bv && __float_as_int(o.y) < bi)) {
+                bv = o.x;
+                bi = __float_as_int(o.y);
+            }
+        } else {
+            const float2 o = *reinterpret_cast<const float2 *>(slots + q);
+            if (o.x > bv || (o.x == bv && __float_as_int(o.y) < bi)) {
+                bv = o.x;
+                bi = __float_as_int(o.y);
+            }
+        }
+    }
+    v = bv;
+    idx = bi;
+    if (SUMS) {
+        s0 = t0;
+        s1 = t1;
+    }
+}
+
+// Statement S for every register-held rank m < n (n uniform across the CTA),
+// in groups of four so that register indices stay static.
+#define ACA_REG_GROUP(m0, n, S)                                  \
+    _Pragma("unroll") for (int m = (m0); m < (m0) + 4; ++m) if (m < (n)) \
+    {                                                            \
+        S;                                                       \
+    }
+#define ACA_REG_LOOP(n, S)                                       \
+    do {                                                         \
+        ACA_REG_GROUP(0, n, S)                                   \
+        if ((n) > 4) {                                           \
+            ACA_REG_GROUP(4, n, S)                               \
+            if ((n) > 8) {                                       \
+                ACA_REG_GROUP(8, n, S)                           \
+                if ((n) > 12) { ACA_REG_GROUP(12, n, S) }        \
+            }                                                    \
+        }                                                        \
+    } while (0)
+// Statement S for the register slot m == n only.
+#define ACA_REG_SLOT(m0, n, S)                                      \
+    _Pragma("unroll") for (int m = (m0); m < (m0) + 4; ++m) if (m == (n)) \
+    {                                                               \
+        S;                                                          \
+    }
+#define ACA_REG_SET(n, S)                   \
+    do {                                    \
+        if ((n) < 4) {                      \
+            ACA_REG_SLOT(0, n, S)           \
+        } else if ((n) < 8) {               \
+            ACA_REG_SLOT(4, n, S)           \
+        } else if ((n) < 12) {              \
+            ACA_REG_SLOT(8, n, S)           \
+        } else {                            \
+            ACA_REG_SLOT(12, n, S)          \
+        }                                   \
+    } while (0)
+static_assert(kAcaRegRanks == 16, "ACA_REG_LOOP and ACA_REG_SET cover 16 register-held ranks");
+
+// x - u v (complex)
+__device__ __forceinline__ float2 csub_mul(float2 x, float2 u, float2 v)
+{
+    x.x -= u.x * v.x - u.y * v.y;
+    x.y -= u.x * v.y + u.y * v.x;
+    return x;
+}
+
+// One CTA per block, thread t owns row t and column t of the block.  Its own
+// fragment data (column: source i = t, row: destination j = t) and its
+// entries of the first kAcaRegRanks factor columns stay in registers; the
+// pivot row's U entries and the pivot column's V entries are published
+// through shared memory.  Four barriers per rank step.  The factors are also
+// written to U and V (the low-rank apply reads them there); ranks past
+// kAcaRegRanks are re-read from there, and with one block per CTA the
+// factors of the blocks in flight stay in L2.
+template <bool ATT>
+__global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks, const uint8_t *cls, const int *cap,
+                                                  const long long *off, int nblocks, float tol, float limit,
+                                                  float2 *U, float2 *V, int *rank, float *fro, float *err)
+{
+    __shared__ float4 slotA[kAcaWarps], slotB[kAcaWarps];
+    __shared__ float2 su[kLrRankLimit], sv[kLrRankLimit + 1];  // sv[kLrRankLimit]: the pivot
+    const int t = threadIdx.x, b = blockIdx.x;
+    if (b >= nblocks) return;  // CTA-uniform
+    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = min(cap[b], kLrRankLimit);
     const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
     const float4 *PI = a.srcA + I * kTile, *NI = a.srcB + I * kTile, *PJ = a.srcA + J * kTile, *NJ = a.srcB + J * kTile;
     float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
     // mask word w of destination row j: bw[w * pitch + j]
     const uint32_t *bw = a.mask.bits + (long long)I * kWordsPerTile * a.mask.pitch + (long long)J * kTile;
-    unsigned used = 0u;  // bit q: row lane + 32 q taken (or absent)
+    const long long pitch = a.mask.pitch;
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float2 z2 = make_float2(0.0f, 0.0f);
+    const bool coli = t < ni, rowj = t < nj;
+    const float4 pi = coli ? __ldg(PI + t) : z4, qi = coli ? __ldg(NI + t) : z4;
+    const float4 pj = rowj ? __ldg(PJ + t) : z4, qj = rowj ? __ldg(NJ + t) : z4;
+    float2 ur[kAcaRegRanks], vr[kAcaRegRanks];
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
-        if (lane + 32 * q >= nj) used |= 1u << q;
+    for (int m = 0; m < kAcaRegRanks; ++m) ur[m] = vr[m] = z2;
+    bool used = !rowj;  // row t taken (or absent)
     int r = 0, k = 0, zero_rows = 0;
     float norm2 = 0.0f;
     while (k < K) {
-        // ---- residual row r over the columns
-        float2 val[8];
-        const float4 pr = __ldg(PJ + r), nr = __ldg(NJ + r);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int i = lane + 32 * q;
-            const bool bit =
-                bc == kFlagBits && i < ni ? ((bw[(long long)q * a.mask.pitch + r] >> lane) & 1u) : true;
-            val[q] = i < ni ? lr_entry<ATT>(a, bc, bit, __ldg(PI + i), __ldg(NI + i), pr, nr) : make_float2(0.0f, 0.0f);
+        // ---- publish U[r][m], m < k
+        if (t == r) {
+            ACA_REG_LOOP(k, su[m] = ur[m]);
+            for (int m = kAcaRegRanks; m < k; ++m) su[m] = Ub[m * kTile + r];
         }
-#pragma unroll 4
-        for (int m = 0; m < k; ++m) {
-            const float2 u = Ub[m * kTile + r];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const float2 v = Vb[m * kTile + lane + 32 * q];
-                val[q].x -= u.x * v.x - u.y * v.y;
-                val[q].y -= u.x * v.y + u.y * v.x;
-            }
+        __syncthreads();
+        // ---- residual row r, entry (r, t)
+        float2 val = z2;
+        if (coli) {
+            const bool bit = bc == kFlagBits ? ((bw[(long long)(t >> 5) * pitch + r] >> (t & 31)) & 1u) : true;
+            val = lr_entry<ATT>(a, bc, bit, pi, qi, __ldg(PJ + r), __ldg(NJ + r));
+            ACA_REG_LOOP(k, val = csub_mul(val, su[m], vr[m]));
+            for (int m = kAcaRegRanks; m < k; ++m) val = csub_mul(val, su[m], Vb[m * kTile + t]);
         }
-        float best = -1.0f;
-        int c = 0;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int i = lane + 32 * q;
-            const float m2 = i < ni ? val[q].x * val[q].x + val[q].y * val[q].y : -1.0f;
-            if (m2 > best) {
-                best = m2;
-                c = i;
-            }
-        }
-        warp_argmax(best, c);
+        float best = coli ? val.x * val.x + val.y * val.y : -1.0f, d0 = 0.0f, d1 = 0.0f;
+        int c = t;
+        cta_argmax<false>(best, c, d0, d1, slotA);
         if (!(best > 1e-30f)) {
-            // the residual row vanished: take the next unused row instead
-            if ((r & 31) == lane) used |= 1u << (r >> 5);
+            // the residual row vanished: take the lowest unused row instead
+            if (t == r) used = true;
             if (++zero_rows > kAcaMaxZeroRows) break;
-            int nr_ = 1 << 30;
-#pragma unroll
-            for (int q = 7; q >= 0; --q)
-                if (!((used >> q) & 1u)) nr_ = lane + 32 * q;
-#pragma unroll
-            for (int off2 = 16; off2 > 0; off2 >>= 1) nr_ = min(nr_, __shfl_xor_sync(0xffffffffu, nr_, off2));
-            if (nr_ >= kTile) break;
-            r = nr_;
+            float f = used ? -1.0f : 1.0f;
+            int nr = t;
+            cta_argmax<false>(f, nr, d0, d1, slotB);
+            if (f < 0.0f) break;
+            r = nr;
             continue;
         }
-        // pivot value from the owner lane of column c
-        float2 pv = val[0];
-#pragma unroll
-        for (int q = 1; q < 8; ++q)
-            if ((c >> 5) == q) pv = val[q];
-        pv.x = __shfl_sync(0xffffffffu, pv.x, c & 31);
-        pv.y = __shfl_sync(0xffffffffu, pv.y, c & 31);
+        // ---- publish V[m][c], m < k, and the pivot
+        if (t == c) {
+            ACA_REG_LOOP(k, sv[m] = vr[m]);
+            for (int m = kAcaRegRanks; m < k; ++m) sv[m] = Vb[m * kTile + c];
+            sv[kLrRankLimit] = val;
+        }
+        __syncthreads();
+        const float2 pv = sv[kLrRankLimit];
         const float inv = 1.0f / (pv.x * pv.x + pv.y * pv.y);
-        float nv2 = 0.0f;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const float2 vv = make_float2((val[q].x * pv.x + val[q].y * pv.y) * inv,
-                                          (val[q].y * pv.x - val[q].x * pv.y) * inv);
-            Vb[k * kTile + lane + 32 * q] = vv;
-            nv2 += vv.x * vv.x + vv.y * vv.y;
+        const float2 vv = coli ? make_float2((val.x * pv.x + val.y * pv.y) * inv, (val.y * pv.x - val.x * pv.y) * inv)
+                               : z2;
+        Vb[k * kTile + t] = vv;
+        ACA_REG_SET(k, vr[m] = vv);
+        // ---- residual column c, entry (t, c)
+        float2 uu = z2;
+        if (rowj) {
+            const bool bit = bc == kFlagBits ? ((bw[(long long)(c >> 5) * pitch + t] >> (c & 31)) & 1u) : true;
+            uu = lr_entry<ATT>(a, bc, bit, __ldg(PI + c), __ldg(NI + c), pj, qj);
+            ACA_REG_LOOP(k, uu = csub_mul(uu, ur[m], sv[m]));
+            for (int m = kAcaRegRanks; m < k; ++m) uu = csub_mul(uu, Ub[m * kTile + t], sv[m]);
         }
-        // ---- residual column c over the rows
-        const float4 pc = __ldg(PI + c), nc = __ldg(NI + c);
-        const uint32_t *cw = bw + (long long)(c >> 5) * a.mask.pitch;
-        float2 uu[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int j = lane + 32 * q;
-            const bool bit = bc == kFlagBits && j < nj ? ((cw[j] >> (c & 31)) & 1u) : true;
-            uu[q] = j < nj ? lr_entry<ATT>(a, bc, bit, pc, nc, __ldg(PJ + j), __ldg(NJ + j)) : make_float2(0.0f, 0.0f);
-        }
-#pragma unroll 4
-        for (int m = 0; m < k; ++m) {
-            const float2 vc = Vb[m * kTile + c];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const float2 um = Ub[m * kTile + lane + 32 * q];
-                uu[q].x -= um.x * vc.x - um.y * vc.y;
-                uu[q].y -= um.x * vc.y + um.y * vc.x;
-            }
-        }
-        float nu2 = 0.0f;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            Ub[k * kTile + lane + 32 * q] = uu[q];
-            nu2 += uu[q].x * uu[q].x + uu[q].y * uu[q].y;
-        }
-        nu2 = warp_sum(nu2);
-        nv2 = warp_sum(nv2);
+        Ub[k * kTile + t] = uu;
+        ACA_REG_SET(k, ur[m] = uu);
+        if (t == r) used = true;
+        // ---- norms and the next pivot row: the largest residual-column entry among unused rows
+        float nu2 = uu.x * uu.x + uu.y * uu.y, nv2 = vv.x * vv.x + vv.y * vv.y;
+        float bn = used ? -1.0f : nu2;
+        int nr = t;
+        cta_argmax<true>(bn, nr, nu2, nv2, slotB);
         norm2 += nu2 * nv2;
         ++k;
-        __syncwarp();  // U and V column k-1 visible to every lane
         if (nu2 * nv2 <= tol * tol * norm2) break;
-        if ((r & 31) == lane) used |= 1u << (r >> 5);
-        // next pivot row: largest residual-column entry among unused rows
-        best = -1.0f;
-        int nr_ = 0;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const float m2 = ((used >> q) & 1u) ? -1.0f : uu[q].x * uu[q].x + uu[q].y * uu[q].y;
-            if (m2 > best) {
-                best = m2;
-                nr_ = lane + 32 * q;
-            }
-        }
-        warp_argmax(best, nr_);
-        if (best < 0.0f) break;  // every row taken
-        r = nr_;
+        if (bn < 0.0f) break;  // every row taken
+        r = nr;
     }
-    // ---- the exact entries judge the approximation (same warp, factors still
-    // in L1/L2): every row once at a hashed column, every column once at a
-    // hashed row; relative RMS error against the sampled entries' RMS
+    // ---- the exact entries judge the approximation: every row once at a
+    // hashed column, every column once at a hashed row; relative RMS error
+    // against the sampled entries' RMS
     float e2 = 0.0f, x2 = 0.0f;
     const bool converged = k > 0 && k < K;
+    __syncthreads();  // every factor entry written to U and V is visible; the slots are free
     if (converged) {
-        __syncwarp();
-#pragma unroll 1
-        for (int q = 0; q < 16; ++q) {
-            const int s = lane + 32 * q;  // sample 0..511
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+            const int s = t + kTile * h2;  // sample 0..511
             unsigned h = (unsigned)b * 2654435761u + (unsigned)s * 40503u + 12345u;
             h ^= h >> 13;
             h *= 0x5bd1e995u;
             h ^= h >> 15;
-            const int jj = s < kTile ? s : (int)(h & 255u), ii = s < kTile ? (int)(h & 255u) : s - kTile;
+            const int jj = h2 == 0 ? t : (int)(h & 255u), ii = h2 == 0 ? (int)(h & 255u) : t;
             if (ii < ni && jj < nj) {
-                const bool bit =
-                    bc == kFlagBits ? ((bw[(long long)(ii >> 5) * a.mask.pitch + jj] >> (ii & 31)) & 1u) : true;
-                const float2 ex = lr_entry<ATT>(a, bc, bit, __ldg(PI + ii), __ldg(NI + ii), __ldg(PJ + jj),
-                                                __ldg(NJ + jj));
-                float ar = 0.0f, ai = 0.0f;
-#pragma unroll 4
-                for (int m = 0; m < k; ++m) {
-                    const float2 u = Ub[m * kTile + jj], v = Vb[m * kTile + ii];
-                    ar += u.x * v.x - u.y * v.y;
-                    ai += u.x * v.y + u.y * v.x;
-                }
-                e2 += (ex.x - ar) * (ex.x - ar) + (ex.y - ai) * (ex.y - ai);
+                const bool bit = bc == kFlagBits ? ((bw[(long long)(ii >> 5) * pitch + jj] >> (ii & 31)) & 1u) : true;
+                const float2 ex = lr_entry<ATT>(a, bc, bit, h2 == 0 ? __ldg(PI + ii) : pi, h2 == 0 ? __ldg(NI + ii) : qi,
+                                                h2 == 0 ? pj : __ldg(PJ + jj), h2 == 0 ? qj : __ldg(NJ + jj));
+                float2 ap = z2;  // minus the approximation
+                if (h2 == 0)
+                    ACA_REG_LOOP(k, ap = csub_mul(ap, ur[m], Vb[m * kTile + ii]));
+                else
+                    ACA_REG_LOOP(k, ap = csub_mul(ap, Ub[m * kTile + jj], vr[m]));
+                for (int m = kAcaRegRanks; m < k; ++m) ap = csub_mul(ap, Ub[m * kTile + jj], Vb[m * kTile + ii]);
+                e2 += (ex.x + ap.x) * (ex.x + ap.x) + (ex.y + ap.y) * (ex.y + ap.y);
                 x2 += ex.x * ex.x + ex.y * ex.y;
             }
         }
-        e2 = warp_sum(e2);
-        x2 = warp_sum(x2);
     }
-    if (lane == 0) {
+    {
+        float f = 0.0f;
+        int fi = 0;
+        cta_argmax<true>(f, fi, e2, x2, slotA);
+    }
+    if (t == 0) {
         const float rel = x2 > 0.0f ? sqrtf(e2 / x2) : (e2 > 0.0f ? 1.0f : 0.0f);
         rank[b] = converged && rel <= limit ? k : -1;
         fro[b] = sqrtf(norm2);
@@ -1911,12 +1974,12 @@ void launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const 
                 cudaStream_t s)
 {
     if (nblocks <= 0) return;
-    const unsigned grid = (unsigned)((nblocks + kAcaWarps - 1) / kAcaWarps);
+    const unsigned grid = (unsigned)nblocks;
     if (a.ka != 0.0f) {
-        k_aca<true><<<grid, 32 * kAcaWarps, 0, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro,
+        k_aca<true><<<grid, kTile, 0, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro,
                                                      err);
     } else {
-        k_aca<false><<<grid, 32 * kAcaWarps, 0, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro,
+        k_aca<false><<<grid, kTile, 0, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro,
                                                       err);
     }
 }
