@@ -314,6 +314,105 @@ def e2e_path(api, cfg, args, world, pairs_step):
             "d2h_bytes_per_step": int(d2h), "s_per_step": round(e2e_s, 4)}
 
 
+def batch_leg(args, flush, rank):
+    """The many-source, many-frequency batch (16 seeded scenes, 64 arc
+    positions as sources and receivers, 8 frequencies): device time of the
+    captured run graph (CUDA events inside the graph, on the plan's stream),
+    L2 flushed between runs; e2e = plan + run + result read-back + free
+    through the C ABI from host buffers; error vs the FP64 oracle on sampled
+    items and sources (rank 0)."""
+    import torch
+    from sonar_render_gb300 import batch, scenes
+    cfg = scenes.batch_config(0)
+    args_b = (cfg["scenes"], cfg["sources"], cfg["receivers"], cfg["freqs"], cfg["cp"], cfg["attenuation"],
+              cfg["per_wavelength"])
+    t0 = time.perf_counter()
+    plan = batch.Plan(*args_b)
+    plan_s = time.perf_counter() - t0
+    for _ in range(max(args.warmup, 1)):
+        plan.run(copy=False)
+    dev = []
+    parts = {"vis_ms": [], "gemm_ms": [], "reduce_ms": []}
+    for _ in range(max(args.steps, 1)):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        plan.run(copy=False)
+        st = plan.stats()
+        for k in parts:
+            parts[k].append(st[k])
+        dev.append(st["vis_ms"] + st["gemm_ms"] + st["reduce_ms"])
+    out = plan.run()
+    st = plan.stats()
+    ms = statistics.median(dev)
+    pairs = st["pairs"]
+    # e2e: the one-shot entry point from host buffers (fragmentation on the
+    # host, uploads, tuning from the process cache, graph, run, read-back)
+    e2e = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        batch.run_batch(*args_b)
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = min(e2e)
+    nfrag = st["fragments"]
+    h2d = int(nfrag * (3 * 16 + 4) + sum(t.nbytes for t in cfg["scenes"]))
+    d2h = int(out.size * 16)
+    err = None
+    if rank == 0:
+        err = batch_error(cfg, out, st)
+    # tensor-core work of the run: 3 split products x 2 (real embedding)
+    # x 2 flop per MAC over the 128 x 64 x (2 K) products
+    flops = 3 * 2 * 128 * 64 * 2 * nfrag
+    res = {"workload": cfg["name"], "items": st["items"], "fragments": nfrag, "pairs_per_run": pairs,
+           "value": pairs / (ms * 1e-3), "unit": UNIT, "ms_per_run": round(ms, 4),
+           "kernel_ms": {k: round(statistics.median(v), 4) for k, v in parts.items()},
+           "tensor_tflops_achieved": round(flops / (statistics.median(parts["gemm_ms"]) * 1e-3) / 1e12, 2),
+           "green_evaluations_per_run": int(nfrag * (st["receivers"] + st["sources"])),
+           "tuning": st["tuning"], "plan_s": round(plan_s, 3), "convex_scenes": st["convex_scenes"],
+           "e2e": {"value": pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                   "s_per_step": round(e2e_s, 4)},
+           "rel_err_vs_fp64": err, "dtype": "split bf16 x3, fp32 accumulate, fp64 reduce",
+           "l2": "flushed between runs (256 MB write)"}
+    plan.close()
+    return res
+
+
+def batch_error(cfg, out, st):
+    """Relative L2 error of sampled (scene, frequency) items, 4 sources each,
+    against the FP64 oracle's per-source runs."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    try:
+        nf = len(cfg["freqs"])
+        nfr = st["item_fragments"]
+        rng = np.random.default_rng(11)
+        # the items with the fewest fragments above 1,000 (the oracle is serial per source)
+        order = [i for i in np.argsort(nfr) if nfr[i] >= 1000][:3]
+        errs = {}
+        for it in order:
+            s, k = int(it) // nf, int(it) % nf
+            f = float(cfg["freqs"][k])
+            delta = float(np.float32(cfg["cp"]) / np.float32(f) / np.float32(cfg["per_wavelength"]))
+            qs = np.sort(rng.choice(len(cfg["sources"]), 4, replace=False))
+            ref = np.zeros((len(cfg["receivers"]), len(qs)), np.complex128)
+            for c, q in enumerate(qs):
+                o = O.Oracle()
+                o.set_initial_conditions(cfg["cp"], f, cfg["attenuation"])
+                o.load_geometry(cfg["scenes"][s], 0, delta)
+                o.load_source_points(cfg["sources"][q:q + 1])
+                o.load_field_points(cfg["receivers"])
+                o.render()
+                o.project_sources(False)
+                o.project_field_points()
+                ref[:, c] = o.field_points()
+                o.close()
+            got = out[s, k][:, qs]
+            errs["scene%d_%s_%.0fHz_%dfrag" % (s, cfg["kinds"][s], f, nfr[it])] = float(
+                np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        return errs
+    except Exception as ex:
+        return {"failed": str(ex)}
+
+
 def run_gb300(args):
     import torch
     import torch.distributed as dist
@@ -372,6 +471,7 @@ def run_gb300(args):
                   "value": pairs_step * args.steps * world / (total_ms * 1e-3), "pairs_step": pairs_step,
                   "kernels_ms_per_step": {k: round(v, 4) for k, v in kernel_times(stats, args.steps).items()},
                   "launches_per_step": stats["launches"] / max(args.steps, 1)}
+    batch_res = batch_leg(args, flush, rank) if args.batch else None
     f2f_plain = [h for h in res.get("plain", res[modes[0]])["stats"]["hops"] if h["hop"] == 2]
     roof_sym, _ = sym_roofline(api, f2f_plain)
 
@@ -442,6 +542,7 @@ def run_gb300(args):
         "mask_block_classes": mask_classes,
         "cpu_baseline": cpu, "e2e": H["e2e"], "clocks": H["clocks"], "gpu_launches": int(H["launches_per_step"] * args.steps),
         "rel_err_vs_fp64": errs.get(head), "grazing": errs.get("grazing"),
+        "batch_config": batch_res,
     }
     if head == "compressed":
         line["rel_err_compressed_vs_plain"] = errs.get("compressed_vs_plain_all_fragments")
@@ -602,6 +703,8 @@ def main():
     ap.add_argument("--select", type=int, default=2,
                     help="compressed blocks: 0 separation rule, 1 every interacting block, 2 the trained network")
     ap.add_argument("--train-epochs", type=int, default=40)
+    ap.add_argument("--batch", type=int, default=1,
+                    help="also run the many-source, many-frequency batch configuration (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

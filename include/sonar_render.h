@@ -190,6 +190,41 @@ int sonar_mlp_predict(const float *X, int n, float *out);
  * compressed bounce.  Returns n; copies when cap >= n. */
 long long sonar_get_block_samples(float *X, float *y, long long cap);
 
+/* Many sources, receivers, frequencies and scenes at once (the reference's
+ * run scripts loop over these on the host, one render per source and
+ * frequency: load_source_points / set_initial_conditions /
+ * ProjectSrcPointsToObjects / ProjectTargetToFieldPoints /
+ * GetFieldPointPressures, src/python_interface.cpp:21-90).  For every scene s
+ * (triangles tris[9*scene_tri_off[s] .. 9*scene_tri_off[s+1]), all of them
+ * target objects), frequency f (fragment size cp / f / per_wavelength, k as
+ * set_initial_conditions computes it), receiver p and source q, out holds the
+ * field-point pressure at p when source q alone radiates with unit pressure:
+ * the source hop onto every fragment cell then the readout of the target
+ * fragments, both shadowed like the reference's.  Layout: out[((s*nfreq + f)
+ * * nrx + p) * nsrc + q] as 2 doubles (re, im).  At most 64 sources and 64
+ * receivers.
+ *
+ * sonar_batch_plan fragments every (scene, frequency) item on the host,
+ * uploads it, times the candidate tile shapes and captures the run as a CUDA
+ * graph; it returns a plan id (> 0) or a negative code.  sonar_batch_run
+ * replays the graph (interaction masks, one persistent tensor-core launch,
+ * reduction) and copies the result into out (NULL: leave it on the device).
+ * sonar_batch_stats writes JSON (items, fragments, credited pairs, kernel
+ * times of the last run, the tuning chosen and every candidate's time) and
+ * returns its length.  sonar_batch_stream gives the plan's cudaStream_t.
+ * sonar_run_batch = plan, run, free.  Plans are independent of the
+ * single-scene model above.  Return 0 or a negative code (sonar_last_error). */
+long long sonar_batch_plan(const float *tris, const int *scene_tri_off, int nscenes, const float *src_xyz, int nsrc,
+                           const float *rx_xyz, int nrx, const float *freqs, int nfreq, float cp, float attenuation,
+                           float per_wavelength);
+int sonar_batch_run(long long plan, double *out);
+int sonar_batch_stats(long long plan, char *json, int cap);
+int sonar_batch_stream(long long plan, void **stream);
+int sonar_batch_free(long long plan);
+int sonar_run_batch(const float *tris, const int *scene_tri_off, int nscenes, const float *src_xyz, int nsrc,
+                    const float *rx_xyz, int nrx, const float *freqs, int nfreq, float cp, float attenuation,
+                    float per_wavelength, double *out);
+
 /* Fragment -> field-point readout that allocates no memory.  No counterpart in
  * the reference: it exists for callers that cannot call cudaMalloc while they
  * run (a host framework that owns all device memory through its own pool, a

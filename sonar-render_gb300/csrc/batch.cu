@@ -1,0 +1,452 @@
+// batch.cu -- many sources, receivers, frequencies and scenes in one launch.
+//
+// The reference answers "what does receiver p hear when source q radiates"
+// one source at a time: load_source_points({q}), ProjectSrcPointsToObjects
+// (source -> every fragment cell, src/OptiX.cu:35-110) and
+// ProjectTargetToFieldPoints (every fragment -> every field point,
+// src/OptiX.cu:112-190).  For S sources and R receivers over N fragments
+// that is S * (N + N * R) Green's function evaluations, and the readout
+// kernel G(p, n) = A_n cos_scat(n -> p) G(r_pn) is recomputed for every
+// source although it does not depend on it.
+//
+// Here the two hops of one (scene, frequency) item become one complex
+// matrix product
+//     out[p][q] = sum_n  G(p, n) * Pinc(n, q),
+//     Pinc(n, q) = cos_inc(q -> n) e^{ikr}/r  (unit source pressure),
+// with both factors materialised tile by tile in shared memory (R + S
+// evaluations per fragment instead of S (1 + R)) and contracted on the
+// tensor cores:
+//   * complex -> real: D (128 x 64) = [[Gr, -Gi], [Gi, Gr]] (128 x 2K) times
+//     [Pr; Pi] (2K x 64): rows 0..63 of D are Re out, rows 64..127 Im out;
+//   * split BF16: every FP32 value x = hi + lo with hi = bf16(x),
+//     lo = bf16(x - hi); D += Ahi Bhi + Ahi Blo + Alo Bhi (relative error of
+//     a product about 2^-16), accumulated in FP32 in tensor memory;
+//   * tcgen05.mma (kind::f16, M = 128, N = 64, K = 16) issued by one thread,
+//     operands in the no-swizzle K-major canonical layout (8-row x 16-byte
+//     core matrices), completion tracked by tcgen05.commit on an mbarrier per
+//     operand stage (two stages: the next tile is generated while the tensor
+//     core consumes the previous one);
+//   * the accumulator is read back with tcgen05.ld at the end of each
+//     segment (at most kBatchSegChunks chunks, so that an FP32 accumulation
+//     never spans more than a few thousand fragments) into FP32 partials
+//     that k_batch_reduce adds per item in a fixed order in FP64.
+// One persistent launch covers every chunk of every item: CTA b processes a
+// contiguous range of the global chunk list (balanced over the grid), cut
+// into segments at item boundaries.
+//
+// Visibility: per fragment one 64-bit word per hop (k_batch_vis: the cosine
+// gates and the shadow test of every pair) gates the entries.
+#include "sonar_internal.h"
+
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+namespace sonar {
+namespace {
+
+constexpr float kInv4PiB = 0.0795774715459476679f;
+constexpr float kTwoPiB = 6.28318530717958647692f;
+constexpr int kBatchThreads = 256;
+constexpr uint32_t kTmemCols = 64;          // FP32 accumulator: 128 lanes x 64 columns
+constexpr long long kWaitLimit = 1LL << 20;  // mbarrier polls before a CTA gives up
+
+// ---------------------------------------------------------------- PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the completion of the phase with the given parity; false
+// when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    for (long long i = 0; i < kWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// D[tmem] (+)= A[smem] * B[smem]^T, both K-major, BF16 in, FP32 accumulate
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "setp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+// arrive on bar once every tcgen05 operation issued so far by this thread completed
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// 32 TMEM lanes (this warp's quarter) x 16 consecutive 32-bit columns
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+// Shared-memory matrix descriptor, no swizzle: start address, leading byte
+// offset (between the two core matrices along K), stride byte offset
+// (between 8-row groups), descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N = 64, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(64 >> 3) << 17) |
+                            ((uint32_t)(128 >> 4) << 24);
+
+// ---------------------------------------------------------------- the two kernels of an item
+// Phase k r as a fraction of a turn: r * (k / 2 pi) as an exact two-float
+// product plus the low part of k / 2 pi, the integer turns removed exactly.
+__device__ __forceinline__ void phase(float r, float k2hi, float k2lo, float &sn, float &cs)
+{
+    const float th = __fmul_rn(r, k2hi);
+    const float tl = fmaf(r, k2lo, fmaf(r, k2hi, -th));
+    const float frac = (th - rintf(th)) + tl;
+    __sincosf(frac * kTwoPiB, &sn, &cs);
+}
+
+__device__ __forceinline__ float dist(float vx, float vy, float vz, float &rinv)
+{
+    // |v|^2 rounded like the reference's dot; r within an ulp of the rounded root
+    const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
+    rinv = rsqrtf(r2);
+    const float r0 = r2 * rinv;
+    return fmaf(fmaf(-r0, r0, r2), 0.5f * rinv, r0);
+}
+
+// Readout entry G(p, n) = A_n cos_scat G(r), G = -e^{ikr}/(4 pi) (ik/r) + 1/r^2
+// (src/OptiX.cu:150-186; cos_scat from the fragment's facet normal).
+template <bool ATT>
+__device__ __forceinline__ float2 readout_entry(const BatchItem &it, float4 f, float4 nf, float3 p)
+{
+    const float vx = __fsub_rn(p.x, f.x), vy = __fsub_rn(p.y, f.y), vz = __fsub_rn(p.z, f.z);
+    float rinv;
+    const float r = dist(vx, vy, vz, rinv);
+    float sn, cs;
+    phase(r, it.k2hi, it.k2lo, sn, cs);
+    const float rinv2 = rinv * rinv;
+    float gr, gi;
+    if (ATT) {
+        const float amp = rinv * kInv4PiB * __expf(-it.ka * r);
+        gr = fmaf(amp, fmaf(it.ka, cs, it.kr * sn), rinv2);
+        gi = amp * fmaf(it.ka, sn, -it.kr * cs);
+    } else {
+        const float ampk = rinv * it.kr4pi;
+        gr = fmaf(ampk, sn, rinv2);
+        gi = -ampk * cs;
+    }
+    const float w = (vx * nf.x + vy * nf.y + vz * nf.z) * rinv * f.w;  // cos_scat A_n
+    return make_float2(gr * w, gi * w);
+}
+
+// Incident entry Pinc(n, q) = cos_inc e^{ikr} / r at the fragment's
+// source-hop centroid (src/OptiX.cu:45-106; unit source pressure).
+template <bool ATT>
+__device__ __forceinline__ float2 incident_entry(const BatchItem &it, float3 q, float4 s, float4 nf)
+{
+    const float vx = __fsub_rn(s.x, q.x), vy = __fsub_rn(s.y, q.y), vz = __fsub_rn(s.z, q.z);
+    float rinv;
+    const float r = dist(vx, vy, vz, rinv);
+    float sn, cs;
+    phase(r, it.k2hi, it.k2lo, sn, cs);
+    float amp = -(vx * nf.x + vy * nf.y + vz * nf.z) * rinv * rinv;  // cos_inc / r
+    if (ATT) amp *= __expf(-it.ka * r);
+    return make_float2(amp * cs, amp * sn);
+}
+
+// two FP32 values -> (hi, lo) BF16 pairs packed for a 16-byte row store
+__device__ __forceinline__ void split8(const float *x, uint4 &hi, uint4 &lo)
+{
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const __nv_bfloat16 h0 = __float2bfloat16_rn(x[2 * q]), h1 = __float2bfloat16_rn(x[2 * q + 1]);
+        const __nv_bfloat16 l0 = __float2bfloat16_rn(x[2 * q] - __bfloat162float(h0));
+        const __nv_bfloat16 l1 = __float2bfloat16_rn(x[2 * q + 1] - __bfloat162float(h1));
+        h[q] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+        l[q] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+__device__ __forceinline__ void st16(uint8_t *p, uint4 v) { *reinterpret_cast<uint4 *>(p) = v; }
+
+// Operand stage of KC fragments: A (128 rows x 2KC) hi and lo, B (64 rows x
+// 2KC) hi and lo, each row-group/k-group core matrix 128 bytes; element
+// (row, k) of A at (k / 8) * 2048 + row * 16 + (k % 8) * 2.
+template <int KC>
+struct Stage {
+    static constexpr int kA = 128 * 2 * KC * 2;  // bytes of one A copy (hi or lo)
+    static constexpr int kB = 64 * 2 * KC * 2;
+    static constexpr int kBytes = 2 * kA + 2 * kB;
+    static constexpr int kLboA = 128 * 16, kLboB = 64 * 16;
+};
+
+template <int KC, bool ATT>
+__device__ __forceinline__ void generate(uint8_t *st, const BatchArgs &a, const BatchItem &it, int chunk, int tid,
+                                         float3 prx, bool rx_ok, float3 psrc, bool src_ok)
+{
+    using S = Stage<KC>;
+    uint8_t *Ahi = st, *Alo = st + S::kA, *Bhi = st + 2 * S::kA, *Blo = st + 2 * S::kA + S::kB;
+    const int row = tid & 63;  // receiver (A) or source (B)
+    const int n0 = chunk * KC;
+#pragma unroll 1
+    for (int q = tid >> 6; q < KC / 8; q += kBatchThreads / 64) {
+        const int nb = n0 + 8 * q;  // first fragment of this k-group (item-relative)
+        float gr[8], gi[8], pr[8], pi[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int n = nb + j;
+            gr[j] = gi[j] = pr[j] = pi[j] = 0.0f;
+            if (n < it.nfrag) {
+                const long long g = (long long)it.frag0 + n;
+                const uint4 vw = __ldg(a.vis + g);  // receiver bits (x, y), source bits (z, w)
+                const float4 nf = __ldg(a.frag_n + g);
+                if (rx_ok && (((row < 32 ? vw.x : vw.y) >> (row & 31)) & 1u)) {
+                    const float2 v = readout_entry<ATT>(it, __ldg(a.frag_pos + g), nf, prx);
+                    gr[j] = v.x;
+                    gi[j] = v.y;
+                }
+                if (src_ok && (((row < 32 ? vw.z : vw.w) >> (row & 31)) & 1u)) {
+                    const float2 v = incident_entry<ATT>(it, psrc, __ldg(a.frag_spos + g), nf);
+                    pr[j] = v.x;
+                    pi[j] = v.y;
+                }
+            }
+        }
+        uint4 h, l;
+        float ngi[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) ngi[j] = -gi[j];
+        const int kr0 = q, ki0 = KC / 8 + q;  // k-groups of the real and imaginary halves
+        // A row p:      [ Gr | -Gi ];  A row 64 + p: [ Gi | Gr ]
+        split8(gr, h, l);
+        st16(Ahi + kr0 * S::kLboA + row * 16, h);
+        st16(Alo + kr0 * S::kLboA + row * 16, l);
+        st16(Ahi + ki0 * S::kLboA + (64 + row) * 16, h);
+        st16(Alo + ki0 * S::kLboA + (64 + row) * 16, l);
+        split8(ngi, h, l);
+        st16(Ahi + ki0 * S::kLboA + row * 16, h);
+        st16(Alo + ki0 * S::kLboA + row * 16, l);
+        split8(gi, h, l);
+        st16(Ahi + kr0 * S::kLboA + (64 + row) * 16, h);
+        st16(Alo + kr0 * S::kLboA + (64 + row) * 16, l);
+        // B row q_src: [ Pr | Pi ]
+        split8(pr, h, l);
+        st16(Bhi + kr0 * S::kLboB + row * 16, h);
+        st16(Blo + kr0 * S::kLboB + row * 16, l);
+        split8(pi, h, l);
+        st16(Bhi + ki0 * S::kLboB + row * 16, h);
+        st16(Blo + ki0 * S::kLboB + row * 16, l);
+    }
+}
+
+template <int KC, bool ATT>
+__global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
+{
+    using S = Stage<KC>;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) tmem_alloc(&tmem_base, kTmemCols);
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const int row = tid & 63;
+    const bool rx_ok = row < a.nrx, src_ok = row < a.nsrc;
+    const float4 rx4 = rx_ok ? a.rx[row] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float4 sq4 = src_ok ? a.src[row] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float3 prx = make_float3(rx4.x, rx4.y, rx4.z), psrc = make_float3(sq4.x, sq4.y, sq4.z);
+    const uint32_t sbase = smem_u32(smem);
+    uint32_t commits0 = 0, commits1 = 0;  // commits issued on each stage's barrier
+    int local = 0;                        // chunks this CTA has generated
+    bool ok = true;
+    const int g0 = a.cta_seg[blockIdx.x], g1 = a.cta_seg[blockIdx.x + 1];
+    for (int sg = g0; sg < g1 && ok; ++sg) {
+        const int4 seg = a.segs[sg];
+        const BatchItem it = a.items[seg.x];
+        for (int cc = 0; cc < seg.z && ok; ++cc, ++local) {
+            const int st = local & 1;
+            // the stage is free once the MMAs that read it (two chunks back) completed
+            if (local >= 2) {
+                const uint32_t c = st ? commits1 : commits0;
+                const bool done = mbar_wait(&bar[st], (c - 1) & 1u);
+                ok = __syncthreads_and(done);
+                if (!ok) break;
+            }
+            generate<KC, ATT>(smem + st * S::kBytes, a, it, seg.y + cc, tid, prx, rx_ok, psrc, src_ok);
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t sA = sbase + st * S::kBytes, sB = sA + 2 * S::kA;
+#pragma unroll
+                for (int ks = 0; ks < 2 * KC / 16; ++ks) {
+                    const uint64_t ahi = sdesc(sA + ks * 2 * S::kLboA, S::kLboA, 128);
+                    const uint64_t alo = sdesc(sA + S::kA + ks * 2 * S::kLboA, S::kLboA, 128);
+                    const uint64_t bhi = sdesc(sB + ks * 2 * S::kLboB, S::kLboB, 128);
+                    const uint64_t blo = sdesc(sB + S::kB + ks * 2 * S::kLboB, S::kLboB, 128);
+                    mma_bf16(tmem, ahi, bhi, kIdesc, (cc > 0 || ks > 0) ? 1u : 0u);
+                    mma_bf16(tmem, ahi, blo, kIdesc, 1u);
+                    mma_bf16(tmem, alo, bhi, kIdesc, 1u);
+                }
+                mma_commit(&bar[st]);
+            }
+            if (st) ++commits1; else ++commits0;
+        }
+        if (!ok) break;
+        // ---- segment end: the accumulator -> FP32 partial [128][64]
+        {
+            const int st = (local - 1) & 1;
+            const uint32_t c = st ? commits1 : commits0;
+            const bool done = mbar_wait(&bar[st], (c - 1) & 1u);
+            ok = __syncthreads_and(done);
+            if (!ok) break;
+        }
+        tc_fence_after();
+        {
+            const int quarter = warp & 3, half = warp >> 2;
+            const int drow = quarter * 32 + lane;
+            float v[32];
+            const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(half * 32);
+            tmem_ld16(taddr, v);
+            tmem_ld16(taddr + 16, v + 16);
+            float4 *out = reinterpret_cast<float4 *>(a.partial + ((long long)sg * 128 + drow) * 64 + half * 32);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) out[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (!ok && tid == 0) atomicExch(a.status, 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+}
+
+// out[item][p][q] = sum over the item's segments, fixed order, FP64
+__global__ void __launch_bounds__(256) k_batch_reduce(const float *partial, const int *item_seg_off,
+                                                      const int *item_segs, int nrx, int nsrc, double2 *out)
+{
+    const int item = blockIdx.x;
+    const int s0 = item_seg_off[item], s1 = item_seg_off[item + 1];
+    for (int e = threadIdx.x; e < nrx * nsrc; e += blockDim.x) {
+        const int p = e / nsrc, q = e - p * nsrc;
+        double re = 0.0, im = 0.0;
+        for (int s = s0; s < s1; ++s) {
+            const float *P = partial + (long long)item_segs[s] * 128 * 64;
+            re += (double)P[p * 64 + q];
+            im += (double)P[(64 + p) * 64 + q];
+        }
+        out[(long long)item * nrx * nsrc + e] = make_double2(re, im);
+    }
+}
+
+}  // namespace
+
+size_t batch_smem_bytes(int kc)
+{
+    return kc == 64 ? (size_t)2 * Stage<64>::kBytes : (size_t)2 * Stage<32>::kBytes;
+}
+
+cudaError_t batch_prepare()
+{
+    cudaError_t e = cudaFuncSetAttribute(k_batch<32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)batch_smem_bytes(32));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)batch_smem_bytes(32));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch<64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)batch_smem_bytes(64));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch<64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)batch_smem_bytes(64));
+    return e;
+}
+
+void launch_batch(const BatchArgs &a, int kc, int grid, bool att, cudaStream_t s)
+{
+    const size_t sm = batch_smem_bytes(kc);
+    if (grid <= 0) return;
+    if (kc == 64) {
+        if (att) k_batch<64, true><<<grid, kBatchThreads, sm, s>>>(a);
+        else k_batch<64, false><<<grid, kBatchThreads, sm, s>>>(a);
+    } else {
+        if (att) k_batch<32, true><<<grid, kBatchThreads, sm, s>>>(a);
+        else k_batch<32, false><<<grid, kBatchThreads, sm, s>>>(a);
+    }
+}
+
+void launch_batch_reduce(const float *partial, const int *item_seg_off, const int *item_segs, int nitems, int nrx,
+                         int nsrc, double2 *out, cudaStream_t s)
+{
+    if (nitems > 0) k_batch_reduce<<<nitems, 256, 0, s>>>(partial, item_seg_off, item_segs, nrx, nsrc, out);
+}
+
+}  // namespace sonar

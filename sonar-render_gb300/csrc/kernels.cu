@@ -665,6 +665,70 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
     if (tid == 0) a.mask.flags[fidx] = clear ? kFlagClear : (blk ? kFlagBits : kFlagNone);
 }
 
+// ---------------------------------------------------------------- batch visibility
+// Interaction bits of the two hops of a batch item, per fragment: bit q of
+// the source word when source q -> fragment passes the cos_inc gate and is
+// not shadowed (ray from the source to the source-hop centroid), bit p of
+// the receiver word when fragment -> receiver p passes the cos_scat gate
+// and is not shadowed (ray from the receiver to the readout centroid).  The
+// gates are the reference's exact FP32 decisions (cos_gate).
+//
+// Convex scenes (every vertex on or behind every triangle's plane within
+// 1e-6 (1 + max |coordinate|), checked on the host): a ray from a point in
+// front of the fragment's facet plane stays in front of it up to tmax =
+// r - 1e-3, at least 1e-3 cos from the plane, while every triangle lies on
+// or behind it; no triangle can hold the crossing point.  With a cosine of at
+// least kConvexCos that margin (5e-5 m) exceeds the convexity tolerance and
+// the FP32 rounding of the crossing test, so such pairs need no occlusion
+// test; the others (and every pair of a non-convex scene) walk the BVH.
+constexpr float kConvexCos = 0.05f;
+
+__global__ void __launch_bounds__(kTile) k_batch_vis(BatchVisArgs a)
+{
+    __shared__ float4 sP[2 * kBatchMaxPoints];  // receivers, then sources
+    const int tid = threadIdx.x;
+    for (int q = tid; q < a.nrx + a.nsrc; q += kTile) sP[q] = q < a.nrx ? a.rx[q] : a.src[q - a.nrx];
+    __syncthreads();
+    const long long n = (long long)blockIdx.x * kTile + tid;
+    if (n >= a.nfrag) return;
+    // the item holding fragment n
+    int lo = 0, hi = a.nitems - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.items[mid].frag0 <= n) lo = mid;
+        else hi = mid - 1;
+    }
+    const BatchItem it = a.items[lo];
+    const BvhView bvh = a.bvh[it.scene];
+    const float4 f = a.frag_pos[n], fs = a.frag_spos[n], nf = a.frag_n[n];
+    unsigned long long wrx = 0ull, wsrc = 0ull;
+    for (int p = 0; p < a.nrx; ++p) {
+        const float4 P = sP[p];
+        // readout: v = field point - fragment, cos_scat = dot(v, n) / r (OptiX.cu:150-160)
+        const float vx = __fsub_rn(P.x, f.x), vy = __fsub_rn(P.y, f.y), vz = __fsub_rn(P.z, f.z);
+        const float rinv = rsqrtf(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+        if (!cos_gate(vx, vy, vz, rinv, 1.0f, nf.x, nf.y, nf.z)) continue;
+        const float est = fmaf(vx, nf.x, fmaf(vy, nf.y, vz * nf.z)) * rinv;
+        bool vis = true;
+        if (!(it.convex && est >= kConvexCos))
+            vis = !occluded_full(bvh, make_float3(P.x, P.y, P.z), make_float3(f.x, f.y, f.z));
+        if (vis) wrx |= 1ull << p;
+    }
+    for (int q = 0; q < a.nsrc; ++q) {
+        const float4 P = sP[a.nrx + q];
+        // source hop: v = fragment - source, cos_inc = dot(-v, n) / r (OptiX.cu:60-79)
+        const float vx = __fsub_rn(fs.x, P.x), vy = __fsub_rn(fs.y, P.y), vz = __fsub_rn(fs.z, P.z);
+        const float rinv = rsqrtf(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+        if (!cos_gate(vx, vy, vz, rinv, -1.0f, nf.x, nf.y, nf.z)) continue;
+        const float est = -fmaf(vx, nf.x, fmaf(vy, nf.y, vz * nf.z)) * rinv;
+        bool vis = true;
+        if (!(it.convex && est >= kConvexCos))
+            vis = !occluded_full(bvh, make_float3(P.x, P.y, P.z), make_float3(fs.x, fs.y, fs.z));
+        if (vis) wsrc |= 1ull << q;
+    }
+    a.vis[n] = make_uint4((unsigned)wrx, (unsigned)(wrx >> 32), (unsigned)wsrc, (unsigned)(wsrc >> 32));
+}
+
 // ---------------------------------------------------------------- sums
 struct Dst {
     float px, py, pz;
@@ -1331,52 +1395,51 @@ constexpr int kAcaMaxZeroRows = 48;
 constexpr int kAcaRegRanks = 16;  // factor entries a thread keeps in registers; higher ranks are re-read from global
 constexpr int kAcaWarps = kTile / 32;
 
-// Block-wide argmax of v (ties: lowest index) and, with SUMS, the block-wide
-// sums of s0 and s1.  Every thread receives the result.  One barrier;
-// callers alternate between two slot arrays so that a slot array is never
-// rewritten while a thread may still read it.
-template <bool SUMS>
-__device__ __forceinline__ void cta_argmax(float &v, int &idx, float &s0, float &s1, float4 *slots)
+// Block-wide argmax (ARG) of v over the threads with valid set (ties: lowest
+// index) and block-wide sums (SUMS) of s0 and s1; every thread receives the
+// results (v = -1 when no thread was valid).  The argmax is a shared-memory
+// atomicMax on a 64-bit key (value bits + 1, then the complemented index),
+// which is order-independent; the sums go through one slot per warp, added
+// in warp order (deterministic).  One barrier.  The key must be zero on
+// entry; the caller resets it once every thread has read it.
+template <bool ARG, bool SUMS>
+__device__ __forceinline__ void cta_reduce(float &v, int &idx, bool valid, float &s0, float &s1,
+                                           unsigned long long *key, float2 *sums)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long k = 0ull;
+    if (ARG && valid)
+        k = ((unsigned long long)(__float_as_uint(fmaxf(v, 0.0f)) + 1u) << 32) |
+            (unsigned long long)(0xFFFFFFFFu - (unsigned)idx);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, v, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (ARG) {
+            const unsigned long long ok = __shfl_xor_sync(0xffffffffu, k, o);
+            k = ok > k ? ok : k;
+        }
         if (SUMS) {
             s0 += __shfl_xor_sync(0xffffffffu, s0, o);
             s1 += __shfl_xor_sync(0xffffffffu, s1, o);
         }
-        if (ov > v || (ov == v && oi < idx)) {
-            v = ov;
-            idx = oi;
-        }
     }
-    if (lane == 0) slots[warp] = make_float4(v, __int_as_float(idx), s0, s1);
+    if (lane == 0) {
+        if (ARG && k) atomicMax(key, k);
+        if (SUMS) sums[warp] = make_float2(s0, s1);
+    }
     __syncthreads();
-    float bv = -3.0e38f, t0 = 0.0f, t1 = 0.0f;
-    int bi = 0x7fffffff;
-#pragma unroll
-    for (int q = 0; q < kAcaWarps; ++q) {
-        if (SUMS) {
-            const float4 o = slots[q];
-            t0 += o.z;
-            t1 += o.w;
-            if (o.x > bv || (o.x == bv && __float_as_int(o.y) < bi)) {
-                bv = o.x;
-                bi = __float_as_int(o.y);
-            }
-        } else {
-            const float2 o = *reinterpret_cast<const float2 *>(slots + q);
-            if (o.x > bv || (o.x == bv && __float_as_int(o.y) < bi)) {
-                bv = o.x;
-                bi = __float_as_int(o.y);
-            }
-        }
+    if (ARG) {
+        const unsigned long long w = *key;
+        v = w ? __uint_as_float((unsigned)(w >> 32) - 1u) : -1.0f;
+        idx = (int)(0xFFFFFFFFu - (unsigned)(w & 0xFFFFFFFFull));
     }
-    v = bv;
-    idx = bi;
     if (SUMS) {
+        float t0 = 0.0f, t1 = 0.0f;
+#pragma unroll
+        for (int q = 0; q < kAcaWarps; ++q) {
+            const float2 o = sums[q];
+            t0 += o.x;
+            t1 += o.y;
+        }
         s0 = t0;
         s1 = t1;
     }
@@ -1441,7 +1504,8 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
                                                   const long long *off, int nblocks, float tol, float limit,
                                                   float2 *U, float2 *V, int *rank, float *fro, float *err)
 {
-    __shared__ float4 slotA[kAcaWarps], slotB[kAcaWarps];
+    __shared__ unsigned long long keyA, keyB;  // argmax keys: pivot column / next row, lowest unused row
+    __shared__ float2 sums[kAcaWarps];
     __shared__ float2 su[kLrRankLimit], sv[kLrRankLimit + 1];  // sv[kLrRankLimit]: the pivot
     const int t = threadIdx.x, b = blockIdx.x;
     if (b >= nblocks) return;  // CTA-uniform
@@ -1463,13 +1527,17 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
     bool used = !rowj;  // row t taken (or absent)
     int r = 0, k = 0, zero_rows = 0;
     float norm2 = 0.0f;
+    if (t == 0) keyB = 0ull;
     while (k < K) {
+        // keyA was last read before the previous iteration's second barrier
+        if (t == 0) keyA = 0ull;
         // ---- publish U[r][m], m < k
         if (t == r) {
             ACA_REG_LOOP(k, su[m] = ur[m]);
             for (int m = kAcaRegRanks; m < k; ++m) su[m] = Ub[m * kTile + r];
         }
         __syncthreads();
+        if (t == 0) keyB = 0ull;  // last read before the barrier above
         // ---- residual row r, entry (r, t)
         float2 val = z2;
         if (coli) {
@@ -1478,16 +1546,16 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
             ACA_REG_LOOP(k, val = csub_mul(val, su[m], vr[m]));
             for (int m = kAcaRegRanks; m < k; ++m) val = csub_mul(val, su[m], Vb[m * kTile + t]);
         }
-        float best = coli ? val.x * val.x + val.y * val.y : -1.0f, d0 = 0.0f, d1 = 0.0f;
+        float best = val.x * val.x + val.y * val.y, d0 = 0.0f, d1 = 0.0f;
         int c = t;
-        cta_argmax<false>(best, c, d0, d1, slotA);
+        cta_reduce<true, false>(best, c, coli, d0, d1, &keyA, sums);
         if (!(best > 1e-30f)) {
             // the residual row vanished: take the lowest unused row instead
             if (t == r) used = true;
             if (++zero_rows > kAcaMaxZeroRows) break;
-            float f = used ? -1.0f : 1.0f;
+            float f = 1.0f;
             int nr = t;
-            cta_argmax<false>(f, nr, d0, d1, slotB);
+            cta_reduce<true, false>(f, nr, !used, d0, d1, &keyB, sums);
             if (f < 0.0f) break;
             r = nr;
             continue;
@@ -1518,9 +1586,9 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
         if (t == r) used = true;
         // ---- norms and the next pivot row: the largest residual-column entry among unused rows
         float nu2 = uu.x * uu.x + uu.y * uu.y, nv2 = vv.x * vv.x + vv.y * vv.y;
-        float bn = used ? -1.0f : nu2;
+        float bn = nu2;
         int nr = t;
-        cta_argmax<true>(bn, nr, nu2, nv2, slotB);
+        cta_reduce<true, true>(bn, nr, !used, nu2, nv2, &keyB, sums);
         norm2 += nu2 * nv2;
         ++k;
         if (nu2 * nv2 <= tol * tol * norm2) break;
@@ -1560,7 +1628,7 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
     {
         float f = 0.0f;
         int fi = 0;
-        cta_argmax<true>(f, fi, e2, x2, slotA);
+        cta_reduce<false, true>(f, fi, false, e2, x2, &keyA, sums);
     }
     if (t == 0) {
         const float rel = x2 > 0.0f ? sqrtf(e2 / x2) : (e2 > 0.0f ? 1.0f : 0.0f);
@@ -1909,6 +1977,11 @@ void launch_mask(const MaskArgs &a, cudaStream_t s)
     case HOP_F2F: k_mask<HOP_F2F><<<grid, kTile, 0, s>>>(a); break;
     default: k_mask<HOP_NORESP><<<grid, kTile, 0, s>>>(a); break;
     }
+}
+
+void launch_batch_vis(const BatchVisArgs &a, cudaStream_t s)
+{
+    if (a.nfrag > 0) k_batch_vis<<<(unsigned)((a.nfrag + kTile - 1) / kTile), kTile, 0, s>>>(a);
 }
 
 void launch_sum(const SumArgs &a, cudaStream_t s)

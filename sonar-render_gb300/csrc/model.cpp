@@ -1018,6 +1018,9 @@ int guarded(F &&f)
 bool finite3(const float *p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
 
 }  // namespace
+
+void set_error_message(const std::string &m) { g.err = m; }
+
 }  // namespace sonar
 
 using namespace sonar;

@@ -153,6 +153,46 @@ cudaError_t mlp_predict_dev(const float *dX, int n, float *dY, cudaStream_t s);
 // surface.cu: pressure -> RGBA colour map of the reference's surface textures
 void launch_colour_map(const double2 *P, long long n, float min_db, float max_db, int phase, float4 *out,
                        cudaStream_t s);
+// batch.cu: many (scene, frequency) items, each a source hop from up to 64
+// sources and a readout to up to 64 receivers, contracted on the tensor cores.
+struct BatchItem {
+    int frag0, nfrag;              // the item's fragments [frag0, frag0 + nfrag) of the batch arrays
+    int scene, convex;             // scene index (occluders); 1 when the scene is convex
+    float kr, ka, k2hi, k2lo, kr4pi;
+    int pad[3];
+};
+struct BatchArgs {
+    const BatchItem *items;
+    const int4 *segs;              // (item, first chunk, chunk count, -)
+    const int *cta_seg;            // segments [cta_seg[b], cta_seg[b + 1]) of CTA b
+    const float4 *frag_pos;        // readout centroid (no x shift), area
+    const float4 *frag_spos;       // source-hop centroid (x shift)
+    const float4 *frag_n;          // facet normal
+    const uint4 *vis;              // per fragment: receiver bits (x, y), source bits (z, w)
+    const float4 *rx, *src;        // receivers, sources (at most 64 each)
+    int nrx, nsrc;
+    float *partial;                // [segment][128][64] FP32
+    int *status;                   // set to 1 when a CTA gave up waiting on the tensor core
+};
+// kernels.cu: interaction bits of both batch hops, one thread per fragment
+struct BatchVisArgs {
+    const BatchItem *items;
+    int nitems;
+    long long nfrag;               // fragments of all items
+    const float4 *frag_pos, *frag_spos, *frag_n;
+    const float4 *rx, *src;
+    int nrx, nsrc;
+    const BvhView *bvh;            // per scene
+    uint4 *vis;
+};
+void launch_batch_vis(const BatchVisArgs &a, cudaStream_t s);
+constexpr int kBatchMaxPoints = 64;  // sources and receivers per item
+size_t batch_smem_bytes(int kc);
+cudaError_t batch_prepare();        // dynamic shared-memory limits of the batch kernels (outside stream capture)
+void launch_batch(const BatchArgs &a, int kc, int grid, bool att, cudaStream_t s);
+void launch_batch_reduce(const float *partial, const int *item_seg_off, const int *item_segs, int nitems, int nrx,
+                         int nsrc, double2 *out, cudaStream_t s);
+
 // FP32 FMA rate in FLOP/s (which = 0) or MUFU sine rate in op/s (which = 1)
 // on the current device; < 0 on failure.
 double measure_peak(int which);

@@ -13,6 +13,8 @@ as seeded synthetic inputs of the same shapes and sizes:
                         field plane through the centre
 * ``trihedral_config``  orthogonal trihedral, 1 m legs, 3 bounces at 40 kHz
                         (60 kHz, 2 bounces for the compression workload)
+* ``batch_config``      16 seeded plates, boxes and spheres (2k-200k fragments),
+                        64 arc positions as sources and receivers, 8 frequencies
 
 Mesh helpers mirror the reference's run_scripts/modules/geo.py builders
 (make_rectangle, halve_facets, make_cube, generate_field_points) without
@@ -210,3 +212,43 @@ def trihedral_config(frequency=40e3, bounces=3, n_theta=256, n_phi=256):
     return dict(name="trihedral_1m_%dkHz_%db" % (int(frequency / 1e3), bounces), frequency=frequency,
                 cp=CP_WATER, attenuation=0.0, targets=[(trihedral(1.0), delta_for(frequency))], fields=[],
                 sources=src, field_points=fp, bounces=bounces)
+
+
+def batch_config(seed=0, nscenes=16, npos=64, nfreq=8, n_lo=2000, n_hi=200000, f_lo=5e3, f_hi=40e3):
+    """Seeded batch of scenes for the many-source, many-frequency path.
+
+    ``nscenes`` scenes (plates, boxes and spheres, drawn uniformly) sized so
+    that each has about U[n_lo, n_hi] active fragments at the top frequency
+    (fragment side lambda / 7.5); ``npos`` positions on a 30 m arc in the
+    xz-plane from -60 to +60 degrees, used both as sources and as receivers
+    (monostatic and bistatic pairs); ``nfreq`` frequencies log-spaced from
+    f_lo to f_hi.  The fragment count of a scene scales with f^2 below the top
+    frequency, and every (scene, frequency) is fragmented separately."""
+    rng = np.random.default_rng(seed)
+    d_hi = delta_for(f_hi)
+    scenes, kinds, targets = [], [], []
+    for _ in range(nscenes):
+        kind = ("plate", "box", "sphere")[int(rng.integers(0, 3))]
+        n = float(rng.uniform(n_lo, n_hi))
+        area = n * d_hi * d_hi
+        if kind == "plate":
+            ar = float(rng.uniform(0.5, 2.0))
+            w = math.sqrt(area * ar)
+            t = rectangle(w, area / w)
+            t = rotate(t, "x", float(rng.uniform(-20.0, 20.0)))
+            t = rotate(t, "z", float(rng.uniform(0.0, 180.0)))
+        elif kind == "box":
+            a, b, c = 1.0, float(rng.uniform(0.5, 1.5)), float(rng.uniform(0.5, 1.5))
+            s = math.sqrt(area / (2.0 * (a * b + b * c + c * a)))
+            t = box(a * s, b * s, c * s)
+            t = rotate(t, "y", float(rng.uniform(0.0, 90.0)))
+        else:
+            t = icosphere(3, math.sqrt(area / (4.0 * math.pi)))
+        scenes.append(np.asarray(t, np.float32))
+        kinds.append(kind)
+        targets.append(int(n))
+    pos = arc_xz(30.0, np.linspace(-60.0, 60.0, npos))
+    freqs = np.geomspace(f_lo, f_hi, nfreq).astype(np.float32)
+    return dict(name="batch_%dscenes_%dpos_%dfreq" % (nscenes, npos, nfreq), scenes=scenes, kinds=kinds,
+                target_fragments=targets, sources=pos, receivers=pos, freqs=freqs, cp=CP_WATER, attenuation=0.0,
+                per_wavelength=7.5)

@@ -148,3 +148,38 @@ def test_options(api):
         api.set_option("no_such_option", 1)
     s = api.stats()
     assert "hops" in s
+
+
+@pytest.mark.parametrize("bad", ["too_many_sources", "no_receivers", "zero_frequency", "nan_vertex", "empty_scene",
+                                 "bad_offsets"])
+def test_batch_plan_validates_before_touching_the_gpu(api, bad):
+    """sonar_batch_plan checks every argument before any CUDA call and
+    returns a negative code with a message (no GPU needed to see it)."""
+    from sonar_render_gb300 import batch
+    L = batch._lib()
+    f_, i_ = C.POINTER(C.c_float), C.POINTER(C.c_int)
+    tris = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
+    off = np.array([0, 1], np.int32)
+    pts = np.zeros((65, 3), np.float32)
+    pts[:, 2] = 10.0
+    freqs = np.array([10e3], np.float32)
+    nsrc, nrx = 4, 4
+    if bad == "too_many_sources":
+        nsrc = 65
+    elif bad == "no_receivers":
+        nrx = 0
+    elif bad == "zero_frequency":
+        freqs = np.array([0.0], np.float32)
+    elif bad == "nan_vertex":
+        tris = tris.copy()
+        tris[0, 4] = np.nan
+    elif bad == "empty_scene":
+        off = np.array([0, 0], np.int32)
+    elif bad == "bad_offsets":
+        off = np.array([1, 1], np.int32)
+    r = L.sonar_batch_plan(tris.ctypes.data_as(f_), off.ctypes.data_as(i_), 1, pts.ctypes.data_as(f_), nsrc,
+                           pts.ctypes.data_as(f_), nrx, freqs.ctypes.data_as(f_), 1, C.c_float(1480.0),
+                           C.c_float(0.0), C.c_float(7.5))
+    assert r < 0
+    assert L.sonar_last_error().decode().startswith("sonar_batch_plan")
+    assert L.sonar_batch_run(12345, None) < 0  # unknown plan id

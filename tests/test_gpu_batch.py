@@ -1,0 +1,133 @@
+"""GPU parity of the many-source, many-frequency batch (sonar_batch_*).
+
+Each (scene, frequency, source) column of a batch run must equal, within the
+split-BF16 tolerance, what the reference's per-source sequence gives:
+load_source_points({q}); ProjectSrcPointsToObjects; ProjectTargetToFieldPoints
+-- computed by the FP64 oracle, and by the library's own single-scene path.
+
+Tolerance: relative L2 over every (receiver, source) output of an item,
+1e-4 against FP64 (split BF16 products are exact to about 2^-16 relative,
+accumulated in FP32 over at most 2,048 fragments per segment, FP64 across
+segments).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def small_batch(scenes):
+    """Three small scenes (plate, box, coarse sphere), two frequencies,
+    8 sources and 6 receivers on an arc (6 < 64: padded rows)."""
+    plate = scenes.rotate(scenes.rectangle(0.30, 0.20), "x", 15.0)
+    box = scenes.rotate(scenes.box(0.12, 0.08, 0.10), "y", 30.0)
+    sph = scenes.icosphere(2, 0.07)
+    src = scenes.arc_xz(6.0, np.linspace(-50.0, 50.0, 8))
+    rx = scenes.arc_xz(5.0, np.linspace(-40.0, 45.0, 6))
+    return [plate, box, sph], src, rx, np.array([15e3, 25e3], np.float32)
+
+
+def oracle_columns(oracle_mod, tris, src, rx, f, cp=1480.0, att=0.0, per_wl=7.5):
+    delta = float(np.float32(cp) / np.float32(f) / np.float32(per_wl))
+    out = np.zeros((len(rx), len(src)), np.complex128)
+    for q in range(len(src)):
+        o = oracle_mod.Oracle()
+        o.set_initial_conditions(cp, float(f), att)
+        o.load_geometry(tris, 0, delta)
+        o.load_source_points(src[q:q + 1])
+        o.load_field_points(rx)
+        o.render()
+        o.project_sources(False)
+        o.project_field_points()
+        out[:, q] = o.field_points()
+        o.close()
+    return out
+
+
+def library_columns(api, tris, src, rx, f, cp=1480.0, att=0.0, per_wl=7.5):
+    delta = float(np.float32(cp) / np.float32(f) / np.float32(per_wl))
+    out = np.zeros((len(rx), len(src)), np.complex128)
+    for q in range(len(src)):
+        api.TearDownCuda()
+        api.set_initial_conditions(cp, float(f), att)
+        api.load_stl_mesh_to_cuda(tris, api.TARGET, delta)
+        api.load_points_to_cuda(src[q:q + 1], isSource=True)
+        api.load_points_to_cuda(rx, isSource=False)
+        api.render_cuda()
+        api.project_source_points_to_objects(False)
+        api.project_target_to_field_points()
+        out[:, q] = api.get_field_point_pressures(len(rx))
+    api.TearDownCuda()
+    return out
+
+
+def test_batch_matches_oracle_and_library(api, oracle_mod, scenes):
+    from sonar_render_gb300 import batch
+    tris, src, rx, freqs = small_batch(scenes)
+    plan = batch.Plan(tris, src, rx, freqs)
+    out = plan.run()
+    st = plan.stats()
+    assert out.shape == (3, 2, 6, 8)
+    print("batch stats: items %d fragments %d pairs %.3g tuning %s" %
+          (st["items"], st["fragments"], st["pairs"], st["tuning"]))
+    for s in range(3):
+        for k, f in enumerate(freqs):
+            ref = oracle_columns(oracle_mod, tris[s], src, rx, f)
+            lib = library_columns(api, tris[s], src, rx, f)
+            e_o, e_l = rel_l2(out[s, k], ref), rel_l2(out[s, k], lib)
+            print("scene %d f %.0f Hz: vs FP64 oracle %.3e, vs single-scene path %.3e" % (s, f, e_o, e_l))
+            assert np.linalg.norm(ref) > 0
+            assert e_o < TOL
+            assert e_l < TOL
+    plan.close()
+
+
+def test_batch_64_points_attenuation_and_determinism(api, oracle_mod, scenes):
+    """64 sources and receivers (the full tile), attenuation on, two runs bit
+    for bit equal, one-shot entry point equal to the plan's result."""
+    from sonar_render_gb300 import batch
+    tris = [scenes.rotate(scenes.rectangle(0.25, 0.25), "x", -10.0)]
+    pos = scenes.arc_xz(8.0, np.linspace(-60.0, 60.0, 64))
+    freqs = np.array([20e3], np.float32)
+    plan = batch.Plan(tris, pos, pos, freqs, attenuation=0.05)
+    a = plan.run()
+    b = plan.run()
+    assert np.array_equal(a, b)
+    c = batch.run_batch(tris, pos, pos, freqs, attenuation=0.05)
+    # the one-shot call may tune differently; results agree to roundoff
+    assert rel_l2(c, a) < 1e-6
+    cols = [0, 21, 42, 63]
+    ref = oracle_columns(oracle_mod, tris[0], pos[cols], pos, freqs[0], att=0.05)
+    e = rel_l2(a[0, 0][:, cols], ref)
+    print("64 x 64 attenuated plate: vs FP64 oracle %.3e; tuning %s" % (e, plan.stats()["tuning"]))
+    assert e < TOL
+    plan.close()
+
+
+def test_batch_shadowed_scene(api, oracle_mod, scenes):
+    """Two plates, the upper one shadowing part of the lower from some
+    sources and receivers: the masks of both hops gate the entries."""
+    from sonar_render_gb300 import batch
+    lower = scenes.rectangle(0.4, 0.4, z=0.0)
+    upper = scenes.translate(scenes.rectangle(0.15, 0.15, z=0.0), (0.05, 0.0, 0.12))
+    tris = [np.concatenate([lower, upper])]
+    src = scenes.arc_xz(4.0, np.linspace(-45.0, 45.0, 5))
+    rx = scenes.arc_xz(3.0, np.linspace(-30.0, 60.0, 7))
+    freqs = np.array([12e3], np.float32)
+    out = batch.run_batch(tris, src, rx, freqs)
+    ref = oracle_columns(oracle_mod, tris[0], src, rx, freqs[0])
+    e = rel_l2(out[0, 0], ref)
+    print("shadowed plates: vs FP64 oracle %.3e" % e)
+    assert e < TOL
+
+
+def test_batch_rejects_bad_sizes(api, scenes):
+    from sonar_render_gb300 import batch
+    tris = [scenes.rectangle(0.1, 0.1)]
+    pos = scenes.arc_xz(5.0, np.linspace(-10.0, 10.0, 65))
+    with pytest.raises(api.SonarError, match="65 sources"):
+        batch.Plan(tris, pos, pos[:4], [10e3])
