@@ -1,7 +1,8 @@
 """Benchmark of the discrete Kirchhoff hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload trihedral60|trihedral40|sphere|plate] [--mode both|plain|compressed]
+                    [--workload trihedral60|trihedral40|sphere|plate|batch] [--mode both|plain|compressed]
+                    [--batch 0|1]
 
 Metric: fragment-pair interactions per second (the reference loops' candidate
 pairs after the area gates, before the cosine and visibility gates): source
@@ -164,9 +165,13 @@ def step_pairs(stats):
     return sum(h["pairs"] for h in stats["hops"])
 
 
+RCUT = [24.0]  # the admissibility network proposes blocks with predicted rank below this
+
+
 def set_path(api, compressed, select):
     api.set_option("compress", 1 if compressed else 0)
     api.set_option("compress_select", select if compressed else 0)
+    api.set_option("compress_rcut", RCUT[0])
 
 
 def time_path(api, cfg, args, flush, local, world):
@@ -425,6 +430,27 @@ def run_gb300(args):
     from sonar_render_gb300 import api, build
     build.build()
     api.load_library()
+    if args.workload == "batch":
+        # the many-source, many-frequency batch alone
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+        if args.profile_only:
+            from sonar_render_gb300 import batch, scenes
+            bc = scenes.batch_config(0)
+            plan = batch.Plan(bc["scenes"], bc["sources"], bc["receivers"], bc["freqs"], bc["cp"], bc["attenuation"],
+                              bc["per_wavelength"])
+            for _ in range(args.warmup + args.steps):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                plan.run(copy=False)
+            st = plan.stats()
+            st.pop("item_fragments")
+            st.pop("item_cells")
+            print("profile-only: %d runs of %s done" % (args.warmup + args.steps, bc["name"]))
+            print(json.dumps(st))
+            plan.close()
+        else:
+            print(json.dumps(batch_leg(args, flush, rank)))
+        return
     cfg = workload(args.workload)
     modes = ["plain", "compressed"] if args.mode == "both" else [args.mode]
     select = args.select
@@ -700,6 +726,8 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
     ap.add_argument("--mode", default="both", choices=["both", "plain", "compressed"])
+    ap.add_argument("--rcut", type=float, default=24.0,
+                    help="network: propose blocks whose predicted rank is below this")
     ap.add_argument("--select", type=int, default=2,
                     help="compressed blocks: 0 separation rule, 1 every interacting block, 2 the trained network")
     ap.add_argument("--train-epochs", type=int, default=40)
@@ -708,6 +736,7 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
+    RCUT[0] = args.rcut
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -238,42 +238,62 @@ struct Stage {
     static constexpr int kLboA = 128 * 16, kLboB = 64 * 16;
 };
 
+// Fragment data of one chunk in shared memory: per fragment the readout
+// centroid + area, the source-hop centroid, the facet normal and the
+// visibility words (receiver bits x, y; source bits z, w).
+template <int KC>
+struct ChunkFrags {
+    float4 v[KC][4];
+};
+
+// Element e (fragment e / 4, field e % 4) of chunk `chunk` of item it, zero
+// past the item's fragments (their visibility words are zero, so padded
+// fragments contribute nothing).
+__device__ __forceinline__ float4 fetch_frag(const BatchArgs &a, const BatchItem &it, int chunk, int kc, int e)
+{
+    const int n = chunk * kc + (e >> 2);
+    if (n >= it.nfrag) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const long long g = (long long)it.frag0 + n;
+    switch (e & 3) {
+    case 0: return __ldg(a.frag_pos + g);
+    case 1: return __ldg(a.frag_spos + g);
+    case 2: return __ldg(a.frag_n + g);
+    default: {
+        const uint4 w = __ldg(a.vis + g);
+        return make_float4(__uint_as_float(w.x), __uint_as_float(w.y), __uint_as_float(w.z), __uint_as_float(w.w));
+    }
+    }
+}
+
 template <int KC, bool ATT>
-__device__ __forceinline__ void generate(uint8_t *st, const BatchArgs &a, const BatchItem &it, int chunk, int tid,
+__device__ __forceinline__ void generate(uint8_t *st, const ChunkFrags<KC> &F, const BatchItem &it, int tid,
                                          float3 prx, bool rx_ok, float3 psrc, bool src_ok)
 {
     using S = Stage<KC>;
     uint8_t *Ahi = st, *Alo = st + S::kA, *Bhi = st + 2 * S::kA, *Blo = st + 2 * S::kA + S::kB;
     const int row = tid & 63;  // receiver (A) or source (B)
-    const int n0 = chunk * KC;
 #pragma unroll 1
     for (int q = tid >> 6; q < KC / 8; q += kBatchThreads / 64) {
-        const int nb = n0 + 8 * q;  // first fragment of this k-group (item-relative)
         float gr[8], gi[8], pr[8], pi[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            const int n = nb + j;
+            const float4 *f = F.v[8 * q + j];
+            const float4 w4 = f[3];
+            const unsigned wrx = __float_as_uint(row < 32 ? w4.x : w4.y);
+            const unsigned wsrc = __float_as_uint(row < 32 ? w4.z : w4.w);
             gr[j] = gi[j] = pr[j] = pi[j] = 0.0f;
-            if (n < it.nfrag) {
-                const long long g = (long long)it.frag0 + n;
-                const uint4 vw = __ldg(a.vis + g);  // receiver bits (x, y), source bits (z, w)
-                const float4 nf = __ldg(a.frag_n + g);
-                if (rx_ok && (((row < 32 ? vw.x : vw.y) >> (row & 31)) & 1u)) {
-                    const float2 v = readout_entry<ATT>(it, __ldg(a.frag_pos + g), nf, prx);
-                    gr[j] = v.x;
-                    gi[j] = v.y;
-                }
-                if (src_ok && (((row < 32 ? vw.z : vw.w) >> (row & 31)) & 1u)) {
-                    const float2 v = incident_entry<ATT>(it, psrc, __ldg(a.frag_spos + g), nf);
-                    pr[j] = v.x;
-                    pi[j] = v.y;
-                }
+            if (rx_ok && ((wrx >> (row & 31)) & 1u)) {
+                const float2 v = readout_entry<ATT>(it, f[0], f[2], prx);
+                gr[j] = v.x;
+                gi[j] = v.y;
+            }
+            if (src_ok && ((wsrc >> (row & 31)) & 1u)) {
+                const float2 v = incident_entry<ATT>(it, psrc, f[1], f[2]);
+                pr[j] = v.x;
+                pi[j] = v.y;
             }
         }
         uint4 h, l;
-        float ngi[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) ngi[j] = -gi[j];
         const int kr0 = q, ki0 = KC / 8 + q;  // k-groups of the real and imaginary halves
         // A row p:      [ Gr | -Gi ];  A row 64 + p: [ Gi | Gr ]
         split8(gr, h, l);
@@ -281,12 +301,13 @@ __device__ __forceinline__ void generate(uint8_t *st, const BatchArgs &a, const 
         st16(Alo + kr0 * S::kLboA + row * 16, l);
         st16(Ahi + ki0 * S::kLboA + (64 + row) * 16, h);
         st16(Alo + ki0 * S::kLboA + (64 + row) * 16, l);
-        split8(ngi, h, l);
-        st16(Ahi + ki0 * S::kLboA + row * 16, h);
-        st16(Alo + ki0 * S::kLboA + row * 16, l);
         split8(gi, h, l);
         st16(Ahi + kr0 * S::kLboA + (64 + row) * 16, h);
         st16(Alo + kr0 * S::kLboA + (64 + row) * 16, l);
+        // -Gi: the same split with every sign bit flipped (exact)
+        const uint4 sg = make_uint4(0x80008000u, 0x80008000u, 0x80008000u, 0x80008000u);
+        st16(Ahi + ki0 * S::kLboA + row * 16, make_uint4(h.x ^ sg.x, h.y ^ sg.y, h.z ^ sg.z, h.w ^ sg.w));
+        st16(Alo + ki0 * S::kLboA + row * 16, make_uint4(l.x ^ sg.x, l.y ^ sg.y, l.z ^ sg.z, l.w ^ sg.w));
         // B row q_src: [ Pr | Pi ]
         split8(pr, h, l);
         st16(Bhi + kr0 * S::kLboB + row * 16, h);
@@ -304,6 +325,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ uint32_t tmem_base;
+    __shared__ ChunkFrags<KC> sfrag[2];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) tmem_alloc(&tmem_base, kTmemCols);
     if (tid == 0) {
@@ -311,64 +333,83 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
         mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = tmem_base;
     const int row = tid & 63;
     const bool rx_ok = row < a.nrx, src_ok = row < a.nsrc;
     const float4 rx4 = rx_ok ? a.rx[row] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float4 sq4 = src_ok ? a.src[row] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float3 prx = make_float3(rx4.x, rx4.y, rx4.z), psrc = make_float3(sq4.x, sq4.y, sq4.z);
     const uint32_t sbase = smem_u32(smem);
+    const bool loader = tid < 4 * KC;  // thread tid stages element tid of each chunk's fragment data
+    // this CTA's chunks: segments [g0, g1), chunk cc of segment sg
+    const int g0 = a.cta_seg[blockIdx.x], g1 = a.cta_seg[blockIdx.x + 1];
+    int sg = g0, cc = 0;
+    int4 seg = make_int4(0, 0, 0, 0);
+    BatchItem it{};
+    if (sg < g1) {
+        seg = a.segs[sg];
+        it = a.items[seg.x];
+        if (loader) sfrag[0].v[tid >> 2][tid & 3] = fetch_frag(a, it, seg.y, KC, tid);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
     uint32_t commits0 = 0, commits1 = 0;  // commits issued on each stage's barrier
     int local = 0;                        // chunks this CTA has generated
     bool ok = true;
-    const int g0 = a.cta_seg[blockIdx.x], g1 = a.cta_seg[blockIdx.x + 1];
-    for (int sg = g0; sg < g1 && ok; ++sg) {
-        const int4 seg = a.segs[sg];
-        const BatchItem it = a.items[seg.x];
-        for (int cc = 0; cc < seg.z && ok; ++cc, ++local) {
-            const int st = local & 1;
-            // the stage is free once the MMAs that read it (two chunks back) completed
-            if (local >= 2) {
-                const uint32_t c = st ? commits1 : commits0;
-                const bool done = mbar_wait(&bar[st], (c - 1) & 1u);
-                ok = __syncthreads_and(done);
-                if (!ok) break;
+    while (sg < g1 && ok) {
+        const int st = local & 1;
+        // the next chunk: its fragment data is loaded now and staged after this chunk's generation
+        int nsg = sg, ncc = cc + 1;
+        int4 nseg = seg;
+        BatchItem nit = it;
+        if (ncc >= seg.z) {
+            nsg = sg + 1;
+            ncc = 0;
+            if (nsg < g1) {
+                nseg = a.segs[nsg];
+                nit = a.items[nseg.x];
             }
-            generate<KC, ATT>(smem + st * S::kBytes, a, it, seg.y + cc, tid, prx, rx_ok, psrc, src_ok);
-            fence_async_smem();
-            tc_fence_before();
-            __syncthreads();
-            if (tid == 0) {
-                tc_fence_after();
-                const uint32_t sA = sbase + st * S::kBytes, sB = sA + 2 * S::kA;
-#pragma unroll
-                for (int ks = 0; ks < 2 * KC / 16; ++ks) {
-                    const uint64_t ahi = sdesc(sA + ks * 2 * S::kLboA, S::kLboA, 128);
-                    const uint64_t alo = sdesc(sA + S::kA + ks * 2 * S::kLboA, S::kLboA, 128);
-                    const uint64_t bhi = sdesc(sB + ks * 2 * S::kLboB, S::kLboB, 128);
-                    const uint64_t blo = sdesc(sB + S::kB + ks * 2 * S::kLboB, S::kLboB, 128);
-                    mma_bf16(tmem, ahi, bhi, kIdesc, (cc > 0 || ks > 0) ? 1u : 0u);
-                    mma_bf16(tmem, ahi, blo, kIdesc, 1u);
-                    mma_bf16(tmem, alo, bhi, kIdesc, 1u);
-                }
-                mma_commit(&bar[st]);
-            }
-            if (st) ++commits1; else ++commits0;
         }
-        if (!ok) break;
-        // ---- segment end: the accumulator -> FP32 partial [128][64]
-        {
-            const int st = (local - 1) & 1;
+        float4 nf = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (loader && nsg < g1) nf = fetch_frag(a, nit, nseg.y + ncc, KC, tid);
+        // the operand stage is free once the MMAs that read it (two chunks back) completed
+        if (local >= 2) {
             const uint32_t c = st ? commits1 : commits0;
             const bool done = mbar_wait(&bar[st], (c - 1) & 1u);
             ok = __syncthreads_and(done);
             if (!ok) break;
         }
-        tc_fence_after();
-        {
+        generate<KC, ATT>(smem + st * S::kBytes, sfrag[st], it, tid, prx, rx_ok, psrc, src_ok);
+        if (loader) sfrag[st ^ 1].v[tid >> 2][tid & 3] = nf;
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t sA = sbase + st * S::kBytes, sB = sA + 2 * S::kA;
+#pragma unroll
+            for (int ks = 0; ks < 2 * KC / 16; ++ks) {
+                const uint64_t ahi = sdesc(sA + ks * 2 * S::kLboA, S::kLboA, 128);
+                const uint64_t alo = sdesc(sA + S::kA + ks * 2 * S::kLboA, S::kLboA, 128);
+                const uint64_t bhi = sdesc(sB + ks * 2 * S::kLboB, S::kLboB, 128);
+                const uint64_t blo = sdesc(sB + S::kB + ks * 2 * S::kLboB, S::kLboB, 128);
+                mma_bf16(tmem, ahi, bhi, kIdesc, (cc > 0 || ks > 0) ? 1u : 0u);
+                mma_bf16(tmem, ahi, blo, kIdesc, 1u);
+                mma_bf16(tmem, alo, bhi, kIdesc, 1u);
+            }
+            mma_commit(&bar[st]);
+        }
+        if (st) ++commits1;
+        else ++commits0;
+        ++local;
+        if (cc + 1 == seg.z) {
+            // ---- segment end: the accumulator -> FP32 partial [128][64]
+            const uint32_t c = st ? commits1 : commits0;
+            const bool done = mbar_wait(&bar[st], (c - 1) & 1u);
+            ok = __syncthreads_and(done);
+            if (!ok) break;
+            tc_fence_after();
             const int quarter = warp & 3, half = warp >> 2;
             const int drow = quarter * 32 + lane;
             float v[32];
@@ -378,9 +419,13 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
             float4 *out = reinterpret_cast<float4 *>(a.partial + ((long long)sg * 128 + drow) * 64 + half * 32);
 #pragma unroll
             for (int q = 0; q < 8; ++q) out[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            tc_fence_before();
+            __syncthreads();
         }
-        tc_fence_before();
-        __syncthreads();
+        sg = nsg;
+        cc = ncc;
+        seg = nseg;
+        it = nit;
     }
     if (!ok && tid == 0) atomicExch(a.status, 1);
     tc_fence_before();
@@ -389,22 +434,23 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
     if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
-// out[item][p][q] = sum over the item's segments, fixed order, FP64
+// out[item][p][q] = sum over the item's segments, fixed order, FP64.  Grid
+// (items, entry chunks of 256): one thread per (receiver, source) entry.
 __global__ void __launch_bounds__(256) k_batch_reduce(const float *partial, const int *item_seg_off,
                                                       const int *item_segs, int nrx, int nsrc, double2 *out)
 {
     const int item = blockIdx.x;
+    const int e = blockIdx.y * 256 + threadIdx.x;
+    if (e >= nrx * nsrc) return;
     const int s0 = item_seg_off[item], s1 = item_seg_off[item + 1];
-    for (int e = threadIdx.x; e < nrx * nsrc; e += blockDim.x) {
-        const int p = e / nsrc, q = e - p * nsrc;
-        double re = 0.0, im = 0.0;
-        for (int s = s0; s < s1; ++s) {
-            const float *P = partial + (long long)item_segs[s] * 128 * 64;
-            re += (double)P[p * 64 + q];
-            im += (double)P[(64 + p) * 64 + q];
-        }
-        out[(long long)item * nrx * nsrc + e] = make_double2(re, im);
+    const int p = e / nsrc, q = e - p * nsrc;
+    double re = 0.0, im = 0.0;
+    for (int s = s0; s < s1; ++s) {
+        const float *P = partial + (long long)item_segs[s] * 128 * 64;
+        re += (double)__ldg(P + p * 64 + q);
+        im += (double)__ldg(P + (64 + p) * 64 + q);
     }
+    out[(long long)item * nrx * nsrc + e] = make_double2(re, im);
 }
 
 }  // namespace
@@ -446,7 +492,9 @@ void launch_batch(const BatchArgs &a, int kc, int grid, bool att, cudaStream_t s
 void launch_batch_reduce(const float *partial, const int *item_seg_off, const int *item_segs, int nitems, int nrx,
                          int nsrc, double2 *out, cudaStream_t s)
 {
-    if (nitems > 0) k_batch_reduce<<<nitems, 256, 0, s>>>(partial, item_seg_off, item_segs, nrx, nsrc, out);
+    if (nitems > 0)
+        k_batch_reduce<<<dim3(nitems, (nrx * nsrc + 255) / 256), 256, 0, s>>>(partial, item_seg_off, item_segs, nrx,
+                                                                            nsrc, out);
 }
 
 }  // namespace sonar

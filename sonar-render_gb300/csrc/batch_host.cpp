@@ -112,6 +112,9 @@ struct Plan {
     float4 *d_nodes = nullptr, *d_tris = nullptr;
     BvhView *d_bvh = nullptr;
     uint4 *d_vis = nullptr;
+    unsigned *d_hard = nullptr, *d_hard_count = nullptr;
+    unsigned hard_cap = 0;
+    int nsm = 0;
     BatchItem *d_items = nullptr;
     int4 *d_segs = nullptr;
     int *d_cta_seg = nullptr, *d_item_seg_off = nullptr, *d_item_segs = nullptr, *d_status = nullptr;
@@ -131,7 +134,7 @@ struct Plan {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         bfree(d_pos); bfree(d_spos); bfree(d_nrm); bfree(d_facet_n); bfree(d_facet); bfree(d_src); bfree(d_rx);
-        bfree(d_nodes); bfree(d_tris); bfree(d_bvh); bfree(d_vis); bfree(d_items);
+        bfree(d_nodes); bfree(d_tris); bfree(d_bvh); bfree(d_vis); bfree(d_hard); bfree(d_hard_count); bfree(d_items);
         bfree(d_segs); bfree(d_cta_seg); bfree(d_item_seg_off); bfree(d_item_segs); bfree(d_status);
         bfree(d_partial); bfree(d_out);
         for (cudaEvent_t &e : ev)
@@ -289,6 +292,9 @@ BatchVisArgs vis_args(const Plan &p)
     v.nsrc = p.nsrc;
     v.bvh = p.d_bvh;
     v.vis = p.d_vis;
+    v.hard = p.d_hard;
+    v.hard_count = p.d_hard_count;
+    v.hard_cap = p.hard_cap;
     return v;
 }
 
@@ -297,7 +303,7 @@ BatchVisArgs vis_args(const Plan &p)
 void enqueue_run(Plan &p)
 {
     BCK(cudaEventRecordWithFlags(p.ev[0], p.stream, cudaEventRecordExternal));
-    launch_batch_vis(vis_args(p), p.stream);
+    launch_batch_vis(vis_args(p), p.nsm, p.stream);
     BCK(cudaEventRecordWithFlags(p.ev[1], p.stream, cudaEventRecordExternal));
     launch_batch(batch_args(p), p.tune.kc, p.tune.grid, p.att != 0.0f, p.stream);
     BCK(cudaEventRecordWithFlags(p.ev[2], p.stream, cudaEventRecordExternal));
@@ -353,7 +359,7 @@ void autotune(Plan &p)
     BCK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
     std::vector<Tuning> cand;
     for (int kc : {32, 64}) {
-        const size_t sm = batch_smem_bytes(kc) + 2048;
+        const size_t sm = batch_smem_bytes(kc) + 10240;  // + static shared memory and the per-CTA reserve
         const int per_sm = std::max(1, std::min(2, (int)((size_t)smem_optin / sm)));
         for (int c = 1; c <= per_sm; c++) {
             Tuning t;
@@ -363,7 +369,7 @@ void autotune(Plan &p)
         }
     }
     // interaction bits once (the candidates share them)
-    launch_batch_vis(vis_args(p), p.stream);
+    launch_batch_vis(vis_args(p), p.nsm, p.stream);
     BCK(cudaGetLastError());
     p.tried.clear();
     Tuning best;
@@ -536,6 +542,17 @@ std::unique_ptr<Plan> make_plan(const float *tris, const int *tri_off, int nscen
     p->d_src = balloc<float4>(nsrc);
     p->d_rx = balloc<float4>(nrx);
     p->d_vis = balloc<uint4>(frag0);
+    // shadow-test queue: pair ids 128 n + point fit 32 bits below 2^25 fragments (else every
+    // pair is tested where it is found); up to 1/16 of all pairs or 32 M entries
+    p->hard_cap = frag0 < (1LL << 25) ? (unsigned)std::min<long long>(1LL << 25, std::max<long long>(frag0 * 8, 1024))
+                                      : 0u;
+    p->d_hard = balloc<unsigned>(std::max<unsigned>(p->hard_cap, 1u));
+    p->d_hard_count = balloc<unsigned>(1);
+    {
+        int dev = 0;
+        BCK(cudaGetDevice(&dev));
+        BCK(cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
     p->d_items = balloc<BatchItem>(p->nitems);
     p->d_item_seg_off = balloc<int>(p->nitems + 1);
     p->d_status = balloc<int>(1);

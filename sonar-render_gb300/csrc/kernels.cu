@@ -46,12 +46,14 @@ __device__ __forceinline__ float dot_rn(float ax, float ay, float az, float bx, 
 }
 
 // ---------------------------------------------------------------- visibility
-__device__ __forceinline__ bool seg_box(float3 o, float3 inv, float4 a, float4 b)
+// Does the part [tlo, 1] of segment o + t (e - o) touch the box?  (inv =
+// componentwise 1 / (e - o))
+__device__ __forceinline__ bool seg_box(float3 o, float3 inv, float4 a, float4 b, float tlo = 0.0f)
 {
     const float tx0 = (a.x - o.x) * inv.x, tx1 = (b.x - o.x) * inv.x;
     const float ty0 = (a.y - o.y) * inv.y, ty1 = (b.y - o.y) * inv.y;
     const float tz0 = (a.z - o.z) * inv.z, tz1 = (b.z - o.z) * inv.z;
-    const float t0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
+    const float t0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tlo));
     const float t1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), 1.0f));
     return t0 <= t1;
 }
@@ -101,7 +103,10 @@ __device__ __forceinline__ bool tri_blocks_v(float4 P, float4 M1, float4 M2, flo
 
 constexpr int kStack = 64;
 
-__device__ bool occluded(const BvhView &B, float3 o, float3 e, float r, float tmax)
+// tlo: only BVH boxes that the part [tlo, 1] of the segment touches are
+// opened (callers pass tlo > 0 only where no triangle can hold a crossing
+// point before it; the triangle tests themselves are unchanged).
+__device__ bool occluded(const BvhView &B, float3 o, float3 e, float r, float tmax, float tlo = 0.0f)
 {
     if (B.ntri == 0) return false;
     const float sc = 1.0f + fmaxf(fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fmaxf(fabsf(o.z), fabsf(e.x))),
@@ -117,7 +122,7 @@ __device__ bool occluded(const BvhView &B, float3 o, float3 e, float r, float tm
     for (int guard = 0; guard < B.nnodes; ++guard) {
         const float4 a = __ldg(B.nodes + 2 * node), b = __ldg(B.nodes + 2 * node + 1);
         bool descend = false;
-        if (seg_box(o, inv, a, b)) {
+        if (seg_box(o, inv, a, b, tlo)) {
             const int left = __float_as_int(a.w), right = __float_as_int(b.w);
             if (left < 0) {
                 const int t0 = -left - 1;
@@ -238,11 +243,13 @@ __device__ __forceinline__ bool occluded_list(const float4 *sT, int n, float3 o,
     return false;
 }
 
-__device__ __forceinline__ bool occluded_full(const BvhView &B, float3 o, float3 e)
+__device__ __forceinline__ bool occluded_full(const BvhView &B, float3 o, float3 e, float reach = 3.0e38f)
 {
     const float vx = __fsub_rn(e.x, o.x), vy = __fsub_rn(e.y, o.y), vz = __fsub_rn(e.z, o.z);
     const float r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
-    return occluded(B, o, e, r, __fsub_rn(r, 1e-3f));
+    // reach: only the last `reach` metres of the ray can hold a crossing point
+    const float tlo = reach < r ? 1.0f - reach / r : 0.0f;
+    return occluded(B, o, e, r, __fsub_rn(r, 1e-3f), tlo);
 }
 
 // ---- block-level occluder culling
@@ -680,53 +687,114 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
 // or behind it; no triangle can hold the crossing point.  With a cosine of at
 // least kConvexCos that margin (5e-5 m) exceeds the convexity tolerance and
 // the FP32 rounding of the crossing test, so such pairs need no occlusion
-// test; the others (and every pair of a non-convex scene) walk the BVH.
+// test.  Below it, a crossing point before the last 1e-4 / cos + 1e-3 metres
+// of the ray lies at least 1e-4 m in front of the plane, beyond the reach of
+// the same tolerances, so the BVH walk opens only boxes near the end of the
+// ray.  Every pair of a non-convex scene walks the whole ray.
 constexpr float kConvexCos = 0.05f;
 
-__global__ void __launch_bounds__(kTile) k_batch_vis(BatchVisArgs a)
+__device__ __forceinline__ float convex_reach(float cosv) { return 1e-4f / fmaxf(cosv, 1e-9f) + 1e-3f; }
+
+// Pass 1: one thread per fragment evaluates the 128 cosine gates; a pair
+// that passes and needs a shadow test is appended to a queue (pair id
+// 128 n + point, warp-aggregated) and provisionally marked visible; when the
+// queue is full the thread tests it itself.  Pass 2 (k_batch_vis_hard) walks
+// the BVH for the queued pairs, one thread each, and clears the bits of the
+// shadowed ones: the divergent walks no longer hold warps of easy pairs.
+__device__ __forceinline__ void vis_pair(const BatchVisArgs &a, const BatchItem &it, long long n, int pt,
+                                         const float4 P, bool &gate, bool &hard, float &est)
 {
-    __shared__ float4 sP[2 * kBatchMaxPoints];  // receivers, then sources
-    const int tid = threadIdx.x;
-    for (int q = tid; q < a.nrx + a.nsrc; q += kTile) sP[q] = q < a.nrx ? a.rx[q] : a.src[q - a.nrx];
-    __syncthreads();
-    const long long n = (long long)blockIdx.x * kTile + tid;
-    if (n >= a.nfrag) return;
-    // the item holding fragment n
+    const bool readout = pt < kBatchMaxPoints;
+    const float4 f = readout ? a.frag_pos[n] : a.frag_spos[n];
+    const float4 nf = a.frag_n[n];
+    // readout: v = field point - fragment, cos_scat = dot(v, n) / r (OptiX.cu:150-160);
+    // source hop: v = fragment - source, cos_inc = dot(-v, n) / r (OptiX.cu:60-79)
+    const float sg = readout ? 1.0f : -1.0f;
+    const float vx = readout ? __fsub_rn(P.x, f.x) : __fsub_rn(f.x, P.x);
+    const float vy = readout ? __fsub_rn(P.y, f.y) : __fsub_rn(f.y, P.y);
+    const float vz = readout ? __fsub_rn(P.z, f.z) : __fsub_rn(f.z, P.z);
+    const float rinv = rsqrtf(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+    gate = cos_gate(vx, vy, vz, rinv, sg, nf.x, nf.y, nf.z);
+    est = sg * fmaf(vx, nf.x, fmaf(vy, nf.y, vz * nf.z)) * rinv;
+    hard = gate && !(it.convex && est >= kConvexCos);
+}
+
+__device__ __forceinline__ bool vis_shadowed(const BatchVisArgs &a, const BatchItem &it, long long n, int pt,
+                                             const float4 P, float est)
+{
+    const bool readout = pt < kBatchMaxPoints;
+    const float4 f = readout ? a.frag_pos[n] : a.frag_spos[n];
+    return occluded_full(a.bvh[it.scene], make_float3(P.x, P.y, P.z), make_float3(f.x, f.y, f.z),
+                         it.convex ? convex_reach(est) : 3.0e38f);
+}
+
+__device__ __forceinline__ int item_of(const BatchVisArgs &a, long long n)
+{
     int lo = 0, hi = a.nitems - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (a.items[mid].frag0 <= n) lo = mid;
         else hi = mid - 1;
     }
-    const BatchItem it = a.items[lo];
-    const BvhView bvh = a.bvh[it.scene];
-    const float4 f = a.frag_pos[n], fs = a.frag_spos[n], nf = a.frag_n[n];
-    unsigned long long wrx = 0ull, wsrc = 0ull;
-    for (int p = 0; p < a.nrx; ++p) {
-        const float4 P = sP[p];
-        // readout: v = field point - fragment, cos_scat = dot(v, n) / r (OptiX.cu:150-160)
-        const float vx = __fsub_rn(P.x, f.x), vy = __fsub_rn(P.y, f.y), vz = __fsub_rn(P.z, f.z);
-        const float rinv = rsqrtf(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
-        if (!cos_gate(vx, vy, vz, rinv, 1.0f, nf.x, nf.y, nf.z)) continue;
-        const float est = fmaf(vx, nf.x, fmaf(vy, nf.y, vz * nf.z)) * rinv;
-        bool vis = true;
-        if (!(it.convex && est >= kConvexCos))
-            vis = !occluded_full(bvh, make_float3(P.x, P.y, P.z), make_float3(f.x, f.y, f.z));
-        if (vis) wrx |= 1ull << p;
+    return lo;
+}
+
+__global__ void __launch_bounds__(kTile) k_batch_vis(BatchVisArgs a)
+{
+    __shared__ float4 sP[2 * kBatchMaxPoints];  // receivers at 0.., sources at 64..
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int q = tid; q < 2 * kBatchMaxPoints; q += kTile) {
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (q < kBatchMaxPoints && q < a.nrx) v = a.rx[q];
+        if (q >= kBatchMaxPoints && q - kBatchMaxPoints < a.nsrc) v = a.src[q - kBatchMaxPoints];
+        sP[q] = v;
     }
-    for (int q = 0; q < a.nsrc; ++q) {
-        const float4 P = sP[a.nrx + q];
-        // source hop: v = fragment - source, cos_inc = dot(-v, n) / r (OptiX.cu:60-79)
-        const float vx = __fsub_rn(fs.x, P.x), vy = __fsub_rn(fs.y, P.y), vz = __fsub_rn(fs.z, P.z);
-        const float rinv = rsqrtf(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
-        if (!cos_gate(vx, vy, vz, rinv, -1.0f, nf.x, nf.y, nf.z)) continue;
-        const float est = -fmaf(vx, nf.x, fmaf(vy, nf.y, vz * nf.z)) * rinv;
-        bool vis = true;
-        if (!(it.convex && est >= kConvexCos))
-            vis = !occluded_full(bvh, make_float3(P.x, P.y, P.z), make_float3(fs.x, fs.y, fs.z));
-        if (vis) wsrc |= 1ull << q;
+    __syncthreads();
+    const long long n = (long long)blockIdx.x * kTile + tid;
+    const bool live = n < a.nfrag;
+    const BatchItem it = live ? a.items[item_of(a, n)] : BatchItem{};
+    unsigned w[4] = {0u, 0u, 0u, 0u};  // receivers 0-31, 32-63, sources 0-31, 32-63
+    for (int pt = 0; pt < 2 * kBatchMaxPoints; ++pt) {
+        const bool readout = pt < kBatchMaxPoints;
+        const int idx = readout ? pt : pt - kBatchMaxPoints;
+        const bool active = live && idx < (readout ? a.nrx : a.nsrc);  // uniform over the warp but for live
+        bool gate = false, hard = false;
+        float est = 0.0f;
+        if (active) vis_pair(a, it, n, pt, sP[pt], gate, hard, est);
+        bool vis = gate;
+        // queue the shadow tests of this point, one atomic per warp
+        const unsigned need = __ballot_sync(0xffffffffu, hard);
+        if (need) {
+            unsigned base = 0u;
+            if (lane == 0) base = atomicAdd(a.hard_count, (unsigned)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (hard) {
+                const unsigned slot = base + (unsigned)__popc(need & ((1u << lane) - 1u));
+                if (slot < a.hard_cap) a.hard[slot] = (unsigned)(n * (2 * kBatchMaxPoints) + pt);
+                else vis = !vis_shadowed(a, it, n, pt, sP[pt], est);  // queue full: test here
+            }
+        }
+        if (vis) w[pt >> 5] |= 1u << (pt & 31);
     }
-    a.vis[n] = make_uint4((unsigned)wrx, (unsigned)(wrx >> 32), (unsigned)wsrc, (unsigned)(wsrc >> 32));
+    if (live) a.vis[n] = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// Pass 2: the queued shadow tests (grid-stride over the device count).
+__global__ void __launch_bounds__(kTile) k_batch_vis_hard(BatchVisArgs a)
+{
+    const unsigned cnt = min(*a.hard_count, a.hard_cap);
+    for (unsigned e = blockIdx.x * kTile + threadIdx.x; e < cnt; e += gridDim.x * kTile) {
+        const unsigned id = a.hard[e];
+        const long long n = id / (2 * kBatchMaxPoints);
+        const int pt = (int)(id % (2 * kBatchMaxPoints));
+        const BatchItem it = a.items[item_of(a, n)];
+        const float4 P = pt < kBatchMaxPoints ? a.rx[pt] : a.src[pt - kBatchMaxPoints];
+        bool gate, hard;
+        float est;
+        vis_pair(a, it, n, pt, P, gate, hard, est);
+        if (vis_shadowed(a, it, n, pt, P, est))
+            atomicAnd(reinterpret_cast<unsigned *>(a.vis + n) + (pt >> 5), ~(1u << (pt & 31)));
+    }
 }
 
 // ---------------------------------------------------------------- sums
@@ -1395,29 +1463,28 @@ constexpr int kAcaMaxZeroRows = 48;
 constexpr int kAcaRegRanks = 16;  // factor entries a thread keeps in registers; higher ranks are re-read from global
 constexpr int kAcaWarps = kTile / 32;
 
-// Block-wide argmax (ARG) of v over the threads with valid set (ties: lowest
-// index) and block-wide sums (SUMS) of s0 and s1; every thread receives the
-// results (v = -1 when no thread was valid).  The argmax is a shared-memory
-// atomicMax on a 64-bit key (value bits + 1, then the complemented index),
-// which is order-independent; the sums go through one slot per warp, added
-// in warp order (deterministic).  One barrier.  The key must be zero on
-// entry; the caller resets it once every thread has read it.
+// Block-wide argmax (ARG) of v >= 0 over the threads with valid set and
+// block-wide sums (SUMS) of s0 and s1; every thread receives the results
+// (v = -1 when no thread was valid).  The argmax key is the value's float
+// bits with the low 8 mantissa bits replaced by 255 - idx (idx < 256): the
+// largest value to 2^-15 relative wins, ties go to the lowest index; a warp
+// reduction (redux.sync) then a shared-memory atomicMax, which is
+// order-independent.  The sums go through one slot per warp, added in warp
+// order (deterministic).  One barrier.  The key must be zero on entry; the
+// caller resets it once every thread has read it.
 template <bool ARG, bool SUMS>
-__device__ __forceinline__ void cta_reduce(float &v, int &idx, bool valid, float &s0, float &s1,
-                                           unsigned long long *key, float2 *sums)
+__device__ __forceinline__ void cta_reduce(float &v, int &idx, bool valid, float &s0, float &s1, unsigned *key,
+                                           float2 *sums)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned long long k = 0ull;
-    if (ARG && valid)
-        k = ((unsigned long long)(__float_as_uint(fmaxf(v, 0.0f)) + 1u) << 32) |
-            (unsigned long long)(0xFFFFFFFFu - (unsigned)idx);
+    unsigned k = 0u;
+    if (ARG) {
+        if (valid) k = ((__float_as_uint(fmaxf(v, 0.0f)) + 0x100u) & 0xFFFFFF00u) | (255u - (unsigned)idx);
+        k = __reduce_max_sync(0xffffffffu, k);
+    }
+    if (SUMS) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        if (ARG) {
-            const unsigned long long ok = __shfl_xor_sync(0xffffffffu, k, o);
-            k = ok > k ? ok : k;
-        }
-        if (SUMS) {
+        for (int o = 16; o > 0; o >>= 1) {
             s0 += __shfl_xor_sync(0xffffffffu, s0, o);
             s1 += __shfl_xor_sync(0xffffffffu, s1, o);
         }
@@ -1428,9 +1495,9 @@ __device__ __forceinline__ void cta_reduce(float &v, int &idx, bool valid, float
     }
     __syncthreads();
     if (ARG) {
-        const unsigned long long w = *key;
-        v = w ? __uint_as_float((unsigned)(w >> 32) - 1u) : -1.0f;
-        idx = (int)(0xFFFFFFFFu - (unsigned)(w & 0xFFFFFFFFull));
+        const unsigned w = *key;
+        v = w ? __uint_as_float((w & 0xFFFFFF00u) - 0x100u) : -1.0f;
+        idx = (int)(255u - (w & 0xFFu));
     }
     if (SUMS) {
         float t0 = 0.0f, t1 = 0.0f;
@@ -1486,8 +1553,8 @@ static_assert(kAcaRegRanks == 16, "ACA_REG_LOOP and ACA_REG_SET cover 16 registe
 // x - u v (complex)
 __device__ __forceinline__ float2 csub_mul(float2 x, float2 u, float2 v)
 {
-    x.x -= u.x * v.x - u.y * v.y;
-    x.y -= u.x * v.y + u.y * v.x;
+    x.x = fmaf(u.y, v.y, fmaf(-u.x, v.x, x.x));
+    x.y = fmaf(-u.y, v.x, fmaf(-u.x, v.y, x.y));
     return x;
 }
 
@@ -1504,7 +1571,7 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
                                                   const long long *off, int nblocks, float tol, float limit,
                                                   float2 *U, float2 *V, int *rank, float *fro, float *err)
 {
-    __shared__ unsigned long long keyA, keyB;  // argmax keys: pivot column / next row, lowest unused row
+    __shared__ unsigned keyA, keyB;  // argmax keys: pivot column / next row, lowest unused row
     __shared__ float2 sums[kAcaWarps];
     __shared__ float2 su[kLrRankLimit], sv[kLrRankLimit + 1];  // sv[kLrRankLimit]: the pivot
     const int t = threadIdx.x, b = blockIdx.x;
@@ -1527,17 +1594,17 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
     bool used = !rowj;  // row t taken (or absent)
     int r = 0, k = 0, zero_rows = 0;
     float norm2 = 0.0f;
-    if (t == 0) keyB = 0ull;
+    if (t == 0) keyB = 0u;
     while (k < K) {
         // keyA was last read before the previous iteration's second barrier
-        if (t == 0) keyA = 0ull;
+        if (t == 0) keyA = 0u;
         // ---- publish U[r][m], m < k
         if (t == r) {
             ACA_REG_LOOP(k, su[m] = ur[m]);
             for (int m = kAcaRegRanks; m < k; ++m) su[m] = Ub[m * kTile + r];
         }
         __syncthreads();
-        if (t == 0) keyB = 0ull;  // last read before the barrier above
+        if (t == 0) keyB = 0u;  // last read before the barrier above
         // ---- residual row r, entry (r, t)
         float2 val = z2;
         if (coli) {
@@ -1568,7 +1635,7 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
         }
         __syncthreads();
         const float2 pv = sv[kLrRankLimit];
-        const float inv = 1.0f / (pv.x * pv.x + pv.y * pv.y);
+        const float inv = __frcp_rn(pv.x * pv.x + pv.y * pv.y);
         const float2 vv = coli ? make_float2((val.x * pv.x + val.y * pv.y) * inv, (val.y * pv.x - val.x * pv.y) * inv)
                                : z2;
         Vb[k * kTile + t] = vv;
@@ -1979,9 +2046,12 @@ void launch_mask(const MaskArgs &a, cudaStream_t s)
     }
 }
 
-void launch_batch_vis(const BatchVisArgs &a, cudaStream_t s)
+void launch_batch_vis(const BatchVisArgs &a, int nsm, cudaStream_t s)
 {
-    if (a.nfrag > 0) k_batch_vis<<<(unsigned)((a.nfrag + kTile - 1) / kTile), kTile, 0, s>>>(a);
+    if (a.nfrag <= 0) return;
+    cudaMemsetAsync(a.hard_count, 0, sizeof(unsigned), s);
+    k_batch_vis<<<(unsigned)((a.nfrag + kTile - 1) / kTile), kTile, 0, s>>>(a);
+    k_batch_vis_hard<<<(unsigned)(8 * nsm), kTile, 0, s>>>(a);
 }
 
 void launch_sum(const SumArgs &a, cudaStream_t s)

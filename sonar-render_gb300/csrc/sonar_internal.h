@@ -184,8 +184,12 @@ struct BatchVisArgs {
     int nrx, nsrc;
     const BvhView *bvh;            // per scene
     uint4 *vis;
+    unsigned *hard;                // queue of pairs that need a shadow test: 128 fragment + point
+    unsigned *hard_count;          // (points: receivers 0-63, sources 64-127)
+    unsigned hard_cap;
 };
-void launch_batch_vis(const BatchVisArgs &a, cudaStream_t s);
+// nsm: SM count (grid of the queue pass); the queue count is reset on the stream
+void launch_batch_vis(const BatchVisArgs &a, int nsm, cudaStream_t s);
 constexpr int kBatchMaxPoints = 64;  // sources and receivers per item
 size_t batch_smem_bytes(int kc);
 cudaError_t batch_prepare();        // dynamic shared-memory limits of the batch kernels (outside stream capture)
