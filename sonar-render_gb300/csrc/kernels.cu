@@ -1712,11 +1712,12 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
 // pairs that interact (1 for ALL, the stored bits for BITS, 256 sampled gate
 // pairs for CLEAR).
 __global__ void __launch_bounds__(128) k_block_desc(SumArgs a, const int2 *blocks, const uint8_t *cls, int nblocks,
-                                                    const float4 *cen, const float4 *nm, float inv_lambda, float *X)
+                                                    const float4 *cen, const float4 *nm, float inv_lambda, float *X,
+                                                    const int *ndev)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int b = blockIdx.x * 4 + warp;
-    if (b >= nblocks) return;
+    if (b >= (ndev ? min(*ndev, nblocks) : nblocks)) return;
     const int I = blocks[b].x, J = blocks[b].y, bc = cls[b];
     const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
     float vis = 1.0f;
@@ -1774,12 +1775,12 @@ constexpr int kLrMaxRank = 64;
 // second pass over them hits L2.
 __global__ void __launch_bounds__(kTile) k_lr_block(SumArgs a, const int2 *blocks, const long long *off,
                                                     const int *bidx, int nb, const float2 *U, const float2 *V,
-                                                    const int *rank, float2 *brow, float2 *bcol)
+                                                    const int *rank, float2 *brow, float2 *bcol, const int *ndev)
 {
     __shared__ float4 sRed[kTile / 32][kLrMaxRank];
     __shared__ float2 sTv[kLrMaxRank], sSu[kLrMaxRank];
     const int q = blockIdx.x;
-    if (q >= nb) return;
+    if (q >= (ndev ? min(*ndev, nb) : nb)) return;
     const int b = bidx[q];
     const int k = rank[b];
     const int I = blocks[b].x, J = blocks[b].y, t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -2128,18 +2129,18 @@ void launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const 
 }
 
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
-                       const float4 *nm, float inv_lambda, float *X, cudaStream_t s)
+                       const float4 *nm, float inv_lambda, float *X, cudaStream_t s, const int *ndev)
 {
     if (nblocks > 0)
-        k_block_desc<<<(nblocks + 3) / 4, 128, 0, s>>>(a, blocks, cls, nblocks, cen, nm, inv_lambda, X);
+        k_block_desc<<<(nblocks + 3) / 4, 128, 0, s>>>(a, blocks, cls, nblocks, cen, nm, inv_lambda, X, ndev);
 }
 
 void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
                      const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
-                     double2 *ycol, cudaStream_t s)
+                     double2 *ycol, cudaStream_t s, const int *ndev)
 {
-    if (nb > 0) k_lr_block<<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol);
+    if (nb > 0) k_lr_block<<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev);
     if (ntiles > 0) k_lr_gather<<<ntiles, kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, yrow, ycol);
 }
 

@@ -168,6 +168,11 @@ struct Compression {
     int *d_byJ_off = nullptr, *d_byJ = nullptr, *d_byI_off = nullptr, *d_byI = nullptr;
     uint8_t *d_flags = nullptr;  // the mask flags with accepted blocks removed (dense kernel)
     double2 *d_yrow = nullptr, *d_ycol = nullptr;
+    const int *d_nacc = nullptr;    // accepted-block count (device)
+    double *d_stats = nullptr;      // accepted count, rank sum, largest judged error, ordered pairs
+    float *d_desc = nullptr;        // descriptors of the candidates
+    int *d_kmap = nullptr, *d_acap = nullptr;  // kept block -> candidate, rank caps
+    bool stats_pending = false;     // statistics and timings not read back yet
     // descriptors and rank labels of the approximated blocks (network training)
     std::vector<float> desc, label;
     Arena arena;    // the candidate- and block-level arrays above
@@ -209,6 +214,7 @@ struct Model {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr, ev4 = nullptr, ev5 = nullptr;
     cudaEvent_t ev6 = nullptr, ev7 = nullptr, ev8 = nullptr;
+    cudaEvent_t evb[4] = {nullptr, nullptr, nullptr, nullptr};  // compression build: start, selected, ACA end, end
     float4 *d_src_pos = nullptr, *d_fp_pos = nullptr;
     double2 *d_src_P = nullptr, *d_fp_P = nullptr;
     // field points are kept in Morton (spatial) order on the device so that a
@@ -264,7 +270,7 @@ struct Model {
         dfree(d_blist); dfree(d_rowcnt); dfree(d_chunk_off); dfree(d_nchunks); dfree(d_chunks); dfree(d_rowpart);
         pack_cap = partial_cap = limit_cap = colpart_cap = 0;
         sym_tiles = 0;
-        for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3, &ev4, &ev5, &ev6, &ev7, &ev8})
+        for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3, &ev4, &ev5, &ev6, &ev7, &ev8, &evb[0], &evb[1], &evb[2], &evb[3]})
             if (*e) {
                 cudaEventDestroy(*e);
                 *e = nullptr;
@@ -414,7 +420,9 @@ void render()
 {
     if (g.rendered) fail(-2, "render_cuda called twice without TearDownCuda");
     CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
-    for (cudaEvent_t *e : {&g.ev0, &g.ev1, &g.ev2, &g.ev3, &g.ev4, &g.ev5, &g.ev6, &g.ev7, &g.ev8}) CK(cudaEventCreate(e));
+    for (cudaEvent_t *e : {&g.ev0, &g.ev1, &g.ev2, &g.ev3, &g.ev4, &g.ev5, &g.ev6, &g.ev7, &g.ev8, &g.evb[0], &g.evb[1],
+                           &g.evb[2], &g.evb[3]})
+        CK(cudaEventCreate(e));
     for (int t : {OBJ_TARGET, OBJ_FIELD})
         for (auto &o : g.obj[t]) render_object(*o);
     // occluders: every triangle of every target object (OptiX.cpp:264-296)
@@ -642,9 +650,11 @@ void ensure_colpart(int ntiles)
 // below the rank cut are approximated with a rank cap from the prediction,
 // the rest stay dense without an attempt.  Every approximated block is
 // built by adaptive cross approximation and judged on sampled exact entries;
-// accepted blocks leave the dense kernel's flags.  Rank labels of the
-// approximated blocks (log2(1 + rank), log2(1 + 2 cap) when rejected) are
-// kept with their descriptors for training the network.
+// accepted blocks leave the dense kernel's flags.  The lists are built on the
+// device (select.cu); the host reads back only the kept-block count and the
+// factor-column total, to size the factor arrays.  Statistics (and, for
+// select 1, the training samples: descriptors with log2(1 + rank) labels,
+// log2(1 + 2 cap) when rejected) are read after the hop (finish_compression).
 void build_compression(int a, MaskEntry &M, const SumArgs &s)
 {
     Compression &C = g.cmp;
@@ -655,187 +665,135 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     if (select == 2 && !mlp_ready())
         fail(-2, "compress_select 2 needs the admissibility network's parameters (train or load them first)");
     cudaStream_t st = g.stream;
-    CK(cudaEventRecord(g.ev2, st));
-    // one arena for the whole build, sized for the worst case (every
-    // upper block approximated at the full rank cap)
-    const size_t nmax = (size_t)nt * (nt + 1) / 2;
+    CK(cudaEventRecord(g.evb[0], st));
+    // every upper block I < J, I < nt
+    const size_t nmax = std::max<size_t>((size_t)nt * (nt - 1) / 2 + (size_t)nt * std::max(nb - nt, 0), 1);
+    const size_t ngrid = (size_t)nt * nb;
     {
-        size_t bytes = 2 * Arena::bytes_of(nt, sizeof(float4)) + Arena::bytes_of(nmax, sizeof(int2)) +
-                       Arena::bytes_of(nmax, 1) + Arena::bytes_of(nmax * 8, sizeof(float)) +
-                       Arena::bytes_of(nmax, sizeof(float)) + Arena::bytes_of((size_t)nt * nb, 1) +
-                       2 * Arena::bytes_of(M.nsrc, sizeof(double2)) + Arena::bytes_of(nmax, sizeof(int2)) +
-                       Arena::bytes_of(nmax, 1) + Arena::bytes_of(nmax, sizeof(int)) +
-                       Arena::bytes_of(nmax, sizeof(long long)) + 3 * Arena::bytes_of(nmax, sizeof(int)) +
-                       2 * Arena::bytes_of(nmax, sizeof(float)) + 4 * Arena::bytes_of(nb + 1, sizeof(int)) +
-                       2 * Arena::bytes_of(nmax, sizeof(int)) + 4096;
+        size_t bytes = 2 * Arena::bytes_of(nt, sizeof(float4)) + 6 * Arena::bytes_of(nb + 1, sizeof(int)) +
+                       2 * Arena::bytes_of(nt + 1, sizeof(int)) + 2 * Arena::bytes_of(nmax, sizeof(int2)) +
+                       2 * Arena::bytes_of(nmax, 1) + Arena::bytes_of(nmax * 8, sizeof(float)) +
+                       Arena::bytes_of(nmax, sizeof(float)) + Arena::bytes_of(nmax, sizeof(long long)) +
+                       9 * Arena::bytes_of(nmax, sizeof(int)) + 3 * Arena::bytes_of(nmax, sizeof(float)) +
+                       Arena::bytes_of(nmax * 64, 1) + 2 * Arena::bytes_of(ngrid, 1) +
+                       Arena::bytes_of(ngrid, sizeof(int)) + 2 * Arena::bytes_of(M.nsrc, sizeof(double2)) +
+                       Arena::bytes_of(4, sizeof(double)) + 8192;
         C.arena.reserve(bytes);
     }
     Arena &ar = C.arena;
-    // tile geometry
     float4 *d_cen = ar.take<float4>(nt), *d_nm = ar.take<float4>(nt);
     launch_tile_stats(g.d_packA, g.d_packB, M.nsrc, d_cen, d_nm, st);
-    std::vector<float4> cen(nt);
-    std::vector<uint8_t> flags((size_t)nt * nb);
-    CK(cudaMemcpyAsync(cen.data(), d_cen, nt * sizeof(float4), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(flags.data(), M.view.flags, flags.size(), cudaMemcpyDeviceToHost, st));
+    // ---- candidates
+    int *d_ccnt = ar.take<int>(nb), *d_coff = ar.take<int>(nb + 1);
+    int2 *d_cblocks = ar.take<int2>(nmax);
+    uint8_t *d_ccls = ar.take<uint8_t>(nmax);
+    launch_cand_lists(M.view.flags, nt, nb, select, g.opt_cmp_eta, d_cen, d_ccnt, d_coff, d_cblocks, d_ccls, st);
+    C.d_desc = ar.take<float>(nmax * 8);
+    const float inv_lambda = (float)(g.kr / (2.0 * M_PI));
+    launch_block_desc(s, d_cblocks, d_ccls, (int)nmax, d_cen, d_nm, inv_lambda, C.d_desc, st, d_coff + nb);
+    float *d_pred = nullptr;
+    if (select == 2) {
+        d_pred = ar.take<float>(nmax);
+        CK(mlp_predict_dev(C.d_desc, (int)nmax, d_pred, st));  // rows past the candidate count are not read
+    }
+    // ---- kept blocks, rank caps, factor columns
+    int *d_kcnt = ar.take<int>(nb), *d_ksum = ar.take<int>(nb);
+    int *d_koff = ar.take<int>(nb + 1), *d_kcol = ar.take<int>(nb + 1);
+    C.d_blocks = ar.take<int2>(nmax);
+    C.d_cls = ar.take<uint8_t>(nmax);
+    C.d_acap = ar.take<int>(nmax);
+    C.d_off = ar.take<long long>(nmax);
+    C.d_kmap = ar.take<int>(nmax);
+    const float cut = std::log2(1.0f + g.opt_cmp_rcut);
+    launch_keep_lists(nb, d_coff, d_pred, cut, rmax, d_cblocks, d_ccls, d_kcnt, d_ksum, d_koff, d_kcol, C.d_blocks,
+                      C.d_cls, C.d_acap, C.d_off, C.d_kmap, st);
+    CK(cudaEventRecord(g.evb[1], st));
+    int hcnt[3] = {0, 0, 0};  // candidates, kept blocks, factor columns
+    CK(cudaMemcpyAsync(&hcnt[0], d_coff + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&hcnt[1], d_koff + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&hcnt[2], d_kcol + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    std::vector<int2> blocks;
-    std::vector<uint8_t> cls;
-    for (int J = 0; J < nb; J++)
-        for (int I = 0; I < std::min(J, nt); I++) {
-            const uint8_t f = flags[(size_t)I * nb + J];
-            if (f == kFlagNone) continue;
-            if (select == 0) {
-                if (f != kFlagAll) continue;
-                const float dx = cen[I].x - cen[J].x, dy = cen[I].y - cen[J].y, dz = cen[I].z - cen[J].z;
-                const float sep = std::sqrt(dx * dx + dy * dy + dz * dz);
-                if (!(sep > g.opt_cmp_eta * (cen[I].w + cen[J].w))) continue;
-            }
-            blocks.push_back(make_int2(I, J));
-            cls.push_back(f);
-        }
+    const int n = hcnt[1];
+    const long long cols = hcnt[2];
     C.select = select;
-    C.ncand = (int)blocks.size();
-    C.obj = a;
-    C.kr = g.kr;
-    C.ki = g.ki;
-    // descriptors of every candidate
-    const int nc = C.ncand;
-    int2 *d_cblocks = ar.take<int2>(nc);
-    uint8_t *d_ccls = ar.take<uint8_t>(nc);
-    float *d_desc = ar.take<float>((size_t)nc * 8);
-    if (nc > 0) {
-        CK(cudaMemcpyAsync(d_cblocks, blocks.data(), nc * sizeof(int2), cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(d_ccls, cls.data(), nc, cudaMemcpyHostToDevice, st));
-        const float inv_lambda = (float)(g.kr / (2.0 * M_PI));
-        launch_block_desc(s, d_cblocks, d_ccls, nc, d_cen, d_nm, inv_lambda, d_desc, st);
-    }
-    // descriptors come back to the host only when the build labels training samples
-    std::vector<float> desc(select == 1 ? (size_t)nc * 8 : 0);
-    std::vector<int> cap(nc, rmax);
-    std::vector<int> keep;  // candidates that are approximated
-    if (!desc.empty()) CK(cudaMemcpyAsync(desc.data(), d_desc, desc.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
-    if (select == 2 && nc > 0) {
-        float *d_pred = ar.take<float>(nc);
-        CK(mlp_predict_dev(d_desc, nc, d_pred, st));
-        std::vector<float> pred(nc);
-        CK(cudaMemcpyAsync(pred.data(), d_pred, nc * sizeof(float), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        const float cut = std::log2(1.0f + g.opt_cmp_rcut);
-        for (int q = 0; q < nc; q++) {
-            if (!(pred[q] < cut)) continue;
-            const float r = std::exp2(pred[q]) - 1.0f;
-            cap[q] = std::max(4, std::min(rmax, (int)std::ceil(1.5f * r) + 4));
-            keep.push_back(q);
-        }
-    } else {
-        CK(cudaStreamSynchronize(st));
-        for (int q = 0; q < nc; q++) keep.push_back(q);
-    }
-    CK(cudaEventRecord(g.ev6, st));
-    // approximated blocks, their caps and factor offsets
-    const int n = (int)keep.size();
-    std::vector<int2> ab(n);
-    std::vector<uint8_t> acls(n);
-    std::vector<int> acap(n);
-    std::vector<long long> off(n);
-    long long cols = 0;
-    for (int q = 0; q < n; q++) {
-        ab[q] = blocks[keep[q]];
-        acls[q] = cls[keep[q]];
-        acap[q] = cap[keep[q]];
-        off[q] = cols;
-        cols += acap[q];
-    }
+    C.ncand = hcnt[0];
     C.nblocks = n;
     C.ncols = cols;
     C.rmax = rmax;
-    C.d_flags = ar.take<uint8_t>(flags.size());
+    C.obj = a;
+    C.kr = g.kr;
+    C.ki = g.ki;
+    // ---- cross approximation of the kept blocks
+    C.factors.reserve(2 * Arena::bytes_of((size_t)std::max<long long>(cols, 1) * kTile, sizeof(float2)) +
+                      2 * Arena::bytes_of((size_t)std::max(n, 1) * kTile, sizeof(float2)));
+    C.d_U = C.factors.take<float2>((size_t)std::max<long long>(cols, 1) * kTile);
+    C.d_V = C.factors.take<float2>((size_t)std::max<long long>(cols, 1) * kTile);
+    C.d_brow = C.factors.take<float2>((size_t)std::max(n, 1) * kTile);
+    C.d_bcol = C.factors.take<float2>((size_t)std::max(n, 1) * kTile);
+    C.d_rank = ar.take<int>(nmax);
+    C.d_fro = ar.take<float>(nmax);
+    C.d_err = ar.take<float>(nmax);
+    launch_aca(s, C.d_blocks, C.d_cls, C.d_acap, C.d_off, n, g.opt_cmp_tol, C.d_U, C.d_V, C.d_rank, C.d_fro,
+               g.opt_cmp_judge, C.d_err, st);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(g.evb[2], st));
+    // ---- accepted blocks: dense flags off, owner lists, statistics
+    C.d_flags = ar.take<uint8_t>(ngrid);
+    CK(cudaMemcpyAsync(C.d_flags, M.view.flags, ngrid, cudaMemcpyDeviceToDevice, st));
+    uint8_t *d_accbm = ar.take<uint8_t>(ngrid);
+    int *d_qidx = ar.take<int>(ngrid);
+    int *d_acnt = ar.take<int>(nb), *d_icnt = ar.take<int>(nt);
+    C.d_byJ_off = ar.take<int>(nb + 1);
+    C.d_byI_off = ar.take<int>(nt + 1);
+    C.d_bidx = ar.take<int>(nmax);
+    C.d_byJ = ar.take<int>(nmax);
+    C.d_byI = ar.take<int>(nmax);
+    launch_accept_lists(nt, nb, d_koff, C.d_blocks, C.d_rank, C.d_flags, d_accbm, d_qidx, d_acnt, C.d_byJ_off, C.d_bidx,
+                        C.d_byJ, d_icnt, C.d_byI_off, C.d_byI, st);
+    C.d_nacc = C.d_byJ_off + nb;
+    C.d_stats = ar.take<double>(4);
+    launch_cmp_stats(d_koff + nb, C.d_blocks, C.d_rank, C.d_err, M.nsrc, C.d_stats, st);
     C.d_yrow = ar.take<double2>(M.nsrc);
     C.d_ycol = ar.take<double2>(M.nsrc);
-    std::vector<int> rank(n);
-    std::vector<float> err(n);
-    if (n > 0) {
-        C.d_blocks = ar.take<int2>(n);
-        C.d_cls = ar.take<uint8_t>(n);
-        C.d_cap = ar.take<int>(n);
-        C.d_off = ar.take<long long>(n);
-        C.factors.reserve(2 * Arena::bytes_of((size_t)cols * kTile, sizeof(float2)) +
-                          2 * Arena::bytes_of((size_t)n * kTile, sizeof(float2)));
-        C.d_U = C.factors.take<float2>((size_t)cols * kTile);
-        C.d_V = C.factors.take<float2>((size_t)cols * kTile);
-        C.d_rank = ar.take<int>(n);
-        C.d_fro = ar.take<float>(n);
-        C.d_err = ar.take<float>(n);
-        CK(cudaMemcpyAsync(C.d_blocks, ab.data(), n * sizeof(int2), cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(C.d_cls, acls.data(), n, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(C.d_cap, acap.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(C.d_off, off.data(), n * sizeof(long long), cudaMemcpyHostToDevice, st));
-        CK(cudaEventRecord(g.ev7, st));
-        launch_aca(s, C.d_blocks, C.d_cls, C.d_cap, C.d_off, n, g.opt_cmp_tol, C.d_U, C.d_V, C.d_rank, C.d_fro,
-                   g.opt_cmp_judge, C.d_err, st);
-        CK(cudaGetLastError());
-        CK(cudaEventRecord(g.ev8, st));
-        CK(cudaMemcpyAsync(rank.data(), C.d_rank, n * sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(err.data(), C.d_err, n * sizeof(float), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        CK(cudaEventElapsedTime(&C.aca_ms, g.ev7, g.ev8));
-    } else {
-        C.aca_ms = 0.0f;
-    }
-    // accepted blocks: dense flags off, owner lists; training samples
-    std::vector<int> bidx;
-    std::vector<std::vector<int>> byJ(nb), byI(nb);
-    double rsum = 0.0, emax = 0.0, pairs = 0.0;
-    C.desc.assign(desc.empty() ? 0 : (size_t)n * 8, 0.0f);
-    C.label.assign(desc.empty() ? 0 : n, 0.0f);
-    for (int b = 0; b < n; b++) {
-        if (!desc.empty()) {
-            std::copy(desc.begin() + (size_t)keep[b] * 8, desc.begin() + (size_t)keep[b] * 8 + 8,
-                      C.desc.begin() + (size_t)b * 8);
-            C.label[b] = rank[b] > 0 ? std::log2(1.0f + (float)rank[b]) : std::log2(1.0f + 2.0f * (float)acap[b]);
-        }
-        if (rank[b] <= 0) continue;
-        const int q = (int)bidx.size();  // accepted position: the block's output slots
-        bidx.push_back(b);
-        flags[(size_t)ab[b].x * nb + ab[b].y] = kFlagNone;
-        byJ[ab[b].y].push_back(q);
-        byI[ab[b].x].push_back(q);
-        rsum += rank[b];
-        emax = std::max(emax, (double)err[b]);
-        const double ni = std::min(kTile, M.nsrc - ab[b].x * kTile), nj = std::min(kTile, M.nsrc - ab[b].y * kTile);
-        pairs += 2.0 * ni * nj;
-    }
-    C.naccepted = (int)bidx.size();
-    C.mean_rank = C.naccepted ? rsum / C.naccepted : 0.0;
-    C.max_err = emax;
-    C.pairs_cmp = pairs;
-    auto csr = [&](const std::vector<std::vector<int>> &lists, int *&d_o, int *&d_i) {
-        std::vector<int> o(lists.size() + 1, 0), idx;
-        for (size_t x = 0; x < lists.size(); x++) {
-            o[x + 1] = o[x] + (int)lists[x].size();
-            idx.insert(idx.end(), lists[x].begin(), lists[x].end());
-        }
-        d_o = ar.take<int>(o.size());
-        d_i = ar.take<int>(std::max<size_t>(idx.size(), 1));
-        CK(cudaMemcpyAsync(d_o, o.data(), o.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-        if (!idx.empty()) CK(cudaMemcpyAsync(d_i, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    };
-    // the expansion runs per tile X covering both roles (J = X rows, I = X columns)
-    csr(byJ, C.d_byJ_off, C.d_byJ);
-    csr(byI, C.d_byI_off, C.d_byI);
-    C.d_bidx = ar.take<int>(std::max<size_t>(bidx.size(), 1));
-    if (n == 0) C.factors.reserve(2 * Arena::bytes_of(kTile, sizeof(float2)));
-    C.d_brow = C.factors.take<float2>(std::max<size_t>(bidx.size(), 1) * kTile);
-    C.d_bcol = C.factors.take<float2>(std::max<size_t>(bidx.size(), 1) * kTile);
-    if (!bidx.empty())
-        CK(cudaMemcpyAsync(C.d_bidx, bidx.data(), bidx.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(C.d_flags, flags.data(), flags.size(), cudaMemcpyHostToDevice, st));
-    CK(cudaEventRecord(g.ev3, st));
-    CK(cudaEventSynchronize(g.ev3));
-    CK(cudaEventElapsedTime(&C.build_ms, g.ev2, g.ev3));
-    CK(cudaEventElapsedTime(&C.select_ms, g.ev2, g.ev6));
+    CK(cudaEventRecord(g.evb[3], st));
     C.valid = true;
+    C.stats_pending = true;
+}
+
+// Statistics, timings and (select 1) training samples of the last build,
+// once the stream has passed it.
+void finish_compression()
+{
+    Compression &C = g.cmp;
+    if (!C.stats_pending) return;
+    C.stats_pending = false;
+    double st[4] = {0.0, 0.0, 0.0, 0.0};
+    CK(cudaMemcpy(st, C.d_stats, sizeof(st), cudaMemcpyDeviceToHost));
+    C.naccepted = (int)st[0];
+    C.mean_rank = st[0] > 0.0 ? st[1] / st[0] : 0.0;
+    C.max_err = st[2];
+    C.pairs_cmp = st[3];
+    CK(cudaEventElapsedTime(&C.build_ms, g.evb[0], g.evb[3]));
+    CK(cudaEventElapsedTime(&C.select_ms, g.evb[0], g.evb[1]));
+    CK(cudaEventElapsedTime(&C.aca_ms, g.evb[1], g.evb[2]));
+    C.desc.clear();
+    C.label.clear();
+    if (C.select == 1 && C.nblocks > 0) {
+        const int n = C.nblocks;
+        std::vector<float> desc((size_t)C.ncand * 8);
+        std::vector<int> kmap(n), rank(n), cap(n);
+        CK(cudaMemcpy(desc.data(), C.d_desc, desc.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(kmap.data(), C.d_kmap, n * sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(rank.data(), C.d_rank, n * sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(cap.data(), C.d_acap, n * sizeof(int), cudaMemcpyDeviceToHost));
+        C.desc.resize((size_t)n * 8);
+        C.label.resize(n);
+        for (int b = 0; b < n; b++) {
+            std::copy(desc.begin() + (size_t)kmap[b] * 8, desc.begin() + (size_t)kmap[b] * 8 + 8,
+                      C.desc.begin() + (size_t)b * 8);
+            C.label[b] = rank[b] > 0 ? std::log2(1.0f + (float)rank[b]) : std::log2(1.0f + 2.0f * (float)cap[b]);
+        }
+    }
 }
 
 int choose_split(int ntiles, int ndstblocks)
@@ -874,7 +832,7 @@ void run_hop(int hop, int a, int b)
     MaskEntry &M = get_mask(hop, a, b);
     const bool mask_rebuilt = M.mask_ms > 0.0f;  // built for this call (reported once)
     float rec_cmp_build = 0.0f;
-    bool rec_cmp = false;
+    bool rec_cmp = false, built = false;
     if (M.nsrc == 0 || M.ndst == 0) return;
     HopSets hs = hop_sets(hop, a, b);
     SumArgs s{};
@@ -926,12 +884,13 @@ void run_hop(int hop, int a, int b)
                 Compression &C = g.cmp;
                 if (!C.valid || C.obj != a || C.kr != g.kr || C.ki != g.ki || mask_rebuilt) {
                     build_compression(a, M, s);
-                    rec_cmp_build = C.build_ms;
+                    built = true;
                 }
                 s.mask.flags = C.d_flags;  // accepted blocks are left to the low-rank path
                 CK(cudaEventRecord(g.ev4, st));
-                launch_lr_apply(s, C.d_blocks, C.d_off, C.d_bidx, C.naccepted, C.d_U, C.d_V, C.d_rank, C.d_brow, C.d_bcol,
-                                M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, st);
+                launch_lr_apply(s, C.d_blocks, C.d_off, C.d_bidx, C.nblocks, C.d_U, C.d_V, C.d_rank, C.d_brow, C.d_bcol,
+                                M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, st,
+                                C.d_nacc);
                 CK(cudaEventRecord(g.ev5, st));
                 yrow = C.d_yrow;
                 ycol = C.d_ycol;
@@ -963,6 +922,10 @@ void run_hop(int hop, int a, int b)
     CK(cudaGetLastError());
     CK(cudaEventRecord(g.ev1, st));
     CK(cudaEventSynchronize(g.ev1));
+    if (built) {
+        finish_compression();
+        rec_cmp_build = g.cmp.build_ms;
+    }
     float ms = 0.0f, sum_ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
     CK(cudaEventElapsedTime(&sum_ms, g.ev2, g.ev3));

@@ -133,12 +133,24 @@ constexpr int kLrRankLimit = 64;
 void launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                 int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
                 cudaStream_t s);
+// ndev (optional): the block count in device memory; nblocks / nb bound the grid
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
-                       const float4 *nm, float inv_lambda, float *X, cudaStream_t s);
+                       const float4 *nm, float inv_lambda, float *X, cudaStream_t s, const int *ndev = nullptr);
 void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
                      const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
-                     double2 *ycol, cudaStream_t s);
+                     double2 *ycol, cudaStream_t s, const int *ndev = nullptr);
+// select.cu: block lists of the compressed bounce, built on the device
+void launch_cand_lists(const uint8_t *flags, int nt, int nb, int select, float eta, const float4 *cen, int *cnt,
+                       int *off, int2 *blocks, uint8_t *cls, cudaStream_t s);
+void launch_keep_lists(int nb, const int *coff, const float *pred, float cut, int rmax, const int2 *cblocks,
+                       const uint8_t *ccls, int *kcnt, int *ksum, int *koff, int *kcoloff, int2 *ab, uint8_t *acls,
+                       int *acap, long long *aoff, int *kmap, cudaStream_t s);
+void launch_accept_lists(int nt, int nb, const int *koff, const int2 *ab, const int *rank, uint8_t *flags_out,
+                         uint8_t *accbm, int *qidx, int *acnt, int *byJ_off, int *bidx, int *byJ, int *icnt,
+                         int *byI_off, int *byI, cudaStream_t s);
+void launch_cmp_stats(const int *nkeep, const int2 *ab, const int *rank, const float *err, int nsrc, double *out,
+                      cudaStream_t s);
 void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s);
 // mlp.cu: the admissibility network (8 -> 128 -> 128 -> 128 -> 1, ReLU, FP32)
 size_t mlp_param_count();
