@@ -480,14 +480,23 @@ def run_gb300(args):
     train_info = None
     if "compressed" in modes and select == 2:
         # the admissibility network learns from the exact method's blocks of
-        # the same trihedral at other frequencies (untimed set-up)
+        # the same trihedral at other frequencies (untimed set-up); with
+        # --mlp-cache the trained parameters are kept in a file and reused
+        # (profiler runs then launch no training kernels)
         from sonar_render_gb300 import admissibility, scenes
         t0 = time.time()
-        train_cfgs = [scenes.trihedral_config(f, bounces=1, n_theta=0, n_phi=0) for f in (40e3, 50e3)]
-        X, y, loss = admissibility.train_on_scenes(train_cfgs, epochs=args.train_epochs, batch=256, lr=1e-3, seed=0)
-        train_info = {"samples": int(len(y)), "scenes": ["trihedral_1m_40kHz", "trihedral_1m_50kHz"],
-                      "epochs": args.train_epochs, "final_mse_log2rank": round(loss, 5),
-                      "seconds": round(time.time() - t0, 2)}
+        if args.mlp_cache and os.path.exists(args.mlp_cache):
+            admissibility.set_params(np.load(args.mlp_cache))
+            train_info = {"loaded": os.path.basename(args.mlp_cache)}
+        else:
+            train_cfgs = [scenes.trihedral_config(f, bounces=1, n_theta=0, n_phi=0) for f in (40e3, 50e3)]
+            X, y, loss = admissibility.train_on_scenes(train_cfgs, epochs=args.train_epochs, batch=256, lr=1e-3,
+                                                       seed=0)
+            train_info = {"samples": int(len(y)), "scenes": ["trihedral_1m_40kHz", "trihedral_1m_50kHz"],
+                          "epochs": args.train_epochs, "final_mse_log2rank": round(loss, 5),
+                          "seconds": round(time.time() - t0, 2)}
+            if args.mlp_cache:
+                np.save(args.mlp_cache, admissibility.get_params())
 
     load_scene(api, cfg)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
@@ -769,6 +778,8 @@ def main():
     ap.add_argument("--select", type=int, default=2,
                     help="compressed blocks: 0 separation rule, 1 every interacting block, 2 the trained network")
     ap.add_argument("--train-epochs", type=int, default=40)
+    ap.add_argument("--mlp-cache", default="",
+                    help="file (.npy) for the trained network's parameters: loaded when present, else written")
     ap.add_argument("--batch", type=int, default=1,
                     help="also run the many-source, many-frequency batch configuration (0: skip)")
     args = ap.parse_args()

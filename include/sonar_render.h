@@ -79,9 +79,13 @@ void ProjectTargetToTargetObjects(int number_reflections);
  * copies min(NumPoints, loaded) and records an error when NumPoints is short. */
 void GetFieldPointPressures(dcomplex *field_points_pressure, int NumPoints);
 
-/* :92-96 -- GL/EGL rendering is not available (no graphics stack): records the
- * reason in sonar_last_error (without making it a pending error) and returns.
- * Surface pressures are read with sonar_get_object_pressures. */
+/* :92-96 -- the picture the reference draws through EGL/GL (every facet of the
+ * target and field objects textured with its pressure colour map, camera
+ * glm::perspective(45 deg, width/height, 0.1, 10000) * glm::lookAt(eye =
+ * viewSettings[0..2], centre = [3..5], up = [6..8]), ModelGl.cpp:98-106,
+ * 222-341), rasterised by CUDA kernels instead (no graphics stack is needed)
+ * and written to `filename` as an RGB PNG, top row first.  Triangles with a
+ * vertex behind the near plane are not drawn. */
 void RenderOpenGL(int width, int height, char *filename, float viewSettings[9]);
 
 /* :98-101 -- free all device memory, drop target/field objects and points
@@ -119,6 +123,9 @@ int sonar_get_fragment_layout(int objectType, int objIdx, int *nx_ny_neg, int nf
  * phase flags of SoundVisualisationInit.  Returns the number of cells written
  * or < 0. */
 int sonar_get_surface_colours(int objectType, int objIdx, float *rgba, long long ncells);
+/* The picture of RenderOpenGL into a caller buffer: height rows of width x 3
+ * bytes (RGB), top row first.  Returns 0 or a negative code. */
+int sonar_render_image(int width, int height, const float *viewSettings, unsigned char *rgb);
 /* JSON statistics of the last projection calls (pairs, kernel ms, grazing). */
 int sonar_get_stats(char *json, int cap);
 /* Options: "split" (source splits of the sum kernels, 0 = automatic),

@@ -147,6 +147,120 @@ __global__ void k_gather(const float *X, const float *y, const int *idx, int B, 
 
 inline dim3 tiles(int cols, int rows) { return dim3((cols + kT - 1) / kT, (rows + kT - 1) / kT); }
 
+// Inference of the whole network in one kernel: the parameters are staged
+// once per CTA in shared memory (hidden layers transposed, [in][out], so
+// that the 32 lanes of a warp read 32 consecutive outputs' weights), and each
+// warp runs groups of kInferRows rows through the layers: lane l owns hidden
+// units l, l + 32, l + 64, l + 96 of every row, the activations of the group
+// pass between layers through the warp's shared-memory slice.
+constexpr int kInferRows = 8;
+constexpr int kInferWarps = 8;
+constexpr size_t kInferSmem =
+    sizeof(float) * ((size_t)kIn * kWidth + 2 * (size_t)kWidth * kWidth + 4 * kWidth + 1 +
+                     (size_t)kInferWarps * kInferRows * (kWidth + kIn));
+
+__global__ void __launch_bounds__(32 * kInferWarps) k_mlp_infer(const float *P, const float *X, int n, float *Y)
+{
+    extern __shared__ float sm[];
+    float *W1 = sm;                                   // [kIn][kWidth]
+    float *W2 = W1 + kIn * kWidth;                    // [kWidth][kWidth] (in, out)
+    float *W3 = W2 + kWidth * kWidth;                 // [kWidth][kWidth]
+    float *B1 = W3 + kWidth * kWidth, *B2 = B1 + kWidth, *B3 = B2 + kWidth, *W4 = B3 + kWidth, *B4 = W4 + kWidth;
+    float *act = B4 + 1;                              // per warp: kInferRows x kWidth, then kInferRows x kIn
+    // parameter vector: per layer W (out x in) then b (out)
+    const float *p1 = P, *pb1 = p1 + kWidth * kIn, *p2 = pb1 + kWidth, *pb2 = p2 + kWidth * kWidth,
+                *p3 = pb2 + kWidth, *pb3 = p3 + kWidth * kWidth, *p4 = pb3 + kWidth, *pb4 = p4 + kWidth;
+    for (int e = threadIdx.x; e < kWidth * kWidth; e += blockDim.x) {
+        const int o = e / kWidth, i = e - o * kWidth;
+        W2[i * kWidth + o] = p2[e];
+        W3[i * kWidth + o] = p3[e];
+    }
+    for (int e = threadIdx.x; e < kWidth * kIn; e += blockDim.x) {
+        const int o = e / kIn, i = e - o * kIn;
+        W1[i * kWidth + o] = p1[e];
+    }
+    for (int e = threadIdx.x; e < kWidth; e += blockDim.x) {
+        B1[e] = pb1[e];
+        B2[e] = pb2[e];
+        B3[e] = pb3[e];
+        W4[e] = p4[e];
+    }
+    if (threadIdx.x == 0) B4[0] = pb4[0];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float *H = act + (size_t)warp * kInferRows * (kWidth + kIn);  // [kInferRows][kWidth]
+    float *XI = H + kInferRows * kWidth;                          // [kInferRows][kIn]
+    const int ngroups = (n + kInferRows - 1) / kInferRows;
+    for (int g = blockIdx.x * kInferWarps + warp; g < ngroups; g += gridDim.x * kInferWarps) {
+        const int r0 = g * kInferRows;
+        for (int e = lane; e < kInferRows * kIn; e += 32) {
+            const int r = r0 + e / kIn;
+            XI[e] = r < n ? X[(size_t)r0 * kIn + e] : 0.0f;
+        }
+        __syncwarp();
+        float acc[kInferRows][4];
+        // layer 1: 8 -> 128, ReLU
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float b = B1[lane + 32 * q];
+#pragma unroll
+            for (int r = 0; r < kInferRows; ++r) acc[r][q] = b;
+        }
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) {
+            float w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) w[q] = W1[i * kWidth + lane + 32 * q];
+#pragma unroll
+            for (int r = 0; r < kInferRows; ++r) {
+                const float x = XI[r * kIn + i];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[r][q] = fmaf(w[q], x, acc[r][q]);
+            }
+        }
+        // layers 2 and 3: 128 -> 128, ReLU
+#pragma unroll 1
+        for (int layer = 0; layer < 2; ++layer) {
+            const float *W = layer == 0 ? W2 : W3, *Bv = layer == 0 ? B2 : B3;
+            __syncwarp();
+#pragma unroll
+            for (int r = 0; r < kInferRows; ++r)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) H[r * kWidth + lane + 32 * q] = fmaxf(acc[r][q], 0.0f);
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float b = Bv[lane + 32 * q];
+#pragma unroll
+                for (int r = 0; r < kInferRows; ++r) acc[r][q] = b;
+            }
+#pragma unroll 4
+            for (int i = 0; i < kWidth; ++i) {
+                float w[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) w[q] = W[i * kWidth + lane + 32 * q];
+#pragma unroll
+                for (int r = 0; r < kInferRows; ++r) {
+                    const float h = H[r * kWidth + i];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[r][q] = fmaf(w[q], h, acc[r][q]);
+                }
+            }
+        }
+        // output layer: 128 -> 1
+#pragma unroll
+        for (int r = 0; r < kInferRows; ++r) {
+            float v = 0.0f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v = fmaf(W4[lane + 32 * q], fmaxf(acc[r][q], 0.0f), v);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0 && r0 + r < n) Y[r0 + r] = v + B4[0];
+        }
+        __syncwarp();
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- host model
@@ -381,28 +495,27 @@ cudaError_t mlp_train(const float *X, const float *y, int n, int epochs, int bat
     return e;
 }
 
-// Predicted log2(rank) of n descriptor rows (device arrays), on stream s.
-// The activations live in a grow-only buffer kept between calls.
-static Acts g_pred;
-cudaError_t mlp_predict_dev(const float *dX, int n, float *dY, cudaStream_t s)
+// Predicted log2(1 + rank) of n descriptor rows (device arrays), on stream s,
+// by the fused inference kernel.
+cudaError_t mlp_infer_dev(const float *dX, int n, float *dY, cudaStream_t s)
 {
     if (!g_mlp.ready) return cudaErrorInvalidValue;
     if (n <= 0) return cudaSuccess;
-    if (n > g_pred.B) {
-        cudaError_t e = g_pred.alloc(n);
-        if (e != cudaSuccess) {
-            g_pred.release();
-            g_pred.B = 0;
-            return e;
-        }
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
     }
-    cudaError_t e = cudaMemcpyAsync(g_pred.a[0], dX, (size_t)n * kIn * sizeof(float), cudaMemcpyDeviceToDevice, s);
-    if (e == cudaSuccess) {
-        forward(g_pred, n, s);
-        e = cudaMemcpyAsync(dY, g_pred.a[kLayers], (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, s);
-    }
-    if (e == cudaSuccess) e = cudaGetLastError();
-    return e;
+    int dev = 0, nsm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int groups = (n + kInferRows - 1) / kInferRows;
+    const int grid = std::max(1, std::min(nsm, (groups + kInferWarps - 1) / kInferWarps));
+    k_mlp_infer<<<grid, 32 * kInferWarps, kInferSmem, s>>>(g_mlp.d_p, dX, n, dY);
+    return cudaGetLastError();
 }
 
 }  // namespace sonar

@@ -31,6 +31,9 @@
 #include "host.h"
 
 namespace sonar {
+
+bool write_png(const std::string &path, int width, int height, const unsigned char *rgb);  // png.cpp
+
 namespace {
 
 constexpr int OBJ_TARGET = 0, OBJ_SOURCE = 1, OBJ_FIELD = 2;
@@ -677,7 +680,7 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
                        9 * Arena::bytes_of(nmax, sizeof(int)) + 3 * Arena::bytes_of(nmax, sizeof(float)) +
                        Arena::bytes_of(nmax * 64, 1) + 2 * Arena::bytes_of(ngrid, 1) +
                        Arena::bytes_of(ngrid, sizeof(int)) + 2 * Arena::bytes_of(M.nsrc, sizeof(double2)) +
-                       Arena::bytes_of(4, sizeof(double)) + 8192;
+                       Arena::bytes_of((size_t)4 * cmp_stats_parts(), sizeof(double)) + 8192;
         C.arena.reserve(bytes);
     }
     Arena &ar = C.arena;
@@ -694,7 +697,7 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     float *d_pred = nullptr;
     if (select == 2) {
         d_pred = ar.take<float>(nmax);
-        CK(mlp_predict_dev(C.d_desc, (int)nmax, d_pred, st));  // rows past the candidate count are not read
+        CK(mlp_infer_dev(C.d_desc, (int)nmax, d_pred, st));  // rows past the candidate count are not read
     }
     // ---- kept blocks, rank caps, factor columns
     int *d_kcnt = ar.take<int>(nb), *d_ksum = ar.take<int>(nb);
@@ -751,7 +754,7 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     launch_accept_lists(nt, nb, d_koff, C.d_blocks, C.d_rank, C.d_flags, d_accbm, d_qidx, d_acnt, C.d_byJ_off, C.d_bidx,
                         C.d_byJ, d_icnt, C.d_byI_off, C.d_byI, st);
     C.d_nacc = C.d_byJ_off + nb;
-    C.d_stats = ar.take<double>(4);
+    C.d_stats = ar.take<double>((size_t)4 * cmp_stats_parts());
     launch_cmp_stats(d_koff + nb, C.d_blocks, C.d_rank, C.d_err, M.nsrc, C.d_stats, st);
     C.d_yrow = ar.take<double2>(M.nsrc);
     C.d_ycol = ar.take<double2>(M.nsrc);
@@ -767,8 +770,15 @@ void finish_compression()
     Compression &C = g.cmp;
     if (!C.stats_pending) return;
     C.stats_pending = false;
+    std::vector<double> part((size_t)4 * cmp_stats_parts());
+    CK(cudaMemcpy(part.data(), C.d_stats, part.size() * sizeof(double), cudaMemcpyDeviceToHost));
     double st[4] = {0.0, 0.0, 0.0, 0.0};
-    CK(cudaMemcpy(st, C.d_stats, sizeof(st), cudaMemcpyDeviceToHost));
+    for (size_t b = 0; b < part.size() / 4; b++) {
+        st[0] += part[4 * b];
+        st[1] += part[4 * b + 1];
+        st[2] = std::max(st[2], part[4 * b + 2]);
+        st[3] += part[4 * b + 3];
+    }
     C.naccepted = (int)st[0];
     C.mean_rank = st[0] > 0.0 ? st[1] / st[0] : 0.0;
     C.max_err = st[2];
@@ -956,6 +966,144 @@ void need_render()
     if (!g.rendered) fail(-5, "render_cuda has not been called");
 }
 
+// ---------------------------------------------------------------- headless rendering
+// glm::perspective(radians(45), width / height, 0.1, 10000) times
+// glm::lookAt(eye, centre, up) (src/ModelGl.cpp:98-106), row-major.
+void camera_matrix(int width, int height, const float *vs, float *M)
+{
+    const float fovy = 45.0f * (float)M_PI / 180.0f, aspect = (float)width / (float)height;
+    const float zn = 0.1f, zf = 10000.0f, th = std::tan(fovy / 2.0f);
+    float P[16] = {1.0f / (aspect * th), 0, 0, 0, 0, 1.0f / th, 0, 0, 0, 0, -(zf + zn) / (zf - zn),
+                   -(2.0f * zf * zn) / (zf - zn), 0, 0, -1.0f, 0};
+    const float ex = vs[0], ey = vs[1], ez = vs[2];
+    float fx = vs[3] - ex, fy = vs[4] - ey, fz = vs[5] - ez;
+    float L = std::sqrt(fx * fx + fy * fy + fz * fz);
+    if (!(L > 0.0f)) fail(-6, "view settings: the camera looks at its own position");
+    fx /= L; fy /= L; fz /= L;
+    const float ux0 = vs[6], uy0 = vs[7], uz0 = vs[8];
+    float sx = fy * uz0 - fz * uy0, sy = fz * ux0 - fx * uz0, sz = fx * uy0 - fy * ux0;
+    L = std::sqrt(sx * sx + sy * sy + sz * sz);
+    if (!(L > 0.0f)) fail(-6, "view settings: the up vector is parallel to the view direction");
+    sx /= L; sy /= L; sz /= L;
+    const float ux = sy * fz - sz * fy, uy = sz * fx - sx * fz, uz = sx * fy - sy * fx;
+    const float V[16] = {sx, sy, sz, -(sx * ex + sy * ey + sz * ez), ux, uy, uz, -(ux * ex + uy * ey + uz * ez),
+                         -fx, -fy, -fz, fx * ex + fy * ey + fz * ez, 0, 0, 0, 1};
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) {
+            float acc = 0.0f;
+            for (int k = 0; k < 4; k++) acc += P[4 * r + k] * V[4 * k + c];
+            M[4 * r + c] = acc;
+        }
+}
+
+// The picture RenderOpenGL draws, into rgb (height x width x 3, top row first).
+void render_image(int width, int height, const float *vs, unsigned char *rgb_host)
+{
+    need_render();
+    if (width <= 0 || height <= 0 || (long long)width * height > (1LL << 28))
+        fail(-6, "render: image size %d x %d out of range", width, height);
+    if (!vs || !rgb_host) fail(-6, "render: null argument");
+    for (int k = 0; k < 9; k++)
+        if (!std::isfinite(vs[k])) fail(-6, "render: non-finite view setting");
+    RasterArgs ra{};
+    camera_matrix(width, height, vs, ra.mvp);
+    ra.width = width;
+    ra.height = height;
+    // triangles and textures: target objects, then field objects (ModelGl.cpp:311-319)
+    std::vector<RasterTri> tris;
+    std::vector<RasterTex> tex;
+    long long cells = 0;
+    std::vector<std::pair<Object *, long long>> objs;
+    for (int t : {OBJ_TARGET, OBJ_FIELD})
+        for (auto &o : g.obj[t]) {
+            objs.push_back({o.get(), cells});
+            for (size_t f = 0; f < o->facets.size(); f++) {
+                const FacetFrame &F = o->facets[f];
+                RasterTri T{};
+                const Vec3 vv[3] = {F.v1, F.v2, F.v3};
+                // texture coordinates: base origin (0, 0), base end (1, 0), apex
+                // (BaseLengthNeg / BaseLength, 1) (src/Facet.cpp:18-60)
+                const float e[3] = {std::sqrt((F.v1.x - F.v2.x) * (F.v1.x - F.v2.x) + (F.v1.y - F.v2.y) * (F.v1.y - F.v2.y) +
+                                              (F.v1.z - F.v2.z) * (F.v1.z - F.v2.z)),
+                                    std::sqrt((F.v1.x - F.v3.x) * (F.v1.x - F.v3.x) + (F.v1.y - F.v3.y) * (F.v1.y - F.v3.y) +
+                                              (F.v1.z - F.v3.z) * (F.v1.z - F.v3.z)),
+                                    std::sqrt((F.v2.x - F.v3.x) * (F.v2.x - F.v3.x) + (F.v2.y - F.v3.y) * (F.v2.y - F.v3.y) +
+                                              (F.v2.z - F.v3.z) * (F.v2.z - F.v3.z))};
+                int m = 0;
+                if (e[1] > e[m]) m = 1;
+                if (e[2] > e[m]) m = 2;
+                const int origin = m == 2 ? 1 : 0, end = m == 0 ? 1 : 2, apex = m == 0 ? 2 : (m == 1 ? 1 : 0);
+                const float ua = F.baseNeg / (F.basePos + F.baseNeg);
+                for (int k = 0; k < 3; k++) T.v[k] = make_float4(vv[k].x, vv[k].y, vv[k].z, 1.0f);
+                T.uv[origin] = make_float2(0.0f, 0.0f);
+                T.uv[end] = make_float2(1.0f, 0.0f);
+                T.uv[apex] = make_float2(ua, 1.0f);
+                T.facet = (int)tex.size();
+                tris.push_back(T);
+                tex.push_back(RasterTex{cells + o->cell0[f], std::max(F.nx, 1), std::max(F.ny, 1)});
+            }
+            cells += o->ncells;
+        }
+    // work list: 32 x 32-pixel tiles of each triangle's screen box
+    const int tile = raster_tile();
+    std::vector<int4> work;
+    for (size_t i = 0; i < tris.size(); i++) {
+        float xmin = 3e38f, xmax = -3e38f, ymin = 3e38f, ymax = -3e38f;
+        bool ok = true;
+        for (int k = 0; k < 3; k++) {
+            const float4 v = tris[i].v[k];
+            const float *M = ra.mvp;
+            const float cx = M[0] * v.x + M[1] * v.y + M[2] * v.z + M[3];
+            const float cy = M[4] * v.x + M[5] * v.y + M[6] * v.z + M[7];
+            const float cw = M[12] * v.x + M[13] * v.y + M[14] * v.z + M[15];
+            if (!(cw > 0.1f)) ok = false;
+            const float sx = (cx / cw + 1.0f) * 0.5f * width, sy = (cy / cw + 1.0f) * 0.5f * height;
+            xmin = std::min(xmin, sx); xmax = std::max(xmax, sx);
+            ymin = std::min(ymin, sy); ymax = std::max(ymax, sy);
+        }
+        if (!ok || xmax < 0.0f || ymax < 0.0f || xmin > (float)width || ymin > (float)height) continue;
+        const int tx0 = std::max(0, (int)std::floor(xmin) / tile), tx1 = std::min((width - 1) / tile, (int)std::ceil(xmax) / tile);
+        const int ty0 = std::max(0, (int)std::floor(ymin) / tile), ty1 = std::min((height - 1) / tile, (int)std::ceil(ymax) / tile);
+        for (int ty = ty0; ty <= ty1; ty++)
+            for (int tx = tx0; tx <= tx1; tx++) work.push_back(make_int4((int)i, tx, ty, 0));
+    }
+    cudaStream_t st = g.stream;
+    RasterTri *d_tris = dalloc<RasterTri>(tris.size());
+    RasterTex *d_tex = dalloc<RasterTex>(tex.size());
+    float4 *d_col = dalloc<float4>((size_t)std::max<long long>(cells, 1));
+    int4 *d_work = dalloc<int4>(work.size());
+    unsigned long long *d_z = dalloc<unsigned long long>((size_t)width * height);
+    unsigned char *d_rgb = dalloc<unsigned char>((size_t)width * height * 3);
+    cudaError_t e = cudaSuccess;
+    if (!tris.empty()) e = cudaMemcpyAsync(d_tris, tris.data(), tris.size() * sizeof(RasterTri), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !tex.empty())
+        e = cudaMemcpyAsync(d_tex, tex.data(), tex.size() * sizeof(RasterTex), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !work.empty())
+        e = cudaMemcpyAsync(d_work, work.data(), work.size() * sizeof(int4), cudaMemcpyHostToDevice, st);
+    for (auto &oc : objs) {
+        Object *o = oc.first;
+        if (e != cudaSuccess || o->ncells == 0) continue;
+        const int phase = o->type == OBJ_FIELD ? g.phase_field : g.phase_target;
+        launch_colour_map(o->d_P, o->ncells, g.min_db, g.max_db, phase, d_col + oc.second, st);
+    }
+    ra.tris = d_tris;
+    ra.tex = d_tex;
+    ra.colours = d_col;
+    ra.work = d_work;
+    ra.zbuf = d_z;
+    ra.rgb = d_rgb;
+    if (e == cudaSuccess) {
+        launch_raster(ra, (int)work.size(), st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(rgb_host, d_rgb, (size_t)width * height * 3, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dfree(d_tris); dfree(d_tex); dfree(d_col); dfree(d_work); dfree(d_z); dfree(d_rgb);
+    if (e != cudaSuccess) fail(-10, "render failed: %s", cudaGetErrorString(e));
+    g.launches += 3 + (long long)objs.size();
+}
+
 // ---------------------------------------------------------------- ABI glue
 template <class F>
 int guarded(F &&f)
@@ -1119,10 +1267,12 @@ void GetFieldPointPressures(dcomplex *field_points_pressure, int NumPoints)
 
 void RenderOpenGL(int width, int height, char *filename, float viewSettings[9])
 {
-    (void)width; (void)height; (void)filename; (void)viewSettings;
-    // not sticky: the scene stays usable (run_scripts call this before TearDownCuda)
-    g.err = "RenderOpenGL: no graphics stack; read surfaces with sonar_get_object_pressures";
-    if (g.verbose) fprintf(stderr, "sonar: %s\n", g.err.c_str());
+    guarded([&] {
+        if (!filename) fail(-6, "RenderOpenGL: null file name");
+        std::vector<unsigned char> rgb((size_t)std::max(width, 0) * std::max(height, 0) * 3);
+        render_image(width, height, viewSettings, rgb.data());
+        if (!write_png(filename, width, height, rgb.data())) fail(-7, "RenderOpenGL: cannot write %s", filename);
+    });
 }
 
 void TearDownCuda(void)
@@ -1369,6 +1519,11 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
     return st != 0 ? st : nbytes;
 }
 
+int sonar_render_image(int width, int height, const float *viewSettings, unsigned char *rgb)
+{
+    return guarded([&] { render_image(width, height, viewSettings, rgb); });
+}
+
 int sonar_get_surface_colours(int objectType, int objIdx, float *rgba, long long ncells)
 {
     int written = 0;
@@ -1481,7 +1636,7 @@ int sonar_mlp_predict(const float *X, int n, float *out)
         if (n == 0) return;
         float *dX = dalloc<float>((size_t)n * 8), *dY = dalloc<float>(n);
         cudaError_t e = cudaMemcpy(dX, X, (size_t)n * 8 * sizeof(float), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = mlp_predict_dev(dX, n, dY, 0);
+        if (e == cudaSuccess) e = mlp_infer_dev(dX, n, dY, 0);
         if (e == cudaSuccess) e = cudaMemcpy(out, dY, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
         dfree(dX);
         dfree(dY);

@@ -245,17 +245,21 @@ __global__ void __launch_bounds__(kSelThreads) k_byI_fill(const uint8_t *accbm, 
 }
 
 // statistics of the accepted blocks: count, rank sum, largest judged error,
-// ordered pairs (one CTA, fixed order)
+// ordered pairs; one partial per CTA (grid-stride over the kept blocks), the
+// host adds the partials in order
+constexpr int kStatCtas = 128;
+
 __global__ void __launch_bounds__(kSelThreads) k_cmp_stats(const int *nkeep, const int2 *ab, const int *rank,
-                                                           const float *err, int nsrc, double *out)
+                                                           const float *err, int nsrc, double *part)
 {
-    __shared__ double sd[3][kSelThreads];
+    __shared__ double sd[4][kSelThreads];
     const int n = *nkeep;
     double na = 0.0, rs = 0.0, pairs = 0.0, emax = 0.0;
-    for (int k = threadIdx.x; k < n; k += kSelThreads) {
-        if (rank[k] > 0) {
+    for (int k = blockIdx.x * kSelThreads + threadIdx.x; k < n; k += gridDim.x * kSelThreads) {
+        const int r = rank[k];
+        if (r > 0) {
             na += 1.0;
-            rs += rank[k];
+            rs += r;
             emax = fmax(emax, (double)err[k]);
             const double ni = min(kTile, nsrc - ab[k].x * kTile), nj = min(kTile, nsrc - ab[k].y * kTile);
             pairs += 2.0 * ni * nj;
@@ -263,27 +267,19 @@ __global__ void __launch_bounds__(kSelThreads) k_cmp_stats(const int *nkeep, con
     }
     sd[0][threadIdx.x] = na;
     sd[1][threadIdx.x] = rs;
-    sd[2][threadIdx.x] = pairs;
+    sd[2][threadIdx.x] = emax;
+    sd[3][threadIdx.x] = pairs;
     __syncthreads();
     for (int s = kSelThreads / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s)
-            for (int q = 0; q < 3; ++q) sd[q][threadIdx.x] += sd[q][threadIdx.x + s];
+        if (threadIdx.x < s) {
+            sd[0][threadIdx.x] += sd[0][threadIdx.x + s];
+            sd[1][threadIdx.x] += sd[1][threadIdx.x + s];
+            sd[2][threadIdx.x] = fmax(sd[2][threadIdx.x], sd[2][threadIdx.x + s]);
+            sd[3][threadIdx.x] += sd[3][threadIdx.x + s];
+        }
         __syncthreads();
     }
-    // the maximum: reduce through the same buffer
-    __shared__ double se[kSelThreads];
-    se[threadIdx.x] = emax;
-    __syncthreads();
-    for (int s = kSelThreads / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) se[threadIdx.x] = fmax(se[threadIdx.x], se[threadIdx.x + s]);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        out[0] = sd[0][0];
-        out[1] = sd[1][0];
-        out[2] = se[0];
-        out[3] = sd[2][0];
-    }
+    if (threadIdx.x < 4) part[blockIdx.x * 4 + threadIdx.x] = sd[threadIdx.x][0];
 }
 
 }  // namespace
@@ -325,10 +321,12 @@ void launch_accept_lists(int nt, int nb, const int *koff, const int2 *ab, const 
     }
 }
 
+int cmp_stats_parts() { return kStatCtas; }
+
 void launch_cmp_stats(const int *nkeep, const int2 *ab, const int *rank, const float *err, int nsrc, double *out,
                       cudaStream_t s)
 {
-    k_cmp_stats<<<1, kSelThreads, 0, s>>>(nkeep, ab, rank, err, nsrc, out);
+    k_cmp_stats<<<kStatCtas, kSelThreads, 0, s>>>(nkeep, ab, rank, err, nsrc, out);
 }
 
 }  // namespace sonar

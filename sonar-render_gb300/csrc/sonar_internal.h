@@ -149,6 +149,8 @@ void launch_keep_lists(int nb, const int *coff, const float *pred, float cut, in
 void launch_accept_lists(int nt, int nb, const int *koff, const int2 *ab, const int *rank, uint8_t *flags_out,
                          uint8_t *accbm, int *qidx, int *acnt, int *byJ_off, int *bidx, int *byJ, int *icnt,
                          int *byI_off, int *byI, cudaStream_t s);
+// out: cmp_stats_parts() x 4 doubles (accepted, rank sum, largest error, ordered pairs) to add in order
+int cmp_stats_parts();
 void launch_cmp_stats(const int *nkeep, const int2 *ab, const int *rank, const float *err, int nsrc, double *out,
                       cudaStream_t s);
 void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s);
@@ -161,7 +163,7 @@ cudaError_t mlp_get_params(float *p, size_t n);
 cudaError_t mlp_grad(const float *X, const float *y, int B, float *grad, float *loss);
 cudaError_t mlp_train(const float *X, const float *y, int n, int epochs, int batch, float lr, unsigned seed,
                       float *last_loss);
-cudaError_t mlp_predict_dev(const float *dX, int n, float *dY, cudaStream_t s);
+cudaError_t mlp_infer_dev(const float *dX, int n, float *dY, cudaStream_t s);  // fused inference kernel
 // surface.cu: pressure -> RGBA colour map of the reference's surface textures
 void launch_colour_map(const double2 *P, long long n, float min_db, float max_db, int phase, float4 *out,
                        cudaStream_t s);
@@ -208,6 +210,29 @@ cudaError_t batch_prepare();        // dynamic shared-memory limits of the batch
 void launch_batch(const BatchArgs &a, int kc, int grid, bool att, cudaStream_t s);
 void launch_batch_reduce(const float *partial, const int *item_seg_off, const int *item_segs, int nitems, int nrx,
                          int nsrc, double2 *out, cudaStream_t s);
+
+// raster.cu: headless rendering of the textured facets (RenderOpenGL)
+struct RasterTri {
+    float4 v[3];                   // vertices (w unused)
+    float2 uv[3];                  // texture coordinates of the vertices
+    int facet, pad;                // index into the facet texture table
+};
+struct RasterTex {
+    long long cell0;               // first colour cell of the facet
+    int nx, ny;                    // texture size (the facet's fragment grid)
+};
+struct RasterArgs {
+    const RasterTri *tris;
+    const RasterTex *tex;
+    const float4 *colours;         // RGBA per cell
+    const int4 *work;              // (triangle, tile x, tile y, -)
+    float mvp[16];                 // row-major, clip = M [x y z 1]
+    int width, height;
+    unsigned long long *zbuf;      // width x height
+    unsigned char *rgb;            // height x width x 3, top row first
+};
+int raster_tile();
+void launch_raster(const RasterArgs &a, int nwork, cudaStream_t s);
 
 // FP32 FMA rate in FLOP/s (which = 0) or MUFU sine rate in op/s (which = 1)
 // on the current device; < 0 on failure.

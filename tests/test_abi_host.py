@@ -134,12 +134,19 @@ def test_cell_count_before_render(api, scenes):
     api.TearDownCuda()
 
 
-def test_render_opengl_is_headless_and_not_sticky(api):
+def test_render_opengl_needs_a_rendered_scene(api, tmp_path):
+    """RenderOpenGL draws headless (CUDA rasteriser); without render_cuda it
+    records an error instead of drawing, and TearDownCuda clears it."""
     api.TearDownCuda()
-    api.render_openGL(64, 64, [0.0] * 9, "x")
-    assert "graphics" in api.last_error()
-    assert api.status() == 0
+    out = str(tmp_path / "x.png")
+    L = api.lib()
+    vs = (C.c_float * 9)(10.0, 10.0, 10.0, 0.0, 0.0, 0.0, 0.0, 1.0, 0.0)
+    L.RenderOpenGL(64, 64, out.encode(), vs)
+    assert L.sonar_status() != 0
+    assert "render_cuda" in api.last_error()
+    assert not os.path.exists(out)
     api.TearDownCuda()
+    assert L.sonar_status() == 0
 
 
 def test_options(api):
