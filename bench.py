@@ -166,12 +166,15 @@ def step_pairs(stats):
 
 
 RCUT = [24.0]  # the admissibility network proposes blocks with predicted rank below this
+TOL = [1e-4]   # cross-approximation tolerance (the judge accepts 3 x this RMS error)
 
 
 def set_path(api, compressed, select):
     api.set_option("compress", 1 if compressed else 0)
     api.set_option("compress_select", select if compressed else 0)
     api.set_option("compress_rcut", RCUT[0])
+    api.set_option("compress_tol", TOL[0])
+    api.set_option("compress_judge", 3.0 * TOL[0])
 
 
 def time_path(api, cfg, args, flush, local, world):
@@ -576,7 +579,7 @@ def run_gb300(args):
                        [h["cmp_select"]], "candidate_blocks": h["cmp_cand"], "approximated": h["cmp_blocks"],
                        "accepted": h["cmp_accepted"], "pair_fraction_compressed": round(h["cmp_pairs"] / h["pairs"], 4),
                        "mean_rank": h["cmp_mean_rank"], "max_judged_block_err": h["cmp_max_err"],
-                       "tolerance": 1e-4, "judge_limit": 3e-4, "network_training": train_info}
+                       "tolerance": TOL[0], "judge_limit": 3.0 * TOL[0], "network_training": train_info}
     kms = H["kernels_ms_per_step"]
     kshare = {k: round(v / H["ms_per_step"], 4) for k, v in kms.items()}
     roof_lr = lowrank_roofline(st) if head == "compressed" else None
@@ -773,6 +776,8 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
     ap.add_argument("--mode", default="both", choices=["both", "plain", "compressed"])
+    ap.add_argument("--tol", type=float, default=1e-4,
+                    help="cross-approximation tolerance of the compressed path (judge limit 3 x tol)")
     ap.add_argument("--rcut", type=float, default=24.0,
                     help="network: propose blocks whose predicted rank is below this")
     ap.add_argument("--select", type=int, default=2,
@@ -786,6 +791,7 @@ def main():
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     RCUT[0] = args.rcut
+    TOL[0] = args.tol
     if args.impl == "reference":
         run_reference(args)
     else:

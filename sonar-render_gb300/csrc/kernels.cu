@@ -1777,7 +1777,7 @@ __global__ void __launch_bounds__(kTile) k_lr_block(SumArgs a, const int2 *block
                                                     const int *bidx, int nb, const float2 *U, const float2 *V,
                                                     const int *rank, float2 *brow, float2 *bcol, const int *ndev)
 {
-    __shared__ float4 sRed[kTile / 32][kLrMaxRank];
+    __shared__ float4 sW[kTile];  // (Re w_I, Im w_I, Re w_J, Im w_J) of every row t
     __shared__ float2 sTv[kLrMaxRank], sSu[kLrMaxRank];
     const int q = blockIdx.x;
     if (q >= (ndev ? min(*ndev, nb) : nb)) return;
@@ -1785,13 +1785,25 @@ __global__ void __launch_bounds__(kTile) k_lr_block(SumArgs a, const int2 *block
     const int k = rank[b];
     const int I = blocks[b].x, J = blocks[b].y, t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int i = I * kTile + t, j = J * kTile + t;
-    const float wir = i < a.nsrc ? a.srcA[i].w : 0.0f, wii = i < a.nsrc ? a.srcB[i].w : 0.0f;
-    const float wjr = j < a.nsrc ? a.srcA[j].w : 0.0f, wji = j < a.nsrc ? a.srcB[j].w : 0.0f;
-    const float2 *Ub = U + off[b] * kTile + t, *Vb = V + off[b] * kTile + t;
-    for (int m = 0; m < k; ++m) {
-        const float2 v = Vb[m * kTile], u = Ub[m * kTile];
-        float4 p = make_float4(v.x * wir - v.y * wii, v.x * wii + v.y * wir, u.x * wjr - u.y * wji,
-                               u.x * wji + u.y * wjr);
+    sW[t] = make_float4(i < a.nsrc ? a.srcA[i].w : 0.0f, i < a.nsrc ? a.srcB[i].w : 0.0f,
+                        j < a.nsrc ? a.srcA[j].w : 0.0f, j < a.nsrc ? a.srcB[j].w : 0.0f);
+    const float2 *U0 = U + off[b] * kTile, *V0 = V + off[b] * kTile;
+    const float2 *Ub = U0 + t, *Vb = V0 + t;
+    __syncthreads();
+    // projections V^T w_I and U^T w_J: warp w takes the ranks m = w (mod 8),
+    // each lane 8 rows, one warp reduction per rank
+    for (int m = warp; m < k; m += kTile / 32) {
+        float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+        for (int r = 0; r < kTile / 32; ++r) {
+            const int tt = lane + 32 * r;
+            const float2 v = __ldg(V0 + (size_t)m * kTile + tt), u = __ldg(U0 + (size_t)m * kTile + tt);
+            const float4 w = sW[tt];
+            p.x = fmaf(v.x, w.x, fmaf(-v.y, w.y, p.x));
+            p.y = fmaf(v.x, w.y, fmaf(v.y, w.x, p.y));
+            p.z = fmaf(u.x, w.z, fmaf(-u.y, w.w, p.z));
+            p.w = fmaf(u.x, w.w, fmaf(u.y, w.z, p.w));
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             p.x += __shfl_xor_sync(0xffffffffu, p.x, o);
@@ -1799,21 +1811,10 @@ __global__ void __launch_bounds__(kTile) k_lr_block(SumArgs a, const int2 *block
             p.z += __shfl_xor_sync(0xffffffffu, p.z, o);
             p.w += __shfl_xor_sync(0xffffffffu, p.w, o);
         }
-        if (lane == 0) sRed[warp][m] = p;
-    }
-    __syncthreads();
-    if (t < k) {
-        float4 s4 = sRed[0][t];
-#pragma unroll
-        for (int w = 1; w < kTile / 32; ++w) {
-            const float4 p = sRed[w][t];
-            s4.x += p.x;
-            s4.y += p.y;
-            s4.z += p.z;
-            s4.w += p.w;
+        if (lane == 0) {
+            sTv[m] = make_float2(p.x, p.y);
+            sSu[m] = make_float2(p.z, p.w);
         }
-        sTv[t] = make_float2(s4.x, s4.y);
-        sSu[t] = make_float2(s4.z, s4.w);
     }
     __syncthreads();
     float rr = 0.0f, ri = 0.0f, cr = 0.0f, ci = 0.0f;
@@ -1829,28 +1830,42 @@ __global__ void __launch_bounds__(kTile) k_lr_block(SumArgs a, const int2 *block
 }
 
 // Per owner tile X: rows of every accepted block with J = X and columns of
-// every accepted block with I = X, in list order, summed in FP64
-// (deterministic).  The lists hold accepted-block positions q.
+// every accepted block with I = X, in list order, summed with compensated
+// FP32 (Kahan) arithmetic -- FP64 adds run at a small fraction of the FP32
+// rate on this GPU -- and stored as FP64 (deterministic order).  The lists
+// hold accepted-block positions q.
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
+{
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
 __global__ void __launch_bounds__(kTile) k_lr_gather(int n, const float2 *brow, const float2 *bcol,
                                                      const int *byJ_off, const int *byJ, const int *byI_off,
                                                      const int *byI, double2 *yrow, double2 *ycol)
 {
     const int X = blockIdx.x, t = threadIdx.x;
     const int q = X * kTile + t;
-    double fr = 0.0, fi = 0.0, cr = 0.0, ci = 0.0;
-    for (int p = byJ_off[X]; p < byJ_off[X + 1]; ++p) {
-        const float2 v = brow[(size_t)byJ[p] * kTile + t];
-        fr += (double)v.x;
-        fi += (double)v.y;
+    float fr = 0.0f, fi = 0.0f, cr = 0.0f, ci = 0.0f;
+    float efr = 0.0f, efi = 0.0f, ecr = 0.0f, eci = 0.0f;
+    const int j0 = byJ_off[X], j1 = byJ_off[X + 1], i0 = byI_off[X], i1 = byI_off[X + 1];
+#pragma unroll 4
+    for (int p = j0; p < j1; ++p) {
+        const float2 v = __ldg(brow + (size_t)byJ[p] * kTile + t);
+        kahan_add(fr, efr, v.x);
+        kahan_add(fi, efi, v.y);
     }
-    for (int p = byI_off[X]; p < byI_off[X + 1]; ++p) {
-        const float2 v = bcol[(size_t)byI[p] * kTile + t];
-        cr += (double)v.x;
-        ci += (double)v.y;
+#pragma unroll 4
+    for (int p = i0; p < i1; ++p) {
+        const float2 v = __ldg(bcol + (size_t)byI[p] * kTile + t);
+        kahan_add(cr, ecr, v.x);
+        kahan_add(ci, eci, v.y);
     }
     if (q < n) {
-        yrow[q] = make_double2(fr, fi);
-        ycol[q] = make_double2(cr, ci);
+        yrow[q] = make_double2((double)fr - (double)efr, (double)fi - (double)efi);
+        ycol[q] = make_double2((double)cr - (double)ecr, (double)ci - (double)eci);
     }
 }
 
