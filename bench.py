@@ -167,6 +167,7 @@ def step_pairs(stats):
 
 RCUT = [24.0]  # the admissibility network proposes blocks with predicted rank below this
 TOL = [1e-4]   # cross-approximation tolerance (the judge accepts 3 x this RMS error)
+ACA_VARIANT = [0]  # cross-approximation kernel shape (factor ranks in shared memory, CTAs per SM)
 
 
 def set_path(api, compressed, select):
@@ -175,6 +176,7 @@ def set_path(api, compressed, select):
     api.set_option("compress_rcut", RCUT[0])
     api.set_option("compress_tol", TOL[0])
     api.set_option("compress_judge", 3.0 * TOL[0])
+    api.set_option("aca_variant", ACA_VARIANT[0])
 
 
 def time_path(api, cfg, args, flush, local, world):
@@ -776,6 +778,9 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
     ap.add_argument("--mode", default="both", choices=["both", "plain", "compressed"])
+    ap.add_argument("--aca-variant", type=int, default=0, choices=(0, 1, 2),
+                    help="cross-approximation kernel: 0 = 8 factor ranks in shared memory, 4 CTAs per SM; "
+                         "1 = 12 ranks, 4 CTAs; 2 = 16 ranks, 3 CTAs")
     ap.add_argument("--tol", type=float, default=1e-4,
                     help="cross-approximation tolerance of the compressed path (judge limit 3 x tol)")
     ap.add_argument("--rcut", type=float, default=24.0,
@@ -791,6 +796,7 @@ def main():
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     RCUT[0] = args.rcut
+    ACA_VARIANT[0] = args.aca_variant
     TOL[0] = args.tol
     if args.impl == "reference":
         run_reference(args)

@@ -1460,20 +1460,20 @@ __device__ __forceinline__ void warp_argmax(float &v, int &idx)
 }
 
 constexpr int kAcaMaxZeroRows = 48;
-constexpr int kAcaRegRanks = 16;  // factor entries a thread keeps in registers; higher ranks are re-read from global
 constexpr int kAcaWarps = kTile / 32;
 
 // Block-wide argmax (ARG) of v >= 0 over the threads with valid set and
 // block-wide sums (SUMS) of s0 and s1; every thread receives the results
 // (v = -1 when no thread was valid).  The argmax key is the value's float
 // bits with the low 8 mantissa bits replaced by 255 - idx (idx < 256): the
-// largest value to 2^-15 relative wins, ties go to the lowest index; a warp
-// reduction (redux.sync) then a shared-memory atomicMax, which is
-// order-independent.  The sums go through one slot per warp, added in warp
-// order (deterministic).  One barrier.  The key must be zero on entry; the
-// caller resets it once every thread has read it.
+// largest value to 2^-15 relative wins, ties go to the lowest index.  A warp
+// reduction (redux.sync) leaves one key per warp in slot[warp]; after the
+// barrier every thread takes the maximum of the eight slots.  The sums go
+// through one slot per warp, added in warp order (deterministic).  One
+// barrier.  A slot array is rewritten only after every thread has passed a
+// later barrier, so callers give each reduction site its own slots.
 template <bool ARG, bool SUMS>
-__device__ __forceinline__ void cta_reduce(float &v, int &idx, bool valid, float &s0, float &s1, unsigned *key,
+__device__ __forceinline__ void cta_reduce(float &v, int &idx, bool valid, float &s0, float &s1, unsigned *slot,
                                            float2 *sums)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1490,12 +1490,14 @@ __device__ __forceinline__ void cta_reduce(float &v, int &idx, bool valid, float
         }
     }
     if (lane == 0) {
-        if (ARG && k) atomicMax(key, k);
+        if (ARG) slot[warp] = k;
         if (SUMS) sums[warp] = make_float2(s0, s1);
     }
     __syncthreads();
     if (ARG) {
-        const unsigned w = *key;
+        static_assert(kAcaWarps == 8, "two 16-byte slot reads");
+        const uint4 a = reinterpret_cast<const uint4 *>(slot)[0], b = reinterpret_cast<const uint4 *>(slot)[1];
+        const unsigned w = max(max(max(a.x, a.y), max(a.z, a.w)), max(max(b.x, b.y), max(b.z, b.w)));
         v = w ? __uint_as_float((w & 0xFFFFFF00u) - 0x100u) : -1.0f;
         idx = (int)(255u - (w & 0xFFu));
     }
@@ -1512,44 +1514,6 @@ __device__ __forceinline__ void cta_reduce(float &v, int &idx, bool valid, float
     }
 }
 
-// Statement S for every register-held rank m < n (n uniform across the CTA),
-// in groups of four so that register indices stay static.
-#define ACA_REG_GROUP(m0, n, S)                                  \
-    _Pragma("unroll") for (int m = (m0); m < (m0) + 4; ++m) if (m < (n)) \
-    {                                                            \
-        S;                                                       \
-    }
-#define ACA_REG_LOOP(n, S)                                       \
-    do {                                                         \
-        ACA_REG_GROUP(0, n, S)                                   \
-        if ((n) > 4) {                                           \
-            ACA_REG_GROUP(4, n, S)                               \
-            if ((n) > 8) {                                       \
-                ACA_REG_GROUP(8, n, S)                           \
-                if ((n) > 12) { ACA_REG_GROUP(12, n, S) }        \
-            }                                                    \
-        }                                                        \
-    } while (0)
-// Statement S for the register slot m == n only.
-#define ACA_REG_SLOT(m0, n, S)                                      \
-    _Pragma("unroll") for (int m = (m0); m < (m0) + 4; ++m) if (m == (n)) \
-    {                                                               \
-        S;                                                          \
-    }
-#define ACA_REG_SET(n, S)                   \
-    do {                                    \
-        if ((n) < 4) {                      \
-            ACA_REG_SLOT(0, n, S)           \
-        } else if ((n) < 8) {               \
-            ACA_REG_SLOT(4, n, S)           \
-        } else if ((n) < 12) {              \
-            ACA_REG_SLOT(8, n, S)           \
-        } else {                            \
-            ACA_REG_SLOT(12, n, S)          \
-        }                                   \
-    } while (0)
-static_assert(kAcaRegRanks == 16, "ACA_REG_LOOP and ACA_REG_SET cover 16 register-held ranks");
-
 // x - u v (complex)
 __device__ __forceinline__ float2 csub_mul(float2 x, float2 u, float2 v)
 {
@@ -1558,22 +1522,31 @@ __device__ __forceinline__ float2 csub_mul(float2 x, float2 u, float2 v)
     return x;
 }
 
-// One CTA per block, thread t owns row t and column t of the block.  Its own
-// fragment data (column: source i = t, row: destination j = t) and its
-// entries of the first kAcaRegRanks factor columns stay in registers; the
-// pivot row's U entries and the pivot column's V entries are published
-// through shared memory.  Four barriers per rank step.  The factors are also
-// written to U and V (the low-rank apply reads them there); ranks past
-// kAcaRegRanks are re-read from there, and with one block per CTA the
-// factors of the blocks in flight stay in L2.
-template <bool ATT>
-__global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks, const uint8_t *cls, const int *cap,
-                                                  const long long *off, int nblocks, float tol, float limit,
-                                                  float2 *U, float2 *V, int *rank, float *fro, float *err)
+// One CTA per block, thread t owns row t and column t of the block (its own
+// fragment data stays in registers).  The factor columns of the first RS
+// ranks live in shared memory (sU[m][j], sV[m][i]), later ones only in the
+// U and V arrays in global memory, which the low-rank apply reads.  Each
+// rank step has two barriers:
+//   1. every thread stores its residual-row entry (r, t) in sRow and the
+//      block argmax picks the pivot column c; everyone then reads the pivot
+//      value sRow[c];
+//   2. after the residual column c, the argmax over unused rows picks the
+//      next pivot row and the same barrier carries the norms.
+// Factor entries written before a barrier are read by other threads only
+// after it: the pivot row's U entries (step 1 of the next rank) and the
+// pivot column's V entries (the column residual) were all written at
+// earlier ranks.
+template <bool ATT, int RS, int MINB>
+__global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *blocks, const uint8_t *cls,
+                                                     const int *cap, const long long *off, int nblocks, float tol,
+                                                     float limit, float2 *U, float2 *V, int *rank, float *fro,
+                                                     float *err)
 {
-    __shared__ unsigned keyA, keyB;  // argmax keys: pivot column / next row, lowest unused row
-    __shared__ float2 sums[kAcaWarps];
-    __shared__ float2 su[kLrRankLimit], sv[kLrRankLimit + 1];  // sv[kLrRankLimit]: the pivot
+    extern __shared__ float2 aca_smem[];  // sU[RS][kTile], then sV[RS][kTile]
+    float2 *sU = aca_smem, *sV = aca_smem + RS * kTile;
+    __shared__ float2 sRow[kTile];
+    __shared__ __align__(16) unsigned slotA[kAcaWarps], slotB[kAcaWarps], slotZ[kAcaWarps];
+    __shared__ float2 sumB[kAcaWarps];
     const int t = threadIdx.x, b = blockIdx.x;
     if (b >= nblocks) return;  // CTA-uniform
     const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = min(cap[b], kLrRankLimit);
@@ -1588,74 +1561,56 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
     const bool coli = t < ni, rowj = t < nj;
     const float4 pi = coli ? __ldg(PI + t) : z4, qi = coli ? __ldg(NI + t) : z4;
     const float4 pj = rowj ? __ldg(PJ + t) : z4, qj = rowj ? __ldg(NJ + t) : z4;
-    float2 ur[kAcaRegRanks], vr[kAcaRegRanks];
-#pragma unroll
-    for (int m = 0; m < kAcaRegRanks; ++m) ur[m] = vr[m] = z2;
     bool used = !rowj;  // row t taken (or absent)
     int r = 0, k = 0, zero_rows = 0;
     float norm2 = 0.0f;
-    if (t == 0) keyB = 0u;
     while (k < K) {
-        // keyA was last read before the previous iteration's second barrier
-        if (t == 0) keyA = 0u;
-        // ---- publish U[r][m], m < k
-        if (t == r) {
-            ACA_REG_LOOP(k, su[m] = ur[m]);
-            for (int m = kAcaRegRanks; m < k; ++m) su[m] = Ub[m * kTile + r];
-        }
-        __syncthreads();
-        if (t == 0) keyB = 0u;  // last read before the barrier above
+        const int ks = min(k, RS);
         // ---- residual row r, entry (r, t)
         float2 val = z2;
         if (coli) {
             const bool bit = bc == kFlagBits ? ((bw[(long long)(t >> 5) * pitch + r] >> (t & 31)) & 1u) : true;
             val = lr_entry<ATT>(a, bc, bit, pi, qi, __ldg(PJ + r), __ldg(NJ + r));
-            ACA_REG_LOOP(k, val = csub_mul(val, su[m], vr[m]));
-            for (int m = kAcaRegRanks; m < k; ++m) val = csub_mul(val, su[m], Vb[m * kTile + t]);
+            for (int m = 0; m < ks; ++m) val = csub_mul(val, sU[m * kTile + r], sV[m * kTile + t]);
+            for (int m = RS; m < k; ++m) val = csub_mul(val, Ub[m * kTile + r], Vb[m * kTile + t]);
         }
+        sRow[t] = val;
         float best = val.x * val.x + val.y * val.y, d0 = 0.0f, d1 = 0.0f;
         int c = t;
-        cta_reduce<true, false>(best, c, coli, d0, d1, &keyA, sums);
+        cta_reduce<true, false>(best, c, coli, d0, d1, slotA, nullptr);
         if (!(best > 1e-30f)) {
             // the residual row vanished: take the lowest unused row instead
             if (t == r) used = true;
             if (++zero_rows > kAcaMaxZeroRows) break;
             float f = 1.0f;
             int nr = t;
-            cta_reduce<true, false>(f, nr, !used, d0, d1, &keyB, sums);
+            cta_reduce<true, false>(f, nr, !used, d0, d1, slotZ, nullptr);
             if (f < 0.0f) break;
             r = nr;
             continue;
         }
-        // ---- publish V[m][c], m < k, and the pivot
-        if (t == c) {
-            ACA_REG_LOOP(k, sv[m] = vr[m]);
-            for (int m = kAcaRegRanks; m < k; ++m) sv[m] = Vb[m * kTile + c];
-            sv[kLrRankLimit] = val;
-        }
-        __syncthreads();
-        const float2 pv = sv[kLrRankLimit];
+        const float2 pv = sRow[c];
         const float inv = __frcp_rn(pv.x * pv.x + pv.y * pv.y);
         const float2 vv = coli ? make_float2((val.x * pv.x + val.y * pv.y) * inv, (val.y * pv.x - val.x * pv.y) * inv)
                                : z2;
         Vb[k * kTile + t] = vv;
-        ACA_REG_SET(k, vr[m] = vv);
+        if (k < RS) sV[k * kTile + t] = vv;
         // ---- residual column c, entry (t, c)
         float2 uu = z2;
         if (rowj) {
             const bool bit = bc == kFlagBits ? ((bw[(long long)(c >> 5) * pitch + t] >> (c & 31)) & 1u) : true;
             uu = lr_entry<ATT>(a, bc, bit, __ldg(PI + c), __ldg(NI + c), pj, qj);
-            ACA_REG_LOOP(k, uu = csub_mul(uu, ur[m], sv[m]));
-            for (int m = kAcaRegRanks; m < k; ++m) uu = csub_mul(uu, Ub[m * kTile + t], sv[m]);
+            for (int m = 0; m < ks; ++m) uu = csub_mul(uu, sU[m * kTile + t], sV[m * kTile + c]);
+            for (int m = RS; m < k; ++m) uu = csub_mul(uu, Ub[m * kTile + t], Vb[m * kTile + c]);
         }
         Ub[k * kTile + t] = uu;
-        ACA_REG_SET(k, ur[m] = uu);
+        if (k < RS) sU[k * kTile + t] = uu;
         if (t == r) used = true;
         // ---- norms and the next pivot row: the largest residual-column entry among unused rows
         float nu2 = uu.x * uu.x + uu.y * uu.y, nv2 = vv.x * vv.x + vv.y * vv.y;
         float bn = nu2;
         int nr = t;
-        cta_reduce<true, true>(bn, nr, !used, nu2, nv2, &keyB, sums);
+        cta_reduce<true, true>(bn, nr, !used, nu2, nv2, slotB, sumB);
         norm2 += nu2 * nv2;
         ++k;
         if (nu2 * nv2 <= tol * tol * norm2) break;
@@ -1667,8 +1622,9 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
     // against the sampled entries' RMS
     float e2 = 0.0f, x2 = 0.0f;
     const bool converged = k > 0 && k < K;
-    __syncthreads();  // every factor entry written to U and V is visible; the slots are free
+    __syncthreads();  // every factor entry is visible; the sum slots are free
     if (converged) {
+        const int ks = min(k, RS);
 #pragma unroll
         for (int h2 = 0; h2 < 2; ++h2) {
             const int s = t + kTile * h2;  // sample 0..511
@@ -1682,11 +1638,8 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
                 const float2 ex = lr_entry<ATT>(a, bc, bit, h2 == 0 ? __ldg(PI + ii) : pi, h2 == 0 ? __ldg(NI + ii) : qi,
                                                 h2 == 0 ? pj : __ldg(PJ + jj), h2 == 0 ? qj : __ldg(NJ + jj));
                 float2 ap = z2;  // minus the approximation
-                if (h2 == 0)
-                    ACA_REG_LOOP(k, ap = csub_mul(ap, ur[m], Vb[m * kTile + ii]));
-                else
-                    ACA_REG_LOOP(k, ap = csub_mul(ap, Ub[m * kTile + jj], vr[m]));
-                for (int m = kAcaRegRanks; m < k; ++m) ap = csub_mul(ap, Ub[m * kTile + jj], Vb[m * kTile + ii]);
+                for (int m = 0; m < ks; ++m) ap = csub_mul(ap, sU[m * kTile + jj], sV[m * kTile + ii]);
+                for (int m = RS; m < k; ++m) ap = csub_mul(ap, Ub[m * kTile + jj], Vb[m * kTile + ii]);
                 e2 += (ex.x + ap.x) * (ex.x + ap.x) + (ex.y + ap.y) * (ex.y + ap.y);
                 x2 += ex.x * ex.x + ex.y * ex.y;
             }
@@ -1695,7 +1648,7 @@ __global__ void __launch_bounds__(kTile, 2) k_aca(SumArgs a, const int2 *blocks,
     {
         float f = 0.0f;
         int fi = 0;
-        cta_reduce<false, true>(f, fi, false, e2, x2, &keyA, sums);
+        cta_reduce<false, true>(f, fi, false, e2, x2, nullptr, sumB);
     }
     if (t == 0) {
         const float rel = x2 > 0.0f ? sqrtf(e2 / x2) : (e2 > 0.0f ? 1.0f : 0.0f);
@@ -2128,19 +2081,47 @@ void launch_finalize_f2f_sym(const double2 *rowpart, const int *chunk_off, int n
                                                                  cell, Pin, Pout, P, yrow, ycol);
 }
 
+namespace {
+template <bool ATT, int RS, int MINB>
+void launch_aca_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
+                  int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
+                  cudaStream_t s)
+{
+    const size_t smem = (size_t)2 * RS * kTile * sizeof(float2);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_aca<ATT, RS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    k_aca<ATT, RS, MINB><<<(unsigned)nblocks, kTile, smem, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit, U, V,
+                                                                 rank, fro, err);
+}
+
+template <bool ATT>
+void launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap,
+                  const long long *off, int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro,
+                  float limit, float *err, cudaStream_t s)
+{
+    switch (variant) {
+    case 1: launch_aca_t<ATT, 12, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
+    case 2: launch_aca_t<ATT, 16, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
+    default: launch_aca_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
+    }
+}
+}  // namespace
+
+// variant: factor ranks kept in shared memory and CTAs per SM -- 0: 8 ranks,
+// 4 CTAs (the fastest on the 60 kHz trihedral: 5.95 ms against 6.07 and
+// 6.69 ms); 1: 12 ranks, 4 CTAs; 2: 16 ranks, 3 CTAs
 void launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                 int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
-                cudaStream_t s)
+                cudaStream_t s, int variant)
 {
     if (nblocks <= 0) return;
-    const unsigned grid = (unsigned)nblocks;
-    if (a.ka != 0.0f) {
-        k_aca<true><<<grid, kTile, 0, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro,
-                                                     err);
-    } else {
-        k_aca<false><<<grid, kTile, 0, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro,
-                                                      err);
-    }
+    if (a.ka != 0.0f)
+        launch_aca_v<true>(variant, a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s);
+    else
+        launch_aca_v<false>(variant, a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s);
 }
 
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,

@@ -253,6 +253,7 @@ struct Model {
     int opt_cmp_rmax = 32;
     int opt_cmp_select = 0;     // 0 rule (class ALL, eta-separated), 1 every interacting block, 2 the network
     float opt_cmp_rcut = 24.0f; // network: propose blocks whose predicted rank is below this
+    int opt_aca_variant = 0;    // cross-approximation kernel shape (factor ranks in shared memory, CTAs per SM)
     Compression cmp;
     std::vector<HopRecord> log;
     long long launches = 0, h2d_bytes = 0, d2h_bytes = 0;
@@ -737,7 +738,7 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     C.d_fro = ar.take<float>(nmax);
     C.d_err = ar.take<float>(nmax);
     launch_aca(s, C.d_blocks, C.d_cls, C.d_acap, C.d_off, n, g.opt_cmp_tol, C.d_U, C.d_V, C.d_rank, C.d_fro,
-               g.opt_cmp_judge, C.d_err, st);
+               g.opt_cmp_judge, C.d_err, st, g.opt_aca_variant);
     CK(cudaGetLastError());
     CK(cudaEventRecord(g.evb[2], st));
     // ---- accepted blocks: dense flags off, owner lists, statistics
@@ -1425,6 +1426,11 @@ int sonar_set_option(const char *key, double value)
     if (!strcmp(key, "compress_select")) {
         g.opt_cmp_select = std::max(0, std::min(2, (int)value));
         g.cmp.release();
+        return 0;
+    }
+    if (!strcmp(key, "aca_variant")) {
+        if (value < 0 || value > 2) return -1;
+        g.opt_aca_variant = (int)value;
         return 0;
     }
     if (!strcmp(key, "compress_rcut")) { g.opt_cmp_rcut = (float)value; g.cmp.release(); return 0; }

@@ -132,7 +132,7 @@ void launch_finalize_f2f_sym(const double2 *rowpart, const int *chunk_off, int n
 constexpr int kLrRankLimit = 64;
 void launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                 int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
-                cudaStream_t s);
+                cudaStream_t s, int variant = 0);
 // ndev (optional): the block count in device memory; nblocks / nb bound the grid
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
                        const float4 *nm, float inv_lambda, float *X, cudaStream_t s, const int *ndev = nullptr);

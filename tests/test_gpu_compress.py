@@ -71,6 +71,30 @@ def test_compressed_deterministic(api, scenes):
     assert np.array_equal(a, b)
 
 
+def test_cross_approximation_variants_identical(api, scenes):
+    """The kernel shapes of the cross approximation (factor ranks kept in
+    shared memory: 8, 12 or 16; the rest read from the factor arrays) do the
+    same arithmetic in the same order: bit-identical bounces, with every
+    interacting block approximated so that ranks past 16 occur."""
+    sc = _trihedral(scenes, 30e3)
+    api.set_option("compress_select", 1)
+    out = []
+    ranks = []
+    for v in (0, 1, 2):
+        api.set_option("aca_variant", v)
+        _, P, st = _bounces(api, sc, 1)
+        hop = [h for h in st["hops"] if h["hop"] == 2][0]
+        out.append(P)
+        ranks.append(hop["cmp_mean_rank"])
+    api.set_option("aca_variant", 0)
+    api.set_option("compress_select", 0)
+    print("mean ranks per variant", ranks)
+    assert np.array_equal(out[0], out[1])
+    assert np.array_equal(out[0], out[2])
+    with pytest.raises(api.SonarError):
+        api.set_option("aca_variant", 3)
+
+
 @pytest.mark.parametrize("select", [1])
 def test_every_interacting_block_compressed_matches_plain_and_oracle(api, oracle_mod, scenes, select):
     """Blocks of every class (per-pair mask bits, inline gates, all pairs
