@@ -228,18 +228,31 @@ __device__ __forceinline__ void pair_ray(float4 s, float4 ns, float4 t, int ft, 
     e = src_first ? make_float3(t.x, t.y, t.z) : make_float3(s.x, s.y, s.z);
 }
 
-// Occlusion by the block's candidate triangles held in shared memory.
+// Occlusion by the block's candidate triangles held in shared memory.  A
+// triangle whose plane the segment does not cross strictly (the first test
+// of tri_blocks_v, which needs neither the length nor the exclusion radius)
+// is passed over before those are computed; the verdict is tri_blocks_v's.
 __device__ __forceinline__ bool occluded_list(const float4 *sT, int n, float3 o, float3 e)
 {
-    const float vx = __fsub_rn(e.x, o.x), vy = __fsub_rn(e.y, o.y), vz = __fsub_rn(e.z, o.z);
-    const float r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
-    const float tmax = __fsub_rn(r, 1e-3f);
-    const float sc = 1.0f + fmaxf(fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fmaxf(fabsf(o.z), fabsf(e.x))),
-                                  fmaxf(fabsf(e.y), fabsf(e.z)));
-    const float eps = 1e-4f * sc;
+    bool ready = false;
+    float r = 0.0f, tmax = 0.0f, eps = 0.0f;
     const float3 d = make_float3(e.x - o.x, e.y - o.y, e.z - o.z);
-    for (int k = 0; k < n; ++k)
-        if (tri_blocks_v(sT[4 * k], sT[4 * k + 1], sT[4 * k + 2], sT[4 * k + 3], o, e, d, r, tmax, eps)) return true;
+    for (int k = 0; k < n; ++k) {
+        const float4 P = sT[4 * k];
+        const float d0 = fmaf(P.x, o.x, fmaf(P.y, o.y, P.z * o.z)) - P.w;
+        const float d1 = fmaf(P.x, e.x, fmaf(P.y, e.y, P.z * e.z)) - P.w;
+        if (!((d0 > 0.0f && d1 < 0.0f) || (d0 < 0.0f && d1 > 0.0f))) continue;
+        if (!ready) {
+            const float vx = __fsub_rn(e.x, o.x), vy = __fsub_rn(e.y, o.y), vz = __fsub_rn(e.z, o.z);
+            r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
+            tmax = __fsub_rn(r, 1e-3f);
+            const float sc = 1.0f + fmaxf(fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fmaxf(fabsf(o.z), fabsf(e.x))),
+                                          fmaxf(fabsf(e.y), fabsf(e.z)));
+            eps = 1e-4f * sc;
+            ready = true;
+        }
+        if (tri_blocks_v(P, sT[4 * k + 1], sT[4 * k + 2], sT[4 * k + 3], o, e, d, r, tmax, eps)) return true;
+    }
     return false;
 }
 
@@ -275,17 +288,21 @@ __device__ __forceinline__ float plane_dist(const float4 P, float x, float y, fl
 //  (a) all origins and endpoints on one closed side: no strict crossing;
 //  (b) every origin within 1e-4 of the plane: the origin-plane exclusion
 //      (eps = 1e-4 * scale >= 1e-4) removes it from every ray;
-//  (c) origins at distance >= o0 > 0 on one side and endpoints within e1 of
-//      the plane: any crossing lies within rmax*e1/o0 of the endpoint, beyond
+//  (c) every origin that can cross is at distance >= o0 from the plane --
+//      o0 = 1e-4 by the exclusion of (b), or the nearest origin's distance
+//      when all origins lie on one side -- and the endpoints lie within e1
+//      of it: a crossing lies within rmax*e1/o0 of the endpoint, beyond
 //      tmax = r - 1e-3 when o0 * 0.8e-3 > 1.1 * rmax * e1 (the margins cover
-//      the rounding of tmax and of the FP32 comparison in tri_blocks).
+//      the rounding of tmax for rays shorter than 1,000 m and of the FP32
+//      comparison in tri_blocks).  Endpoints on the plane itself (e1 = 0:
+//      rays ending on the triangle's own facet) never cross.
 __device__ __forceinline__ bool may_occlude(float o_lo, float o_hi, float e_lo, float e_hi, float rmax)
 {
     if (fminf(o_lo, e_lo) >= 0.0f || fmaxf(o_hi, e_hi) <= 0.0f) return false;
     if (fmaxf(fabsf(o_lo), fabsf(o_hi)) <= 1e-4f) return false;
-    const bool one_side = o_lo > 0.0f || o_hi < 0.0f;
-    if (one_side) {
-        const float o0 = fminf(fabsf(o_lo), fabsf(o_hi));
+    if (rmax < 1000.0f) {
+        const bool one_side = o_lo > 0.0f || o_hi < 0.0f;
+        const float o0 = fmaxf(one_side ? fminf(fabsf(o_lo), fabsf(o_hi)) : 0.0f, 1e-4f);
         const float e1 = fmaxf(fabsf(e_lo), fabsf(e_hi));
         if (o0 * 0.8e-3f > rmax * e1 * 1.1f + 1e-30f) return false;
     }
