@@ -322,13 +322,20 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
     __shared__ int sFac[4];            // src facet lo/hi, dst facet lo/hi
     __shared__ int sNc, sKeep, sOverflow;
     const int tid = threadIdx.x;
-    const int tile = blockIdx.y;
+    int tile = blockIdx.y, jb = blockIdx.x;
+    if (a.blist) {
+        // the blocks a classification pass left for per-pair bits
+        if ((int)blockIdx.x >= *a.blist_count) return;  // CTA-uniform
+        const int2 e = a.blist[blockIdx.x];
+        tile = e.x;
+        jb = e.y;
+    }
     const int i0 = tile * kTile;
-    const int j = blockIdx.x * kTile + tid;
+    const int j = jb * kTile + tid;
     const bool src_ok = i0 + tid < a.nsrc;
     const bool live = j < a.ndst;
-    const long long fidx = (long long)tile * a.mask.ndstblocks + blockIdx.x;
-    if (HOP == HOP_F2F && a.upper_only && tile > (int)blockIdx.x) {
+    const long long fidx = (long long)tile * a.mask.ndstblocks + jb;
+    if (HOP == HOP_F2F && a.upper_only && tile > jb) {
         // the symmetric bounce sum reads each unordered block once, from its upper side
         if (tid == 0) a.mask.flags[fidx] = kFlagNone;
         return;
@@ -603,21 +610,23 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
     // keep per-pair bits: the inline gates do not see the source facet.
     bool clear = !overflow && nkeep == 0;
     if (HOP == HOP_F2F) clear = clear && (sFac[1] < sFac[2] || sFac[3] < sFac[0]);
-    if (clear && !a.full) {
-        // ALL: every pair passes its cosine gates with margin.  With one source
-        // facet normal n_s and one destination facet normal n_d per block, the
-        // gate values are dot(+-v, n) / |v| with v = p_dst - p_src; their minima
-        // are bounded below by plane-distance ranges over the block divided by
-        // the longest pair distance.  When the bound clears 1e-5 (the per-pair
-        // estimates are within 1e-6 of the exact values, so the exact gates
-        // pass), no pair needs a gate.
+    // ALL GATES: every pair passes its cosine gates with margin.  With one
+    // source facet normal n_s and one destination facet normal n_d per block,
+    // the gate values are dot(+-v, n) / |v| with v = p_dst - p_src; their minima
+    // are bounded below by plane-distance ranges over the block divided by
+    // the longest pair distance.  When the bound clears 1e-5 (the per-pair
+    // estimates are within 1e-6 of the exact values, so the exact gates pass),
+    // no pair needs a gate.  (Uniform facets on both sides of a FACET_SELF
+    // block that is not NONE are two different facets.)  A CLEAR block with
+    // all gates passing is ALL; a block with per-pair bits skips the gates.
+    bool gates_all = false;
+    {
         const bool need_s = HOP != HOP_SRC, need_d = (HOP == HOP_SRC && !a.dst_is_field) || HOP == HOP_F2F;
         const bool uni = (!need_s || sFac[0] == sFac[1]) && (!need_d || sFac[2] == sFac[3]);
-        bool all = false;
         if (uni) {
             const float4 ns = sN[0];
             float4 nd = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (need_d) nd = a.dst_facet_n[a.dst_facet[blockIdx.x * kTile]];
+            if (need_d) nd = a.dst_facet_n[a.dst_facet[jb * kTile]];
             // ranges of p.n_s and p.n_d over sources and destinations
             float s_s = -3.0e38f, s_d = 3.0e38f, d_s = 3.0e38f, d_d = -3.0e38f;
             if (src_ok) {
@@ -634,7 +643,8 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
                 d_s = fminf(d_s, __shfl_xor_sync(0xffffffffu, d_s, off));
                 d_d = fmaxf(d_d, __shfl_xor_sync(0xffffffffu, d_d, off));
             }
-            if (tid < kMaxCand && tid < 4) sRed[0][tid] = (tid == 0 || tid == 3) ? f2o(-3.0e38f) : f2o(3.0e38f);
+            __syncthreads();  // every thread has read the candidate ranges in sRed
+            if (tid < 4) sRed[0][tid] = (tid == 0 || tid == 3) ? f2o(-3.0e38f) : f2o(3.0e38f);
             __syncthreads();
             if ((tid & 31) == 0) {
                 atomicMax(&sRed[0][0], f2o(s_s));
@@ -653,13 +663,35 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
             // source-side gate: dot(v, n_s) >= d_s - s_s ; destination side: -dot(v, n_d) >= s_d - d_d
             const bool ok_s = !need_s || (o2f(sRed[0][2]) - o2f(sRed[0][0]) > thr);
             const bool ok_d = !need_d || (o2f(sRed[0][1]) - o2f(sRed[0][3]) > thr);
-            all = ok_s && ok_d;
+            gates_all = ok_s && ok_d;
         }
-        if (tid == 0) a.mask.flags[fidx] = all ? kFlagAll : kFlagClear;
+    }
+    if (clear && !a.full) {
+        if (tid == 0) a.mask.flags[fidx] = gates_all ? kFlagAll : kFlagClear;
         return;
     }
 
-    // ---- pairs (every lane runs the loop: the gates vote across the warp)
+    // ---- pairs (every lane runs the loop: the gates vote across the warp).
+    // With a candidate list, a pair is tested only when some candidate's
+    // plane separates its two points strictly (the first test of
+    // tri_blocks_v, on the same plane distances): bit c of the signs of each
+    // source (shared memory) and of the thread's destination.
+    __shared__ uint2 sSg[kTile];
+    const bool signs = !clear && !overflow && nkeep > 0;
+    unsigned tpos = 0u, tneg = 0u;
+    if (signs) {
+        unsigned spos = 0u, sneg = 0u;
+        for (int c = 0; c < nkeep; ++c) {
+            const float4 Pl = sTri[4 * c];
+            const float ds = plane_dist(Pl, p.x, p.y, p.z), dd = plane_dist(Pl, t.x, t.y, t.z);
+            spos |= (ds > 0.0f ? 1u : 0u) << c;
+            sneg |= (ds < 0.0f ? 1u : 0u) << c;
+            tpos |= (dd > 0.0f ? 1u : 0u) << c;
+            tneg |= (dd < 0.0f ? 1u : 0u) << c;
+        }
+        sSg[tid] = make_uint2(spos, sneg);
+    }
+    __syncthreads();
     const int ntile = min(kTile, a.nsrc - i0);
     const int nw = (ntile + 31) >> 5;
     uint32_t any = 0;
@@ -670,15 +702,23 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
         for (int b = 0; b < 32; ++b) {
             const int q = w * 32 + b;
             const bool act = live && b < bmax;
-            const float4 sq = sP[q], nq = sN[q];
-            bool pass = pair_gates_vote<HOP>(a, sq, nq, t, nt, ft, act) && act;
+            bool pass = act;
+            if (!gates_all) pass = pair_gates_vote<HOP>(a, sP[q], sN[q], t, nt, ft, act) && act;
             if (!clear && pass) {
-                float3 o, e;
-                pair_ray<HOP>(sq, nq, t, ft, o, e);
-                if (overflow)
-                    pass = !occluded_full(a.bvh, o, e);
-                else if (nkeep > 0)
-                    pass = !occluded_list(sTri, nkeep, o, e);
+                bool test = true;
+                if (signs) {
+                    const uint2 sg = sSg[q];
+                    test = ((sg.x & tneg) | (sg.y & tpos)) != 0u;
+                }
+                if (test) {
+                    const float4 sq = sP[q], nq = sN[q];
+                    float3 o, e;
+                    pair_ray<HOP>(sq, nq, t, ft, o, e);
+                    if (overflow)
+                        pass = !occluded_full(a.bvh, o, e);
+                    else if (nkeep > 0)
+                        pass = !occluded_list(sTri, nkeep, o, e);
+                }
             }
             word |= pass ? (1u << b) : 0u;
         }
@@ -687,6 +727,205 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
     }
     const int blk = __syncthreads_or(any != 0u);
     if (tid == 0) a.mask.flags[fidx] = clear ? kFlagClear : (blk ? kFlagBits : kFlagNone);
+}
+
+// ---------------------------------------------------------------- bounce-mask classification
+// The block decisions of k_mask<HOP_F2F> (same facet, occluder culling, the
+// ALL test of the cosine gates) taken by one warp per block from the same
+// values -- min / max reductions of the same per-point expressions, which
+// do not depend on the order of reduction -- so every verdict equals
+// k_mask's.  NONE, CLEAR and ALL blocks get their flag here (the flags start
+// at NONE); blocks that need per-pair bits are appended to a list that
+// k_mask then runs on (it repeats the culling to build its triangle list and
+// writes the flag).  The order of the list does not matter: each block's
+// bits and flag depend only on the block.
+constexpr int kClsWarps = 8;
+
+struct WarpRange {
+    float lo, hi;
+};
+
+__device__ __forceinline__ float warp_min(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__global__ void __launch_bounds__(32 * kClsWarps) k_mask_classify_f2f(MaskArgs a, int2 *blist, int *count)
+{
+    __shared__ int sCand[kClsWarps][kMaxCand];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int I = blockIdx.y;
+    const int J = (a.upper_only ? I : 0) + (int)blockIdx.x * kClsWarps + warp;
+    const int nt = a.mask.ntiles, nb = a.mask.ndstblocks;
+    if (J >= nb || I >= nt) return;  // warp-uniform; no block-wide barrier below
+    const int i0 = I * kTile, j0 = J * kTile;
+    const int ni = min(kTile, a.nsrc - i0), nj = min(kTile, a.ndst - j0);
+    // this lane's points: q = lane + 32 m, m < 8, of both tiles
+    float4 P[8], T[8];
+    int fs_lo = 2147483647, fs_hi = -2147483647, fd_lo = 2147483647, fd_hi = -2147483647;
+    float slo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, shi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+    float dlo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, dhi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int q = lane + 32 * m;
+        P[m] = q < ni ? __ldg(a.src_pos + i0 + q) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        T[m] = q < nj ? __ldg(a.dst_pos + j0 + q) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (q < ni) {
+            const int f = __ldg(a.src_facet + i0 + q);
+            fs_lo = min(fs_lo, f);
+            fs_hi = max(fs_hi, f);
+            slo[0] = fminf(slo[0], P[m].x); shi[0] = fmaxf(shi[0], P[m].x);
+            slo[1] = fminf(slo[1], P[m].y); shi[1] = fmaxf(shi[1], P[m].y);
+            slo[2] = fminf(slo[2], P[m].z); shi[2] = fmaxf(shi[2], P[m].z);
+        }
+        if (q < nj) {
+            const int f = __ldg(a.dst_facet + j0 + q);
+            fd_lo = min(fd_lo, f);
+            fd_hi = max(fd_hi, f);
+            dlo[0] = fminf(dlo[0], T[m].x); dhi[0] = fmaxf(dhi[0], T[m].x);
+            dlo[1] = fminf(dlo[1], T[m].y); dhi[1] = fmaxf(dhi[1], T[m].y);
+            dlo[2] = fminf(dlo[2], T[m].z); dhi[2] = fmaxf(dhi[2], T[m].z);
+        }
+    }
+    fs_lo = __reduce_min_sync(0xffffffffu, fs_lo);
+    fs_hi = __reduce_max_sync(0xffffffffu, fs_hi);
+    fd_lo = __reduce_min_sync(0xffffffffu, fd_lo);
+    fd_hi = __reduce_max_sync(0xffffffffu, fd_hi);
+    // blocks whose fragments all share one facet interact nowhere (flag stays NONE)
+    if (fs_lo == fs_hi && fd_lo == fd_hi && fs_lo == fd_lo) return;
+    float lo[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        slo[k] = warp_min(slo[k]);
+        shi[k] = warp_max(shi[k]);
+        dlo[k] = warp_min(dlo[k]);
+        dhi[k] = warp_max(dhi[k]);
+        lo[k] = fminf(slo[k], dlo[k]);
+        hi[k] = fmaxf(shi[k], dhi[k]);
+    }
+    const long long fidx = (long long)I * nb + J;
+    bool bits = false;
+    if (a.bvh.ntri > 0) {
+        // candidates: every triangle in small scenes, else the BVH leaves
+        // whose boxes overlap the union box (the walk of k_mask, by lane 0)
+        int nc = 0;
+        bool over = false;
+        if (a.bvh.ntri <= kMaxCand) {
+            nc = a.bvh.ntri;
+        } else if (lane == 0) {
+            int stack[kStack];
+            int sp = 0, node = 0;
+            for (int guard = 0; guard < a.bvh.nnodes && !over; ++guard) {
+                const float4 na = __ldg(a.bvh.nodes + 2 * node), nb4 = __ldg(a.bvh.nodes + 2 * node + 1);
+                bool descend = false;
+                if (na.x <= hi[0] && nb4.x >= lo[0] && na.y <= hi[1] && nb4.y >= lo[1] && na.z <= hi[2] &&
+                    nb4.z >= lo[2]) {
+                    const int left = __float_as_int(na.w), right = __float_as_int(nb4.w);
+                    if (left < 0) {
+                        for (int q = -left - 1; q < -left - 1 + right; ++q) {
+                            if (nc >= kMaxCand) {
+                                over = true;
+                                break;
+                            }
+                            sCand[warp][nc++] = q;
+                        }
+                    } else {
+                        if (sp < kStack) stack[sp++] = right;
+                        node = left;
+                        descend = true;
+                    }
+                }
+                if (!descend) {
+                    if (sp == 0) break;
+                    node = stack[--sp];
+                }
+            }
+        }
+        __syncwarp();
+        nc = __shfl_sync(0xffffffffu, nc, 0);
+        over = __shfl_sync(0xffffffffu, (int)over, 0) != 0;
+        if (over) {
+            bits = true;
+        } else {
+            const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+            const float rmax = sqrtf(dx * dx + dy * dy + dz * dz) * 1.0001f;
+            const bool src_origin = fs_lo < fd_hi, dst_origin = fd_lo < fs_hi;
+            for (int c = 0; c < nc && !bits; ++c) {
+                const int tri = a.bvh.ntri <= kMaxCand ? c : sCand[warp][c];
+                const float4 Pl = __ldg(a.bvh.tris + 4 * tri);
+                float sl = 3.0e38f, sh = -3.0e38f, dl = 3.0e38f, dh = -3.0e38f;
+#pragma unroll
+                for (int m = 0; m < 8; ++m) {
+                    const int q = lane + 32 * m;
+                    if (q < ni) {
+                        const float v = plane_dist(Pl, P[m].x, P[m].y, P[m].z);
+                        sl = fminf(sl, v);
+                        sh = fmaxf(sh, v);
+                    }
+                    if (q < nj) {
+                        const float v = plane_dist(Pl, T[m].x, T[m].y, T[m].z);
+                        dl = fminf(dl, v);
+                        dh = fmaxf(dh, v);
+                    }
+                }
+                sl = warp_min(sl);
+                sh = warp_max(sh);
+                dl = warp_min(dl);
+                dh = warp_max(dh);
+                bool mo = false;
+                if (src_origin) mo = mo || may_occlude(sl, sh, dl, dh, rmax);
+                if (dst_origin) mo = mo || may_occlude(dl, dh, sl, sh, rmax);
+                bits = mo;
+            }
+        }
+    }
+    // overlapping facet ranges keep per-pair bits (the inline gates do not see the source facet)
+    if (!(fs_hi < fd_lo || fd_hi < fs_lo)) bits = true;
+    if (bits) {
+        if (lane == 0) {
+            const int slot = atomicAdd(count, 1);
+            blist[slot] = make_int2(I, J);
+        }
+        return;
+    }
+    // ALL: both cosine gates of every pair pass with margin (the test of k_mask)
+    bool all = false;
+    if (fs_lo == fs_hi && fd_lo == fd_hi) {
+        const float4 ns = __ldg(a.src_facet_n + fs_lo), nd = __ldg(a.dst_facet_n + fd_lo);
+        float s_s = -3.0e38f, s_d = 3.0e38f, d_s = 3.0e38f, d_d = -3.0e38f;
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const int q = lane + 32 * m;
+            if (q < ni) {
+                s_s = fmaxf(s_s, fmaf(P[m].x, ns.x, fmaf(P[m].y, ns.y, P[m].z * ns.z)));
+                s_d = fminf(s_d, fmaf(P[m].x, nd.x, fmaf(P[m].y, nd.y, P[m].z * nd.z)));
+            }
+            if (q < nj) {
+                d_s = fminf(d_s, fmaf(T[m].x, ns.x, fmaf(T[m].y, ns.y, T[m].z * ns.z)));
+                d_d = fmaxf(d_d, fmaf(T[m].x, nd.x, fmaf(T[m].y, nd.y, T[m].z * nd.z)));
+            }
+        }
+        s_s = warp_max(s_s);
+        s_d = warp_min(s_d);
+        d_s = warp_min(d_s);
+        d_d = warp_max(d_d);
+        const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        const float rmax = sqrtf(dx * dx + dy * dy + dz * dz) * 1.0001f;
+        float S = 1.0f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) S = fmaxf(S, fmaxf(1.0f + fabsf(lo[k]), 1.0f + fabsf(hi[k])));
+        const float thr = rmax * 1e-5f + S * 1e-6f;
+        all = (d_s - s_s > thr) && (s_d - d_d > thr);
+    }
+    if (lane == 0) a.mask.flags[fidx] = all ? kFlagAll : kFlagClear;
 }
 
 // ---------------------------------------------------------------- batch visibility
@@ -2018,6 +2257,26 @@ double measure_peak(int which)
     cudaEventDestroy(e1);
     cudaStreamDestroy(st);
     return ok ? best : -1.0;
+}
+
+int launch_mask_classified(const MaskArgs &a0, int2 *blist, int *count_dev, int *count_host, cudaStream_t s)
+{
+    if (a0.nsrc <= 0 || a0.ndst <= 0) return 0;
+    const size_t nflags = (size_t)a0.mask.ntiles * a0.mask.ndstblocks;
+    cudaMemsetAsync(a0.mask.flags, kFlagNone, nflags, s);
+    cudaMemsetAsync(count_dev, 0, sizeof(int), s);
+    dim3 grid((a0.mask.ndstblocks + kClsWarps - 1) / kClsWarps, a0.mask.ntiles);
+    k_mask_classify_f2f<<<grid, 32 * kClsWarps, 0, s>>>(a0, blist, count_dev);
+    cudaMemcpyAsync(count_host, count_dev, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    const int n = *count_host;
+    if (n > 0) {
+        MaskArgs a = a0;
+        a.blist = blist;
+        a.blist_count = count_dev;
+        k_mask<HOP_F2F><<<(unsigned)n, kTile, 0, s>>>(a);
+    }
+    return n > 0 ? 2 : 1;
 }
 
 void launch_mask(const MaskArgs &a, cudaStream_t s)

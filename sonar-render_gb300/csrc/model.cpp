@@ -109,8 +109,17 @@ struct MaskEntry {
     long long classes[4] = {0, 0, 0, 0};  // blocks per flag: none, bits, clear, all
     int nsrc, ndst;
     MaskView view{};
+    int2 *blist = nullptr;  // bounce masks: blocks the classification pass leaves for per-pair bits
+    int *bcount = nullptr;
     float mask_ms = 0.0f;
     bool stale = false;  // rebuild into the same buffers before the next use
+    void free_device()
+    {
+        dfree(view.bits);
+        dfree(view.flags);
+        dfree(blist);
+        dfree(bcount);
+    }
 };
 
 // Low-rank compression of the FACET_SELF blocks of one object (built with its
@@ -254,6 +263,7 @@ struct Model {
     int opt_cmp_select = 0;     // 0 rule (class ALL, eta-separated), 1 every interacting block, 2 the network
     float opt_cmp_rcut = 24.0f; // network: propose blocks whose predicted rank is below this
     int opt_aca_variant = 0;    // cross-approximation kernel shape (factor ranks in shared memory, CTAs per SM)
+    int opt_mask_classify = 1;  // bounce masks: warp-per-block classification, pair kernel on the listed blocks
     Compression cmp;
     std::vector<HopRecord> log;
     long long launches = 0, h2d_bytes = 0, d2h_bytes = 0;
@@ -264,10 +274,7 @@ struct Model {
             for (auto &o : obj[t]) o->free_device();
         dfree(d_src_pos); dfree(d_fp_pos); dfree(d_src_P); dfree(d_fp_P); dfree(d_fp_order);
         dfree(d_nodes); dfree(d_tris);
-        for (auto &m : masks) {
-            dfree(m.view.bits);
-            dfree(m.view.flags);
-        }
+        for (auto &m : masks) m.free_device();
         masks.clear();
         cmp.free_all();
         dfree(d_packA); dfree(d_packB); dfree(d_partial); dfree(d_limit); dfree(d_colpart);
@@ -550,9 +557,18 @@ MaskEntry build_mask(int hop, int a, int b, int full, const MaskEntry *reuse = n
     if (reuse) {
         v.bits = reuse->view.bits;
         v.flags = reuse->view.flags;
+        e.blist = reuse->blist;
+        e.bcount = reuse->bcount;
     } else {
         v.bits = dalloc<uint32_t>(words);
         v.flags = dalloc<uint8_t>(nflags);
+    }
+    // bounce masks: one warp per block classifies, only the blocks that need
+    // per-pair bits run the pair kernel
+    const bool classify = hop == HOP_F2F && !full && g.opt_mask_classify;
+    if (classify && !e.blist) {
+        e.blist = dalloc<int2>(std::max<size_t>(nflags, 1));
+        e.bcount = dalloc<int>(1);
     }
     // every block writes its flag, and the sums read bits only of blocks that
     // stored them; the full export also reads blocks that store none
@@ -561,9 +577,14 @@ MaskEntry build_mask(int hop, int a, int b, int full, const MaskEntry *reuse = n
     hs.m.full = full;
     hs.m.upper_only = (hop == HOP_F2F && !full && g.opt_f2f_sym) ? 1 : 0;
     CK(cudaEventRecord(g.ev0, g.stream));
-    launch_mask(hs.m, g.stream);
+    if (classify) {
+        int nbits = 0;
+        g.launches += launch_mask_classified(hs.m, e.blist, e.bcount, &nbits, g.stream);
+    } else {
+        launch_mask(hs.m, g.stream);
+        g.launches += (hs.nsrc > 0 && hs.ndst > 0) ? 1 : 0;
+    }
     CK(cudaGetLastError());
-    g.launches += (hs.nsrc > 0 && hs.ndst > 0) ? 1 : 0;
     CK(cudaEventRecord(g.ev1, g.stream));
     CK(cudaEventSynchronize(g.ev1));
     CK(cudaEventElapsedTime(&e.mask_ms, g.ev0, g.ev1));
@@ -1428,6 +1449,11 @@ int sonar_set_option(const char *key, double value)
         g.cmp.release();
         return 0;
     }
+    if (!strcmp(key, "mask_classify")) {
+        g.opt_mask_classify = value != 0.0 ? 1 : 0;
+        for (auto &m : g.masks) m.stale = true;
+        return 0;
+    }
     if (!strcmp(key, "aca_variant")) {
         if (value < 0 || value > 2) return -1;
         g.opt_aca_variant = (int)value;
@@ -1466,7 +1492,7 @@ int sonar_set_option(const char *key, double value)
         return 0;
     }
     if (!strcmp(key, "free_masks")) {
-        for (auto &m : g.masks) { dfree(m.view.bits); dfree(m.view.flags); }
+        for (auto &m : g.masks) m.free_device();
         g.masks.clear();
         return 0;
     }
@@ -1496,8 +1522,7 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
         if (e == cudaSuccess) e = cudaMemcpyAsync(tmp.data(), d, (size_t)nbytes, cudaMemcpyDeviceToHost, g.stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
         if (d) cudaFree(d);
-        dfree(M.view.bits);
-        dfree(M.view.flags);
+        M.free_device();
         if (e != cudaSuccess) fail(-10, "mask export failed: %s", cudaGetErrorString(e));
         // active fragments are stored in patch order; report them in cell order
         auto canon = [](const Object &o) {

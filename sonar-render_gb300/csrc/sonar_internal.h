@@ -70,6 +70,8 @@ struct MaskArgs {
     int upper_only;                 // FACET_SELF: only blocks with source tile <= destination block
     BvhView bvh;
     MaskView mask;
+    const int2 *blist = nullptr;    // optional: (source tile, destination block) of the blocks to build
+    const int *blist_count = nullptr;
 };
 
 struct SumArgs {
@@ -94,6 +96,11 @@ struct SumArgs {
 
 // kernels.cu
 void launch_mask(const MaskArgs &a, cudaStream_t s);
+// Bounce masks (HOP_F2F, no full export): classification pass, then the pair
+// kernel on the blocks it lists (blist: one entry per block at most; the
+// stream is synchronised once to read their count into *count_host).
+// Returns the number of kernels launched.
+int launch_mask_classified(const MaskArgs &a, int2 *blist, int *count_dev, int *count_host, cudaStream_t s);
 void launch_sum(const SumArgs &a, cudaStream_t s);
 void launch_pack_points(const float4 *pts, const double2 *P, int n, float4 *A, float4 *B, cudaStream_t s);
 void launch_pack_frags(const float4 *act_pos, const int *act_facet, const int *act_cell, const float4 *facet_n,

@@ -243,3 +243,40 @@ def test_symmetric_bounce_sum_matches_ordered(api, scenes):
     err = rel_l2(P1, P0)
     print("symmetric vs ordered bounce sums: rel L2 %.3e" % err)
     assert err < 1e-6
+
+
+@pytest.mark.parametrize("extra", ["none", "box", "sphere"])
+def test_bounce_mask_classification_pass_identical(api, scenes, extra):
+    """The bounce mask built by the warp-per-block classification pass (pair
+    kernel on the listed blocks only) and by the pair kernel over every block
+    give the same block classes and bit-identical bounces: the trihedral
+    alone (3 triangles), with a box in the corner (15 triangles, occluded
+    pairs) and with an icosphere in the corner (83 triangles: occluder
+    candidates from the BVH walk)."""
+    tri = scenes.trihedral(1.0)
+    if extra == "box":
+        tri = np.concatenate([tri, scenes.box(0.2, 0.15, 0.25, center=(0.35, 0.3, 0.2))])
+    elif extra == "sphere":
+        tri = np.concatenate([tri, scenes.icosphere(1, 0.18, center=(0.35, 0.35, 0.3))])
+    f = 15e3
+    sc = dict(cp=1480.0, f=f, att=0.0, bounces=2, field_objects=False,
+              sources=np.array([[6.0, 5.0, 4.0]], np.float32),
+              field_points=scenes.hemisphere(3, 3, 2.0), targets=[(tri, scenes.delta_for(f))], fields=[])
+    out, classes = {}, {}
+    for mode in (1, 0):
+        api.set_option("mask_classify", mode)
+        api.set_option("class_stats", 1)
+        out[mode] = run_gpu(api, sc)
+        classes[mode] = [c for c in api.stats()["mask_classes"] if c["hop"] == 2]
+        api.set_option("class_stats", 0)
+    api.set_option("mask_classify", 1)
+    api.TearDownCuda()
+    print(extra, "bounce mask classes", classes[1])
+    assert classes[1] == classes[0]
+    c = classes[1][0]
+    # the bare corner has blocks proved free of occluders; an object in the
+    # corner may occlude almost every block's rays
+    assert (c["clear"] + c["all"] > 0) if extra == "none" else (c["bits"] > 0)
+    for k in out[1]:
+        assert np.array_equal(out[1][k], out[0][k]), k
+    assert np.abs(out[1]["P_target0"]).max() > 0
