@@ -620,6 +620,13 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
     // block that is not NONE are two different facets.)  A CLEAR block with
     // all gates passing is ALL; a block with per-pair bits skips the gates.
     bool gates_all = false;
+    // FACET_SELF blocks with one facet on each side: the per-point
+    // projections on both normals decide most pairs' gates without the
+    // pair's own vector (see the pair loop)
+    bool proj = false;
+    float t_s = 0.0f, t_d = 0.0f, proj_hi = 0.0f, proj_lo = 0.0f;
+    __shared__ float2 sProj[kTile];
+    __shared__ float4 sWP[kWordsPerTile];  // per word: min, max of p.n_s; min, max of p.n_d
     {
         const bool need_s = HOP != HOP_SRC, need_d = (HOP == HOP_SRC && !a.dst_is_field) || HOP == HOP_F2F;
         const bool uni = (!need_s || sFac[0] == sFac[1]) && (!need_d || sFac[2] == sFac[3]);
@@ -637,12 +644,27 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
                 d_s = fmaf(t.x, ns.x, fmaf(t.y, ns.y, t.z * ns.z));
                 d_d = fmaf(t.x, nd.x, fmaf(t.y, nd.y, t.z * nd.z));
             }
+            float ps_min = 3.0e38f, pd_max = -3.0e38f;
+            if (HOP == HOP_F2F && a.gate_proj) {
+                proj = true;
+                sProj[tid] = make_float2(s_s, s_d);
+                t_s = d_s;
+                t_d = d_d;
+                if (src_ok) {
+                    ps_min = s_s;
+                    pd_max = s_d;
+                }
+            }
             for (int off = 16; off > 0; off >>= 1) {
                 s_s = fmaxf(s_s, __shfl_xor_sync(0xffffffffu, s_s, off));
                 s_d = fminf(s_d, __shfl_xor_sync(0xffffffffu, s_d, off));
                 d_s = fminf(d_s, __shfl_xor_sync(0xffffffffu, d_s, off));
                 d_d = fmaxf(d_d, __shfl_xor_sync(0xffffffffu, d_d, off));
+                ps_min = fminf(ps_min, __shfl_xor_sync(0xffffffffu, ps_min, off));
+                pd_max = fmaxf(pd_max, __shfl_xor_sync(0xffffffffu, pd_max, off));
             }
+            // warp w holds the sources of mask word w: their projection ranges
+            if (proj && (tid & 31) == 0) sWP[tid >> 5] = make_float4(ps_min, s_s, s_d, pd_max);
             __syncthreads();  // every thread has read the candidate ranges in sRed
             if (tid < 4) sRed[0][tid] = (tid == 0 || tid == 3) ? f2o(-3.0e38f) : f2o(3.0e38f);
             __syncthreads();
@@ -664,6 +686,21 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
             const bool ok_s = !need_s || (o2f(sRed[0][2]) - o2f(sRed[0][0]) > thr);
             const bool ok_d = !need_d || (o2f(sRed[0][1]) - o2f(sRed[0][3]) > thr);
             gates_all = ok_s && ok_d;
+            if (proj) {
+                // D = dot(v, n) of a pair (v = p_dst - p_src rounded to FP32)
+                // differs from the difference of the two points' projections
+                // by at most 1e-6 (rmax + sum_k max |coordinate_k|) (rounding
+                // of v, of the projections and of their difference); with
+                // |v| <= rmax, D above proj_hi means a gate value above
+                // 3e-6 (cos_gate's estimate above 2e-6: pass) and D below
+                // proj_lo one below -2e-6 (estimate negative: fail)
+                float Ssum = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) Ssum += fmaxf(fabsf(o2f(sBox[k])), fabsf(o2f(sBox[3 + k])));
+                const float E = 1e-6f * (rmax + Ssum);
+                proj_hi = E + 3e-6f * rmax;
+                proj_lo = -(E + 2e-6f * rmax);
+            }
         }
     }
     if (clear && !a.full) {
@@ -671,57 +708,144 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
         return;
     }
 
-    // ---- pairs (every lane runs the loop: the gates vote across the warp).
-    // With a candidate list, a pair is tested only when some candidate's
-    // plane separates its two points strictly (the first test of
-    // tri_blocks_v, on the same plane distances): bit c of the signs of each
-    // source (shared memory) and of the thread's destination.
-    __shared__ uint2 sSg[kTile];
+    // ---- pairs, one 32-source word at a time per destination thread.
+    // Gates: with the projections, a word whose extreme sources pass (or
+    // fail) with certainty decides all its pairs at once -- the difference
+    // of projections is monotone in the source's projection, so the
+    // per-pair differences lie between the extremes' -- otherwise the pairs
+    // of the word are decided one by one (projections where certain, the
+    // exact gates under a warp vote where not).
+    // Occlusion, with a candidate list: a pair needs the test only when some
+    // candidate's plane separates its two points strictly (the first test of
+    // tri_blocks_v, on the same plane distances); the sources on each side of
+    // each plane are bit masks per word, so the pairs to test are found for
+    // 32 sources at once.  They are queued with their bit set, and tested
+    // by all threads together after the word, clearing the bits of the
+    // occluded pairs: the few segments that cross a plane do not hold whole
+    // warps.  Without a list (too many candidates) the test runs in place.
+    constexpr int kQCap = kTile * 32;  // one word's pairs
+    __shared__ uint32_t sPos[kMaxCand][kWordsPerTile], sNeg[kMaxCand][kWordsPerTile];
+    __shared__ unsigned short sQ[kQCap];
+    __shared__ uint32_t sW[kWordsPerTile][kTile];
+    __shared__ float4 sTd[kTile];
+    __shared__ int sQn[2];
+    const int lane = tid & 31;
     const bool signs = !clear && !overflow && nkeep > 0;
     unsigned tpos = 0u, tneg = 0u;
     if (signs) {
-        unsigned spos = 0u, sneg = 0u;
         for (int c = 0; c < nkeep; ++c) {
             const float4 Pl = sTri[4 * c];
             const float ds = plane_dist(Pl, p.x, p.y, p.z), dd = plane_dist(Pl, t.x, t.y, t.z);
-            spos |= (ds > 0.0f ? 1u : 0u) << c;
-            sneg |= (ds < 0.0f ? 1u : 0u) << c;
+            const unsigned bp = __ballot_sync(0xffffffffu, src_ok && ds > 0.0f);
+            const unsigned bn = __ballot_sync(0xffffffffu, src_ok && ds < 0.0f);
+            if (lane == 0) {
+                sPos[c][tid >> 5] = bp;
+                sNeg[c][tid >> 5] = bn;
+            }
             tpos |= (dd > 0.0f ? 1u : 0u) << c;
             tneg |= (dd < 0.0f ? 1u : 0u) << c;
         }
-        sSg[tid] = make_uint2(spos, sneg);
+        sTd[tid] = make_float4(t.x, t.y, t.z, __int_as_float(ft));
+        if (tid < 2) sQn[tid] = 0;
     }
     __syncthreads();
     const int ntile = min(kTile, a.nsrc - i0);
     const int nw = (ntile + 31) >> 5;
-    uint32_t any = 0;
     for (int w = 0; w < nw; ++w) {
-        uint32_t word = 0;
         const int bmax = min(32, ntile - w * 32);
+        const uint32_t valid = live ? (bmax == 32 ? 0xffffffffu : ((1u << bmax) - 1u)) : 0u;
+        uint32_t word = valid;
+        bool mixed = !gates_all && live;
+        if (mixed && proj) {
+            const float4 wp = sWP[w];
+            const bool all_ok = (t_s - wp.y > proj_hi) && (wp.z - t_d > proj_hi);
+            const bool all_fail = (t_s - wp.x < proj_lo) || (wp.w - t_d < proj_lo);
+            if (all_ok || all_fail) {
+                mixed = false;
+                word = all_ok ? valid : 0u;
+            }
+        }
+        if (__any_sync(0xffffffffu, mixed)) {
+            uint32_t pw = 0;
 #pragma unroll 4
-        for (int b = 0; b < 32; ++b) {
-            const int q = w * 32 + b;
-            const bool act = live && b < bmax;
-            bool pass = act;
-            if (!gates_all) pass = pair_gates_vote<HOP>(a, sP[q], sN[q], t, nt, ft, act) && act;
-            if (!clear && pass) {
-                bool test = true;
-                if (signs) {
-                    const uint2 sg = sSg[q];
-                    test = ((sg.x & tneg) | (sg.y & tpos)) != 0u;
+            for (int b = 0; b < 32; ++b) {
+                const int q = w * 32 + b;
+                const bool act = mixed && b < bmax;
+                bool pass = act, unsure = act;
+                if (proj) {
+                    // gate 1: cos(v, n_s) from D1 = (t - p).n_s; gate 2:
+                    // cos(-v, n_d) from D2 = (p - t).n_d
+                    const float2 pq = sProj[q];
+                    const float D1 = t_s - pq.x, D2 = pq.y - t_d;
+                    const bool fail = D1 < proj_lo || D2 < proj_lo;
+                    const bool ok = D1 > proj_hi && D2 > proj_hi;
+                    pass = act && ok;
+                    unsure = act && !fail && !ok;
                 }
-                if (test) {
-                    const float4 sq = sP[q], nq = sN[q];
+                if (__any_sync(0xffffffffu, unsure)) {
+                    const bool g = pair_gates_vote<HOP>(a, sP[q], sN[q], t, nt, ft, unsure);
+                    if (unsure) pass = g;
+                }
+                pw |= pass ? (1u << b) : 0u;
+            }
+            if (mixed) word = pw;
+        }
+        if (!clear && (overflow || nkeep > 0)) {
+            if (signs) {
+                uint32_t cross = 0u;
+                for (int c = 0; c < nkeep; ++c) {
+                    if ((tneg >> c) & 1u) cross |= sPos[c][w];
+                    if ((tpos >> c) & 1u) cross |= sNeg[c][w];
+                }
+                uint32_t tq = word & cross;
+                // warp-aggregated slots for this lane's pairs to test
+                const int cnt = __popc(tq);
+                int incl = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                int base = 0;
+                if (lane == 31 && incl > 0) base = atomicAdd(&sQn[w & 1], incl);
+                base = __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
+                while (tq) {
+                    const int b = __ffs(tq) - 1;
+                    tq &= tq - 1u;
+                    sQ[base++] = (unsigned short)(((w * 32 + b) << 8) | tid);
+                }
+            } else {
+                uint32_t tq = word;
+                while (tq) {
+                    const int b = __ffs(tq) - 1;
+                    tq &= tq - 1u;
+                    const int q = w * 32 + b;
                     float3 o, e;
-                    pair_ray<HOP>(sq, nq, t, ft, o, e);
-                    if (overflow)
-                        pass = !occluded_full(a.bvh, o, e);
-                    else if (nkeep > 0)
-                        pass = !occluded_list(sTri, nkeep, o, e);
+                    pair_ray<HOP>(sP[q], sN[q], t, ft, o, e);
+                    if (occluded_full(a.bvh, o, e)) word &= ~(1u << b);
                 }
             }
-            word |= pass ? (1u << b) : 0u;
         }
+        sW[w][tid] = word;
+        if (signs) {
+            if (tid == 0) sQn[(w + 1) & 1] = 0;  // last read before the previous word's second barrier
+            __syncthreads();
+            const int nq = sQn[w & 1];
+            for (int e = tid; e < nq; e += kTile) {
+                const unsigned code = sQ[e];
+                const int q = (int)(code >> 8), jl = (int)(code & 255u);
+                const float4 td = sTd[jl];
+                float3 o, en;
+                pair_ray<HOP>(sP[q], sN[q], td, __float_as_int(td.w), o, en);
+                if (occluded_list(sTri, nkeep, o, en)) atomicAnd(&sW[w][jl], ~(1u << (q & 31)));
+            }
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+    uint32_t any = 0;
+    for (int w = 0; w < nw; ++w) {
+        const uint32_t word = sW[w][tid];
         if (live) a.mask.bits[(long long)(tile * kWordsPerTile + w) * a.mask.pitch + j] = word;
         any |= word;
     }

@@ -264,6 +264,7 @@ struct Model {
     float opt_cmp_rcut = 24.0f; // network: propose blocks whose predicted rank is below this
     int opt_aca_variant = 0;    // cross-approximation kernel shape (factor ranks in shared memory, CTAs per SM)
     int opt_mask_classify = 1;  // bounce masks: warp-per-block classification, pair kernel on the listed blocks
+    int opt_gate_proj = 1;      // bounce masks: gates decided from per-point projections where certain
     Compression cmp;
     std::vector<HopRecord> log;
     long long launches = 0, h2d_bytes = 0, d2h_bytes = 0;
@@ -575,6 +576,7 @@ MaskEntry build_mask(int hop, int a, int b, int full, const MaskEntry *reuse = n
     if (full) CK(cudaMemsetAsync(v.bits, 0, std::max<size_t>(words, 1) * sizeof(uint32_t), g.stream));
     hs.m.mask = v;
     hs.m.full = full;
+    hs.m.gate_proj = g.opt_gate_proj;
     hs.m.upper_only = (hop == HOP_F2F && !full && g.opt_f2f_sym) ? 1 : 0;
     CK(cudaEventRecord(g.ev0, g.stream));
     if (classify) {
@@ -1447,6 +1449,11 @@ int sonar_set_option(const char *key, double value)
     if (!strcmp(key, "compress_select")) {
         g.opt_cmp_select = std::max(0, std::min(2, (int)value));
         g.cmp.release();
+        return 0;
+    }
+    if (!strcmp(key, "mask_gate_proj")) {
+        g.opt_gate_proj = value != 0.0 ? 1 : 0;
+        for (auto &m : g.masks) m.stale = true;
         return 0;
     }
     if (!strcmp(key, "mask_classify")) {

@@ -72,6 +72,7 @@ struct MaskArgs {
     MaskView mask;
     const int2 *blist = nullptr;    // optional: (source tile, destination block) of the blocks to build
     const int *blist_count = nullptr;
+    int gate_proj = 1;              // FACET_SELF: decide gates from per-point projections where certain
 };
 
 struct SumArgs {

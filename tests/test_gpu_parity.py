@@ -246,7 +246,7 @@ def test_symmetric_bounce_sum_matches_ordered(api, scenes):
 
 
 @pytest.mark.parametrize("extra", ["none", "box", "sphere"])
-def test_bounce_mask_classification_pass_identical(api, scenes, extra):
+def test_bounce_mask_classification_pass_identical(api, oracle_mod, scenes, extra):
     """The bounce mask built by the warp-per-block classification pass (pair
     kernel on the listed blocks only) and by the pair kernel over every block
     give the same block classes and bit-identical bounces: the trihedral
@@ -280,3 +280,25 @@ def test_bounce_mask_classification_pass_identical(api, scenes, extra):
     for k in out[1]:
         assert np.array_equal(out[1][k], out[0][k]), k
     assert np.abs(out[1]["P_target0"]).max() > 0
+    # the exported bounce mask (every pair) with the gates decided from the
+    # per-point projections where certain, and always per pair: identical,
+    # and equal to the oracle's outside grazing pairs on seeded destinations
+    load_scene(api, sc)
+    masks = {}
+    for gp in (1, 0):
+        api.set_option("mask_gate_proj", gp)
+        masks[gp] = api.get_mask(2, 0, 0)
+    api.set_option("mask_gate_proj", 1)
+    api.TearDownCuda()
+    assert np.array_equal(masks[1], masks[0])
+    o = oracle_scene(oracle_mod, sc)
+    n = o.nact(0, 0)
+    dst = np.sort(np.random.default_rng(5).choice(n, 96, replace=False))
+    gm = masks[1].reshape(n, n)[dst]
+    _, om = o.hop_subset(2, 0, 0, dst, want_mask=True, nsrc=n)
+    o.close()
+    graze = (om & 2) != 0
+    diff = (gm != (om & 1)) & ~graze
+    print(extra, "bounce mask vs oracle: pairs %d interacting %d grazing %d mismatches %d"
+          % (gm.size, int(gm.sum()), int(graze.sum()), int(diff.sum())))
+    assert diff.sum() == 0
