@@ -1572,10 +1572,12 @@ __global__ void __launch_bounds__(1024) k_sym_chunks(const int *rowcnt, int nb, 
     }
 }
 
-// Persistent CTAs take the chunks round-robin (a fixed assignment: results
-// do not depend on timing).  Per chunk: the row terms of its blocks into
-// rowpart[chunk] (FP64), the column terms of block (t, J), t < J, into
-// colpart[256 J (J-1) / 2 + i].
+// Persistent CTAs take the chunks from a counter in chunk order, so chunks of
+// uneven cost (diagonal blocks, the few dense blocks left by compression)
+// balance over the CTAs; every chunk writes its own output locations, so the
+// results do not depend on which CTA took it.  Per chunk: the row terms of
+// its blocks into rowpart[chunk] (FP64), the column terms of block (t, J),
+// t < J, into colpart[256 J (J-1) / 2 + i].
 template <bool ATT>
 __global__ void __launch_bounds__(kTile, 3) k_sum_f2f_sym(SumArgs a, SymWork wl, double2 *colpart, double2 *rowpart)
 {
@@ -1585,9 +1587,15 @@ __global__ void __launch_bounds__(kTile, 3) k_sum_f2f_sym(SumArgs a, SymWork wl,
     __shared__ float2 sCol[kTile / 32][kTile];
     __shared__ float sTb[6];  // source tile box
     __shared__ int sDb[6];    // destination block box
+    __shared__ int sCh;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nch = *wl.nchunks;
-    for (int ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+    for (;;) {
+        // sCh was last read before the previous chunk's barriers
+        if (tid == 0) sCh = atomicAdd(wl.next, 1);
+        __syncthreads();
+        const int ch = sCh;
+        if (ch >= nch) break;  // CTA-uniform
         const int4 cw = wl.chunks[ch];
         const int J = cw.x;
         const int j = J * kTile + tid;
@@ -1757,11 +1765,23 @@ __global__ void k_finalize_f2f_sym(const double2 *rowpart, const int *chunk_off,
     }
     if (pin.x != 0.0 || pin.y != 0.0) {
         double cr = 0.0, ci = 0.0;
-        for (int J = I + 1; J < ntiles; ++J) {
-            if (flags[(long long)I * ntiles + J] == kFlagNone) continue;
-            const double2 v = colpart[(long long)kTile * J * (J - 1) / 2 + q];
-            cr += v.x;
-            ci += v.y;
+        // the tile's flag row, 16 flags at a time where aligned (rows of a
+        // compressed bounce are mostly NONE); columns added in J order
+        const uint8_t *frow = flags + (long long)I * ntiles;
+        for (int J = I + 1; J < ntiles;) {
+            if ((reinterpret_cast<uintptr_t>(frow + J) & 15u) == 0 && J + 16 <= ntiles) {
+                const uint4 v = *reinterpret_cast<const uint4 *>(frow + J);
+                if ((v.x | v.y | v.z | v.w) == 0u) {
+                    J += 16;
+                    continue;
+                }
+            }
+            if (frow[J] != kFlagNone) {
+                const double2 v = colpart[(long long)kTile * J * (J - 1) / 2 + q];
+                cr += v.x;
+                ci += v.y;
+            }
+            ++J;
         }
         if (ycol) {
             cr += ycol[q].x;
@@ -2466,6 +2486,7 @@ void launch_sum_f2f_sym(const SumArgs &a, const SymWork &wl, int grid, double2 *
         cudaFuncSetAttribute(k_sum_f2f_sym<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymDynSmem);
         attr_set = true;
     }
+    cudaMemsetAsync(wl.next, 0, sizeof(int), s);
     if (a.ka != 0.0f)
         k_sum_f2f_sym<true><<<grid, kTile, kSymDynSmem, s>>>(a, wl, colpart, rowpart);
     else

@@ -647,7 +647,7 @@ void ensure_symwork(int ntiles)
     g.d_blist = dalloc<int>((size_t)ntiles * ntiles);
     g.d_rowcnt = dalloc<int>(ntiles);
     g.d_chunk_off = dalloc<int>(ntiles + 1);
-    g.d_nchunks = dalloc<int>(1);
+    g.d_nchunks = dalloc<int>(2);  // chunk count, next-chunk counter
     g.d_chunks = dalloc<int4>(maxch);
     g.d_rowpart = dalloc<double2>(maxch * kTile);
     g.sym_tiles = ntiles;
@@ -934,7 +934,7 @@ void run_hop(int hop, int a, int b)
             ensure_symwork(M.view.ntiles);
             launch_sym_worklist(s.mask.flags, M.view.ntiles, M.view.ndstblocks, kSymChunk, g.d_blist, g.d_rowcnt,
                                 g.d_chunk_off, g.d_chunks, g.d_nchunks, st);
-            const SymWork wl{g.d_blist, g.d_chunks, g.d_nchunks, M.view.ntiles};
+            const SymWork wl{g.d_blist, g.d_chunks, g.d_nchunks, M.view.ntiles, g.d_nchunks + 1};
             CK(cudaEventRecord(g.ev2, st));
             launch_sum_f2f_sym(s, wl, 3 * g.nsm, g.d_colpart, g.d_rowpart, st);
             CK(cudaEventRecord(g.ev3, st));

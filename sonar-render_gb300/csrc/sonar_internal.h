@@ -124,6 +124,7 @@ struct SymWork {
     const int4 *chunks;    // (J, k0, k1)
     const int *nchunks;    // device count
     int ntiles;
+    int *next;             // device counter of the next chunk to take (zeroed by the launcher)
 };
 void launch_sym_worklist(const uint8_t *flags, int ntiles, int nb, int per, int *blist, int *rowcnt, int *chunk_off,
                          int4 *chunks, int *nchunks, cudaStream_t s);
