@@ -135,7 +135,18 @@ int sonar_get_stats(char *json, int cap);
  * "verbose" (0/1), "reset_stats", "reset_pressures" (zero every surface and
  * field-point pressure), "drop_masks" (rebuild the cached interaction masks,
  * in place, at their next use), "free_masks" (free them), "class_stats"
- * (count the mask's block classes).
+ * (count the mask's block classes), "mask_classify" (1, default: bounce
+ * masks classify their blocks one warp per block and build per-pair bits
+ * only for the blocks that need them; 0: every block in the pair kernel),
+ * "mask_gate_proj" (1, default: the pair kernel decides gates from per-point
+ * projections where that is certain; 0: every pair's gates evaluated).
+ * "cross_objects" (0, default: bounces stay within each target, as in the
+ * reference's ProjectTargetToTargetObjects; 1: every bounce also carries
+ * the terms between every pair of targets -- the reference's FACET_RESP
+ * projection, src/OptiX.cu:192-406, :427-429, which its host never calls --
+ * forward into the higher-index object, reciprocal into the lower, all
+ * from the bounce's inputs).
+ * "aca_variant" (cross-approximation kernel shape, 0-2; bit-identical).
  * Low-rank bounce blocks (no counterpart in the reference, which evaluates
  * every pair): "compress" (0/1), "compress_tol" (cross-approximation stopping
  * tolerance, 1e-4), "compress_judge" (largest accepted relative RMS error of
@@ -159,8 +170,10 @@ double sonar_measure_peak(int which);
  * and visibility gates.  hop 0 sources -> cells of object dstIdx of type
  * srcIdx (0 target, 2 field); hop 1 active cells of target srcIdx -> field
  * points; hop 2 active cells of target srcIdx -> themselves; hop 3 active
- * cells of target srcIdx -> active cells of field object dstIdx.  Returns
- * the number of bytes (ndst*nsrc), or < 0.  The mask is built if needed. */
+ * cells of target srcIdx -> active cells of field object dstIdx; hop 4
+ * (FACET_RESP) active cells of target srcIdx -> active cells of target
+ * dstIdx != srcIdx.  Returns the number of bytes (ndst*nsrc), or < 0.  The
+ * mask is built if needed. */
 long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, long long cap);
 
 /* Host only (no GPU needed): frame and clipped area grid of one triangle

@@ -82,6 +82,7 @@ def lib():
             getattr(L, n).argtypes = [_vp]
         L.orc_project_sources.argtypes = [_vp, C.c_int]
         L.orc_project_bounces.argtypes = [_vp, C.c_int]
+        L.orc_project_bounces_cross.argtypes = [_vp, C.c_int]
         L.orc_hop_subset.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _l, C.c_long, _d, _d, _u8]
         L.orc_hop_subset.restype = C.c_long
         L.orc_counter.argtypes = [_vp, C.c_int]
@@ -205,8 +206,13 @@ class Oracle:
     def project_sources(self, field_objects=False):
         self.L.orc_project_sources(self.h, int(bool(field_objects)))
 
-    def project_bounces(self, n):
-        self.L.orc_project_bounces(self.h, int(n))
+    def project_bounces(self, n, cross_objects=False):
+        """FACET_SELF bounces of every target (the reference's sequence); with
+        cross_objects also FACET_RESP between every pair of targets."""
+        if cross_objects:
+            self.L.orc_project_bounces_cross(self.h, int(n))
+        else:
+            self.L.orc_project_bounces(self.h, int(n))
 
     def project_field_objects(self):
         self.L.orc_project_field_objects(self.h)

@@ -21,6 +21,7 @@
  *   hop_fieldpoint()        src/OptiX.cu:112-190  (fragment -> field point)
  *   hop_f2f_cell()          src/OptiX.cu:192-406  (FACET_SELF with reciprocity)
  *   hop_noresp_cell()       src/OptiX.cu:192-406  (FACET_NO_RESP, target -> field object)
+ *   hop_resp_cell()         src/OptiX.cu:192-406, :427-429 (FACET_RESP, target -> other target)
  *   orc_project_*()         src/ModelCuda.cpp:242-356, src/FacetCuda.cpp:114-137,
  *                           src/FacetCuda.cu:87-101 (prime / swap / accumulate)
  *
@@ -909,6 +910,71 @@ static void hop_noresp_cell(scene_t *s, const object_t *A, const object_t *B, lo
     acc[0] = ar; acc[1] = ai;
 }
 
+/* ---- hop a6, FACET_RESP (target object A -> another target object B, with
+ * reciprocity): src/OptiX.cu:192-406 with useReciprocity and not isSelf
+ * (:427-429; the reference has no host caller for it).  Every active cell
+ * pair (i of A, j of B): uv from p_i to p_j, cos_scat at A's normal, cos_inc
+ * at B's, the ray from p_i, G regularised below A's delta and damped by 0.9.
+ * Destination-owned restatement:
+ *   fwd = 1: cell j of B receives A_i cos_scat cos_inc P_in,A[i] G from every
+ *            cell i of A with P_in,A[i] != 0 (OptiX.cu:241-245, :354-364);
+ *   fwd = 0: cell i of A receives B_j cos_scat cos_inc P_in,B[j] G from every
+ *            cell j of B (the reciprocal write, :367-390), nothing at all when
+ *            P_in,A[i] == 0 (the zero-input skip of the A side kills it). */
+static void hop_resp_cell(scene_t *s, const object_t *A, const object_t *B, int fwd, long q_d, double *acc,
+                          uint8_t *mask_row, long long *cnt)
+{
+    const object_t *D = fwd ? B : A, *S = fwd ? A : B;
+    const long cd = D->act[q_d];
+    int fd, xd, yd;
+    cell_xy(D, cd, &fd, &xd, &yd);
+    const facet_t *Fd = &D->f[fd];
+    const f3 pd = frag_pos(Fd, xd, yd, 0);
+    const float rmin = A->delta;
+    const int gate_zero = !fwd && A->Pin[2 * cd] == 0.0 && A->Pin[2 * cd + 1] == 0.0;
+    double ar = 0.0, ai = 0.0;
+    for (long q = 0; q < S->nact; q++) {
+        const long cs_ = S->act[q];
+        int fs, xs, ys;
+        cell_xy(S, cs_, &fs, &xs, &ys);
+        const facet_t *Fs = &S->f[fs];
+        const f3 ps = frag_pos(Fs, xs, ys, 0);
+        const f3 pA = fwd ? ps : pd, pB = fwd ? pd : ps;
+        const facet_t *FA = fwd ? Fs : Fd, *FB = fwd ? Fd : Fs;
+        uint8_t m = 0;
+        f3 v = {pB.x - pA.x, pB.y - pA.y, pB.z - pA.z};
+        float r = sqrtf(dot_sc(v, v));
+        float inv = 1.0f / r;
+        f3 uv = {v.x * inv, v.y * inv, v.z * inv};
+        float cs = dot_sc(uv, FA->normal);
+        f3 nuv = {-uv.x, -uv.y, -uv.z};
+        float cin = dot_sc(nuv, FB->normal);
+        if (!(cs < 1e-6f) && !(cin < 1e-6f)) {
+            double o[3], e[3];
+            to_d3(pA, o); to_d3(pB, e);
+            int graze, spf;
+            int hit = seg_occluded(s, o, e, (double)(r - 1e-3f), &graze, &spf);
+            if (graze) { m |= 2; cnt[1]++; }
+            if (spf) cnt[2]++;
+            if (!hit) {
+                m |= 1;
+                const double Pr = S->Pin[2 * cs_], Pim = S->Pin[2 * cs_ + 1];
+                if (!gate_zero && !(Pr == 0.0 && Pim == 0.0)) {
+                    double gr, gi;
+                    green_f2f(s, r, rmin, &gr, &gi);
+                    const double w = (double)((S->area[cs_] * cs) * cin);
+                    const double pr = w * Pr, pim = w * Pim;
+                    ar += pr * gr - pim * gi;
+                    ai += pr * gi + pim * gr;
+                }
+            }
+        }
+        cnt[0]++;
+        if (mask_row) mask_row[q] = m;
+    }
+    acc[0] = ar; acc[1] = ai;
+}
+
 static void reset_counters(scene_t *s) { s->c_pairs = s->c_graze = s->c_selfplane = 0; }
 
 #define OMP_COUNTERS long long c0 = 0, c1 = 0, c2 = 0;
@@ -939,6 +1005,71 @@ int orc_project_sources(void *h, int field_objects)
     for (int i = 0; i < s->nobj[OBJ_TARGET]; i++) project_sources_obj(s, s->obj[OBJ_TARGET][i]);
     if (field_objects)
         for (int i = 0; i < s->nobj[OBJ_FIELD]; i++) project_sources_obj(s, s->obj[OBJ_FIELD][i]);
+    return 0;
+}
+
+/* Bounces with cross-object terms (an extension; the reference's host never
+ * calls FACET_RESP): prime P_out <- P on every target; per bounce every
+ * target takes P_in <- P_out, P_out <- 0; then each target's FACET_SELF
+ * projection, then FACET_RESP for every pair a < b (forward into b, the
+ * reciprocal terms into a), all from this bounce's inputs; then P += P_out
+ * on every target. */
+int orc_project_bounces_cross(void *h, int nb)
+{
+    scene_t *s = (scene_t *)h;
+    if (!s->rendered) return -1;
+    reset_counters(s);
+    const int nt = s->nobj[OBJ_TARGET];
+    for (int oi = 0; oi < nt; oi++) {
+        object_t *O = s->obj[OBJ_TARGET][oi];
+        memcpy(O->Pout, O->P, sizeof(double) * 2 * O->ncells);
+    }
+    for (int b = 0; b < nb; b++) {
+        for (int oi = 0; oi < nt; oi++) {
+            object_t *O = s->obj[OBJ_TARGET][oi];
+            memcpy(O->Pin, O->Pout, sizeof(double) * 2 * O->ncells);
+            memset(O->Pout, 0, sizeof(double) * 2 * O->ncells);
+        }
+        for (int oi = 0; oi < nt; oi++) {
+            object_t *O = s->obj[OBJ_TARGET][oi];
+            OMP_COUNTERS
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : c0, c1, c2)
+            for (long q = 0; q < O->nact; q++) {
+                double acc[2];
+                long long cnt[3] = {0, 0, 0};
+                hop_f2f_cell(s, O, q, O->Pin, acc, NULL, cnt);
+                O->Pout[2 * O->act[q]] = acc[0];
+                O->Pout[2 * O->act[q] + 1] = acc[1];
+                c0 += cnt[0]; c1 += cnt[1]; c2 += cnt[2];
+            }
+            OMP_COUNTERS_ADD
+        }
+        for (int ai_ = 0; ai_ < nt; ai_++)
+            for (int bi_ = ai_ + 1; bi_ < nt; bi_++) {
+                object_t *A = s->obj[OBJ_TARGET][ai_], *B = s->obj[OBJ_TARGET][bi_];
+                for (int fwd = 1; fwd >= 0; fwd--) {
+                    object_t *D = fwd ? B : A;
+                    OMP_COUNTERS
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : c0, c1, c2)
+                    for (long q = 0; q < D->nact; q++) {
+                        double acc[2];
+                        long long cnt[3] = {0, 0, 0};
+                        hop_resp_cell(s, A, B, fwd, q, acc, NULL, cnt);
+                        D->Pout[2 * D->act[q]] += acc[0];
+                        D->Pout[2 * D->act[q] + 1] += acc[1];
+                        c0 += cnt[0]; c1 += cnt[1]; c2 += cnt[2];
+                    }
+                    OMP_COUNTERS_ADD
+                }
+            }
+        for (int oi = 0; oi < nt; oi++) {
+            object_t *O = s->obj[OBJ_TARGET][oi];
+            for (long c = 0; c < O->ncells; c++) {
+                O->P[2 * c] += O->Pout[2 * c];
+                O->P[2 * c + 1] += O->Pout[2 * c + 1];
+            }
+        }
+    }
     return 0;
 }
 
@@ -1063,6 +1194,16 @@ long orc_hop_subset(void *h, int hop, int a_idx, int b_idx, const long *dst, lon
         B = s->obj[OBJ_FIELD][b_idx];
         nsrc = A->nact;
         break;
+    case 4:
+        /* FACET_RESP between targets a_idx (sources) and b_idx (destinations):
+         * the forward terms when a_idx < b_idx, the reciprocal ones when
+         * a_idx > b_idx; the inputs are the objects' P_in */
+        if (a_idx < 0 || a_idx >= s->nobj[OBJ_TARGET] || b_idx < 0 || b_idx >= s->nobj[OBJ_TARGET] || a_idx == b_idx)
+            return -2;
+        A = s->obj[OBJ_TARGET][a_idx < b_idx ? a_idx : b_idx];
+        B = s->obj[OBJ_TARGET][a_idx < b_idx ? b_idx : a_idx];
+        nsrc = s->obj[OBJ_TARGET][a_idx]->nact;
+        break;
     default:
         return -3;
     }
@@ -1077,6 +1218,7 @@ long orc_hop_subset(void *h, int hop, int a_idx, int b_idx, const long *dst, lon
         case 1: hop_fieldpoint(s, A, (int)dst[k], acc, row, cnt); break;
         case 2: hop_f2f_cell(s, A, dst[k], pin, acc, row, cnt); break;
         case 3: hop_noresp_cell(s, A, B, dst[k], acc, row, cnt); break;
+        case 4: hop_resp_cell(s, A, B, a_idx < b_idx, dst[k], acc, row, cnt); break;
         }
         out[2 * k] = acc[0];
         out[2 * k + 1] = acc[1];

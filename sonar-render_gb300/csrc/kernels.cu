@@ -194,7 +194,8 @@ __device__ __forceinline__ bool pair_gates_vote(const MaskArgs &a, float4 s, flo
         return cos_gate_vote(vx, vy, vz, rinv, -1.0f, nt.x, nt.y, nt.z, active);
     }
     if (HOP == HOP_FP || HOP == HOP_NORESP) return cos_gate_vote(vx, vy, vz, rinv, 1.0f, ns.x, ns.y, ns.z, active);
-    const bool other = __float_as_int(ns.w) != ft;
+    // FACET_RESP: two objects, no same-facet rule
+    const bool other = HOP == HOP_RESP || __float_as_int(ns.w) != ft;
     const bool g1 = cos_gate_vote(vx, vy, vz, rinv, 1.0f, ns.x, ns.y, ns.z, active && other);
     const bool g2 = cos_gate_vote(vx, vy, vz, rinv, -1.0f, nt.x, nt.y, nt.z, active && other);
     return other && g1 && g2;
@@ -214,16 +215,21 @@ __device__ __forceinline__ bool pair_gates(const MaskArgs &a, float4 s, float4 n
     if (HOP == HOP_SRC) return cos_gate(vx, vy, vz, rinv, -1.0f, nt.x, nt.y, nt.z);   // cos_inc = dot(-uv, n_B)
     if (HOP == HOP_FP) return cos_gate(vx, vy, vz, rinv, 1.0f, ns.x, ns.y, ns.z);     // cos_scat = dot(-uv_ji, n_A)
     if (HOP == HOP_NORESP) return cos_gate(vx, vy, vz, rinv, 1.0f, ns.x, ns.y, ns.z); // cos_scat = dot(uv, n_A)
+    // FACET_SELF and FACET_RESP: cos_scat at the source's facet, cos_inc at the destination's
     return cos_gate(vx, vy, vz, rinv, 1.0f, ns.x, ns.y, ns.z) && cos_gate(vx, vy, vz, rinv, -1.0f, nt.x, nt.y, nt.z);
 }
 
 // The shadow ray of a pair: origin and end point (OptiX.cu:81-93, 163-175, 321-333).
+// FACET_RESP: from the point of the enumeration's source object (the lower
+// object index), i.e. from the destination when dst_origin.
 template <int HOP>
-__device__ __forceinline__ void pair_ray(float4 s, float4 ns, float4 t, int ft, float3 &o, float3 &e)
+__device__ __forceinline__ void pair_ray(float4 s, float4 ns, float4 t, int ft, float3 &o, float3 &e,
+                                         bool dst_origin = false)
 {
     bool src_first = true;  // source point, target fragment (NO_RESP), lower facet (SELF)
     if (HOP == HOP_FP) src_first = false;  // from the field point
     if (HOP == HOP_F2F) src_first = __float_as_int(ns.w) < ft;
+    if (HOP == HOP_RESP) src_first = !dst_origin;
     o = src_first ? make_float3(s.x, s.y, s.z) : make_float3(t.x, t.y, t.z);
     e = src_first ? make_float3(t.x, t.y, t.z) : make_float3(s.x, s.y, s.z);
 }
@@ -501,8 +507,8 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
                             dz = o2f(sBox[5]) - o2f(sBox[2]);
                 const float rmax = sqrtf(dx * dx + dy * dy + dz * dz) * 1.0001f;
                 // which side holds the ray origins
-                bool src_origin = (HOP == HOP_SRC || HOP == HOP_NORESP);
-                bool dst_origin = (HOP == HOP_FP);
+                bool src_origin = (HOP == HOP_SRC || HOP == HOP_NORESP || (HOP == HOP_RESP && !a.resp_dst_origin));
+                bool dst_origin = (HOP == HOP_FP || (HOP == HOP_RESP && a.resp_dst_origin));
                 if (HOP == HOP_F2F) {
                     src_origin = sFac[0] < sFac[3];  // some source facet below some destination facet
                     dst_origin = sFac[2] < sFac[1];
@@ -529,7 +535,8 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
             // inside, before tmax (ray origins on one side: sources for the
             // source hop and NO_RESP, destinations for the field-point readout)
             if (HOP != HOP_F2F && sKeep > 0) {
-                const int ob = (HOP == HOP_FP) ? 12 : 6, eb = (HOP == HOP_FP) ? 6 : 12;
+                const bool from_dst = HOP == HOP_FP || (HOP == HOP_RESP && a.resp_dst_origin);
+                const int ob = from_dst ? 12 : 6, eb = from_dst ? 6 : 12;
                 const float ol[3] = {o2f(sBox[ob]), o2f(sBox[ob + 1]), o2f(sBox[ob + 2])};
                 const float oh[3] = {o2f(sBox[ob + 3]), o2f(sBox[ob + 4]), o2f(sBox[ob + 5])};
                 const float el[3] = {o2f(sBox[eb]), o2f(sBox[eb + 1]), o2f(sBox[eb + 2])};
@@ -628,7 +635,8 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
     __shared__ float2 sProj[kTile];
     __shared__ float4 sWP[kWordsPerTile];  // per word: min, max of p.n_s; min, max of p.n_d
     {
-        const bool need_s = HOP != HOP_SRC, need_d = (HOP == HOP_SRC && !a.dst_is_field) || HOP == HOP_F2F;
+        const bool need_s = HOP != HOP_SRC,
+                   need_d = (HOP == HOP_SRC && !a.dst_is_field) || HOP == HOP_F2F || HOP == HOP_RESP;
         const bool uni = (!need_s || sFac[0] == sFac[1]) && (!need_d || sFac[2] == sFac[3]);
         if (uni) {
             const float4 ns = sN[0];
@@ -821,7 +829,7 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
                     tq &= tq - 1u;
                     const int q = w * 32 + b;
                     float3 o, e;
-                    pair_ray<HOP>(sP[q], sN[q], t, ft, o, e);
+                    pair_ray<HOP>(sP[q], sN[q], t, ft, o, e, a.resp_dst_origin);
                     if (occluded_full(a.bvh, o, e)) word &= ~(1u << b);
                 }
             }
@@ -836,7 +844,7 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
                 const int q = (int)(code >> 8), jl = (int)(code & 255u);
                 const float4 td = sTd[jl];
                 float3 o, en;
-                pair_ray<HOP>(sP[q], sN[q], td, __float_as_int(td.w), o, en);
+                pair_ray<HOP>(sP[q], sN[q], td, __float_as_int(td.w), o, en, a.resp_dst_origin);
                 if (occluded_list(sTri, nkeep, o, en)) atomicAnd(&sW[w][jl], ~(1u << (q & 31)));
             }
             __syncthreads();
@@ -1242,7 +1250,7 @@ __device__ __forceinline__ void pair_term(const SumArgs &a, const float4 A, cons
         }
         const float c1 = (vx * B.x + vy * B.y + vz * B.z) * rinv;  // cos_scat (source side)
         float wgt;
-        if (HOP == HOP_F2F) {
+        if (HOP == HOP_F2F || HOP == HOP_RESP) {
             const float c2 = -(vx * d.nx + vy * d.ny + vz * d.nz) * rinv;  // cos_inc (destination side)
             wgt = c1 * c2;
             if (GATE) ok = gate_from(c1, vx, vy, vz, 1.0f, B.x, B.y, B.z) && gate_from(c2, vx, vy, vz, -1.0f, d.nx, d.ny, d.nz);
@@ -2318,6 +2326,35 @@ __global__ void k_finalize_f2f(const double2 *partial, int nsplit, int ndst, con
     P[c] = o;
 }
 
+// FACET_RESP: P_out[cell] += s, P[cell] += s; with gate_pin, destinations
+// whose P_in is 0 receive nothing (the zero-input skip of the first object's
+// cell also kills its reciprocal term, OptiX.cu:241-245, :367-390)
+__global__ void k_finalize_resp(const double2 *partial, int nsplit, int ndst, const int *cell,
+                                const double2 *gate_pin, double2 *Pout, double2 *P)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= ndst) return;
+    const int c = cell[j];
+    if (gate_pin) {
+        const double2 g = gate_pin[c];
+        if (g.x == 0.0 && g.y == 0.0) return;
+    }
+    double sr = 0.0, si = 0.0;
+    for (int k = 0; k < nsplit; ++k) {
+        const double2 v = partial[(long long)k * ndst + j];
+        sr += v.x;
+        si += v.y;
+    }
+    double2 o = Pout[c];
+    o.x += sr;
+    o.y += si;
+    Pout[c] = o;
+    o = P[c];
+    o.x += sr;
+    o.y += si;
+    P[c] = o;
+}
+
 __global__ void k_mask_export(MaskView m, int nsrc, int ndst, uint8_t *out)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2431,6 +2468,7 @@ void launch_mask(const MaskArgs &a, cudaStream_t s)
     case HOP_SRC: k_mask<HOP_SRC><<<grid, kTile, 0, s>>>(a); break;
     case HOP_FP: k_mask<HOP_FP><<<grid, kTile, 0, s>>>(a); break;
     case HOP_F2F: k_mask<HOP_F2F><<<grid, kTile, 0, s>>>(a); break;
+    case HOP_RESP: k_mask<HOP_RESP><<<grid, kTile, 0, s>>>(a); break;
     default: k_mask<HOP_NORESP><<<grid, kTile, 0, s>>>(a); break;
     }
 }
@@ -2460,6 +2498,10 @@ void launch_sum(const SumArgs &a, cudaStream_t s)
     case HOP_F2F:
         if (att) k_sum<HOP_F2F, true><<<grid, kTile, 0, s>>>(a);
         else k_sum<HOP_F2F, false><<<grid, kTile, 0, s>>>(a);
+        break;
+    case HOP_RESP:
+        if (att) k_sum<HOP_RESP, true><<<grid, kTile, 0, s>>>(a);
+        else k_sum<HOP_RESP, false><<<grid, kTile, 0, s>>>(a);
         break;
     default:
         if (att) k_sum<HOP_NORESP, true><<<grid, kTile, 0, s>>>(a);
@@ -2592,6 +2634,12 @@ void launch_finalize_f2f(const double2 *partial, int nsplit, int ndst, const int
                          cudaStream_t s)
 {
     if (ndst > 0) k_finalize_f2f<<<blocks_for(ndst, 256), 256, 0, s>>>(partial, nsplit, ndst, cell, Pout, P);
+}
+
+void launch_finalize_resp(const double2 *partial, int nsplit, int ndst, const int *cell, const double2 *gate_pin,
+                          double2 *Pout, double2 *P, cudaStream_t s)
+{
+    if (ndst > 0) k_finalize_resp<<<blocks_for(ndst, 256), 256, 0, s>>>(partial, nsplit, ndst, cell, gate_pin, Pout, P);
 }
 
 void launch_mask_export(const MaskView &m, int nsrc, int ndst, uint8_t *out, cudaStream_t s)

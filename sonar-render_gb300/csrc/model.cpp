@@ -265,6 +265,7 @@ struct Model {
     int opt_aca_variant = 0;    // cross-approximation kernel shape (factor ranks in shared memory, CTAs per SM)
     int opt_mask_classify = 1;  // bounce masks: warp-per-block classification, pair kernel on the listed blocks
     int opt_gate_proj = 1;      // bounce masks: gates decided from per-point projections where certain
+    int opt_cross_objects = 0;  // bounces also between different targets (FACET_RESP); 0: the reference's behaviour
     Compression cmp;
     std::vector<HopRecord> log;
     long long launches = 0, h2d_bytes = 0, d2h_bytes = 0;
@@ -516,6 +517,21 @@ HopSets hop_sets(int hop, int a, int b)
         m.src_pos = m.dst_pos = A.d_act_pos;
         m.src_facet = m.dst_facet = A.d_act_facet;
         m.src_facet_n = m.dst_facet_n = A.d_facet_n;
+    } else if (hop == HOP_RESP) {
+        // FACET_RESP between two targets: sources of a, destinations of b; the
+        // ray starts at the lower-index object's point
+        if (a == b) fail(-6, "FACET_RESP needs two different target objects (got %d and %d)", a, b);
+        Object &A = get(OBJ_TARGET, a);
+        Object &B = get(OBJ_TARGET, b);
+        m.nsrc = A.nact();
+        m.src_pos = A.d_act_pos;
+        m.src_facet = A.d_act_facet;
+        m.src_facet_n = A.d_facet_n;
+        m.ndst = B.nact();
+        m.dst_pos = B.d_act_pos;
+        m.dst_facet = B.d_act_facet;
+        m.dst_facet_n = B.d_facet_n;
+        m.resp_dst_origin = a > b ? 1 : 0;
     } else {
         Object &A = get(OBJ_TARGET, a);
         Object &B = get(OBJ_FIELD, b);
@@ -848,6 +864,7 @@ long long pair_count(int hop, int a, int b)
         for (long long n : A.facet_nact) sq += n * n;
         return tot * tot - sq;
     }
+    if (hop == HOP_RESP) return (long long)get(OBJ_TARGET, a).nact() * get(OBJ_TARGET, b).nact();
     return (long long)get(OBJ_TARGET, a).nact() * get(OBJ_FIELD, b).nact();
 }
 
@@ -944,6 +961,19 @@ void run_hop(int hop, int a, int b)
             timed_sum(s, st);
             launch_finalize_f2f(g.d_partial, s.nsplit, M.ndst, A.d_act_cell, A.d_Pout, A.d_P, st);
         }
+    } else if (hop == HOP_RESP) {
+        // FACET_RESP, one direction: sources of target a (their P_in, 0.9 A_i),
+        // destinations of target b; r_min is the delta of the lower-index
+        // object (the reference's source object of the FACET_RESP call)
+        Object &A = get(OBJ_TARGET, a);
+        Object &B = get(OBJ_TARGET, b);
+        s.rmin = get(OBJ_TARGET, std::min(a, b)).delta;
+        launch_pack_frags(A.d_act_pos, A.d_act_facet, A.d_act_cell, A.d_facet_n, A.d_Pin, 0.9f, M.nsrc, g.d_packA,
+                          g.d_packB, st);
+        timed_sum(s, st);
+        // reciprocal direction (into the lower-index object): gated by its P_in
+        launch_finalize_resp(g.d_partial, s.nsplit, M.ndst, B.d_act_cell, a > b ? B.d_Pin : nullptr, B.d_Pout, B.d_P,
+                             st);
     } else {
         Object &A = get(OBJ_TARGET, a);
         Object &B = get(OBJ_FIELD, b);
@@ -1259,7 +1289,37 @@ void ProjectTargetToTargetObjects(int number_reflections)
         // src/ModelCuda.cpp:323-356: prime P_out <- P; per bounce P_in <- P_out,
         // P_out <- 0, project, P += P_out.  Objects never interact, so each
         // object runs its bounces in turn; P_in/P_out swap by pointer.
-        for (int t = 0; t < (int)g.obj[OBJ_TARGET].size(); t++) {
+        // With the cross_objects option (an extension: FACET_RESP, which the
+        // reference's host never calls) every bounce also carries the terms
+        // between every pair of targets: all targets swap, then each runs its
+        // FACET_SELF projection (which writes P_out and adds it to P), then
+        // each pair a < b adds its forward terms into b and its reciprocal
+        // terms into a (to P_out and P), all from this bounce's P_in.
+        const int nt = (int)g.obj[OBJ_TARGET].size();
+        if (g.opt_cross_objects && nt > 1) {
+            for (int t = 0; t < nt; t++) {
+                Object &A = *g.obj[OBJ_TARGET][t];
+                const size_t bytes = std::max<size_t>((size_t)A.ncells, 1) * sizeof(double2);
+                CK(cudaMemcpyAsync(A.d_Pout, A.d_P, bytes, cudaMemcpyDeviceToDevice, g.stream));
+            }
+            for (int b = 0; b < number_reflections; b++) {
+                for (int t = 0; t < nt; t++) {
+                    Object &A = *g.obj[OBJ_TARGET][t];
+                    const size_t bytes = std::max<size_t>((size_t)A.ncells, 1) * sizeof(double2);
+                    std::swap(A.d_Pin, A.d_Pout);
+                    CK(cudaMemsetAsync(A.d_Pout, 0, bytes, g.stream));
+                }
+                for (int t = 0; t < nt; t++) run_hop(HOP_F2F, t, 0);
+                for (int t = 0; t < nt; t++)
+                    for (int u = t + 1; u < nt; u++) {
+                        run_hop(HOP_RESP, t, u);
+                        run_hop(HOP_RESP, u, t);
+                    }
+            }
+            CK(cudaStreamSynchronize(g.stream));
+            return;
+        }
+        for (int t = 0; t < nt; t++) {
             Object &A = *g.obj[OBJ_TARGET][t];
             const size_t bytes = std::max<size_t>((size_t)A.ncells, 1) * sizeof(double2);
             CK(cudaMemcpyAsync(A.d_Pout, A.d_P, bytes, cudaMemcpyDeviceToDevice, g.stream));
@@ -1451,6 +1511,10 @@ int sonar_set_option(const char *key, double value)
         g.cmp.release();
         return 0;
     }
+    if (!strcmp(key, "cross_objects")) {
+        g.opt_cross_objects = value != 0.0 ? 1 : 0;
+        return 0;
+    }
     if (!strcmp(key, "mask_gate_proj")) {
         g.opt_gate_proj = value != 0.0 ? 1 : 0;
         for (auto &m : g.masks) m.stale = true;
@@ -1511,7 +1575,7 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
     long long nbytes = 0;
     int st = guarded([&] {
         need_render();
-        if (hop < HOP_SRC || hop > HOP_NORESP) fail(-6, "invalid hop %d", hop);
+        if (hop < HOP_SRC || hop > HOP_RESP) fail(-6, "invalid hop %d", hop);
         HopSets hs = hop_sets(hop, srcIdx, dstIdx);
         nbytes = (long long)hs.nsrc * hs.ndst;
         if (!out) return;
@@ -1540,8 +1604,9 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
             return rank;
         };
         std::vector<int> rs, rd;  // internal index -> canonical index (empty: identity)
-        if (hop == HOP_FP || hop == HOP_F2F || hop == HOP_NORESP) rs = canon(get(OBJ_TARGET, srcIdx));
+        if (hop == HOP_FP || hop == HOP_F2F || hop == HOP_NORESP || hop == HOP_RESP) rs = canon(get(OBJ_TARGET, srcIdx));
         if (hop == HOP_F2F) rd = rs;
+        if (hop == HOP_RESP) rd = canon(get(OBJ_TARGET, dstIdx));
         if (hop == HOP_FP) rd = g.fp_order;  // stored field point k is load index fp_order[k]
         if (hop == HOP_NORESP) rd = canon(get(OBJ_FIELD, dstIdx));
         for (long long jd = 0; jd < M.ndst; jd++) {

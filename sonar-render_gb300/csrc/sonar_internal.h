@@ -23,7 +23,10 @@
 
 namespace sonar {
 
-enum Hop : int { HOP_SRC = 0, HOP_FP = 1, HOP_F2F = 2, HOP_NORESP = 3 };
+// HOP_RESP: target object -> another target object with reciprocity
+// (FACET_RESP); mask and sum of one direction, keyed (source object,
+// destination object); the ray starts at the lower-index object's point
+enum Hop : int { HOP_SRC = 0, HOP_FP = 1, HOP_F2F = 2, HOP_NORESP = 3, HOP_RESP = 4 };
 
 constexpr int kTile = 256;          // sources per tile, destinations per block
 constexpr int kWordsPerTile = kTile / 32;
@@ -73,6 +76,7 @@ struct MaskArgs {
     const int2 *blist = nullptr;    // optional: (source tile, destination block) of the blocks to build
     const int *blist_count = nullptr;
     int gate_proj = 1;              // FACET_SELF: decide gates from per-point projections where certain
+    int resp_dst_origin = 0;        // FACET_RESP: the ray starts at the destination point
 };
 
 struct SumArgs {
@@ -97,6 +101,10 @@ struct SumArgs {
 
 // kernels.cu
 void launch_mask(const MaskArgs &a, cudaStream_t s);
+// FACET_RESP finalize: partial sums into P_out and P of the destination
+// cells; with gate_pin, destinations whose P_in is 0 receive nothing
+void launch_finalize_resp(const double2 *partial, int nsplit, int ndst, const int *cell, const double2 *gate_pin,
+                          double2 *Pout, double2 *P, cudaStream_t s);
 // Bounce masks (HOP_F2F, no full export): classification pass, then the pair
 // kernel on the blocks it lists (blist: one entry per block at most; the
 // stream is synchronised once to read their count into *count_host).
