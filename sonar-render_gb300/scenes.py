@@ -17,8 +17,10 @@ as seeded synthetic inputs of the same shapes and sizes:
                         64 arc positions as sources and receivers, 8 frequencies
 
 Mesh helpers mirror the reference's run_scripts/modules/geo.py builders
-(make_rectangle, halve_facets, make_cube, generate_field_points) without
-numpy-stl / trimesh, and ``read_stl`` reads binary STL files.
+(make_rectangle, make_right_angle_triangle, make_cube, create_plate,
+create_plate_triangle, create_reflector, create_trihedral_reflector,
+halve_facets, rotate, translate, join, generate_field_points) without
+numpy-stl / trimesh; ``read_stl`` and ``write_stl`` read and write binary STL.
 """
 from __future__ import annotations
 
@@ -54,12 +56,15 @@ def rectangle(width, height, z=0.0, normal_up=True):
 
 
 def halve_facets(tris):
-    """Split every triangle into four through its edge midpoints (geo.py:158-196)."""
+    """Split every triangle into four through its edge midpoints, in the
+    reference's vertex order (geo.py:158-196): (v1, m12, m31), (m12, v2, m23),
+    (m23, v3, m31), (m12, m23, m31).  The order fixes each facet's frame, so
+    the fragment grids equal the reference's."""
     t = np.asarray(tris, np.float64).reshape(-1, 3, 3)
     a, b, c = t[:, 0], t[:, 1], t[:, 2]
     ab, bc, ca = (a + b) / 2, (b + c) / 2, (c + a) / 2
     out = np.stack([np.stack([a, ab, ca], 1), np.stack([ab, b, bc], 1),
-                    np.stack([ca, bc, c], 1), np.stack([ab, bc, ca], 1)], 1)
+                    np.stack([bc, c, ca], 1), np.stack([ab, bc, ca], 1)], 1)
     return out.reshape(-1, 9).astype(np.float32)
 
 
@@ -134,8 +139,99 @@ def read_stl(path):
 
 
 def translate(tris, offset):
-    t = np.asarray(tris, np.float32).reshape(-1, 3, 3) + np.asarray(offset, np.float32)
-    return t.reshape(-1, 9)
+    """Shift by offset (geo.py:456-472: the sum in FP64, stored as FP32)."""
+    t = np.asarray(tris, np.float32).reshape(-1, 3, 3).astype(np.float64) + np.asarray(offset, np.float64)
+    return t.reshape(-1, 9).astype(np.float32)
+
+
+def write_stl(path, tris, header=b"sonar-render_gb300"):
+    """(n, 9) triangles -> binary STL; each record's normal is
+    unit((v2 - v1) x (v3 - v1)), the normal the library derives itself."""
+    t = np.asarray(tris, np.float32).reshape(-1, 3, 3)
+    n = np.cross((t[:, 1] - t[:, 0]).astype(np.float64), (t[:, 2] - t[:, 0]).astype(np.float64))
+    L = np.linalg.norm(n, axis=1, keepdims=True)
+    n = np.where(L > 0, n / np.where(L > 0, L, 1.0), 0.0).astype("<f4")
+    rec = np.zeros(len(t), dtype=[("n", "<f4", 3), ("v", "<f4", 9), ("attr", "<u2")])
+    rec["n"] = n
+    rec["v"] = t.reshape(-1, 9)
+    with open(path, "wb") as fh:
+        fh.write(header[:80].ljust(80, b"\0"))
+        fh.write(struct.pack("<I", len(t)))
+        fh.write(rec.tobytes())
+
+
+def join(*meshes):
+    """Concatenate triangle arrays (geo.py:244-264 join_meshes)."""
+    return np.concatenate([np.asarray(m, np.float32).reshape(-1, 9) for m in meshes])
+
+
+# Solids built from vertex and face tables: the tables (coordinates, face
+# order and winding) are the reference's (geo.py), so that a scene script
+# produces the same triangles -- and so the same facet frames -- here.
+def _from_table(vertices, faces):
+    v = np.asarray(vertices, np.float64)
+    f = np.asarray(faces, np.int64)
+    return np.concatenate([v[f[:, 0]], v[f[:, 1]], v[f[:, 2]]], axis=1).astype(np.float32)
+
+
+def make_rectangle(length, width, xy_plane=True):
+    """Two-triangle rectangle centred at the origin in the xy-plane (normal
+    +z) or the xz-plane (geo.py:75-113)."""
+    l, w = length / 2.0, width / 2.0
+    if xy_plane:
+        v = [(-l, -w, 0.0), (l, -w, 0.0), (l, w, 0.0), (-l, w, 0.0)]
+    else:
+        v = [(-l, 0.0, -w), (l, 0.0, -w), (l, 0.0, w), (-l, 0.0, w)]
+    return _from_table(v, [(0, 1, 2), (0, 2, 3)])
+
+
+def make_right_angle_triangle(x_length, y_length):
+    """One right triangle in the xy-plane, right angle at the origin (geo.py:115-145)."""
+    return _from_table([(0, 0, 0), (x_length, 0, 0), (0, y_length, 0)], [(0, 1, 2)])
+
+
+def make_cube():
+    """Unit cube [0, 1]^3, 12 triangles (geo.py:198-242)."""
+    v = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    f = [(2, 1, 0), (3, 2, 0), (5, 6, 4), (6, 7, 4), (0, 4, 5), (0, 5, 1),
+         (6, 2, 3), (7, 6, 3), (7, 3, 0), (4, 7, 0), (6, 5, 1), (2, 6, 1)]
+    return _from_table(v, f)
+
+
+def create_plate(length, width, thickness=0.01):
+    """Plate of the given thickness above z = 0, 12 triangles (geo.py:282-310)."""
+    l, w, t = length / 2.0, width / 2.0, thickness
+    v = [(-l, -w, 0), (l, -w, 0), (l, w, 0), (-l, w, 0), (-l, -w, t), (l, -w, t), (l, w, t), (-l, w, t)]
+    f = [(2, 1, 0), (3, 2, 0), (4, 5, 6), (4, 6, 7), (0, 1, 5), (0, 5, 4),
+         (1, 2, 6), (1, 6, 5), (2, 3, 7), (2, 7, 6), (3, 0, 4), (3, 4, 7)]
+    return _from_table(v, f)
+
+
+def create_plate_triangle(length, width, thickness=0.01):
+    """Triangular prism (base length along x, apex at the origin side), 8
+    triangles (geo.py:313-356)."""
+    l, w, t = length / 2.0, width / 2.0, thickness
+    v = [(-l, -w, 0), (l, -w, 0), (0, 0, 0), (-l, -w, t), (l, -w, t), (0, 0, t)]
+    f = [(2, 1, 0), (4, 5, 3), (0, 1, 4), (0, 4, 3), (1, 2, 5), (1, 5, 4), (2, 0, 3), (2, 3, 5)]
+    return _from_table(v, f)
+
+
+def create_reflector(width, thickness):
+    """Four triangular prisms forming a corner reflector (geo.py:359-384)."""
+    side = (2 * ((width / 2) ** 2)) ** 0.5
+    p1 = rotate(create_plate_triangle(side, width, thickness), "x", 45)
+    p2 = rotate(create_plate_triangle(side, width, thickness), "x", -45)
+    p3 = rotate(rotate(create_plate_triangle(side, width, thickness), "y", 90), "z", 45)
+    p4 = rotate(rotate(create_plate_triangle(side, width, thickness), "y", 90), "z", -45)
+    return rotate(join(p1, p2, p3, p4), "x", -90)
+
+
+def create_trihedral_reflector(side_length, thickness):
+    """Three thick square plates meeting at a corner (geo.py:387-411)."""
+    xy = rotate(create_plate(side_length, side_length, thickness), "z", 45)
+    xz = rotate(rotate(create_plate(side_length, side_length, thickness), "z", 45), "y", 90)
+    yz = rotate(rotate(create_plate(side_length, side_length, thickness), "z", 45), "x", 90)
+    return rotate(rotate(join(xy, xz, yz), "z", 45), "x", 45)
 
 
 def rotate(tris, axis, degrees):
