@@ -1953,6 +1953,7 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *bloc
     extern __shared__ float2 aca_smem[];  // sU[RS][kTile], then sV[RS][kTile]
     float2 *sU = aca_smem, *sV = aca_smem + RS * kTile;
     __shared__ float2 sRow[kTile];
+    __shared__ float4 sFrag[4][kTile];  // position and normal of the columns' (I) and rows' (J) fragments
     __shared__ __align__(16) unsigned slotA[kAcaWarps], slotB[kAcaWarps], slotZ[kAcaWarps];
     __shared__ float2 sumB[kAcaWarps];
     const int t = threadIdx.x, b = blockIdx.x;
@@ -1969,6 +1970,12 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *bloc
     const bool coli = t < ni, rowj = t < nj;
     const float4 pi = coli ? __ldg(PI + t) : z4, qi = coli ? __ldg(NI + t) : z4;
     const float4 pj = rowj ? __ldg(PJ + t) : z4, qj = rowj ? __ldg(NJ + t) : z4;
+    // both tiles' fragment data in shared memory: the pivots' data are read from here
+    sFrag[0][t] = pi;
+    sFrag[1][t] = qi;
+    sFrag[2][t] = pj;
+    sFrag[3][t] = qj;
+    __syncthreads();
     bool used = !rowj;  // row t taken (or absent)
     int r = 0, k = 0, zero_rows = 0;
     float norm2 = 0.0f;
@@ -1978,7 +1985,7 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *bloc
         float2 val = z2;
         if (coli) {
             const bool bit = bc == kFlagBits ? ((bw[(long long)(t >> 5) * pitch + r] >> (t & 31)) & 1u) : true;
-            val = lr_entry<ATT>(a, bc, bit, pi, qi, __ldg(PJ + r), __ldg(NJ + r));
+            val = lr_entry<ATT>(a, bc, bit, pi, qi, sFrag[2][r], sFrag[3][r]);
             for (int m = 0; m < ks; ++m) val = csub_mul(val, sU[m * kTile + r], sV[m * kTile + t]);
             for (int m = RS; m < k; ++m) val = csub_mul(val, Ub[m * kTile + r], Vb[m * kTile + t]);
         }
@@ -2007,7 +2014,7 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *bloc
         float2 uu = z2;
         if (rowj) {
             const bool bit = bc == kFlagBits ? ((bw[(long long)(c >> 5) * pitch + t] >> (c & 31)) & 1u) : true;
-            uu = lr_entry<ATT>(a, bc, bit, __ldg(PI + c), __ldg(NI + c), pj, qj);
+            uu = lr_entry<ATT>(a, bc, bit, sFrag[0][c], sFrag[1][c], pj, qj);
             for (int m = 0; m < ks; ++m) uu = csub_mul(uu, sU[m * kTile + t], sV[m * kTile + c]);
             for (int m = RS; m < k; ++m) uu = csub_mul(uu, Ub[m * kTile + t], Vb[m * kTile + c]);
         }
@@ -2043,8 +2050,8 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *bloc
             const int jj = h2 == 0 ? t : (int)(h & 255u), ii = h2 == 0 ? (int)(h & 255u) : t;
             if (ii < ni && jj < nj) {
                 const bool bit = bc == kFlagBits ? ((bw[(long long)(ii >> 5) * pitch + jj] >> (ii & 31)) & 1u) : true;
-                const float2 ex = lr_entry<ATT>(a, bc, bit, h2 == 0 ? __ldg(PI + ii) : pi, h2 == 0 ? __ldg(NI + ii) : qi,
-                                                h2 == 0 ? pj : __ldg(PJ + jj), h2 == 0 ? qj : __ldg(NJ + jj));
+                const float2 ex = lr_entry<ATT>(a, bc, bit, h2 == 0 ? sFrag[0][ii] : pi, h2 == 0 ? sFrag[1][ii] : qi,
+                                                h2 == 0 ? pj : sFrag[2][jj], h2 == 0 ? qj : sFrag[3][jj]);
                 float2 ap = z2;  // minus the approximation
                 for (int m = 0; m < ks; ++m) ap = csub_mul(ap, sU[m * kTile + jj], sV[m * kTile + ii]);
                 for (int m = RS; m < k; ++m) ap = csub_mul(ap, Ub[m * kTile + jj], Vb[m * kTile + ii]);
