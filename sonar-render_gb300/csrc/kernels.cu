@@ -1089,12 +1089,23 @@ __device__ __forceinline__ float convex_reach(float cosv) { return 1e-4f / fmaxf
 // queue is full the thread tests it itself.  Pass 2 (k_batch_vis_hard) walks
 // the BVH for the queued pairs, one thread each, and clears the bits of the
 // shadowed ones: the divergent walks no longer hold warps of easy pairs.
-__device__ __forceinline__ void vis_pair(const BatchVisArgs &a, const BatchItem &it, long long n, int pt,
-                                         const float4 P, bool &gate, bool &hard, float &est)
+// The fragment's data of a pair: its readout centroid, its source-hop
+// centroid and its facet normal.
+struct VisFrag {
+    float4 pos, spos, n;
+};
+
+__device__ __forceinline__ VisFrag vis_frag(const BatchVisArgs &a, long long n)
+{
+    return VisFrag{a.frag_pos[n], a.frag_spos[n], a.frag_n[n]};
+}
+
+__device__ __forceinline__ void vis_pair(const BatchItem &it, const VisFrag &F, int pt, const float4 P, bool &gate,
+                                         bool &hard, float &est)
 {
     const bool readout = pt < kBatchMaxPoints;
-    const float4 f = readout ? a.frag_pos[n] : a.frag_spos[n];
-    const float4 nf = a.frag_n[n];
+    const float4 f = readout ? F.pos : F.spos;
+    const float4 nf = F.n;
     // readout: v = field point - fragment, cos_scat = dot(v, n) / r (OptiX.cu:150-160);
     // source hop: v = fragment - source, cos_inc = dot(-v, n) / r (OptiX.cu:60-79)
     const float sg = readout ? 1.0f : -1.0f;
@@ -1107,11 +1118,11 @@ __device__ __forceinline__ void vis_pair(const BatchVisArgs &a, const BatchItem 
     hard = gate && !(it.convex && est >= kConvexCos);
 }
 
-__device__ __forceinline__ bool vis_shadowed(const BatchVisArgs &a, const BatchItem &it, long long n, int pt,
+__device__ __forceinline__ bool vis_shadowed(const BatchVisArgs &a, const BatchItem &it, const VisFrag &F, int pt,
                                              const float4 P, float est)
 {
     const bool readout = pt < kBatchMaxPoints;
-    const float4 f = readout ? a.frag_pos[n] : a.frag_spos[n];
+    const float4 f = readout ? F.pos : F.spos;
     return occluded_full(a.bvh[it.scene], make_float3(P.x, P.y, P.z), make_float3(f.x, f.y, f.z),
                          it.convex ? convex_reach(est) : 3.0e38f);
 }
@@ -1141,6 +1152,8 @@ __global__ void __launch_bounds__(kTile) k_batch_vis(BatchVisArgs a)
     const long long n = (long long)blockIdx.x * kTile + tid;
     const bool live = n < a.nfrag;
     const BatchItem it = live ? a.items[item_of(a, n)] : BatchItem{};
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const VisFrag F = live ? vis_frag(a, n) : VisFrag{z4, z4, z4};
     unsigned w[4] = {0u, 0u, 0u, 0u};  // receivers 0-31, 32-63, sources 0-31, 32-63
     for (int pt = 0; pt < 2 * kBatchMaxPoints; ++pt) {
         const bool readout = pt < kBatchMaxPoints;
@@ -1148,7 +1161,7 @@ __global__ void __launch_bounds__(kTile) k_batch_vis(BatchVisArgs a)
         const bool active = live && idx < (readout ? a.nrx : a.nsrc);  // uniform over the warp but for live
         bool gate = false, hard = false;
         float est = 0.0f;
-        if (active) vis_pair(a, it, n, pt, sP[pt], gate, hard, est);
+        if (active) vis_pair(it, F, pt, sP[pt], gate, hard, est);
         bool vis = gate;
         // queue the shadow tests of this point, one atomic per warp
         const unsigned need = __ballot_sync(0xffffffffu, hard);
@@ -1159,7 +1172,7 @@ __global__ void __launch_bounds__(kTile) k_batch_vis(BatchVisArgs a)
             if (hard) {
                 const unsigned slot = base + (unsigned)__popc(need & ((1u << lane) - 1u));
                 if (slot < a.hard_cap) a.hard[slot] = (unsigned)(n * (2 * kBatchMaxPoints) + pt);
-                else vis = !vis_shadowed(a, it, n, pt, sP[pt], est);  // queue full: test here
+                else vis = !vis_shadowed(a, it, F, pt, sP[pt], est);  // queue full: test here
             }
         }
         if (vis) w[pt >> 5] |= 1u << (pt & 31);
@@ -1179,8 +1192,9 @@ __global__ void __launch_bounds__(kTile) k_batch_vis_hard(BatchVisArgs a)
         const float4 P = pt < kBatchMaxPoints ? a.rx[pt] : a.src[pt - kBatchMaxPoints];
         bool gate, hard;
         float est;
-        vis_pair(a, it, n, pt, P, gate, hard, est);
-        if (vis_shadowed(a, it, n, pt, P, est))
+        const VisFrag F = vis_frag(a, n);
+        vis_pair(it, F, pt, P, gate, hard, est);
+        if (vis_shadowed(a, it, F, pt, P, est))
             atomicAnd(reinterpret_cast<unsigned *>(a.vis + n) + (pt >> 5), ~(1u << (pt & 31)));
     }
 }
