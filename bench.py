@@ -413,6 +413,7 @@ def batch_leg(args, flush, rank):
            "tensor_tflops_achieved": round(flops / (statistics.median(parts["gemm_ms"]) * 1e-3) / 1e12, 2),
            "green_evaluations_per_run": int(nfrag * (st["receivers"] + st["sources"])),
            "tuning": st["tuning"], "plan_s": round(plan_s, 3), "convex_scenes": st["convex_scenes"],
+           "shadow_tests_per_run": st.get("shadow_tests"),
            "e2e": {"value": pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                    "s_per_step": round(e2e_s, 4)},
            "rel_err_vs_fp64": err, "dtype": "split bf16 x3, fp32 accumulate, fp64 reduce",

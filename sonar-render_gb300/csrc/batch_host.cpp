@@ -591,7 +591,10 @@ std::unique_ptr<Plan> make_plan(const float *tris, const int *tri_off, int nscen
             t.push_back(a);
         }
         p->convex[s] = scene_is_convex(t, 1e-6 * (1.0 + maxv)) ? 1 : 0;
-        BvhHost b = build_bvh(t, 1e-3 * (1.0 + maxc));
+        // node boxes padded by 1e-5 (1 + largest coordinate of triangles and points):
+        // the FP32 slab test and the crossing point of a hit are within a few 1e-7
+        // (1 + coordinate) of exact, so every box a hit needs is opened
+        BvhHost b = build_bvh(t, 1e-5 * (1.0 + maxc));
         node0[s] = (int)nodes.size();
         tri0[s] = (int)(trec.size() / 4);
         nodes.insert(nodes.end(), b.nodes.begin(), b.nodes.end());
@@ -701,15 +704,22 @@ int sonar_batch_stats(long long plan, char *json, int cap)
     return (int)bguard([&]() -> long long {
         const Plan &p = find(plan);
         std::string s;
-        char buf[512];
+        char buf[640];
+        // pairs queued for a shadow test by the last run
+        unsigned hard = 0;
+        if (p.runs > 0) {
+            BCK(cudaStreamSynchronize(p.stream));
+            BCK(cudaMemcpy(&hard, p.d_hard_count, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        }
         snprintf(buf, sizeof(buf),
                  "{\"items\": %d, \"scenes\": %d, \"frequencies\": %d, \"sources\": %d, \"receivers\": %d, "
                  "\"fragments\": %lld, \"cells\": %lld, \"pairs\": %.0f, \"segments\": %d, \"convex_scenes\": %d, "
-                 "\"runs\": %d, \"vis_ms\": %.6f, \"gemm_ms\": %.6f, \"reduce_ms\": %.6f, "
+                 "\"runs\": %d, \"vis_ms\": %.6f, \"gemm_ms\": %.6f, \"reduce_ms\": %.6f, \"shadow_tests\": %u, "
                  "\"tuning\": {\"fragments_per_stage\": %d, \"grid\": %d, \"cached\": %s, \"candidates\": [",
                  p.nitems, p.nscenes, p.nfreq, p.nsrc, p.nrx, p.nfrag, p.ncells, p.pairs, p.nseg,
                  (int)std::count(p.convex.begin(), p.convex.end(), 1),
-                 p.runs, p.vis_ms, p.gemm_ms, p.reduce_ms, p.tune.kc, p.tune.grid, p.tune_cached ? "true" : "false");
+                 p.runs, p.vis_ms, p.gemm_ms, p.reduce_ms, hard, p.tune.kc, p.tune.grid,
+                 p.tune_cached ? "true" : "false");
         s += buf;
         for (size_t i = 0; i < p.tried.size(); i++) {
             snprintf(buf, sizeof(buf), "%s{\"fragments_per_stage\": %d, \"grid\": %d, \"ms\": %.6f}", i ? ", " : "",

@@ -449,7 +449,10 @@ void render()
         }
     for (auto &p : g.src) maxc = std::max({maxc, (double)std::fabs(p.x), (double)std::fabs(p.y), (double)std::fabs(p.z)});
     for (auto &p : g.fp) maxc = std::max({maxc, (double)std::fabs(p.x), (double)std::fabs(p.y), (double)std::fabs(p.z)});
-    BvhHost bvh = build_bvh(tris, 1e-3 * (1.0 + maxc));
+    // node boxes padded by 1e-5 (1 + largest coordinate of triangles and points):
+    // the FP32 slab test and the crossing point of a hit are within a few 1e-7
+    // (1 + coordinate) of exact, so every box a hit needs is opened
+    BvhHost bvh = build_bvh(tris, 1e-5 * (1.0 + maxc));
     g.ntri = (int)tris.size();
     g.nnodes = (int)bvh.nodes.size();
     g.d_nodes = dalloc<float4>(2 * bvh.nodes.size());
