@@ -1154,28 +1154,37 @@ __global__ void __launch_bounds__(kTile) k_batch_vis(BatchVisArgs a)
     const BatchItem it = live ? a.items[item_of(a, n)] : BatchItem{};
     const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const VisFrag F = live ? vis_frag(a, n) : VisFrag{z4, z4, z4};
-    unsigned w[4] = {0u, 0u, 0u, 0u};  // receivers 0-31, 32-63, sources 0-31, 32-63
-    for (int pt = 0; pt < 2 * kBatchMaxPoints; ++pt) {
-        const bool readout = pt < kBatchMaxPoints;
-        const int idx = readout ? pt : pt - kBatchMaxPoints;
-        const bool active = live && idx < (readout ? a.nrx : a.nsrc);  // uniform over the warp but for live
-        bool gate = false, hard = false;
-        float est = 0.0f;
-        if (active) vis_pair(it, F, pt, sP[pt], gate, hard, est);
-        bool vis = gate;
-        // queue the shadow tests of this point, one atomic per warp
-        const unsigned need = __ballot_sync(0xffffffffu, hard);
-        if (need) {
-            unsigned base = 0u;
-            if (lane == 0) base = atomicAdd(a.hard_count, (unsigned)__popc(need));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (hard) {
-                const unsigned slot = base + (unsigned)__popc(need & ((1u << lane) - 1u));
-                if (slot < a.hard_cap) a.hard[slot] = (unsigned)(n * (2 * kBatchMaxPoints) + pt);
-                else vis = !vis_shadowed(a, it, F, pt, sP[pt], est);  // queue full: test here
+    // one word per 32 points: receivers 0-31, 32-63, sources 0-31, 32-63; the
+    // hop (and so the centroid and the sign of the gate) is fixed per word
+    unsigned w[4];
+#pragma unroll
+    for (int seg = 0; seg < 4; ++seg) {
+        const bool readout = seg < 2;
+        const int npts = readout ? a.nrx : a.nsrc;
+        unsigned word = 0u;
+#pragma unroll 2
+        for (int b = 0; b < 32; ++b) {
+            const int pt = seg * 32 + b;
+            const bool active = live && (seg & 1) * 32 + b < npts;  // uniform over the warp but for live
+            bool gate = false, hard = false;
+            float est = 0.0f;
+            if (active) vis_pair(it, F, pt, sP[pt], gate, hard, est);
+            bool vis = gate;
+            // queue the shadow tests of this point, one atomic per warp
+            const unsigned need = __ballot_sync(0xffffffffu, hard);
+            if (need) {
+                unsigned base = 0u;
+                if (lane == 0) base = atomicAdd(a.hard_count, (unsigned)__popc(need));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (hard) {
+                    const unsigned slot = base + (unsigned)__popc(need & ((1u << lane) - 1u));
+                    if (slot < a.hard_cap) a.hard[slot] = (unsigned)(n * (2 * kBatchMaxPoints) + pt);
+                    else vis = !vis_shadowed(a, it, F, pt, sP[pt], est);  // queue full: test here
+                }
             }
+            word |= vis ? (1u << b) : 0u;
         }
-        if (vis) w[pt >> 5] |= 1u << (pt & 31);
+        w[seg] = word;
     }
     if (live) a.vis[n] = make_uint4(w[0], w[1], w[2], w[3]);
 }
