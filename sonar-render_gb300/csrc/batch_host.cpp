@@ -178,29 +178,6 @@ void fragment_item(const float *tris, int ntri, int facet0, float delta, ItemFra
     }
 }
 
-// Every vertex of the scene on or behind every triangle's plane (within tol,
-// in double).  Scenes of more than 20,000 triangles are not checked (treated
-// as non-convex: every pair gets the exact shadow test).
-bool scene_is_convex(const std::vector<std::array<float, 9>> &t, double tol)
-{
-    if (t.size() > 20000) return false;
-    for (const auto &a : t) {
-        const double ux = (double)a[3] - a[0], uy = (double)a[4] - a[1], uz = (double)a[5] - a[2];
-        const double vx = (double)a[6] - a[0], vy = (double)a[7] - a[1], vz = (double)a[8] - a[2];
-        double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
-        const double L = std::sqrt(nx * nx + ny * ny + nz * nz);
-        if (!(L > 0.0)) return false;
-        nx /= L;
-        ny /= L;
-        nz /= L;
-        const double c = nx * a[0] + ny * a[1] + nz * a[2];
-        for (const auto &b : t)
-            for (int k = 0; k < 3; k++)
-                if (nx * b[3 * k] + ny * b[3 * k + 1] + nz * b[3 * k + 2] - c > tol) return false;
-    }
-    return true;
-}
-
 WorkList make_worklist(const Plan &p, int kc, int grid)
 {
     WorkList w;

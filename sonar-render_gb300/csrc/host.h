@@ -43,4 +43,8 @@ struct BvhHost {
 // Median-split BVH over triangles (9 floats each), boxes padded by pad.
 BvhHost build_bvh(const std::vector<std::array<float, 9>> &tris, double pad);
 
+// Every vertex of the scene on or behind every triangle's plane (within tol,
+// in double); scenes of more than 20,000 triangles count as non-convex.
+bool scene_is_convex(const std::vector<std::array<float, 9>> &t, double tol);
+
 }  // namespace sonar

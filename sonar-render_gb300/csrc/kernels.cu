@@ -48,13 +48,13 @@ __device__ __forceinline__ float dot_rn(float ax, float ay, float az, float bx, 
 // ---------------------------------------------------------------- visibility
 // Does the part [tlo, 1] of segment o + t (e - o) touch the box?  (inv =
 // componentwise 1 / (e - o))
-__device__ __forceinline__ bool seg_box(float3 o, float3 inv, float4 a, float4 b, float tlo = 0.0f)
+__device__ __forceinline__ bool seg_box(float3 o, float3 inv, float4 a, float4 b, float tlo = 0.0f, float thi = 1.0f)
 {
     const float tx0 = (a.x - o.x) * inv.x, tx1 = (b.x - o.x) * inv.x;
     const float ty0 = (a.y - o.y) * inv.y, ty1 = (b.y - o.y) * inv.y;
     const float tz0 = (a.z - o.z) * inv.z, tz1 = (b.z - o.z) * inv.z;
     const float t0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tlo));
-    const float t1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), 1.0f));
+    const float t1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), thi));
     return t0 <= t1;
 }
 
@@ -103,10 +103,11 @@ __device__ __forceinline__ bool tri_blocks_v(float4 P, float4 M1, float4 M2, flo
 
 constexpr int kStack = 64;
 
-// tlo: only BVH boxes that the part [tlo, 1] of the segment touches are
-// opened (callers pass tlo > 0 only where no triangle can hold a crossing
-// point before it; the triangle tests themselves are unchanged).
-__device__ bool occluded(const BvhView &B, float3 o, float3 e, float r, float tmax, float tlo = 0.0f)
+// tlo, thi: only BVH boxes that the part [tlo, thi] of the segment touches
+// are opened (callers narrow it only where no triangle can hold a crossing
+// point outside it; the triangle tests themselves are unchanged).
+__device__ bool occluded(const BvhView &B, float3 o, float3 e, float r, float tmax, float tlo = 0.0f,
+                         float thi = 1.0f)
 {
     if (B.ntri == 0) return false;
     const float sc = 1.0f + fmaxf(fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fmaxf(fabsf(o.z), fabsf(e.x))),
@@ -122,7 +123,7 @@ __device__ bool occluded(const BvhView &B, float3 o, float3 e, float r, float tm
     for (int guard = 0; guard < B.nnodes; ++guard) {
         const float4 a = __ldg(B.nodes + 2 * node), b = __ldg(B.nodes + 2 * node + 1);
         bool descend = false;
-        if (seg_box(o, inv, a, b, tlo)) {
+        if (seg_box(o, inv, a, b, tlo, thi)) {
             const int left = __float_as_int(a.w), right = __float_as_int(b.w);
             if (left < 0) {
                 const int t0 = -left - 1;
@@ -262,13 +263,16 @@ __device__ __forceinline__ bool occluded_list(const float4 *sT, int n, float3 o,
     return false;
 }
 
-__device__ __forceinline__ bool occluded_full(const BvhView &B, float3 o, float3 e, float reach = 3.0e38f)
+__device__ __forceinline__ bool occluded_full(const BvhView &B, float3 o, float3 e, float reach = 3.0e38f,
+                                              float near = 3.0e38f)
 {
     const float vx = __fsub_rn(e.x, o.x), vy = __fsub_rn(e.y, o.y), vz = __fsub_rn(e.z, o.z);
     const float r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
-    // reach: only the last `reach` metres of the ray can hold a crossing point
+    // reach: only the last `reach` metres of the ray can hold a crossing
+    // point; near: only the first `near` metres can
     const float tlo = reach < r ? 1.0f - reach / r : 0.0f;
-    return occluded(B, o, e, r, __fsub_rn(r, 1e-3f), tlo);
+    const float thi = near < r ? near / r : 1.0f;
+    return occluded(B, o, e, r, __fsub_rn(r, 1e-3f), tlo, thi);
 }
 
 // ---- block-level occluder culling
@@ -313,6 +317,70 @@ __device__ __forceinline__ bool may_occlude(float o_lo, float o_hi, float e_lo, 
         if (o0 * 0.8e-3f > rmax * e1 * 1.1f + 1e-30f) return false;
     }
     return true;
+}
+
+// Shadow test of one pair when every target triangle lies on or behind every
+// target triangle's plane (a convex target, within tau = 1e-6 (1 + vmax)).
+// A crossing that tri_blocks reports lies inside a triangle, so behind the
+// fragment's facet plane up to E = 2e-6 (1 + vmax + sc) (tau plus the FP32
+// errors of the fragment's position, of the crossing point and of the edge
+// tests, each a few ulp of sc = 1 + the largest coordinate of the ray, with
+// a factor two to spare); a ray point at distance rho from the fragment is
+// rho cos in front of that plane (cos > 0: the pair passed its gate there).
+//  * Rays that leave a target fragment (FACET_NO_RESP): a crossing has
+//    rho <= E / cos, and its triangle's plane is at least 1e-4 sc from the
+//    origin (tri_blocks' exclusion), so rho >= 1e-4 sc: no room, no test;
+//    else only the first 1.1 E / cos metres of the ray are searched.
+//  * Rays that end on a target fragment (source hop onto a target, readout
+//    from a field point): tri_blocks ignores crossings within 1e-3 of the end
+//    (tmax = r - 1e-3), so no test when 0.9e-3 cos > E; else only the last
+//    1.1 E / cos metres.
+// Every triangle that can report a hit is still tested, so the verdict is the
+// full walk's.
+template <int HOP>
+__device__ __forceinline__ bool occluded_pair(const MaskArgs &a, float4 ns, float4 nt, float3 o, float3 e)
+{
+    if (a.convex && (HOP == HOP_NORESP || HOP == HOP_FP || (HOP == HOP_SRC && !a.dst_is_field))) {
+        const float vx = __fsub_rn(e.x, o.x), vy = __fsub_rn(e.y, o.y), vz = __fsub_rn(e.z, o.z);
+        const float rinv = rsqrtf(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+        const float sc = 1.0f + fmaxf(fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fmaxf(fabsf(o.z), fabsf(e.x))),
+                                      fmaxf(fabsf(e.y), fabsf(e.z)));
+        const float E = 2e-6f * (1.0f + a.convex_vmax + sc);
+        if (HOP == HOP_NORESP) {
+            const float cosv = fmaf(vx, ns.x, fmaf(vy, ns.y, vz * ns.z)) * rinv;  // leaving the source fragment
+            if (cosv > 0.0f) {
+                if (E < 0.99e-4f * sc * cosv) return false;
+                return occluded_full(a.bvh, o, e, 3.0e38f, 1.1f * E / cosv);
+            }
+        } else {
+            // arriving at the fragment: the readout's source, the source hop's destination
+            const float4 n = HOP == HOP_FP ? ns : nt;
+            const float cosv = -fmaf(vx, n.x, fmaf(vy, n.y, vz * n.z)) * rinv;
+            if (cosv > 0.0f) {
+                if (cosv * 0.9e-3f > E) return false;
+                return occluded_full(a.bvh, o, e, 1.1f * E / cosv);
+            }
+        }
+    }
+    return occluded_full(a.bvh, o, e);
+}
+
+// false when occluded_pair is sure to answer "not occluded" without a walk
+template <int HOP>
+__device__ __forceinline__ bool convex_needs_test(const MaskArgs &a, float4 ns, float4 nt, float3 o, float3 e)
+{
+    const float vx = __fsub_rn(e.x, o.x), vy = __fsub_rn(e.y, o.y), vz = __fsub_rn(e.z, o.z);
+    const float rinv = rsqrtf(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+    const float sc = 1.0f + fmaxf(fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fmaxf(fabsf(o.z), fabsf(e.x))),
+                                  fmaxf(fabsf(e.y), fabsf(e.z)));
+    const float E = 2e-6f * (1.0f + a.convex_vmax + sc);
+    if (HOP == HOP_NORESP) {
+        const float cosv = fmaf(vx, ns.x, fmaf(vy, ns.y, vz * ns.z)) * rinv;
+        return !(cosv > 0.0f && E < 0.99e-4f * sc * cosv);
+    }
+    const float4 n = HOP == HOP_FP ? ns : nt;
+    const float cosv = -fmaf(vx, n.x, fmaf(vy, n.y, vz * n.z)) * rinv;
+    return !(cosv > 0.0f && cosv * 0.9e-3f > E);
 }
 
 template <int HOP>
@@ -738,7 +806,11 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
     __shared__ float4 sTd[kTile];
     __shared__ int sQn[2];
     const int lane = tid & 31;
-    const bool signs = !clear && !overflow && nkeep > 0;
+    // convex targets: each pair's test is first narrowed by occluded_pair (most
+    // need none), so the candidate-list queue is not used
+    const bool convex_hop = a.convex && (HOP == HOP_NORESP || HOP == HOP_FP || (HOP == HOP_SRC && !a.dst_is_field));
+    const bool signs = !clear && !overflow && nkeep > 0 && !convex_hop;
+    const bool use_queue = signs || (!clear && convex_hop && (overflow || nkeep > 0));
     unsigned tpos = 0u, tneg = 0u;
     if (signs) {
         for (int c = 0; c < nkeep; ++c) {
@@ -753,6 +825,8 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
             tpos |= (dd > 0.0f ? 1u : 0u) << c;
             tneg |= (dd < 0.0f ? 1u : 0u) << c;
         }
+    }
+    if (use_queue) {
         sTd[tid] = make_float4(t.x, t.y, t.z, __int_as_float(ft));
         if (tid < 2) sQn[tid] = 0;
     }
@@ -799,13 +873,36 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
             if (mixed) word = pw;
         }
         if (!clear && (overflow || nkeep > 0)) {
+            uint32_t tq = 0u;  // this lane's pairs of the word to test after the word
             if (signs) {
                 uint32_t cross = 0u;
                 for (int c = 0; c < nkeep; ++c) {
                     if ((tneg >> c) & 1u) cross |= sPos[c][w];
                     if ((tpos >> c) & 1u) cross |= sNeg[c][w];
                 }
-                uint32_t tq = word & cross;
+                tq = word & cross;
+            } else if (convex_hop) {
+                uint32_t c = word;
+                while (c) {
+                    const int b = __ffs(c) - 1;
+                    c &= c - 1u;
+                    const int q = w * 32 + b;
+                    float3 o, e;
+                    pair_ray<HOP>(sP[q], sN[q], t, ft, o, e, a.resp_dst_origin);
+                    if (convex_needs_test<HOP>(a, sN[q], nt, o, e)) tq |= 1u << b;
+                }
+            } else {
+                uint32_t c = word;
+                while (c) {
+                    const int b = __ffs(c) - 1;
+                    c &= c - 1u;
+                    const int q = w * 32 + b;
+                    float3 o, e;
+                    pair_ray<HOP>(sP[q], sN[q], t, ft, o, e, a.resp_dst_origin);
+                    if (occluded_full(a.bvh, o, e)) word &= ~(1u << b);
+                }
+            }
+            if (use_queue) {
                 // warp-aggregated slots for this lane's pairs to test
                 const int cnt = __popc(tq);
                 int incl = cnt;
@@ -822,20 +919,10 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
                     tq &= tq - 1u;
                     sQ[base++] = (unsigned short)(((w * 32 + b) << 8) | tid);
                 }
-            } else {
-                uint32_t tq = word;
-                while (tq) {
-                    const int b = __ffs(tq) - 1;
-                    tq &= tq - 1u;
-                    const int q = w * 32 + b;
-                    float3 o, e;
-                    pair_ray<HOP>(sP[q], sN[q], t, ft, o, e, a.resp_dst_origin);
-                    if (occluded_full(a.bvh, o, e)) word &= ~(1u << b);
-                }
             }
         }
         sW[w][tid] = word;
-        if (signs) {
+        if (use_queue) {
             if (tid == 0) sQn[(w + 1) & 1] = 0;  // last read before the previous word's second barrier
             __syncthreads();
             const int nq = sQn[w & 1];
@@ -843,9 +930,17 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
                 const unsigned code = sQ[e];
                 const int q = (int)(code >> 8), jl = (int)(code & 255u);
                 const float4 td = sTd[jl];
+                const int fd = __float_as_int(td.w);
                 float3 o, en;
-                pair_ray<HOP>(sP[q], sN[q], td, __float_as_int(td.w), o, en, a.resp_dst_origin);
-                if (occluded_list(sTri, nkeep, o, en)) atomicAnd(&sW[w][jl], ~(1u << (q & 31)));
+                pair_ray<HOP>(sP[q], sN[q], td, fd, o, en, a.resp_dst_origin);
+                bool occ;
+                if (signs) {
+                    occ = occluded_list(sTri, nkeep, o, en);
+                } else {
+                    const float4 ntd = (a.dst_facet && fd >= 0) ? a.dst_facet_n[fd] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    occ = occluded_pair<HOP>(a, sN[q], ntd, o, en);
+                }
+                if (occ) atomicAnd(&sW[w][jl], ~(1u << (q & 31)));
             }
             __syncthreads();
         }

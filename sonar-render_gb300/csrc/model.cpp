@@ -266,6 +266,9 @@ struct Model {
     int opt_mask_classify = 1;  // bounce masks: warp-per-block classification, pair kernel on the listed blocks
     int opt_gate_proj = 1;      // bounce masks: gates decided from per-point projections where certain
     int opt_cross_objects = 0;  // bounces also between different targets (FACET_RESP); 0: the reference's behaviour
+    int opt_convex_masks = 1;   // convex targets: shadow tests search only where a crossing is possible
+    int scene_convex = 0;       // every target vertex on or behind every target triangle's plane
+    float scene_vmax = 0.0f;    // largest |coordinate| of the target vertices
     Compression cmp;
     std::vector<HopRecord> log;
     long long launches = 0, h2d_bytes = 0, d2h_bytes = 0;
@@ -447,6 +450,11 @@ void render()
             for (float v : t) maxc = std::max(maxc, (double)std::fabs(v));
             tris.push_back(t);
         }
+    // convex target (every target vertex on or behind every target triangle's
+    // plane): the masks' shadow tests then search only the part of a ray
+    // where a crossing is possible
+    g.scene_vmax = (float)maxc;
+    g.scene_convex = scene_is_convex(tris, 1e-6 * (1.0 + maxc)) ? 1 : 0;
     for (auto &p : g.src) maxc = std::max({maxc, (double)std::fabs(p.x), (double)std::fabs(p.y), (double)std::fabs(p.z)});
     for (auto &p : g.fp) maxc = std::max({maxc, (double)std::fabs(p.x), (double)std::fabs(p.y), (double)std::fabs(p.z)});
     // node boxes padded by 1e-5 (1 + largest coordinate of triangles and points):
@@ -497,6 +505,8 @@ HopSets hop_sets(int hop, int a, int b)
     MaskArgs &m = h.m;
     m.hop = hop;
     m.bvh = BvhView{g.d_nodes, g.d_tris, g.nnodes, g.ntri};
+    m.convex = g.opt_convex_masks ? g.scene_convex : 0;
+    m.convex_vmax = g.scene_vmax;
     if (hop == HOP_SRC) {
         Object &B = get(a, b);  // a = object type (target or field), b = index
         m.nsrc = (int)g.src.size();
@@ -1512,6 +1522,11 @@ int sonar_set_option(const char *key, double value)
     if (!strcmp(key, "compress_select")) {
         g.opt_cmp_select = std::max(0, std::min(2, (int)value));
         g.cmp.release();
+        return 0;
+    }
+    if (!strcmp(key, "convex_masks")) {
+        g.opt_convex_masks = value != 0.0 ? 1 : 0;
+        for (auto &m : g.masks) m.stale = true;
         return 0;
     }
     if (!strcmp(key, "cross_objects")) {

@@ -77,6 +77,8 @@ struct MaskArgs {
     const int *blist_count = nullptr;
     int gate_proj = 1;              // FACET_SELF: decide gates from per-point projections where certain
     int resp_dst_origin = 0;        // FACET_RESP: the ray starts at the destination point
+    int convex = 0;                 // every target vertex on or behind every target triangle's plane
+    float convex_vmax = 0.0f;       // largest |coordinate| of the target vertices
 };
 
 struct SumArgs {

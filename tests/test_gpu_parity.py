@@ -302,3 +302,29 @@ def test_bounce_mask_classification_pass_identical(api, oracle_mod, scenes, extr
     print(extra, "bounce mask vs oracle: pairs %d interacting %d grazing %d mismatches %d"
           % (gm.size, int(gm.sum()), int(graze.sum()), int(diff.sum())))
     assert diff.sum() == 0
+
+
+def test_convex_target_masks_identical(api, scenes):
+    """A convex target (icosphere): the masks' shadow tests search only the
+    part of each ray where a crossing is possible; the masks of the source
+    hop, the readout to field points and the target -> field-object hop are
+    bit-identical to those of the full BVH walk."""
+    sph = scenes.icosphere(3, 0.5)
+    plane = scenes.rotate(scenes.rectangle(2.0, 2.0, z=0.0), "y", 90.0)  # x = 0 plane through the centre
+    fp = np.concatenate([scenes.grid_xy(12, 1.5, 1.2), scenes.grid_xy(12, 1.5, -1.2)])
+    f = 6e3
+    sc = dict(cp=1480.0, f=f, att=0.0, bounces=0, field_objects=True,
+              sources=np.array([[0.2, 0.1, 5.0]], np.float32), field_points=fp,
+              targets=[(sph, scenes.delta_for(f))], fields=[(plane, 2.0 / 96)])
+    load_scene(api, sc)
+    masks = {}
+    for cv in (1, 0):
+        api.set_option("convex_masks", cv)
+        masks[cv] = [api.get_mask(0, 0, 0), api.get_mask(1, 0, 0), api.get_mask(3, 0, 0)]
+    api.set_option("convex_masks", 1)
+    st = api.stats()
+    api.TearDownCuda()
+    for k, (m1, m0) in enumerate(zip(masks[1], masks[0])):
+        print("hop %d: pairs %d interacting %d" % ((0, 1, 3)[k], m1.size, int(m1.sum())))
+        assert m1.sum() > 0
+        assert np.array_equal(m1, m0)
