@@ -286,6 +286,19 @@ __device__ __forceinline__ int f2o(float f)
 }
 __device__ __forceinline__ float o2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
 
+__device__ __forceinline__ float warp_min(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
 __device__ __forceinline__ float plane_dist(const float4 P, float x, float y, float z)
 {
     // the same expression as tri_blocks, so verdicts derived from it agree
@@ -779,6 +792,80 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
             }
         }
     }
+    // Hops whose only gate is the source fragment's (readout, target -> field
+    // object): per source s the range of dot(t - s, n_s) over the
+    // destination box (exact ranges of an affine function) bounds every
+    // pair's gate value, whatever the facets of the tile.  No pair passes when
+    // the largest upper bound is below -thr; every pair passes when the
+    // smallest lower bound clears thr (the margins of the ALL test).  With a
+    // convex target and every pair passing by a wide margin, no pair can be
+    // occluded either (occluded_pair's bounds, with the block's largest
+    // coordinate and cos >= the smallest bound / rmax): the block is ALL.
+    if (HOP == HOP_NORESP || HOP == HOP_FP) {
+        __shared__ int sGB[2];
+        const float dl[3] = {o2f(sBox[12]), o2f(sBox[13]), o2f(sBox[14])};
+        const float dh[3] = {o2f(sBox[15]), o2f(sBox[16]), o2f(sBox[17])};
+        float lo = 3.0e38f, hi = -3.0e38f;
+        if (src_ok) {
+            const float nv[3] = {n.x, n.y, n.z};
+            float bmin = 0.0f, bmax = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                bmin += fminf(nv[k] * dl[k], nv[k] * dh[k]);
+                bmax += fmaxf(nv[k] * dl[k], nv[k] * dh[k]);
+            }
+            const float sp = fmaf(p.x, n.x, fmaf(p.y, n.y, p.z * n.z));
+            lo = bmin - sp;
+            hi = bmax - sp;
+        }
+        lo = warp_min(lo);
+        hi = warp_max(hi);
+        __syncthreads();  // sGB is free
+        if (tid == 0) {
+            sGB[0] = f2o(3.0e38f);
+            sGB[1] = f2o(-3.0e38f);
+        }
+        __syncthreads();
+        if ((tid & 31) == 0) {
+            atomicMin(&sGB[0], f2o(lo));
+            atomicMax(&sGB[1], f2o(hi));
+        }
+        __syncthreads();
+        const float LO = o2f(sGB[0]), HI = o2f(sGB[1]);
+        const float dx = o2f(sBox[3]) - o2f(sBox[0]), dy = o2f(sBox[4]) - o2f(sBox[1]),
+                    dz = o2f(sBox[5]) - o2f(sBox[2]);
+        const float rmax = sqrtf(dx * dx + dy * dy + dz * dz) * 1.0001f;
+        float S = 1.0f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) S = fmaxf(S, 1.0f + fabsf(o2f(sBox[k])));
+        const float thr = rmax * 1e-5f + S * 1e-6f;
+        const int ntile = min(kTile, a.nsrc - i0);
+        const int nw = (ntile + 31) >> 5;
+        if (HI < -thr) {
+            // no pair passes its gate
+            if (tid == 0) a.mask.flags[fidx] = kFlagNone;
+            if (a.full && live)
+                for (int w = 0; w < nw; ++w) a.mask.bits[(long long)(tile * kWordsPerTile + w) * a.mask.pitch + j] = 0u;
+            return;
+        }
+        if (LO > thr) {
+            gates_all = true;
+            const float E = 2e-6f * (1.0f + a.convex_vmax + S);
+            const float cmin = LO / rmax;
+            const bool no_occ = clear || (a.convex && (HOP == HOP_NORESP ? E < 0.99e-4f * 0.999f * cmin
+                                                                          : cmin * 0.9e-3f * 0.999f > E));
+            if (no_occ) {
+                if (tid == 0) a.mask.flags[fidx] = kFlagAll;
+                if (a.full && live)
+                    for (int w = 0; w < nw; ++w) {
+                        const int bmax = min(32, ntile - w * 32);
+                        a.mask.bits[(long long)(tile * kWordsPerTile + w) * a.mask.pitch + j] =
+                            bmax == 32 ? 0xffffffffu : ((1u << bmax) - 1u);
+                    }
+                return;
+            }
+        }
+    }
     if (clear && !a.full) {
         if (tid == 0) a.mask.flags[fidx] = gates_all ? kFlagAll : kFlagClear;
         return;
@@ -972,18 +1059,6 @@ struct WarpRange {
     float lo, hi;
 };
 
-__device__ __forceinline__ float warp_min(float v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ float warp_max(float v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
 
 __global__ void __launch_bounds__(32 * kClsWarps) k_mask_classify_f2f(MaskArgs a, int2 *blist, int *count)
 {
