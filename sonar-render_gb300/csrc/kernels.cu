@@ -1610,12 +1610,6 @@ __device__ __forceinline__ void sym_pair(const SumArgs &a, const float4 A, const
     }
 }
 
-__device__ __forceinline__ float warp_sum(float v)
-{
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
-}
 
 // minimum distance between two axis-aligned boxes
 __device__ __forceinline__ float box_gap(const float *lo1, const float *hi1, const float *lo2, const float *hi2)
@@ -2041,24 +2035,7 @@ __device__ __forceinline__ float2 lr_entry(const SumArgs &a, int cls, bool bit, 
     return ok ? make_float2(Tr, Ti) : make_float2(0.0f, 0.0f);
 }
 
-__device__ __forceinline__ float2 cmul(float2 x, float2 y)
-{
-    return make_float2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
-}
 
-// warp-wide argmax of v (ties: lowest index)
-__device__ __forceinline__ void warp_argmax(float &v, int &idx)
-{
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, v, off);
-        const int oi = __shfl_xor_sync(0xffffffffu, idx, off);
-        if (ov > v || (ov == v && oi < idx)) {
-            v = ov;
-            idx = oi;
-        }
-    }
-}
 
 constexpr int kAcaMaxZeroRows = 48;
 constexpr int kAcaWarps = kTile / 32;
