@@ -73,6 +73,9 @@ def workload(name):
         cfg = scenes.trihedral_config(40e3, bounces=2, n_theta=0, n_phi=0)
     elif name == "sphere":
         cfg = scenes.sphere_config(512, field_surface=True)
+    elif name == "sphere10":
+        # the same scene at 10 kHz (a quarter of the fragments): profiler captures
+        cfg = scenes.sphere_config(512, field_surface=True, frequency=10e3)
     elif name == "plate":
         cfg = scenes.plate_config()
     else:

@@ -801,8 +801,42 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
     // convex target and every pair passing by a wide margin, no pair can be
     // occluded either (occluded_pair's bounds, with the block's largest
     // coordinate and cos >= the smallest bound / rmax): the block is ALL.
+    // Facet runs of each source word (word w = warp w's sources, in facet
+    // order): per run its facet normal, the range of s.n over its sources and
+    // their bits.  A destination t then bounds the gate values n.(t - s) of
+    // a whole run with one dot product.  Words of more than kRuns runs are
+    // evaluated pair by pair.
+    constexpr int kRuns = 8;
+    __shared__ float4 sRunN[kWordsPerTile][kRuns];  // normal, (unused)
+    __shared__ float2 sRunB[kWordsPerTile][kRuns];  // min, max of s.n
+    __shared__ uint32_t sRunM[kWordsPerTile][kRuns];
+    __shared__ int sRunC[kWordsPerTile];
+    float sg_thr = 0.0f, sg_rmax = 1.0f, sg_E = 0.0f;
     if (HOP == HOP_NORESP || HOP == HOP_FP) {
         __shared__ int sGB[2];
+        {
+            const int lane_ = tid & 31, wq = tid >> 5;
+            const int fac = src_ok ? __float_as_int(n.w) : -1;
+            const int prev = __shfl_up_sync(0xffffffffu, fac, 1);
+            const bool start = src_ok && (lane_ == 0 || prev != fac);
+            const unsigned starts = __ballot_sync(0xffffffffu, start);
+            const int nruns = __popc(starts);
+            const int myrun = src_ok ? __popc(starts & ((2u << lane_) - 1u)) - 1 : -1;
+            const float b = fmaf(p.x, n.x, fmaf(p.y, n.y, p.z * n.z));
+            if (nruns <= kRuns) {
+                for (int r = 0; r < nruns; ++r) {
+                    const bool in = myrun == r;
+                    const unsigned m = __ballot_sync(0xffffffffu, in);
+                    const float bl = warp_min(in ? b : 3.0e38f), bh = warp_max(in ? b : -3.0e38f);
+                    if (lane_ == __ffs(m) - 1) {
+                        sRunN[wq][r] = make_float4(n.x, n.y, n.z, 0.0f);
+                        sRunB[wq][r] = make_float2(bl, bh);
+                        sRunM[wq][r] = m;
+                    }
+                }
+            }
+            if (lane_ == 0) sRunC[wq] = nruns <= kRuns ? nruns : -1;
+        }
         const float dl[3] = {o2f(sBox[12]), o2f(sBox[13]), o2f(sBox[14])};
         const float dh[3] = {o2f(sBox[15]), o2f(sBox[16]), o2f(sBox[17])};
         float lo = 3.0e38f, hi = -3.0e38f;
@@ -839,6 +873,9 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
 #pragma unroll
         for (int k = 0; k < 6; ++k) S = fmaxf(S, 1.0f + fabsf(o2f(sBox[k])));
         const float thr = rmax * 1e-5f + S * 1e-6f;
+        sg_thr = thr;
+        sg_rmax = rmax;
+        sg_E = 2e-6f * (1.0f + a.convex_vmax + S);
         const int ntile = min(kTile, a.nsrc - i0);
         const int nw = (ntile + 31) >> 5;
         if (HI < -thr) {
@@ -925,6 +962,36 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
         const uint32_t valid = live ? (bmax == 32 ? 0xffffffffu : ((1u << bmax) - 1u)) : 0u;
         uint32_t word = valid;
         bool mixed = !gates_all && live;
+        uint32_t todo = valid;    // pairs whose gates are evaluated one by one
+        uint32_t no_walk = 0u;    // pairs that pass by a margin that rules out a crossing
+        if ((HOP == HOP_NORESP || HOP == HOP_FP) && mixed) {
+            const int nr = sRunC[w];
+            if (nr >= 0) {
+                // per run: n.t - max(s.n) <= n.(t - s) <= n.t - min(s.n) (thr for rounding)
+                uint32_t pass = 0u;
+                todo = 0u;
+                for (int r = 0; r < nr; ++r) {
+                    const float4 rn = sRunN[w][r];
+                    const float2 rb = sRunB[w][r];
+                    const uint32_t rm = sRunM[w][r];
+                    const float vt = fmaf(rn.x, t.x, fmaf(rn.y, t.y, rn.z * t.z));
+                    const float lower = vt - rb.y, upper = vt - rb.x;
+                    if (upper < -sg_thr) continue;
+                    if (lower > sg_thr) {
+                        pass |= rm;
+                        const float cmin = lower / sg_rmax;
+                        if (a.convex && (HOP == HOP_NORESP ? sg_E < 0.99e-4f * 0.999f * cmin
+                                                           : cmin * 0.9e-3f * 0.999f > sg_E))
+                            no_walk |= rm;
+                    } else {
+                        todo |= rm;
+                    }
+                }
+                word = pass & valid;
+                todo &= valid;
+                mixed = todo != 0u;
+            }
+        }
         if (mixed && proj) {
             const float4 wp = sWP[w];
             const bool all_ok = (t_s - wp.y > proj_hi) && (wp.z - t_d > proj_hi);
@@ -939,7 +1006,7 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
 #pragma unroll 4
             for (int b = 0; b < 32; ++b) {
                 const int q = w * 32 + b;
-                const bool act = mixed && b < bmax;
+                const bool act = mixed && ((todo >> b) & 1u);
                 bool pass = act, unsure = act;
                 if (proj) {
                     // gate 1: cos(v, n_s) from D1 = (t - p).n_s; gate 2:
@@ -957,7 +1024,7 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
                 }
                 pw |= pass ? (1u << b) : 0u;
             }
-            if (mixed) word = pw;
+            if (mixed) word = (word & ~todo) | (pw & todo);
         }
         if (!clear && (overflow || nkeep > 0)) {
             uint32_t tq = 0u;  // this lane's pairs of the word to test after the word
@@ -969,7 +1036,7 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
                 }
                 tq = word & cross;
             } else if (convex_hop) {
-                uint32_t c = word;
+                uint32_t c = word & ~no_walk;
                 while (c) {
                     const int b = __ffs(c) - 1;
                     c &= c - 1u;

@@ -284,16 +284,16 @@ def plate_config():
                 field_points=grid_xy(64, 1.0, 3.0), bounces=0)
 
 
-def sphere_config(field_points_side=512, field_surface=True):
+def sphere_config(field_points_side=512, field_surface=True, frequency=20e3):
     """Icosphere (r = 1 m, 5,120 triangles), 20 kHz, source at 10 m on +z;
     readout onto the 4 x 4 m field plane x = 0 through the centre."""
-    f = 20e3
+    f = float(frequency)
     plane = np.array([[0, -2, -2, 0, 2, -2, 0, 2, 2], [0, -2, -2, 0, 2, 2, 0, -2, 2]], np.float32)
     fields = [(plane, 4.0 / field_points_side)] if field_surface else []
     g = np.linspace(-2, 2, field_points_side)
     Y, Z = np.meshgrid(g, g)
     fp = np.stack([np.zeros(Y.size), Y.ravel(), Z.ravel()], 1).astype(np.float32)
-    return dict(name="icosphere_r1m_20kHz", frequency=f, cp=CP_WATER, attenuation=0.0,
+    return dict(name="icosphere_r1m_%dkHz" % int(f / 1e3), frequency=f, cp=CP_WATER, attenuation=0.0,
                 targets=[(icosphere(4, 1.0), delta_for(f))], fields=fields,
                 sources=np.array([[0.0, 0.0, 10.0]], np.float32),
                 field_points=None if field_surface else fp, bounces=0)
