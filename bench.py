@@ -225,13 +225,20 @@ def time_path(api, cfg, args, flush, local, world, reuse=False):
     return times, api.stats(), clk
 
 
-def max_over_ranks(ms, world):
+def max_over_ranks(ms, world, device="cuda"):
+    """The slowest rank's time (replicas: the job ends with its last rank)."""
     import torch
     import torch.distributed as dist
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_value(pairs_step, steps, world, total_ms):
+    """Whole-job pairs/s: every rank runs the same workload (weak scaling),
+    over the slowest rank's time."""
+    return pairs_step * steps * world / (total_ms * 1e-3)
 
 
 def kernel_times(stats, steps):
@@ -547,7 +554,7 @@ def run_gb300(args):
         total_ms = max_over_ranks(float(sum(times)), world)
         pairs_step = step_pairs(stats) / max(args.steps, 1)
         res[m] = {"times": times, "stats": stats, "clocks": clk, "ms_per_step": total_ms / args.steps,
-                  "value": pairs_step * args.steps * world / (total_ms * 1e-3), "pairs_step": pairs_step,
+                  "value": job_value(pairs_step, args.steps, world, total_ms), "pairs_step": pairs_step,
                   "kernels_ms_per_step": {k: round(v, 4) for k, v in kernel_times(stats, args.steps).items()},
                   "launches_per_step": stats["launches"] / max(args.steps, 1)}
     # the same steps with the masks and compressed blocks of the static target
@@ -559,7 +566,7 @@ def run_gb300(args):
         times, stats, _ = time_path(api, cfg, args, flush, local, world, reuse=True)
         total_ms = max_over_ranks(float(sum(times)), world)
         pairs_step = step_pairs(stats) / max(args.steps, 1)
-        reuse[m] = {"value": pairs_step * args.steps * world / (total_ms * 1e-3), "ms_per_step": total_ms / args.steps,
+        reuse[m] = {"value": job_value(pairs_step, args.steps, world, total_ms), "ms_per_step": total_ms / args.steps,
                     "kernel_ms_per_step": {k: round(v, 4) for k, v in kernel_times(stats, args.steps).items()}}
     batch_res = batch_leg(args, flush, rank) if args.batch else None
     f2f_plain = [h for h in res.get("plain", res[modes[0]])["stats"]["hops"] if h["hop"] == 2]
