@@ -352,6 +352,7 @@ def e2e_path(api, cfg, args, world, pairs_step):
     h2d = d2h = 0
     npts = 0 if cfg.get("field_points") is None else len(cfg["field_points"])
     for k in range(max(1, min(args.steps, 3)) + 1):
+        api.set_option("reset_stats", 1)  # the transfer counters of this step only
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         load_scene(api, cfg)

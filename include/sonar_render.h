@@ -147,6 +147,13 @@ int sonar_get_stats(char *json, int cap);
  * forward into the higher-index object, reciprocal into the lower, all
  * from the bounce's inputs).
  * "aca_variant" (cross-approximation kernel shape, 0-2; bit-identical).
+ * Device memory: every buffer comes from a stream-ordered pool kept for the
+ * process; "memory_cache_mb" (32768, default: unused pool memory kept at a
+ * synchronisation point, in MiB; 0 gives it all back there; negative: -6),
+ * "release_memory" (wait for the device and give the pool's unused memory
+ * back now).  The statistics report "pool_reserved_bytes" (memory the pool
+ * has mapped) and "render_host_ms" (host time of the last render_cuda:
+ * setup, fragments, uploads, occluders, points).
  * Low-rank bounce blocks (no counterpart in the reference, which evaluates
  * every pair): "compress" (0/1), "compress_tol" (cross-approximation stopping
  * tolerance, 1e-4), "compress_judge" (largest accepted relative RMS error of

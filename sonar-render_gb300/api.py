@@ -204,12 +204,12 @@ def object_cells(object_type, idx=0):
 def get_object_pressures(object_type, idx=0):
     """Total pressure of every cell (facet-major, row-major y*nx + x) as complex128."""
     n = object_cells(object_type, idx)
-    out = np.zeros((max(n, 0), 2), dtype=np.double)
+    out = np.empty(max(n, 0), dtype=np.complex128)  # (re, im) double pairs, written in place
     r = lib().sonar_get_object_pressures(int(object_type), int(idx), out.ctypes.data_as(_d), n)
     _check()
     if r < 0:
         raise SonarError("sonar_get_object_pressures failed (%d)" % r)
-    return out[:, 0] + 1j * out[:, 1]
+    return out
 
 
 def get_surface_colours(object_type, idx=0):

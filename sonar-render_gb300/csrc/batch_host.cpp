@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/sonar_render.h"
+#include "devpool.h"
 #include "host.h"
 
 namespace sonar {
@@ -63,18 +64,20 @@ struct BatchError : std::runtime_error {
         if (e_ != cudaSuccess) bfail(-10, "%s failed: %s", #call, cudaGetErrorString(e_));         \
     } while (0)
 
+// A plan's buffers come from the stream-ordered pool, ordered on the plan's
+// stream.
 template <class T>
-T *balloc(size_t n)
+T *balloc(cudaStream_t s, size_t n)
 {
     void *p = nullptr;
-    BCK(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
+    BCK(pool_alloc(&p, std::max<size_t>(n, 1) * sizeof(T), s));
     return (T *)p;
 }
 
 template <class T>
-void bfree(T *&p)
+void bfree(cudaStream_t s, T *&p)
 {
-    if (p) cudaFree(p);
+    pool_free(p, s);
     p = nullptr;
 }
 
@@ -133,10 +136,12 @@ struct Plan {
     {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
-        bfree(d_pos); bfree(d_spos); bfree(d_nrm); bfree(d_facet_n); bfree(d_facet); bfree(d_src); bfree(d_rx);
-        bfree(d_nodes); bfree(d_tris); bfree(d_bvh); bfree(d_vis); bfree(d_hard); bfree(d_hard_count); bfree(d_items);
-        bfree(d_segs); bfree(d_cta_seg); bfree(d_item_seg_off); bfree(d_item_segs); bfree(d_status);
-        bfree(d_partial); bfree(d_out);
+        bfree(stream, d_pos); bfree(stream, d_spos); bfree(stream, d_nrm); bfree(stream, d_facet_n);
+        bfree(stream, d_facet); bfree(stream, d_src); bfree(stream, d_rx); bfree(stream, d_nodes);
+        bfree(stream, d_tris); bfree(stream, d_bvh); bfree(stream, d_vis); bfree(stream, d_hard);
+        bfree(stream, d_hard_count); bfree(stream, d_items); bfree(stream, d_segs); bfree(stream, d_cta_seg);
+        bfree(stream, d_item_seg_off); bfree(stream, d_item_segs); bfree(stream, d_status);
+        bfree(stream, d_partial); bfree(stream, d_out);
         for (cudaEvent_t &e : ev)
             if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
@@ -211,26 +216,25 @@ void upload_worklist(Plan &p, const WorkList &w, int grid)
 {
     const size_t nseg = w.segs.size();
     if (nseg > p.segs_cap) {
-        bfree(p.d_segs);
-        bfree(p.d_item_segs);
-        bfree(p.d_partial);
-        p.d_segs = balloc<int4>(nseg);
-        p.d_item_segs = balloc<int>(nseg);
-        p.d_partial = balloc<float>(nseg * 128 * 64);
+        bfree(p.stream, p.d_segs);
+        bfree(p.stream, p.d_item_segs);
+        bfree(p.stream, p.d_partial);
+        p.d_segs = balloc<int4>(p.stream, nseg);
+        p.d_item_segs = balloc<int>(p.stream, nseg);
+        p.d_partial = balloc<float>(p.stream, nseg * 128 * 64);
         p.segs_cap = nseg;
     }
     if ((size_t)grid + 1 > p.cta_cap) {
-        bfree(p.d_cta_seg);
-        p.d_cta_seg = balloc<int>((size_t)grid + 1);
+        bfree(p.stream, p.d_cta_seg);
+        p.d_cta_seg = balloc<int>(p.stream, (size_t)grid + 1);
         p.cta_cap = (size_t)grid + 1;
     }
     std::vector<int> ids(nseg);
     for (size_t i = 0; i < nseg; i++) ids[i] = (int)i;
-    BCK(cudaMemcpyAsync(p.d_segs, w.segs.data(), nseg * sizeof(int4), cudaMemcpyHostToDevice, p.stream));
-    BCK(cudaMemcpyAsync(p.d_item_segs, ids.data(), nseg * sizeof(int), cudaMemcpyHostToDevice, p.stream));
-    BCK(cudaMemcpyAsync(p.d_cta_seg, w.cta_seg.data(), (grid + 1) * sizeof(int), cudaMemcpyHostToDevice, p.stream));
-    BCK(cudaMemcpyAsync(p.d_item_seg_off, w.item_seg_off.data(), (p.nitems + 1) * sizeof(int),
-                        cudaMemcpyHostToDevice, p.stream));
+    BCK(stage_to_device(p.d_segs, w.segs.data(), nseg * sizeof(int4), p.stream));
+    BCK(stage_to_device(p.d_item_segs, ids.data(), nseg * sizeof(int), p.stream));
+    BCK(stage_to_device(p.d_cta_seg, w.cta_seg.data(), (grid + 1) * sizeof(int), p.stream));
+    BCK(stage_to_device(p.d_item_seg_off, w.item_seg_off.data(), (p.nitems + 1) * sizeof(int), p.stream));
     BCK(cudaStreamSynchronize(p.stream));
     p.nseg = (int)nseg;
 }
@@ -511,39 +515,39 @@ std::unique_ptr<Plan> make_plan(const float *tris, const int *tri_off, int nscen
     std::vector<float4> s4(nsrc), r4(nrx);
     for (int i = 0; i < nsrc; i++) s4[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.0f);
     for (int i = 0; i < nrx; i++) r4[i] = make_float4(rx[3 * i], rx[3 * i + 1], rx[3 * i + 2], 0.0f);
-    p->d_pos = balloc<float4>(frag0);
-    p->d_spos = balloc<float4>(frag0);
-    p->d_nrm = balloc<float4>(frag0);
-    p->d_facet = balloc<int>(frag0);
-    p->d_facet_n = balloc<float4>(ntri);
-    p->d_src = balloc<float4>(nsrc);
-    p->d_rx = balloc<float4>(nrx);
-    p->d_vis = balloc<uint4>(frag0);
+    p->d_pos = balloc<float4>(p->stream, frag0);
+    p->d_spos = balloc<float4>(p->stream, frag0);
+    p->d_nrm = balloc<float4>(p->stream, frag0);
+    p->d_facet = balloc<int>(p->stream, frag0);
+    p->d_facet_n = balloc<float4>(p->stream, ntri);
+    p->d_src = balloc<float4>(p->stream, nsrc);
+    p->d_rx = balloc<float4>(p->stream, nrx);
+    p->d_vis = balloc<uint4>(p->stream, frag0);
     // shadow-test queue: pair ids 128 n + point fit 32 bits below 2^25 fragments (else every
     // pair is tested where it is found); up to 1/16 of all pairs or 32 M entries
     p->hard_cap = frag0 < (1LL << 25) ? (unsigned)std::min<long long>(1LL << 25, std::max<long long>(frag0 * 8, 1024))
                                       : 0u;
-    p->d_hard = balloc<unsigned>(std::max<unsigned>(p->hard_cap, 1u));
-    p->d_hard_count = balloc<unsigned>(1);
+    p->d_hard = balloc<unsigned>(p->stream, std::max<unsigned>(p->hard_cap, 1u));
+    p->d_hard_count = balloc<unsigned>(p->stream, 1);
     {
         int dev = 0;
         BCK(cudaGetDevice(&dev));
         BCK(cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev));
     }
-    p->d_items = balloc<BatchItem>(p->nitems);
-    p->d_item_seg_off = balloc<int>(p->nitems + 1);
-    p->d_status = balloc<int>(1);
-    p->d_out = balloc<double2>((size_t)p->nitems * nrx * nsrc);
+    p->d_items = balloc<BatchItem>(p->stream, p->nitems);
+    p->d_item_seg_off = balloc<int>(p->stream, p->nitems + 1);
+    p->d_status = balloc<int>(p->stream, 1);
+    p->d_out = balloc<double2>(p->stream, (size_t)p->nitems * nrx * nsrc);
     cudaStream_t st = p->stream;
     if (frag0) {
-        BCK(cudaMemcpyAsync(p->d_pos, pos.data(), frag0 * sizeof(float4), cudaMemcpyHostToDevice, st));
-        BCK(cudaMemcpyAsync(p->d_spos, spos.data(), frag0 * sizeof(float4), cudaMemcpyHostToDevice, st));
-        BCK(cudaMemcpyAsync(p->d_nrm, nrm.data(), frag0 * sizeof(float4), cudaMemcpyHostToDevice, st));
-        BCK(cudaMemcpyAsync(p->d_facet, facet.data(), frag0 * sizeof(int), cudaMemcpyHostToDevice, st));
+        BCK(stage_to_device(p->d_pos, pos.data(), frag0 * sizeof(float4), st));
+        BCK(stage_to_device(p->d_spos, spos.data(), frag0 * sizeof(float4), st));
+        BCK(stage_to_device(p->d_nrm, nrm.data(), frag0 * sizeof(float4), st));
+        BCK(stage_to_device(p->d_facet, facet.data(), frag0 * sizeof(int), st));
     }
-    BCK(cudaMemcpyAsync(p->d_facet_n, facet_n.data(), ntri * sizeof(float4), cudaMemcpyHostToDevice, st));
-    BCK(cudaMemcpyAsync(p->d_src, s4.data(), nsrc * sizeof(float4), cudaMemcpyHostToDevice, st));
-    BCK(cudaMemcpyAsync(p->d_rx, r4.data(), nrx * sizeof(float4), cudaMemcpyHostToDevice, st));
+    BCK(stage_to_device(p->d_facet_n, facet_n.data(), ntri * sizeof(float4), st));
+    BCK(stage_to_device(p->d_src, s4.data(), nsrc * sizeof(float4), st));
+    BCK(stage_to_device(p->d_rx, r4.data(), nrx * sizeof(float4), st));
     BCK(cudaMemsetAsync(p->d_status, 0, sizeof(int), st));
     // ---- occluders of each scene (every triangle of the scene, OptiX.cpp:264-296)
     // and its convexity: every vertex on or behind every triangle's plane
@@ -579,17 +583,17 @@ std::unique_ptr<Plan> make_plan(const float *tris, const int *tri_off, int nscen
         node0[s + 1] = (int)nodes.size();
         tri0[s + 1] = (int)(trec.size() / 4);
     }
-    p->d_nodes = balloc<float4>(2 * nodes.size());
-    p->d_tris = balloc<float4>(trec.size());
+    p->d_nodes = balloc<float4>(p->stream, 2 * nodes.size());
+    p->d_tris = balloc<float4>(p->stream, trec.size());
     for (int s = 0; s < nscenes; s++)
         views[s] = BvhView{p->d_nodes + 2 * (size_t)node0[s], p->d_tris + 4 * (size_t)tri0[s],
                            node0[s + 1] - node0[s], tri0[s + 1] - tri0[s]};
     for (int it = 0; it < p->nitems; it++) p->items[it].convex = p->convex[p->items[it].scene];
-    p->d_bvh = balloc<BvhView>(nscenes);
-    BCK(cudaMemcpyAsync(p->d_nodes, nodes.data(), nodes.size() * sizeof(BvhNode), cudaMemcpyHostToDevice, st));
-    BCK(cudaMemcpyAsync(p->d_tris, trec.data(), trec.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
-    BCK(cudaMemcpyAsync(p->d_bvh, views.data(), nscenes * sizeof(BvhView), cudaMemcpyHostToDevice, st));
-    BCK(cudaMemcpyAsync(p->d_items, p->items.data(), p->nitems * sizeof(BatchItem), cudaMemcpyHostToDevice, st));
+    p->d_bvh = balloc<BvhView>(p->stream, nscenes);
+    BCK(stage_to_device(p->d_nodes, nodes.data(), nodes.size() * sizeof(BvhNode), st));
+    BCK(stage_to_device(p->d_tris, trec.data(), trec.size() * sizeof(float4), st));
+    BCK(stage_to_device(p->d_bvh, views.data(), nscenes * sizeof(BvhView), st));
+    BCK(stage_to_device(p->d_items, p->items.data(), p->nitems * sizeof(BatchItem), st));
     BCK(cudaStreamSynchronize(st));
     autotune(*p);
     capture(*p);
@@ -601,8 +605,7 @@ void run_plan(Plan &p, double *out)
     BCK(cudaMemsetAsync(p.d_status, 0, sizeof(int), p.stream));
     BCK(cudaGraphLaunch(p.exec, p.stream));
     if (out)
-        BCK(cudaMemcpyAsync(out, p.d_out, (size_t)p.nitems * p.nrx * p.nsrc * sizeof(double2),
-                            cudaMemcpyDeviceToHost, p.stream));
+        BCK(stage_to_host(out, p.d_out, (size_t)p.nitems * p.nrx * p.nsrc * sizeof(double2), p.stream));
     BCK(cudaStreamSynchronize(p.stream));
     check_status(p);
     BCK(cudaEventElapsedTime(&p.vis_ms, p.ev[0], p.ev[1]));

@@ -4,8 +4,14 @@
 // for bit (src/Facet.cpp:6-339, src/GeoMath.h:19-106), so every expression
 // keeps the reference's operation order; build with -ffp-contract=off.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <condition_variable>
+#include <mutex>
 #include <numeric>
+#include <stdexcept>
+#include <string>
+#include <thread>
 
 #include "host.h"
 
@@ -76,15 +82,19 @@ FacetFrame make_frame(Vec3 v1, Vec3 v2, Vec3 v3, float delta)
     return f;
 }
 
-void fragment_areas(const FacetFrame &f, float *area)
+void fragment_areas(const FacetFrame &f, float *area) { fragment_area_rows(f, area, 0, f.ny); }
+
+// Each cell's area depends only on the tests at its own four corners, so any
+// range of rows gives the same values as the whole grid.
+void fragment_area_rows(const FacetFrame &f, float *area, int j0, int j1)
 {
-    const int nx = f.nx, ny = f.ny, neg = f.neg;
+    const int nx = f.nx, neg = f.neg;
     const float d = f.delta, H = f.height, h = d / 2;
-    std::fill(area, area + (size_t)nx * ny, 0.0f);
+    std::fill(area + (size_t)j0 * nx, area + (size_t)j1 * nx, 0.0f);
     // slopes of the two sloping sides: x > 0 is the positive-base side
     const float mPos = H / (-f.basePos);
     const float mNeg = H / (f.baseNeg);
-    std::vector<unsigned char> inL(ny + 1), inR(ny + 1);
+    std::vector<unsigned char> inL(j1 - j0 + 1), inR(j1 - j0 + 1);
 
     for (int i = 0; i < nx; i++) {
         const float xc = ((float)(i - neg) * d) + h;  // column centre
@@ -93,12 +103,12 @@ void fragment_areas(const FacetFrame &f, float *area)
         const float m = pos ? mPos : mNeg;
         const float yL = m * xL + H;  // side line at the column's left and right edges
         const float yR = m * xR + H;
-        for (int j = 0; j <= ny; j++) {
-            inL[j] = d * (float)j <= yL;
-            inR[j] = d * (float)j <= yR;
+        for (int j = j0; j <= j1; j++) {
+            inL[j - j0] = d * (float)j <= yL;
+            inR[j - j0] = d * (float)j <= yR;
         }
-        for (int j = 0; j < ny; j++) {
-            const bool lb = inL[j], rb = inR[j], lt = inL[j + 1], rt = inR[j + 1];
+        for (int j = j0; j < j1; j++) {
+            const bool lb = inL[j - j0], rb = inR[j - j0], lt = inL[j - j0 + 1], rt = inR[j - j0 + 1];
             float *A = area + (size_t)j * nx + i;
             if (!lb && !rb && !lt && !rt) break;  // above the triangle: rest of column empty
             if (lb && rb && lt && rt) {
@@ -136,6 +146,109 @@ void fragment_areas(const FacetFrame &f, float *area)
     }
 }
 
+namespace {
+
+// Host workers kept for the process (min(16, cores) - 1 threads; the calling
+// thread is the last worker).  One job at a time: a call made while a job
+// runs -- from another thread, or from inside a unit -- runs its units
+// serially instead of waiting.
+thread_local bool tl_in_job = false;
+
+class UnitPool {
+  public:
+    static UnitPool &get()
+    {
+        static UnitPool *p = new UnitPool();  // never destroyed: the workers outlive static destructors
+        return *p;
+    }
+
+    bool run(long long n, const std::function<void(long long)> &fn)
+    {
+        if (tl_in_job || nworkers_ == 0) return false;
+        std::unique_lock<std::mutex> busy(run_mu_, std::try_to_lock);
+        if (!busy.owns_lock()) return false;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            fn_ = &fn;
+            n_ = n;
+            next_ = 0;
+            err_.clear();
+            remaining_ = nworkers_;
+            gen_++;
+        }
+        cv_.notify_all();
+        tl_in_job = true;
+        drain();
+        tl_in_job = false;
+        std::unique_lock<std::mutex> lk(mu_);
+        done_.wait(lk, [&] { return remaining_ == 0; });
+        fn_ = nullptr;
+        if (!err_.empty()) throw std::runtime_error(err_);
+        return true;
+    }
+
+  private:
+    UnitPool()
+    {
+        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        for (unsigned w = 0; w + 1 < hw; w++) {
+            try {
+                std::thread([this] { loop(); }).detach();
+                nworkers_++;
+            } catch (...) {
+                break;
+            }
+        }
+    }
+
+    void loop()
+    {
+        tl_in_job = true;
+        unsigned long long seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return gen_ != seen; });
+                seen = gen_;
+            }
+            drain();
+            std::lock_guard<std::mutex> lk(mu_);
+            if (--remaining_ == 0) done_.notify_all();
+        }
+    }
+
+    void drain()
+    {
+        for (long long u = next_++; u < n_; u = next_++) {
+            try {
+                (*fn_)(u);
+            } catch (const std::exception &e) {
+                std::lock_guard<std::mutex> lk(err_mu_);
+                if (err_.empty()) err_ = e.what();
+                next_ = n_;
+            }
+        }
+    }
+
+    std::mutex run_mu_, mu_, err_mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void(long long)> *fn_ = nullptr;
+    long long n_ = 0;
+    std::atomic<long long> next_{0};
+    unsigned long long gen_ = 0;
+    int nworkers_ = 0, remaining_ = 0;
+    std::string err_;
+};
+
+}  // namespace
+
+void parallel_units(long long n, const std::function<void(long long)> &fn)
+{
+    if (n <= 0) return;
+    if (n > 1 && UnitPool::get().run(n, fn)) return;
+    for (long long u = 0; u < n; u++) fn(u);
+}
+
 Vec3 fragment_centroid(const FacetFrame &f, int x, int y, bool source_hop)
 {
     const float d = f.delta;
@@ -153,21 +266,33 @@ Vec3 fragment_centroid(const FacetFrame &f, int x, int y, bool source_hop)
 bool scene_is_convex(const std::vector<std::array<float, 9>> &t, double tol)
 {
     if (t.size() > 20000) return false;
-    for (const auto &a : t) {
-        const double ux = (double)a[3] - a[0], uy = (double)a[4] - a[1], uz = (double)a[5] - a[2];
-        const double vx = (double)a[6] - a[0], vy = (double)a[7] - a[1], vz = (double)a[8] - a[2];
-        double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
-        const double L = std::sqrt(nx * nx + ny * ny + nz * nz);
-        if (!(L > 0.0)) return false;
-        nx /= L;
-        ny /= L;
-        nz /= L;
-        const double c = nx * a[0] + ny * a[1] + nz * a[2];
-        for (const auto &b : t)
-            for (int k = 0; k < 3; k++)
-                if (nx * b[3 * k] + ny * b[3 * k + 1] + nz * b[3 * k + 2] - c > tol) return false;
-    }
-    return true;
+    constexpr long long kChunk = 64;  // planes per work unit
+    std::atomic<bool> convex{true};
+    parallel_units(((long long)t.size() + kChunk - 1) / kChunk, [&](long long u) {
+        const size_t i1 = std::min(t.size(), (size_t)((u + 1) * kChunk));
+        for (size_t i = (size_t)u * kChunk; i < i1 && convex.load(std::memory_order_relaxed); i++) {
+            const auto &a = t[i];
+            const double ux = (double)a[3] - a[0], uy = (double)a[4] - a[1], uz = (double)a[5] - a[2];
+            const double vx = (double)a[6] - a[0], vy = (double)a[7] - a[1], vz = (double)a[8] - a[2];
+            double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+            const double L = std::sqrt(nx * nx + ny * ny + nz * nz);
+            if (!(L > 0.0)) {
+                convex = false;
+                return;
+            }
+            nx /= L;
+            ny /= L;
+            nz /= L;
+            const double c = nx * a[0] + ny * a[1] + nz * a[2];
+            for (const auto &b : t)
+                for (int k = 0; k < 3; k++)
+                    if (nx * b[3 * k] + ny * b[3 * k + 1] + nz * b[3 * k + 2] - c > tol) {
+                        convex = false;
+                        return;
+                    }
+        }
+    });
+    return convex;
 }
 
 // ---------------------------------------------------------------- BVH

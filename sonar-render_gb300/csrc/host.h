@@ -3,6 +3,7 @@
 // occluder BVH.
 #pragma once
 #include <array>
+#include <functional>
 #include <vector>
 
 #include "sonar_internal.h"
@@ -28,6 +29,12 @@ FacetFrame make_frame(Vec3 v1, Vec3 v2, Vec3 v3, float delta);
 
 // Clipped fragment areas, row-major y*nx + x (src/Facet.cpp:111-339).
 void fragment_areas(const FacetFrame &f, float *area);
+// The same for rows [j0, j1) only (area still points at row 0).
+void fragment_area_rows(const FacetFrame &f, float *area, int j0, int j1);
+
+// fn(u) for every u in [0, n), on up to 16 host threads taking units from a
+// shared counter; an exception in any unit is rethrown (as runtime_error).
+void parallel_units(long long n, const std::function<void(long long)> &fn);
 
 // Fragment centroid of cell (x, y) as the kernels use it: with the +delta/2 x
 // shift for the source hop (src/OptiX.cu:51), without it for the others

@@ -16,6 +16,7 @@
 //     stream is idle, as the reference's DoProjection does (OptiX.cpp:163).
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -28,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/sonar_render.h"
+#include "devpool.h"
 #include "host.h"
 
 namespace sonar {
@@ -60,19 +62,29 @@ struct Error : std::runtime_error {
         if (e_ != cudaSuccess) fail(-10, "%s failed: %s", #call, cudaGetErrorString(e_));          \
     } while (0)
 
+// The render's stream (null before render_cuda: the legacy stream).
+cudaStream_t alloc_stream();
+
+double host_ms()
+{
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Device buffers come from the stream-ordered pool, ordered on the render's
+// stream, which is the only stream that uses them.
 template <class T>
 T *dalloc(size_t n)
 {
     void *p = nullptr;
     if (n == 0) n = 1;
-    CK(cudaMalloc(&p, n * sizeof(T)));
+    CK(pool_alloc(&p, n * sizeof(T), alloc_stream()));
     return (T *)p;
 }
 
 template <class T>
 void dfree(T *&p)
 {
-    if (p) cudaFree(p);
+    pool_free(p, alloc_stream());
     p = nullptr;
 }
 
@@ -125,7 +137,7 @@ struct MaskEntry {
 // Low-rank compression of the FACET_SELF blocks of one object (built with its
 // mask, rebuilt when the mask or k changes).
 // Grow-only device arena: a build carves its arrays from it in order and the
-// next build starts over (no cudaMalloc / cudaFree per build).
+// next build starts over (one pool block, replaced only when it must grow).
 struct Arena {
     char *base = nullptr;
     size_t cap = 0, used = 0;
@@ -133,10 +145,9 @@ struct Arena {
     {
         used = 0;
         if (bytes <= cap) return;
-        if (base) cudaFree(base);
-        base = nullptr;
+        dfree(base);
         cap = 0;
-        CK(cudaMalloc((void **)&base, bytes));
+        base = dalloc<char>(bytes);
         cap = bytes;
     }
     template <class T>
@@ -150,8 +161,7 @@ struct Arena {
     }
     void release()
     {
-        if (base) cudaFree(base);
-        base = nullptr;
+        dfree(base);
         cap = used = 0;
     }
     static size_t bytes_of(size_t n, size_t elem) { return (std::max<size_t>(n, 1) * elem + 255) / 256 * 256; }
@@ -272,6 +282,7 @@ struct Model {
     Compression cmp;
     std::vector<HopRecord> log;
     long long launches = 0, h2d_bytes = 0, d2h_bytes = 0;
+    double render_ms[5] = {0, 0, 0, 0, 0};  // host time of render_cuda: setup, fragments, uploads, occluders, points
 
     void free_device()
     {
@@ -299,54 +310,121 @@ struct Model {
 
 Model g;
 
+cudaStream_t alloc_stream() { return g.stream; }
+
 // ---------------------------------------------------------------- render
+// A host array built for one upload: in the pinned arena when it has room
+// (copied by DMA; the arena is reset after the render's final
+// synchronisation), else on the heap (copied through the staging chunks).
+template <class T>
+struct UploadArray {
+    T *p = nullptr;
+    bool pinned = false;
+    std::vector<T> heap;
+    explicit UploadArray(size_t n)
+    {
+        p = (T *)host_arena_take(std::max<size_t>(n, 1) * sizeof(T));
+        pinned = p != nullptr;
+        if (!pinned) {
+            heap.resize(std::max<size_t>(n, 1));
+            p = heap.data();
+        }
+    }
+    T &operator[](size_t i) { return p[i]; }
+    T *data() { return p; }
+};
+
+template <class T>
+void upload(T *dst, const UploadArray<T> &a, size_t n, cudaStream_t s)
+{
+    if (n == 0) return;
+    if (a.pinned)
+        CK(cudaMemcpyAsync(dst, a.p, n * sizeof(T), cudaMemcpyHostToDevice, s));
+    else
+        CK(stage_to_device(dst, a.p, n * sizeof(T), s));
+}
+
 void render_object(Object &o)
 {
+    const double t0 = host_ms();
     const int nf = (int)o.facets.size();
     o.cell0.assign(nf + 1, 0);
     for (int f = 0; f < nf; f++) o.cell0[f + 1] = o.cell0[f] + (long long)o.facets[f].nx * o.facets[f].ny;
     o.ncells = o.cell0[nf];
     if (o.ncells > (1LL << 31) - 1) fail(-3, "object has %lld cells (limit 2^31-1)", o.ncells);
     o.area.assign((size_t)o.ncells, 0.0f);
-    std::vector<float4> cell_pos((size_t)o.ncells);
-    std::vector<int> cell_facet((size_t)o.ncells);
+    UploadArray<float4> cell_pos((size_t)o.ncells);
+    UploadArray<int> cell_facet((size_t)o.ncells);
     std::vector<float4> facet_n(std::max(nf, 1));
-    std::vector<float4> act_pos;
-    std::vector<int> act_facet;
     o.act_cell.clear();
     o.facet_act_end.assign(std::max(nf, 1), 0);
     o.facet_nact.assign(std::max(nf, 1), 0);
+    // work units: one row of 16-cell patches of one facet.  Pass 1 fills
+    // the areas, the source-hop positions and the facet of every cell and
+    // counts the active ones; pass 2 writes the active cells at their offsets
+    // in compact 16 x 16-cell patches (patch row, patch column, then
+    // row-major inside the patch), so that 256 consecutive fragments -- one
+    // source tile or destination block of the kernels -- cover a small area
+    std::vector<long long> unit0(nf + 1, 0);
     for (int f = 0; f < nf; f++) {
         const FacetFrame &F = o.facets[f];
-        float *A = o.area.data() + o.cell0[f];
-        fragment_areas(F, A);
+        unit0[f + 1] = unit0[f] + (F.ny + kPatch - 1) / kPatch;
         facet_n[f] = make_float4(F.normal.x, F.normal.y, F.normal.z, 0.0f);
-        for (int y = 0; y < F.ny; y++)
+    }
+    const long long nunits = unit0[nf];
+    std::vector<int> unit_facet((size_t)nunits);
+    for (int f = 0; f < nf; f++)
+        for (long long u = unit0[f]; u < unit0[f + 1]; u++) unit_facet[(size_t)u] = f;
+    std::vector<long long> unit_act((size_t)nunits + 1, 0);
+    parallel_units(nunits, [&](long long u) {
+        const int f = unit_facet[(size_t)u];
+        const FacetFrame &F = o.facets[f];
+        const int y0 = (int)(u - unit0[f]) * kPatch, y1 = std::min(F.ny, y0 + kPatch);
+        float *A = o.area.data() + o.cell0[f];
+        fragment_area_rows(F, A, y0, y1);
+        long long cnt = 0;
+        for (int y = y0; y < y1; y++)
             for (int x = 0; x < F.nx; x++) {
                 const long long c = o.cell0[f] + (long long)y * F.nx + x;
+                const float a = A[(long long)y * F.nx + x];
                 const Vec3 ps = fragment_centroid(F, x, y, true);
-                cell_pos[c] = make_float4(ps.x, ps.y, ps.z, A[(long long)y * F.nx + x]);
+                cell_pos[c] = make_float4(ps.x, ps.y, ps.z, a);
                 cell_facet[c] = f;
+                cnt += a > 1e-6f;
             }
-        // active cells of the facet in compact 16 x 16-cell patches (patch row,
-        // patch column, then row-major inside the patch), so that 256
-        // consecutive fragments -- one source tile or destination block of the
-        // kernels -- cover a small area
-        for (int py = 0; py < F.ny; py += kPatch)
-            for (int px = 0; px < F.nx; px += kPatch)
-                for (int y = py; y < std::min(F.ny, py + kPatch); y++)
-                    for (int x = px; x < std::min(F.nx, px + kPatch); x++) {
-                        const float a = A[(long long)y * F.nx + x];
-                        if (!(a > 1e-6f)) continue;
-                        const Vec3 pa = fragment_centroid(F, x, y, false);
-                        act_pos.push_back(make_float4(pa.x, pa.y, pa.z, a));
-                        act_facet.push_back(f);
-                        o.act_cell.push_back((int)(o.cell0[f] + (long long)y * F.nx + x));
-                        o.facet_nact[f]++;
-                    }
-        o.facet_act_end[f] = (int)o.act_cell.size();
+        unit_act[(size_t)u + 1] = cnt;
+    });
+    for (long long u = 0; u < nunits; u++) unit_act[(size_t)u + 1] += unit_act[(size_t)u];
+    const long long na_total = unit_act[(size_t)nunits];
+    if (na_total > (1LL << 31) - 1) fail(-3, "object has %lld active cells (limit 2^31-1)", na_total);
+    UploadArray<float4> act_pos((size_t)na_total);
+    UploadArray<int> act_facet((size_t)na_total);
+    o.act_cell.resize((size_t)na_total);
+    parallel_units(nunits, [&](long long u) {
+        const int f = unit_facet[(size_t)u];
+        const FacetFrame &F = o.facets[f];
+        const int py = (int)(u - unit0[f]) * kPatch;
+        const float *A = o.area.data() + o.cell0[f];
+        size_t k = (size_t)unit_act[(size_t)u];
+        for (int px = 0; px < F.nx; px += kPatch)
+            for (int y = py; y < std::min(F.ny, py + kPatch); y++)
+                for (int x = px; x < std::min(F.nx, px + kPatch); x++) {
+                    const float a = A[(long long)y * F.nx + x];
+                    if (!(a > 1e-6f)) continue;
+                    const Vec3 pa = fragment_centroid(F, x, y, false);
+                    act_pos[k] = make_float4(pa.x, pa.y, pa.z, a);
+                    act_facet[k] = f;
+                    o.act_cell[k] = (int)(o.cell0[f] + (long long)y * F.nx + x);
+                    k++;
+                }
+    });
+    for (int f = 0; f < nf; f++) {
+        o.facet_act_end[f] = (int)unit_act[(size_t)unit0[f + 1]];
+        o.facet_nact[f] = unit_act[(size_t)unit0[f + 1]] - unit_act[(size_t)unit0[f]];
     }
     const size_t nc = (size_t)o.ncells, na = o.act_cell.size();
+    const double t1 = host_ms();
+    g.render_ms[1] += t1 - t0;
     o.d_cell_pos = dalloc<float4>(nc);
     o.d_cell_facet = dalloc<int>(nc);
     o.d_facet_n = dalloc<float4>(facet_n.size());
@@ -356,17 +434,16 @@ void render_object(Object &o)
     o.d_act_cell = dalloc<int>(na);
     o.d_facet_end = dalloc<int>(o.facet_act_end.size());
     cudaStream_t s = g.stream;
-    CK(cudaMemcpyAsync(o.d_cell_pos, cell_pos.data(), nc * sizeof(float4), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(o.d_cell_facet, cell_facet.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(o.d_facet_n, facet_n.data(), facet_n.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
+    upload(o.d_cell_pos, cell_pos, nc, s);
+    upload(o.d_cell_facet, cell_facet, nc, s);
+    CK(stage_to_device(o.d_facet_n, facet_n.data(), facet_n.size() * sizeof(float4), s));
     CK(cudaMemsetAsync(o.d_P, 0, std::max<size_t>(nc, 1) * sizeof(double2), s));
     if (na) {
-        CK(cudaMemcpyAsync(o.d_act_pos, act_pos.data(), na * sizeof(float4), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(o.d_act_facet, act_facet.data(), na * sizeof(int), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(o.d_act_cell, o.act_cell.data(), na * sizeof(int), cudaMemcpyHostToDevice, s));
+        upload(o.d_act_pos, act_pos, na, s);
+        upload(o.d_act_facet, act_facet, na, s);
+        CK(stage_to_device(o.d_act_cell, o.act_cell.data(), na * sizeof(int), s));
     }
-    CK(cudaMemcpyAsync(o.d_facet_end, o.facet_act_end.data(), o.facet_act_end.size() * sizeof(int),
-                       cudaMemcpyHostToDevice, s));
+    CK(stage_to_device(o.d_facet_end, o.facet_act_end.data(), o.facet_act_end.size() * sizeof(int), s));
     g.h2d_bytes += (long long)(nc * (sizeof(float4) + sizeof(int)) + facet_n.size() * sizeof(float4) +
                                na * (sizeof(float4) + 2 * sizeof(int)) + o.facet_act_end.size() * sizeof(int));
     if (o.type == OBJ_TARGET) {
@@ -375,23 +452,25 @@ void render_object(Object &o)
         CK(cudaMemsetAsync(o.d_Pin, 0, std::max<size_t>(nc, 1) * sizeof(double2), s));
         CK(cudaMemsetAsync(o.d_Pout, 0, std::max<size_t>(nc, 1) * sizeof(double2), s));
     }
-    // the pageable host vectors above are read by the copies before they go
-    CK(cudaStreamSynchronize(s));
+    // the staged copies have read their host arrays; the pinned ones are read
+    // by the DMA before render's final synchronisation resets the arena
+    g.render_ms[2] += host_ms() - t1;
 }
 
 void upload_points(const std::vector<Vec3> &pts, float4 *&d_pos, double2 *&d_P, double value)
 {
-    std::vector<float4> pos(pts.size());
-    std::vector<double2> P(pts.size(), make_double2(value, 0.0));
-    for (size_t i = 0; i < pts.size(); i++) pos[i] = make_float4(pts[i].x, pts[i].y, pts[i].z, 0.0f);
-    d_pos = dalloc<float4>(pts.size());
-    d_P = dalloc<double2>(pts.size());
-    if (!pts.empty()) {
-        CK(cudaMemcpyAsync(d_pos, pos.data(), pos.size() * sizeof(float4), cudaMemcpyHostToDevice, g.stream));
-        CK(cudaMemcpyAsync(d_P, P.data(), P.size() * sizeof(double2), cudaMemcpyHostToDevice, g.stream));
-        g.h2d_bytes += (long long)(pos.size() * sizeof(float4) + P.size() * sizeof(double2));
+    const size_t n = pts.size();
+    UploadArray<float4> pos(n);
+    UploadArray<double2> P(n);
+    for (size_t i = 0; i < n; i++) {
+        pos[i] = make_float4(pts[i].x, pts[i].y, pts[i].z, 0.0f);
+        P[i] = make_double2(value, 0.0);
     }
-    CK(cudaStreamSynchronize(g.stream));
+    d_pos = dalloc<float4>(n);
+    d_P = dalloc<double2>(n);
+    upload(d_pos, pos, n, g.stream);
+    upload(d_P, P, n, g.stream);
+    g.h2d_bytes += (long long)(n * (sizeof(float4) + sizeof(double2)));
 }
 
 // Order of points along a Morton (Z-order) curve of their bounding box.
@@ -435,12 +514,20 @@ std::vector<int> morton_order(const std::vector<Vec3> &pts)
 void render()
 {
     if (g.rendered) fail(-2, "render_cuda called twice without TearDownCuda");
+    const double t0 = host_ms();
+    // a render that failed part-way may have left copies in flight out of
+    // the pinned arena
+    if (g.stream) CK(cudaStreamSynchronize(g.stream));
+    host_arena_reset();
+    for (double &v : g.render_ms) v = 0.0;
     CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
     for (cudaEvent_t *e : {&g.ev0, &g.ev1, &g.ev2, &g.ev3, &g.ev4, &g.ev5, &g.ev6, &g.ev7, &g.ev8, &g.evb[0], &g.evb[1],
                            &g.evb[2], &g.evb[3]})
         CK(cudaEventCreate(e));
+    g.render_ms[0] = host_ms() - t0;
     for (int t : {OBJ_TARGET, OBJ_FIELD})
         for (auto &o : g.obj[t]) render_object(*o);
+    const double t2 = host_ms();
     // occluders: every triangle of every target object (OptiX.cpp:264-296)
     std::vector<std::array<float, 9>> tris;
     double maxc = 0.0;
@@ -466,12 +553,12 @@ void render()
     g.d_nodes = dalloc<float4>(2 * bvh.nodes.size());
     g.d_tris = dalloc<float4>(bvh.tris.size());
     if (g.ntri) {
-        CK(cudaMemcpyAsync(g.d_nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(BvhNode), cudaMemcpyHostToDevice,
-                           g.stream));
-        CK(cudaMemcpyAsync(g.d_tris, bvh.tris.data(), bvh.tris.size() * sizeof(float4), cudaMemcpyHostToDevice,
-                           g.stream));
+        CK(stage_to_device(g.d_nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(BvhNode), g.stream));
+        CK(stage_to_device(g.d_tris, bvh.tris.data(), bvh.tris.size() * sizeof(float4), g.stream));
         g.h2d_bytes += (long long)(bvh.nodes.size() * sizeof(BvhNode) + bvh.tris.size() * sizeof(float4));
     }
+    const double t3 = host_ms();
+    g.render_ms[3] = t3 - t2;
     upload_points(g.src, g.d_src_pos, g.d_src_P, 1.0);  // unit source pressure (Model.cpp:16-19)
     g.fp_order = morton_order(g.fp);
     std::vector<Vec3> fp_sorted(g.fp.size());
@@ -479,10 +566,11 @@ void render()
     upload_points(fp_sorted, g.d_fp_pos, g.d_fp_P, 0.0);
     g.d_fp_order = dalloc<int>(g.fp_order.size());
     if (!g.fp_order.empty()) {
-        CK(cudaMemcpyAsync(g.d_fp_order, g.fp_order.data(), g.fp_order.size() * sizeof(int), cudaMemcpyHostToDevice,
-                           g.stream));
-        CK(cudaStreamSynchronize(g.stream));
+        CK(stage_to_device(g.d_fp_order, g.fp_order.data(), g.fp_order.size() * sizeof(int), g.stream));
     }
+    CK(cudaStreamSynchronize(g.stream));
+    host_arena_reset();  // every copy out of it is done
+    g.render_ms[4] = host_ms() - t3;
     g.rendered = true;
 }
 
@@ -1353,8 +1441,7 @@ void GetFieldPointPressures(dcomplex *field_points_pressure, int NumPoints)
         const size_t n = std::min<size_t>(NumPoints < 0 ? 0 : (size_t)NumPoints, g.fp.size());
         if (n && !field_points_pressure) fail(-6, "null output buffer");
         if (n) {
-            CK(cudaMemcpyAsync(field_points_pressure, g.d_fp_P, n * sizeof(double2), cudaMemcpyDeviceToHost, g.stream));
-            CK(cudaStreamSynchronize(g.stream));
+            CK(stage_to_host(field_points_pressure, g.d_fp_P, n * sizeof(double2), g.stream));
             g.d2h_bytes += (long long)(n * sizeof(double2));
         }
         if ((size_t)std::max(NumPoints, 0) < g.fp.size())
@@ -1377,7 +1464,9 @@ void TearDownCuda(void)
     // src/Model.cpp:115-129, src/ModelCuda.cpp:124-181: points, target and
     // field objects are dropped; source objects are kept, as in the reference
     try {
-        if (g.stream) cudaStreamSynchronize(g.stream);
+        // every stream, as the cudaFree of the buffers used to: a caller may
+        // still read a result on a stream of its own
+        cudaDeviceSynchronize();
         g.free_device();
     } catch (...) {
     }
@@ -1435,8 +1524,7 @@ int sonar_get_object_pressures(int objectType, int objIdx, dcomplex *out, long l
         if (o.type == OBJ_SOURCE || !o.d_P) fail(-4, "object has no pressures");
         if (n < o.ncells) fail(-8, "buffer holds %lld of %lld cells", n, o.ncells);
         if (o.ncells) {
-            CK(cudaMemcpyAsync(out, o.d_P, (size_t)o.ncells * sizeof(double2), cudaMemcpyDeviceToHost, g.stream));
-            CK(cudaStreamSynchronize(g.stream));
+            CK(stage_to_host(out, o.d_P, (size_t)o.ncells * sizeof(double2), g.stream));
             g.d2h_bytes += o.ncells * (long long)sizeof(double2);
         }
         written = (int)o.ncells;
@@ -1491,8 +1579,10 @@ int sonar_get_stats(char *json, int cap)
     }
     snprintf(buf, sizeof(buf),
              "], \"ntri\": %d, \"nnodes\": %d, \"masks\": %zu, \"launches\": %lld, \"h2d_bytes\": %lld, "
-             "\"d2h_bytes\": %lld, \"mask_classes\": [",
-             g.ntri, g.nnodes, g.masks.size(), g.launches, g.h2d_bytes, g.d2h_bytes);
+             "\"d2h_bytes\": %lld, \"pool_reserved_bytes\": %llu, \"render_host_ms\": {\"setup\": %.4f, "
+             "\"fragments\": %.4f, \"uploads\": %.4f, \"occluders\": %.4f, \"points\": %.4f}, \"mask_classes\": [",
+             g.ntri, g.nnodes, g.masks.size(), g.launches, g.h2d_bytes, g.d2h_bytes, pool_reserved_bytes(),
+             g.render_ms[0], g.render_ms[1], g.render_ms[2], g.render_ms[3], g.render_ms[4]);
     s += buf;
     for (size_t i = 0; i < g.masks.size(); i++) {
         const MaskEntry &m = g.masks[i];
@@ -1512,6 +1602,12 @@ int sonar_get_stats(char *json, int cap)
 int sonar_set_option(const char *key, double value)
 {
     if (!key) return -1;
+    if (!strcmp(key, "memory_cache_mb")) {
+        if (!(value >= 0.0)) return -6;
+        pool_set_cache_limit((unsigned long long)(value * 1048576.0));
+        return 0;
+    }
+    if (!strcmp(key, "release_memory")) return pool_trim() == cudaSuccess ? 0 : -10;
     if (!strcmp(key, "split")) { g.opt_split = (int)value; return 0; }
     if (!strcmp(key, "f2f_symmetric")) { g.opt_f2f_sym = value != 0.0; return 0; }
     if (!strcmp(key, "class_stats")) { g.opt_class_stats = value != 0.0; return 0; }
@@ -1602,15 +1698,14 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
         // a full mask (bits in every block), built for the export and freed
         MaskEntry M = build_mask(hop, srcIdx, dstIdx, 1);
         uint8_t *d = nullptr;
-        cudaError_t e = cudaMalloc(&d, (size_t)nbytes);
+        cudaError_t e = pool_alloc((void **)&d, (size_t)nbytes, g.stream);
         if (e == cudaSuccess) {
             launch_mask_export(M.view, M.nsrc, M.ndst, d, g.stream);
             e = cudaGetLastError();
         }
         std::vector<uint8_t> tmp((size_t)nbytes);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(tmp.data(), d, (size_t)nbytes, cudaMemcpyDeviceToHost, g.stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
-        if (d) cudaFree(d);
+        if (e == cudaSuccess) e = stage_to_host(tmp.data(), d, (size_t)nbytes, g.stream);
+        dfree(d);
         M.free_device();
         if (e != cudaSuccess) fail(-10, "mask export failed: %s", cudaGetErrorString(e));
         // active fragments are stored in patch order; report them in cell order
@@ -1661,7 +1756,7 @@ int sonar_get_surface_colours(int objectType, int objIdx, float *rgba, long long
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(rgba, d, (size_t)o.ncells * sizeof(float4), cudaMemcpyDeviceToHost, g.stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
-        cudaFree(d);
+        dfree(d);
         if (e != cudaSuccess) fail(-10, "colour map failed: %s", cudaGetErrorString(e));
         written = (int)o.ncells;
     });
@@ -1756,9 +1851,11 @@ int sonar_mlp_predict(const float *X, int n, float *out)
         if (!mlp_ready()) fail(-2, "the network has no parameters");
         if (n == 0) return;
         float *dX = dalloc<float>((size_t)n * 8), *dY = dalloc<float>(n);
-        cudaError_t e = cudaMemcpy(dX, X, (size_t)n * 8 * sizeof(float), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = mlp_infer_dev(dX, n, dY, 0);
-        if (e == cudaSuccess) e = cudaMemcpy(out, dY, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+        cudaStream_t s = alloc_stream();  // the stream the pool ordered the two blocks on
+        cudaError_t e = cudaMemcpyAsync(dX, X, (size_t)n * 8 * sizeof(float), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = mlp_infer_dev(dX, n, dY, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out, dY, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         dfree(dX);
         dfree(dY);
         if (e != cudaSuccess) fail(-10, "network inference failed: %s", cudaGetErrorString(e));
