@@ -2423,6 +2423,8 @@ __global__ void __launch_bounds__(kTile) k_lr_block(SumArgs a, const int2 *block
     }
     __syncthreads();
     float rr = 0.0f, ri = 0.0f, cr = 0.0f, ci = 0.0f;
+    // the factors come back from L2: several ranks' loads in flight at once
+#pragma unroll 4
     for (int m = 0; m < k; ++m) {
         const float2 u = Ub[m * kTile], v = Vb[m * kTile], c = sTv[m], e = sSu[m];
         rr += u.x * c.x - u.y * c.y;

@@ -44,23 +44,32 @@ def test_compressed_bounces_match_plain(api, scenes):
     assert err < 1e-3
 
 
-def test_compressed_bounce_vs_oracle(api, oracle_mod, scenes):
+@pytest.mark.parametrize("tol", [1e-4, 5e-4])
+def test_compressed_bounce_vs_oracle(api, oracle_mod, scenes, tol):
+    """The library default (1e-4) and the benchmark's tolerance (5e-4, judge
+    limit 1.5e-3) both stay within the 1e-3 target against FP64."""
     sc = _trihedral(scenes, 30e3)
     api.set_option("compress", 1)
-    load_scene(api, sc)
-    api.project_source_points_to_objects(False)
-    P0 = api.get_object_pressures(api.TARGET, 0)
-    api.project_target_to_target_objects(1)
-    P1 = api.get_object_pressures(api.TARGET, 0)
-    api.set_option("compress", 0)
-    api.TearDownCuda()
+    api.set_option("compress_tol", tol)
+    api.set_option("compress_judge", 3.0 * tol)
+    try:
+        load_scene(api, sc)
+        api.project_source_points_to_objects(False)
+        P0 = api.get_object_pressures(api.TARGET, 0)
+        api.project_target_to_target_objects(1)
+        P1 = api.get_object_pressures(api.TARGET, 0)
+    finally:
+        api.set_option("compress", 0)
+        api.set_option("compress_tol", 1e-4)
+        api.set_option("compress_judge", 3e-4)
+        api.TearDownCuda()
     o = oracle_scene(oracle_mod, sc)
     act = o.active(0, 0)
     rng = np.random.default_rng(77)
     q = np.sort(rng.choice(len(act), 64, replace=False))
     v1, _ = o.hop_subset(2, 0, 0, q, pin=P0)
     err = rel_l2((P1 - P0)[act[q]], v1)
-    print("compressed bounce vs FP64 oracle (64 seeded destinations): rel L2 %.3e" % err)
+    print("compressed bounce (tol %.0e) vs FP64 oracle (64 seeded destinations): rel L2 %.3e" % (tol, err))
     assert err < 1e-3
 
 
