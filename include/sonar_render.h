@@ -147,6 +147,9 @@ int sonar_get_stats(char *json, int cap);
  * forward into the higher-index object, reciprocal into the lower, all
  * from the bounce's inputs).
  * "aca_variant" (cross-approximation kernel shape, 0-2; bit-identical).
+ * "overlap_streams" (1, default: a compressed bounce runs its low-rank apply
+ * on a second stream beside the dense remainder, joined before the
+ * finalize; 0: one stream; the same results either way).
  * Device memory: every buffer comes from a stream-ordered pool kept for the
  * process; "memory_cache_mb" (32768, default: unused pool memory kept at a
  * synchronisation point, in MiB; 0 gives it all back there; negative: -6),

@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cmath>
 #include <condition_variable>
+#include <pthread.h>
 #include <mutex>
 #include <numeric>
 #include <stdexcept>
@@ -187,9 +188,13 @@ class UnitPool {
         return true;
     }
 
+    // a forked child has none of the workers: every call there runs serially
+    void forget_workers() { nworkers_ = 0; }
+
   private:
     UnitPool()
     {
+        pthread_atfork(nullptr, nullptr, [] { UnitPool::get().forget_workers(); });
         const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
         for (unsigned w = 0; w + 1 < hw; w++) {
             try {

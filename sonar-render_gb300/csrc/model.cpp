@@ -236,6 +236,10 @@ struct Model {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr, ev4 = nullptr, ev5 = nullptr;
     cudaEvent_t ev6 = nullptr, ev7 = nullptr, ev8 = nullptr;
+    // second stream of a compressed bounce: the low-rank apply (HBM-bound)
+    // runs there beside the dense remainder (FP32 / SFU-bound)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t evb[4] = {nullptr, nullptr, nullptr, nullptr};  // compression build: start, selected, ACA end, end
     float4 *d_src_pos = nullptr, *d_fp_pos = nullptr;
     double2 *d_src_P = nullptr, *d_fp_P = nullptr;
@@ -277,6 +281,7 @@ struct Model {
     int opt_gate_proj = 1;      // bounce masks: gates decided from per-point projections where certain
     int opt_cross_objects = 0;  // bounces also between different targets (FACET_RESP); 0: the reference's behaviour
     int opt_convex_masks = 1;   // convex targets: shadow tests search only where a crossing is possible
+    int opt_overlap = 1;        // compressed bounce: low-rank apply on the second stream beside the dense remainder
     int scene_convex = 0;       // every target vertex on or behind every target triangle's plane
     float scene_vmax = 0.0f;    // largest |coordinate| of the target vertices
     Compression cmp;
@@ -302,6 +307,13 @@ struct Model {
                 cudaEventDestroy(*e);
                 *e = nullptr;
             }
+        for (cudaEvent_t *e : {&ev_fork, &ev_join})
+            if (*e) {
+                cudaEventDestroy(*e);
+                *e = nullptr;
+            }
+        if (side) cudaStreamDestroy(side);
+        side = nullptr;
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
         nnodes = ntri = 0;
@@ -524,6 +536,9 @@ void render()
     for (cudaEvent_t *e : {&g.ev0, &g.ev1, &g.ev2, &g.ev3, &g.ev4, &g.ev5, &g.ev6, &g.ev7, &g.ev8, &g.evb[0], &g.evb[1],
                            &g.evb[2], &g.evb[3]})
         CK(cudaEventCreate(e));
+    CK(cudaStreamCreateWithFlags(&g.side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&g.ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&g.ev_join, cudaEventDisableTiming));
     g.render_ms[0] = host_ms() - t0;
     for (int t : {OBJ_TARGET, OBJ_FIELD})
         for (auto &o : g.obj[t]) render_object(*o);
@@ -1039,11 +1054,20 @@ void run_hop(int hop, int a, int b)
                     built = true;
                 }
                 s.mask.flags = C.d_flags;  // accepted blocks are left to the low-rank path
-                CK(cudaEventRecord(g.ev4, st));
+                // both paths read the packed inputs and write their own buffers;
+                // the finalize below waits for the low-rank stream
+                cudaStream_t lst = st;
+                if (g.opt_overlap) {
+                    CK(cudaEventRecord(g.ev_fork, st));
+                    CK(cudaStreamWaitEvent(g.side, g.ev_fork, 0));
+                    lst = g.side;
+                }
+                CK(cudaEventRecord(g.ev4, lst));
                 launch_lr_apply(s, C.d_blocks, C.d_off, C.d_bidx, C.nblocks, C.d_U, C.d_V, C.d_rank, C.d_brow, C.d_bcol,
-                                M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, st,
+                                M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, lst,
                                 C.d_nacc);
-                CK(cudaEventRecord(g.ev5, st));
+                CK(cudaEventRecord(g.ev5, lst));
+                if (g.opt_overlap) CK(cudaEventRecord(g.ev_join, lst));
                 yrow = C.d_yrow;
                 ycol = C.d_ycol;
                 rec_cmp = true;
@@ -1056,6 +1080,7 @@ void run_hop(int hop, int a, int b)
             CK(cudaEventRecord(g.ev2, st));
             launch_sum_f2f_sym(s, wl, 3 * g.nsm, g.d_colpart, g.d_rowpart, st);
             CK(cudaEventRecord(g.ev3, st));
+            if (yrow && g.opt_overlap) CK(cudaStreamWaitEvent(st, g.ev_join, 0));
             launch_finalize_f2f_sym(g.d_rowpart, g.d_chunk_off, M.ndst, g.d_colpart, s.mask.flags, M.view.ntiles,
                                     A.d_act_cell, A.d_Pin, A.d_Pout, A.d_P, st, yrow, ycol);
         } else {
@@ -1618,6 +1643,10 @@ int sonar_set_option(const char *key, double value)
     if (!strcmp(key, "compress_select")) {
         g.opt_cmp_select = std::max(0, std::min(2, (int)value));
         g.cmp.release();
+        return 0;
+    }
+    if (!strcmp(key, "overlap_streams")) {
+        g.opt_overlap = value != 0.0 ? 1 : 0;
         return 0;
     }
     if (!strcmp(key, "convex_masks")) {
