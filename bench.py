@@ -313,10 +313,11 @@ def lowrank_roofline(stats):
     ms = sum(x["lr_ms"] for x in hops) / len(hops)
     peak, src = hbm_peak()
     ach = bytes_launch / (ms * 1e-3) / 1e9
-    # k_lr_block's DRAM bytes were 0.988 x these algorithmic bytes in the ncu
-    # capture on the 40 kHz trihedral (1.385 GB for 19,316 blocks at rank 15.7)
+    # k_lr_block's DRAM bytes were 0.945 x these algorithmic bytes in the ncu
+    # capture on the 40 kHz trihedral at tolerance 5e-4 (1.152 GB for 19,452
+    # blocks at rank 13.3)
     return {"kernel": "k_lr_block + k_lr_gather (low-rank apply)", "bound": "hbm", "achieved": round(ach, 1),
-            "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": round(0.988 * bytes_launch),
+            "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": round(0.945 * bytes_launch),
             "traffic_source": "ncu dram bytes of k_lr_block on the 40 kHz capture, scaled by algorithmic bytes",
             "bytes_per_launch": int(bytes_launch), "launch_ms": round(ms, 4), "peak_source": src,
             "blocks": nacc, "mean_rank": h["cmp_mean_rank"]}
@@ -339,10 +340,10 @@ def aca_roofline(stats, fp32_peak):
     ach = nb * flop_block / (ms * 1e-3) / 1e12
     peak = fp32_peak / 1e12
     # DRAM bytes per (block x rank) from the ncu capture of this kernel on the
-    # 40 kHz trihedral with every interacting block approximated (1.335 GB for
-    # 20,170 blocks at mean rank 15.7: the factors written once), scaled to
-    # this launch by its blocks x ranks
-    traffic = 4209.0 * nb * k
+    # 40 kHz trihedral with every interacting block approximated at tolerance
+    # 5e-4 (1.119 GB for 20,170 blocks at mean rank 13.3: the factors written
+    # once), scaled to this launch by its blocks x ranks
+    traffic = 4172.0 * nb * k
     return {"kernel": "k_aca (cross approximation + exact-entry judge)", "bound": "fp32 issue (serial pivots)",
             "achieved": round(ach, 3), "peak": round(peak, 3), "unit": "TFLOP/s", "frac": round(ach / peak, 4),
             "traffic": round(traffic), "traffic_source": "ncu dram bytes of the 40 kHz capture, scaled by blocks x rank",
