@@ -16,6 +16,7 @@
 // one from pinned memory at the link's rate, so the host fills (or drains)
 // one chunk while the other is on the link.
 #include "devpool.h"
+#include "host.h"
 
 #include <algorithm>
 #include <cstring>
@@ -172,6 +173,22 @@ bool stage_ready(Stage &st)
     return true;
 }
 
+// memcpy on the host workers for large copies (the caller's pages, often
+// fresh, fault in on several threads at once)
+void host_copy(void *dst, const void *src, size_t n)
+{
+    constexpr size_t kPiece = 512u << 10;
+    if (n < 2 * kPiece) {
+        memcpy(dst, src, n);
+        return;
+    }
+    const long long pieces = (long long)((n + kPiece - 1) / kPiece);
+    parallel_units(pieces, [&](long long u) {
+        const size_t off = (size_t)u * kPiece;
+        memcpy((char *)dst + off, (const char *)src + off, std::min(kPiece, n - off));
+    });
+}
+
 // Waits until chunk b's last copy is done.
 cudaError_t stage_wait(Stage &st, int b)
 {
@@ -197,7 +214,7 @@ cudaError_t stage_to_device(void *dst, const void *src, size_t bytes, cudaStream
         const size_t n = std::min(kStageChunk, bytes - off);
         cudaError_t e = stage_wait(st, b);
         if (e != cudaSuccess) return e;
-        memcpy(st.buf[b], (const char *)src + off, n);
+        host_copy(st.buf[b], (const char *)src + off, n);
         e = cudaMemcpyAsync((char *)dst + off, st.buf[b], n, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = cudaEventRecord(st.done[b], s);
         if (e != cudaSuccess) return e;
@@ -233,7 +250,7 @@ cudaError_t stage_to_host(void *dst, const void *src, size_t bytes, cudaStream_t
         const size_t off = k * kStageChunk, n = std::min(kStageChunk, bytes - off);
         e = stage_wait(st, b);
         if (e != cudaSuccess) break;
-        memcpy((char *)dst + off, st.buf[b], n);
+        host_copy((char *)dst + off, st.buf[b], n);
         if (k + 2 < nch) e = issue(k + 2);
     }
     return e;
