@@ -16,7 +16,8 @@
  * interaction mask (test/diagnostic use).
  *
  * Pointers are plain host pointers; sizes are element counts.  The library
- * owns all device memory (freed by TearDownCuda).  Calls are synchronous and
+ * owns all device memory (returned to its memory pool by TearDownCuda; see
+ * the options "memory_cache_mb" and "release_memory").  Calls are synchronous and
  * not thread-safe, as in the reference (one process-global model,
  * src/python_interface.cpp:11).
  */
