@@ -2,7 +2,7 @@
  *
  * TEST INFRASTRUCTURE ONLY: the GPU's forward and backward kernels are
  * checked against these loops.  The reference has no learned component; the
- * network is defined here by its mathematics: layers 8 -> 128 -> 128 -> 128
+ * network is defined here by its mathematics: layers 8 -> 64 -> 64 -> 64
  * -> 1, y = W x + b, ReLU after every layer but the last, loss = mean over
  * the batch of (y_hat - y)^2.  Parameter layout: per layer the weights
  * (out x in, row-major) then the biases.
@@ -11,7 +11,7 @@
 #include <string.h>
 
 #define NL 4
-static const int dims[NL + 1] = {8, 128, 128, 128, 1};
+static const int dims[NL + 1] = {8, 64, 64, 64, 1};
 
 int orc_mlp_param_count(void)
 {

@@ -1,4 +1,4 @@
-// mlp.cu -- the learned admissibility model: a 4-layer, width-128 perceptron
+// mlp.cu -- the learned admissibility model: a 4-layer, width-64 perceptron
 // trained and evaluated by this library's own CUDA kernels.
 //
 // It maps the descriptors of a fragment-cluster pair (separation and radii in
@@ -8,7 +8,7 @@
 // attempt; the others are approximated with a rank cap derived from the
 // prediction, and the exact tile still judges every approximation.
 //
-// Layers: 8 -> 128 -> 128 -> 128 -> 1, ReLU between, FP32 weights, activations
+// Layers: 8 -> 64 -> 64 -> 64 -> 1, ReLU between, FP32 weights, activations
 // and gradients.  Training: mean-squared error on log2(rank), Adam.
 // Kernels: a shared-memory tiled dense layer (forward, input gradient, weight
 // gradient), bias/ReLU epilogues, the loss gradient and the Adam update.
@@ -25,7 +25,7 @@
 namespace sonar {
 namespace {
 
-constexpr int kIn = 8, kWidth = 128, kLayers = 4;
+constexpr int kIn = 8, kWidth = 64, kLayers = 4;
 constexpr int kDims[kLayers + 1] = {kIn, kWidth, kWidth, kWidth, 1};
 constexpr int kT = 16;  // tile of the dense-layer kernels
 
@@ -151,9 +151,10 @@ inline dim3 tiles(int cols, int rows) { return dim3((cols + kT - 1) / kT, (rows 
 // once per CTA in shared memory (hidden layers transposed, [in][out], so
 // that the 32 lanes of a warp read 32 consecutive outputs' weights), and each
 // warp runs groups of kInferRows rows through the layers: lane l owns hidden
-// units l, l + 32, l + 64, l + 96 of every row, the activations of the group
+// units l, l + 32, ... (kUnits of them) of every row, the activations of the group
 // pass between layers through the warp's shared-memory slice.
 constexpr int kInferRows = 8;
+constexpr int kUnits = kWidth / 32;  // hidden units per lane
 constexpr int kInferWarps = 8;
 constexpr size_t kInferSmem =
     sizeof(float) * ((size_t)kIn * kWidth + 2 * (size_t)kWidth * kWidth + 4 * kWidth + 1 +
@@ -198,27 +199,27 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_mlp_infer(const float *P, 
             XI[e] = r < n ? X[(size_t)r0 * kIn + e] : 0.0f;
         }
         __syncwarp();
-        float acc[kInferRows][4];
-        // layer 1: 8 -> 128, ReLU
+        float acc[kInferRows][kUnits];
+        // layer 1: 8 -> kWidth, ReLU
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < kUnits; ++q) {
             const float b = B1[lane + 32 * q];
 #pragma unroll
             for (int r = 0; r < kInferRows; ++r) acc[r][q] = b;
         }
 #pragma unroll
         for (int i = 0; i < kIn; ++i) {
-            float w[4];
+            float w[kUnits];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) w[q] = W1[i * kWidth + lane + 32 * q];
+            for (int q = 0; q < kUnits; ++q) w[q] = W1[i * kWidth + lane + 32 * q];
 #pragma unroll
             for (int r = 0; r < kInferRows; ++r) {
                 const float x = XI[r * kIn + i];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) acc[r][q] = fmaf(w[q], x, acc[r][q]);
+                for (int q = 0; q < kUnits; ++q) acc[r][q] = fmaf(w[q], x, acc[r][q]);
             }
         }
-        // layers 2 and 3: 128 -> 128, ReLU
+        // layers 2 and 3: kWidth -> kWidth, ReLU
 #pragma unroll 1
         for (int layer = 0; layer < 2; ++layer) {
             const float *W = layer == 0 ? W2 : W3, *Bv = layer == 0 ? B2 : B3;
@@ -226,33 +227,33 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_mlp_infer(const float *P, 
 #pragma unroll
             for (int r = 0; r < kInferRows; ++r)
 #pragma unroll
-                for (int q = 0; q < 4; ++q) H[r * kWidth + lane + 32 * q] = fmaxf(acc[r][q], 0.0f);
+                for (int q = 0; q < kUnits; ++q) H[r * kWidth + lane + 32 * q] = fmaxf(acc[r][q], 0.0f);
             __syncwarp();
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < kUnits; ++q) {
                 const float b = Bv[lane + 32 * q];
 #pragma unroll
                 for (int r = 0; r < kInferRows; ++r) acc[r][q] = b;
             }
 #pragma unroll 4
             for (int i = 0; i < kWidth; ++i) {
-                float w[4];
+                float w[kUnits];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) w[q] = W[i * kWidth + lane + 32 * q];
+                for (int q = 0; q < kUnits; ++q) w[q] = W[i * kWidth + lane + 32 * q];
 #pragma unroll
                 for (int r = 0; r < kInferRows; ++r) {
                     const float h = H[r * kWidth + i];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) acc[r][q] = fmaf(w[q], h, acc[r][q]);
+                    for (int q = 0; q < kUnits; ++q) acc[r][q] = fmaf(w[q], h, acc[r][q]);
                 }
             }
         }
-        // output layer: 128 -> 1
+        // output layer: kWidth -> 1
 #pragma unroll
         for (int r = 0; r < kInferRows; ++r) {
             float v = 0.0f;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) v = fmaf(W4[lane + 32 * q], fmaxf(acc[r][q], 0.0f), v);
+            for (int q = 0; q < kUnits; ++q) v = fmaf(W4[lane + 32 * q], fmaxf(acc[r][q], 0.0f), v);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
             if (lane == 0 && r0 + r < n) Y[r0 + r] = v + B4[0];

@@ -3,7 +3,7 @@ against the FP64 oracle, Adam training, and the ablation that shows what the
 trained network gains over compression without it.
 
 Gradient check: GPU gradient of the mean squared error within 1e-4 relative
-L2 of the oracle's FP64 gradient (FP32 kernels, 128-wide sums).
+L2 of the oracle's FP64 gradient (FP32 kernels, 64-wide sums).
 Ablation (trihedral, 30 kHz, network trained on its 20 and 25 kHz versions):
 the network's proposals compress more of the bounce's pair work than the
 separation rule at the same 1e-3 error bound, and need fewer approximation
@@ -43,7 +43,7 @@ def test_forward_and_gradient_match_oracle(adm, oracle_mod):
     assert e_grad < 1e-4
     # per layer (the last layers' gradients are the smallest)
     off = 0
-    for fin, fout in ((8, 128), (128, 128), (128, 128), (128, 1)):
+    for fin, fout in ((8, 64), (64, 64), (64, 64), (64, 1)):
         n = fin * fout + fout
         assert rel_l2(g[off:off + n], g_ref[off:off + n]) < 1e-4
         off += n

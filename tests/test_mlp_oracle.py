@@ -7,7 +7,7 @@ import numpy as np
 def test_oracle_gradient_matches_finite_differences(oracle_mod):
     rng = np.random.default_rng(5)
     n = oracle_mod.mlp_param_count()
-    assert n == 8 * 128 + 128 + 2 * (128 * 128 + 128) + 128 + 1
+    assert n == 8 * 64 + 64 + 2 * (64 * 64 + 64) + 64 + 1
     p = (rng.standard_normal(n) * 0.2).astype(np.float32)
     X = rng.standard_normal((6, 8)).astype(np.float32)
     y = rng.standard_normal(6).astype(np.float32)
