@@ -100,12 +100,13 @@ class Clocks:
     def __init__(self, gpu_index):
         self.idx = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % gpu_index)
+        self.path = None
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.fh = open(self.path, "w")
+            import tempfile
+            fd, self.path = tempfile.mkstemp(prefix="sonar_clocks_rank%d_" % self.idx, suffix=".csv")
+            self.fh = os.fdopen(fd, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.fh,
                                          stderr=subprocess.DEVNULL)
@@ -137,6 +138,10 @@ class Clocks:
                     reasons.add(n)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
                 "reasons": sorted(reasons)}
 
@@ -439,6 +444,151 @@ def batch_leg(args, flush, rank):
     return res
 
 
+def sum_roofline(stats, hop, fp32_peak, mufu_peak, name):
+    """FP32 + MUFU roofline of one hop's sum kernel (k_sum: 40 flop + 3 MUFU
+    per ordered pair): algorithmic flop per launch over its event time."""
+    hs = [h for h in stats["hops"] if h["hop"] == hop and h["sum_ms"] > 0]
+    if not hs or not (fp32_peak > 0 and mufu_peak > 0):
+        return None
+    pairs = sum(h["pairs"] for h in hs) / len(hs)
+    ms = sum(h["sum_ms"] for h in hs) / len(hs)
+    roof = min(fp32_peak / FLOP_PER_PAIR, mufu_peak / SFU_PER_PAIR)
+    ach = pairs * FLOP_PER_PAIR / (ms * 1e-3) / 1e12
+    peak = roof * FLOP_PER_PAIR / 1e12
+    return {"kernel": name, "bound": "fp32+sfu", "achieved": round(ach, 3), "peak": round(peak, 3),
+            "unit": "TFLOP/s", "frac": round(ach / peak, 4), "traffic": None, "pairs_per_launch": int(pairs),
+            "launch_ms": round(ms, 4),
+            "peak_source": "measured now by sonar_measure_peak: FP32 %.1f TFLOP/s, MUFU %.2f Top/s; roofline = "
+                           "min(FP32/40, MUFU/3) pairs/s x 40 flop" % (fp32_peak / 1e12, mufu_peak / 1e12)}
+
+
+def mask_roofline(stats, hop, name):
+    """The mask kernel against HBM at its algorithmic 0.125 B (one bit) per
+    candidate pair: how far the shadow tests keep it from the bandwidth
+    bound."""
+    hs = [h for h in stats["hops"] if h["hop"] == hop and h["mask_ms"] > 0]
+    if not hs:
+        return None
+    pairs = sum(h["pairs"] for h in hs) / len(hs)
+    ms = sum(h["mask_ms"] for h in hs) / len(hs)
+    peak, src = hbm_peak()
+    ach = pairs * 0.125 / (ms * 1e-3) / 1e9
+    return {"kernel": name, "bound": "hbm (algorithmic bit per pair); shadow tests make it ALU/issue-bound",
+            "achieved": round(ach, 1), "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": None,
+            "launch_ms": round(ms, 4), "pairs_per_launch": int(pairs), "peak_source": src}
+
+
+def config_leg(api, name, args, flush, local, world, rank):
+    """One of the other benchmark configurations on the plain FP32 path:
+    device-timed steps (masks rebuilt every step, L2 flushed between steps),
+    pairs/s, kernel times, the dominant kernels' rooflines, error vs the
+    FP64 oracle on seeded destinations and the grazing counts (rank 0).
+      sphere20   r = 1 m icosphere (5,120 triangles) at 20 kHz, source at
+                 10 m, shadowed source hop + FACET_NO_RESP onto the 512 x 512
+                 cell field plane through the centre;
+      trihedral40  trihedral at 40 kHz, source hop, 3 bounces, readout to a
+                 256 x 256 hemisphere of field points."""
+    from sonar_render_gb300 import scenes
+    if name == "sphere20":
+        cfg = scenes.sphere_config(512, field_surface=True)
+    else:
+        cfg = scenes.trihedral_config(40e3, bounces=3, n_theta=256, n_phi=256)
+    set_path(api, False, 0)
+    load_scene(api, cfg)
+
+    import types
+    A = types.SimpleNamespace(steps=max(3, min(args.steps, 10)), warmup=3)
+    times, stats, clk = time_path(api, cfg, A, flush, local, world)
+    total_ms = max_over_ranks(float(sum(times)), world)
+    pairs_step = step_pairs(stats) / A.steps
+    kms = {k: round(v, 4) for k, v in kernel_times(stats, A.steps).items()}
+    fp32_peak, mufu_peak = api.measure_peak(0), api.measure_peak(1)
+    res = {"workload": cfg["name"], "value": job_value(pairs_step, A.steps, world, total_ms), "unit": UNIT,
+           "ms_per_step": round(total_ms / A.steps, 4), "steps": A.steps, "warmup": A.warmup,
+           "pairs_per_step": pairs_step, "kernel_ms_per_step": kms, "clocks": clk,
+           "l2": "flushed between steps (256 MB write)", "dtype": "fp32"}
+    if name == "sphere20":
+        res["roofline_sum"] = sum_roofline(stats, 3, fp32_peak, mufu_peak, "k_sum<NORESP> (sphere -> field plane)")
+        res["roofline_mask"] = mask_roofline(stats, 3, "k_mask<NORESP> (sphere -> field plane, shadowed)")
+    else:
+        roof, _ = sym_roofline(api, [h for h in stats["hops"] if h["hop"] == 2])
+        res["roofline_bounce_sum"] = roof
+        res["roofline_readout"] = sum_roofline(stats, 1, fp32_peak, mufu_peak, "k_sum<FP> (readout)")
+    res["dominant_kernel"] = max(kms, key=kms.get) if kms else None
+    if rank == 0:
+        res.update(config_error(api, cfg, name))
+    api.TearDownCuda()
+    return res
+
+
+def config_error(api, cfg, name):
+    """Errors vs the FP64 oracle of the configuration legs on seeded
+    destinations, each hop given the GPU's own input, and grazing counts."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    try:
+        load_scene(api, cfg)
+        api.project_source_points_to_objects(False)
+        P0 = api.get_object_pressures(api.TARGET, 0)
+        o = O.Oracle()
+        o.set_initial_conditions(cfg["cp"], cfg["frequency"], cfg.get("attenuation", 0.0))
+        for tris, d in cfg["targets"]:
+            o.load_geometry(tris, 0, d)
+        for tris, d in cfg.get("fields", []):
+            o.load_geometry(tris, 2, d)
+        o.load_source_points(cfg["sources"])
+        if cfg.get("field_points") is not None:
+            o.load_field_points(cfg["field_points"])
+        o.render()
+        rng = np.random.default_rng(7)
+        act = o.active(0, 0)
+        e, g = {}, {}
+        cs = np.sort(rng.choice(o.ncells(0, 0), 1024, replace=False))
+        v0, m0 = o.hop_subset(0, 0, 0, cs, want_mask=True, nsrc=1)
+        e["source_hop"] = float(np.linalg.norm(P0[cs] - v0) / np.linalg.norm(v0))
+        g["source_hop_grazing"] = int(((m0 & 2) != 0).sum())
+        if name == "sphere20":
+            api.project_target_to_field_objects()
+            F = api.get_object_pressures(api.FIELD, 0)
+            actf = o.active(2, 0)
+            q = np.sort(rng.choice(len(actf), 256, replace=False))
+            o.set_pressures(0, 0, P0)
+            v, m = o.hop_subset(3, 0, 0, q, want_mask=True, nsrc=len(act))
+            c = o.counters()
+            e["field_surface"] = float(np.linalg.norm(F[actf[q]] - v) / np.linalg.norm(v))
+            g.update({"field_surface_pairs_checked": c["pairs"], "field_surface_grazing": c["grazing"],
+                      "destinations_checked": len(q)})
+        else:
+            outs = [P0]
+            tot = [P0]
+            for nb in (1, 2, 3):
+                load_scene(api, cfg)
+                api.project_source_points_to_objects(False)
+                api.project_target_to_target_objects(nb)
+                tot.append(api.get_object_pressures(api.TARGET, 0))
+                outs.append(tot[-1] - tot[-2])
+            api.project_target_to_field_points()
+            fp = api.get_field_point_pressures(len(cfg["field_points"]))
+            q = np.sort(rng.choice(len(act), 32, replace=False))
+            for k in (1, 2, 3):
+                v, m = o.hop_subset(2, 0, 0, q, pin=outs[k - 1], want_mask=(k == 1), nsrc=len(act))
+                e["bounce%d" % k] = float(np.linalg.norm(outs[k][act[q]] - v) / np.linalg.norm(v))
+                if k == 1:
+                    c = o.counters()
+                    g.update({"bounce_pairs_checked": c["pairs"], "bounce_grazing": c["grazing"]})
+            o.set_pressures(0, 0, tot[3])
+            jj = np.sort(rng.choice(len(cfg["field_points"]), 256, replace=False))
+            vf, mf = o.hop_subset(1, 0, 0, jj, want_mask=True, nsrc=len(act))
+            c = o.counters()
+            e["readout"] = float(np.linalg.norm(fp[jj] - vf) / np.linalg.norm(vf))
+            g.update({"readout_pairs_checked": c["pairs"], "readout_grazing": c["grazing"]})
+        o.close()
+        api.TearDownCuda()
+        return {"rel_err_vs_fp64": e, "grazing": g}
+    except Exception as ex:
+        return {"rel_err_vs_fp64": {"failed": str(ex)}}
+
+
 def batch_error(cfg, out, st):
     """Relative L2 error of sampled (scene, frequency) items, 4 sources each,
     against the FP64 oracle's per-source runs."""
@@ -588,6 +738,10 @@ def run_gb300(args):
         _, lr_alone, _ = time_path(api, cfg, args, flush, local, world, reuse=True)
         api.set_option("overlap_streams", OVERLAP[0])
     batch_res = batch_leg(args, flush, rank) if args.batch else None
+    legs = {}
+    for leg in [x for x in args.configs.split(",") if x]:
+        legs[leg] = config_leg(api, leg, args, flush, local, world, rank)
+    load_scene(api, cfg)
     f2f_plain = [h for h in res.get("plain", res[modes[0]])["stats"]["hops"] if h["hop"] == 2]
     roof_sym, fp32_peak = sym_roofline(api, f2f_plain)
 
@@ -671,6 +825,7 @@ def run_gb300(args):
         "cpu_baseline": cpu, "e2e": H["e2e"], "clocks": H["clocks"], "gpu_launches": int(H["launches_per_step"] * args.steps),
         "rel_err_vs_fp64": errs.get(head), "grazing": errs.get("grazing"),
         "batch_config": batch_res,
+        "config_sphere20": legs.get("sphere20"), "config_trihedral40_3b": legs.get("trihedral40"),
         "operator_reuse": dict(reuse, note="masks and compressed blocks built once per target and reused by every "
                                            "step (not the headline: the headline rebuilds them every step)"),
     }
@@ -855,6 +1010,9 @@ def main():
                     help="file (.npy) for the trained network's parameters: loaded when present, else written")
     ap.add_argument("--batch", type=int, default=1,
                     help="also run the many-source, many-frequency batch configuration (0: skip)")
+    ap.add_argument("--configs", default="sphere20,trihedral40",
+                    help="other configurations timed beside the headline (comma list of sphere20, trihedral40; "
+                         "empty: none)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

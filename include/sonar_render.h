@@ -186,6 +186,11 @@ double sonar_measure_peak(int which);
  * dstIdx != srcIdx.  Returns the number of bytes (ndst*nsrc), or < 0.  The
  * mask is built if needed. */
 long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, long long cap);
+/* The same for the destination rows rows[0..nrows) only (indices in the
+ * order sonar_get_mask uses), row q at out[q * nsrc]: for masks too large to
+ * export whole.  Returns nrows * nsrc, or < 0. */
+long long sonar_get_mask_rows(int hop, int srcIdx, int dstIdx, const int *rows, int nrows, unsigned char *out,
+                              long long cap);
 
 /* Host only (no GPU needed): frame and clipped area grid of one triangle
  * (src/Facet.cpp:6-339).  nx_ny_neg gets numXpnts, numYpnts,
@@ -275,15 +280,24 @@ int sonar_run_batch(const float *tris, const int *scene_tri_off, int nscenes, co
  * ((float)(2 pi f) / c and the attenuation).  The work is queued on `stream`
  * (a cudaStream_t, NULL for the default stream); the call does not wait.
  *
+ * Every buffer must start on a 16-byte boundary (the kernels read them as
+ * float4 / double2 vectors): a caller's sub-allocation or slice at another
+ * offset is refused with SONAR_NOALLOC_EINVAL.  The cosine gate is decided
+ * with the reference's FP32 rounding, as in the library's own readout.
+ *
  * Its only working memory is a fixed 8 MiB device array inside this library
  * (held by every GPU that loads it, until the process exits), so n_points is
  * limited to SONAR_NOALLOC_MAX_POINTS.  The array's address is looked up on
- * the first call made on each device; make that first call before any stream
- * capture begins.  All calls share the array: calls whose work overlaps on the
- * GPU (e.g. on two streams at once) race and give wrong results.
- * Returns 0, SONAR_NOALLOC_EINVAL (bad size or null pointer),
+ * the first call made in each CUDA context; make that first call before any
+ * stream capture begins.  A context destroyed and re-created (cudaDeviceReset)
+ * invalidates the cached address; the next call looks it up again, so that
+ * call too must come before any capture.  All calls share the array: calls
+ * whose work overlaps on the GPU (e.g. on two streams at once) race and give
+ * wrong results.
+ * Returns 0, SONAR_NOALLOC_EINVAL (bad size, null or misaligned pointer),
  * SONAR_NOALLOC_ETOOBIG (n_points above the maximum) or SONAR_NOALLOC_ECUDA
- * (device lookup or launch failed; a line goes to stderr). */
+ * (device lookup or launch failed, or a CUDA error from the caller's own
+ * work was already pending -- it is left pending; a line goes to stderr). */
 #define SONAR_NOALLOC_MAX_POINTS 524288
 #define SONAR_NOALLOC_EINVAL (-1)
 #define SONAR_NOALLOC_ETOOBIG (-2)

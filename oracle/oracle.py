@@ -48,9 +48,14 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_ref() -> str | None:
+# where the reference's sources lie in the build container (absent on the GPU
+# machines, which use the harness built beforehand or none)
+REFERENCE_ROOT = os.environ.get("SONAR_REFERENCE_ROOT", "/root/reference")
+
+
+def build_ref(root: str | None = None) -> str | None:
     """Build the reference harness where the reference sources exist."""
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")])
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), root or REFERENCE_ROOT])
     return REF_LIB if os.path.exists(REF_LIB) else None
 
 

@@ -81,6 +81,9 @@ def load_library(path: str | None = None, build: bool = False):
     L.sonar_set_option.argtypes = [C.c_char_p, C.c_double]
     L.sonar_get_mask.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_ubyte), C.c_longlong]
     L.sonar_get_mask.restype = C.c_longlong
+    L.sonar_get_mask_rows.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_ubyte),
+                                      C.c_longlong]
+    L.sonar_get_mask_rows.restype = C.c_longlong
     L.sonar_get_stream.restype = C.c_void_p
     L.sonar_get_surface_colours.argtypes = [C.c_int, C.c_int, _f, C.c_longlong]
     L.sonar_measure_peak.argtypes = [C.c_int]
@@ -255,6 +258,23 @@ def get_mask(hop, src_idx, dst_idx):
     if r < 0:
         raise SonarError("sonar_get_mask failed (%d)" % r)
     return out[:n]
+
+
+def get_mask_rows(hop, src_idx, dst_idx, rows):
+    """Rows of the interaction mask, (len(rows), nsrc) uint8 (see
+    sonar_get_mask_rows)."""
+    L = lib()
+    rows = np.ascontiguousarray(np.asarray(rows, dtype=np.int32))
+    rp = rows.ctypes.data_as(C.POINTER(C.c_int))
+    n = L.sonar_get_mask_rows(int(hop), int(src_idx), int(dst_idx), rp, len(rows), None, 0)
+    _check()
+    out = np.zeros(max(n, 1), np.uint8)
+    r = L.sonar_get_mask_rows(int(hop), int(src_idx), int(dst_idx), rp, len(rows),
+                              out.ctypes.data_as(C.POINTER(C.c_ubyte)), n)
+    _check()
+    if r < 0:
+        raise SonarError("sonar_get_mask_rows failed (%d)" % r)
+    return out[:n].reshape(len(rows), -1)
 
 
 def stats():

@@ -355,6 +355,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
     tc_fence_after();
     const uint32_t tmem = tmem_base;
     uint32_t commits0 = 0, commits1 = 0;  // commits issued on each stage's barrier
+    int last_st = -1;                     // stage of the most recent commit
     int local = 0;                        // chunks this CTA has generated
     bool ok = true;
     while (sg < g1 && ok) {
@@ -402,6 +403,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
         }
         if (st) ++commits1;
         else ++commits0;
+        last_st = st;
         ++local;
         if (cc + 1 == seg.z) {
             // ---- segment end: the accumulator -> FP32 partial [128][64]
@@ -427,11 +429,23 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
         seg = nseg;
         it = nit;
     }
-    if (!ok && tid == 0) atomicExch(a.status, 1);
+    // After a timed-out wait, MMAs committed earlier may still be writing the
+    // accumulator and reading the operand stages.  tcgen05 operations of one
+    // thread complete in issue order, so once the most recent commit has
+    // arrived nothing is in flight: wait for it (bounded again) before the
+    // tensor memory is released.  If that wait runs out as well, the tensor
+    // memory is left allocated rather than released under a running MMA, and
+    // the status says so (2).
+    bool drained = true;
+    if (!ok && last_st >= 0) {
+        const uint32_t c = last_st ? commits1 : commits0;
+        drained = __syncthreads_and(mbar_wait(&bar[last_st], (c - 1) & 1u));
+    }
+    if (!ok && tid == 0) atomicExch(a.status, drained ? 1 : 2);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+    if (warp == 0 && drained) tmem_dealloc(tmem, kTmemCols);
 }
 
 // out[item][p][q] = sum over the item's segments, fixed order, FP64.  Grid

@@ -297,7 +297,9 @@ void check_status(Plan &p)
     int st = 0;
     BCK(cudaMemcpyAsync(&st, p.d_status, sizeof(int), cudaMemcpyDeviceToHost, p.stream));
     BCK(cudaStreamSynchronize(p.stream));
-    if (st != 0) bfail(-11, "batch: a CTA gave up waiting for the tensor core (status %d)", st);
+    if (st != 0)
+        bfail(-11, "batch: a CTA gave up waiting for the tensor core (status %d%s)", st,
+              st == 2 ? ": its tensor memory was left allocated because an MMA was still in flight" : "");
 }
 
 // Time the candidate tile shapes on this plan's items and keep the fastest.

@@ -2613,6 +2613,20 @@ __global__ void k_mask_export(MaskView m, int nsrc, int ndst, uint8_t *out)
     for (int b = 0; b < bmax; ++b) out[(long long)j * nsrc + w * 32 + b] = (word >> b) & 1u;
 }
 
+// the rows rows[0..nrows) of the mask (internal destination indices) as
+// bytes, row q at out[q * nsrc]
+__global__ void k_mask_export_rows(MaskView m, int nsrc, const int *rows, int nrows, uint8_t *out)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)nrows * m.nwords;
+    if (idx >= total) return;
+    const int q = (int)(idx / m.nwords);
+    const int w = (int)(idx % m.nwords);
+    const uint32_t word = m.bits[(long long)w * m.pitch + rows[q]];
+    const int bmax = min(32, nsrc - w * 32);
+    for (int b = 0; b < bmax; ++b) out[(long long)q * nsrc + w * 32 + b] = (word >> b) & 1u;
+}
+
 inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 // ---------------------------------------------------------------- peaks
@@ -2892,6 +2906,12 @@ void launch_mask_export(const MaskView &m, int nsrc, int ndst, uint8_t *out, cud
 {
     const long long total = (long long)ndst * m.nwords;
     if (total > 0) k_mask_export<<<blocks_for(total, 256), 256, 0, s>>>(m, nsrc, ndst, out);
+}
+
+void launch_mask_export_rows(const MaskView &m, int nsrc, const int *rows, int nrows, uint8_t *out, cudaStream_t s)
+{
+    const long long total = (long long)nrows * m.nwords;
+    if (total > 0) k_mask_export_rows<<<blocks_for(total, 256), 256, 0, s>>>(m, nsrc, rows, nrows, out);
 }
 
 }  // namespace sonar

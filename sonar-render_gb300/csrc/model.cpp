@@ -1764,6 +1764,69 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
     return st != 0 ? st : nbytes;
 }
 
+long long sonar_get_mask_rows(int hop, int srcIdx, int dstIdx, const int *rows, int nrows, unsigned char *out,
+                              long long cap)
+{
+    long long nbytes = 0;
+    int st = guarded([&] {
+        need_render();
+        if (hop < HOP_SRC || hop > HOP_RESP) fail(-6, "invalid hop %d", hop);
+        if (nrows < 0 || (nrows > 0 && !rows)) fail(-6, "invalid row list");
+        HopSets hs = hop_sets(hop, srcIdx, dstIdx);
+        nbytes = (long long)hs.nsrc * nrows;
+        if (!out) return;
+        if (cap < nbytes) fail(-8, "mask buffer holds %lld of %lld bytes", cap, nbytes);
+        if (nbytes == 0) return;
+        auto canon = [](const Object &o) {
+            std::vector<int> idx(o.act_cell.size()), rank(o.act_cell.size());
+            for (size_t q = 0; q < idx.size(); q++) idx[q] = (int)q;
+            std::sort(idx.begin(), idx.end(), [&](int x, int y) { return o.act_cell[x] < o.act_cell[y]; });
+            for (size_t k = 0; k < idx.size(); k++) rank[idx[k]] = (int)k;
+            return rank;
+        };
+        std::vector<int> rs, rd;  // internal index -> canonical index (empty: identity)
+        if (hop == HOP_FP || hop == HOP_F2F || hop == HOP_NORESP || hop == HOP_RESP) rs = canon(get(OBJ_TARGET, srcIdx));
+        if (hop == HOP_F2F) rd = rs;
+        if (hop == HOP_RESP) rd = canon(get(OBJ_TARGET, dstIdx));
+        if (hop == HOP_FP) rd = g.fp_order;
+        if (hop == HOP_NORESP) rd = canon(get(OBJ_FIELD, dstIdx));
+        // canonical destination -> internal row
+        std::vector<int> inv(hs.ndst);
+        for (int jd = 0; jd < hs.ndst; jd++) inv[rd.empty() ? jd : rd[jd]] = jd;
+        std::vector<int> irow(nrows);
+        for (int q = 0; q < nrows; q++) {
+            if (rows[q] < 0 || rows[q] >= hs.ndst) fail(-6, "row %d outside [0, %d)", rows[q], hs.ndst);
+            irow[q] = inv[rows[q]];
+        }
+        MaskEntry M = build_mask(hop, srcIdx, dstIdx, 1);
+        uint8_t *d = nullptr;
+        int *drows = nullptr;
+        cudaError_t e = pool_alloc((void **)&d, (size_t)nbytes, g.stream);
+        if (e == cudaSuccess) e = pool_alloc((void **)&drows, sizeof(int) * (size_t)nrows, g.stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(drows, irow.data(), sizeof(int) * (size_t)nrows, cudaMemcpyHostToDevice, g.stream);
+        if (e == cudaSuccess) {
+            launch_mask_export_rows(M.view, M.nsrc, drows, nrows, d, g.stream);
+            e = cudaGetLastError();
+        }
+        std::vector<uint8_t> tmp((size_t)nbytes);
+        if (e == cudaSuccess) e = stage_to_host(tmp.data(), d, (size_t)nbytes, g.stream);
+        dfree(d);
+        dfree(drows);
+        M.free_device();
+        if (e != cudaSuccess) fail(-10, "mask export failed: %s", cudaGetErrorString(e));
+        for (int q = 0; q < nrows; q++) {
+            const uint8_t *row = tmp.data() + (size_t)q * M.nsrc;
+            uint8_t *orow = out + (size_t)q * M.nsrc;
+            if (rs.empty())
+                memcpy(orow, row, (size_t)M.nsrc);
+            else
+                for (long long js = 0; js < M.nsrc; js++) orow[rs[js]] = row[js];
+        }
+    });
+    return st != 0 ? st : nbytes;
+}
+
 int sonar_render_image(int width, int height, const float *viewSettings, unsigned char *rgb)
 {
     return guarded([&] { render_image(width, height, viewSettings, rgb); });

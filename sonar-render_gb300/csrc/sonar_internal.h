@@ -125,6 +125,7 @@ void launch_finalize_add(const double2 *partial, int nsplit, int ndst, const int
 void launch_finalize_f2f(const double2 *partial, int nsplit, int ndst, const int *cell, double2 *Pout,
                          double2 *P, cudaStream_t s);
 void launch_mask_export(const MaskView &m, int nsrc, int ndst, uint8_t *out, cudaStream_t s);
+void launch_mask_export_rows(const MaskView &m, int nsrc, const int *rows, int nrows, uint8_t *out, cudaStream_t s);
 // FACET_SELF with reciprocity: one Green's function per unordered pair, over
 // a work list of the non-empty upper blocks cut into chunks of `per` blocks
 // of one destination row.  colpart holds 256 * ntiles * (ntiles - 1) / 2

@@ -275,10 +275,10 @@ def hemisphere(n_theta, n_phi, radius, axis=(1.0, 1.0, 1.0), center=(0.0, 0.0, 0
 
 
 # ---------------------------------------------------------------- workloads
-def plate_config():
+def plate_config(frequency=10e3):
     """Plate, 10 kHz, source at (0, 0, 5), 64 x 64 field points at z = 3."""
-    f = 10e3
-    return dict(name="plate_1x0.5m_10kHz", frequency=f, cp=CP_WATER, attenuation=0.0,
+    f = float(frequency)
+    return dict(name="plate_1x0.5m_%dkHz" % int(f / 1e3), frequency=f, cp=CP_WATER, attenuation=0.0,
                 targets=[(plate_1x05(), delta_for(f))], fields=[],
                 sources=np.array([[0.0, 0.0, 5.0]], np.float32),
                 field_points=grid_xy(64, 1.0, 3.0), bounces=0)
