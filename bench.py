@@ -993,9 +993,10 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
     ap.add_argument("--mode", default="both", choices=["both", "plain", "compressed"])
-    ap.add_argument("--aca-variant", type=int, default=0, choices=(0, 1, 2),
+    ap.add_argument("--aca-variant", type=int, default=0, choices=tuple(range(7)),
                     help="cross-approximation kernel: 0 = 8 factor ranks in shared memory, 4 CTAs per SM; "
-                         "1 = 12 ranks, 4 CTAs; 2 = 16 ranks, 3 CTAs")
+                         "1 = 12 ranks, 4 CTAs; 2 = 16 ranks, 3 CTAs; panel form (4 pivot rows per step): "
+                         "3 = 8 ranks, 3 CTAs; 4 = 8 ranks, 2 CTAs; 5 = 4 ranks, 4 CTAs; 6 = 8 ranks, 4 CTAs")
     ap.add_argument("--overlap", type=int, default=1, choices=(0, 1),
                     help="compressed bounce: low-rank apply on a second stream beside the dense remainder")
     ap.add_argument("--tol", type=float, default=5e-4,

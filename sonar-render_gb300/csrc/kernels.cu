@@ -2105,6 +2105,7 @@ __device__ __forceinline__ float2 lr_entry(const SumArgs &a, int cls, bool bit, 
 
 
 constexpr int kAcaMaxZeroRows = 48;
+constexpr int kLrMaxRank = 64;
 constexpr int kAcaWarps = kTile / 32;
 
 // Block-wide argmax (ARG) of v >= 0 over the threads with valid set and
@@ -2310,6 +2311,408 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *bloc
     }
 }
 
+// Low-rank apply of one accepted block of rank k, by the whole CTA: tv =
+// V^T w_I and su = U^T w_J (warp w takes the ranks m = w (mod 8), each lane 8
+// rows, one warp reduction per rank; one barrier), then the block's forward
+// terms U tv (rows of J) and reciprocal terms V su (columns of I) into its
+// output slots brow_b, bcol_b (FP32).  The weights w are the packed inputs
+// (srcA.w, srcB.w).  sW holds kTile float4, sTv and sSu kLrMaxRank float2.
+// Starts with a barrier (the caller may reuse the shared arrays).
+__device__ __forceinline__ void lr_block_apply(const SumArgs &a, int I, int J, const float2 *U0, const float2 *V0,
+                                               int k, float2 *brow_b, float2 *bcol_b, float4 *sW, float2 *sTv,
+                                               float2 *sSu)
+{
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int i = I * kTile + t, j = J * kTile + t;
+    __syncthreads();
+    sW[t] = make_float4(i < a.nsrc ? a.srcA[i].w : 0.0f, i < a.nsrc ? a.srcB[i].w : 0.0f,
+                        j < a.nsrc ? a.srcA[j].w : 0.0f, j < a.nsrc ? a.srcB[j].w : 0.0f);
+    const float2 *Ub = U0 + t, *Vb = V0 + t;
+    __syncthreads();
+    for (int m = warp; m < k; m += kTile / 32) {
+        float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+        for (int r = 0; r < kTile / 32; ++r) {
+            const int tt = lane + 32 * r;
+            const float2 v = V0[(size_t)m * kTile + tt], u = U0[(size_t)m * kTile + tt];
+            const float4 w = sW[tt];
+            p.x = fmaf(v.x, w.x, fmaf(-v.y, w.y, p.x));
+            p.y = fmaf(v.x, w.y, fmaf(v.y, w.x, p.y));
+            p.z = fmaf(u.x, w.z, fmaf(-u.y, w.w, p.z));
+            p.w = fmaf(u.x, w.w, fmaf(u.y, w.z, p.w));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            p.x += __shfl_xor_sync(0xffffffffu, p.x, o);
+            p.y += __shfl_xor_sync(0xffffffffu, p.y, o);
+            p.z += __shfl_xor_sync(0xffffffffu, p.z, o);
+            p.w += __shfl_xor_sync(0xffffffffu, p.w, o);
+        }
+        if (lane == 0) {
+            sTv[m] = make_float2(p.x, p.y);
+            sSu[m] = make_float2(p.z, p.w);
+        }
+    }
+    __syncthreads();
+    float rr = 0.0f, ri = 0.0f, cr = 0.0f, ci = 0.0f;
+    // the factors come back from L2: several ranks' loads in flight at once
+#pragma unroll 4
+    for (int m = 0; m < k; ++m) {
+        const float2 u = Ub[m * kTile], v = Vb[m * kTile], c = sTv[m], e = sSu[m];
+        rr += u.x * c.x - u.y * c.y;
+        ri += u.x * c.y + u.y * c.x;
+        cr += v.x * e.x - v.y * e.y;
+        ci += v.x * e.y + v.y * e.x;
+    }
+    brow_b[t] = make_float2(rr, ri);
+    bcol_b[t] = make_float2(cr, ci);
+}
+
+// ---------------------------------------------------------------- panel cross approximation
+// The same approximation taken kPanel pivot rows at a time.  A panel step
+//   A. computes the residual rows of the panel's kPanel rows (every thread
+//      its column t of each: kPanel Green's entries and one pass over the
+//      earlier ranks, each factor entry V(t, m) loaded once for all rows);
+//   B. chooses the panel's pivot columns greedily: row q's pivot column is
+//      the argmax of its residual after the elimination of the panel's
+//      earlier rows (one block argmax per row, the panel rows exchanged
+//      through a shared buffer); v_q = that row / its pivot;
+//   C. computes the residual columns at the chosen columns (every thread its
+//      row t: kPanel entries, one pass over the earlier ranks) and eliminates
+//      the panel's earlier ranks from them: u_q;
+//   then one block reduction carries the 2 kPanel norms of the new ranks and,
+//   per new rank, the argmax of |u_q| over unused rows: the next panel's rows
+//   (duplicates dropped).  The stopping rule is the classic one, applied rank
+//   by rank in the panel's order; ranks past the stop are discarded.  Rows of
+//   a panel that vanish (masked rows) give no rank; a panel without any
+//   continues with the lowest unused row alone.  Per rank this takes
+//   (kPanel + 2) / kPanel barriers instead of two, loads each own factor entry
+//   once per panel instead of once per rank, and evaluates kPanel independent
+//   entries at a time.  Factor layout, judge and outputs are those of k_aca.
+constexpr int kPanel = 4;
+
+// Warp sums of eight values per lane with nine shuffles: at each level a lane
+// keeps the half of its partial sums that its partner does not and adds the
+// partner's copy of them.  Returns the warp total of value (lane >> 2) & 7.
+__device__ __forceinline__ float warp_sum8(const float (&x)[8], int lane)
+{
+    const bool h4 = (lane >> 4) & 1, h3 = (lane >> 3) & 1, h2 = (lane >> 2) & 1;
+    float y[4], z[2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float keep = h4 ? x[4 + i] : x[i], send = h4 ? x[i] : x[4 + i];
+        y[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const float keep = h3 ? y[2 + i] : y[i], send = h3 ? y[i] : y[2 + i];
+        z[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    const float keep = h2 ? z[1] : z[0], send = h2 ? z[0] : z[1];
+    float w = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    w += __shfl_xor_sync(0xffffffffu, w, 2);
+    w += __shfl_xor_sync(0xffffffffu, w, 1);
+    return w;
+}
+
+// 32-bit argmax key of v >= 0 at index idx < 256 (0: not a candidate): the
+// float bits with the low byte replaced by 255 - idx, as in cta_reduce
+__device__ __forceinline__ unsigned argmax_key(float v, int idx, bool valid)
+{
+    return valid ? ((__float_as_uint(fmaxf(v, 0.0f)) + 0x100u) & 0xFFFFFF00u) | (255u - (unsigned)idx) : 0u;
+}
+
+__device__ __forceinline__ unsigned max8(const unsigned *slot)
+{
+    const uint4 a = reinterpret_cast<const uint4 *>(slot)[0], b = reinterpret_cast<const uint4 *>(slot)[1];
+    return max(max(max(a.x, a.y), max(a.z, a.w)), max(max(b.x, b.y), max(b.z, b.w)));
+}
+
+__device__ __forceinline__ float key_value(unsigned w) { return w ? __uint_as_float((w & 0xFFFFFF00u) - 0x100u) : -1.0f; }
+
+// mask bit of pair (row j of tile J, column i of tile I) of a BITS block
+__device__ __forceinline__ bool block_bit(const uint32_t *bw, long long pitch, int j, int i)
+{
+    return (bw[(long long)(i >> 5) * pitch + j] >> (i & 31)) & 1u;
+}
+
+// brow, bcol (optional): the low-rank apply of every accepted block with the
+// packed inputs of this launch, fused (lr_block_apply into slot b).
+template <bool ATT, int RS, int MINB>
+__global__ void __launch_bounds__(kTile, MINB) k_aca_panel(SumArgs a, const int2 *blocks, const uint8_t *cls,
+                                                           const int *cap, const long long *off, int nblocks,
+                                                           float tol, float limit, float2 *U, float2 *V, int *rank,
+                                                           float *fro, float *err, float2 *brow, float2 *bcol)
+{
+    extern __shared__ float2 aca_smem[];  // sU[RS][kTile], then sV[RS][kTile]
+    float2 *sU = aca_smem, *sV = aca_smem + RS * kTile;
+    __shared__ float2 sE[2][kPanel][kTile];  // panel rows during the column choice, by step parity
+    __shared__ __align__(16) unsigned sKey[2][kAcaWarps];
+    __shared__ __align__(16) unsigned sRowKey[kPanel][kAcaWarps];
+    __shared__ __align__(16) float sSum[kAcaWarps][2 * kPanel];
+    __shared__ float2 sumB[kAcaWarps];
+    const int t = threadIdx.x, b = blockIdx.x, lane = t & 31, warp = t >> 5;
+    if (b >= nblocks) return;  // CTA-uniform
+    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = min(cap[b], kLrRankLimit);
+    const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
+    const float4 *PI = a.srcA + I * kTile, *NI = a.srcB + I * kTile, *PJ = a.srcA + J * kTile, *NJ = a.srcB + J * kTile;
+    float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
+    const uint32_t *bw = a.mask.bits + (long long)I * kWordsPerTile * a.mask.pitch + (long long)J * kTile;
+    const long long pitch = a.mask.pitch;
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float2 z2 = make_float2(0.0f, 0.0f);
+    const bool coli = t < ni, rowj = t < nj;
+    const float4 pi = coli ? __ldg(PI + t) : z4, qi = coli ? __ldg(NI + t) : z4;
+    const float4 pj = rowj ? __ldg(PJ + t) : z4, qj = rowj ? __ldg(NJ + t) : z4;
+    bool colused = !coli, rowused = !rowj;
+    // the first panel's rows spread over the tile
+    int rows[kPanel];
+    int nr = 0;
+#pragma unroll
+    for (int q = 0; q < kPanel; ++q) {
+        rows[q] = (q * nj) / kPanel;  // distinct when nj >= kPanel
+        if (q == 0 || rows[q] != rows[q - 1]) nr = q + 1;
+    }
+    if (nj < kPanel) nr = nj;  // rows 0 .. nj - 1
+    int k = 0, zero_rows = 0;
+    float norm2 = 0.0f;
+    bool done = nr == 0;
+    while (!done && k < K) {
+        // ---- A. residual rows of the panel at column t
+        float2 e[kPanel];
+#pragma unroll
+        for (int q = 0; q < kPanel; ++q) e[q] = z2;
+        if (coli) {
+#pragma unroll
+            for (int q = 0; q < kPanel; ++q)
+                if (q < nr) {
+                    const int r = rows[q];
+                    const bool bit = bc == kFlagBits ? block_bit(bw, pitch, r, t) : true;
+                    e[q] = lr_entry<ATT>(a, bc, bit, pi, qi, __ldg(PJ + r), __ldg(NJ + r));
+                }
+            const int ks = min(k, RS);
+            for (int m = 0; m < ks; ++m) {
+                const float2 v = sV[m * kTile + t];
+#pragma unroll
+                for (int q = 0; q < kPanel; ++q)
+                    if (q < nr) e[q] = csub_mul(e[q], sU[m * kTile + rows[q]], v);
+            }
+            for (int m = RS; m < k; ++m) {
+                const float2 v = Vb[m * kTile + t];
+#pragma unroll
+                for (int q = 0; q < kPanel; ++q)
+                    if (q < nr) e[q] = csub_mul(e[q], Ub[m * kTile + rows[q]], v);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kPanel; ++q)
+            if (q < nr && t == rows[q]) rowused = true;
+        // ---- B. pivot columns, greedy within the panel
+        int cols[kPanel];
+        float2 vq[kPanel];
+        int np = 0;
+        const int room = K - k;  // ranks that still fit under the cap
+#pragma unroll
+        for (int q = 0; q < kPanel; ++q) {
+            if (q >= nr || np >= room) break;  // uniform
+            const int buf = q & 1;
+#pragma unroll
+            for (int q2 = 0; q2 < kPanel; ++q2)
+                if (q2 >= q && q2 < nr) sE[buf][q2][t] = e[q2];
+            const unsigned key = __reduce_max_sync(0xffffffffu,
+                                                   argmax_key(e[q].x * e[q].x + e[q].y * e[q].y, t, !colused));
+            if (lane == 0) sKey[buf][warp] = key;
+            __syncthreads();
+            const unsigned w = max8(sKey[buf]);
+            if (!(key_value(w) > 1e-30f)) continue;  // the row vanished: no rank from it
+            const int c = (int)(255u - (w & 0xFFu));
+            const float2 pv = sE[buf][q][c];
+            const float inv = __frcp_rn(pv.x * pv.x + pv.y * pv.y);
+            const float2 v = coli ? make_float2((e[q].x * pv.x + e[q].y * pv.y) * inv,
+                                                (e[q].y * pv.x - e[q].x * pv.y) * inv)
+                                  : z2;
+#pragma unroll
+            for (int q2 = 0; q2 < kPanel; ++q2)
+                if (q2 > q && q2 < nr) e[q2] = csub_mul(e[q2], sE[buf][q2][c], v);
+            if (t == c) colused = true;
+            const int m = k + np;
+            Vb[m * kTile + t] = v;
+            if (m < RS) sV[m * kTile + t] = v;
+#pragma unroll
+            for (int q3 = 0; q3 < kPanel; ++q3)
+                if (q3 == np) {
+                    cols[q3] = c;
+                    vq[q3] = v;
+                }
+            ++np;
+        }
+        if (np == 0) {
+            // every row of the panel vanished: continue with the lowest unused row
+            zero_rows += nr;
+            if (zero_rows > kAcaMaxZeroRows) break;
+            float f = 1.0f, d0 = 0.0f, d1 = 0.0f;
+            int nrw = t;
+            cta_reduce<true, false>(f, nrw, !rowused, d0, d1, sKey[0], nullptr);
+            if (f < 0.0f) break;
+            rows[0] = nrw;
+            nr = 1;
+            __syncthreads();  // sKey[0] is rewritten by the next panel's first step
+            continue;
+        }
+        // ---- C. residual columns at the chosen columns, row t
+        float2 u[kPanel];
+#pragma unroll
+        for (int q = 0; q < kPanel; ++q) u[q] = z2;
+        if (rowj) {
+#pragma unroll
+            for (int q = 0; q < kPanel; ++q)
+                if (q < np) {
+                    const int c = cols[q];
+                    const bool bit = bc == kFlagBits ? block_bit(bw, pitch, t, c) : true;
+                    u[q] = lr_entry<ATT>(a, bc, bit, __ldg(PI + c), __ldg(NI + c), pj, qj);
+                }
+            const int ks = min(k, RS);
+            for (int m = 0; m < ks; ++m) {
+                const float2 uu = sU[m * kTile + t];
+#pragma unroll
+                for (int q = 0; q < kPanel; ++q)
+                    if (q < np) u[q] = csub_mul(u[q], uu, sV[m * kTile + cols[q]]);
+            }
+            for (int m = RS; m < k; ++m) {
+                const float2 uu = Ub[m * kTile + t];
+#pragma unroll
+                for (int q = 0; q < kPanel; ++q)
+                    if (q < np) u[q] = csub_mul(u[q], uu, Vb[m * kTile + cols[q]]);
+            }
+            // the panel's earlier ranks: u_q -= u_q2 v_q2(c_q)
+#pragma unroll
+            for (int q = 1; q < kPanel; ++q)
+#pragma unroll
+                for (int q2 = 0; q2 < kPanel; ++q2)
+                    if (q2 < q && q < np) {
+                        const int m2 = k + q2;
+                        const float2 vc = m2 < RS ? sV[m2 * kTile + cols[q]] : Vb[m2 * kTile + cols[q]];
+                        u[q] = csub_mul(u[q], u[q2], vc);
+                    }
+        }
+#pragma unroll
+        for (int q = 0; q < kPanel; ++q)
+            if (q < np) {
+                const int m = k + q;
+                Ub[m * kTile + t] = u[q];
+                if (m < RS) sU[m * kTile + t] = u[q];
+            }
+        // ---- norms of the new ranks and the next panel's rows
+        {
+            float x[8];
+#pragma unroll
+            for (int q = 0; q < kPanel; ++q) {
+                x[2 * q] = q < np ? u[q].x * u[q].x + u[q].y * u[q].y : 0.0f;
+                x[2 * q + 1] = q < np ? vq[q].x * vq[q].x + vq[q].y * vq[q].y : 0.0f;
+            }
+            const float ws = warp_sum8(x, lane);
+            if ((lane & 3) == 0) sSum[warp][lane >> 2] = ws;
+#pragma unroll
+            for (int q = 0; q < kPanel; ++q)
+                if (q < np) {
+                    const unsigned key = __reduce_max_sync(
+                        0xffffffffu, argmax_key(u[q].x * u[q].x + u[q].y * u[q].y, t, !rowused));
+                    if (lane == 0) sRowKey[q][warp] = key;
+                }
+        }
+        __syncthreads();
+        float S[8];
+#pragma unroll
+        for (int v = 0; v < 8; ++v) S[v] = 0.0f;
+#pragma unroll
+        for (int w = 0; w < kAcaWarps; ++w) {
+            const float4 lo = reinterpret_cast<const float4 *>(sSum[w])[0];
+            const float4 hi = reinterpret_cast<const float4 *>(sSum[w])[1];
+            S[0] += lo.x; S[1] += lo.y; S[2] += lo.z; S[3] += lo.w;
+            S[4] += hi.x; S[5] += hi.y; S[6] += hi.z; S[7] += hi.w;
+        }
+        int kept = np;
+#pragma unroll
+        for (int q = 0; q < kPanel; ++q)
+            if (q < kept) {
+                const float nn = S[2 * q] * S[2 * q + 1];
+                norm2 += nn;
+                if (nn <= tol * tol * norm2) {
+                    kept = q + 1;
+                    done = true;
+                }
+            }
+        k += kept;
+        if (done) break;
+        // next rows: the argmax of |u_q| over unused rows, per new rank
+        int nn2 = 0;
+#pragma unroll
+        for (int q = 0; q < kPanel; ++q)
+            if (q < np) {
+                const unsigned w = max8(sRowKey[q]);
+                if (w) {
+                    const int r = (int)(255u - (w & 0xFFu));
+                    bool dup = false;
+#pragma unroll
+                    for (int q2 = 0; q2 < kPanel; ++q2)
+                        if (q2 < nn2 && rows[q2] == r) dup = true;
+                    if (!dup) {
+#pragma unroll
+                        for (int q3 = 0; q3 < kPanel; ++q3)
+                            if (q3 == nn2) rows[q3] = r;
+                        ++nn2;
+                    }
+                }
+            }
+        nr = nn2;
+        if (nr == 0) break;  // every row taken
+    }
+    // ---- the exact entries judge the approximation (as k_aca)
+    float e2 = 0.0f, x2 = 0.0f;
+    const bool converged = k > 0 && k < K;
+    __syncthreads();
+    if (converged) {
+        const int ks = min(k, RS);
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+            const int s = t + kTile * h2;
+            unsigned h = (unsigned)b * 2654435761u + (unsigned)s * 40503u + 12345u;
+            h ^= h >> 13;
+            h *= 0x5bd1e995u;
+            h ^= h >> 15;
+            const int jj = h2 == 0 ? t : (int)(h & 255u), ii = h2 == 0 ? (int)(h & 255u) : t;
+            if (ii < ni && jj < nj) {
+                const bool bit = bc == kFlagBits ? block_bit(bw, pitch, jj, ii) : true;
+                const float2 ex = lr_entry<ATT>(a, bc, bit, h2 == 0 ? __ldg(PI + ii) : pi, h2 == 0 ? __ldg(NI + ii) : qi,
+                                                h2 == 0 ? pj : __ldg(PJ + jj), h2 == 0 ? qj : __ldg(NJ + jj));
+                float2 ap = z2;
+                for (int m = 0; m < ks; ++m) ap = csub_mul(ap, sU[m * kTile + jj], sV[m * kTile + ii]);
+                for (int m = RS; m < k; ++m) ap = csub_mul(ap, Ub[m * kTile + jj], Vb[m * kTile + ii]);
+                e2 += (ex.x + ap.x) * (ex.x + ap.x) + (ex.y + ap.y) * (ex.y + ap.y);
+                x2 += ex.x * ex.x + ex.y * ex.y;
+            }
+        }
+    }
+    {
+        float f = 0.0f;
+        int fi = 0;
+        cta_reduce<false, true>(f, fi, false, e2, x2, nullptr, sumB);
+    }
+    const float rel = x2 > 0.0f ? sqrtf(e2 / x2) : (e2 > 0.0f ? 1.0f : 0.0f);  // the same in every thread
+    const bool accepted = converged && rel <= limit;
+    if (t == 0) {
+        rank[b] = accepted ? k : -1;
+        fro[b] = sqrtf(norm2);
+        err[b] = converged ? rel : -1.0f;
+    }
+    if (brow && accepted) {
+        // the panel buffer is free now: weights and projections of the apply
+        float4 *sW = reinterpret_cast<float4 *>(&sE[0][0][0]);
+        float2 *sTv = reinterpret_cast<float2 *>(sW + kTile), *sSu = sTv + kLrMaxRank;
+        lr_block_apply(a, I, J, Ub, Vb, k, brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv, sSu);
+    }
+}
+
 // Block descriptors of the admissibility network, one warp per block:
 // log2(1 + separation / lambda), log2(1 + radius / lambda) of both tiles, the
 // cosines of both mean normals with the separation direction and with each
@@ -2371,13 +2774,9 @@ __global__ void __launch_bounds__(128) k_block_desc(SumArgs a, const int2 *block
     }
 }
 
-constexpr int kLrMaxRank = 64;
-
-// Compressed bounce, one CTA per accepted block: tv = V^T w_I and
-// su = U^T w_J (warp partial sums, one barrier), then the block's forward
-// terms U tv (rows of J) and reciprocal terms V su (columns of I) into the
-// block's own output slots (FP32).  The factors are read from HBM once; the
-// second pass over them hits L2.
+// Compressed bounce, one CTA per accepted block q (kept block b = bidx[q]):
+// lr_block_apply into the block's output slots b.  The factors are read from
+// HBM once; the second pass over them hits L2.
 __global__ void __launch_bounds__(kTile) k_lr_block(SumArgs a, const int2 *blocks, const long long *off,
                                                     const int *bidx, int nb, const float2 *U, const float2 *V,
                                                     const int *rank, float2 *brow, float2 *bcol, const int *ndev)
@@ -2387,60 +2786,15 @@ __global__ void __launch_bounds__(kTile) k_lr_block(SumArgs a, const int2 *block
     const int q = blockIdx.x;
     if (q >= (ndev ? min(*ndev, nb) : nb)) return;
     const int b = bidx[q];
-    const int k = rank[b];
-    const int I = blocks[b].x, J = blocks[b].y, t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int i = I * kTile + t, j = J * kTile + t;
-    sW[t] = make_float4(i < a.nsrc ? a.srcA[i].w : 0.0f, i < a.nsrc ? a.srcB[i].w : 0.0f,
-                        j < a.nsrc ? a.srcA[j].w : 0.0f, j < a.nsrc ? a.srcB[j].w : 0.0f);
-    const float2 *U0 = U + off[b] * kTile, *V0 = V + off[b] * kTile;
-    const float2 *Ub = U0 + t, *Vb = V0 + t;
-    __syncthreads();
-    // projections V^T w_I and U^T w_J: warp w takes the ranks m = w (mod 8),
-    // each lane 8 rows, one warp reduction per rank
-    for (int m = warp; m < k; m += kTile / 32) {
-        float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-#pragma unroll
-        for (int r = 0; r < kTile / 32; ++r) {
-            const int tt = lane + 32 * r;
-            const float2 v = __ldg(V0 + (size_t)m * kTile + tt), u = __ldg(U0 + (size_t)m * kTile + tt);
-            const float4 w = sW[tt];
-            p.x = fmaf(v.x, w.x, fmaf(-v.y, w.y, p.x));
-            p.y = fmaf(v.x, w.y, fmaf(v.y, w.x, p.y));
-            p.z = fmaf(u.x, w.z, fmaf(-u.y, w.w, p.z));
-            p.w = fmaf(u.x, w.w, fmaf(u.y, w.z, p.w));
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            p.x += __shfl_xor_sync(0xffffffffu, p.x, o);
-            p.y += __shfl_xor_sync(0xffffffffu, p.y, o);
-            p.z += __shfl_xor_sync(0xffffffffu, p.z, o);
-            p.w += __shfl_xor_sync(0xffffffffu, p.w, o);
-        }
-        if (lane == 0) {
-            sTv[m] = make_float2(p.x, p.y);
-            sSu[m] = make_float2(p.z, p.w);
-        }
-    }
-    __syncthreads();
-    float rr = 0.0f, ri = 0.0f, cr = 0.0f, ci = 0.0f;
-    // the factors come back from L2: several ranks' loads in flight at once
-#pragma unroll 4
-    for (int m = 0; m < k; ++m) {
-        const float2 u = Ub[m * kTile], v = Vb[m * kTile], c = sTv[m], e = sSu[m];
-        rr += u.x * c.x - u.y * c.y;
-        ri += u.x * c.y + u.y * c.x;
-        cr += v.x * e.x - v.y * e.y;
-        ci += v.x * e.y + v.y * e.x;
-    }
-    brow[(size_t)q * kTile + t] = make_float2(rr, ri);
-    bcol[(size_t)q * kTile + t] = make_float2(cr, ci);
+    lr_block_apply(a, blocks[b].x, blocks[b].y, U + off[b] * kTile, V + off[b] * kTile, rank[b],
+                   brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv, sSu);
 }
 
 // Per owner tile X: rows of every accepted block with J = X and columns of
 // every accepted block with I = X, in list order, summed with compensated
 // FP32 (Kahan) arithmetic -- FP64 adds run at a small fraction of the FP32
 // rate on this GPU -- and stored as FP64 (deterministic order).  The lists
-// hold accepted-block positions q.
+// hold accepted-block positions q; their outputs sit at slot bidx[q].
 __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 {
     const float y = x - c;
@@ -2451,7 +2805,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 
 __global__ void __launch_bounds__(kTile) k_lr_gather(int n, const float2 *brow, const float2 *bcol,
                                                      const int *byJ_off, const int *byJ, const int *byI_off,
-                                                     const int *byI, double2 *yrow, double2 *ycol)
+                                                     const int *byI, const int *bidx, double2 *yrow, double2 *ycol)
 {
     const int X = blockIdx.x, t = threadIdx.x;
     const int q = X * kTile + t;
@@ -2460,13 +2814,13 @@ __global__ void __launch_bounds__(kTile) k_lr_gather(int n, const float2 *brow, 
     const int j0 = byJ_off[X], j1 = byJ_off[X + 1], i0 = byI_off[X], i1 = byI_off[X + 1];
 #pragma unroll 4
     for (int p = j0; p < j1; ++p) {
-        const float2 v = __ldg(brow + (size_t)byJ[p] * kTile + t);
+        const float2 v = __ldg(brow + (size_t)bidx[byJ[p]] * kTile + t);
         kahan_add(fr, efr, v.x);
         kahan_add(fi, efi, v.y);
     }
 #pragma unroll 4
     for (int p = i0; p < i1; ++p) {
-        const float2 v = __ldg(bcol + (size_t)byI[p] * kTile + t);
+        const float2 v = __ldg(bcol + (size_t)bidx[byI[p]] * kTile + t);
         kahan_add(cr, ecr, v.x);
         kahan_add(ci, eci, v.y);
     }
@@ -2820,31 +3174,54 @@ void launch_aca_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, cons
                                                                  rank, fro, err);
 }
 
+template <bool ATT, int RS, int MINB>
+void launch_aca_panel_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
+                        int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
+                        cudaStream_t s, float2 *brow, float2 *bcol)
+{
+    const size_t smem = (size_t)2 * RS * kTile * sizeof(float2);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_aca_panel<ATT, RS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    k_aca_panel<ATT, RS, MINB><<<(unsigned)nblocks, kTile, smem, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit,
+                                                                       U, V, rank, fro, err, brow, bcol);
+}
+
 template <bool ATT>
-void launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap,
+bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap,
                   const long long *off, int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro,
-                  float limit, float *err, cudaStream_t s)
+                  float limit, float *err, cudaStream_t s, float2 *brow, float2 *bcol)
 {
     switch (variant) {
+    case 3: launch_aca_panel_t<ATT, 8, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 4: launch_aca_panel_t<ATT, 8, 2>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 5: launch_aca_panel_t<ATT, 4, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 6: launch_aca_panel_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 1: launch_aca_t<ATT, 12, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     case 2: launch_aca_t<ATT, 16, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     default: launch_aca_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     }
+    return false;
 }
 }  // namespace
 
 // variant: factor ranks kept in shared memory and CTAs per SM -- 0: 8 ranks,
 // 4 CTAs (the fastest on the 60 kHz trihedral: 5.95 ms against 6.07 and
-// 6.69 ms); 1: 12 ranks, 4 CTAs; 2: 16 ranks, 3 CTAs
-void launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
+// 6.69 ms); 1: 12 ranks, 4 CTAs; 2: 16 ranks, 3 CTAs; the panel form
+// (k_aca_panel): 3: 8 ranks, 3 CTAs; 4: 8 ranks, 2 CTAs; 5: 4 ranks, 4 CTAs;
+// 6: 8 ranks, 4 CTAs
+bool launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                 int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
-                cudaStream_t s, int variant)
+                cudaStream_t s, int variant, float2 *brow, float2 *bcol)
 {
-    if (nblocks <= 0) return;
+    if (nblocks <= 0) return false;
     if (a.ka != 0.0f)
-        launch_aca_v<true>(variant, a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s);
-    else
-        launch_aca_v<false>(variant, a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s);
+        return launch_aca_v<true>(variant, a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow,
+                                  bcol);
+    return launch_aca_v<false>(variant, a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow,
+                               bcol);
 }
 
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
@@ -2857,10 +3234,11 @@ void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls,
 void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
                      const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
-                     double2 *ycol, cudaStream_t s, const int *ndev)
+                     double2 *ycol, cudaStream_t s, const int *ndev, bool outputs_ready)
 {
-    if (nb > 0) k_lr_block<<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev);
-    if (ntiles > 0) k_lr_gather<<<ntiles, kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, yrow, ycol);
+    if (nb > 0 && !outputs_ready) k_lr_block<<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev);
+    if (ntiles > 0)
+        k_lr_gather<<<ntiles, kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, bidx, yrow, ycol);
 }
 
 void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s)

@@ -195,6 +195,7 @@ struct Compression {
     float *d_desc = nullptr;        // descriptors of the candidates
     int *d_kmap = nullptr, *d_acap = nullptr;  // kept block -> candidate, rank caps
     bool stats_pending = false;     // statistics and timings not read back yet
+    bool outputs_ready = false;     // the build also wrote the block outputs of its bounce's inputs
     // descriptors and rank labels of the approximated blocks (network training)
     std::vector<float> desc, label;
     Arena arena;    // the candidate- and block-level arrays above
@@ -277,6 +278,7 @@ struct Model {
     int opt_cmp_select = 0;     // 0 rule (class ALL, eta-separated), 1 every interacting block, 2 the network
     float opt_cmp_rcut = 24.0f; // network: propose blocks whose predicted rank is below this
     int opt_aca_variant = 0;    // cross-approximation kernel shape (factor ranks in shared memory, CTAs per SM)
+    int opt_fused_apply = 1;    // panel cross approximation: apply the accepted blocks to the building bounce's inputs
     int opt_mask_classify = 1;  // bounce masks: warp-per-block classification, pair kernel on the listed blocks
     int opt_gate_proj = 1;      // bounce masks: gates decided from per-point projections where certain
     int opt_cross_objects = 0;  // bounces also between different targets (FACET_RESP); 0: the reference's behaviour
@@ -892,8 +894,11 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     C.d_rank = ar.take<int>(nmax);
     C.d_fro = ar.take<float>(nmax);
     C.d_err = ar.take<float>(nmax);
-    launch_aca(s, C.d_blocks, C.d_cls, C.d_acap, C.d_off, n, g.opt_cmp_tol, C.d_U, C.d_V, C.d_rank, C.d_fro,
-               g.opt_cmp_judge, C.d_err, st, g.opt_aca_variant);
+    // the panel kernels also apply the accepted blocks to this bounce's packed
+    // inputs: the first bounce's low-rank apply then only gathers
+    C.outputs_ready = launch_aca(s, C.d_blocks, C.d_cls, C.d_acap, C.d_off, n, g.opt_cmp_tol, C.d_U, C.d_V, C.d_rank,
+                                 C.d_fro, g.opt_cmp_judge, C.d_err, st, g.opt_aca_variant,
+                                 g.opt_fused_apply ? C.d_brow : nullptr, g.opt_fused_apply ? C.d_bcol : nullptr);
     CK(cudaGetLastError());
     CK(cudaEventRecord(g.evb[2], st));
     // ---- accepted blocks: dense flags off, owner lists, statistics
@@ -1065,7 +1070,7 @@ void run_hop(int hop, int a, int b)
                 CK(cudaEventRecord(g.ev4, lst));
                 launch_lr_apply(s, C.d_blocks, C.d_off, C.d_bidx, C.nblocks, C.d_U, C.d_V, C.d_rank, C.d_brow, C.d_bcol,
                                 M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, lst,
-                                C.d_nacc);
+                                C.d_nacc, built && C.outputs_ready);
                 CK(cudaEventRecord(g.ev5, lst));
                 if (g.opt_overlap) CK(cudaEventRecord(g.ev_join, lst));
                 yrow = C.d_yrow;
@@ -1119,8 +1124,9 @@ void run_hop(int hop, int a, int b)
     float ms = 0.0f, sum_ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
     CK(cudaEventElapsedTime(&sum_ms, g.ev2, g.ev3));
-    const int nl = (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + (M.mask_ms > 0.0f ? 1 : 0) + (rec_cmp ? 2 : 0);
-    g.launches += (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + (rec_cmp ? 2 : 0) + (rec_cmp_build > 0.0f ? 4 : 0);
+    const int lr_launches = rec_cmp ? (built && g.cmp.outputs_ready ? 1 : 2) : 0;
+    const int nl = (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + (M.mask_ms > 0.0f ? 1 : 0) + lr_launches;
+    g.launches += (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + lr_launches + (rec_cmp_build > 0.0f ? 4 : 0);
     HopRecord rec{hop, pair_count(hop, a, b), M.mask_ms, sum_ms, ms, s.nsplit, nl};
     if (rec_cmp) {
         rec.cmp_cand = g.cmp.ncand;
@@ -1668,8 +1674,9 @@ int sonar_set_option(const char *key, double value)
         for (auto &m : g.masks) m.stale = true;
         return 0;
     }
+    if (!strcmp(key, "aca_fused_apply")) { g.opt_fused_apply = value != 0.0; g.cmp.release(); return 0; }
     if (!strcmp(key, "aca_variant")) {
-        if (value < 0 || value > 2) return -1;
+        if (value < 0 || value > 6) return -1;
         g.opt_aca_variant = (int)value;
         return 0;
     }

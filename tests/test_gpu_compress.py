@@ -101,7 +101,47 @@ def test_cross_approximation_variants_identical(api, scenes):
     assert np.array_equal(out[0], out[1])
     assert np.array_equal(out[0], out[2])
     with pytest.raises(api.SonarError):
-        api.set_option("aca_variant", 3)
+        api.set_option("aca_variant", 7)
+
+
+def test_panel_cross_approximation(api, oracle_mod, scenes):
+    """The panel form of the cross approximation (four pivot rows per step):
+    its kernel shapes (factor ranks in shared memory, CTAs per SM) give
+    bit-identical bounces, which stay within 1e-3 of the plain path and of
+    the FP64 oracle with every interacting block approximated."""
+    sc = _trihedral(scenes, 30e3)
+    _, P_plain, _ = _bounces(api, sc, 0)
+    api.set_option("compress_select", 1)
+    out, ranks = [], []
+    try:
+        for v in (3, 5, 6):
+            api.set_option("aca_variant", v)
+            P0, P, st = _bounces(api, sc, 1)
+            hop = [h for h in st["hops"] if h["hop"] == 2][0]
+            out.append(P)
+            ranks.append((hop["cmp_mean_rank"], hop["cmp_accepted"], hop["cmp_blocks"]))
+        api.set_option("compress", 1)
+        load_scene(api, sc)
+        api.project_source_points_to_objects(False)
+        Q0 = api.get_object_pressures(api.TARGET, 0)
+        api.project_target_to_target_objects(1)
+        Q1 = api.get_object_pressures(api.TARGET, 0)
+    finally:
+        api.set_option("compress", 0)
+        api.set_option("aca_variant", 0)
+        api.set_option("compress_select", 0)
+        api.TearDownCuda()
+    print("panel variants: (mean rank, accepted, approximated)", ranks)
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
+    assert ranks[0][1] > 0.9 * ranks[0][2]
+    err = rel_l2(out[0] - P0, P_plain - P0)
+    o = oracle_scene(oracle_mod, sc)
+    act = o.active(0, 0)
+    q = np.sort(np.random.default_rng(79).choice(len(act), 64, replace=False))
+    v1, _ = o.hop_subset(2, 0, 0, q, pin=Q0)
+    e1 = rel_l2((Q1 - Q0)[act[q]], v1)
+    print("panel compressed vs plain %.3e, one bounce vs FP64 oracle %.3e" % (err, e1))
+    assert err < 1e-3 and e1 < 1e-3
 
 
 @pytest.mark.parametrize("select", [1])
