@@ -177,6 +177,7 @@ RCUT = [24.0]  # the admissibility network proposes blocks with predicted rank b
 TOL = [5e-4]   # cross-approximation tolerance (the judge accepts 3 x this RMS error)
 ACA_VARIANT = [0]  # cross-approximation kernel shape (factor ranks in shared memory, CTAs per SM)
 OVERLAP = [1]      # compressed bounce: low-rank apply on a second stream beside the dense remainder
+FUSED = [1]        # cross approximation: the first bounce's low-rank apply fused into it
 
 
 def set_path(api, compressed, select):
@@ -186,6 +187,7 @@ def set_path(api, compressed, select):
     api.set_option("compress_tol", TOL[0])
     api.set_option("compress_judge", 3.0 * TOL[0])
     api.set_option("aca_variant", ACA_VARIANT[0])
+    api.set_option("aca_fused_apply", FUSED[0])
     api.set_option("overlap_streams", OVERLAP[0])
 
 
@@ -993,10 +995,14 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
     ap.add_argument("--mode", default="both", choices=["both", "plain", "compressed"])
-    ap.add_argument("--aca-variant", type=int, default=0, choices=tuple(range(7)),
+    ap.add_argument("--aca-variant", type=int, default=0, choices=tuple(range(10)),
                     help="cross-approximation kernel: 0 = 8 factor ranks in shared memory, 4 CTAs per SM; "
                          "1 = 12 ranks, 4 CTAs; 2 = 16 ranks, 3 CTAs; panel form (4 pivot rows per step): "
-                         "3 = 8 ranks, 3 CTAs; 4 = 8 ranks, 2 CTAs; 5 = 4 ranks, 4 CTAs; 6 = 8 ranks, 4 CTAs")
+                         "3 = 8 ranks, 3 CTAs; 4 = 8 ranks, 2 CTAs; 5 = 4 ranks, 4 CTAs; 6 = 8 ranks, 4 CTAs; two rows and "
+                         "columns per thread (128 threads): 7 = 8 ranks, 4 CTAs; 8 = 6 ranks, 5 CTAs; 9 = 4 ranks, 6 CTAs")
+    ap.add_argument("--fused-apply", type=int, default=1, choices=(0, 1),
+                    help="cross approximation: apply the accepted blocks to the first bounce's inputs in the same "
+                         "kernel")
     ap.add_argument("--overlap", type=int, default=1, choices=(0, 1),
                     help="compressed bounce: low-rank apply on a second stream beside the dense remainder")
     ap.add_argument("--tol", type=float, default=5e-4,
@@ -1020,6 +1026,7 @@ def main():
     RCUT[0] = args.rcut
     ACA_VARIANT[0] = args.aca_variant
     OVERLAP[0] = args.overlap
+    FUSED[0] = args.fused_apply
     TOL[0] = args.tol
     if args.impl == "reference":
         run_reference(args)

@@ -2085,20 +2085,64 @@ __device__ __forceinline__ float block_sum(float v, float *sv)
     return t;
 }
 
-// T(j, i) of one pair of a block of class cls (bit: the pair's mask bit for BITS)
+// The exact FP32 cosine gate where the estimate is inside the band (rare):
+// kept out of line so that kernels that unroll several entries carry one
+// copy of it.
+__device__ __noinline__ bool gate_exact(float vx, float vy, float vz, float sign, float nx, float ny, float nz)
+{
+    return !(exact_cos(vx, vy, vz, sign, nx, ny, nz) < 1e-6f);
+}
+
+__device__ __forceinline__ bool gate_est(float est, float vx, float vy, float vz, float sign, float nx, float ny,
+                                         float nz)
+{
+    if (est > 2e-6f) return true;
+    if (est < 0.0f) return false;
+    return gate_exact(vx, vy, vz, sign, nx, ny, nz);
+}
+
+// T(j, i) of one pair of a block of class cls (bit: the pair's mask bit for
+// BITS; CLEAR blocks evaluate the cosine gates inline).  One code path for
+// every class: the Green's function of sym_pair (same operations, same
+// rounding), then the pair's gate.
 template <bool ATT>
 __device__ __forceinline__ float2 lr_entry(const SumArgs &a, int cls, bool bit, float4 pi, float4 ni, float4 pj,
                                            float4 nj)
 {
-    const Dst d{pj.x, pj.y, pj.z, nj.x, nj.y, nj.z};
+    const float vx = __fsub_rn(pj.x, pi.x), vy = __fsub_rn(pj.y, pi.y), vz = __fsub_rn(pj.z, pi.z);
+    const float r2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+    const float rinv = rsqrtf(r2);
+    const float r0 = r2 * rinv;
+    const float r = fmaf(fmaf(-r0, r0, r2), 0.5f * rinv, r0);
+    const float th = __fmul_rn(r, a.k2hi);
+    const float tl = fmaf(r, a.k2lo, fmaf(r, a.k2hi, -th));
+    const float frac = (th - rintf(th)) + tl;
+    float sn, cs;
+    __sincosf(frac * kTwoPi, &sn, &cs);
+    const float d1 = vx * ni.x + vy * ni.y + vz * ni.z;  // r cos_scat
+    const float d2 = vx * nj.x + vy * nj.y + vz * nj.z;  // -r cos_inc
+    const float rinv2 = rinv * rinv;
+    const float u = (d1 * d2) * (-rinv2);
     float Tr, Ti;
-    bool ok;
-    if (cls == kFlagClear) {
-        sym_pair<ATT, true, true>(a, pi, ni, d, Tr, Ti, ok);
+    if (ATT) {
+        const float amp = rinv * kInv4Pi * __expf(-a.ka * r);
+        Tr = u * fmaf(amp, fmaf(a.ka, cs, a.kr * sn), rinv2);
+        Ti = u * (amp * fmaf(a.ka, sn, -a.kr * cs));
     } else {
-        sym_pair<ATT, false, true>(a, pi, ni, d, Tr, Ti, ok);
-        ok = cls == kFlagAll || bit;
+        const float ua = (u * rinv) * a.kr4pi;
+        Tr = fmaf(ua, sn, u * rinv2);
+        Ti = -ua * cs;
     }
+    float rr = r;
+    if (fabsf(r - a.rmin) <= a.rmin * 1e-6f) rr = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
+    if (rr < a.rmin) {
+        Tr = u * (-a.ka * kInv4Pi);
+        Ti = u * (a.kr * kInv4Pi);
+    }
+    bool ok = cls == kFlagBits ? bit : true;
+    if (cls == kFlagClear)
+        ok = gate_est(d1 * rinv, vx, vy, vz, 1.0f, ni.x, ni.y, ni.z) &&
+             gate_est(-d2 * rinv, vx, vy, vz, -1.0f, nj.x, nj.y, nj.z);
     return ok ? make_float2(Tr, Ti) : make_float2(0.0f, 0.0f);
 }
 
@@ -2311,25 +2355,29 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *bloc
     }
 }
 
-// Low-rank apply of one accepted block of rank k, by the whole CTA: tv =
-// V^T w_I and su = U^T w_J (warp w takes the ranks m = w (mod 8), each lane 8
-// rows, one warp reduction per rank; one barrier), then the block's forward
-// terms U tv (rows of J) and reciprocal terms V su (columns of I) into its
-// output slots brow_b, bcol_b (FP32).  The weights w are the packed inputs
-// (srcA.w, srcB.w).  sW holds kTile float4, sTv and sSu kLrMaxRank float2.
-// Starts with a barrier (the caller may reuse the shared arrays).
+// Low-rank apply of one accepted block of rank k, by the whole CTA of NT
+// threads: tv = V^T w_I and su = U^T w_J (warp w takes the ranks m = w (mod
+// NT / 32), each lane 8 rows, one warp reduction per rank; one barrier),
+// then the block's forward terms U tv (rows of J) and reciprocal terms V su
+// (columns of I) into its output slots brow_b, bcol_b (FP32).  The weights w
+// are the packed inputs (srcA.w, srcB.w).  sW holds kTile float4, sTv and
+// sSu kLrMaxRank float2.  Starts with a barrier (the caller may reuse the
+// shared arrays).
+template <int NT = kTile>
 __device__ __forceinline__ void lr_block_apply(const SumArgs &a, int I, int J, const float2 *U0, const float2 *V0,
                                                int k, float2 *brow_b, float2 *bcol_b, float4 *sW, float2 *sTv,
                                                float2 *sSu)
 {
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int i = I * kTile + t, j = J * kTile + t;
     __syncthreads();
-    sW[t] = make_float4(i < a.nsrc ? a.srcA[i].w : 0.0f, i < a.nsrc ? a.srcB[i].w : 0.0f,
-                        j < a.nsrc ? a.srcA[j].w : 0.0f, j < a.nsrc ? a.srcB[j].w : 0.0f);
-    const float2 *Ub = U0 + t, *Vb = V0 + t;
+#pragma unroll
+    for (int h = 0; h < kTile / NT; ++h) {
+        const int tt = t + h * NT, i = I * kTile + tt, j = J * kTile + tt;
+        sW[tt] = make_float4(i < a.nsrc ? a.srcA[i].w : 0.0f, i < a.nsrc ? a.srcB[i].w : 0.0f,
+                             j < a.nsrc ? a.srcA[j].w : 0.0f, j < a.nsrc ? a.srcB[j].w : 0.0f);
+    }
     __syncthreads();
-    for (int m = warp; m < k; m += kTile / 32) {
+    for (int m = warp; m < k; m += NT / 32) {
         float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
         for (int r = 0; r < kTile / 32; ++r) {
@@ -2354,18 +2402,23 @@ __device__ __forceinline__ void lr_block_apply(const SumArgs &a, int I, int J, c
         }
     }
     __syncthreads();
-    float rr = 0.0f, ri = 0.0f, cr = 0.0f, ci = 0.0f;
-    // the factors come back from L2: several ranks' loads in flight at once
+#pragma unroll
+    for (int h = 0; h < kTile / NT; ++h) {
+        const int tt = t + h * NT;
+        const float2 *Ub = U0 + tt, *Vb = V0 + tt;
+        float rr = 0.0f, ri = 0.0f, cr = 0.0f, ci = 0.0f;
+        // the factors come back from L2: several ranks' loads in flight at once
 #pragma unroll 4
-    for (int m = 0; m < k; ++m) {
-        const float2 u = Ub[m * kTile], v = Vb[m * kTile], c = sTv[m], e = sSu[m];
-        rr += u.x * c.x - u.y * c.y;
-        ri += u.x * c.y + u.y * c.x;
-        cr += v.x * e.x - v.y * e.y;
-        ci += v.x * e.y + v.y * e.x;
+        for (int m = 0; m < k; ++m) {
+            const float2 u = Ub[m * kTile], v = Vb[m * kTile], c = sTv[m], e = sSu[m];
+            rr += u.x * c.x - u.y * c.y;
+            ri += u.x * c.y + u.y * c.x;
+            cr += v.x * e.x - v.y * e.y;
+            ci += v.x * e.y + v.y * e.x;
+        }
+        brow_b[tt] = make_float2(rr, ri);
+        bcol_b[tt] = make_float2(cr, ci);
     }
-    brow_b[t] = make_float2(rr, ri);
-    bcol_b[t] = make_float2(cr, ci);
 }
 
 // ---------------------------------------------------------------- panel cross approximation
@@ -2438,6 +2491,10 @@ __device__ __forceinline__ bool block_bit(const uint32_t *bw, long long pitch, i
 
 // brow, bcol (optional): the low-rank apply of every accepted block with the
 // packed inputs of this launch, fused (lr_block_apply into slot b).
+// The panel's row and column indices (< 256) travel packed in one 32-bit
+// word, 8 bits each, so that loops over the panel need no indexed arrays.
+__device__ __forceinline__ int unpack8(unsigned w, int q) { return (int)((w >> (8 * q)) & 0xFFu); }
+
 template <bool ATT, int RS, int MINB>
 __global__ void __launch_bounds__(kTile, MINB) k_aca_panel(SumArgs a, const int2 *blocks, const uint8_t *cls,
                                                            const int *cap, const long long *off, int nblocks,
@@ -2465,62 +2522,67 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca_panel(SumArgs a, const int2
     const float4 pi = coli ? __ldg(PI + t) : z4, qi = coli ? __ldg(NI + t) : z4;
     const float4 pj = rowj ? __ldg(PJ + t) : z4, qj = rowj ? __ldg(NJ + t) : z4;
     bool colused = !coli, rowused = !rowj;
-    // the first panel's rows spread over the tile
-    int rows[kPanel];
-    int nr = 0;
+    // the first panel's rows spread over the tile (rows 0 .. nj - 1 when nj < kPanel)
+    unsigned rows = 0u;
+    int nr = min(nj, kPanel);
 #pragma unroll
-    for (int q = 0; q < kPanel; ++q) {
-        rows[q] = (q * nj) / kPanel;  // distinct when nj >= kPanel
-        if (q == 0 || rows[q] != rows[q - 1]) nr = q + 1;
-    }
-    if (nj < kPanel) nr = nj;  // rows 0 .. nj - 1
+    for (int q = 0; q < kPanel; ++q) rows |= (unsigned)(nj < kPanel ? q : (q * nj) / kPanel) << (8 * q);
     int k = 0, zero_rows = 0;
     float norm2 = 0.0f;
     bool done = nr == 0;
     while (!done && k < K) {
-        // ---- A. residual rows of the panel at column t
-        float2 e[kPanel];
-#pragma unroll
-        for (int q = 0; q < kPanel; ++q) e[q] = z2;
+        const int ks = min(k, RS);
+        // ---- A. residual rows of the panel at column t: entries, then one pass over the earlier ranks
+        float2 e0 = z2, e1 = z2, e2 = z2, e3 = z2;
         if (coli) {
-#pragma unroll
-            for (int q = 0; q < kPanel; ++q)
-                if (q < nr) {
-                    const int r = rows[q];
-                    const bool bit = bc == kFlagBits ? block_bit(bw, pitch, r, t) : true;
-                    e[q] = lr_entry<ATT>(a, bc, bit, pi, qi, __ldg(PJ + r), __ldg(NJ + r));
-                }
-            const int ks = min(k, RS);
+#pragma unroll 1
+            for (int q = 0; q < nr; ++q) {
+                const int r = unpack8(rows, q);
+                const bool bit = bc == kFlagBits ? block_bit(bw, pitch, r, t) : true;
+                const float2 x = lr_entry<ATT>(a, bc, bit, pi, qi, __ldg(PJ + r), __ldg(NJ + r));
+                e0 = q == 0 ? x : e0;
+                e1 = q == 1 ? x : e1;
+                e2 = q == 2 ? x : e2;
+                e3 = q == 3 ? x : e3;
+            }
+            const int r0 = unpack8(rows, 0), r1 = unpack8(rows, 1), r2 = unpack8(rows, 2), r3 = unpack8(rows, 3);
             for (int m = 0; m < ks; ++m) {
                 const float2 v = sV[m * kTile + t];
-#pragma unroll
-                for (int q = 0; q < kPanel; ++q)
-                    if (q < nr) e[q] = csub_mul(e[q], sU[m * kTile + rows[q]], v);
+                const float2 *Um = sU + m * kTile;
+                e0 = csub_mul(e0, Um[r0], v);
+                e1 = csub_mul(e1, Um[r1], v);
+                e2 = csub_mul(e2, Um[r2], v);
+                e3 = csub_mul(e3, Um[r3], v);
             }
             for (int m = RS; m < k; ++m) {
                 const float2 v = Vb[m * kTile + t];
-#pragma unroll
-                for (int q = 0; q < kPanel; ++q)
-                    if (q < nr) e[q] = csub_mul(e[q], Ub[m * kTile + rows[q]], v);
+                const float2 *Um = Ub + m * kTile;
+                e0 = csub_mul(e0, Um[r0], v);
+                e1 = csub_mul(e1, Um[r1], v);
+                e2 = csub_mul(e2, Um[r2], v);
+                e3 = csub_mul(e3, Um[r3], v);
             }
+            // panel slots past nr hold a repeated row: their values are never used
         }
 #pragma unroll
         for (int q = 0; q < kPanel; ++q)
-            if (q < nr && t == rows[q]) rowused = true;
+            if (q < nr && t == unpack8(rows, q)) rowused = true;
         // ---- B. pivot columns, greedy within the panel
-        int cols[kPanel];
-        float2 vq[kPanel];
+        unsigned cols = 0u;
+        float2 v0 = z2, v1 = z2, v2 = z2, v3 = z2;
         int np = 0;
         const int room = K - k;  // ranks that still fit under the cap
 #pragma unroll
         for (int q = 0; q < kPanel; ++q) {
             if (q >= nr || np >= room) break;  // uniform
             const int buf = q & 1;
-#pragma unroll
-            for (int q2 = 0; q2 < kPanel; ++q2)
-                if (q2 >= q && q2 < nr) sE[buf][q2][t] = e[q2];
+            const float2 eq = q == 0 ? e0 : q == 1 ? e1 : q == 2 ? e2 : e3;
+            if (q <= 0) sE[buf][0][t] = e0;
+            if (q <= 1 && nr > 1) sE[buf][1][t] = e1;
+            if (q <= 2 && nr > 2) sE[buf][2][t] = e2;
+            if (q <= 3 && nr > 3) sE[buf][3][t] = e3;
             const unsigned key = __reduce_max_sync(0xffffffffu,
-                                                   argmax_key(e[q].x * e[q].x + e[q].y * e[q].y, t, !colused));
+                                                   argmax_key(eq.x * eq.x + eq.y * eq.y, t, !colused));
             if (lane == 0) sKey[buf][warp] = key;
             __syncthreads();
             const unsigned w = max8(sKey[buf]);
@@ -2528,22 +2590,21 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca_panel(SumArgs a, const int2
             const int c = (int)(255u - (w & 0xFFu));
             const float2 pv = sE[buf][q][c];
             const float inv = __frcp_rn(pv.x * pv.x + pv.y * pv.y);
-            const float2 v = coli ? make_float2((e[q].x * pv.x + e[q].y * pv.y) * inv,
-                                                (e[q].y * pv.x - e[q].x * pv.y) * inv)
+            const float2 v = coli ? make_float2((eq.x * pv.x + eq.y * pv.y) * inv, (eq.y * pv.x - eq.x * pv.y) * inv)
                                   : z2;
-#pragma unroll
-            for (int q2 = 0; q2 < kPanel; ++q2)
-                if (q2 > q && q2 < nr) e[q2] = csub_mul(e[q2], sE[buf][q2][c], v);
+            // eliminate this rank from the panel's later rows
+            if (q < 1 && nr > 1) e1 = csub_mul(e1, sE[buf][1][c], v);
+            if (q < 2 && nr > 2) e2 = csub_mul(e2, sE[buf][2][c], v);
+            if (q < 3 && nr > 3) e3 = csub_mul(e3, sE[buf][3][c], v);
             if (t == c) colused = true;
             const int m = k + np;
             Vb[m * kTile + t] = v;
             if (m < RS) sV[m * kTile + t] = v;
-#pragma unroll
-            for (int q3 = 0; q3 < kPanel; ++q3)
-                if (q3 == np) {
-                    cols[q3] = c;
-                    vq[q3] = v;
-                }
+            cols |= (unsigned)c << (8 * np);
+            v0 = np == 0 ? v : v0;
+            v1 = np == 1 ? v : v1;
+            v2 = np == 2 ? v : v2;
+            v3 = np == 3 ? v : v3;
             ++np;
         }
         if (np == 0) {
@@ -2554,71 +2615,91 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca_panel(SumArgs a, const int2
             int nrw = t;
             cta_reduce<true, false>(f, nrw, !rowused, d0, d1, sKey[0], nullptr);
             if (f < 0.0f) break;
-            rows[0] = nrw;
+            rows = (unsigned)nrw;
             nr = 1;
             __syncthreads();  // sKey[0] is rewritten by the next panel's first step
             continue;
         }
         // ---- C. residual columns at the chosen columns, row t
-        float2 u[kPanel];
-#pragma unroll
-        for (int q = 0; q < kPanel; ++q) u[q] = z2;
+        float2 u0 = z2, u1 = z2, u2 = z2, u3 = z2;
+        const int c0 = unpack8(cols, 0), c1 = unpack8(cols, 1), c2 = unpack8(cols, 2), c3 = unpack8(cols, 3);
         if (rowj) {
-#pragma unroll
-            for (int q = 0; q < kPanel; ++q)
-                if (q < np) {
-                    const int c = cols[q];
-                    const bool bit = bc == kFlagBits ? block_bit(bw, pitch, t, c) : true;
-                    u[q] = lr_entry<ATT>(a, bc, bit, __ldg(PI + c), __ldg(NI + c), pj, qj);
-                }
-            const int ks = min(k, RS);
+#pragma unroll 1
+            for (int q = 0; q < np; ++q) {
+                const int c = unpack8(cols, q);
+                const bool bit = bc == kFlagBits ? block_bit(bw, pitch, t, c) : true;
+                const float2 x = lr_entry<ATT>(a, bc, bit, __ldg(PI + c), __ldg(NI + c), pj, qj);
+                u0 = q == 0 ? x : u0;
+                u1 = q == 1 ? x : u1;
+                u2 = q == 2 ? x : u2;
+                u3 = q == 3 ? x : u3;
+            }
             for (int m = 0; m < ks; ++m) {
                 const float2 uu = sU[m * kTile + t];
-#pragma unroll
-                for (int q = 0; q < kPanel; ++q)
-                    if (q < np) u[q] = csub_mul(u[q], uu, sV[m * kTile + cols[q]]);
+                const float2 *Vm = sV + m * kTile;
+                u0 = csub_mul(u0, uu, Vm[c0]);
+                u1 = csub_mul(u1, uu, Vm[c1]);
+                u2 = csub_mul(u2, uu, Vm[c2]);
+                u3 = csub_mul(u3, uu, Vm[c3]);
             }
             for (int m = RS; m < k; ++m) {
                 const float2 uu = Ub[m * kTile + t];
-#pragma unroll
-                for (int q = 0; q < kPanel; ++q)
-                    if (q < np) u[q] = csub_mul(u[q], uu, Vb[m * kTile + cols[q]]);
+                const float2 *Vm = Vb + m * kTile;
+                u0 = csub_mul(u0, uu, Vm[c0]);
+                u1 = csub_mul(u1, uu, Vm[c1]);
+                u2 = csub_mul(u2, uu, Vm[c2]);
+                u3 = csub_mul(u3, uu, Vm[c3]);
             }
             // the panel's earlier ranks: u_q -= u_q2 v_q2(c_q)
-#pragma unroll
-            for (int q = 1; q < kPanel; ++q)
-#pragma unroll
-                for (int q2 = 0; q2 < kPanel; ++q2)
-                    if (q2 < q && q < np) {
-                        const int m2 = k + q2;
-                        const float2 vc = m2 < RS ? sV[m2 * kTile + cols[q]] : Vb[m2 * kTile + cols[q]];
-                        u[q] = csub_mul(u[q], u[q2], vc);
-                    }
-        }
-#pragma unroll
-        for (int q = 0; q < kPanel; ++q)
-            if (q < np) {
-                const int m = k + q;
-                Ub[m * kTile + t] = u[q];
-                if (m < RS) sU[m * kTile + t] = u[q];
+            auto vpan = [&](int q2, int c) {
+                const int m2 = k + q2;
+                return m2 < RS ? sV[m2 * kTile + c] : Vb[m2 * kTile + c];
+            };
+            if (np > 1) u1 = csub_mul(u1, u0, vpan(0, c1));
+            if (np > 2) {
+                u2 = csub_mul(u2, u0, vpan(0, c2));
+                u2 = csub_mul(u2, u1, vpan(1, c2));
             }
+            if (np > 3) {
+                u3 = csub_mul(u3, u0, vpan(0, c3));
+                u3 = csub_mul(u3, u1, vpan(1, c3));
+                u3 = csub_mul(u3, u2, vpan(2, c3));
+            }
+        }
+        {
+            float2 *Ut = Ub + k * kTile + t;
+            Ut[0] = u0;
+            if (np > 1) Ut[kTile] = u1;
+            if (np > 2) Ut[2 * kTile] = u2;
+            if (np > 3) Ut[3 * kTile] = u3;
+            if (k < RS) sU[k * kTile + t] = u0;
+            if (np > 1 && k + 1 < RS) sU[(k + 1) * kTile + t] = u1;
+            if (np > 2 && k + 2 < RS) sU[(k + 2) * kTile + t] = u2;
+            if (np > 3 && k + 3 < RS) sU[(k + 3) * kTile + t] = u3;
+        }
         // ---- norms of the new ranks and the next panel's rows
         {
             float x[8];
-#pragma unroll
-            for (int q = 0; q < kPanel; ++q) {
-                x[2 * q] = q < np ? u[q].x * u[q].x + u[q].y * u[q].y : 0.0f;
-                x[2 * q + 1] = q < np ? vq[q].x * vq[q].x + vq[q].y * vq[q].y : 0.0f;
-            }
+            x[0] = u0.x * u0.x + u0.y * u0.y;
+            x[1] = v0.x * v0.x + v0.y * v0.y;
+            x[2] = u1.x * u1.x + u1.y * u1.y;
+            x[3] = v1.x * v1.x + v1.y * v1.y;
+            x[4] = u2.x * u2.x + u2.y * u2.y;
+            x[5] = v2.x * v2.x + v2.y * v2.y;
+            x[6] = u3.x * u3.x + u3.y * u3.y;
+            x[7] = v3.x * v3.x + v3.y * v3.y;
             const float ws = warp_sum8(x, lane);
             if ((lane & 3) == 0) sSum[warp][lane >> 2] = ws;
-#pragma unroll
-            for (int q = 0; q < kPanel; ++q)
-                if (q < np) {
-                    const unsigned key = __reduce_max_sync(
-                        0xffffffffu, argmax_key(u[q].x * u[q].x + u[q].y * u[q].y, t, !rowused));
-                    if (lane == 0) sRowKey[q][warp] = key;
-                }
+            const unsigned k0 = __reduce_max_sync(0xffffffffu, argmax_key(x[0], t, !rowused));
+            const unsigned k1 = __reduce_max_sync(0xffffffffu, argmax_key(x[2], t, !rowused && np > 1));
+            const unsigned k2 = __reduce_max_sync(0xffffffffu, argmax_key(x[4], t, !rowused && np > 2));
+            const unsigned k3 = __reduce_max_sync(0xffffffffu, argmax_key(x[6], t, !rowused && np > 3));
+            if (lane == 0) {
+                sRowKey[0][warp] = k0;
+                sRowKey[1][warp] = k1;
+                sRowKey[2][warp] = k2;
+                sRowKey[3][warp] = k3;
+            }
         }
         __syncthreads();
         float S[8];
@@ -2644,27 +2725,25 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca_panel(SumArgs a, const int2
             }
         k += kept;
         if (done) break;
-        // next rows: the argmax of |u_q| over unused rows, per new rank
-        int nn2 = 0;
+        // next rows: the argmax of |u_q| over unused rows, per new rank, duplicates dropped
+        rows = 0u;
+        nr = 0;
 #pragma unroll
         for (int q = 0; q < kPanel; ++q)
             if (q < np) {
                 const unsigned w = max8(sRowKey[q]);
                 if (w) {
-                    const int r = (int)(255u - (w & 0xFFu));
+                    const unsigned r = 255u - (w & 0xFFu);
                     bool dup = false;
 #pragma unroll
                     for (int q2 = 0; q2 < kPanel; ++q2)
-                        if (q2 < nn2 && rows[q2] == r) dup = true;
+                        if (q2 < nr && unpack8(rows, q2) == (int)r) dup = true;
                     if (!dup) {
-#pragma unroll
-                        for (int q3 = 0; q3 < kPanel; ++q3)
-                            if (q3 == nn2) rows[q3] = r;
-                        ++nn2;
+                        rows |= r << (8 * nr);
+                        ++nr;
                     }
                 }
             }
-        nr = nn2;
         if (nr == 0) break;  // every row taken
     }
     // ---- the exact entries judge the approximation (as k_aca)
@@ -2673,7 +2752,7 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca_panel(SumArgs a, const int2
     __syncthreads();
     if (converged) {
         const int ks = min(k, RS);
-#pragma unroll
+#pragma unroll 1
         for (int h2 = 0; h2 < 2; ++h2) {
             const int s = t + kTile * h2;
             unsigned h = (unsigned)b * 2654435761u + (unsigned)s * 40503u + 12345u;
@@ -2683,8 +2762,8 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca_panel(SumArgs a, const int2
             const int jj = h2 == 0 ? t : (int)(h & 255u), ii = h2 == 0 ? (int)(h & 255u) : t;
             if (ii < ni && jj < nj) {
                 const bool bit = bc == kFlagBits ? block_bit(bw, pitch, jj, ii) : true;
-                const float2 ex = lr_entry<ATT>(a, bc, bit, h2 == 0 ? __ldg(PI + ii) : pi, h2 == 0 ? __ldg(NI + ii) : qi,
-                                                h2 == 0 ? pj : __ldg(PJ + jj), h2 == 0 ? qj : __ldg(NJ + jj));
+                const float2 ex = lr_entry<ATT>(a, bc, bit, __ldg(PI + ii), __ldg(NI + ii), __ldg(PJ + jj),
+                                                __ldg(NJ + jj));
                 float2 ap = z2;
                 for (int m = 0; m < ks; ++m) ap = csub_mul(ap, sU[m * kTile + jj], sV[m * kTile + ii]);
                 for (int m = RS; m < k; ++m) ap = csub_mul(ap, Ub[m * kTile + jj], Vb[m * kTile + ii]);
@@ -2710,6 +2789,225 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca_panel(SumArgs a, const int2
         float4 *sW = reinterpret_cast<float4 *>(&sE[0][0][0]);
         float2 *sTv = reinterpret_cast<float2 *>(sW + kTile), *sSu = sTv + kLrMaxRank;
         lr_block_apply(a, I, J, Ub, Vb, k, brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv, sSu);
+    }
+}
+
+// ---------------------------------------------------------------- two entries per thread
+// The classic cross approximation (k_aca's pivot order, stopping rule and
+// judge) by a CTA of 128 threads for the 256 x 256 block: thread t owns rows
+// t and t + 128 and columns t and t + 128.  Every per-step cost that does not
+// depend on the number of entries -- the block argmax, the pivot value and
+// its reciprocal, loop and branch work, the earlier ranks' factor entry at
+// the pivot, which serves both of a thread's entries -- is paid once per two
+// entries, and the two entries give each thread two independent chains.
+// The reductions run over four warps.  Per-rank norms are summed in another
+// order than k_aca's (so a stopping decision at the threshold can differ by
+// rounding); the factors are otherwise those of k_aca.
+constexpr int kAca2Threads = 128;
+constexpr int kAca2Warps = kAca2Threads / 32;
+
+// Block-wide argmax over two candidates per thread and block-wide sums of s0
+// and s1 over four warps (one barrier; see cta_reduce).
+template <bool ARG, bool SUMS>
+__device__ __forceinline__ void cta_reduce2(float va, int ia, bool oka, float vb, int ib, bool okb, float &best,
+                                            int &idx, float &s0, float &s1, unsigned *slot, float2 *sums)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned k = 0u;
+    if (ARG) k = __reduce_max_sync(0xffffffffu, max(argmax_key(va, ia, oka), argmax_key(vb, ib, okb)));
+    if (SUMS) {
+        // two sums with five shuffles: lanes of the upper half keep s1, the lower s0
+        const bool hi = lane & 16;
+        float w = (hi ? s1 : s0) + __shfl_xor_sync(0xffffffffu, hi ? s0 : s1, 16);
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+        s0 = __shfl_sync(0xffffffffu, w, 0);
+        s1 = __shfl_sync(0xffffffffu, w, 16);
+    }
+    if (lane == 0) {
+        if (ARG) slot[warp] = k;
+        if (SUMS) sums[warp] = make_float2(s0, s1);
+    }
+    __syncthreads();
+    if (ARG) {
+        static_assert(kAca2Warps == 4, "one 16-byte slot read");
+        const uint4 a = reinterpret_cast<const uint4 *>(slot)[0];
+        const unsigned w = max(max(a.x, a.y), max(a.z, a.w));
+        best = key_value(w);
+        idx = (int)(255u - (w & 0xFFu));
+    }
+    if (SUMS) {
+        const float4 p = reinterpret_cast<const float4 *>(sums)[0], q = reinterpret_cast<const float4 *>(sums)[1];
+        s0 = (p.x + p.z) + (q.x + q.z);
+        s1 = (p.y + p.w) + (q.y + q.w);
+    }
+}
+
+template <bool ATT, int RS, int MINB>
+__global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const int2 *blocks, const uint8_t *cls,
+                                                             const int *cap, const long long *off, int nblocks,
+                                                             float tol, float limit, float2 *U, float2 *V, int *rank,
+                                                             float *fro, float *err, float2 *brow, float2 *bcol)
+{
+    extern __shared__ float2 aca_smem[];  // sU[RS][kTile], then sV[RS][kTile]
+    float2 *sU = aca_smem, *sV = aca_smem + RS * kTile;
+    __shared__ float2 sRow[kTile];
+    __shared__ float4 sFrag[4][kTile];  // position and normal of the columns' (I) and rows' (J) fragments
+    __shared__ __align__(16) unsigned slotA[kAca2Warps], slotB[kAca2Warps], slotZ[kAca2Warps];
+    __shared__ __align__(16) float2 sumB[kAca2Warps];
+    const int t = threadIdx.x, b = blockIdx.x;
+    const int ta = t, tb = t + kAca2Threads;  // this thread's two rows / columns
+    if (b >= nblocks) return;  // CTA-uniform
+    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = min(cap[b], kLrRankLimit);
+    const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
+    const float4 *PI = a.srcA + I * kTile, *NI = a.srcB + I * kTile, *PJ = a.srcA + J * kTile, *NJ = a.srcB + J * kTile;
+    float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
+    const uint32_t *bw = a.mask.bits + (long long)I * kWordsPerTile * a.mask.pitch + (long long)J * kTile;
+    const long long pitch = a.mask.pitch;
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float2 z2 = make_float2(0.0f, 0.0f);
+    const bool colA = ta < ni, colB = tb < ni, rowA = ta < nj, rowB = tb < nj;
+    const float4 piA = colA ? __ldg(PI + ta) : z4, qiA = colA ? __ldg(NI + ta) : z4;
+    const float4 piB = colB ? __ldg(PI + tb) : z4, qiB = colB ? __ldg(NI + tb) : z4;
+    const float4 pjA = rowA ? __ldg(PJ + ta) : z4, qjA = rowA ? __ldg(NJ + ta) : z4;
+    const float4 pjB = rowB ? __ldg(PJ + tb) : z4, qjB = rowB ? __ldg(NJ + tb) : z4;
+    sFrag[0][ta] = piA; sFrag[0][tb] = piB;
+    sFrag[1][ta] = qiA; sFrag[1][tb] = qiB;
+    sFrag[2][ta] = pjA; sFrag[2][tb] = pjB;
+    sFrag[3][ta] = qjA; sFrag[3][tb] = qjB;
+    __syncthreads();
+    bool usedA = !rowA, usedB = !rowB;  // rows taken (or absent)
+    int r = 0, k = 0, zero_rows = 0;
+    float norm2 = 0.0f;
+    while (k < K) {
+        const int ks = min(k, RS);
+        // ---- residual row r, entries (r, ta) and (r, tb)
+        float2 va = z2, vb = z2;
+        {
+            const float4 pr = sFrag[2][r], qr = sFrag[3][r];
+            if (colA) va = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, r, ta) : true, piA, qiA, pr, qr);
+            if (colB) vb = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, r, tb) : true, piB, qiB, pr, qr);
+            for (int m = 0; m < ks; ++m) {
+                const float2 ur = sU[m * kTile + r];
+                va = csub_mul(va, ur, sV[m * kTile + ta]);
+                vb = csub_mul(vb, ur, sV[m * kTile + tb]);
+            }
+            for (int m = RS; m < k; ++m) {
+                const float2 ur = Ub[m * kTile + r];
+                va = csub_mul(va, ur, Vb[m * kTile + ta]);
+                vb = csub_mul(vb, ur, Vb[m * kTile + tb]);
+            }
+        }
+        sRow[ta] = va;
+        sRow[tb] = vb;
+        float best, d0 = 0.0f, d1 = 0.0f;
+        int c;
+        cta_reduce2<true, false>(va.x * va.x + va.y * va.y, ta, colA, vb.x * vb.x + vb.y * vb.y, tb, colB, best, c,
+                                 d0, d1, slotA, nullptr);
+        if (!(best > 1e-30f)) {
+            // the residual row vanished: take the lowest unused row instead
+            if (ta == r) usedA = true;
+            if (tb == r) usedB = true;
+            if (++zero_rows > kAcaMaxZeroRows) break;
+            float f;
+            int nr;
+            cta_reduce2<true, false>(1.0f, ta, !usedA, 1.0f, tb, !usedB, f, nr, d0, d1, slotZ, nullptr);
+            if (f < 0.0f) break;
+            r = nr;
+            continue;
+        }
+        const float2 pv = sRow[c];
+        const float inv = __frcp_rn(pv.x * pv.x + pv.y * pv.y);
+        const float2 wa = colA ? make_float2((va.x * pv.x + va.y * pv.y) * inv, (va.y * pv.x - va.x * pv.y) * inv) : z2;
+        const float2 wb = colB ? make_float2((vb.x * pv.x + vb.y * pv.y) * inv, (vb.y * pv.x - vb.x * pv.y) * inv) : z2;
+        Vb[k * kTile + ta] = wa;
+        Vb[k * kTile + tb] = wb;
+        if (k < RS) {
+            sV[k * kTile + ta] = wa;
+            sV[k * kTile + tb] = wb;
+        }
+        // ---- residual column c, entries (ta, c) and (tb, c)
+        float2 ua = z2, ub = z2;
+        {
+            const float4 pc = sFrag[0][c], qc = sFrag[1][c];
+            if (rowA) ua = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, ta, c) : true, pc, qc, pjA, qjA);
+            if (rowB) ub = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, tb, c) : true, pc, qc, pjB, qjB);
+            for (int m = 0; m < ks; ++m) {
+                const float2 vc = sV[m * kTile + c];
+                ua = csub_mul(ua, sU[m * kTile + ta], vc);
+                ub = csub_mul(ub, sU[m * kTile + tb], vc);
+            }
+            for (int m = RS; m < k; ++m) {
+                const float2 vc = Vb[m * kTile + c];
+                ua = csub_mul(ua, Ub[m * kTile + ta], vc);
+                ub = csub_mul(ub, Ub[m * kTile + tb], vc);
+            }
+        }
+        Ub[k * kTile + ta] = ua;
+        Ub[k * kTile + tb] = ub;
+        if (k < RS) {
+            sU[k * kTile + ta] = ua;
+            sU[k * kTile + tb] = ub;
+        }
+        if (ta == r) usedA = true;
+        if (tb == r) usedB = true;
+        // ---- norms and the next pivot row: the largest residual-column entry among unused rows
+        const float ma = ua.x * ua.x + ua.y * ua.y, mb = ub.x * ub.x + ub.y * ub.y;
+        float nu2 = ma + mb, nv2 = (wa.x * wa.x + wa.y * wa.y) + (wb.x * wb.x + wb.y * wb.y);
+        float bn;
+        int nr;
+        cta_reduce2<true, true>(ma, ta, !usedA, mb, tb, !usedB, bn, nr, nu2, nv2, slotB, sumB);
+        norm2 += nu2 * nv2;
+        ++k;
+        if (nu2 * nv2 <= tol * tol * norm2) break;
+        if (bn < 0.0f) break;  // every row taken
+        r = nr;
+    }
+    // ---- the exact entries judge the approximation: every row once at a
+    // hashed column, every column once at a hashed row (as k_aca)
+    float e2 = 0.0f, x2 = 0.0f;
+    const bool converged = k > 0 && k < K;
+    __syncthreads();
+    if (converged) {
+        const int ks = min(k, RS);
+#pragma unroll 1
+        for (int q = 0; q < 4; ++q) {
+            const int tt = (q & 1) ? tb : ta, h2 = q >> 1;  // samples tt and tt + 256
+            const int s = tt + kTile * h2;
+            unsigned h = (unsigned)b * 2654435761u + (unsigned)s * 40503u + 12345u;
+            h ^= h >> 13;
+            h *= 0x5bd1e995u;
+            h ^= h >> 15;
+            const int jj = h2 == 0 ? tt : (int)(h & 255u), ii = h2 == 0 ? (int)(h & 255u) : tt;
+            if (ii < ni && jj < nj) {
+                const bool bit = bc == kFlagBits ? block_bit(bw, pitch, jj, ii) : true;
+                const float2 ex = lr_entry<ATT>(a, bc, bit, sFrag[0][ii], sFrag[1][ii], sFrag[2][jj], sFrag[3][jj]);
+                float2 ap = z2;
+                for (int m = 0; m < ks; ++m) ap = csub_mul(ap, sU[m * kTile + jj], sV[m * kTile + ii]);
+                for (int m = RS; m < k; ++m) ap = csub_mul(ap, Ub[m * kTile + jj], Vb[m * kTile + ii]);
+                e2 += (ex.x + ap.x) * (ex.x + ap.x) + (ex.y + ap.y) * (ex.y + ap.y);
+                x2 += ex.x * ex.x + ex.y * ex.y;
+            }
+        }
+    }
+    {
+        float f;
+        int fi;
+        cta_reduce2<false, true>(0.0f, 0, false, 0.0f, 0, false, f, fi, e2, x2, nullptr, sumB);
+    }
+    const float rel = x2 > 0.0f ? sqrtf(e2 / x2) : (e2 > 0.0f ? 1.0f : 0.0f);  // the same in every thread
+    const bool accepted = converged && rel <= limit;
+    if (t == 0) {
+        rank[b] = accepted ? k : -1;
+        fro[b] = sqrtf(norm2);
+        err[b] = converged ? rel : -1.0f;
+    }
+    if (brow && accepted) {
+        // the fragment staging is free now: weights and projections of the apply
+        float4 *sW = &sFrag[0][0];
+        float2 *sTv = reinterpret_cast<float2 *>(&sFrag[1][0]), *sSu = sTv + kLrMaxRank;
+        lr_block_apply<kAca2Threads>(a, I, J, Ub, Vb, k, brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv,
+                                     sSu);
     }
 }
 
@@ -3189,6 +3487,21 @@ void launch_aca_panel_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls
                                                                        U, V, rank, fro, err, brow, bcol);
 }
 
+template <bool ATT, int RS, int MINB>
+void launch_aca2_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
+                   int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
+                   cudaStream_t s, float2 *brow, float2 *bcol)
+{
+    const size_t smem = (size_t)2 * RS * kTile * sizeof(float2);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_aca2<ATT, RS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    k_aca2<ATT, RS, MINB><<<(unsigned)nblocks, kAca2Threads, smem, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit,
+                                                                         U, V, rank, fro, err, brow, bcol);
+}
+
 template <bool ATT>
 bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap,
                   const long long *off, int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro,
@@ -3199,6 +3512,9 @@ bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8
     case 4: launch_aca_panel_t<ATT, 8, 2>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 5: launch_aca_panel_t<ATT, 4, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 6: launch_aca_panel_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 7: launch_aca2_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 8: launch_aca2_t<ATT, 6, 5>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 9: launch_aca2_t<ATT, 4, 6>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 1: launch_aca_t<ATT, 12, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     case 2: launch_aca_t<ATT, 16, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     default: launch_aca_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
