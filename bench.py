@@ -995,11 +995,12 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
     ap.add_argument("--mode", default="both", choices=["both", "plain", "compressed"])
-    ap.add_argument("--aca-variant", type=int, default=0, choices=tuple(range(10)),
+    ap.add_argument("--aca-variant", type=int, default=0, choices=tuple(range(12)),
                     help="cross-approximation kernel: 0 = 8 factor ranks in shared memory, 4 CTAs per SM; "
                          "1 = 12 ranks, 4 CTAs; 2 = 16 ranks, 3 CTAs; panel form (4 pivot rows per step): "
                          "3 = 8 ranks, 3 CTAs; 4 = 8 ranks, 2 CTAs; 5 = 4 ranks, 4 CTAs; 6 = 8 ranks, 4 CTAs; two rows and "
-                         "columns per thread (128 threads): 7 = 8 ranks, 4 CTAs; 8 = 6 ranks, 5 CTAs; 9 = 4 ranks, 6 CTAs")
+                         "columns per thread (128 threads): 7 = 8 ranks, 4 CTAs; 8 = 6 ranks, 5 CTAs; 9 = 4 ranks, 6 CTAs; "
+                         "10 = 2 ranks, 8 CTAs; 11 = 3 ranks, 7 CTAs")
     ap.add_argument("--fused-apply", type=int, default=1, choices=(0, 1),
                     help="cross approximation: apply the accepted blocks to the first bounce's inputs in the same "
                          "kernel")

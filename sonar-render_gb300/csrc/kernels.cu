@@ -3515,6 +3515,8 @@ bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8
     case 7: launch_aca2_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 8: launch_aca2_t<ATT, 6, 5>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 9: launch_aca2_t<ATT, 4, 6>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 10: launch_aca2_t<ATT, 2, 8>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 11: launch_aca2_t<ATT, 3, 7>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 1: launch_aca_t<ATT, 12, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     case 2: launch_aca_t<ATT, 16, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     default: launch_aca_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;

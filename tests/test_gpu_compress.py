@@ -101,7 +101,7 @@ def test_cross_approximation_variants_identical(api, scenes):
     assert np.array_equal(out[0], out[1])
     assert np.array_equal(out[0], out[2])
     with pytest.raises(api.SonarError):
-        api.set_option("aca_variant", 10)
+        api.set_option("aca_variant", 12)
 
 
 def test_panel_cross_approximation(api, oracle_mod, scenes):
