@@ -178,7 +178,6 @@ TOL = [5e-4]   # cross-approximation tolerance (the judge accepts 3 x this RMS e
 ACA_VARIANT = [0]  # cross-approximation kernel shape (factor ranks in shared memory, CTAs per SM)
 OVERLAP = [1]      # compressed bounce: low-rank apply on a second stream beside the dense remainder
 FUSED = [1]        # cross approximation: the first bounce's low-rank apply fused into it
-FP16F = [1]        # cross-approximation variants 7-11: factors stored as scaled FP16 columns
 
 
 def set_path(api, compressed, select):
@@ -189,7 +188,6 @@ def set_path(api, compressed, select):
     api.set_option("compress_judge", 3.0 * TOL[0])
     api.set_option("aca_variant", ACA_VARIANT[0])
     api.set_option("aca_fused_apply", FUSED[0])
-    api.set_option("factors_fp16", FP16F[0])
     api.set_option("overlap_streams", OVERLAP[0])
 
 
@@ -1003,8 +1001,6 @@ def main():
                          "3 = 8 ranks, 3 CTAs; 4 = 8 ranks, 2 CTAs; 5 = 4 ranks, 4 CTAs; 6 = 8 ranks, 4 CTAs; two rows and "
                          "columns per thread (128 threads): 7 = 8 ranks, 4 CTAs; 8 = 6 ranks, 5 CTAs; 9 = 4 ranks, 6 CTAs; "
                          "10 = 2 ranks, 8 CTAs; 11 = 3 ranks, 7 CTAs")
-    ap.add_argument("--fp16-factors", type=int, default=1, choices=(0, 1),
-                    help="cross-approximation variants 7-11: store the factors as FP16 columns scaled to unit RMS")
     ap.add_argument("--fused-apply", type=int, default=1, choices=(0, 1),
                     help="cross approximation: apply the accepted blocks to the first bounce's inputs in the same "
                          "kernel")
@@ -1032,7 +1028,6 @@ def main():
     ACA_VARIANT[0] = args.aca_variant
     OVERLAP[0] = args.overlap
     FUSED[0] = args.fused_apply
-    FP16F[0] = args.fp16_factors
     TOL[0] = args.tol
     if args.impl == "reference":
         run_reference(args)

@@ -29,8 +29,6 @@
 //   G(r) = -e^{ikr}/(4 pi) (ik/r) + 1/r^2,  G_reg = ik/(4 pi) when r < delta_src.
 #include "sonar_internal.h"
 
-#include <cuda_fp16.h>
-
 #include <algorithm>
 #include <cstdio>
 
@@ -2423,70 +2421,6 @@ __device__ __forceinline__ void lr_block_apply(const SumArgs &a, int I, int J, c
     }
 }
 
-// The same apply from FP16 factors: column m of U (V) is su_m (sv_m) times
-// the stored __half2 column.  The scales fold into the projections (tv_m =
-// su_m sv_m sum_i v16(i, m) w_i, likewise su), so the inner loops convert
-// and multiply the stored values only.  FP32 accumulation throughout.
-template <int NT = kTile>
-__device__ __forceinline__ void lr_block_apply_h(const SumArgs &a, int I, int J, const __half2 *U0, const __half2 *V0,
-                                                 const float2 *sc, int k, float2 *brow_b, float2 *bcol_b, float4 *sW,
-                                                 float2 *sTv, float2 *sSu)
-{
-    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    __syncthreads();
-#pragma unroll
-    for (int h = 0; h < kTile / NT; ++h) {
-        const int tt = t + h * NT, i = I * kTile + tt, j = J * kTile + tt;
-        sW[tt] = make_float4(i < a.nsrc ? a.srcA[i].w : 0.0f, i < a.nsrc ? a.srcB[i].w : 0.0f,
-                             j < a.nsrc ? a.srcA[j].w : 0.0f, j < a.nsrc ? a.srcB[j].w : 0.0f);
-    }
-    __syncthreads();
-    for (int m = warp; m < k; m += NT / 32) {
-        float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-#pragma unroll
-        for (int r = 0; r < kTile / 32; ++r) {
-            const int tt = lane + 32 * r;
-            const float2 v = __half22float2(V0[(size_t)m * kTile + tt]), u = __half22float2(U0[(size_t)m * kTile + tt]);
-            const float4 w = sW[tt];
-            p.x = fmaf(v.x, w.x, fmaf(-v.y, w.y, p.x));
-            p.y = fmaf(v.x, w.y, fmaf(v.y, w.x, p.y));
-            p.z = fmaf(u.x, w.z, fmaf(-u.y, w.w, p.z));
-            p.w = fmaf(u.x, w.w, fmaf(u.y, w.z, p.w));
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            p.x += __shfl_xor_sync(0xffffffffu, p.x, o);
-            p.y += __shfl_xor_sync(0xffffffffu, p.y, o);
-            p.z += __shfl_xor_sync(0xffffffffu, p.z, o);
-            p.w += __shfl_xor_sync(0xffffffffu, p.w, o);
-        }
-        if (lane == 0) {
-            const float2 f = sc[m];
-            const float g = f.x * f.y;
-            sTv[m] = make_float2(p.x * g, p.y * g);
-            sSu[m] = make_float2(p.z * g, p.w * g);
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int h = 0; h < kTile / NT; ++h) {
-        const int tt = t + h * NT;
-        const __half2 *Ub = U0 + tt, *Vb = V0 + tt;
-        float rr = 0.0f, ri = 0.0f, cr = 0.0f, ci = 0.0f;
-#pragma unroll 4
-        for (int m = 0; m < k; ++m) {
-            const float2 u = __half22float2(Ub[m * kTile]), v = __half22float2(Vb[m * kTile]);
-            const float2 c = sTv[m], e = sSu[m];
-            rr += u.x * c.x - u.y * c.y;
-            ri += u.x * c.y + u.y * c.x;
-            cr += v.x * e.x - v.y * e.y;
-            ci += v.x * e.y + v.y * e.x;
-        }
-        brow_b[tt] = make_float2(rr, ri);
-        bcol_b[tt] = make_float2(cr, ci);
-    }
-}
-
 // ---------------------------------------------------------------- panel cross approximation
 // The same approximation taken kPanel pivot rows at a time.  A panel step
 //   A. computes the residual rows of the panel's kPanel rows (every thread
@@ -2909,17 +2843,11 @@ __device__ __forceinline__ void cta_reduce2(float va, int ia, bool oka, float vb
     }
 }
 
-// F16: persistent CTAs (grid = resident CTAs, block b = blockIdx.x, +grid,
-// ...); ranks past RS live in this CTA's FP32 scratch slot instead of the
-// factor arrays, and an accepted block's factors are written once, as FP16
-// columns scaled to unit RMS (scale = the rank's norm / 16, from the sums the
-// stopping rule reduces anyway), which the apply reads at half the bytes.
-template <bool ATT, int RS, int MINB, bool F16>
+template <bool ATT, int RS, int MINB>
 __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const int2 *blocks, const uint8_t *cls,
                                                              const int *cap, const long long *off, int nblocks,
                                                              float tol, float limit, float2 *U, float2 *V, int *rank,
-                                                             float *fro, float *err, float2 *brow, float2 *bcol,
-                                                             LrHalf hf)
+                                                             float *fro, float *err, float2 *brow, float2 *bcol)
 {
     extern __shared__ float2 aca_smem[];  // sU[RS][kTile], then sV[RS][kTile]
     float2 *sU = aca_smem, *sV = aca_smem + RS * kTile;
@@ -2927,33 +2855,22 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
     __shared__ float4 sFrag[4][kTile];  // position and normal of the columns' (I) and rows' (J) fragments
     __shared__ __align__(16) unsigned slotA[kAca2Warps], slotB[kAca2Warps], slotZ[kAca2Warps];
     __shared__ __align__(16) float2 sumB[kAca2Warps];
-    __shared__ float2 sNorm[F16 ? kLrRankLimit : 1];  // per rank: |u|^2, |v|^2
-    const int t = threadIdx.x;
+    const int t = threadIdx.x, b = blockIdx.x;
     const int ta = t, tb = t + kAca2Threads;  // this thread's two rows / columns
-    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    const float2 z2 = make_float2(0.0f, 0.0f);
-    for (int b = blockIdx.x; b < nblocks; b += (F16 ? gridDim.x : nblocks)) {
-    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = min(cap[b], F16 ? RS + hf.scratch_ranks : kLrRankLimit);
+    if (b >= nblocks) return;  // CTA-uniform
+    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = min(cap[b], kLrRankLimit);
     const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
     const float4 *PI = a.srcA + I * kTile, *NI = a.srcB + I * kTile, *PJ = a.srcA + J * kTile, *NJ = a.srcB + J * kTile;
-    // FP32 storage of the ranks past RS (and, without F16, of every rank)
-    float2 *Ub, *Vb;
-    if (F16) {
-        float2 *slot = hf.scratch + (size_t)blockIdx.x * 2 * hf.scratch_ranks * kTile;
-        Ub = slot - (size_t)RS * kTile;  // indexed by rank m >= RS
-        Vb = slot + (size_t)(hf.scratch_ranks - RS) * kTile;
-    } else {
-        Ub = U + off[b] * kTile;
-        Vb = V + off[b] * kTile;
-    }
+    float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
     const uint32_t *bw = a.mask.bits + (long long)I * kWordsPerTile * a.mask.pitch + (long long)J * kTile;
     const long long pitch = a.mask.pitch;
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float2 z2 = make_float2(0.0f, 0.0f);
     const bool colA = ta < ni, colB = tb < ni, rowA = ta < nj, rowB = tb < nj;
     const float4 piA = colA ? __ldg(PI + ta) : z4, qiA = colA ? __ldg(NI + ta) : z4;
     const float4 piB = colB ? __ldg(PI + tb) : z4, qiB = colB ? __ldg(NI + tb) : z4;
     const float4 pjA = rowA ? __ldg(PJ + ta) : z4, qjA = rowA ? __ldg(NJ + ta) : z4;
     const float4 pjB = rowB ? __ldg(PJ + tb) : z4, qjB = rowB ? __ldg(NJ + tb) : z4;
-    __syncthreads();  // the previous block's readers of the shared arrays are done
     sFrag[0][ta] = piA; sFrag[0][tb] = piB;
     sFrag[1][ta] = qiA; sFrag[1][tb] = qiB;
     sFrag[2][ta] = pjA; sFrag[2][tb] = pjB;
@@ -3003,13 +2920,11 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
         const float inv = __frcp_rn(pv.x * pv.x + pv.y * pv.y);
         const float2 wa = colA ? make_float2((va.x * pv.x + va.y * pv.y) * inv, (va.y * pv.x - va.x * pv.y) * inv) : z2;
         const float2 wb = colB ? make_float2((vb.x * pv.x + vb.y * pv.y) * inv, (vb.y * pv.x - vb.x * pv.y) * inv) : z2;
+        Vb[k * kTile + ta] = wa;
+        Vb[k * kTile + tb] = wb;
         if (k < RS) {
             sV[k * kTile + ta] = wa;
             sV[k * kTile + tb] = wb;
-        }
-        if (!F16 || k >= RS) {
-            Vb[k * kTile + ta] = wa;
-            Vb[k * kTile + tb] = wb;
         }
         // ---- residual column c, entries (ta, c) and (tb, c)
         float2 ua = z2, ub = z2;
@@ -3028,13 +2943,11 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
                 ub = csub_mul(ub, Ub[m * kTile + tb], vc);
             }
         }
+        Ub[k * kTile + ta] = ua;
+        Ub[k * kTile + tb] = ub;
         if (k < RS) {
             sU[k * kTile + ta] = ua;
             sU[k * kTile + tb] = ub;
-        }
-        if (!F16 || k >= RS) {
-            Ub[k * kTile + ta] = ua;
-            Ub[k * kTile + tb] = ub;
         }
         if (ta == r) usedA = true;
         if (tb == r) usedB = true;
@@ -3044,7 +2957,6 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
         float bn;
         int nr;
         cta_reduce2<true, true>(ma, ta, !usedA, mb, tb, !usedB, bn, nr, nu2, nv2, slotB, sumB);
-        if (F16 && t == 0) sNorm[k] = make_float2(nu2, nv2);
         norm2 += nu2 * nv2;
         ++k;
         if (nu2 * nv2 <= tol * tol * norm2) break;
@@ -3090,41 +3002,13 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
         fro[b] = sqrtf(norm2);
         err[b] = converged ? rel : -1.0f;
     }
-    if (F16 && accepted) {
-        // the block's factors as FP16 columns of unit RMS: entry / scale,
-        // scale = sqrt(|column|^2 / 256)
-        __half2 *U16 = reinterpret_cast<__half2 *>(hf.U16) + off[b] * kTile;
-        __half2 *V16 = reinterpret_cast<__half2 *>(hf.V16) + off[b] * kTile;
-        for (int m = 0; m < k; ++m) {
-            const float2 nn = sNorm[m];
-            const float su = nn.x > 0.0f ? sqrtf(nn.x * (1.0f / kTile)) : 1.0f;
-            const float sv = nn.y > 0.0f ? sqrtf(nn.y * (1.0f / kTile)) : 1.0f;
-            const float iu = 1.0f / su, iv = 1.0f / sv;
-            const float2 u0 = m < RS ? sU[m * kTile + ta] : Ub[m * kTile + ta];
-            const float2 u1 = m < RS ? sU[m * kTile + tb] : Ub[m * kTile + tb];
-            const float2 v0 = m < RS ? sV[m * kTile + ta] : Vb[m * kTile + ta];
-            const float2 v1 = m < RS ? sV[m * kTile + tb] : Vb[m * kTile + tb];
-            U16[m * kTile + ta] = __floats2half2_rn(u0.x * iu, u0.y * iu);
-            U16[m * kTile + tb] = __floats2half2_rn(u1.x * iu, u1.y * iu);
-            V16[m * kTile + ta] = __floats2half2_rn(v0.x * iv, v0.y * iv);
-            V16[m * kTile + tb] = __floats2half2_rn(v1.x * iv, v1.y * iv);
-            if (t == 0) hf.scale[off[b] + m] = make_float2(su, sv);
-        }
-    }
     if (brow && accepted) {
         // the fragment staging is free now: weights and projections of the apply
         float4 *sW = &sFrag[0][0];
         float2 *sTv = reinterpret_cast<float2 *>(&sFrag[1][0]), *sSu = sTv + kLrMaxRank;
-        if (F16)
-            lr_block_apply_h<kAca2Threads>(a, I, J, reinterpret_cast<const __half2 *>(hf.U16) + off[b] * kTile,
-                                           reinterpret_cast<const __half2 *>(hf.V16) + off[b] * kTile,
-                                           hf.scale + off[b], k, brow + (size_t)b * kTile, bcol + (size_t)b * kTile,
-                                           sW, sTv, sSu);
-        else
-            lr_block_apply<kAca2Threads>(a, I, J, Ub, Vb, k, brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW,
-                                         sTv, sSu);
+        lr_block_apply<kAca2Threads>(a, I, J, Ub, Vb, k, brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv,
+                                     sSu);
     }
-    }  // blocks of this CTA
 }
 
 // Block descriptors of the admissibility network, one warp per block:
@@ -3189,26 +3073,19 @@ __global__ void __launch_bounds__(128) k_block_desc(SumArgs a, const int2 *block
 }
 
 // Compressed bounce, one CTA per accepted block q (kept block b = bidx[q]):
-// lr_block_apply (FP32 factors) or lr_block_apply_h (FP16 factors, hf.U16
-// set) into the block's output slots b.  The factors are read from HBM once;
-// the second pass over them hits L2.
+// lr_block_apply into the block's output slots b.  The factors are read from
+// HBM once; the second pass over them hits L2.
 __global__ void __launch_bounds__(kTile) k_lr_block(SumArgs a, const int2 *blocks, const long long *off,
                                                     const int *bidx, int nb, const float2 *U, const float2 *V,
-                                                    const int *rank, float2 *brow, float2 *bcol, const int *ndev,
-                                                    LrHalf hf)
+                                                    const int *rank, float2 *brow, float2 *bcol, const int *ndev)
 {
     __shared__ float4 sW[kTile];  // (Re w_I, Im w_I, Re w_J, Im w_J) of every row t
     __shared__ float2 sTv[kLrMaxRank], sSu[kLrMaxRank];
     const int q = blockIdx.x;
     if (q >= (ndev ? min(*ndev, nb) : nb)) return;
     const int b = bidx[q];
-    if (hf.U16)
-        lr_block_apply_h(a, blocks[b].x, blocks[b].y, reinterpret_cast<const __half2 *>(hf.U16) + off[b] * kTile,
-                         reinterpret_cast<const __half2 *>(hf.V16) + off[b] * kTile, hf.scale + off[b], rank[b],
-                         brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv, sSu);
-    else
-        lr_block_apply(a, blocks[b].x, blocks[b].y, U + off[b] * kTile, V + off[b] * kTile, rank[b],
-                       brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv, sSu);
+    lr_block_apply(a, blocks[b].x, blocks[b].y, U + off[b] * kTile, V + off[b] * kTile, rank[b],
+                   brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv, sSu);
 }
 
 // Per owner tile X: rows of every accepted block with J = X and columns of
@@ -3613,41 +3490,33 @@ void launch_aca_panel_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls
 template <bool ATT, int RS, int MINB>
 void launch_aca2_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                    int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
-                   cudaStream_t s, float2 *brow, float2 *bcol, const LrHalf *half, int nsm)
+                   cudaStream_t s, float2 *brow, float2 *bcol)
 {
     const size_t smem = (size_t)2 * RS * kTile * sizeof(float2);
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_aca2<ATT, RS, MINB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_aca2<ATT, RS, MINB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_aca2<ATT, RS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
-    if (half) {
-        const int grid = std::min(nblocks, MINB * std::max(nsm, 1));
-        k_aca2<ATT, RS, MINB, true><<<(unsigned)grid, kAca2Threads, smem, s>>>(a, blocks, cls, cap, off, nblocks, tol,
-                                                                               limit, U, V, rank, fro, err, brow, bcol,
-                                                                               *half);
-    } else {
-        k_aca2<ATT, RS, MINB, false><<<(unsigned)nblocks, kAca2Threads, smem, s>>>(
-            a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro, err, brow, bcol, LrHalf{});
-    }
+    k_aca2<ATT, RS, MINB><<<(unsigned)nblocks, kAca2Threads, smem, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit,
+                                                                         U, V, rank, fro, err, brow, bcol);
 }
 
 template <bool ATT>
 bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap,
                   const long long *off, int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro,
-                  float limit, float *err, cudaStream_t s, float2 *brow, float2 *bcol, const LrHalf *half, int nsm)
+                  float limit, float *err, cudaStream_t s, float2 *brow, float2 *bcol)
 {
     switch (variant) {
     case 3: launch_aca_panel_t<ATT, 8, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 4: launch_aca_panel_t<ATT, 8, 2>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 5: launch_aca_panel_t<ATT, 4, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 6: launch_aca_panel_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 7: launch_aca2_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, half, nsm); return brow != nullptr;
-    case 8: launch_aca2_t<ATT, 6, 5>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, half, nsm); return brow != nullptr;
-    case 9: launch_aca2_t<ATT, 4, 6>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, half, nsm); return brow != nullptr;
-    case 10: launch_aca2_t<ATT, 2, 8>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, half, nsm); return brow != nullptr;
-    case 11: launch_aca2_t<ATT, 3, 7>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, half, nsm); return brow != nullptr;
+    case 7: launch_aca2_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 8: launch_aca2_t<ATT, 6, 5>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 9: launch_aca2_t<ATT, 4, 6>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 10: launch_aca2_t<ATT, 2, 8>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 11: launch_aca2_t<ATT, 3, 7>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 1: launch_aca_t<ATT, 12, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     case 2: launch_aca_t<ATT, 16, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     default: launch_aca_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
@@ -3661,25 +3530,16 @@ bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8
 // 6.69 ms); 1: 12 ranks, 4 CTAs; 2: 16 ranks, 3 CTAs; the panel form
 // (k_aca_panel): 3: 8 ranks, 3 CTAs; 4: 8 ranks, 2 CTAs; 5: 4 ranks, 4 CTAs;
 // 6: 8 ranks, 4 CTAs
-bool aca_variant_f16(int variant) { return variant >= 7 && variant <= 11; }
-
-int aca_grid_ctas(int variant, int nsm)
-{
-    const int per_sm = variant == 7 ? 4 : variant == 8 ? 5 : variant == 9 ? 6 : variant == 10 ? 8 : 7;
-    return per_sm * std::max(nsm, 1);
-}
-
 bool launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                 int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
-                cudaStream_t s, int variant, float2 *brow, float2 *bcol, const LrHalf *half, int nsm)
+                cudaStream_t s, int variant, float2 *brow, float2 *bcol)
 {
     if (nblocks <= 0) return false;
-    if (!aca_variant_f16(variant)) half = nullptr;
     if (a.ka != 0.0f)
         return launch_aca_v<true>(variant, a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow,
-                                  bcol, half, nsm);
+                                  bcol);
     return launch_aca_v<false>(variant, a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow,
-                               bcol, half, nsm);
+                               bcol);
 }
 
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
@@ -3692,10 +3552,9 @@ void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls,
 void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
                      const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
-                     double2 *ycol, cudaStream_t s, const int *ndev, bool outputs_ready, const LrHalf *half)
+                     double2 *ycol, cudaStream_t s, const int *ndev, bool outputs_ready)
 {
-    if (nb > 0 && !outputs_ready)
-        k_lr_block<<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev, half ? *half : LrHalf{});
+    if (nb > 0 && !outputs_ready) k_lr_block<<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev);
     if (ntiles > 0)
         k_lr_gather<<<ntiles, kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, bidx, yrow, ycol);
 }

@@ -196,8 +196,6 @@ struct Compression {
     int *d_kmap = nullptr, *d_acap = nullptr;  // kept block -> candidate, rank caps
     bool stats_pending = false;     // statistics and timings not read back yet
     bool outputs_ready = false;     // the build also wrote the block outputs of its bounce's inputs
-    bool fp16 = false;              // factors stored as FP16 columns (half)
-    LrHalf half;
     // descriptors and rank labels of the approximated blocks (network training)
     std::vector<float> desc, label;
     Arena arena;    // the candidate- and block-level arrays above
@@ -280,8 +278,7 @@ struct Model {
     int opt_cmp_select = 0;     // 0 rule (class ALL, eta-separated), 1 every interacting block, 2 the network
     float opt_cmp_rcut = 24.0f; // network: propose blocks whose predicted rank is below this
     int opt_aca_variant = 0;    // cross-approximation kernel shape (factor ranks in shared memory, CTAs per SM)
-    int opt_fused_apply = 1;    // cross approximation: apply the accepted blocks to the building bounce's inputs
-    int opt_fp16_factors = 1;   // cross-approximation variants 7-11: factors stored as scaled FP16 columns
+    int opt_fused_apply = 1;    // panel cross approximation: apply the accepted blocks to the building bounce's inputs
     int opt_mask_classify = 1;  // bounce masks: warp-per-block classification, pair kernel on the listed blocks
     int opt_gate_proj = 1;      // bounce masks: gates decided from per-point projections where certain
     int opt_cross_objects = 0;  // bounces also between different targets (FACET_RESP); 0: the reference's behaviour
@@ -823,11 +820,6 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
 {
     Compression &C = g.cmp;
     C.release();
-    if (g.nsm == 0) {
-        int dev = 0;
-        CK(cudaGetDevice(&dev));
-        CK(cudaDeviceGetAttribute(&g.nsm, cudaDevAttrMultiProcessorCount, dev));
-    }
     const int nt = M.view.ntiles, nb = M.view.ndstblocks;
     const int rmax = std::min(g.opt_cmp_rmax, kLrRankLimit);
     const int select = g.opt_cmp_select;
@@ -893,28 +885,10 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     C.kr = g.kr;
     C.ki = g.ki;
     // ---- cross approximation of the kept blocks
-    C.fp16 = g.opt_fp16_factors && aca_variant_f16(g.opt_aca_variant);
-    const size_t ncol = (size_t)std::max<long long>(cols, 1);
-    const int nslots = C.fp16 ? aca_grid_ctas(g.opt_aca_variant, g.nsm) : 0;
-    if (C.fp16)
-        C.factors.reserve(2 * Arena::bytes_of(ncol * kTile, 4) + Arena::bytes_of(ncol, sizeof(float2)) +
-                          Arena::bytes_of((size_t)nslots * 2 * rmax * kTile, sizeof(float2)) +
-                          2 * Arena::bytes_of((size_t)std::max(n, 1) * kTile, sizeof(float2)));
-    else
-        C.factors.reserve(2 * Arena::bytes_of(ncol * kTile, sizeof(float2)) +
-                          2 * Arena::bytes_of((size_t)std::max(n, 1) * kTile, sizeof(float2)));
-    C.half = LrHalf{};
-    if (C.fp16) {
-        C.d_U = C.d_V = nullptr;
-        C.half.U16 = C.factors.take<uint32_t>(ncol * kTile);  // __half2
-        C.half.V16 = C.factors.take<uint32_t>(ncol * kTile);
-        C.half.scale = C.factors.take<float2>(ncol);
-        C.half.scratch = C.factors.take<float2>((size_t)nslots * 2 * rmax * kTile);
-        C.half.scratch_ranks = rmax;
-    } else {
-        C.d_U = C.factors.take<float2>(ncol * kTile);
-        C.d_V = C.factors.take<float2>(ncol * kTile);
-    }
+    C.factors.reserve(2 * Arena::bytes_of((size_t)std::max<long long>(cols, 1) * kTile, sizeof(float2)) +
+                      2 * Arena::bytes_of((size_t)std::max(n, 1) * kTile, sizeof(float2)));
+    C.d_U = C.factors.take<float2>((size_t)std::max<long long>(cols, 1) * kTile);
+    C.d_V = C.factors.take<float2>((size_t)std::max<long long>(cols, 1) * kTile);
     C.d_brow = C.factors.take<float2>((size_t)std::max(n, 1) * kTile);
     C.d_bcol = C.factors.take<float2>((size_t)std::max(n, 1) * kTile);
     C.d_rank = ar.take<int>(nmax);
@@ -924,8 +898,7 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     // inputs: the first bounce's low-rank apply then only gathers
     C.outputs_ready = launch_aca(s, C.d_blocks, C.d_cls, C.d_acap, C.d_off, n, g.opt_cmp_tol, C.d_U, C.d_V, C.d_rank,
                                  C.d_fro, g.opt_cmp_judge, C.d_err, st, g.opt_aca_variant,
-                                 g.opt_fused_apply ? C.d_brow : nullptr, g.opt_fused_apply ? C.d_bcol : nullptr,
-                                 C.fp16 ? &C.half : nullptr, g.nsm);
+                                 g.opt_fused_apply ? C.d_brow : nullptr, g.opt_fused_apply ? C.d_bcol : nullptr);
     CK(cudaGetLastError());
     CK(cudaEventRecord(g.evb[2], st));
     // ---- accepted blocks: dense flags off, owner lists, statistics
@@ -1097,7 +1070,7 @@ void run_hop(int hop, int a, int b)
                 CK(cudaEventRecord(g.ev4, lst));
                 launch_lr_apply(s, C.d_blocks, C.d_off, C.d_bidx, C.nblocks, C.d_U, C.d_V, C.d_rank, C.d_brow, C.d_bcol,
                                 M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, lst,
-                                C.d_nacc, built && C.outputs_ready, C.fp16 ? &C.half : nullptr);
+                                C.d_nacc, built && C.outputs_ready);
                 CK(cudaEventRecord(g.ev5, lst));
                 if (g.opt_overlap) CK(cudaEventRecord(g.ev_join, lst));
                 yrow = C.d_yrow;
@@ -1702,7 +1675,6 @@ int sonar_set_option(const char *key, double value)
         return 0;
     }
     if (!strcmp(key, "aca_fused_apply")) { g.opt_fused_apply = value != 0.0; g.cmp.release(); return 0; }
-    if (!strcmp(key, "factors_fp16")) { g.opt_fp16_factors = value != 0.0; g.cmp.release(); return 0; }
     if (!strcmp(key, "aca_variant")) {
         if (value < 0 || value > 11) return -1;
         g.opt_aca_variant = (int)value;

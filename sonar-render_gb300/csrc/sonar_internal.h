@@ -152,33 +152,16 @@ void launch_finalize_f2f_sym(const double2 *rowpart, const int *chunk_off, int n
 constexpr int kLrRankLimit = 64;
 // Returns true when the kernel also wrote the low-rank apply's block outputs
 // for the packed inputs of this launch (panel variants given brow, bcol).
-// FP16 factor storage of the compressed blocks (cross-approximation
-// variants 7 and up): U16, V16 hold __half2 [columns][kTile] with every
-// factor column scaled to unit RMS, scale the (su, sv) of each column; the
-// kernel keeps its working FP32 ranks past the shared-memory ones in scratch,
-// scratch_ranks columns of U and of V per resident CTA.
-struct LrHalf {
-    void *U16 = nullptr, *V16 = nullptr;
-    float2 *scale = nullptr;
-    float2 *scratch = nullptr;
-    int scratch_ranks = 0;
-};
-// Variants that store FP16 factors; CTAs of their persistent grid (the
-// scratch holds one slot per CTA).
-bool aca_variant_f16(int variant);
-int aca_grid_ctas(int variant, int nsm);
 bool launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                 int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
-                cudaStream_t s, int variant = 0, float2 *brow = nullptr, float2 *bcol = nullptr,
-                const LrHalf *half = nullptr, int nsm = 0);
+                cudaStream_t s, int variant = 0, float2 *brow = nullptr, float2 *bcol = nullptr);
 // ndev (optional): the block count in device memory; nblocks / nb bound the grid
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
                        const float4 *nm, float inv_lambda, float *X, cudaStream_t s, const int *ndev = nullptr);
 void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
                      const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
-                     double2 *ycol, cudaStream_t s, const int *ndev = nullptr, bool outputs_ready = false,
-                     const LrHalf *half = nullptr);
+                     double2 *ycol, cudaStream_t s, const int *ndev = nullptr, bool outputs_ready = false);
 // select.cu: block lists of the compressed bounce, built on the device
 void launch_cand_lists(const uint8_t *flags, int nt, int nb, int select, float eta, const float4 *cen, int *cnt,
                        int *off, int2 *blocks, uint8_t *cls, cudaStream_t s);
