@@ -175,9 +175,9 @@ def step_pairs(stats):
 
 RCUT = [24.0]  # the admissibility network proposes blocks with predicted rank below this
 TOL = [5e-4]   # cross-approximation tolerance (the judge accepts 3 x this RMS error)
-ACA_VARIANT = [0]  # cross-approximation kernel shape (factor ranks in shared memory, CTAs per SM)
+ACA_VARIANT = [5]  # cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
 OVERLAP = [1]      # compressed bounce: low-rank apply on a second stream beside the dense remainder
-FUSED = [1]        # cross approximation: the first bounce's low-rank apply fused into it
+FUSED = [1]        # k_aca2: the first bounce's low-rank apply fused into the cross approximation
 
 
 def set_path(api, compressed, select):
@@ -995,15 +995,13 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
     ap.add_argument("--mode", default="both", choices=["both", "plain", "compressed"])
-    ap.add_argument("--aca-variant", type=int, default=0, choices=tuple(range(12)),
-                    help="cross-approximation kernel: 0 = 8 factor ranks in shared memory, 4 CTAs per SM; "
-                         "1 = 12 ranks, 4 CTAs; 2 = 16 ranks, 3 CTAs; panel form (4 pivot rows per step): "
-                         "3 = 8 ranks, 3 CTAs; 4 = 8 ranks, 2 CTAs; 5 = 4 ranks, 4 CTAs; 6 = 8 ranks, 4 CTAs; two rows and "
-                         "columns per thread (128 threads): 7 = 8 ranks, 4 CTAs; 8 = 6 ranks, 5 CTAs; 9 = 4 ranks, 6 CTAs; "
-                         "10 = 2 ranks, 8 CTAs; 11 = 3 ranks, 7 CTAs")
+    ap.add_argument("--aca-variant", type=int, default=5, choices=tuple(range(8)),
+                    help="cross-approximation kernel: k_aca (one row and column per thread): 0 = 8 factor ranks in "
+                         "shared memory, 4 CTAs per SM; 1 = 12 ranks, 4 CTAs; 2 = 16 ranks, 3 CTAs; k_aca2 (two rows "
+                         "and columns per thread, first bounce's apply fused): 3 = 8 ranks, 4 CTAs; 4 = 6 ranks, "
+                         "5 CTAs; 5 = 4 ranks, 6 CTAs; 6 = 2 ranks, 8 CTAs; 7 = 3 ranks, 7 CTAs")
     ap.add_argument("--fused-apply", type=int, default=1, choices=(0, 1),
-                    help="cross approximation: apply the accepted blocks to the first bounce's inputs in the same "
-                         "kernel")
+                    help="k_aca2: apply the accepted blocks to the first bounce's inputs in the same kernel")
     ap.add_argument("--overlap", type=int, default=1, choices=(0, 1),
                     help="compressed bounce: low-rank apply on a second stream beside the dense remainder")
     ap.add_argument("--tol", type=float, default=5e-4,

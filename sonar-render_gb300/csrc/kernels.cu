@@ -2421,53 +2421,7 @@ __device__ __forceinline__ void lr_block_apply(const SumArgs &a, int I, int J, c
     }
 }
 
-// ---------------------------------------------------------------- panel cross approximation
-// The same approximation taken kPanel pivot rows at a time.  A panel step
-//   A. computes the residual rows of the panel's kPanel rows (every thread
-//      its column t of each: kPanel Green's entries and one pass over the
-//      earlier ranks, each factor entry V(t, m) loaded once for all rows);
-//   B. chooses the panel's pivot columns greedily: row q's pivot column is
-//      the argmax of its residual after the elimination of the panel's
-//      earlier rows (one block argmax per row, the panel rows exchanged
-//      through a shared buffer); v_q = that row / its pivot;
-//   C. computes the residual columns at the chosen columns (every thread its
-//      row t: kPanel entries, one pass over the earlier ranks) and eliminates
-//      the panel's earlier ranks from them: u_q;
-//   then one block reduction carries the 2 kPanel norms of the new ranks and,
-//   per new rank, the argmax of |u_q| over unused rows: the next panel's rows
-//   (duplicates dropped).  The stopping rule is the classic one, applied rank
-//   by rank in the panel's order; ranks past the stop are discarded.  Rows of
-//   a panel that vanish (masked rows) give no rank; a panel without any
-//   continues with the lowest unused row alone.  Per rank this takes
-//   (kPanel + 2) / kPanel barriers instead of two, loads each own factor entry
-//   once per panel instead of once per rank, and evaluates kPanel independent
-//   entries at a time.  Factor layout, judge and outputs are those of k_aca.
-constexpr int kPanel = 4;
-
-// Warp sums of eight values per lane with nine shuffles: at each level a lane
-// keeps the half of its partial sums that its partner does not and adds the
-// partner's copy of them.  Returns the warp total of value (lane >> 2) & 7.
-__device__ __forceinline__ float warp_sum8(const float (&x)[8], int lane)
-{
-    const bool h4 = (lane >> 4) & 1, h3 = (lane >> 3) & 1, h2 = (lane >> 2) & 1;
-    float y[4], z[2];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const float keep = h4 ? x[4 + i] : x[i], send = h4 ? x[i] : x[4 + i];
-        y[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-    }
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        const float keep = h3 ? y[2 + i] : y[i], send = h3 ? y[i] : y[2 + i];
-        z[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-    }
-    const float keep = h2 ? z[1] : z[0], send = h2 ? z[0] : z[1];
-    float w = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-    w += __shfl_xor_sync(0xffffffffu, w, 2);
-    w += __shfl_xor_sync(0xffffffffu, w, 1);
-    return w;
-}
-
+// ---------------------------------------------------------------- block argmax helpers
 // 32-bit argmax key of v >= 0 at index idx < 256 (0: not a candidate): the
 // float bits with the low byte replaced by 255 - idx, as in cta_reduce
 __device__ __forceinline__ unsigned argmax_key(float v, int idx, bool valid)
@@ -2487,309 +2441,6 @@ __device__ __forceinline__ float key_value(unsigned w) { return w ? __uint_as_fl
 __device__ __forceinline__ bool block_bit(const uint32_t *bw, long long pitch, int j, int i)
 {
     return (bw[(long long)(i >> 5) * pitch + j] >> (i & 31)) & 1u;
-}
-
-// brow, bcol (optional): the low-rank apply of every accepted block with the
-// packed inputs of this launch, fused (lr_block_apply into slot b).
-// The panel's row and column indices (< 256) travel packed in one 32-bit
-// word, 8 bits each, so that loops over the panel need no indexed arrays.
-__device__ __forceinline__ int unpack8(unsigned w, int q) { return (int)((w >> (8 * q)) & 0xFFu); }
-
-template <bool ATT, int RS, int MINB>
-__global__ void __launch_bounds__(kTile, MINB) k_aca_panel(SumArgs a, const int2 *blocks, const uint8_t *cls,
-                                                           const int *cap, const long long *off, int nblocks,
-                                                           float tol, float limit, float2 *U, float2 *V, int *rank,
-                                                           float *fro, float *err, float2 *brow, float2 *bcol)
-{
-    extern __shared__ float2 aca_smem[];  // sU[RS][kTile], then sV[RS][kTile]
-    float2 *sU = aca_smem, *sV = aca_smem + RS * kTile;
-    __shared__ float2 sE[2][kPanel][kTile];  // panel rows during the column choice, by step parity
-    __shared__ __align__(16) unsigned sKey[2][kAcaWarps];
-    __shared__ __align__(16) unsigned sRowKey[kPanel][kAcaWarps];
-    __shared__ __align__(16) float sSum[kAcaWarps][2 * kPanel];
-    __shared__ float2 sumB[kAcaWarps];
-    const int t = threadIdx.x, b = blockIdx.x, lane = t & 31, warp = t >> 5;
-    if (b >= nblocks) return;  // CTA-uniform
-    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = min(cap[b], kLrRankLimit);
-    const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
-    const float4 *PI = a.srcA + I * kTile, *NI = a.srcB + I * kTile, *PJ = a.srcA + J * kTile, *NJ = a.srcB + J * kTile;
-    float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
-    const uint32_t *bw = a.mask.bits + (long long)I * kWordsPerTile * a.mask.pitch + (long long)J * kTile;
-    const long long pitch = a.mask.pitch;
-    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    const float2 z2 = make_float2(0.0f, 0.0f);
-    const bool coli = t < ni, rowj = t < nj;
-    const float4 pi = coli ? __ldg(PI + t) : z4, qi = coli ? __ldg(NI + t) : z4;
-    const float4 pj = rowj ? __ldg(PJ + t) : z4, qj = rowj ? __ldg(NJ + t) : z4;
-    bool colused = !coli, rowused = !rowj;
-    // the first panel's rows spread over the tile (rows 0 .. nj - 1 when nj < kPanel)
-    unsigned rows = 0u;
-    int nr = min(nj, kPanel);
-#pragma unroll
-    for (int q = 0; q < kPanel; ++q) rows |= (unsigned)(nj < kPanel ? q : (q * nj) / kPanel) << (8 * q);
-    int k = 0, zero_rows = 0;
-    float norm2 = 0.0f;
-    bool done = nr == 0;
-    while (!done && k < K) {
-        const int ks = min(k, RS);
-        // ---- A. residual rows of the panel at column t: entries, then one pass over the earlier ranks
-        float2 e0 = z2, e1 = z2, e2 = z2, e3 = z2;
-        if (coli) {
-#pragma unroll 1
-            for (int q = 0; q < nr; ++q) {
-                const int r = unpack8(rows, q);
-                const bool bit = bc == kFlagBits ? block_bit(bw, pitch, r, t) : true;
-                const float2 x = lr_entry<ATT>(a, bc, bit, pi, qi, __ldg(PJ + r), __ldg(NJ + r));
-                e0 = q == 0 ? x : e0;
-                e1 = q == 1 ? x : e1;
-                e2 = q == 2 ? x : e2;
-                e3 = q == 3 ? x : e3;
-            }
-            const int r0 = unpack8(rows, 0), r1 = unpack8(rows, 1), r2 = unpack8(rows, 2), r3 = unpack8(rows, 3);
-            for (int m = 0; m < ks; ++m) {
-                const float2 v = sV[m * kTile + t];
-                const float2 *Um = sU + m * kTile;
-                e0 = csub_mul(e0, Um[r0], v);
-                e1 = csub_mul(e1, Um[r1], v);
-                e2 = csub_mul(e2, Um[r2], v);
-                e3 = csub_mul(e3, Um[r3], v);
-            }
-            for (int m = RS; m < k; ++m) {
-                const float2 v = Vb[m * kTile + t];
-                const float2 *Um = Ub + m * kTile;
-                e0 = csub_mul(e0, Um[r0], v);
-                e1 = csub_mul(e1, Um[r1], v);
-                e2 = csub_mul(e2, Um[r2], v);
-                e3 = csub_mul(e3, Um[r3], v);
-            }
-            // panel slots past nr hold a repeated row: their values are never used
-        }
-#pragma unroll
-        for (int q = 0; q < kPanel; ++q)
-            if (q < nr && t == unpack8(rows, q)) rowused = true;
-        // ---- B. pivot columns, greedy within the panel
-        unsigned cols = 0u;
-        float2 v0 = z2, v1 = z2, v2 = z2, v3 = z2;
-        int np = 0;
-        const int room = K - k;  // ranks that still fit under the cap
-#pragma unroll
-        for (int q = 0; q < kPanel; ++q) {
-            if (q >= nr || np >= room) break;  // uniform
-            const int buf = q & 1;
-            const float2 eq = q == 0 ? e0 : q == 1 ? e1 : q == 2 ? e2 : e3;
-            if (q <= 0) sE[buf][0][t] = e0;
-            if (q <= 1 && nr > 1) sE[buf][1][t] = e1;
-            if (q <= 2 && nr > 2) sE[buf][2][t] = e2;
-            if (q <= 3 && nr > 3) sE[buf][3][t] = e3;
-            const unsigned key = __reduce_max_sync(0xffffffffu,
-                                                   argmax_key(eq.x * eq.x + eq.y * eq.y, t, !colused));
-            if (lane == 0) sKey[buf][warp] = key;
-            __syncthreads();
-            const unsigned w = max8(sKey[buf]);
-            if (!(key_value(w) > 1e-30f)) continue;  // the row vanished: no rank from it
-            const int c = (int)(255u - (w & 0xFFu));
-            const float2 pv = sE[buf][q][c];
-            const float inv = __frcp_rn(pv.x * pv.x + pv.y * pv.y);
-            const float2 v = coli ? make_float2((eq.x * pv.x + eq.y * pv.y) * inv, (eq.y * pv.x - eq.x * pv.y) * inv)
-                                  : z2;
-            // eliminate this rank from the panel's later rows
-            if (q < 1 && nr > 1) e1 = csub_mul(e1, sE[buf][1][c], v);
-            if (q < 2 && nr > 2) e2 = csub_mul(e2, sE[buf][2][c], v);
-            if (q < 3 && nr > 3) e3 = csub_mul(e3, sE[buf][3][c], v);
-            if (t == c) colused = true;
-            const int m = k + np;
-            Vb[m * kTile + t] = v;
-            if (m < RS) sV[m * kTile + t] = v;
-            cols |= (unsigned)c << (8 * np);
-            v0 = np == 0 ? v : v0;
-            v1 = np == 1 ? v : v1;
-            v2 = np == 2 ? v : v2;
-            v3 = np == 3 ? v : v3;
-            ++np;
-        }
-        if (np == 0) {
-            // every row of the panel vanished: continue with the lowest unused row
-            zero_rows += nr;
-            if (zero_rows > kAcaMaxZeroRows) break;
-            float f = 1.0f, d0 = 0.0f, d1 = 0.0f;
-            int nrw = t;
-            cta_reduce<true, false>(f, nrw, !rowused, d0, d1, sKey[0], nullptr);
-            if (f < 0.0f) break;
-            rows = (unsigned)nrw;
-            nr = 1;
-            __syncthreads();  // sKey[0] is rewritten by the next panel's first step
-            continue;
-        }
-        // ---- C. residual columns at the chosen columns, row t
-        float2 u0 = z2, u1 = z2, u2 = z2, u3 = z2;
-        const int c0 = unpack8(cols, 0), c1 = unpack8(cols, 1), c2 = unpack8(cols, 2), c3 = unpack8(cols, 3);
-        if (rowj) {
-#pragma unroll 1
-            for (int q = 0; q < np; ++q) {
-                const int c = unpack8(cols, q);
-                const bool bit = bc == kFlagBits ? block_bit(bw, pitch, t, c) : true;
-                const float2 x = lr_entry<ATT>(a, bc, bit, __ldg(PI + c), __ldg(NI + c), pj, qj);
-                u0 = q == 0 ? x : u0;
-                u1 = q == 1 ? x : u1;
-                u2 = q == 2 ? x : u2;
-                u3 = q == 3 ? x : u3;
-            }
-            for (int m = 0; m < ks; ++m) {
-                const float2 uu = sU[m * kTile + t];
-                const float2 *Vm = sV + m * kTile;
-                u0 = csub_mul(u0, uu, Vm[c0]);
-                u1 = csub_mul(u1, uu, Vm[c1]);
-                u2 = csub_mul(u2, uu, Vm[c2]);
-                u3 = csub_mul(u3, uu, Vm[c3]);
-            }
-            for (int m = RS; m < k; ++m) {
-                const float2 uu = Ub[m * kTile + t];
-                const float2 *Vm = Vb + m * kTile;
-                u0 = csub_mul(u0, uu, Vm[c0]);
-                u1 = csub_mul(u1, uu, Vm[c1]);
-                u2 = csub_mul(u2, uu, Vm[c2]);
-                u3 = csub_mul(u3, uu, Vm[c3]);
-            }
-            // the panel's earlier ranks: u_q -= u_q2 v_q2(c_q)
-            auto vpan = [&](int q2, int c) {
-                const int m2 = k + q2;
-                return m2 < RS ? sV[m2 * kTile + c] : Vb[m2 * kTile + c];
-            };
-            if (np > 1) u1 = csub_mul(u1, u0, vpan(0, c1));
-            if (np > 2) {
-                u2 = csub_mul(u2, u0, vpan(0, c2));
-                u2 = csub_mul(u2, u1, vpan(1, c2));
-            }
-            if (np > 3) {
-                u3 = csub_mul(u3, u0, vpan(0, c3));
-                u3 = csub_mul(u3, u1, vpan(1, c3));
-                u3 = csub_mul(u3, u2, vpan(2, c3));
-            }
-        }
-        {
-            float2 *Ut = Ub + k * kTile + t;
-            Ut[0] = u0;
-            if (np > 1) Ut[kTile] = u1;
-            if (np > 2) Ut[2 * kTile] = u2;
-            if (np > 3) Ut[3 * kTile] = u3;
-            if (k < RS) sU[k * kTile + t] = u0;
-            if (np > 1 && k + 1 < RS) sU[(k + 1) * kTile + t] = u1;
-            if (np > 2 && k + 2 < RS) sU[(k + 2) * kTile + t] = u2;
-            if (np > 3 && k + 3 < RS) sU[(k + 3) * kTile + t] = u3;
-        }
-        // ---- norms of the new ranks and the next panel's rows
-        {
-            float x[8];
-            x[0] = u0.x * u0.x + u0.y * u0.y;
-            x[1] = v0.x * v0.x + v0.y * v0.y;
-            x[2] = u1.x * u1.x + u1.y * u1.y;
-            x[3] = v1.x * v1.x + v1.y * v1.y;
-            x[4] = u2.x * u2.x + u2.y * u2.y;
-            x[5] = v2.x * v2.x + v2.y * v2.y;
-            x[6] = u3.x * u3.x + u3.y * u3.y;
-            x[7] = v3.x * v3.x + v3.y * v3.y;
-            const float ws = warp_sum8(x, lane);
-            if ((lane & 3) == 0) sSum[warp][lane >> 2] = ws;
-            const unsigned k0 = __reduce_max_sync(0xffffffffu, argmax_key(x[0], t, !rowused));
-            const unsigned k1 = __reduce_max_sync(0xffffffffu, argmax_key(x[2], t, !rowused && np > 1));
-            const unsigned k2 = __reduce_max_sync(0xffffffffu, argmax_key(x[4], t, !rowused && np > 2));
-            const unsigned k3 = __reduce_max_sync(0xffffffffu, argmax_key(x[6], t, !rowused && np > 3));
-            if (lane == 0) {
-                sRowKey[0][warp] = k0;
-                sRowKey[1][warp] = k1;
-                sRowKey[2][warp] = k2;
-                sRowKey[3][warp] = k3;
-            }
-        }
-        __syncthreads();
-        float S[8];
-#pragma unroll
-        for (int v = 0; v < 8; ++v) S[v] = 0.0f;
-#pragma unroll
-        for (int w = 0; w < kAcaWarps; ++w) {
-            const float4 lo = reinterpret_cast<const float4 *>(sSum[w])[0];
-            const float4 hi = reinterpret_cast<const float4 *>(sSum[w])[1];
-            S[0] += lo.x; S[1] += lo.y; S[2] += lo.z; S[3] += lo.w;
-            S[4] += hi.x; S[5] += hi.y; S[6] += hi.z; S[7] += hi.w;
-        }
-        int kept = np;
-#pragma unroll
-        for (int q = 0; q < kPanel; ++q)
-            if (q < kept) {
-                const float nn = S[2 * q] * S[2 * q + 1];
-                norm2 += nn;
-                if (nn <= tol * tol * norm2) {
-                    kept = q + 1;
-                    done = true;
-                }
-            }
-        k += kept;
-        if (done) break;
-        // next rows: the argmax of |u_q| over unused rows, per new rank, duplicates dropped
-        rows = 0u;
-        nr = 0;
-#pragma unroll
-        for (int q = 0; q < kPanel; ++q)
-            if (q < np) {
-                const unsigned w = max8(sRowKey[q]);
-                if (w) {
-                    const unsigned r = 255u - (w & 0xFFu);
-                    bool dup = false;
-#pragma unroll
-                    for (int q2 = 0; q2 < kPanel; ++q2)
-                        if (q2 < nr && unpack8(rows, q2) == (int)r) dup = true;
-                    if (!dup) {
-                        rows |= r << (8 * nr);
-                        ++nr;
-                    }
-                }
-            }
-        if (nr == 0) break;  // every row taken
-    }
-    // ---- the exact entries judge the approximation (as k_aca)
-    float e2 = 0.0f, x2 = 0.0f;
-    const bool converged = k > 0 && k < K;
-    __syncthreads();
-    if (converged) {
-        const int ks = min(k, RS);
-#pragma unroll 1
-        for (int h2 = 0; h2 < 2; ++h2) {
-            const int s = t + kTile * h2;
-            unsigned h = (unsigned)b * 2654435761u + (unsigned)s * 40503u + 12345u;
-            h ^= h >> 13;
-            h *= 0x5bd1e995u;
-            h ^= h >> 15;
-            const int jj = h2 == 0 ? t : (int)(h & 255u), ii = h2 == 0 ? (int)(h & 255u) : t;
-            if (ii < ni && jj < nj) {
-                const bool bit = bc == kFlagBits ? block_bit(bw, pitch, jj, ii) : true;
-                const float2 ex = lr_entry<ATT>(a, bc, bit, __ldg(PI + ii), __ldg(NI + ii), __ldg(PJ + jj),
-                                                __ldg(NJ + jj));
-                float2 ap = z2;
-                for (int m = 0; m < ks; ++m) ap = csub_mul(ap, sU[m * kTile + jj], sV[m * kTile + ii]);
-                for (int m = RS; m < k; ++m) ap = csub_mul(ap, Ub[m * kTile + jj], Vb[m * kTile + ii]);
-                e2 += (ex.x + ap.x) * (ex.x + ap.x) + (ex.y + ap.y) * (ex.y + ap.y);
-                x2 += ex.x * ex.x + ex.y * ex.y;
-            }
-        }
-    }
-    {
-        float f = 0.0f;
-        int fi = 0;
-        cta_reduce<false, true>(f, fi, false, e2, x2, nullptr, sumB);
-    }
-    const float rel = x2 > 0.0f ? sqrtf(e2 / x2) : (e2 > 0.0f ? 1.0f : 0.0f);  // the same in every thread
-    const bool accepted = converged && rel <= limit;
-    if (t == 0) {
-        rank[b] = accepted ? k : -1;
-        fro[b] = sqrtf(norm2);
-        err[b] = converged ? rel : -1.0f;
-    }
-    if (brow && accepted) {
-        // the panel buffer is free now: weights and projections of the apply
-        float4 *sW = reinterpret_cast<float4 *>(&sE[0][0][0]);
-        float2 *sTv = reinterpret_cast<float2 *>(sW + kTile), *sSu = sTv + kLrMaxRank;
-        lr_block_apply(a, I, J, Ub, Vb, k, brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv, sSu);
-    }
 }
 
 // ---------------------------------------------------------------- two entries per thread
@@ -3473,21 +3124,6 @@ void launch_aca_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, cons
 }
 
 template <bool ATT, int RS, int MINB>
-void launch_aca_panel_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
-                        int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
-                        cudaStream_t s, float2 *brow, float2 *bcol)
-{
-    const size_t smem = (size_t)2 * RS * kTile * sizeof(float2);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_aca_panel<ATT, RS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr = true;
-    }
-    k_aca_panel<ATT, RS, MINB><<<(unsigned)nblocks, kTile, smem, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit,
-                                                                       U, V, rank, fro, err, brow, bcol);
-}
-
-template <bool ATT, int RS, int MINB>
 void launch_aca2_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                    int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
                    cudaStream_t s, float2 *brow, float2 *bcol)
@@ -3508,15 +3144,11 @@ bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8
                   float limit, float *err, cudaStream_t s, float2 *brow, float2 *bcol)
 {
     switch (variant) {
-    case 3: launch_aca_panel_t<ATT, 8, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 4: launch_aca_panel_t<ATT, 8, 2>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 5: launch_aca_panel_t<ATT, 4, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 6: launch_aca_panel_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 7: launch_aca2_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 8: launch_aca2_t<ATT, 6, 5>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 9: launch_aca2_t<ATT, 4, 6>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 10: launch_aca2_t<ATT, 2, 8>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 11: launch_aca2_t<ATT, 3, 7>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 3: launch_aca2_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 4: launch_aca2_t<ATT, 6, 5>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 5: launch_aca2_t<ATT, 4, 6>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 6: launch_aca2_t<ATT, 2, 8>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 7: launch_aca2_t<ATT, 3, 7>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 1: launch_aca_t<ATT, 12, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     case 2: launch_aca_t<ATT, 16, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     default: launch_aca_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
@@ -3525,11 +3157,12 @@ bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8
 }
 }  // namespace
 
-// variant: factor ranks kept in shared memory and CTAs per SM -- 0: 8 ranks,
-// 4 CTAs (the fastest on the 60 kHz trihedral: 5.95 ms against 6.07 and
-// 6.69 ms); 1: 12 ranks, 4 CTAs; 2: 16 ranks, 3 CTAs; the panel form
-// (k_aca_panel): 3: 8 ranks, 3 CTAs; 4: 8 ranks, 2 CTAs; 5: 4 ranks, 4 CTAs;
-// 6: 8 ranks, 4 CTAs
+// variant: factor ranks kept in shared memory and CTAs per SM -- k_aca (one
+// row and one column per thread): 0: 8 ranks, 4 CTAs; 1: 12 ranks, 4 CTAs;
+// 2: 16 ranks, 3 CTAs; k_aca2 (two rows and two columns per thread, the first
+// bounce's apply fused): 3: 8 ranks, 4 CTAs; 4: 6 ranks, 5 CTAs; 5: 4 ranks,
+// 6 CTAs (the fastest on the 60 kHz trihedral); 6: 2 ranks, 8 CTAs; 7: 3
+// ranks, 7 CTAs
 bool launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                 int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
                 cudaStream_t s, int variant, float2 *brow, float2 *bcol)

@@ -277,8 +277,8 @@ struct Model {
     int opt_cmp_rmax = 32;
     int opt_cmp_select = 0;     // 0 rule (class ALL, eta-separated), 1 every interacting block, 2 the network
     float opt_cmp_rcut = 24.0f; // network: propose blocks whose predicted rank is below this
-    int opt_aca_variant = 0;    // cross-approximation kernel shape (factor ranks in shared memory, CTAs per SM)
-    int opt_fused_apply = 1;    // panel cross approximation: apply the accepted blocks to the building bounce's inputs
+    int opt_aca_variant = 5;    // cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
+    int opt_fused_apply = 1;    // k_aca2: apply the accepted blocks to the building bounce's inputs in the same kernel
     int opt_mask_classify = 1;  // bounce masks: warp-per-block classification, pair kernel on the listed blocks
     int opt_gate_proj = 1;      // bounce masks: gates decided from per-point projections where certain
     int opt_cross_objects = 0;  // bounces also between different targets (FACET_RESP); 0: the reference's behaviour
@@ -1676,7 +1676,7 @@ int sonar_set_option(const char *key, double value)
     }
     if (!strcmp(key, "aca_fused_apply")) { g.opt_fused_apply = value != 0.0; g.cmp.release(); return 0; }
     if (!strcmp(key, "aca_variant")) {
-        if (value < 0 || value > 11) return -1;
+        if (value < 0 || value > 7) return -1;
         g.opt_aca_variant = (int)value;
         return 0;
     }
