@@ -192,6 +192,15 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
 long long sonar_get_mask_rows(int hop, int srcIdx, int dstIdx, const int *rows, int nrows, unsigned char *out,
                               long long cap);
 
+/* Audit of the last compressed bounce's accepted blocks (no counterpart in
+ * the reference): for up to nsample of them, chosen by seed, the relative RMS
+ * error of the low-rank factors over every entry of the 256 x 256 block
+ * (full_err) beside the error the judge measured on its 512 sampled entries
+ * (judged_err).  Needs a compressed bounce of a target without attenuation
+ * and a build with FP32 factors.  Returns the number of blocks audited, or
+ * < 0 (sonar_last_error). */
+int sonar_audit_compression(int nsample, unsigned seed, float *full_err, float *judged_err, int cap);
+
 /* Host only (no GPU needed): frame and clipped area grid of one triangle
  * (src/Facet.cpp:6-339).  nx_ny_neg gets numXpnts, numYpnts,
  * numXpntsNegative; frame17 gets normal(3) base point(3) xAxis(3) yAxis(3)

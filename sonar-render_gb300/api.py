@@ -84,6 +84,8 @@ def load_library(path: str | None = None, build: bool = False):
     L.sonar_get_mask_rows.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_ubyte),
                                       C.c_longlong]
     L.sonar_get_mask_rows.restype = C.c_longlong
+    L.sonar_audit_compression.argtypes = [C.c_int, C.c_uint, _f, _f, C.c_int]
+    L.sonar_audit_compression.restype = C.c_int
     L.sonar_get_stream.restype = C.c_void_p
     L.sonar_get_surface_colours.argtypes = [C.c_int, C.c_int, _f, C.c_longlong]
     L.sonar_measure_peak.argtypes = [C.c_int]
@@ -258,6 +260,20 @@ def get_mask(hop, src_idx, dst_idx):
     if r < 0:
         raise SonarError("sonar_get_mask failed (%d)" % r)
     return out[:n]
+
+
+def audit_compression(nsample=256, seed=0):
+    """Full-tile errors of sampled accepted blocks of the last compressed
+    bounce and the judge's sampled errors of the same blocks (see
+    sonar_audit_compression): two float32 arrays."""
+    full = np.zeros(max(nsample, 1), np.float32)
+    judged = np.zeros(max(nsample, 1), np.float32)
+    n = lib().sonar_audit_compression(int(nsample), int(seed), full.ctypes.data_as(_f), judged.ctypes.data_as(_f),
+                                      int(nsample))
+    _check()
+    if n < 0:
+        raise SonarError("sonar_audit_compression failed (%d)" % n)
+    return full[:n], judged[:n]
 
 
 def get_mask_rows(hop, src_idx, dst_idx, rows):

@@ -2662,6 +2662,47 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
     }
 }
 
+// ---------------------------------------------------------------- judge audit
+// Full-tile check of accepted blocks: the relative RMS error of the factors
+// over every one of the block's 256 x 256 entries (exact entries as the
+// cross approximation evaluates them), one CTA per sampled block, thread t
+// the column t.  It tells whether the judge's 512 sampled entries catch the
+// blocks whose error concentrates in a few rows.
+__global__ void __launch_bounds__(kTile) k_lr_audit(SumArgs a, const int2 *blocks, const uint8_t *cls,
+                                                    const long long *off, const int *rank, const int *sample, int ns,
+                                                    const float2 *U, const float2 *V, float *out_err)
+{
+    __shared__ float4 sP[kTile], sN[kTile];
+    __shared__ float2 sums[kAcaWarps];
+    const int t = threadIdx.x;
+    if (blockIdx.x >= ns) return;
+    const int b = sample[blockIdx.x], k = rank[b];
+    const int I = blocks[b].x, J = blocks[b].y, bc = cls[b];
+    const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    sP[t] = t < nj ? a.srcA[J * kTile + t] : z4;
+    sN[t] = t < nj ? a.srcB[J * kTile + t] : z4;
+    __syncthreads();
+    const uint32_t *bw = a.mask.bits + (long long)I * kWordsPerTile * a.mask.pitch + (long long)J * kTile;
+    const float2 *U0 = U + off[b] * kTile, *V0 = V + off[b] * kTile;
+    float e2 = 0.0f, x2 = 0.0f;
+    if (t < ni && k > 0) {
+        const float4 pi = a.srcA[I * kTile + t], qi = a.srcB[I * kTile + t];
+        for (int j = 0; j < nj; ++j) {
+            const bool bit = bc == kFlagBits ? block_bit(bw, a.mask.pitch, j, t) : true;
+            const float2 ex = lr_entry<false>(a, bc, bit, pi, qi, sP[j], sN[j]);
+            float2 ap = ex;
+            for (int m = 0; m < k; ++m) ap = csub_mul(ap, U0[m * kTile + j], V0[m * kTile + t]);
+            e2 += ap.x * ap.x + ap.y * ap.y;
+            x2 += ex.x * ex.x + ex.y * ex.y;
+        }
+    }
+    float f = 0.0f;
+    int fi = 0;
+    cta_reduce<false, true>(f, fi, false, e2, x2, nullptr, sums);
+    if (t == 0) out_err[blockIdx.x] = x2 > 0.0f ? sqrtf(e2 / x2) : 0.0f;
+}
+
 // Block descriptors of the admissibility network, one warp per block:
 // log2(1 + separation / lambda), log2(1 + radius / lambda) of both tiles, the
 // cosines of both mean normals with the separation direction and with each
@@ -3173,6 +3214,13 @@ bool launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const 
                                   bcol);
     return launch_aca_v<false>(variant, a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow,
                                bcol);
+}
+
+void launch_lr_audit(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const long long *off, const int *rank,
+                     const int *sample, int ns, const float2 *U, const float2 *V, float *out_err, cudaStream_t s)
+{
+    if (a.ka != 0.0f) return;  // the audit evaluates entries without attenuation only
+    if (ns > 0) k_lr_audit<<<ns, kTile, 0, s>>>(a, blocks, cls, off, rank, sample, ns, U, V, out_err);
 }
 
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,

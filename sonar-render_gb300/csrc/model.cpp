@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <random>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -1769,6 +1770,67 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
         }
     });
     return st != 0 ? st : nbytes;
+}
+
+int sonar_audit_compression(int nsample, unsigned seed, float *full_err, float *judged_err, int cap)
+{
+    int nout = 0;
+    int st = guarded([&] {
+        need_render();
+        Compression &C = g.cmp;
+        if (!C.valid || !C.d_U || C.nblocks <= 0) fail(-6, "no compressed blocks to audit: run a compressed bounce first");
+        if (g.ki != 0.0) fail(-6, "the audit evaluates entries without attenuation");
+        if (nsample < 0 || cap < 0 || (cap > 0 && (!full_err || !judged_err))) fail(-6, "invalid audit arguments");
+        finish_compression();
+        MaskEntry &M = get_mask(HOP_F2F, C.obj, 0);
+        Object &A = get(OBJ_TARGET, C.obj);
+        const int n = C.nblocks;
+        std::vector<int> rk(n);
+        std::vector<float> er(n);
+        CK(cudaMemcpy(rk.data(), C.d_rank, n * sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(er.data(), C.d_err, n * sizeof(float), cudaMemcpyDeviceToHost));
+        std::vector<int> acc;
+        for (int b = 0; b < n; b++)
+            if (rk[b] > 0) acc.push_back(b);
+        std::mt19937 rng(seed);
+        std::shuffle(acc.begin(), acc.end(), rng);
+        const int ns = std::min({nsample, cap, (int)acc.size()});
+        acc.resize(ns);
+        std::sort(acc.begin(), acc.end());
+        if (ns == 0) return;
+        ensure_scratch(M.nsrc, M.ndst, 1);
+        launch_pack_frags(A.d_act_pos, A.d_act_facet, A.d_act_cell, A.d_facet_n, A.d_Pin, 0.9f, M.nsrc, g.d_packA,
+                          g.d_packB, g.stream);
+        SumArgs s{};
+        s.hop = HOP_F2F;
+        s.nsrc = s.ndst = M.nsrc;
+        s.srcA = g.d_packA;
+        s.srcB = g.d_packB;
+        s.mask = M.view;
+        s.kr = (float)g.kr;
+        s.ka = (float)g.ki;
+        const double k2 = g.kr / (2.0 * M_PI);
+        s.k2hi = (float)k2;
+        s.k2lo = (float)(k2 - (double)s.k2hi);
+        s.kr4pi = (float)(g.kr / (4.0 * M_PI));
+        s.rmin = A.delta;
+        int *d_sample = dalloc<int>(ns);
+        float *d_err = dalloc<float>(ns);
+        CK(cudaMemcpyAsync(d_sample, acc.data(), ns * sizeof(int), cudaMemcpyHostToDevice, g.stream));
+        launch_lr_audit(s, C.d_blocks, C.d_cls, C.d_off, C.d_rank, d_sample, ns, C.d_U, C.d_V, d_err, g.stream);
+        CK(cudaGetLastError());
+        std::vector<float> fe(ns);
+        CK(cudaMemcpyAsync(fe.data(), d_err, ns * sizeof(float), cudaMemcpyDeviceToHost, g.stream));
+        CK(cudaStreamSynchronize(g.stream));
+        dfree(d_sample);
+        dfree(d_err);
+        for (int q = 0; q < ns; q++) {
+            full_err[q] = fe[q];
+            judged_err[q] = er[acc[q]];
+        }
+        nout = ns;
+    });
+    return st != 0 ? st : nout;
 }
 
 long long sonar_get_mask_rows(int hop, int srcIdx, int dstIdx, const int *rows, int nrows, unsigned char *out,

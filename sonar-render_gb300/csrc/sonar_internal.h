@@ -155,6 +155,9 @@ constexpr int kLrRankLimit = 64;
 bool launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                 int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
                 cudaStream_t s, int variant = 0, float2 *brow = nullptr, float2 *bcol = nullptr);
+// Full-tile relative RMS error of the sampled accepted blocks (no attenuation)
+void launch_lr_audit(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const long long *off, const int *rank,
+                     const int *sample, int ns, const float2 *U, const float2 *V, float *out_err, cudaStream_t s);
 // ndev (optional): the block count in device memory; nblocks / nb bound the grid
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
                        const float4 *nm, float inv_lambda, float *X, cudaStream_t s, const int *ndev = nullptr);

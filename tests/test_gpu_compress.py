@@ -171,3 +171,31 @@ def test_every_interacting_block_compressed_matches_plain_and_oracle(api, oracle
     e1 = rel_l2((Q1 - Q0)[act[q]], v1)
     print("select %d one bounce vs FP64 oracle: rel L2 %.3e" % (select, e1))
     assert e1 < 1e-3
+
+
+def test_judge_audit_full_tiles(api, scenes):
+    """The judge accepts a block on 512 sampled exact entries; the audit
+    recomputes every entry of sampled accepted blocks.  At the default
+    tolerance no audited block may exceed the judge's limit by more than 3x,
+    and the full-tile errors follow the sampled ones."""
+    sc = _trihedral(scenes, 30e3)
+    tol = 1e-4
+    api.set_option("compress", 1)
+    api.set_option("compress_select", 1)
+    try:
+        load_scene(api, sc)
+        api.project_source_points_to_objects(False)
+        api.project_target_to_target_objects(1)
+        full, judged = api.audit_compression(256, seed=3)
+    finally:
+        api.set_option("compress", 0)
+        api.set_option("compress_select", 0)
+        api.TearDownCuda()
+    limit = 3.0 * tol
+    above = float(np.mean(full > limit))
+    ratio = np.median(full / np.maximum(judged, 1e-12))
+    print("audit: %d blocks, full-tile error median %.2e max %.2e, judged median %.2e, above the limit %.3f, "
+          "median full/judged %.2f" % (len(full), np.median(full), full.max(), np.median(judged), above, ratio))
+    assert len(full) == 256
+    assert np.all(np.isfinite(full)) and full.max() < 3 * limit
+    assert 0.3 < ratio < 3.0
