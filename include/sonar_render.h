@@ -264,6 +264,11 @@ long long sonar_batch_plan(const float *tris, const int *scene_tri_off, int nsce
                            float per_wavelength);
 int sonar_batch_run(long long plan, double *out);
 int sonar_batch_stats(long long plan, char *json, int cap);
+/* New source and receiver positions for the next sonar_batch_run of a plan
+ * (the same counts as planned), as a sequence of pings moves them: the
+ * geometry, its fragments and the tuning are kept; the run recomputes the
+ * visibility words.  Returns 0 or a negative code. */
+int sonar_batch_set_points(long long plan, const float *src_xyz, int nsrc, const float *rx_xyz, int nrx);
 int sonar_batch_stream(long long plan, void **stream);
 int sonar_batch_free(long long plan);
 int sonar_run_batch(const float *tris, const int *scene_tri_off, int nscenes, const float *src_xyz, int nsrc,

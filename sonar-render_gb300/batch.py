@@ -39,6 +39,7 @@ def _lib():
         L.sonar_batch_run.argtypes = [C.c_longlong, _d]
         L.sonar_batch_stats.argtypes = [C.c_longlong, C.c_char_p, C.c_int]
         L.sonar_batch_stream.argtypes = [C.c_longlong, C.POINTER(C.c_void_p)]
+        L.sonar_batch_set_points.argtypes = [C.c_longlong, _f, C.c_int, _f, C.c_int]
         L.sonar_batch_free.argtypes = [C.c_longlong]
         L.sonar_run_batch.argtypes = [_f, _i, C.c_int, _f, C.c_int, _f, C.c_int, _f, C.c_int, C.c_float,
                                       C.c_float, C.c_float, _d]
@@ -87,6 +88,14 @@ class Plan:
         if not copy:
             return None
         return self._out[..., 0] + 1j * self._out[..., 1]
+
+    def set_points(self, sources, receivers):
+        """New source and receiver positions (same counts) for the next run."""
+        S = np.ascontiguousarray(np.asarray(sources, np.float32).reshape(-1, 3))
+        R = np.ascontiguousarray(np.asarray(receivers, np.float32).reshape(-1, 3))
+        r = _lib().sonar_batch_set_points(self.id, S.ctypes.data_as(_f), S.shape[0], R.ctypes.data_as(_f), R.shape[0])
+        if r != 0:
+            raise _err("sonar_batch_set_points", r)
 
     def stats(self):
         L = _lib()

@@ -471,7 +471,8 @@ __global__ void __launch_bounds__(256) k_batch_reduce(const float *partial, cons
 
 size_t batch_smem_bytes(int kc)
 {
-    return kc == 64 ? (size_t)2 * Stage<64>::kBytes : (size_t)2 * Stage<32>::kBytes;
+    return kc == 64 ? (size_t)2 * Stage<64>::kBytes
+                    : kc == 32 ? (size_t)2 * Stage<32>::kBytes : (size_t)2 * Stage<16>::kBytes;
 }
 
 cudaError_t batch_prepare()
@@ -487,6 +488,12 @@ cudaError_t batch_prepare()
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_batch<64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)batch_smem_bytes(64));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)batch_smem_bytes(16));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)batch_smem_bytes(16));
     return e;
 }
 
@@ -497,6 +504,9 @@ void launch_batch(const BatchArgs &a, int kc, int grid, bool att, cudaStream_t s
     if (kc == 64) {
         if (att) k_batch<64, true><<<grid, kBatchThreads, sm, s>>>(a);
         else k_batch<64, false><<<grid, kBatchThreads, sm, s>>>(a);
+    } else if (kc == 16) {
+        if (att) k_batch<16, true><<<grid, kBatchThreads, sm, s>>>(a);
+        else k_batch<16, false><<<grid, kBatchThreads, sm, s>>>(a);
     } else {
         if (att) k_batch<32, true><<<grid, kBatchThreads, sm, s>>>(a);
         else k_batch<32, false><<<grid, kBatchThreads, sm, s>>>(a);

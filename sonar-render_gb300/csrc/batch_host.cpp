@@ -341,9 +341,11 @@ void autotune(Plan &p)
     int smem_optin = 0;
     BCK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
     std::vector<Tuning> cand;
-    for (int kc : {32, 64}) {
+    // fragments per operand stage x persistent CTAs per SM (as many as shared
+    // memory holds, up to four; each CTA takes 64 of the SM's 512 tensor-memory columns)
+    for (int kc : {16, 32, 64}) {
         const size_t sm = batch_smem_bytes(kc) + 10240;  // + static shared memory and the per-CTA reserve
-        const int per_sm = std::max(1, std::min(2, (int)((size_t)smem_optin / sm)));
+        const int per_sm = std::max(1, std::min(4, (int)((size_t)smem_optin / sm)));
         for (int c = 1; c <= per_sm; c++) {
             Tuning t;
             t.kc = kc;
@@ -666,6 +668,24 @@ int sonar_batch_run(long long plan, double *out)
     std::lock_guard<std::mutex> lk(g_lock);
     return (int)bguard([&]() -> long long {
         run_plan(find(plan), out);
+        return 0;
+    });
+}
+
+int sonar_batch_set_points(long long plan, const float *src_xyz, int nsrc, const float *rx_xyz, int nrx)
+{
+    std::lock_guard<std::mutex> lk(g_lock);
+    return (int)bguard([&]() -> long long {
+        Plan &p = find(plan);
+        if (!src_xyz || !rx_xyz) bfail(-6, "sonar_batch_set_points: null argument");
+        if (nsrc != p.nsrc || nrx != p.nrx)
+            bfail(-6, "sonar_batch_set_points: the plan has %d sources and %d receivers (got %d, %d)", p.nsrc, p.nrx,
+                  nsrc, nrx);
+        std::vector<float4> s4(nsrc), r4(nrx);
+        for (int i = 0; i < nsrc; i++) s4[i] = make_float4(src_xyz[3 * i], src_xyz[3 * i + 1], src_xyz[3 * i + 2], 0.0f);
+        for (int i = 0; i < nrx; i++) r4[i] = make_float4(rx_xyz[3 * i], rx_xyz[3 * i + 1], rx_xyz[3 * i + 2], 0.0f);
+        BCK(stage_to_device(p.d_src, s4.data(), nsrc * sizeof(float4), p.stream));
+        BCK(stage_to_device(p.d_rx, r4.data(), nrx * sizeof(float4), p.stream));
         return 0;
     });
 }

@@ -131,3 +131,28 @@ def test_batch_rejects_bad_sizes(api, scenes):
     pos = scenes.arc_xz(5.0, np.linspace(-10.0, 10.0, 65))
     with pytest.raises(api.SonarError, match="65 sources"):
         batch.Plan(tris, pos, pos[:4], [10e3])
+
+
+def test_plan_reused_with_new_points(api, oracle_mod, scenes):
+    """A plan run again after sonar_batch_set_points gives what a new plan at
+    those points gives (up to the summation order of another tuning) and
+    what the FP64 oracle gives; a mismatched point count is refused."""
+    from sonar_render_gb300 import batch
+    tris, src, rx, freqs = small_batch(scenes)
+    src2 = scenes.arc_xz(7.0, np.linspace(-30.0, 60.0, len(src)))
+    rx2 = scenes.arc_xz(4.5, np.linspace(-60.0, 20.0, len(rx)))
+    plan = batch.Plan(tris, src, rx, freqs)
+    plan.run()
+    plan.set_points(src2, rx2)
+    moved = plan.run()
+    with pytest.raises(Exception):
+        plan.set_points(src2[:-1], rx2)
+    plan.close()
+    fresh = batch.Plan(tris, src2, rx2, freqs)
+    ref = fresh.run()
+    fresh.close()
+    e_fresh = rel_l2(moved, ref)
+    e_orc = rel_l2(moved[1, 0], oracle_columns(oracle_mod, tris[1], src2, rx2, freqs[0]))
+    print("moved points: vs a new plan %.3e, vs FP64 oracle (box, %.0f Hz) %.3e" % (e_fresh, freqs[0], e_orc))
+    assert e_fresh < 1e-6
+    assert e_orc < TOL
