@@ -81,6 +81,7 @@ def lib():
         L.orc_add_sources.argtypes = [_vp, _f, C.c_int]
         L.orc_add_field_points.argtypes = [_vp, _f, C.c_int]
         L.orc_set_conditions.argtypes = [_vp, C.c_float, C.c_float, C.c_float, C.c_float]
+        L.orc_set_exact_geometry.argtypes = [_vp, C.c_int]
         L.orc_get_k.argtypes = [_vp, C.c_int]
         L.orc_get_k.restype = C.c_double
         for n in ("orc_render", "orc_project_field_objects", "orc_project_field_points"):
@@ -200,6 +201,11 @@ class Oracle:
 
     def set_initial_conditions(self, cp, f, att, density=1000.0):
         self.L.orc_set_conditions(self.h, C.c_float(cp), C.c_float(f), C.c_float(att), C.c_float(density))
+
+    def set_exact_geometry(self, on=True):
+        """Source hop and field-point readout with FP64 distances and cosines
+        from the FP32 positions (the reference rounds them in FP32)."""
+        self.L.orc_set_exact_geometry(self.h, int(bool(on)))
 
     def k(self):
         return complex(self.L.orc_get_k(self.h, 0), self.L.orc_get_k(self.h, 1))

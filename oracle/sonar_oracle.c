@@ -312,6 +312,11 @@ typedef struct {
     float cp, freq, att, density;
     double kr, ki;
     int rendered;
+    /* 0: the reference's FP32 geometry (r = sqrtf of an FP32 dot); 1: the
+     * source hop and the field-point readout take the distance and cosines
+     * in FP64 from the same FP32 positions (the accuracy yardstick of the
+     * library's centroid-relative geometry; the gates stay FP32) */
+    int exact_geom;
     /* occluders */
     otri_t *tri; int ntri;
     bnode_t *node; int nnode;
@@ -392,6 +397,11 @@ int orc_add_field_points(void *h, const float *xyz, int n)
 }
 
 /* src/Model.cpp:44-54: omega and k are FP32 members; k_wave = ((double)k, att). */
+void orc_set_exact_geometry(void *h, int on)
+{
+    ((scene_t *)h)->exact_geom = on != 0;
+}
+
 void orc_set_conditions(void *h, float cp, float f, float att, float density)
 {
     scene_t *s = (scene_t *)h;
@@ -694,6 +704,26 @@ static void green(const scene_t *s, float r, double *gr, double *gi)
     *gi = a_r * b_i + a_i * b_r;
 }
 
+/* G at an FP64 distance (exact-geometry mode) */
+static void green_d(const scene_t *s, double rd, double *gr, double *gi)
+{
+    const double ea = exp(-s->ki * rd);
+    const double er = ea * cos(s->kr * rd), ei = ea * sin(s->kr * rd);
+    const double a_r = -er / (4 * M_PI), a_i = -ei / (4 * M_PI);
+    const double b_r = (-s->ki) / rd, b_i = s->kr / rd;
+    *gr = a_r * b_r - a_i * b_i + 1.0 / (rd * rd);
+    *gi = a_r * b_i + a_i * b_r;
+}
+
+/* FP64 distance and unit vector of b - a from FP32 points */
+static double dist_d(f3 a, f3 b, double *u)
+{
+    const double vx = (double)b.x - (double)a.x, vy = (double)b.y - (double)a.y, vz = (double)b.z - (double)a.z;
+    const double r = sqrt(vx * vx + vy * vy + vz * vz);
+    u[0] = vx / r; u[1] = vy / r; u[2] = vz / r;
+    return r;
+}
+
 /* ---- hop a4: src/OptiX.cu:35-110 ---------------------------------------- */
 static void hop_source_cell(scene_t *s, const object_t *B, long cell, double *acc, uint8_t *mask_row,
                             long long *cnt)
@@ -722,13 +752,19 @@ static void hop_source_cell(scene_t *s, const object_t *B, long cell, double *ac
             if (spf) cnt[2]++;
             if (!hit) {
                 m |= 1;
-                const double rd = (double)r;
+                double rd = (double)r, cid = (double)ci;
+                if (s->exact_geom) {
+                    double u[3];
+                    rd = dist_d(pi, pj, u);
+                    if (B->type != OBJ_FIELD)
+                        cid = -(u[0] * F->normal.x + u[1] * F->normal.y + u[2] * F->normal.z);
+                }
                 const double ea = exp(-s->ki * rd);
                 const double er = ea * cos(s->kr * rd), ei = ea * sin(s->kr * rd);
                 const double Pr = s->srcP[2 * i], Pi = s->srcP[2 * i + 1];
                 const double tr = Pr * er - Pi * ei, ti = Pr * ei + Pi * er;
-                ar += ((double)ci * tr) / rd;
-                ai += ((double)ci * ti) / rd;
+                ar += (cid * tr) / rd;
+                ai += (cid * ti) / rd;
             }
         }
         cnt[0]++;
@@ -765,9 +801,16 @@ static void hop_fieldpoint(scene_t *s, const object_t *A, int j, double *acc, ui
             if (spf) cnt[2]++;
             if (!hit) {
                 m |= 1;
-                double gr, gi;
-                green(s, r, &gr, &gi);
-                const double w = (double)(Ai * cs);
+                double gr, gi, w;
+                if (s->exact_geom) {
+                    double u[3];
+                    const double rd = dist_d(pj, pi, u);  /* u: field point -> fragment */
+                    green_d(s, rd, &gr, &gi);
+                    w = (double)Ai * -(u[0] * F->normal.x + u[1] * F->normal.y + u[2] * F->normal.z);
+                } else {
+                    green(s, r, &gr, &gi);
+                    w = (double)(Ai * cs);
+                }
                 const double pr = w * A->P[2 * cell], pim = w * A->P[2 * cell + 1];
                 ar += pr * gr - pim * gi;
                 ai += pr * gi + pim * gr;

@@ -1535,11 +1535,103 @@ __device__ __forceinline__ void pair_term(const SumArgs &a, const float4 A, cons
     }
 }
 
+// pair_term of the source hop and the readout with the phase distance taken
+// relative to an FP64 reference (o: the fragment's offset from its tile
+// centroid for the readout).  The source hop evaluates its distance in FP64
+// outright: it has S x N_cells pairs, a few per fragment.
+struct RelRef;
 template <int HOP, bool ATT>
+__device__ __forceinline__ void pair_term_rel(const SumArgs &a, const float4 A, const float4 B, const Dst &d,
+                                              const RelRef &ref, float4 o, bool gate, float &tr, float &ti, bool &ok);
+
+// Phase of a pair in turns from a distance known in FP64 to within FP32
+// round-off of a small correction: r = R + dr, R (FP64) the distance to a
+// reference point, phase0 = frac(R k / 2 pi) reduced in FP64 once, dr in FP32.
+__device__ __forceinline__ float rel_turns(float phase0, float dr, const SumArgs &a)
+{
+    const float th = __fmul_rn(dr, a.k2hi);
+    const float tl = fmaf(dr, a.k2lo, fmaf(dr, a.k2hi, -th));
+    const float f = phase0 + ((th - rintf(th)) + tl);
+    return f - rintf(f);
+}
+
+// Relative geometry of the readout (HOP_FP): with o = p_i - c (fragment from
+// its tile's centroid, small) and D = p_j - c (field point from the centroid,
+// R = |D| in FP64), r^2 = R^2 - 2 o.D + |o|^2, so r - R = (|o|^2 - 2 o.D) /
+// (r + R): FP32 arithmetic on small numbers, no cancellation at large R.
+struct RelRef {
+    float dx, dy, dz, R, phase0;
+};
+
+__device__ __forceinline__ RelRef rel_ref(const SumArgs &a, double px, double py, double pz, float4 c)
+{
+    const double dx = px - (double)c.x, dy = py - (double)c.y, dz = pz - (double)c.z;
+    const double R = sqrt(dx * dx + dy * dy + dz * dz);
+    const double t = R * a.k2pi;
+    return RelRef{(float)dx, (float)dy, (float)dz, (float)R, (float)(t - floor(t))};
+}
+
+template <int HOP, bool ATT>
+__device__ __forceinline__ void pair_term_rel(const SumArgs &a, const float4 A, const float4 B, const Dst &d,
+                                              const RelRef &ref, float4 o, bool gate, float &tr, float &ti, bool &ok)
+{
+    // direction, cosines and amplitudes from the FP32 difference (relative
+    // accuracy ~1e-7 is enough for them); only the phase needs r to ~1e-9 m
+    const float vx = __fsub_rn(d.px, A.x), vy = __fsub_rn(d.py, A.y), vz = __fsub_rn(d.pz, A.z);
+    const float r2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+    const float rinv = rsqrtf(r2);
+    const float r = r2 * rinv;
+    float turns;
+    if (HOP == HOP_SRC) {
+        const double ex = (double)d.px - (double)A.x, ey = (double)d.py - (double)A.y, ez = (double)d.pz - (double)A.z;
+        const double t = sqrt(ex * ex + ey * ey + ez * ez) * a.k2pi;
+        turns = (float)(t - rint(t));
+    } else {
+        // r - R = (|o|^2 - 2 o.D) / (r + R)
+        const float num = fmaf(-2.0f, fmaf(o.x, ref.dx, fmaf(o.y, ref.dy, o.z * ref.dz)), o.w);
+        turns = rel_turns(ref.phase0, num / (r + ref.R), a);
+    }
+    float sn, cs;
+    __sincosf(turns * kTwoPi, &sn, &cs);
+    const float damp = ATT ? __expf(-a.ka * r) : 1.0f;
+    ok = true;
+    if (HOP == HOP_SRC) {
+        float ci = -(vx * d.nx + vy * d.ny + vz * d.nz) * rinv;
+        if (a.dst_is_field)
+            ci = 1.0f;
+        else if (gate)
+            ok = gate_from(ci, vx, vy, vz, -1.0f, d.nx, d.ny, d.nz);
+        const float amp = ATT ? ci * rinv * damp : ci * rinv;
+        const float er = amp * cs, ei = amp * sn;
+        tr = er * A.w - ei * B.w;
+        ti = er * B.w + ei * A.w;
+    } else {
+        const float rinv2 = rinv * rinv;
+        float gr, gi;
+        if (ATT) {
+            const float amp = rinv * kInv4Pi * damp;
+            gr = fmaf(amp, fmaf(a.ka, cs, a.kr * sn), rinv2);
+            gi = amp * fmaf(a.ka, sn, -a.kr * cs);
+        } else {
+            const float ampk = rinv * (kInv4Pi * a.kr);
+            gr = fmaf(ampk, sn, rinv2);
+            gi = -ampk * cs;
+        }
+        const float c1 = (vx * B.x + vy * B.y + vz * B.z) * rinv;  // cos_scat
+        if (gate) ok = gate_from(c1, vx, vy, vz, 1.0f, B.x, B.y, B.z);
+        gr *= c1;
+        gi *= c1;
+        tr = gr * A.w - gi * B.w;
+        ti = gr * B.w + gi * A.w;
+    }
+}
+
+template <int HOP, bool ATT, bool REL = false>
 __global__ void __launch_bounds__(kTile) k_sum(SumArgs a)
 {
     __shared__ float4 sA[kTile];
     __shared__ float4 sB[kTile];
+    __shared__ float4 sO[REL && HOP == HOP_FP ? kTile : 1];  // fragment offsets from the tile centroid
     const int tid = threadIdx.x;
     const int j = blockIdx.x * kTile + tid;
     const bool live = j < a.ndst;
@@ -1561,11 +1653,19 @@ __global__ void __launch_bounds__(kTile) k_sum(SumArgs a)
         const uint8_t fl = a.mask.flags[(long long)t * a.mask.ndstblocks + blockIdx.x];  // uniform per CTA
         if (fl == kFlagNone) continue;
         __syncthreads();
+        RelRef ref{};
         {
             const int i = t * kTile + tid;
             const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             sA[tid] = i < a.nsrc ? a.srcA[i] : z;
             sB[tid] = i < a.nsrc ? a.srcB[i] : z;
+            if (REL && HOP == HOP_FP) {
+                const float4 c = a.tile_cen[t];
+                const float4 p = sA[tid];
+                const float ox = p.x - c.x, oy = p.y - c.y, oz = p.z - c.z;
+                sO[tid] = make_float4(ox, oy, oz, fmaf(ox, ox, fmaf(oy, oy, oz * oz)));
+                ref = rel_ref(a, (double)d.px, (double)d.py, (double)d.pz, c);
+            }
         }
         __syncthreads();
         const int ntile = min(kTile, a.nsrc - t * kTile);
@@ -1586,7 +1686,21 @@ __global__ void __launch_bounds__(kTile) k_sum(SumArgs a)
                 m &= keep >= 32 ? 0xffffffffu : (keep <= 0 ? 0u : ((1u << keep) - 1u));
             }
             if (!__any_sync(0xffffffffu, m != 0u)) continue;
-            if (fl != kFlagClear) {
+            if (REL) {
+                // centroid-relative phase (the gates of CLEAR blocks inline as below)
+#pragma unroll 4
+                for (int b = 0; b < 32; ++b) {
+                    const float4 A = sA[w * 32 + b];
+                    const float4 B = sB[w * 32 + b];
+                    float tr, ti;
+                    bool ok;
+                    pair_term_rel<HOP, ATT>(a, A, B, d, ref, REL && HOP == HOP_FP ? sO[w * 32 + b] : A,
+                                            fl == kFlagClear, tr, ti, ok);
+                    const bool on = ((m >> b) & 1u) && ok;
+                    fr += on ? tr : 0.0f;
+                    fi += on ? ti : 0.0f;
+                }
+            } else if (fl != kFlagClear) {
 #pragma unroll 8
                 for (int b = 0; b < 32; ++b) {
                     const float4 A = sA[w * 32 + b];
@@ -3092,12 +3206,22 @@ void launch_sum(const SumArgs &a, cudaStream_t s)
     const bool att = a.ka != 0.0f;
     switch (a.hop) {
     case HOP_SRC:
-        if (att) k_sum<HOP_SRC, true><<<grid, kTile, 0, s>>>(a);
-        else k_sum<HOP_SRC, false><<<grid, kTile, 0, s>>>(a);
+        if (a.rel) {
+            if (att) k_sum<HOP_SRC, true, true><<<grid, kTile, 0, s>>>(a);
+            else k_sum<HOP_SRC, false, true><<<grid, kTile, 0, s>>>(a);
+        } else {
+            if (att) k_sum<HOP_SRC, true><<<grid, kTile, 0, s>>>(a);
+            else k_sum<HOP_SRC, false><<<grid, kTile, 0, s>>>(a);
+        }
         break;
     case HOP_FP:
-        if (att) k_sum<HOP_FP, true><<<grid, kTile, 0, s>>>(a);
-        else k_sum<HOP_FP, false><<<grid, kTile, 0, s>>>(a);
+        if (a.rel) {
+            if (att) k_sum<HOP_FP, true, true><<<grid, kTile, 0, s>>>(a);
+            else k_sum<HOP_FP, false, true><<<grid, kTile, 0, s>>>(a);
+        } else {
+            if (att) k_sum<HOP_FP, true><<<grid, kTile, 0, s>>>(a);
+            else k_sum<HOP_FP, false><<<grid, kTile, 0, s>>>(a);
+        }
         break;
     case HOP_F2F:
         if (att) k_sum<HOP_F2F, true><<<grid, kTile, 0, s>>>(a);

@@ -260,6 +260,8 @@ struct Model {
     int *d_limit = nullptr;
     size_t limit_cap = 0;
     double2 *d_colpart = nullptr;
+    float4 *d_tilecen = nullptr, *d_tilenm = nullptr;  // tile centroids of the relative geometry
+    size_t tilecen_cap = 0;
     size_t colpart_cap = 0;
     // work list of the symmetric bounce sum
     int *d_blist = nullptr, *d_rowcnt = nullptr, *d_chunk_off = nullptr, *d_nchunks = nullptr;
@@ -279,6 +281,7 @@ struct Model {
     int opt_cmp_select = 0;     // 0 rule (class ALL, eta-separated), 1 every interacting block, 2 the network
     float opt_cmp_rcut = 24.0f; // network: propose blocks whose predicted rank is below this
     int opt_aca_variant = 5;    // cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
+    int opt_rel_geom = 0;       // source hop and readout: phase distances relative to FP64 references
     int opt_fused_apply = 1;    // k_aca2: apply the accepted blocks to the building bounce's inputs in the same kernel
     int opt_mask_classify = 1;  // bounce masks: warp-per-block classification, pair kernel on the listed blocks
     int opt_gate_proj = 1;      // bounce masks: gates decided from per-point projections where certain
@@ -302,6 +305,8 @@ struct Model {
         masks.clear();
         cmp.free_all();
         dfree(d_packA); dfree(d_packB); dfree(d_partial); dfree(d_limit); dfree(d_colpart);
+        dfree(d_tilecen); dfree(d_tilenm);
+        tilecen_cap = 0;
         dfree(d_blist); dfree(d_rowcnt); dfree(d_chunk_off); dfree(d_nchunks); dfree(d_chunks); dfree(d_rowpart);
         pack_cap = partial_cap = limit_cap = colpart_cap = 0;
         sym_tiles = 0;
@@ -1034,6 +1039,8 @@ void run_hop(int hop, int a, int b)
     cudaStream_t st = g.stream;
 
     CK(cudaEventRecord(g.ev0, st));
+    s.rel = (g.opt_rel_geom && (hop == HOP_SRC || hop == HOP_FP)) ? 1 : 0;
+    s.k2pi = k2;
     if (hop == HOP_SRC) {
         launch_pack_points(g.d_src_pos, g.d_src_P, M.nsrc, g.d_packA, g.d_packB, st);
         timed_sum(s, st);
@@ -1042,6 +1049,19 @@ void run_hop(int hop, int a, int b)
         Object &A = get(OBJ_TARGET, a);
         launch_pack_frags(A.d_act_pos, A.d_act_facet, A.d_act_cell, A.d_facet_n, A.d_P, 1.0f, M.nsrc, g.d_packA,
                           g.d_packB, st);
+        if (s.rel) {
+            // reference points of the relative geometry: the centroid of every source tile
+            const size_t nt = (size_t)M.view.ntiles;
+            if (nt > g.tilecen_cap) {
+                dfree(g.d_tilecen);
+                dfree(g.d_tilenm);
+                g.d_tilecen = dalloc<float4>(nt);
+                g.d_tilenm = dalloc<float4>(nt);
+                g.tilecen_cap = nt;
+            }
+            launch_tile_stats(g.d_packA, g.d_packB, M.nsrc, g.d_tilecen, g.d_tilenm, st);
+            s.tile_cen = g.d_tilecen;
+        }
         timed_sum(s, st);
         launch_finalize_add(g.d_partial, s.nsplit, M.ndst, g.d_fp_order, g.d_fp_P, st);
     } else if (hop == HOP_F2F) {
@@ -1675,6 +1695,7 @@ int sonar_set_option(const char *key, double value)
         for (auto &m : g.masks) m.stale = true;
         return 0;
     }
+    if (!strcmp(key, "relative_geometry")) { g.opt_rel_geom = value != 0.0; return 0; }
     if (!strcmp(key, "aca_fused_apply")) { g.opt_fused_apply = value != 0.0; g.cmp.release(); return 0; }
     if (!strcmp(key, "aca_variant")) {
         if (value < 0 || value > 7) return -1;

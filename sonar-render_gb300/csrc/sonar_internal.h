@@ -99,6 +99,13 @@ struct SumArgs {
     double2 *partial;               // [nsplit][ndst]
     int nsplit;
     int tiles_per_split;
+    // centroid-relative geometry (source hop and field-point readout, option
+    // relative_geometry): the phase distance from FP64 references instead of
+    // the reference's FP32 r; tile_cen: per source tile the centroid of its
+    // fragments (readout), k2pi = Re k / (2 pi) in FP64
+    int rel = 0;
+    const float4 *tile_cen = nullptr;
+    double k2pi = 0.0;
 };
 
 // kernels.cu
