@@ -254,7 +254,8 @@ def kernel_times(stats, steps):
     """Per-step device time of each kernel group from the library's records."""
     k = {}
     for h in stats["hops"]:
-        name = {0: "source", 1: "field_points", 2: "bounce", 3: "field_object"}[h["hop"]]
+        name = {0: "source", 1: "field_points", 2: "bounce", 3: "field_object", 4: "cross_object",
+                5: "piston_target", 6: "piston_field_object"}.get(h["hop"], "hop%d" % h["hop"])
         k["mask_" + name] = k.get("mask_" + name, 0.0) + h["mask_ms"]
         k["sum_" + name] = k.get("sum_" + name, 0.0) + h["sum_ms"]
         if h.get("lr_ms"):

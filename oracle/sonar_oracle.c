@@ -674,6 +674,15 @@ int orc_render(void *h)
     if (s->rendered) return -1;
     for (int i = 0; i < s->nobj[OBJ_TARGET]; i++) obj_fragment(s->obj[OBJ_TARGET][i]);
     for (int i = 0; i < s->nobj[OBJ_FIELD]; i++) obj_fragment(s->obj[OBJ_FIELD][i]);
+    /* piston source objects: fragmented like the others, unit surface pressure */
+    for (int i = 0; i < s->nobj[OBJ_SOURCE]; i++) {
+        object_t *o = s->obj[OBJ_SOURCE][i];
+        obj_fragment(o);
+        for (long c = 0; c < o->ncells; c++) {
+            o->P[2 * c] = o->Pin[2 * c] = 1.0;
+            o->P[2 * c + 1] = o->Pin[2 * c + 1] = 0.0;
+        }
+    }
     build_occluders(s);
     s->rendered = 1;
     return 0;
@@ -1040,6 +1049,33 @@ static void project_sources_obj(scene_t *s, object_t *B)
     OMP_COUNTERS_ADD
 }
 
+/* Piston source objects (objectType 1; the reference stores them unused,
+ * src/Model.cpp:33-35): every fragment radiates its unit surface pressure
+ * through the facet -> facet projection of src/OptiX.cu:192-406 -- area,
+ * cos_scat at the piston, cos_inc at a target destination (1 at a field
+ * object), r < delta regularisation and 0.9 factor, shadow ray from the
+ * piston fragment, destinations gated by their area -- into the active cells
+ * of the target (field) object B: the FACET_RESP (FACET_NO_RESP) cell sums
+ * with the piston in the source object's place. */
+static void project_piston(scene_t *s, object_t *S, object_t *B, int field)
+{
+    OMP_COUNTERS
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : c0, c1, c2)
+    for (long q = 0; q < B->nact; q++) {
+        double acc[2];
+        long long cnt[3] = {0, 0, 0};
+        if (field)
+            hop_noresp_cell(s, S, B, q, acc, NULL, cnt);
+        else
+            hop_resp_cell(s, S, B, 1, q, acc, NULL, cnt);
+        const long c = B->act[q];
+        B->P[2 * c] += acc[0];
+        B->P[2 * c + 1] += acc[1];
+        c0 += cnt[0]; c1 += cnt[1]; c2 += cnt[2];
+    }
+    OMP_COUNTERS_ADD
+}
+
 int orc_project_sources(void *h, int field_objects)
 {
     scene_t *s = (scene_t *)h;
@@ -1048,6 +1084,12 @@ int orc_project_sources(void *h, int field_objects)
     for (int i = 0; i < s->nobj[OBJ_TARGET]; i++) project_sources_obj(s, s->obj[OBJ_TARGET][i]);
     if (field_objects)
         for (int i = 0; i < s->nobj[OBJ_FIELD]; i++) project_sources_obj(s, s->obj[OBJ_FIELD][i]);
+    for (int p = 0; p < s->nobj[OBJ_SOURCE]; p++) {
+        for (int i = 0; i < s->nobj[OBJ_TARGET]; i++) project_piston(s, s->obj[OBJ_SOURCE][p], s->obj[OBJ_TARGET][i], 0);
+        if (field_objects)
+            for (int i = 0; i < s->nobj[OBJ_FIELD]; i++)
+                project_piston(s, s->obj[OBJ_SOURCE][p], s->obj[OBJ_FIELD][i], 1);
+    }
     return 0;
 }
 
@@ -1247,6 +1289,16 @@ long orc_hop_subset(void *h, int hop, int a_idx, int b_idx, const long *dst, lon
         B = s->obj[OBJ_TARGET][a_idx < b_idx ? b_idx : a_idx];
         nsrc = s->obj[OBJ_TARGET][a_idx]->nact;
         break;
+    case 5:
+    case 6:
+        /* piston source object a_idx -> target (5) or field object (6) b_idx */
+        if (a_idx < 0 || a_idx >= s->nobj[OBJ_SOURCE] || b_idx < 0 ||
+            b_idx >= s->nobj[hop == 5 ? OBJ_TARGET : OBJ_FIELD])
+            return -2;
+        A = s->obj[OBJ_SOURCE][a_idx];
+        B = s->obj[hop == 5 ? OBJ_TARGET : OBJ_FIELD][b_idx];
+        nsrc = A->nact;
+        break;
     default:
         return -3;
     }
@@ -1262,6 +1314,8 @@ long orc_hop_subset(void *h, int hop, int a_idx, int b_idx, const long *dst, lon
         case 2: hop_f2f_cell(s, A, dst[k], pin, acc, row, cnt); break;
         case 3: hop_noresp_cell(s, A, B, dst[k], acc, row, cnt); break;
         case 4: hop_resp_cell(s, A, B, a_idx < b_idx, dst[k], acc, row, cnt); break;
+        case 5: hop_resp_cell(s, A, B, 1, dst[k], acc, row, cnt); break;
+        case 6: hop_noresp_cell(s, A, B, dst[k], acc, row, cnt); break;
         }
         out[2 * k] = acc[0];
         out[2 * k + 1] = acc[1];

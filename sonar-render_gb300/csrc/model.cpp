@@ -548,8 +548,16 @@ void render()
     CK(cudaEventCreateWithFlags(&g.ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&g.ev_join, cudaEventDisableTiming));
     g.render_ms[0] = host_ms() - t0;
-    for (int t : {OBJ_TARGET, OBJ_FIELD})
+    for (int t : {OBJ_TARGET, OBJ_SOURCE, OBJ_FIELD})
         for (auto &o : g.obj[t]) render_object(*o);
+    // piston source objects: unit surface pressure on every cell
+    for (auto &o : g.obj[OBJ_SOURCE]) {
+        const size_t nc = (size_t)o->ncells;
+        UploadArray<double2> P(nc);
+        for (size_t c = 0; c < nc; c++) P[c] = make_double2(1.0, 0.0);
+        if (nc) upload(o->d_P, P, nc, g.stream);
+        g.h2d_bytes += (long long)(nc * sizeof(double2));
+    }
     const double t2 = host_ms();
     // occluders: every triangle of every target object (OptiX.cpp:264-296)
     std::vector<std::array<float, 9>> tris;
@@ -656,6 +664,26 @@ HopSets hop_sets(int hop, int a, int b)
         m.dst_facet = B.d_act_facet;
         m.dst_facet_n = B.d_facet_n;
         m.resp_dst_origin = a > b ? 1 : 0;
+    } else if (hop == HOP_PISTON_T || hop == HOP_PISTON_F) {
+        // a piston source object's fragments -> the active cells of a target
+        // (both cosine gates, the FACET_RESP form) or of a field object
+        // (cos_inc = 1, the FACET_NO_RESP form); the ray starts at the
+        // piston fragment.  The convex-target shortcuts assume rays that
+        // leave or end on a target: off here.
+        Object &A = get(OBJ_SOURCE, a);
+        Object &B = get(hop == HOP_PISTON_T ? OBJ_TARGET : OBJ_FIELD, b);
+        m.hop = hop == HOP_PISTON_T ? HOP_RESP : HOP_NORESP;
+        m.convex = 0;
+        m.nsrc = A.nact();
+        m.src_pos = A.d_act_pos;
+        m.src_facet = A.d_act_facet;
+        m.src_facet_n = A.d_facet_n;
+        m.ndst = B.nact();
+        m.dst_pos = B.d_act_pos;
+        m.dst_facet = B.d_act_facet;
+        m.dst_facet_n = B.d_facet_n;
+        m.dst_is_field = hop == HOP_PISTON_F ? 1 : 0;
+        m.resp_dst_origin = 0;
     } else {
         Object &A = get(OBJ_TARGET, a);
         Object &B = get(OBJ_FIELD, b);
@@ -992,6 +1020,8 @@ long long pair_count(int hop, int a, int b)
         return tot * tot - sq;
     }
     if (hop == HOP_RESP) return (long long)get(OBJ_TARGET, a).nact() * get(OBJ_TARGET, b).nact();
+    if (hop == HOP_PISTON_T) return (long long)get(OBJ_SOURCE, a).nact() * get(OBJ_TARGET, b).nact();
+    if (hop == HOP_PISTON_F) return (long long)get(OBJ_SOURCE, a).nact() * get(OBJ_FIELD, b).nact();
     return (long long)get(OBJ_TARGET, a).nact() * get(OBJ_FIELD, b).nact();
 }
 
@@ -1014,7 +1044,7 @@ void run_hop(int hop, int a, int b)
     if (M.nsrc == 0 || M.ndst == 0) return;
     HopSets hs = hop_sets(hop, a, b);
     SumArgs s{};
-    s.hop = hop;
+    s.hop = hs.m.hop;  // the kernels' hop (the piston hops run as FACET_RESP / FACET_NO_RESP)
     s.nsrc = M.nsrc;
     s.ndst = M.ndst;
     s.dst_pos = hs.m.dst_pos;
@@ -1113,6 +1143,17 @@ void run_hop(int hop, int a, int b)
             timed_sum(s, st);
             launch_finalize_f2f(g.d_partial, s.nsplit, M.ndst, A.d_act_cell, A.d_Pout, A.d_P, st);
         }
+    } else if (hop == HOP_PISTON_T || hop == HOP_PISTON_F) {
+        // a piston source object (unit pressure, 0.9 A_i weights as every
+        // facet -> facet projection) into the active cells of a target or a
+        // field object; r_min is the piston's delta
+        Object &A = get(OBJ_SOURCE, a);
+        Object &B = get(hop == HOP_PISTON_T ? OBJ_TARGET : OBJ_FIELD, b);
+        s.rmin = A.delta;
+        launch_pack_frags(A.d_act_pos, A.d_act_facet, A.d_act_cell, A.d_facet_n, A.d_P, 0.9f, M.nsrc, g.d_packA,
+                          g.d_packB, st);
+        timed_sum(s, st);
+        launch_finalize_add(g.d_partial, s.nsplit, M.ndst, B.d_act_cell, B.d_P, st);
     } else if (hop == HOP_RESP) {
         // FACET_RESP, one direction: sources of target a (their P_in, 0.9 A_i),
         // destinations of target b; r_min is the delta of the lower-index
@@ -1415,6 +1456,13 @@ void ProjectSrcPointsToObjects(bool projectFieldObjects)
         for (int i = 0; i < (int)g.obj[OBJ_TARGET].size(); i++) run_hop(HOP_SRC, OBJ_TARGET, i);
         if (projectFieldObjects)
             for (int i = 0; i < (int)g.obj[OBJ_FIELD].size(); i++) run_hop(HOP_SRC, OBJ_FIELD, i);
+        // piston source objects (objectType 1) radiate their unit surface
+        // pressure into the targets and, with projectFieldObjects, the field objects
+        for (int p = 0; p < (int)g.obj[OBJ_SOURCE].size(); p++) {
+            for (int i = 0; i < (int)g.obj[OBJ_TARGET].size(); i++) run_hop(HOP_PISTON_T, p, i);
+            if (projectFieldObjects)
+                for (int i = 0; i < (int)g.obj[OBJ_FIELD].size(); i++) run_hop(HOP_PISTON_F, p, i);
+        }
     });
 }
 
@@ -1514,7 +1562,7 @@ void RenderOpenGL(int width, int height, char *filename, float viewSettings[9])
 void TearDownCuda(void)
 {
     // src/Model.cpp:115-129, src/ModelCuda.cpp:124-181: points, target and
-    // field objects are dropped; source objects are kept, as in the reference
+    // field objects are dropped
     try {
         // every stream, as the cudaFree of the buffers used to: a caller may
         // still read a result on a stream of its own
@@ -1522,7 +1570,10 @@ void TearDownCuda(void)
         g.free_device();
     } catch (...) {
     }
+    // piston source objects are dropped too: they radiate in this library
+    // (the reference stores them without using them, src/Model.cpp:33-35)
     g.obj[OBJ_TARGET].clear();
+    g.obj[OBJ_SOURCE].clear();
     g.obj[OBJ_FIELD].clear();
     g.src.clear();
     g.fp.clear();
@@ -1747,7 +1798,7 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
     long long nbytes = 0;
     int st = guarded([&] {
         need_render();
-        if (hop < HOP_SRC || hop > HOP_RESP) fail(-6, "invalid hop %d", hop);
+        if (hop < HOP_SRC || hop > HOP_PISTON_F) fail(-6, "invalid hop %d", hop);
         HopSets hs = hop_sets(hop, srcIdx, dstIdx);
         nbytes = (long long)hs.nsrc * hs.ndst;
         if (!out) return;
@@ -1780,6 +1831,10 @@ long long sonar_get_mask(int hop, int srcIdx, int dstIdx, unsigned char *out, lo
         if (hop == HOP_RESP) rd = canon(get(OBJ_TARGET, dstIdx));
         if (hop == HOP_FP) rd = g.fp_order;  // stored field point k is load index fp_order[k]
         if (hop == HOP_NORESP) rd = canon(get(OBJ_FIELD, dstIdx));
+        if (hop == HOP_PISTON_T || hop == HOP_PISTON_F) {
+            rs = canon(get(OBJ_SOURCE, srcIdx));
+            rd = canon(get(hop == HOP_PISTON_T ? OBJ_TARGET : OBJ_FIELD, dstIdx));
+        }
         for (long long jd = 0; jd < M.ndst; jd++) {
             const long long cd = rd.empty() ? jd : rd[jd];
             const uint8_t *row = tmp.data() + jd * M.nsrc;
@@ -1860,7 +1915,7 @@ long long sonar_get_mask_rows(int hop, int srcIdx, int dstIdx, const int *rows, 
     long long nbytes = 0;
     int st = guarded([&] {
         need_render();
-        if (hop < HOP_SRC || hop > HOP_RESP) fail(-6, "invalid hop %d", hop);
+        if (hop < HOP_SRC || hop > HOP_PISTON_F) fail(-6, "invalid hop %d", hop);
         if (nrows < 0 || (nrows > 0 && !rows)) fail(-6, "invalid row list");
         HopSets hs = hop_sets(hop, srcIdx, dstIdx);
         nbytes = (long long)hs.nsrc * nrows;
@@ -1880,6 +1935,10 @@ long long sonar_get_mask_rows(int hop, int srcIdx, int dstIdx, const int *rows, 
         if (hop == HOP_RESP) rd = canon(get(OBJ_TARGET, dstIdx));
         if (hop == HOP_FP) rd = g.fp_order;
         if (hop == HOP_NORESP) rd = canon(get(OBJ_FIELD, dstIdx));
+        if (hop == HOP_PISTON_T || hop == HOP_PISTON_F) {
+            rs = canon(get(OBJ_SOURCE, srcIdx));
+            rd = canon(get(hop == HOP_PISTON_T ? OBJ_TARGET : OBJ_FIELD, dstIdx));
+        }
         // canonical destination -> internal row
         std::vector<int> inv(hs.ndst);
         for (int jd = 0; jd < hs.ndst; jd++) inv[rd.empty() ? jd : rd[jd]] = jd;

@@ -27,6 +27,9 @@ namespace sonar {
 // (FACET_RESP); mask and sum of one direction, keyed (source object,
 // destination object); the ray starts at the lower-index object's point
 enum Hop : int { HOP_SRC = 0, HOP_FP = 1, HOP_F2F = 2, HOP_NORESP = 3, HOP_RESP = 4 };
+// Hops of piston source objects (host bookkeeping; the kernels run them as
+// HOP_RESP and HOP_NORESP): source object -> target, source object -> field object
+constexpr int HOP_PISTON_T = 5, HOP_PISTON_F = 6;
 
 constexpr int kTile = 256;          // sources per tile, destinations per block
 constexpr int kWordsPerTile = kTile / 32;
