@@ -1085,11 +1085,12 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
     ap.add_argument("--mode", default="both", choices=["both", "plain", "compressed"])
-    ap.add_argument("--aca-variant", type=int, default=5, choices=tuple(range(8)),
+    ap.add_argument("--aca-variant", type=int, default=5, choices=tuple(range(11)),
                     help="cross-approximation kernel: k_aca (one row and column per thread): 0 = 8 factor ranks in "
                          "shared memory, 4 CTAs per SM; 1 = 12 ranks, 4 CTAs; 2 = 16 ranks, 3 CTAs; k_aca2 (two rows "
                          "and columns per thread, first bounce's apply fused): 3 = 8 ranks, 4 CTAs; 4 = 6 ranks, "
-                         "5 CTAs; 5 = 4 ranks, 6 CTAs; 6 = 2 ranks, 8 CTAs; 7 = 3 ranks, 7 CTAs")
+                         "5 CTAs; 5 = 4 ranks, 6 CTAs; 6 = 2 ranks, 8 CTAs; 7 = 3 ranks, 7 CTAs; without the fragment "
+                         "staging: 8 = 8 ranks, 6 CTAs; 9 = 6 ranks, 7 CTAs; 10 = 4 ranks, 8 CTAs")
     ap.add_argument("--fused-apply", type=int, default=1, choices=(0, 1),
                     help="k_aca2: apply the accepted blocks to the first bounce's inputs in the same kernel")
     ap.add_argument("--overlap", type=int, default=1, choices=(0, 1),

@@ -2608,7 +2608,10 @@ __device__ __forceinline__ void cta_reduce2(float va, int ia, bool oka, float vb
     }
 }
 
-template <bool ATT, int RS, int MINB>
+// FRAG: both tiles' fragment data staged in shared memory (16 KB) for the
+// pivots' and the judge's reads; without it those reads go through L1 and
+// the shared memory is left to factor ranks and CTAs.
+template <bool ATT, int RS, int MINB, bool FRAG = true>
 __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const int2 *blocks, const uint8_t *cls,
                                                              const int *cap, const long long *off, int nblocks,
                                                              float tol, float limit, float2 *U, float2 *V, int *rank,
@@ -2617,7 +2620,7 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
     extern __shared__ float2 aca_smem[];  // sU[RS][kTile], then sV[RS][kTile]
     float2 *sU = aca_smem, *sV = aca_smem + RS * kTile;
     __shared__ float2 sRow[kTile];
-    __shared__ float4 sFrag[4][kTile];  // position and normal of the columns' (I) and rows' (J) fragments
+    __shared__ float4 sFrag[FRAG ? 4 : 1][FRAG ? kTile : 1];  // position and normal of the columns' (I) and rows' (J) fragments
     __shared__ __align__(16) unsigned slotA[kAca2Warps], slotB[kAca2Warps], slotZ[kAca2Warps];
     __shared__ __align__(16) float2 sumB[kAca2Warps];
     const int t = threadIdx.x, b = blockIdx.x;
@@ -2636,11 +2639,20 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
     const float4 piB = colB ? __ldg(PI + tb) : z4, qiB = colB ? __ldg(NI + tb) : z4;
     const float4 pjA = rowA ? __ldg(PJ + ta) : z4, qjA = rowA ? __ldg(NJ + ta) : z4;
     const float4 pjB = rowB ? __ldg(PJ + tb) : z4, qjB = rowB ? __ldg(NJ + tb) : z4;
-    sFrag[0][ta] = piA; sFrag[0][tb] = piB;
-    sFrag[1][ta] = qiA; sFrag[1][tb] = qiB;
-    sFrag[2][ta] = pjA; sFrag[2][tb] = pjB;
-    sFrag[3][ta] = qjA; sFrag[3][tb] = qjB;
+    if (FRAG) {
+        sFrag[0][ta] = piA; sFrag[0][tb] = piB;
+        sFrag[1][ta] = qiA; sFrag[1][tb] = qiB;
+        sFrag[2][ta] = pjA; sFrag[2][tb] = pjB;
+        sFrag[3][ta] = qjA; sFrag[3][tb] = qjB;
+    }
     __syncthreads();
+    // fragment data of column i (tile I) and row j (tile J)
+    auto fragI = [&](int i, float4 &p, float4 &n) {
+        if (FRAG) { p = sFrag[0][i]; n = sFrag[1][i]; } else { p = __ldg(PI + i); n = __ldg(NI + i); }
+    };
+    auto fragJ = [&](int j, float4 &p, float4 &n) {
+        if (FRAG) { p = sFrag[2][j]; n = sFrag[3][j]; } else { p = __ldg(PJ + j); n = __ldg(NJ + j); }
+    };
     bool usedA = !rowA, usedB = !rowB;  // rows taken (or absent)
     int r = 0, k = 0, zero_rows = 0;
     float norm2 = 0.0f;
@@ -2649,7 +2661,8 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
         // ---- residual row r, entries (r, ta) and (r, tb)
         float2 va = z2, vb = z2;
         {
-            const float4 pr = sFrag[2][r], qr = sFrag[3][r];
+            float4 pr, qr;
+            fragJ(r, pr, qr);
             if (colA) va = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, r, ta) : true, piA, qiA, pr, qr);
             if (colB) vb = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, r, tb) : true, piB, qiB, pr, qr);
             for (int m = 0; m < ks; ++m) {
@@ -2694,7 +2707,8 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
         // ---- residual column c, entries (ta, c) and (tb, c)
         float2 ua = z2, ub = z2;
         {
-            const float4 pc = sFrag[0][c], qc = sFrag[1][c];
+            float4 pc, qc;
+            fragI(c, pc, qc);
             if (rowA) ua = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, ta, c) : true, pc, qc, pjA, qjA);
             if (rowB) ub = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, tb, c) : true, pc, qc, pjB, qjB);
             for (int m = 0; m < ks; ++m) {
@@ -2746,7 +2760,10 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
             const int jj = h2 == 0 ? tt : (int)(h & 255u), ii = h2 == 0 ? (int)(h & 255u) : tt;
             if (ii < ni && jj < nj) {
                 const bool bit = bc == kFlagBits ? block_bit(bw, pitch, jj, ii) : true;
-                const float2 ex = lr_entry<ATT>(a, bc, bit, sFrag[0][ii], sFrag[1][ii], sFrag[2][jj], sFrag[3][jj]);
+                float4 fpi, fni, fpj, fnj;
+                fragI(ii, fpi, fni);
+                fragJ(jj, fpj, fnj);
+                const float2 ex = lr_entry<ATT>(a, bc, bit, fpi, fni, fpj, fnj);
                 float2 ap = z2;
                 for (int m = 0; m < ks; ++m) ap = csub_mul(ap, sU[m * kTile + jj], sV[m * kTile + ii]);
                 for (int m = RS; m < k; ++m) ap = csub_mul(ap, Ub[m * kTile + jj], Vb[m * kTile + ii]);
@@ -2768,9 +2785,13 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
         err[b] = converged ? rel : -1.0f;
     }
     if (brow && accepted) {
-        // the fragment staging is free now: weights and projections of the apply
-        float4 *sW = &sFrag[0][0];
-        float2 *sTv = reinterpret_cast<float2 *>(&sFrag[1][0]), *sSu = sTv + kLrMaxRank;
+        // the fragment staging (or the factor ranks' shared memory) is free
+        // now: weights and projections of the apply
+        static_assert(FRAG || 2 * RS * kTile * sizeof(float2) >= (kTile + 2 * kLrMaxRank) * sizeof(float4) / 1,
+                      "room for the apply's shared arrays");
+        float4 *sW = FRAG ? &sFrag[0][0] : reinterpret_cast<float4 *>(aca_smem);
+        float2 *sTv = FRAG ? reinterpret_cast<float2 *>(&sFrag[1][0]) : reinterpret_cast<float2 *>(sW + kTile);
+        float2 *sSu = sTv + kLrMaxRank;
         lr_block_apply<kAca2Threads>(a, I, J, Ub, Vb, k, brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv,
                                      sSu);
     }
@@ -3288,7 +3309,7 @@ void launch_aca_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, cons
                                                                  rank, fro, err);
 }
 
-template <bool ATT, int RS, int MINB>
+template <bool ATT, int RS, int MINB, bool FRAG = true>
 void launch_aca2_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                    int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
                    cudaStream_t s, float2 *brow, float2 *bcol)
@@ -3296,11 +3317,11 @@ void launch_aca2_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, con
     const size_t smem = (size_t)2 * RS * kTile * sizeof(float2);
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_aca2<ATT, RS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_aca2<ATT, RS, MINB, FRAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
-    k_aca2<ATT, RS, MINB><<<(unsigned)nblocks, kAca2Threads, smem, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit,
-                                                                         U, V, rank, fro, err, brow, bcol);
+    k_aca2<ATT, RS, MINB, FRAG><<<(unsigned)nblocks, kAca2Threads, smem, s>>>(
+        a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro, err, brow, bcol);
 }
 
 template <bool ATT>
@@ -3314,6 +3335,9 @@ bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8
     case 5: launch_aca2_t<ATT, 4, 6>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 6: launch_aca2_t<ATT, 2, 8>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 7: launch_aca2_t<ATT, 3, 7>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 8: launch_aca2_t<ATT, 8, 6, false>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 9: launch_aca2_t<ATT, 6, 7, false>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
+    case 10: launch_aca2_t<ATT, 4, 8, false>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
     case 1: launch_aca_t<ATT, 12, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     case 2: launch_aca_t<ATT, 16, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
     default: launch_aca_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
@@ -3327,7 +3351,8 @@ bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8
 // 2: 16 ranks, 3 CTAs; k_aca2 (two rows and two columns per thread, the first
 // bounce's apply fused): 3: 8 ranks, 4 CTAs; 4: 6 ranks, 5 CTAs; 5: 4 ranks,
 // 6 CTAs (the fastest on the 60 kHz trihedral); 6: 2 ranks, 8 CTAs; 7: 3
-// ranks, 7 CTAs
+// ranks, 7 CTAs; without the fragment staging: 8: 8 ranks, 6 CTAs; 9: 6
+// ranks, 7 CTAs; 10: 4 ranks, 8 CTAs
 bool launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                 int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
                 cudaStream_t s, int variant, float2 *brow, float2 *bcol)

@@ -1749,7 +1749,7 @@ int sonar_set_option(const char *key, double value)
     if (!strcmp(key, "relative_geometry")) { g.opt_rel_geom = value != 0.0; return 0; }
     if (!strcmp(key, "aca_fused_apply")) { g.opt_fused_apply = value != 0.0; g.cmp.release(); return 0; }
     if (!strcmp(key, "aca_variant")) {
-        if (value < 0 || value > 7) return -1;
+        if (value < 0 || value > 10) return -1;
         g.opt_aca_variant = (int)value;
         return 0;
     }

@@ -101,7 +101,7 @@ def test_cross_approximation_variants_identical(api, scenes):
     assert np.array_equal(out[0], out[1])
     assert np.array_equal(out[0], out[2])
     with pytest.raises(api.SonarError):
-        api.set_option("aca_variant", 8)
+        api.set_option("aca_variant", 11)
 
 
 def test_two_entry_cross_approximation(api, scenes):
