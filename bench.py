@@ -175,7 +175,7 @@ def step_pairs(stats):
 
 RCUT = [24.0]  # the admissibility network proposes blocks with predicted rank below this
 TOL = [5e-4]   # cross-approximation tolerance (the judge accepts 3 x this RMS error)
-ACA_VARIANT = [5]  # cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
+ACA_VARIANT = [8]  # cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
 OVERLAP = [1]      # compressed bounce: low-rank apply on a second stream beside the dense remainder
 FUSED = [1]        # k_aca2: the first bounce's low-rank apply fused into the cross approximation
 
@@ -1085,7 +1085,7 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up and steps of device work only (for ncu captures)")
     ap.add_argument("--mode", default="both", choices=["both", "plain", "compressed"])
-    ap.add_argument("--aca-variant", type=int, default=5, choices=tuple(range(11)),
+    ap.add_argument("--aca-variant", type=int, default=8, choices=tuple(range(11)),
                     help="cross-approximation kernel: k_aca (one row and column per thread): 0 = 8 factor ranks in "
                          "shared memory, 4 CTAs per SM; 1 = 12 ranks, 4 CTAs; 2 = 16 ranks, 3 CTAs; k_aca2 (two rows "
                          "and columns per thread, first bounce's apply fused): 3 = 8 ranks, 4 CTAs; 4 = 6 ranks, "

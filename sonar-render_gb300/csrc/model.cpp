@@ -280,7 +280,7 @@ struct Model {
     int opt_cmp_rmax = 32;
     int opt_cmp_select = 0;     // 0 rule (class ALL, eta-separated), 1 every interacting block, 2 the network
     float opt_cmp_rcut = 24.0f; // network: propose blocks whose predicted rank is below this
-    int opt_aca_variant = 5;    // cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
+    int opt_aca_variant = 8;    // cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
     int opt_rel_geom = 0;       // source hop and readout: phase distances relative to FP64 references
     int opt_fused_apply = 1;    // k_aca2: apply the accepted blocks to the building bounce's inputs in the same kernel
     int opt_mask_classify = 1;  // bounce masks: warp-per-block classification, pair kernel on the listed blocks

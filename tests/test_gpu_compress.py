@@ -95,7 +95,7 @@ def test_cross_approximation_variants_identical(api, scenes):
         hop = [h for h in st["hops"] if h["hop"] == 2][0]
         out.append(P)
         ranks.append(hop["cmp_mean_rank"])
-    api.set_option("aca_variant", 5)
+    api.set_option("aca_variant", 8)
     api.set_option("compress_select", 0)
     print("mean ranks per variant", ranks)
     assert np.array_equal(out[0], out[1])
@@ -115,14 +115,14 @@ def test_two_entry_cross_approximation(api, scenes):
     api.set_option("compress_select", 1)
     out, ranks = {}, {}
     try:
-        for v, fused in ((0, 1), (3, 1), (5, 1), (5, 0), (7, 1)):
+        for v, fused in ((0, 1), (3, 1), (5, 1), (5, 0), (7, 1), (8, 1), (10, 1)):
             api.set_option("aca_variant", v)
             api.set_option("aca_fused_apply", fused)
             P0, out[(v, fused)], st = _bounces(api, sc, 1)
             hop = [h for h in st["hops"] if h["hop"] == 2][0]
             ranks[(v, fused)] = (hop["cmp_mean_rank"], hop["cmp_accepted"])
     finally:
-        api.set_option("aca_variant", 5)
+        api.set_option("aca_variant", 8)
         api.set_option("aca_fused_apply", 1)
         api.set_option("compress_select", 0)
     print("two-entry variants (mean rank, accepted):", ranks)
