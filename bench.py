@@ -177,6 +177,7 @@ RCUT = [24.0]  # the admissibility network proposes blocks with predicted rank b
 TOL = [5e-4]   # cross-approximation tolerance (the judge accepts 3 x this RMS error)
 ACA_VARIANT = [8]  # cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
 OVERLAP = [1]      # compressed bounce: low-rank apply on a second stream beside the dense remainder
+LR_CTAS = [4]      # low-rank apply: resident CTAs per SM (register cap)
 FUSED = [1]        # k_aca2: the first bounce's low-rank apply fused into the cross approximation
 
 
@@ -188,6 +189,7 @@ def set_path(api, compressed, select):
     api.set_option("compress_judge", 3.0 * TOL[0])
     api.set_option("aca_variant", ACA_VARIANT[0])
     api.set_option("aca_fused_apply", FUSED[0])
+    api.set_option("lr_block_ctas", LR_CTAS[0])
     api.set_option("overlap_streams", OVERLAP[0])
 
 
@@ -1091,6 +1093,8 @@ def main():
                          "and columns per thread, first bounce's apply fused): 3 = 8 ranks, 4 CTAs; 4 = 6 ranks, "
                          "5 CTAs; 5 = 4 ranks, 6 CTAs; 6 = 2 ranks, 8 CTAs; 7 = 3 ranks, 7 CTAs; without the fragment "
                          "staging: 8 = 8 ranks, 6 CTAs; 9 = 6 ranks, 7 CTAs; 10 = 4 ranks, 8 CTAs")
+    ap.add_argument("--lr-ctas", type=int, default=4, choices=(4, 6, 8),
+                    help="low-rank apply kernel: resident CTAs per SM (its register cap)")
     ap.add_argument("--fused-apply", type=int, default=1, choices=(0, 1),
                     help="k_aca2: apply the accepted blocks to the first bounce's inputs in the same kernel")
     ap.add_argument("--overlap", type=int, default=1, choices=(0, 1),
@@ -1117,6 +1121,7 @@ def main():
     ACA_VARIANT[0] = args.aca_variant
     OVERLAP[0] = args.overlap
     FUSED[0] = args.fused_apply
+    LR_CTAS[0] = args.lr_ctas
     TOL[0] = args.tol
     if args.impl == "reference":
         run_reference(args)

@@ -2902,9 +2902,10 @@ __global__ void __launch_bounds__(128) k_block_desc(SumArgs a, const int2 *block
 // Compressed bounce, one CTA per accepted block q (kept block b = bidx[q]):
 // lr_block_apply into the block's output slots b.  The factors are read from
 // HBM once; the second pass over them hits L2.
-__global__ void __launch_bounds__(kTile) k_lr_block(SumArgs a, const int2 *blocks, const long long *off,
-                                                    const int *bidx, int nb, const float2 *U, const float2 *V,
-                                                    const int *rank, float2 *brow, float2 *bcol, const int *ndev)
+template <int MINB>
+__global__ void __launch_bounds__(kTile, MINB) k_lr_block(SumArgs a, const int2 *blocks, const long long *off,
+                                                          const int *bidx, int nb, const float2 *U, const float2 *V,
+                                                          const int *rank, float2 *brow, float2 *bcol, const int *ndev)
 {
     __shared__ float4 sW[kTile];  // (Re w_I, Im w_I, Re w_J, Im w_J) of every row t
     __shared__ float2 sTv[kLrMaxRank], sSu[kLrMaxRank];
@@ -3382,9 +3383,15 @@ void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls,
 void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
                      const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
-                     double2 *ycol, cudaStream_t s, const int *ndev, bool outputs_ready)
+                     double2 *ycol, cudaStream_t s, const int *ndev, bool outputs_ready, int lr_ctas)
 {
-    if (nb > 0 && !outputs_ready) k_lr_block<<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev);
+    // latency-bound on the factor stream: resident CTAs per SM are the lever
+    // (registers capped to fit lr_ctas of them)
+    if (nb > 0 && !outputs_ready) {
+        if (lr_ctas >= 8) k_lr_block<8><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev);
+        else if (lr_ctas >= 6) k_lr_block<6><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev);
+        else k_lr_block<4><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev);
+    }
     if (ntiles > 0)
         k_lr_gather<<<ntiles, kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, bidx, yrow, ycol);
 }

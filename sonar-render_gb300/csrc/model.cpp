@@ -281,6 +281,7 @@ struct Model {
     int opt_cmp_select = 0;     // 0 rule (class ALL, eta-separated), 1 every interacting block, 2 the network
     float opt_cmp_rcut = 24.0f; // network: propose blocks whose predicted rank is below this
     int opt_aca_variant = 8;    // cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
+    int opt_lr_ctas = 4;        // low-rank apply: resident CTAs per SM its register cap allows (4, 6, 8)
     int opt_rel_geom = 0;       // source hop and readout: phase distances relative to FP64 references
     int opt_fused_apply = 1;    // k_aca2: apply the accepted blocks to the building bounce's inputs in the same kernel
     int opt_mask_classify = 1;  // bounce masks: warp-per-block classification, pair kernel on the listed blocks
@@ -1121,7 +1122,7 @@ void run_hop(int hop, int a, int b)
                 CK(cudaEventRecord(g.ev4, lst));
                 launch_lr_apply(s, C.d_blocks, C.d_off, C.d_bidx, C.nblocks, C.d_U, C.d_V, C.d_rank, C.d_brow, C.d_bcol,
                                 M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, lst,
-                                C.d_nacc, built && C.outputs_ready);
+                                C.d_nacc, built && C.outputs_ready, g.opt_lr_ctas);
                 CK(cudaEventRecord(g.ev5, lst));
                 if (g.opt_overlap) CK(cudaEventRecord(g.ev_join, lst));
                 yrow = C.d_yrow;
@@ -1744,6 +1745,11 @@ int sonar_set_option(const char *key, double value)
     if (!strcmp(key, "mask_classify")) {
         g.opt_mask_classify = value != 0.0 ? 1 : 0;
         for (auto &m : g.masks) m.stale = true;
+        return 0;
+    }
+    if (!strcmp(key, "lr_block_ctas")) {
+        if (value != 4 && value != 6 && value != 8) return -1;
+        g.opt_lr_ctas = (int)value;
         return 0;
     }
     if (!strcmp(key, "relative_geometry")) { g.opt_rel_geom = value != 0.0; return 0; }

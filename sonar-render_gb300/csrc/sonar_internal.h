@@ -174,7 +174,8 @@ void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls,
 void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
                      const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
-                     double2 *ycol, cudaStream_t s, const int *ndev = nullptr, bool outputs_ready = false);
+                     double2 *ycol, cudaStream_t s, const int *ndev = nullptr, bool outputs_ready = false,
+                     int lr_ctas = 4);
 // select.cu: block lists of the compressed bounce, built on the device
 void launch_cand_lists(const uint8_t *flags, int nt, int nb, int select, float eta, const float4 *cen, int *cnt,
                        int *off, int2 *blocks, uint8_t *cls, cudaStream_t s);
