@@ -323,38 +323,41 @@ def lowrank_roofline(stats):
     ms = sum(x["lr_ms"] for x in hops) / len(hops)
     peak, src = hbm_peak()
     ach = bytes_launch / (ms * 1e-3) / 1e9
-    # k_lr_block's DRAM bytes were 0.945 x these algorithmic bytes in the ncu
-    # capture on the 40 kHz trihedral at tolerance 5e-4 (1.152 GB for 19,452
-    # blocks at rank 13.3)
+    # k_lr_block's DRAM bytes were 0.985 x these algorithmic bytes in the ncu
+    # capture on the 40 kHz trihedral at tolerance 5e-4 (1.141 GB for 19,502
+    # blocks at rank 13.5)
     return {"kernel": "k_lr_block + k_lr_gather (low-rank apply)", "bound": "hbm", "achieved": round(ach, 1),
-            "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": round(0.945 * bytes_launch),
+            "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": round(0.985 * bytes_launch),
             "traffic_source": "ncu dram bytes of k_lr_block on the 40 kHz capture, scaled by algorithmic bytes",
             "bytes_per_launch": int(bytes_launch), "launch_ms": round(ms, 4), "peak_source": src,
             "blocks": nacc, "mean_rank": h["cmp_mean_rank"]}
 
 
 def aca_roofline(stats, fp32_peak):
-    """Cross approximation (k_aca), FP32 work per launch: per approximated
-    block of rank k, 2 k residual rows/columns of 256 entries plus 512 judged
+    """Cross approximation (k_aca2: with the first bounce's low-rank apply of
+    every accepted block fused), FP32 work per launch: per approximated block
+    of rank k, 2 k residual rows/columns of 256 entries plus 512 judged
     entries at 48 flop per Green's function evaluation, the residual updates
-    (2 x 256 x k (k - 1) / 2 complex MACs, 8 flop each) and the judged
-    entries' approximations (512 k complex MACs); k = the mean accepted rank."""
+    (2 x 256 x k (k - 1) / 2 complex MACs, 8 flop each), the judged entries'
+    approximations (512 k complex MACs) and the fused apply (4 x 256 x k
+    complex MACs); k = the mean accepted rank."""
     hops = [h for h in stats["hops"] if h["hop"] == 2 and h.get("cmp_aca_ms")]
     if not hops or not fp32_peak:
         return None
     h = hops[0]
     k = h["cmp_mean_rank"]
     nb = h["cmp_blocks"]
-    flop_block = 48.0 * (2 * 256 * k + 512) + 8.0 * 256 * k * (k - 1) + 8.0 * 512 * k
+    flop_block = 48.0 * (2 * 256 * k + 512) + 8.0 * 256 * k * (k - 1) + 8.0 * 512 * k + 8.0 * 4 * 256 * k
     ms = sum(x["cmp_aca_ms"] for x in hops) / len(hops)
     ach = nb * flop_block / (ms * 1e-3) / 1e12
     peak = fp32_peak / 1e12
     # DRAM bytes per (block x rank) from the ncu capture of this kernel on the
     # 40 kHz trihedral with every interacting block approximated at tolerance
-    # 5e-4 (1.119 GB for 20,170 blocks at mean rank 13.3: the factors written
-    # once), scaled to this launch by its blocks x ranks
-    traffic = 4172.0 * nb * k
-    return {"kernel": "k_aca (cross approximation + exact-entry judge)", "bound": "fp32 issue (serial pivots)",
+    # 5e-4 (0.116 GB read + 1.138 GB written for 20,170 blocks at mean rank
+    # 13.5: the factors written once), scaled to this launch by blocks x rank
+    traffic = 4605.0 * nb * k
+    return {"kernel": "k_aca2 (cross approximation + exact-entry judge + first bounce's low-rank apply)",
+            "bound": "fp32 issue / load latency (serial pivots)",
             "achieved": round(ach, 3), "peak": round(peak, 3), "unit": "TFLOP/s", "frac": round(ach / peak, 4),
             "traffic": round(traffic), "traffic_source": "ncu dram bytes of the 40 kHz capture, scaled by blocks x rank",
             "blocks_per_launch": nb, "mean_rank": k, "flop_per_block": round(flop_block),
