@@ -269,6 +269,11 @@ int sonar_batch_stats(long long plan, char *json, int cap);
  * geometry, its fragments and the tuning are kept; the run recomputes the
  * visibility words.  Returns 0 or a negative code. */
 int sonar_batch_set_points(long long plan, const float *src_xyz, int nsrc, const float *rx_xyz, int nrx);
+/* Replace the tuned tile shape of a plan (diagnostics and tests): fragments
+ * per operand stage 16, 32 or 64 and persistent CTAs per SM (as many as
+ * shared memory holds, at most 4); the run graph is captured again.  Returns
+ * 0 or a negative code. */
+int sonar_batch_set_shape(long long plan, int fragments_per_stage, int ctas_per_sm);
 int sonar_batch_stream(long long plan, void **stream);
 int sonar_batch_free(long long plan);
 int sonar_run_batch(const float *tris, const int *scene_tri_off, int nscenes, const float *src_xyz, int nsrc,

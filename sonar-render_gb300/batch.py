@@ -40,6 +40,7 @@ def _lib():
         L.sonar_batch_stats.argtypes = [C.c_longlong, C.c_char_p, C.c_int]
         L.sonar_batch_stream.argtypes = [C.c_longlong, C.POINTER(C.c_void_p)]
         L.sonar_batch_set_points.argtypes = [C.c_longlong, _f, C.c_int, _f, C.c_int]
+        L.sonar_batch_set_shape.argtypes = [C.c_longlong, C.c_int, C.c_int]
         L.sonar_batch_free.argtypes = [C.c_longlong]
         L.sonar_run_batch.argtypes = [_f, _i, C.c_int, _f, C.c_int, _f, C.c_int, _f, C.c_int, C.c_float,
                                       C.c_float, C.c_float, _d]
@@ -96,6 +97,12 @@ class Plan:
         r = _lib().sonar_batch_set_points(self.id, S.ctypes.data_as(_f), S.shape[0], R.ctypes.data_as(_f), R.shape[0])
         if r != 0:
             raise _err("sonar_batch_set_points", r)
+
+    def set_shape(self, fragments_per_stage, ctas_per_sm):
+        """Run with this tile shape instead of the tuned one."""
+        r = _lib().sonar_batch_set_shape(self.id, int(fragments_per_stage), int(ctas_per_sm))
+        if r != 0:
+            raise _err("sonar_batch_set_shape", r)
 
     def stats(self):
         L = _lib()

@@ -690,6 +690,30 @@ int sonar_batch_set_points(long long plan, const float *src_xyz, int nsrc, const
     });
 }
 
+int sonar_batch_set_shape(long long plan, int fragments_per_stage, int ctas_per_sm)
+{
+    std::lock_guard<std::mutex> lk(g_lock);
+    return (int)bguard([&]() -> long long {
+        Plan &p = find(plan);
+        if (fragments_per_stage != 16 && fragments_per_stage != 32 && fragments_per_stage != 64)
+            bfail(-6, "sonar_batch_set_shape: fragments per stage must be 16, 32 or 64 (got %d)", fragments_per_stage);
+        int dev = 0, nsm = 0, smem_optin = 0;
+        BCK(cudaGetDevice(&dev));
+        BCK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        BCK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+        const int fit = std::max(1, std::min(4, (int)((size_t)smem_optin / (batch_smem_bytes(fragments_per_stage) + 10240))));
+        if (ctas_per_sm < 1 || ctas_per_sm > fit)
+            bfail(-6, "sonar_batch_set_shape: %d CTAs per SM (1 to %d fit at %d fragments per stage)", ctas_per_sm, fit,
+                  fragments_per_stage);
+        p.tune.kc = fragments_per_stage;
+        p.tune.grid = ctas_per_sm * nsm;
+        WorkList w = make_worklist(p, p.tune.kc, p.tune.grid);
+        upload_worklist(p, w, p.tune.grid);
+        capture(p);
+        return 0;
+    });
+}
+
 int sonar_batch_stream(long long plan, void **stream)
 {
     std::lock_guard<std::mutex> lk(g_lock);

@@ -156,3 +156,27 @@ def test_plan_reused_with_new_points(api, oracle_mod, scenes):
     print("moved points: vs a new plan %.3e, vs FP64 oracle (box, %.0f Hz) %.3e" % (e_fresh, freqs[0], e_orc))
     assert e_fresh < 1e-6
     assert e_orc < TOL
+
+
+def test_every_tuning_shape(api, oracle_mod, scenes):
+    """Every candidate tile shape of the autotuner (16, 32 or 64 fragments per
+    operand stage, 1 to 4 persistent CTAs per SM as shared memory allows)
+    gives the same products, within the FP32 summation-order round-off of
+    each other and within the tolerance of FP64."""
+    from sonar_render_gb300 import batch
+    tris, src, rx, freqs = small_batch(scenes)
+    plan = batch.Plan(tris, src, rx, freqs)
+    out = {}
+    for kc, per_sm in ((16, 1), (16, 2), (16, 3), (32, 1), (32, 2), (64, 1)):
+        plan.set_shape(kc, per_sm)
+        out[(kc, per_sm)] = plan.run()
+    with pytest.raises(Exception):
+        plan.set_shape(48, 1)
+    plan.close()
+    ref = oracle_columns(oracle_mod, tris[2], src, rx, freqs[1])
+    base = out[(32, 2)]
+    for key, o in out.items():
+        e_shape = rel_l2(o, base)
+        e_orc = rel_l2(o[2, 1], ref)
+        print("shape %s: vs 32 x 2 %.2e, vs FP64 (sphere, %.0f Hz) %.2e" % (key, e_shape, freqs[1], e_orc))
+        assert e_shape < 1e-6 and e_orc < TOL
