@@ -2477,7 +2477,9 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *bloc
 // are the packed inputs (srcA.w, srcB.w).  sW holds kTile float4, sTv and
 // sSu kLrMaxRank float2.  Starts with a barrier (the caller may reuse the
 // shared arrays).
-template <int NT = kTile>
+// LDG: the factors were written by an earlier kernel, so the projections may
+// read them through the read-only path (the fused caller wrote them itself).
+template <int NT = kTile, bool LDG = false>
 __device__ __forceinline__ void lr_block_apply(const SumArgs &a, int I, int J, const float2 *U0, const float2 *V0,
                                                int k, float2 *brow_b, float2 *bcol_b, float4 *sW, float2 *sTv,
                                                float2 *sSu)
@@ -2496,7 +2498,8 @@ __device__ __forceinline__ void lr_block_apply(const SumArgs &a, int I, int J, c
 #pragma unroll
         for (int r = 0; r < kTile / 32; ++r) {
             const int tt = lane + 32 * r;
-            const float2 v = V0[(size_t)m * kTile + tt], u = U0[(size_t)m * kTile + tt];
+            const float2 v = LDG ? __ldg(V0 + (size_t)m * kTile + tt) : V0[(size_t)m * kTile + tt];
+            const float2 u = LDG ? __ldg(U0 + (size_t)m * kTile + tt) : U0[(size_t)m * kTile + tt];
             const float4 w = sW[tt];
             p.x = fmaf(v.x, w.x, fmaf(-v.y, w.y, p.x));
             p.y = fmaf(v.x, w.y, fmaf(v.y, w.x, p.y));
@@ -2912,8 +2915,8 @@ __global__ void __launch_bounds__(kTile, MINB) k_lr_block(SumArgs a, const int2 
     const int q = blockIdx.x;
     if (q >= (ndev ? min(*ndev, nb) : nb)) return;
     const int b = bidx[q];
-    lr_block_apply(a, blocks[b].x, blocks[b].y, U + off[b] * kTile, V + off[b] * kTile, rank[b],
-                   brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv, sSu);
+    lr_block_apply<kTile, true>(a, blocks[b].x, blocks[b].y, U + off[b] * kTile, V + off[b] * kTile, rank[b],
+                                brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv, sSu);
 }
 
 // Per owner tile X: rows of every accepted block with J = X and columns of
