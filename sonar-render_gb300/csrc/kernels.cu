@@ -2318,14 +2318,6 @@ __device__ __forceinline__ void cta_reduce(float &v, int &idx, bool valid, float
     }
 }
 
-// acc + u v (complex)
-__device__ __forceinline__ float2 cmac(float2 acc, float2 u, float2 v)
-{
-    acc.x = fmaf(u.x, v.x, fmaf(-u.y, v.y, acc.x));
-    acc.y = fmaf(u.x, v.y, fmaf(u.y, v.x, acc.y));
-    return acc;
-}
-
 // x - u v (complex)
 __device__ __forceinline__ float2 csub_mul(float2 x, float2 u, float2 v)
 {
@@ -2674,31 +2666,18 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
         {
             float4 pr, qr;
             fragJ(r, pr, qr);
-            // the earlier ranks' part, sum_m U(r, m) V(t, m), in two chains per
-            // entry independent of the Green's entry (they overlap with it)
-            float2 sa0 = z2, sa1 = z2, sb0 = z2, sb1 = z2;
-            int m = 0;
-            for (; m + 1 < ks; m += 2) {
-                const float2 u0 = sU[m * kTile + r], u1 = sU[(m + 1) * kTile + r];
-                sa0 = cmac(sa0, u0, sV[m * kTile + ta]);
-                sb0 = cmac(sb0, u0, sV[m * kTile + tb]);
-                sa1 = cmac(sa1, u1, sV[(m + 1) * kTile + ta]);
-                sb1 = cmac(sb1, u1, sV[(m + 1) * kTile + tb]);
-            }
-            if (m < ks) {
-                const float2 u0 = sU[m * kTile + r];
-                sa0 = cmac(sa0, u0, sV[m * kTile + ta]);
-                sb0 = cmac(sb0, u0, sV[m * kTile + tb]);
-            }
-            for (m = RS; m < k; ++m) {
-                const float2 ur = Ub[m * kTile + r];
-                sa1 = cmac(sa1, ur, Vb[m * kTile + ta]);
-                sb1 = cmac(sb1, ur, Vb[m * kTile + tb]);
-            }
             if (colA) va = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, r, ta) : true, piA, qiA, pr, qr);
             if (colB) vb = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, r, tb) : true, piB, qiB, pr, qr);
-            va = colA ? make_float2(va.x - (sa0.x + sa1.x), va.y - (sa0.y + sa1.y)) : z2;
-            vb = colB ? make_float2(vb.x - (sb0.x + sb1.x), vb.y - (sb0.y + sb1.y)) : z2;
+            for (int m = 0; m < ks; ++m) {
+                const float2 ur = sU[m * kTile + r];
+                va = csub_mul(va, ur, sV[m * kTile + ta]);
+                vb = csub_mul(vb, ur, sV[m * kTile + tb]);
+            }
+            for (int m = RS; m < k; ++m) {
+                const float2 ur = Ub[m * kTile + r];
+                va = csub_mul(va, ur, Vb[m * kTile + ta]);
+                vb = csub_mul(vb, ur, Vb[m * kTile + tb]);
+            }
         }
         sRow[ta] = va;
         sRow[tb] = vb;
@@ -2733,29 +2712,18 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
         {
             float4 pc, qc;
             fragI(c, pc, qc);
-            float2 sa0 = z2, sa1 = z2, sb0 = z2, sb1 = z2;
-            int m = 0;
-            for (; m + 1 < ks; m += 2) {
-                const float2 v0 = sV[m * kTile + c], v1 = sV[(m + 1) * kTile + c];
-                sa0 = cmac(sa0, sU[m * kTile + ta], v0);
-                sb0 = cmac(sb0, sU[m * kTile + tb], v0);
-                sa1 = cmac(sa1, sU[(m + 1) * kTile + ta], v1);
-                sb1 = cmac(sb1, sU[(m + 1) * kTile + tb], v1);
-            }
-            if (m < ks) {
-                const float2 v0 = sV[m * kTile + c];
-                sa0 = cmac(sa0, sU[m * kTile + ta], v0);
-                sb0 = cmac(sb0, sU[m * kTile + tb], v0);
-            }
-            for (m = RS; m < k; ++m) {
-                const float2 vc = Vb[m * kTile + c];
-                sa1 = cmac(sa1, Ub[m * kTile + ta], vc);
-                sb1 = cmac(sb1, Ub[m * kTile + tb], vc);
-            }
             if (rowA) ua = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, ta, c) : true, pc, qc, pjA, qjA);
             if (rowB) ub = lr_entry<ATT>(a, bc, bc == kFlagBits ? block_bit(bw, pitch, tb, c) : true, pc, qc, pjB, qjB);
-            ua = rowA ? make_float2(ua.x - (sa0.x + sa1.x), ua.y - (sa0.y + sa1.y)) : z2;
-            ub = rowB ? make_float2(ub.x - (sb0.x + sb1.x), ub.y - (sb0.y + sb1.y)) : z2;
+            for (int m = 0; m < ks; ++m) {
+                const float2 vc = sV[m * kTile + c];
+                ua = csub_mul(ua, sU[m * kTile + ta], vc);
+                ub = csub_mul(ub, sU[m * kTile + tb], vc);
+            }
+            for (int m = RS; m < k; ++m) {
+                const float2 vc = Vb[m * kTile + c];
+                ua = csub_mul(ua, Ub[m * kTile + ta], vc);
+                ub = csub_mul(ub, Ub[m * kTile + tb], vc);
+            }
         }
         Ub[k * kTile + ta] = ua;
         Ub[k * kTile + tb] = ub;
