@@ -179,6 +179,7 @@ ACA_VARIANT = [8]  # cross-approximation kernel shape (k_aca / k_aca2, factor ra
 OVERLAP = [1]      # compressed bounce: low-rank apply on a second stream beside the dense remainder
 LR_CTAS = [4]      # low-rank apply: resident CTAs per SM (register cap)
 FUSED = [1]        # k_aca2: the first bounce's low-rank apply fused into the cross approximation
+INTERP = [1]       # far class-ALL blocks between planar tiles by directional interpolation
 
 
 def set_path(api, compressed, select):
@@ -191,6 +192,7 @@ def set_path(api, compressed, select):
     api.set_option("aca_fused_apply", FUSED[0])
     api.set_option("lr_block_ctas", LR_CTAS[0])
     api.set_option("overlap_streams", OVERLAP[0])
+    api.set_option("compress_interp", INTERP[0])
 
 
 def time_path(api, cfg, args, flush, local, world, reuse=False):
@@ -265,7 +267,9 @@ def kernel_times(stats, steps):
         if h.get("cmp_build_ms"):
             k["select_blocks"] = k.get("select_blocks", 0.0) + h["cmp_select_ms"]
             k["cross_approx"] = k.get("cross_approx", 0.0) + h["cmp_aca_ms"]
-            k["build_other"] = k.get("build_other", 0.0) + h["cmp_build_ms"] - h["cmp_select_ms"] - h["cmp_aca_ms"]
+            k["interpolation"] = k.get("interpolation", 0.0) + h.get("cmp_ip_ms", 0.0)
+            k["build_other"] = k.get("build_other", 0.0) + (h["cmp_build_ms"] - h["cmp_select_ms"] - h["cmp_aca_ms"]
+                                                            - h.get("cmp_ip_ms", 0.0))
     return {n: v / max(steps, 1) for n, v in k.items() if v > 0}
 
 
@@ -905,6 +909,7 @@ def run_gb300(args):
                        [h["cmp_select"]], "candidate_blocks": h["cmp_cand"], "approximated": h["cmp_blocks"],
                        "accepted": h["cmp_accepted"], "pair_fraction_compressed": round(h["cmp_pairs"] / h["pairs"], 4),
                        "mean_rank": h["cmp_mean_rank"], "max_judged_block_err": h["cmp_max_err"],
+                       "interpolated_blocks": h.get("cmp_ip_blocks", 0), "interpolation_mean_nodes": h.get("cmp_ip_nodes", 0.0),
                        "tolerance": TOL[0], "judge_limit": 3.0 * TOL[0], "network_training": train_info,
                        "judge_audit": audit}
     kms = H["kernels_ms_per_step"]
@@ -1121,6 +1126,9 @@ def main():
                     help="low-rank apply kernel: resident CTAs per SM (its register cap)")
     ap.add_argument("--fused-apply", type=int, default=1, choices=(0, 1),
                     help="k_aca2: apply the accepted blocks to the first bounce's inputs in the same kernel")
+    ap.add_argument("--interp", type=int, default=1, choices=(0, 1),
+                    help="compressed bounce: far class-ALL blocks between planar tiles by directional interpolation "
+                         "(the rest by cross approximation)")
     ap.add_argument("--overlap", type=int, default=1, choices=(0, 1),
                     help="compressed bounce: low-rank apply on a second stream beside the dense remainder")
     ap.add_argument("--tol", type=float, default=5e-4,
@@ -1145,6 +1153,7 @@ def main():
     ACA_VARIANT[0] = args.aca_variant
     OVERLAP[0] = args.overlap
     FUSED[0] = args.fused_apply
+    INTERP[0] = args.interp
     LR_CTAS[0] = args.lr_ctas
     TOL[0] = args.tol
     if args.impl == "reference":

@@ -28,6 +28,7 @@
 //   NORESP  P_j += A_i cos_scat P_i 0.9 G_reg(r)                (OptiX.cu:340-362)
 //   G(r) = -e^{ikr}/(4 pi) (ik/r) + 1/r^2,  G_reg = ik/(4 pi) when r < delta_src.
 #include "sonar_internal.h"
+#include "green.cuh"
 
 #include <algorithm>
 #include <cstdio>
@@ -35,15 +36,6 @@
 namespace sonar {
 namespace {
 
-constexpr float kInv4Pi = 0.0795774715459476679f;  // 1 / (4 pi)
-constexpr float kTwoPi = 6.28318530717958647692f;
-
-__device__ __forceinline__ float dot_rn(float ax, float ay, float az, float bx, float by, float bz)
-{
-    // a.x*b.x + a.y*b.y + a.z*b.z evaluated left to right, every product and
-    // sum rounded separately (the reference's vec_math dot without contraction)
-    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
-}
 
 // ---------------------------------------------------------------- visibility
 // Does the part [tlo, 1] of segment o + t (e - o) touch the box?  (inv =
@@ -144,19 +136,6 @@ __device__ bool occluded(const BvhView &B, float3 o, float3 e, float r, float tm
 }
 
 // ---------------------------------------------------------------- gates
-// Cosine gates.  The reference's decision is "cos < 1e-6 -> skip" with
-// cos = dot(v * (1/r), n) in FP32 without contraction (exact_cos below).  A
-// cheaper estimate dot(v, n) * rsqrt(v.v) differs from it by less than 7e-7
-// (both are within a few ulp of the true cosine, |cos| <= 1), so outside the
-// band [0, 2e-6] the estimate decides the same way; inside it the exact
-// expression is evaluated.
-__device__ __forceinline__ float exact_cos(float vx, float vy, float vz, float sign, float nx, float ny, float nz)
-{
-    const float r = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
-    const float inv = __frcp_rn(r);
-    const float ux = __fmul_rn(vx, inv), uy = __fmul_rn(vy, inv), uz = __fmul_rn(vz, inv);
-    return dot_rn(sign * ux, sign * uy, sign * uz, nx, ny, nz);
-}
 
 // true when cos(sign * v, n) passes the reference's ">= 1e-6" gate
 __device__ __forceinline__ bool cos_gate(float vx, float vy, float vz, float rinv, float sign, float nx, float ny,
@@ -2199,66 +2178,6 @@ __device__ __forceinline__ float block_sum(float v, float *sv)
     return t;
 }
 
-// The exact FP32 cosine gate where the estimate is inside the band (rare):
-// kept out of line so that kernels that unroll several entries carry one
-// copy of it.
-__device__ __noinline__ bool gate_exact(float vx, float vy, float vz, float sign, float nx, float ny, float nz)
-{
-    return !(exact_cos(vx, vy, vz, sign, nx, ny, nz) < 1e-6f);
-}
-
-__device__ __forceinline__ bool gate_est(float est, float vx, float vy, float vz, float sign, float nx, float ny,
-                                         float nz)
-{
-    if (est > 2e-6f) return true;
-    if (est < 0.0f) return false;
-    return gate_exact(vx, vy, vz, sign, nx, ny, nz);
-}
-
-// T(j, i) of one pair of a block of class cls (bit: the pair's mask bit for
-// BITS; CLEAR blocks evaluate the cosine gates inline).  One code path for
-// every class: the Green's function of sym_pair (same operations, same
-// rounding), then the pair's gate.
-template <bool ATT>
-__device__ __forceinline__ float2 lr_entry(const SumArgs &a, int cls, bool bit, float4 pi, float4 ni, float4 pj,
-                                           float4 nj)
-{
-    const float vx = __fsub_rn(pj.x, pi.x), vy = __fsub_rn(pj.y, pi.y), vz = __fsub_rn(pj.z, pi.z);
-    const float r2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
-    const float rinv = rsqrtf(r2);
-    const float r0 = r2 * rinv;
-    const float r = fmaf(fmaf(-r0, r0, r2), 0.5f * rinv, r0);
-    const float th = __fmul_rn(r, a.k2hi);
-    const float tl = fmaf(r, a.k2lo, fmaf(r, a.k2hi, -th));
-    const float frac = (th - rintf(th)) + tl;
-    float sn, cs;
-    __sincosf(frac * kTwoPi, &sn, &cs);
-    const float d1 = vx * ni.x + vy * ni.y + vz * ni.z;  // r cos_scat
-    const float d2 = vx * nj.x + vy * nj.y + vz * nj.z;  // -r cos_inc
-    const float rinv2 = rinv * rinv;
-    const float u = (d1 * d2) * (-rinv2);
-    float Tr, Ti;
-    if (ATT) {
-        const float amp = rinv * kInv4Pi * __expf(-a.ka * r);
-        Tr = u * fmaf(amp, fmaf(a.ka, cs, a.kr * sn), rinv2);
-        Ti = u * (amp * fmaf(a.ka, sn, -a.kr * cs));
-    } else {
-        const float ua = (u * rinv) * a.kr4pi;
-        Tr = fmaf(ua, sn, u * rinv2);
-        Ti = -ua * cs;
-    }
-    float rr = r;
-    if (fabsf(r - a.rmin) <= a.rmin * 1e-6f) rr = __fsqrt_rn(dot_rn(vx, vy, vz, vx, vy, vz));
-    if (rr < a.rmin) {
-        Tr = u * (-a.ka * kInv4Pi);
-        Ti = u * (a.kr * kInv4Pi);
-    }
-    bool ok = cls == kFlagBits ? bit : true;
-    if (cls == kFlagClear)
-        ok = gate_est(d1 * rinv, vx, vy, vz, 1.0f, ni.x, ni.y, ni.z) &&
-             gate_est(-d2 * rinv, vx, vy, vz, -1.0f, nj.x, nj.y, nj.z);
-    return ok ? make_float2(Tr, Ti) : make_float2(0.0f, 0.0f);
-}
 
 
 
@@ -2355,6 +2274,14 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *bloc
     const int t = threadIdx.x, b = blockIdx.x;
     if (b >= nblocks) return;  // CTA-uniform
     const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = min(cap[b], kLrRankLimit);
+    if (K <= 0) {  // CTA-uniform: an interpolated block (the interpolation kernel writes its results)
+        if (threadIdx.x == 0) {
+            rank[b] = -1;
+            fro[b] = 0.0f;
+            err[b] = -1.0f;
+        }
+        return;
+    }
     const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
     const float4 *PI = a.srcA + I * kTile, *NI = a.srcB + I * kTile, *PJ = a.srcA + J * kTile, *NJ = a.srcB + J * kTile;
     float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
@@ -2630,6 +2557,14 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
     const int ta = t, tb = t + kAca2Threads;  // this thread's two rows / columns
     if (b >= nblocks) return;  // CTA-uniform
     const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = min(cap[b], kLrRankLimit);
+    if (K <= 0) {  // CTA-uniform: an interpolated block (the interpolation kernel writes its results)
+        if (threadIdx.x == 0) {
+            rank[b] = -1;
+            fro[b] = 0.0f;
+            err[b] = -1.0f;
+        }
+        return;
+    }
     const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
     const float4 *PI = a.srcA + I * kTile, *NI = a.srcB + I * kTile, *PJ = a.srcA + J * kTile, *NJ = a.srcB + J * kTile;
     float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
@@ -2808,13 +2743,15 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
 // blocks whose error concentrates in a few rows.
 __global__ void __launch_bounds__(kTile) k_lr_audit(SumArgs a, const int2 *blocks, const uint8_t *cls,
                                                     const long long *off, const int *rank, const int *sample, int ns,
-                                                    const float2 *U, const float2 *V, float *out_err)
+                                                    const float2 *U, const float2 *V, float *out_err,
+                                                    const uint8_t *lev)
 {
     __shared__ float4 sP[kTile], sN[kTile];
     __shared__ float2 sums[kAcaWarps];
     const int t = threadIdx.x;
     if (blockIdx.x >= ns) return;
     const int b = sample[blockIdx.x], k = rank[b];
+    if (lev && lev[b]) return;  // an interpolated block (audited by the interpolation kernel)
     const int I = blocks[b].x, J = blocks[b].y, bc = cls[b];
     const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
     const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -2908,13 +2845,15 @@ __global__ void __launch_bounds__(128) k_block_desc(SumArgs a, const int2 *block
 template <int MINB>
 __global__ void __launch_bounds__(kTile, MINB) k_lr_block(SumArgs a, const int2 *blocks, const long long *off,
                                                           const int *bidx, int nb, const float2 *U, const float2 *V,
-                                                          const int *rank, float2 *brow, float2 *bcol, const int *ndev)
+                                                          const int *rank, float2 *brow, float2 *bcol, const int *ndev,
+                                                          const uint8_t *lev)
 {
     __shared__ float4 sW[kTile];  // (Re w_I, Im w_I, Re w_J, Im w_J) of every row t
     __shared__ float2 sTv[kLrMaxRank], sSu[kLrMaxRank];
     const int q = blockIdx.x;
     if (q >= (ndev ? min(*ndev, nb) : nb)) return;
     const int b = bidx[q];
+    if (lev && lev[b]) return;  // an interpolated block
     lr_block_apply<kTile, true>(a, blocks[b].x, blocks[b].y, U + off[b] * kTile, V + off[b] * kTile, rank[b],
                                 brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv, sSu);
 }
@@ -3370,10 +3309,11 @@ bool launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const 
 }
 
 void launch_lr_audit(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const long long *off, const int *rank,
-                     const int *sample, int ns, const float2 *U, const float2 *V, float *out_err, cudaStream_t s)
+                     const int *sample, int ns, const float2 *U, const float2 *V, float *out_err, cudaStream_t s,
+                     const uint8_t *lev)
 {
     if (a.ka != 0.0f) return;  // the audit evaluates entries without attenuation only
-    if (ns > 0) k_lr_audit<<<ns, kTile, 0, s>>>(a, blocks, cls, off, rank, sample, ns, U, V, out_err);
+    if (ns > 0) k_lr_audit<<<ns, kTile, 0, s>>>(a, blocks, cls, off, rank, sample, ns, U, V, out_err, lev);
 }
 
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
@@ -3386,14 +3326,20 @@ void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls,
 void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
                      const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
-                     double2 *ycol, cudaStream_t s, const int *ndev, bool outputs_ready, int lr_ctas)
+                     double2 *ycol, cudaStream_t s, const int *ndev, bool outputs_ready, int lr_ctas,
+                     const IpCtx *ip)
 {
     // latency-bound on the factor stream: resident CTAs per SM are the lever
     // (registers capped to fit lr_ctas of them)
     if (nb > 0 && !outputs_ready) {
-        if (lr_ctas >= 8) k_lr_block<8><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev);
-        else if (lr_ctas >= 6) k_lr_block<6><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev);
-        else k_lr_block<4><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev);
+        const uint8_t *lev = ip ? ip->lev : nullptr;
+        if (lr_ctas >= 8)
+            k_lr_block<8><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev, lev);
+        else if (lr_ctas >= 6)
+            k_lr_block<6><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev, lev);
+        else
+            k_lr_block<4><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev, lev);
+        if (ip) launch_ip_apply(a, ip->tile, ip->fxy, ip->lev, ip->delta, blocks, off, bidx, nb, ndev, U, brow, bcol, s);
     }
     if (ntiles > 0)
         k_lr_gather<<<ntiles, kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, bidx, yrow, ycol);

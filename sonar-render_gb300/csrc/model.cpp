@@ -104,6 +104,7 @@ struct Object {
     float4 *d_cell_pos = nullptr;
     int *d_cell_facet = nullptr;
     float4 *d_facet_n = nullptr;
+    float4 *d_facet_grid = nullptr;  // per facet (xAxis, nx), (yAxis, first cell): the interpolated blocks' tile frames
     double2 *d_P = nullptr, *d_Pin = nullptr, *d_Pout = nullptr;
     float4 *d_act_pos = nullptr;
     int *d_act_facet = nullptr, *d_act_cell = nullptr, *d_facet_end = nullptr;
@@ -111,7 +112,8 @@ struct Object {
     int nact() const { return (int)act_cell.size(); }
     void free_device()
     {
-        dfree(d_cell_pos); dfree(d_cell_facet); dfree(d_facet_n); dfree(d_P); dfree(d_Pin); dfree(d_Pout);
+        dfree(d_cell_pos); dfree(d_cell_facet); dfree(d_facet_n); dfree(d_facet_grid); dfree(d_P); dfree(d_Pin);
+        dfree(d_Pout);
         dfree(d_act_pos); dfree(d_act_facet); dfree(d_act_cell); dfree(d_facet_end);
     }
 };
@@ -177,9 +179,10 @@ struct Compression {
     int ncand = 0;              // candidate blocks before selection
     int nblocks = 0;            // blocks approximated (after selection)
     int naccepted = 0;
-    double mean_rank = 0.0, max_err = 0.0;
+    int nip = 0;                // accepted interpolated blocks
+    double mean_rank = 0.0, max_err = 0.0, ip_mean_nodes = 0.0;
     double pairs_cmp = 0.0;     // ordered pairs of the accepted blocks
-    float build_ms = 0.0f, select_ms = 0.0f, aca_ms = 0.0f;
+    float build_ms = 0.0f, select_ms = 0.0f, aca_ms = 0.0f, ip_ms = 0.0f;
     long long ncols = 0;        // factor columns reserved (sum of caps)
     int2 *d_blocks = nullptr;
     uint8_t *d_cls = nullptr;
@@ -195,6 +198,9 @@ struct Compression {
     double *d_stats = nullptr;      // accepted count, rank sum, largest judged error, ordered pairs
     float *d_desc = nullptr;        // descriptors of the candidates
     int *d_kmap = nullptr, *d_acap = nullptr;  // kept block -> candidate, rank caps
+    bool interp = false;        // interpolated blocks in this build
+    uint8_t *d_lev = nullptr;   // per kept block: 0 cross approximation, 1..3 interpolation level
+    IpCtx ip;                   // tile frames and box cells of the interpolated blocks
     bool stats_pending = false;     // statistics and timings not read back yet
     bool outputs_ready = false;     // the build also wrote the block outputs of its bounce's inputs
     // descriptors and rank labels of the approximated blocks (network training)
@@ -219,9 +225,9 @@ struct HopRecord {
     int nsplit;
     int launches;    // kernels launched by this hop, mask included
     // compressed bounce blocks (FACET_SELF with compression on)
-    int cmp_cand = 0, cmp_blocks = 0, cmp_accepted = 0, cmp_select = 0;
-    double cmp_mean_rank = 0.0, cmp_max_err = 0.0, cmp_pairs = 0.0;
-    float cmp_build_ms = 0.0f, cmp_select_ms = 0.0f, cmp_aca_ms = 0.0f, lr_ms = 0.0f;
+    int cmp_cand = 0, cmp_blocks = 0, cmp_accepted = 0, cmp_select = 0, cmp_ip_blocks = 0;
+    double cmp_mean_rank = 0.0, cmp_max_err = 0.0, cmp_pairs = 0.0, cmp_ip_nodes = 0.0;
+    float cmp_build_ms = 0.0f, cmp_select_ms = 0.0f, cmp_aca_ms = 0.0f, cmp_ip_ms = 0.0f, lr_ms = 0.0f;
 };
 
 struct Model {
@@ -242,7 +248,8 @@ struct Model {
     // runs there beside the dense remainder (FP32 / SFU-bound)
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    cudaEvent_t evb[4] = {nullptr, nullptr, nullptr, nullptr};  // compression build: start, selected, ACA end, end
+    // compression build: start, selected, cross approximation end, end, interpolation end
+    cudaEvent_t evb[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     float4 *d_src_pos = nullptr, *d_fp_pos = nullptr;
     double2 *d_src_P = nullptr, *d_fp_P = nullptr;
     // field points are kept in Morton (spatial) order on the device so that a
@@ -284,6 +291,7 @@ struct Model {
     int opt_lr_ctas = 4;        // low-rank apply: resident CTAs per SM its register cap allows (4, 6, 8)
     int opt_rel_geom = 0;       // source hop and readout: phase distances relative to FP64 references
     int opt_fused_apply = 1;    // k_aca2: apply the accepted blocks to the building bounce's inputs in the same kernel
+    int opt_cmp_interp = 1;     // far class-ALL blocks between planar tiles by directional interpolation (not with select 1)
     int opt_mask_classify = 1;  // bounce masks: warp-per-block classification, pair kernel on the listed blocks
     int opt_gate_proj = 1;      // bounce masks: gates decided from per-point projections where certain
     int opt_cross_objects = 0;  // bounces also between different targets (FACET_RESP); 0: the reference's behaviour
@@ -311,7 +319,8 @@ struct Model {
         dfree(d_blist); dfree(d_rowcnt); dfree(d_chunk_off); dfree(d_nchunks); dfree(d_chunks); dfree(d_rowpart);
         pack_cap = partial_cap = limit_cap = colpart_cap = 0;
         sym_tiles = 0;
-        for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3, &ev4, &ev5, &ev6, &ev7, &ev8, &evb[0], &evb[1], &evb[2], &evb[3]})
+        for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3, &ev4, &ev5, &ev6, &ev7, &ev8, &evb[0], &evb[1], &evb[2], &evb[3],
+                               &evb[4]})
             if (*e) {
                 cudaEventDestroy(*e);
                 *e = nullptr;
@@ -449,6 +458,16 @@ void render_object(Object &o)
     o.d_cell_pos = dalloc<float4>(nc);
     o.d_cell_facet = dalloc<int>(nc);
     o.d_facet_n = dalloc<float4>(facet_n.size());
+    std::vector<float4> facet_grid(2 * facet_n.size());
+    for (int f = 0; f < nf; f++) {
+        const FacetFrame &F = o.facets[f];
+        int nx = F.nx, c0 = (int)o.cell0[f];
+        facet_grid[2 * f] = make_float4(F.xAxis.x, F.xAxis.y, F.xAxis.z, 0.0f);
+        facet_grid[2 * f + 1] = make_float4(F.yAxis.x, F.yAxis.y, F.yAxis.z, 0.0f);
+        memcpy(&facet_grid[2 * f].w, &nx, sizeof(int));
+        memcpy(&facet_grid[2 * f + 1].w, &c0, sizeof(int));
+    }
+    o.d_facet_grid = dalloc<float4>(facet_grid.size());
     o.d_P = dalloc<double2>(nc);
     o.d_act_pos = dalloc<float4>(na);
     o.d_act_facet = dalloc<int>(na);
@@ -458,6 +477,7 @@ void render_object(Object &o)
     upload(o.d_cell_pos, cell_pos, nc, s);
     upload(o.d_cell_facet, cell_facet, nc, s);
     CK(stage_to_device(o.d_facet_n, facet_n.data(), facet_n.size() * sizeof(float4), s));
+    CK(stage_to_device(o.d_facet_grid, facet_grid.data(), facet_grid.size() * sizeof(float4), s));
     CK(cudaMemsetAsync(o.d_P, 0, std::max<size_t>(nc, 1) * sizeof(double2), s));
     if (na) {
         upload(o.d_act_pos, act_pos, na, s);
@@ -543,7 +563,7 @@ void render()
     for (double &v : g.render_ms) v = 0.0;
     CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
     for (cudaEvent_t *e : {&g.ev0, &g.ev1, &g.ev2, &g.ev3, &g.ev4, &g.ev5, &g.ev6, &g.ev7, &g.ev8, &g.evb[0], &g.evb[1],
-                           &g.evb[2], &g.evb[3]})
+                           &g.evb[2], &g.evb[3], &g.evb[4]})
         CK(cudaEventCreate(e));
     CK(cudaStreamCreateWithFlags(&g.side, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&g.ev_fork, cudaEventDisableTiming));
@@ -873,12 +893,28 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
                        9 * Arena::bytes_of(nmax, sizeof(int)) + 3 * Arena::bytes_of(nmax, sizeof(float)) +
                        Arena::bytes_of(nmax * 64, 1) + 2 * Arena::bytes_of(ngrid, 1) +
                        Arena::bytes_of(ngrid, sizeof(int)) + 2 * Arena::bytes_of(M.nsrc, sizeof(double2)) +
-                       Arena::bytes_of((size_t)4 * cmp_stats_parts(), sizeof(double)) + 8192;
+                       Arena::bytes_of((size_t)kCmpStats * cmp_stats_parts(), sizeof(double)) +
+                       Arena::bytes_of((size_t)kIpTileRec * nt, sizeof(float4)) + Arena::bytes_of(M.nsrc, sizeof(uint16_t)) +
+                       2 * Arena::bytes_of(nmax, 1) + 8192;
         C.arena.reserve(bytes);
     }
     Arena &ar = C.arena;
     float4 *d_cen = ar.take<float4>(nt), *d_nm = ar.take<float4>(nt);
     launch_tile_stats(g.d_packA, g.d_packB, M.nsrc, d_cen, d_nm, st);
+    // interpolated blocks: far class-ALL blocks between planar tiles (not
+    // when the cross approximation labels training blocks)
+    Object &A = get(OBJ_TARGET, a);
+    C.interp = g.opt_cmp_interp && select != 1;
+    C.d_lev = nullptr;
+    C.ip = IpCtx{};
+    if (C.interp) {
+        C.ip.tile = ar.take<float4>((size_t)kIpTileRec * nt);
+        uint16_t *fxy = ar.take<uint16_t>(M.nsrc);
+        launch_ip_tiles(g.d_packA, g.d_packB, A.d_act_facet, A.d_act_cell, A.d_facet_grid, M.nsrc, A.delta,
+                        const_cast<float4 *>(C.ip.tile), fxy, st);
+        C.ip.fxy = fxy;
+        C.ip.delta = A.delta;
+    }
     // ---- candidates
     int *d_ccnt = ar.take<int>(nb), *d_coff = ar.take<int>(nb + 1);
     int2 *d_cblocks = ar.take<int2>(nmax);
@@ -892,6 +928,14 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
         d_pred = ar.take<float>(nmax);
         CK(mlp_infer_dev(C.d_desc, (int)nmax, d_pred, st));  // rows past the candidate count are not read
     }
+    uint8_t *d_clev = nullptr;
+    if (C.interp) {
+        d_clev = ar.take<uint8_t>(nmax);
+        launch_ip_level(d_cblocks, d_ccls, d_coff + nb, (int)nmax, C.ip.tile, A.delta, (float)g.kr, g.opt_cmp_tol,
+                        d_clev, st);
+        C.d_lev = ar.take<uint8_t>(nmax);
+        C.ip.lev = C.d_lev;
+    }
     // ---- kept blocks, rank caps, factor columns
     int *d_kcnt = ar.take<int>(nb), *d_ksum = ar.take<int>(nb);
     int *d_koff = ar.take<int>(nb + 1), *d_kcol = ar.take<int>(nb + 1);
@@ -902,7 +946,7 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     C.d_kmap = ar.take<int>(nmax);
     const float cut = std::log2(1.0f + g.opt_cmp_rcut);
     launch_keep_lists(nb, d_coff, d_pred, cut, rmax, d_cblocks, d_ccls, d_kcnt, d_ksum, d_koff, d_kcol, C.d_blocks,
-                      C.d_cls, C.d_acap, C.d_off, C.d_kmap, st);
+                      C.d_cls, C.d_acap, C.d_off, C.d_kmap, st, d_clev, C.d_lev);
     CK(cudaEventRecord(g.evb[1], st));
     int hcnt[3] = {0, 0, 0};  // candidates, kept blocks, factor columns
     CK(cudaMemcpyAsync(&hcnt[0], d_coff + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -936,6 +980,15 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
                                  g.opt_fused_apply ? C.d_brow : nullptr, g.opt_fused_apply ? C.d_bcol : nullptr);
     CK(cudaGetLastError());
     CK(cudaEventRecord(g.evb[2], st));
+    if (C.interp) {
+        // the interpolated blocks: node entries, judge, and the fused apply
+        // when the cross approximation applies its own blocks too
+        const bool fused = C.outputs_ready;
+        launch_ip_build(s, C.ip.tile, C.ip.fxy, C.ip.lev, A.delta, C.d_blocks, C.d_off, n, g.opt_cmp_judge, C.d_U,
+                        C.d_rank, C.d_fro, C.d_err, fused ? C.d_brow : nullptr, fused ? C.d_bcol : nullptr, st);
+        CK(cudaGetLastError());
+    }
+    CK(cudaEventRecord(g.evb[4], st));
     // ---- accepted blocks: dense flags off, owner lists, statistics
     C.d_flags = ar.take<uint8_t>(ngrid);
     CK(cudaMemcpyAsync(C.d_flags, M.view.flags, ngrid, cudaMemcpyDeviceToDevice, st));
@@ -950,8 +1003,8 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     launch_accept_lists(nt, nb, d_koff, C.d_blocks, C.d_rank, C.d_flags, d_accbm, d_qidx, d_acnt, C.d_byJ_off, C.d_bidx,
                         C.d_byJ, d_icnt, C.d_byI_off, C.d_byI, st);
     C.d_nacc = C.d_byJ_off + nb;
-    C.d_stats = ar.take<double>((size_t)4 * cmp_stats_parts());
-    launch_cmp_stats(d_koff + nb, C.d_blocks, C.d_rank, C.d_err, M.nsrc, C.d_stats, st);
+    C.d_stats = ar.take<double>((size_t)kCmpStats * cmp_stats_parts());
+    launch_cmp_stats(d_koff + nb, C.d_blocks, C.d_rank, C.d_err, M.nsrc, C.d_stats, st, C.d_lev);
     C.d_yrow = ar.take<double2>(M.nsrc);
     C.d_ycol = ar.take<double2>(M.nsrc);
     CK(cudaEventRecord(g.evb[3], st));
@@ -966,22 +1019,22 @@ void finish_compression()
     Compression &C = g.cmp;
     if (!C.stats_pending) return;
     C.stats_pending = false;
-    std::vector<double> part((size_t)4 * cmp_stats_parts());
+    std::vector<double> part((size_t)kCmpStats * cmp_stats_parts());
     CK(cudaMemcpy(part.data(), C.d_stats, part.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    double st[4] = {0.0, 0.0, 0.0, 0.0};
-    for (size_t b = 0; b < part.size() / 4; b++) {
-        st[0] += part[4 * b];
-        st[1] += part[4 * b + 1];
-        st[2] = std::max(st[2], part[4 * b + 2]);
-        st[3] += part[4 * b + 3];
-    }
+    double st[kCmpStats] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (size_t b = 0; b < part.size() / kCmpStats; b++)
+        for (int q = 0; q < kCmpStats; q++)
+            st[q] = q == 2 ? std::max(st[q], part[kCmpStats * b + q]) : st[q] + part[kCmpStats * b + q];
     C.naccepted = (int)st[0];
-    C.mean_rank = st[0] > 0.0 ? st[1] / st[0] : 0.0;
+    C.nip = (int)st[4];
+    C.mean_rank = st[0] - st[4] > 0.0 ? st[1] / (st[0] - st[4]) : 0.0;  // of the cross-approximated blocks
+    C.ip_mean_nodes = st[4] > 0.0 ? st[5] / st[4] : 0.0;
     C.max_err = st[2];
     C.pairs_cmp = st[3];
     CK(cudaEventElapsedTime(&C.build_ms, g.evb[0], g.evb[3]));
     CK(cudaEventElapsedTime(&C.select_ms, g.evb[0], g.evb[1]));
     CK(cudaEventElapsedTime(&C.aca_ms, g.evb[1], g.evb[2]));
+    CK(cudaEventElapsedTime(&C.ip_ms, g.evb[2], g.evb[4]));
     C.desc.clear();
     C.label.clear();
     if (C.select == 1 && C.nblocks > 0) {
@@ -1122,7 +1175,7 @@ void run_hop(int hop, int a, int b)
                 CK(cudaEventRecord(g.ev4, lst));
                 launch_lr_apply(s, C.d_blocks, C.d_off, C.d_bidx, C.nblocks, C.d_U, C.d_V, C.d_rank, C.d_brow, C.d_bcol,
                                 M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, lst,
-                                C.d_nacc, built && C.outputs_ready, g.opt_lr_ctas);
+                                C.d_nacc, built && C.outputs_ready, g.opt_lr_ctas, C.interp ? &C.ip : nullptr);
                 CK(cudaEventRecord(g.ev5, lst));
                 if (g.opt_overlap) CK(cudaEventRecord(g.ev_join, lst));
                 yrow = C.d_yrow;
@@ -1187,9 +1240,10 @@ void run_hop(int hop, int a, int b)
     float ms = 0.0f, sum_ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
     CK(cudaEventElapsedTime(&sum_ms, g.ev2, g.ev3));
-    const int lr_launches = rec_cmp ? (built && g.cmp.outputs_ready ? 1 : 2) : 0;
+    const int lr_launches = rec_cmp ? (built && g.cmp.outputs_ready ? 1 : 2 + (g.cmp.interp ? 1 : 0)) : 0;
     const int nl = (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + (M.mask_ms > 0.0f ? 1 : 0) + lr_launches;
-    g.launches += (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + lr_launches + (rec_cmp_build > 0.0f ? 4 : 0);
+    g.launches += (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + lr_launches +
+                  (rec_cmp_build > 0.0f ? 4 + (g.cmp.interp ? 3 : 0) : 0);
     HopRecord rec{hop, pair_count(hop, a, b), M.mask_ms, sum_ms, ms, s.nsplit, nl};
     if (rec_cmp) {
         rec.cmp_cand = g.cmp.ncand;
@@ -1197,12 +1251,15 @@ void run_hop(int hop, int a, int b)
         rec.cmp_accepted = g.cmp.naccepted;
         rec.cmp_select = g.cmp.select;
         rec.cmp_mean_rank = g.cmp.mean_rank;
+        rec.cmp_ip_blocks = g.cmp.nip;
+        rec.cmp_ip_nodes = g.cmp.ip_mean_nodes;
         rec.cmp_max_err = g.cmp.max_err;
         rec.cmp_pairs = g.cmp.pairs_cmp;
         rec.cmp_build_ms = rec_cmp_build;
         if (rec_cmp_build > 0.0f) {
             rec.cmp_select_ms = g.cmp.select_ms;
             rec.cmp_aca_ms = g.cmp.aca_ms;
+            rec.cmp_ip_ms = g.cmp.ip_ms;
         }
         CK(cudaEventElapsedTime(&rec.lr_ms, g.ev4, g.ev5));
     }
@@ -1675,10 +1732,12 @@ int sonar_get_stats(char *json, int cap)
                  "%s{\"hop\": %d, \"pairs\": %lld, \"mask_ms\": %.6f, \"sum_ms\": %.6f, \"total_ms\": %.6f, "
                  "\"nsplit\": %d, \"launches\": %d, \"cmp_select\": %d, \"cmp_cand\": %d, \"cmp_blocks\": %d, "
                  "\"cmp_accepted\": %d, \"cmp_pairs\": %.0f, \"cmp_mean_rank\": %.3f, \"cmp_max_err\": %.3e, "
-                 "\"cmp_build_ms\": %.6f, \"cmp_select_ms\": %.6f, \"cmp_aca_ms\": %.6f, \"lr_ms\": %.6f}",
+                 "\"cmp_ip_blocks\": %d, \"cmp_ip_nodes\": %.3f, "
+                 "\"cmp_build_ms\": %.6f, \"cmp_select_ms\": %.6f, \"cmp_aca_ms\": %.6f, \"cmp_ip_ms\": %.6f, "
+                 "\"lr_ms\": %.6f}",
                  i ? ", " : "", r.hop, r.pairs, r.mask_ms, r.sum_ms, r.total_ms, r.nsplit, r.launches, r.cmp_select,
                  r.cmp_cand, r.cmp_blocks, r.cmp_accepted, r.cmp_pairs, r.cmp_mean_rank, r.cmp_max_err,
-                 r.cmp_build_ms, r.cmp_select_ms, r.cmp_aca_ms, r.lr_ms);
+                 r.cmp_ip_blocks, r.cmp_ip_nodes, r.cmp_build_ms, r.cmp_select_ms, r.cmp_aca_ms, r.cmp_ip_ms, r.lr_ms);
         s += buf;
     }
     snprintf(buf, sizeof(buf),
@@ -1754,6 +1813,7 @@ int sonar_set_option(const char *key, double value)
     }
     if (!strcmp(key, "relative_geometry")) { g.opt_rel_geom = value != 0.0; return 0; }
     if (!strcmp(key, "aca_fused_apply")) { g.opt_fused_apply = value != 0.0; g.cmp.release(); return 0; }
+    if (!strcmp(key, "compress_interp")) { g.opt_cmp_interp = value != 0.0; g.cmp.release(); return 0; }
     if (!strcmp(key, "aca_variant")) {
         if (value < 0 || value > 10) return -1;
         g.opt_aca_variant = (int)value;
@@ -1869,8 +1929,10 @@ int sonar_audit_compression(int nsample, unsigned seed, float *full_err, float *
         const int n = C.nblocks;
         std::vector<int> rk(n);
         std::vector<float> er(n);
+        std::vector<uint8_t> lv(n, 0);
         CK(cudaMemcpy(rk.data(), C.d_rank, n * sizeof(int), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(er.data(), C.d_err, n * sizeof(float), cudaMemcpyDeviceToHost));
+        if (C.interp) CK(cudaMemcpy(lv.data(), C.d_lev, n, cudaMemcpyDeviceToHost));
         std::vector<int> acc;
         for (int b = 0; b < n; b++)
             if (rk[b] > 0) acc.push_back(b);
@@ -1899,7 +1961,13 @@ int sonar_audit_compression(int nsample, unsigned seed, float *full_err, float *
         int *d_sample = dalloc<int>(ns);
         float *d_err = dalloc<float>(ns);
         CK(cudaMemcpyAsync(d_sample, acc.data(), ns * sizeof(int), cudaMemcpyHostToDevice, g.stream));
-        launch_lr_audit(s, C.d_blocks, C.d_cls, C.d_off, C.d_rank, d_sample, ns, C.d_U, C.d_V, d_err, g.stream);
+        // cross-approximated and interpolated blocks each by their own audit
+        // kernel (the other kind's CTAs return at once)
+        launch_lr_audit(s, C.d_blocks, C.d_cls, C.d_off, C.d_rank, d_sample, ns, C.d_U, C.d_V, d_err, g.stream,
+                        C.interp ? C.d_lev : nullptr);
+        if (C.interp)
+            launch_ip_audit(s, C.ip.tile, C.ip.fxy, C.ip.lev, C.ip.delta, C.d_blocks, C.d_off, d_sample, ns, C.d_U,
+                            d_err, g.stream);
         CK(cudaGetLastError());
         std::vector<float> fe(ns);
         CK(cudaMemcpyAsync(fe.data(), d_err, ns * sizeof(float), cudaMemcpyDeviceToHost, g.stream));

@@ -120,8 +120,16 @@ __device__ __forceinline__ int cap_of(const float *pred, int c, float cut, int r
 }
 
 // kept blocks and their caps per candidate row J
+// factor columns a kept block reserves: its rank cap, or an interpolated
+// block's node entries
+__device__ __forceinline__ int cols_of(const uint8_t *clev, int c, int cap)
+{
+    const int L = clev ? clev[c] : 0;
+    return L ? ip_columns(L) : cap;
+}
+
 __global__ void __launch_bounds__(kSelThreads) k_keep_count(const int *coff, const float *pred, float cut, int rmax,
-                                                            int *kcnt, int *ksum)
+                                                            const uint8_t *clev, int *kcnt, int *ksum)
 {
     __shared__ int sw[kSelThreads / 32];
     const int J = blockIdx.x, c0 = coff[J], c1 = coff[J + 1];
@@ -131,7 +139,7 @@ __global__ void __launch_bounds__(kSelThreads) k_keep_count(const int *coff, con
         const int cap = cap_of(pred, c, cut, rmax, keep);
         if (keep) {
             k += 1;
-            s += cap;
+            s += cols_of(clev, c, cap);
         }
     }
     int tk, ts;
@@ -145,8 +153,9 @@ __global__ void __launch_bounds__(kSelThreads) k_keep_count(const int *coff, con
 
 __global__ void __launch_bounds__(kSelThreads) k_keep_fill(const int *coff, const float *pred, float cut, int rmax,
                                                            const int2 *cblocks, const uint8_t *ccls,
-                                                           const int *koff, const int *kcoloff, int2 *ab,
-                                                           uint8_t *acls, int *acap, long long *aoff, int *kmap)
+                                                           const uint8_t *clev, const int *koff, const int *kcoloff,
+                                                           int2 *ab, uint8_t *acls, int *acap, long long *aoff,
+                                                           int *kmap, uint8_t *alev)
 {
     __shared__ int sw[kSelThreads / 32];
     const int J = blockIdx.x, c0 = coff[J], c1 = coff[J + 1];
@@ -154,18 +163,23 @@ __global__ void __launch_bounds__(kSelThreads) k_keep_fill(const int *coff, cons
     for (int i0 = c0; i0 < c1; i0 += kSelThreads) {
         const int c = i0 + threadIdx.x;
         bool keep = false;
-        int cap = 0;
-        if (c < c1) cap = cap_of(pred, c, cut, rmax, keep);
+        int cap = 0, cols = 0;
+        if (c < c1) {
+            cap = cap_of(pred, c, cut, rmax, keep);
+            cols = cols_of(clev, c, cap);
+        }
         int tk, tc;
         const int pk = block_scan(keep ? 1 : 0, tk, sw);
-        const int pc = block_scan(keep ? cap : 0, tc, sw);
+        const int pc = block_scan(keep ? cols : 0, tc, sw);
         if (keep) {
             const int k = kbase + pk;
+            const int L = clev ? clev[c] : 0;
             ab[k] = cblocks[c];
             acls[k] = ccls[c];
-            acap[k] = cap;
+            acap[k] = L ? 0 : cap;  // interpolated blocks: no cross approximation
             aoff[k] = (long long)(cbase + pc);
             kmap[k] = c;
+            if (alev) alev[k] = (uint8_t)L;
         }
         kbase += tk;
         cbase += tc;
@@ -244,42 +258,45 @@ __global__ void __launch_bounds__(kSelThreads) k_byI_fill(const uint8_t *accbm, 
     }
 }
 
-// statistics of the accepted blocks: count, rank sum, largest judged error,
-// ordered pairs; one partial per CTA (grid-stride over the kept blocks), the
-// host adds the partials in order
+// statistics of the accepted blocks: count, rank sum of the cross-
+// approximated ones, largest judged error, ordered pairs, interpolated
+// blocks and their node sum; one partial per CTA (grid-stride over the kept
+// blocks), the host adds the partials in order
 constexpr int kStatCtas = 128;
 
 __global__ void __launch_bounds__(kSelThreads) k_cmp_stats(const int *nkeep, const int2 *ab, const int *rank,
-                                                           const float *err, int nsrc, double *part)
+                                                           const float *err, int nsrc, const uint8_t *lev,
+                                                           double *part)
 {
-    __shared__ double sd[4][kSelThreads];
+    __shared__ double sd[kCmpStats][kSelThreads];
     const int n = *nkeep;
-    double na = 0.0, rs = 0.0, pairs = 0.0, emax = 0.0;
+    double v[kCmpStats] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int k = blockIdx.x * kSelThreads + threadIdx.x; k < n; k += gridDim.x * kSelThreads) {
         const int r = rank[k];
         if (r > 0) {
-            na += 1.0;
-            rs += r;
-            emax = fmax(emax, (double)err[k]);
+            const bool ip = lev && lev[k];
+            v[0] += 1.0;
+            v[1] += ip ? 0.0 : (double)r;
+            v[2] = fmax(v[2], (double)err[k]);
             const double ni = min(kTile, nsrc - ab[k].x * kTile), nj = min(kTile, nsrc - ab[k].y * kTile);
-            pairs += 2.0 * ni * nj;
+            v[3] += 2.0 * ni * nj;
+            v[4] += ip ? 1.0 : 0.0;
+            v[5] += ip ? (double)r : 0.0;
         }
     }
-    sd[0][threadIdx.x] = na;
-    sd[1][threadIdx.x] = rs;
-    sd[2][threadIdx.x] = emax;
-    sd[3][threadIdx.x] = pairs;
+#pragma unroll
+    for (int q = 0; q < kCmpStats; ++q) sd[q][threadIdx.x] = v[q];
     __syncthreads();
     for (int s = kSelThreads / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) {
-            sd[0][threadIdx.x] += sd[0][threadIdx.x + s];
-            sd[1][threadIdx.x] += sd[1][threadIdx.x + s];
-            sd[2][threadIdx.x] = fmax(sd[2][threadIdx.x], sd[2][threadIdx.x + s]);
-            sd[3][threadIdx.x] += sd[3][threadIdx.x + s];
+#pragma unroll
+            for (int q = 0; q < kCmpStats; ++q)
+                sd[q][threadIdx.x] = q == 2 ? fmax(sd[q][threadIdx.x], sd[q][threadIdx.x + s])
+                                            : sd[q][threadIdx.x] + sd[q][threadIdx.x + s];
         }
         __syncthreads();
     }
-    if (threadIdx.x < 4) part[blockIdx.x * 4 + threadIdx.x] = sd[threadIdx.x][0];
+    if (threadIdx.x < kCmpStats) part[blockIdx.x * kCmpStats + threadIdx.x] = sd[threadIdx.x][0];
 }
 
 }  // namespace
@@ -295,14 +312,14 @@ void launch_cand_lists(const uint8_t *flags, int nt, int nb, int select, float e
 
 void launch_keep_lists(int nb, const int *coff, const float *pred, float cut, int rmax, const int2 *cblocks,
                        const uint8_t *ccls, int *kcnt, int *ksum, int *koff, int *kcoloff, int2 *ab, uint8_t *acls,
-                       int *acap, long long *aoff, int *kmap, cudaStream_t s)
+                       int *acap, long long *aoff, int *kmap, cudaStream_t s, const uint8_t *clev, uint8_t *alev)
 {
     if (nb <= 0) return;
-    k_keep_count<<<nb, kSelThreads, 0, s>>>(coff, pred, cut, rmax, kcnt, ksum);
+    k_keep_count<<<nb, kSelThreads, 0, s>>>(coff, pred, cut, rmax, clev, kcnt, ksum);
     k_scan<<<1, kSelThreads, 0, s>>>(kcnt, nb, koff);
     k_scan<<<1, kSelThreads, 0, s>>>(ksum, nb, kcoloff);
-    k_keep_fill<<<nb, kSelThreads, 0, s>>>(coff, pred, cut, rmax, cblocks, ccls, koff, kcoloff, ab, acls, acap, aoff,
-                                           kmap);
+    k_keep_fill<<<nb, kSelThreads, 0, s>>>(coff, pred, cut, rmax, cblocks, ccls, clev, koff, kcoloff, ab, acls, acap,
+                                           aoff, kmap, alev);
 }
 
 void launch_accept_lists(int nt, int nb, const int *koff, const int2 *ab, const int *rank, uint8_t *flags_out,
@@ -324,9 +341,9 @@ void launch_accept_lists(int nt, int nb, const int *koff, const int2 *ab, const 
 int cmp_stats_parts() { return kStatCtas; }
 
 void launch_cmp_stats(const int *nkeep, const int2 *ab, const int *rank, const float *err, int nsrc, double *out,
-                      cudaStream_t s)
+                      cudaStream_t s, const uint8_t *lev)
 {
-    k_cmp_stats<<<kStatCtas, kSelThreads, 0, s>>>(nkeep, ab, rank, err, nsrc, out);
+    k_cmp_stats<<<kStatCtas, kSelThreads, 0, s>>>(nkeep, ab, rank, err, nsrc, lev, out);
 }
 
 }  // namespace sonar

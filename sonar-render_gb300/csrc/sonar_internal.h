@@ -167,28 +167,77 @@ bool launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const 
                 cudaStream_t s, int variant = 0, float2 *brow = nullptr, float2 *bcol = nullptr);
 // Full-tile relative RMS error of the sampled accepted blocks (no attenuation)
 void launch_lr_audit(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const long long *off, const int *rank,
-                     const int *sample, int ns, const float2 *U, const float2 *V, float *out_err, cudaStream_t s);
+                     const int *sample, int ns, const float2 *U, const float2 *V, float *out_err, cudaStream_t s,
+                     const uint8_t *lev = nullptr);
 // ndev (optional): the block count in device memory; nblocks / nb bound the grid
 void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls, int nblocks, const float4 *cen,
                        const float4 *nm, float inv_lambda, float *X, cudaStream_t s, const int *ndev = nullptr);
+// interp.cu: directional interpolation of far blocks of class ALL between
+// planar tiles.  Per tile a frame (4 float4: box centre and capability, the
+// facet's grid axes, normal and box size), per fragment its cell in the box;
+// per kept block a level (0: cross approximation; 1..3: nodes (6, 4), (7, 5),
+// (8, 6) of the oscillatory part, 4 x 3 of the smooth part), whose node
+// entries take ip_columns(level) columns of the U array.
+__host__ __device__ constexpr int ip_nodes(int level)
+{
+    return level == 1 ? 24 : level == 2 ? 35 : level == 3 ? 48 : 0;
+}
+__host__ __device__ constexpr int ip_columns(int level)
+{
+    // C with rows of odd pitch (P | 1), then the smooth part's 12 x 13
+    return level >= 1 && level <= 3 ? (ip_nodes(level) * (ip_nodes(level) | 1) + 156 + kTile - 1) / kTile : 0;
+}
+constexpr int kIpTileRec = 6;  // float4 per tile record
+struct IpCtx {
+    const float4 *tile = nullptr;
+    const uint16_t *fxy = nullptr;
+    const uint8_t *lev = nullptr;
+    float delta = 0.0f;
+};
+// facet_grid: per facet (xAxis, nx as int bits), (yAxis, first cell as int bits)
+void launch_ip_tiles(const float4 *pos, const float4 *nrm, const int *act_facet, const int *act_cell,
+                     const float4 *facet_grid, int n, float delta, float4 *tile, uint16_t *fxy, cudaStream_t s);
+// levels of the candidates (ncand: their count on the device, nmax bounds the grid)
+void launch_ip_level(const int2 *cb, const uint8_t *ccls, const int *ncand, int nmax, const float4 *tile,
+                     float delta, float kr, float tol, uint8_t *lev, cudaStream_t s);
+// node entries, judge (rank = node count or -1) and, given brow, the apply to
+// the packed inputs; kept blocks of level 0 are left alone
+void launch_ip_build(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,
+                     const int2 *blocks, const long long *off, int n, float limit, float2 *store, int *rank,
+                     float *fro, float *err, float2 *brow, float2 *bcol, cudaStream_t s);
+void launch_ip_apply(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,
+                     const int2 *blocks, const long long *off, const int *bidx, int nb, const int *ndev,
+                     const float2 *store, float2 *brow, float2 *bcol, cudaStream_t s);
+// full-tile relative RMS error of sampled accepted interpolated blocks (no attenuation)
+void launch_ip_audit(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,
+                     const int2 *blocks, const long long *off, const int *sample, int ns, const float2 *store,
+                     float *out_err, cudaStream_t s);
+// Low-rank apply of the accepted blocks (factors by k_lr_block, interpolated
+// blocks by the interpolation kernel when ip is given) and the per-tile gather.
 void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off, const int *bidx, int nb,
                      const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
                      double2 *ycol, cudaStream_t s, const int *ndev = nullptr, bool outputs_ready = false,
-                     int lr_ctas = 4);
+                     int lr_ctas = 4, const IpCtx *ip = nullptr);
 // select.cu: block lists of the compressed bounce, built on the device
 void launch_cand_lists(const uint8_t *flags, int nt, int nb, int select, float eta, const float4 *cen, int *cnt,
                        int *off, int2 *blocks, uint8_t *cls, cudaStream_t s);
+// clev (optional): candidate levels; an interpolated block reserves
+// ip_columns(level) factor columns and gets rank cap 0 (alev: kept levels)
 void launch_keep_lists(int nb, const int *coff, const float *pred, float cut, int rmax, const int2 *cblocks,
                        const uint8_t *ccls, int *kcnt, int *ksum, int *koff, int *kcoloff, int2 *ab, uint8_t *acls,
-                       int *acap, long long *aoff, int *kmap, cudaStream_t s);
+                       int *acap, long long *aoff, int *kmap, cudaStream_t s, const uint8_t *clev = nullptr,
+                       uint8_t *alev = nullptr);
 void launch_accept_lists(int nt, int nb, const int *koff, const int2 *ab, const int *rank, uint8_t *flags_out,
                          uint8_t *accbm, int *qidx, int *acnt, int *byJ_off, int *bidx, int *byJ, int *icnt,
                          int *byI_off, int *byI, cudaStream_t s);
-// out: cmp_stats_parts() x 4 doubles (accepted, rank sum, largest error, ordered pairs) to add in order
+// out: cmp_stats_parts() x kCmpStats doubles (accepted, rank sum of the
+// cross-approximated ones, largest error, ordered pairs, interpolated blocks
+// accepted, their node sum) to add in order
+constexpr int kCmpStats = 6;
 int cmp_stats_parts();
 void launch_cmp_stats(const int *nkeep, const int2 *ab, const int *rank, const float *err, int nsrc, double *out,
-                      cudaStream_t s);
+                      cudaStream_t s, const uint8_t *lev = nullptr);
 void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s);
 // mlp.cu: the admissibility network (8 -> 128 -> 128 -> 128 -> 1, ReLU, FP32)
 size_t mlp_param_count();
