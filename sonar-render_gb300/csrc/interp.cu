@@ -40,7 +40,7 @@ constexpr int kIpSmooth = kIpSx * kIpSy;
 constexpr int kIpMaxNodes = 48;                // px * py at the highest level
 constexpr int kIpCPitch = 49;                  // largest row pitch of C (odd: no bank conflicts)
 constexpr int kIpSPitch = 13;
-constexpr int kIpSamples = 8;                  // judged rows and columns
+constexpr int kIpCols = 8, kIpRows = 8;        // judged columns of I and rows of J (64 entries)
 
 // Chebyshev points of the first kind cos((2a + 1) pi / (2p)) and the inverse
 // denominators 1 / prod_{b != a} (x_a - x_b) of their Lagrange polynomials,
@@ -208,9 +208,9 @@ __global__ void __launch_bounds__(kTile) k_ip_tiles(const float4 *pos, const flo
 // lengths apart): the interpolation level from kappa = k (W_I^2 + W_J^2) / D,
 // the phase curvature of the plane-wave remainder over the boxes (W: the
 // longer box side); 0 leaves the block to the cross approximation.  The
-// limits hold the relative error to tol (5e-4 at kscale 1) on the blocks of
-// a 60 kHz trihedral; kscale = (tol / 5e-4)^(1 / 4.3) follows the error's
-// decay with kappa.
+// limits hold the relative error of 97 % of the blocks of a 60 kHz trihedral
+// to 2 tol (tol = 5e-4 at kscale 1; the judge accepts up to 3 tol); kscale =
+// (tol / 5e-4)^(1 / 4.3) follows the error's growth with kappa.
 __global__ void k_ip_level(const int2 *cb, const uint8_t *ccls, const int *ncand, const float4 *tile, float delta,
                            float kr, float kscale, uint8_t *lev)
 {
@@ -226,7 +226,7 @@ __global__ void k_ip_level(const int2 *cb, const uint8_t *ccls, const int *ncand
             const float wa = delta * (float)max(A.bx, A.by), wb = delta * (float)max(B.bx, B.by);
             if (D >= 2.0f * fmaxf(wa, wb)) {
                 const float kap = kr * (wa * wa + wb * wb) / D;
-                L = kap <= 5.0f * kscale ? 1 : kap <= 12.0f * kscale ? 2 : kap <= 17.0f * kscale ? 3 : 0;
+                L = kap <= 6.0f * kscale ? 1 : kap <= 14.0f * kscale ? 2 : kap <= 20.0f * kscale ? 3 : 0;
             }
         }
     }
@@ -247,10 +247,11 @@ struct __align__(16) IpShared {
     float2 ys[2][kIpSx][kYvPitch];
     float2 g[2][kIpMaxNodes], gs[2][kIpSmooth];  // node values of the weights (I, J)
     float2 h[2][kIpMaxNodes], hs[2][kIpSmooth];  // coupled node values (into I, into J)
-    float2 c[kIpMaxNodes * kIpCPitch];     // C[b][a], b: node of J, a: node of I
-    float2 cs[kIpSmooth * kIpSPitch];
+    __align__(16) float2 c[kIpMaxNodes * kIpCPitch];  // C[b][a], b: node of J, a: node of I
+    __align__(16) float2 cs[kIpSmooth * kIpSPitch];
     float red[2][2];
-    int si[kIpSamples], sj[kIpSamples];
+    float2 eD;  // e^{i k D}
+    int si[kIpCols], sj[kIpRows];
 };
 static_assert(sizeof(IpShared) <= 48 * 1024, "static shared memory");
 // scratch in the weight grids: the node offset tables ((2 x 48 + 2 x 12)
@@ -259,21 +260,19 @@ constexpr int kIpNodeTab = 0;
 static_assert((2 * kIpMaxNodes + 2 * kIpSmooth) * (int)sizeof(float4) <=
                   (int)sizeof(float2) * 2 * kIpMaxBY * (kIpMaxBX + 1),
               "node tables in the weight grids");
-static_assert((kIpSamples * kIpCPitch + (kIpMaxNodes + kIpSmooth) * kIpSamples) * (int)sizeof(float2) +
-                      kIpSamples * kIpSmooth * (int)sizeof(float) <=
+static_assert((kIpCols * kIpCPitch + (kIpMaxNodes + kIpSmooth) * kIpCols) * (int)sizeof(float2) +
+                      kIpCols * kIpSmooth * (int)sizeof(float) <=
                   (int)sizeof(float2) * 2 * kIpMaxBY * (kIpMaxBX + 1),
               "judge scratch in the weight grids");
 
 using IpArgs = IpCtx;
 
-// Geometry of one block: tiles, levels, centre distance and direction,
-// e^{i k D} (the phase reduced in turns with the split k / (2 pi)).
+// Geometry of one block: tiles, levels, centre distance and direction.
 struct IpBlock {
     IpTile TI, TJ;
     int I, J, px, py, P, ni, nj;
     float D;
     float3 u;
-    float2 eD;
 };
 
 __device__ __forceinline__ IpBlock ip_block(const SumArgs &a, const IpArgs &ip, const int2 *blocks, int b, int L)
@@ -292,11 +291,18 @@ __device__ __forceinline__ IpBlock ip_block(const SumArgs &a, const IpArgs &ip, 
     B.D = sqrtf(dx * dx + dy * dy + dz * dz);
     const float Dinv = 1.0f / B.D;
     B.u = make_float3(dx * Dinv, dy * Dinv, dz * Dinv);
-    const float th = __fmul_rn(B.D, a.k2hi);
-    const float tl = fmaf(B.D, a.k2lo, fmaf(B.D, a.k2hi, -th));
-    const float fr = (th - rintf(th)) + tl;
-    sincospif(2.0f * fr, &B.eD.y, &B.eD.x);
     return B;
+}
+
+// e^{i k D}, the phase reduced in turns with the split k / (2 pi)
+__device__ __forceinline__ float2 ip_phase_D(const SumArgs &a, float D)
+{
+    const float th = __fmul_rn(D, a.k2hi);
+    const float tl = fmaf(D, a.k2lo, fmaf(D, a.k2hi, -th));
+    const float fr = (th - rintf(th)) + tl;
+    float2 e;
+    sincospif(2.0f * fr, &e.y, &e.x);
+    return e;
 }
 
 // e^{2 pi i turns} for a phase of a few hundred turns at most: the whole
@@ -350,7 +356,10 @@ __device__ __forceinline__ void ip_tables(IpShared &S, const SumArgs &a, const I
         lagrange_all(kIpSx, sig, l);
 #pragma unroll
         for (int q = 0; q < kIpSx; ++q) S.ss[s][x][q] = x < bx ? l[q] : 0.0f;
-    } else if (t < 192) {
+    } else if (t == kIpThreads - 1) {
+        S.eD = ip_phase_D(a, B.D);
+    }
+    if (t >= 160 && t < 192) {
         const int s = (t - 160) >> 4, y = (t - 160) & 15, by = s ? B.TJ.by : B.TI.by;
         const float hc = 0.5f * (float)(by - 1), sig = ((float)y - hc) / hc;
         float l[kIpMaxP];
@@ -363,11 +372,16 @@ __device__ __forceinline__ void ip_tables(IpShared &S, const SumArgs &a, const I
 // Node entries are stored as in shared memory: C with the odd row pitch
 // P | 1 (rows and columns both read without bank conflicts), then the smooth
 // part's 12 x 13; the apply copies them linearly.
+__device__ __forceinline__ int ip_smooth_at(int P) { return (P * (P | 1) + 1) & ~1; }
+
 __device__ __forceinline__ void ip_load_entries(IpShared &S, const float2 *cst, int P)
 {
-    const int nc = P * (P | 1);
-    for (int e = threadIdx.x; e < nc; e += kIpThreads) S.c[e] = __ldg(cst + e);
-    for (int e = threadIdx.x; e < kIpSmooth * kIpSPitch; e += kIpThreads) S.cs[e] = __ldg(cst + nc + e);
+    // 16-byte copies: both parts start on even entries of a 2 KB aligned column
+    const int n4 = ip_smooth_at(P) >> 1;
+    const float4 *src = reinterpret_cast<const float4 *>(cst);
+    float4 *dc = reinterpret_cast<float4 *>(S.c), *ds = reinterpret_cast<float4 *>(S.cs);
+    for (int e = threadIdx.x; e < n4; e += kIpThreads) dc[e] = __ldg(src + e);
+    for (int e = threadIdx.x; e < kIpSmooth * kIpSPitch / 2; e += kIpThreads) ds[e] = __ldg(src + n4 + e);
 }
 
 // One CTA of 256 threads per block.  BUILD: kept block blockIdx.x -- node
@@ -378,16 +392,19 @@ template <bool ATT, bool BUILD>
 __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const int2 *blocks, const long long *off,
                                                    const int *bidx, const int *ndev, int n, float limit,
                                                    float2 *store, int *rank, float *fro, float *err, float2 *brow,
-                                                   float2 *bcol)
+                                                   float2 *bcol, const int *list)
 {
     __shared__ IpShared S;
     const int t = threadIdx.x;
     int b;
-    if (BUILD) {
+    if ((int)blockIdx.x >= n) return;
+    if (list) {
+        b = list[blockIdx.x];  // an interpolated kept block
+        if (!BUILD && rank[b] <= 0) return;  // rejected by the judge: dense
+    } else if (BUILD) {
         b = blockIdx.x;
-        if (b >= n) return;
     } else {
-        if ((int)blockIdx.x >= (ndev ? min(*ndev, n) : n)) return;
+        if (ndev && (int)blockIdx.x >= *ndev) return;
         b = bidx[blockIdx.x];
     }
     const int L = ip.lev[b];
@@ -397,7 +414,6 @@ __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const i
     const int I = B.I, J = B.J, px = B.px, py = B.py, P = B.P, ni = B.ni, nj = B.nj;
     const float D = B.D, delta = ip.delta;
     const float3 u = B.u;
-    const float2 eD = B.eD;
     float2 *cst = store + (size_t)off[b] * kTile;
     ip_tables(S, a, B, delta);
     // ---- node entries: evaluated (BUILD) or read back
@@ -422,20 +438,20 @@ __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const i
                 (smooth ? (side ? mJ : mI) : (side ? nJ : nI))[q] = o;
             }
         }
-        if (t < 2 * kIpSamples) {
-            // judged columns of I and rows of J: one per 32-fragment band
-            const int q = t & (kIpSamples - 1);
+        if (t < kIpCols + kIpRows) {
+            // judged columns of I and rows of J, one per 32-fragment band
+            const bool col = t < kIpCols;
+            const int q = col ? t : t - kIpCols, band = col ? kTile / kIpCols : kTile / kIpRows;
             unsigned hsh = (unsigned)b * 2654435761u + (unsigned)t * 40503u + 977u;
             hsh ^= hsh >> 13;
             hsh *= 0x5bd1e995u;
             hsh ^= hsh >> 15;
-            const int m = t < kIpSamples ? ni : nj;
-            const int idx = min(m - 1, 32 * q + (int)(hsh & 31u));
-            if (t < kIpSamples) S.si[q] = idx; else S.sj[q] = idx;
+            const int idx = min((col ? ni : nj) - 1, band * q + (int)(hsh % (unsigned)band));
+            if (col) S.si[q] = idx; else S.sj[q] = idx;
         }
         __syncthreads();
         const float invP = 1.0f / (float)P;
-        const int cp = P | 1, nc = P * cp;
+        const int cp = P | 1, nc = ip_smooth_at(P);
         if (cp != P && t < P) {  // the pad column, zero in the store too
             S.c[t * cp + P] = make_float2(0.0f, 0.0f);
             cst[t * cp + P] = make_float2(0.0f, 0.0f);
@@ -492,10 +508,10 @@ __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const i
         // (oscillatory rows of pitch 49, smooth rows of 12), then
         // W = C L_I(samples), Ws = Cs Ls_I(samples)
         float2 *LIq = &S.zg[0][0][0];                      // [sample][node of I]
-        float2 *W = LIq + kIpSamples * kIpCPitch;          // [node of J][sample]
-        float2 *Ws = W + kIpMaxNodes * kIpSamples;         // [smooth node of J][sample]
-        float *LsIq = reinterpret_cast<float *>(Ws + kIpSmooth * kIpSamples);  // [sample][smooth node of I]
-        for (int e = t; e < kIpSamples * (P + kIpSmooth); e += kIpThreads) {
+        float2 *W = LIq + kIpCols * kIpCPitch;             // [node of J][sample]
+        float2 *Ws = W + kIpMaxNodes * kIpCols;            // [smooth node of J][sample]
+        float *LsIq = reinterpret_cast<float *>(Ws + kIpSmooth * kIpCols);  // [sample][smooth node of I]
+        for (int e = t; e < kIpCols * (P + kIpSmooth); e += kIpThreads) {
             const int q = e / (P + kIpSmooth), ai = e - q * (P + kIpSmooth), xy = ip.fxy[I * kTile + S.si[q]];
             if (ai < P) {
                 const int aix = ai / py;
@@ -506,8 +522,8 @@ __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const i
             }
         }
         __syncthreads();
-        for (int e = t; e < (P + kIpSmooth) * kIpSamples; e += kIpThreads) {
-            const int bj = e / kIpSamples, q = e - bj * kIpSamples;
+        for (int e = t; e < (P + kIpSmooth) * kIpCols; e += kIpThreads) {
+            const int bj = e / kIpCols, q = e - bj * kIpCols;
             float2 acc0 = make_float2(0.0f, 0.0f), acc1 = acc0;
             if (bj < P) {
                 const float2 *cr = S.c + bj * (P | 1), *lq = LIq + q * kIpCPitch;
@@ -518,32 +534,32 @@ __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const i
                     acc1 = cfma(cr[ai + 1], lq[ai + 1], acc1);
                 }
                 if (ai < P) acc0 = cfma(cr[ai], lq[ai], acc0);
-                W[bj * kIpSamples + q] = make_float2(acc0.x + acc1.x, acc0.y + acc1.y);
+                W[bj * kIpCols + q] = make_float2(acc0.x + acc1.x, acc0.y + acc1.y);
             } else {
                 const float2 *cr = S.cs + (bj - P) * kIpSPitch;
                 const float *lq = LsIq + q * kIpSmooth;
 #pragma unroll
                 for (int ai = 0; ai < kIpSmooth; ++ai) acc0 = rfma(lq[ai], cr[ai], acc0);
-                Ws[(bj - P) * kIpSamples + q] = acc0;
+                Ws[(bj - P) * kIpCols + q] = acc0;
             }
         }
         __syncthreads();
         float e2 = 0.0f, x2 = 0.0f;
-        if (t < kIpSamples * kIpSamples) {
-            const int qj = t / kIpSamples, qi = t - qj * kIpSamples;
+        if (t < kIpRows * kIpCols) {
+            const int qj = t / kIpCols, qi = t - qj * kIpCols;
             const int i = I * kTile + S.si[qi], j = J * kTile + S.sj[qj];
             const int xyj = ip.fxy[j], xj = xyj & 255, yj = xyj >> 8;
             float2 ap = make_float2(0.0f, 0.0f);
             for (int bjx = 0; bjx < px; ++bjx) {
                 float2 in = make_float2(0.0f, 0.0f);
                 for (int bjy = 0; bjy < py; ++bjy)
-                    in = cfma(S.lt[1][yj][bjy], W[(bjx * py + bjy) * kIpSamples + qi], in);
+                    in = cfma(S.lt[1][yj][bjy], W[(bjx * py + bjy) * kIpCols + qi], in);
                 ap = cfma(S.ls[1][xj][bjx], in, ap);
             }
-            ap = cmul(ap, eD);
+            ap = cmul(ap, S.eD);
 #pragma unroll
             for (int bj = 0; bj < kIpSmooth; ++bj)
-                ap = rfma(S.ss[1][xj][bj / kIpSy] * S.st[1][yj][bj % kIpSy], Ws[bj * kIpSamples + qi], ap);
+                ap = rfma(S.ss[1][xj][bj / kIpSy] * S.st[1][yj][bj % kIpSy], Ws[bj * kIpCols + qi], ap);
             const float2 ex = lr_entry<ATT>(a, kFlagAll, true, a.srcA[i], a.srcB[i], a.srcA[j], a.srcB[j]);
             e2 = (ex.x - ap.x) * (ex.x - ap.x) + (ex.y - ap.y) * (ex.y - ap.y);
             x2 = ex.x * ex.x + ex.y * ex.y;
@@ -565,14 +581,15 @@ __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const i
         const bool accepted = sx > 0.0f && rel <= limit;
         if (t == 0) {
             rank[b] = accepted ? P : -1;
-            fro[b] = sqrtf(sx * (float)(ni * nj) / (float)(kIpSamples * kIpSamples));
+            fro[b] = sqrtf(sx * (float)(ni * nj) / (float)(kIpRows * kIpCols));
             err[b] = rel;
         }
         if (!accepted || !brow) return;  // CTA-uniform
         __syncthreads();                  // the scratch becomes the weight grids
     }
     // ---- the apply: weights onto the box grids (zero where the box has no fragment)
-    for (int e = t; e < 2 * kIpMaxBY * (kIpMaxBX + 1); e += kIpThreads) (&S.zg[0][0][0])[e] = make_float2(0.0f, 0.0f);
+    for (int e = t; e < kIpMaxBY * (kIpMaxBX + 1); e += kIpThreads)
+        reinterpret_cast<float4 *>(&S.zg[0][0][0])[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     __syncthreads();
     if (t < ni) {
         const int i = I * kTile + t, xy = ip.fxy[i];
@@ -647,7 +664,7 @@ __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const i
         }
         acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 1);
         acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 1);
-        if (bj < P && h0 == 0) S.h[1][bj] = cmul(acc, eD);
+        if (bj < P && h0 == 0) S.h[1][bj] = cmul(acc, S.eD);
     } else if (t >= 128 && t < 128 + 2 * kIpMaxNodes) {
         const int ai = (t - 128) >> 1, h0 = t & 1;
         float2 acc = make_float2(0.0f, 0.0f);
@@ -657,7 +674,7 @@ __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const i
         }
         acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 1);
         acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 1);
-        if (ai < P && h0 == 0) S.h[0][ai] = cmul(acc, eD);
+        if (ai < P && h0 == 0) S.h[0][ai] = cmul(acc, S.eD);
     } else if (t >= 96 && t < 96 + kIpSmooth) {
         const int bj = t - 96;
         float2 acc = make_float2(0.0f, 0.0f);
@@ -746,7 +763,7 @@ __global__ void __launch_bounds__(kIpThreads) k_ip_audit(SumArgs a, IpArgs ip, c
                     const int bjx = bj / B.py;
                     acc = cfma(cmul(S.ls[1][xj][bjx], S.lt[1][yj][bj - bjx * B.py]), S.c[bj * (B.P | 1) + t], acc);
                 }
-                v[t] = cmul(acc, B.eD);
+                v[t] = cmul(acc, S.eD);
             } else if (t >= 64 && t < 64 + kIpSmooth) {
                 const int ai = t - 64;
                 float2 acc = make_float2(0.0f, 0.0f);
@@ -808,7 +825,7 @@ void launch_ip_level(const int2 *cb, const uint8_t *ccls, const int *ncand, int 
 
 void launch_ip_build(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,
                      const int2 *blocks, const long long *off, int n, float limit, float2 *store, int *rank,
-                     float *fro, float *err, float2 *brow, float2 *bcol, cudaStream_t s)
+                     float *fro, float *err, float2 *brow, float2 *bcol, cudaStream_t s, const int *list)
 {
     if (n <= 0) return;
     IpArgs ip;
@@ -818,16 +835,21 @@ void launch_ip_build(const SumArgs &a, const float4 *tile, const uint16_t *fxy, 
     ip.delta = delta;
     if (a.ka != 0.0f)
         k_ip<true, true><<<n, kIpThreads, 0, s>>>(a, ip, blocks, off, nullptr, nullptr, n, limit, store, rank, fro, err,
-                                                   brow, bcol);
+                                                   brow, bcol, list);
     else
         k_ip<false, true><<<n, kIpThreads, 0, s>>>(a, ip, blocks, off, nullptr, nullptr, n, limit, store, rank, fro,
-                                                    err, brow, bcol);
+                                                    err, brow, bcol, list);
 }
 
 void launch_ip_apply(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,
                      const int2 *blocks, const long long *off, const int *bidx, int nb, const int *ndev,
-                     const float2 *store, float2 *brow, float2 *bcol, cudaStream_t s)
+                     const float2 *store, float2 *brow, float2 *bcol, cudaStream_t s, const int *list, int nlist,
+                     const int *rank)
 {
+    if (list) {
+        nb = nlist;
+        ndev = nullptr;
+    }
     if (nb <= 0) return;
     IpArgs ip;
     ip.tile = tile;
@@ -836,11 +858,11 @@ void launch_ip_apply(const SumArgs &a, const float4 *tile, const uint16_t *fxy, 
     ip.delta = delta;
     float2 *st = const_cast<float2 *>(store);  // read only in the apply
     if (a.ka != 0.0f)
-        k_ip<true, false><<<nb, kIpThreads, 0, s>>>(a, ip, blocks, off, bidx, ndev, nb, 0.0f, st, nullptr, nullptr,
-                                                     nullptr, brow, bcol);
+        k_ip<true, false><<<nb, kIpThreads, 0, s>>>(a, ip, blocks, off, bidx, ndev, nb, 0.0f, st,
+                                                     const_cast<int *>(rank), nullptr, nullptr, brow, bcol, list);
     else
-        k_ip<false, false><<<nb, kIpThreads, 0, s>>>(a, ip, blocks, off, bidx, ndev, nb, 0.0f, st, nullptr, nullptr,
-                                                      nullptr, brow, bcol);
+        k_ip<false, false><<<nb, kIpThreads, 0, s>>>(a, ip, blocks, off, bidx, ndev, nb, 0.0f, st,
+                                                      const_cast<int *>(rank), nullptr, nullptr, brow, bcol, list);
 }
 
 void launch_ip_audit(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,

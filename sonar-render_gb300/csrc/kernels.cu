@@ -2263,7 +2263,7 @@ template <bool ATT, int RS, int MINB>
 __global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *blocks, const uint8_t *cls,
                                                      const int *cap, const long long *off, int nblocks, float tol,
                                                      float limit, float2 *U, float2 *V, int *rank, float *fro,
-                                                     float *err)
+                                                     float *err, const int *list)
 {
     extern __shared__ float2 aca_smem[];  // sU[RS][kTile], then sV[RS][kTile]
     float2 *sU = aca_smem, *sV = aca_smem + RS * kTile;
@@ -2271,17 +2271,11 @@ __global__ void __launch_bounds__(kTile, MINB) k_aca(SumArgs a, const int2 *bloc
     __shared__ float4 sFrag[4][kTile];  // position and normal of the columns' (I) and rows' (J) fragments
     __shared__ __align__(16) unsigned slotA[kAcaWarps], slotB[kAcaWarps], slotZ[kAcaWarps];
     __shared__ float2 sumB[kAcaWarps];
-    const int t = threadIdx.x, b = blockIdx.x;
-    if (b >= nblocks) return;  // CTA-uniform
+    const int t = threadIdx.x;
+    if ((int)blockIdx.x >= nblocks) return;  // CTA-uniform
+    const int b = list ? list[blockIdx.x] : (int)blockIdx.x;  // kept block
     const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = min(cap[b], kLrRankLimit);
-    if (K <= 0) {  // CTA-uniform: an interpolated block (the interpolation kernel writes its results)
-        if (threadIdx.x == 0) {
-            rank[b] = -1;
-            fro[b] = 0.0f;
-            err[b] = -1.0f;
-        }
-        return;
-    }
+    if (K <= 0) return;  // CTA-uniform: an interpolated block (the interpolation kernel writes its results)
     const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
     const float4 *PI = a.srcA + I * kTile, *NI = a.srcB + I * kTile, *PJ = a.srcA + J * kTile, *NJ = a.srcB + J * kTile;
     float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
@@ -2545,7 +2539,8 @@ template <bool ATT, int RS, int MINB, bool FRAG = true>
 __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const int2 *blocks, const uint8_t *cls,
                                                              const int *cap, const long long *off, int nblocks,
                                                              float tol, float limit, float2 *U, float2 *V, int *rank,
-                                                             float *fro, float *err, float2 *brow, float2 *bcol)
+                                                             float *fro, float *err, float2 *brow, float2 *bcol,
+                                                             const int *list)
 {
     extern __shared__ float2 aca_smem[];  // sU[RS][kTile], then sV[RS][kTile]
     float2 *sU = aca_smem, *sV = aca_smem + RS * kTile;
@@ -2553,18 +2548,12 @@ __global__ void __launch_bounds__(kAca2Threads, MINB) k_aca2(SumArgs a, const in
     __shared__ float4 sFrag[FRAG ? 4 : 1][FRAG ? kTile : 1];  // position and normal of the columns' (I) and rows' (J) fragments
     __shared__ __align__(16) unsigned slotA[kAca2Warps], slotB[kAca2Warps], slotZ[kAca2Warps];
     __shared__ __align__(16) float2 sumB[kAca2Warps];
-    const int t = threadIdx.x, b = blockIdx.x;
+    const int t = threadIdx.x;
     const int ta = t, tb = t + kAca2Threads;  // this thread's two rows / columns
-    if (b >= nblocks) return;  // CTA-uniform
+    if ((int)blockIdx.x >= nblocks) return;  // CTA-uniform
+    const int b = list ? list[blockIdx.x] : (int)blockIdx.x;  // kept block
     const int I = blocks[b].x, J = blocks[b].y, bc = cls[b], K = min(cap[b], kLrRankLimit);
-    if (K <= 0) {  // CTA-uniform: an interpolated block (the interpolation kernel writes its results)
-        if (threadIdx.x == 0) {
-            rank[b] = -1;
-            fro[b] = 0.0f;
-            err[b] = -1.0f;
-        }
-        return;
-    }
+    if (K <= 0) return;  // CTA-uniform: an interpolated block (the interpolation kernel writes its results)
     const int ni = min(kTile, a.nsrc - I * kTile), nj = min(kTile, a.nsrc - J * kTile);
     const float4 *PI = a.srcA + I * kTile, *NI = a.srcB + I * kTile, *PJ = a.srcA + J * kTile, *NJ = a.srcB + J * kTile;
     float2 *Ub = U + off[b] * kTile, *Vb = V + off[b] * kTile;
@@ -2846,14 +2835,22 @@ template <int MINB>
 __global__ void __launch_bounds__(kTile, MINB) k_lr_block(SumArgs a, const int2 *blocks, const long long *off,
                                                           const int *bidx, int nb, const float2 *U, const float2 *V,
                                                           const int *rank, float2 *brow, float2 *bcol, const int *ndev,
-                                                          const uint8_t *lev)
+                                                          const uint8_t *lev, const int *list)
 {
     __shared__ float4 sW[kTile];  // (Re w_I, Im w_I, Re w_J, Im w_J) of every row t
     __shared__ float2 sTv[kLrMaxRank], sSu[kLrMaxRank];
     const int q = blockIdx.x;
-    if (q >= (ndev ? min(*ndev, nb) : nb)) return;
-    const int b = bidx[q];
-    if (lev && lev[b]) return;  // an interpolated block
+    int b;
+    if (list) {
+        // the cross-approximated kept blocks; rejected ones stay dense
+        if (q >= nb) return;
+        b = list[q];
+        if (rank[b] <= 0) return;
+    } else {
+        if (q >= (ndev ? min(*ndev, nb) : nb)) return;
+        b = bidx[q];
+        if (lev && lev[b]) return;  // an interpolated block
+    }
     lr_block_apply<kTile, true>(a, blocks[b].x, blocks[b].y, U + off[b] * kTile, V + off[b] * kTile, rank[b],
                                 brow + (size_t)b * kTile, bcol + (size_t)b * kTile, sW, sTv, sSu);
 }
@@ -3240,7 +3237,7 @@ namespace {
 template <bool ATT, int RS, int MINB>
 void launch_aca_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                   int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
-                  cudaStream_t s)
+                  cudaStream_t s, const int *list)
 {
     const size_t smem = (size_t)2 * RS * kTile * sizeof(float2);
     static bool attr = false;
@@ -3249,13 +3246,13 @@ void launch_aca_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, cons
         attr = true;
     }
     k_aca<ATT, RS, MINB><<<(unsigned)nblocks, kTile, smem, s>>>(a, blocks, cls, cap, off, nblocks, tol, limit, U, V,
-                                                                 rank, fro, err);
+                                                                 rank, fro, err, list);
 }
 
 template <bool ATT, int RS, int MINB, bool FRAG = true>
 void launch_aca2_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                    int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
-                   cudaStream_t s, float2 *brow, float2 *bcol)
+                   cudaStream_t s, float2 *brow, float2 *bcol, const int *list)
 {
     const size_t smem = (size_t)2 * RS * kTile * sizeof(float2);
     static bool attr = false;
@@ -3264,26 +3261,26 @@ void launch_aca2_t(const SumArgs &a, const int2 *blocks, const uint8_t *cls, con
         attr = true;
     }
     k_aca2<ATT, RS, MINB, FRAG><<<(unsigned)nblocks, kAca2Threads, smem, s>>>(
-        a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro, err, brow, bcol);
+        a, blocks, cls, cap, off, nblocks, tol, limit, U, V, rank, fro, err, brow, bcol, list);
 }
 
 template <bool ATT>
 bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap,
                   const long long *off, int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro,
-                  float limit, float *err, cudaStream_t s, float2 *brow, float2 *bcol)
+                  float limit, float *err, cudaStream_t s, float2 *brow, float2 *bcol, const int *list)
 {
     switch (variant) {
-    case 3: launch_aca2_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 4: launch_aca2_t<ATT, 6, 5>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 5: launch_aca2_t<ATT, 4, 6>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 6: launch_aca2_t<ATT, 2, 8>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 7: launch_aca2_t<ATT, 3, 7>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 8: launch_aca2_t<ATT, 8, 6, false>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 9: launch_aca2_t<ATT, 6, 7, false>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 10: launch_aca2_t<ATT, 4, 8, false>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol); return brow != nullptr;
-    case 1: launch_aca_t<ATT, 12, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
-    case 2: launch_aca_t<ATT, 16, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
-    default: launch_aca_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s); break;
+    case 3: launch_aca2_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, list); return brow != nullptr;
+    case 4: launch_aca2_t<ATT, 6, 5>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, list); return brow != nullptr;
+    case 5: launch_aca2_t<ATT, 4, 6>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, list); return brow != nullptr;
+    case 6: launch_aca2_t<ATT, 2, 8>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, list); return brow != nullptr;
+    case 7: launch_aca2_t<ATT, 3, 7>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, list); return brow != nullptr;
+    case 8: launch_aca2_t<ATT, 8, 6, false>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, list); return brow != nullptr;
+    case 9: launch_aca2_t<ATT, 6, 7, false>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, list); return brow != nullptr;
+    case 10: launch_aca2_t<ATT, 4, 8, false>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow, bcol, list); return brow != nullptr;
+    case 1: launch_aca_t<ATT, 12, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, list); break;
+    case 2: launch_aca_t<ATT, 16, 3>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, list); break;
+    default: launch_aca_t<ATT, 8, 4>(a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, list); break;
     }
     return false;
 }
@@ -3298,14 +3295,14 @@ bool launch_aca_v(int variant, const SumArgs &a, const int2 *blocks, const uint8
 // ranks, 7 CTAs; 10: 4 ranks, 8 CTAs
 bool launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                 int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
-                cudaStream_t s, int variant, float2 *brow, float2 *bcol)
+                cudaStream_t s, int variant, float2 *brow, float2 *bcol, const int *list)
 {
-    if (nblocks <= 0) return false;
+    if (nblocks <= 0) return brow != nullptr && variant >= 3;  // nothing to build; outputs as the variant would write
     if (a.ka != 0.0f)
         return launch_aca_v<true>(variant, a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow,
-                                  bcol);
+                                  bcol, list);
     return launch_aca_v<false>(variant, a, blocks, cls, cap, off, nblocks, tol, U, V, rank, fro, limit, err, s, brow,
-                               bcol);
+                               bcol, list);
 }
 
 void launch_lr_audit(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const long long *off, const int *rank,
@@ -3327,19 +3324,35 @@ void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off,
                      const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
                      double2 *ycol, cudaStream_t s, const int *ndev, bool outputs_ready, int lr_ctas,
-                     const IpCtx *ip)
+                     const IpCtx *ip, const int *aca_list, int naca)
 {
     // latency-bound on the factor stream: resident CTAs per SM are the lever
     // (registers capped to fit lr_ctas of them)
     if (nb > 0 && !outputs_ready) {
         const uint8_t *lev = ip ? ip->lev : nullptr;
-        if (lr_ctas >= 8)
-            k_lr_block<8><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev, lev);
-        else if (lr_ctas >= 6)
-            k_lr_block<6><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev, lev);
-        else
-            k_lr_block<4><<<nb, kTile, 0, s>>>(a, blocks, off, bidx, nb, U, V, rank, brow, bcol, ndev, lev);
-        if (ip) launch_ip_apply(a, ip->tile, ip->fxy, ip->lev, ip->delta, blocks, off, bidx, nb, ndev, U, brow, bcol, s);
+        const bool ip_side = ip && ip->stream && ip->fork && ip->join;
+        // with kept-block lists each kernel gets a grid of its own blocks
+        const int nl = aca_list ? naca : nb;
+        if (ip_side) {
+            cudaEventRecord(ip->fork, s);
+            cudaStreamWaitEvent(ip->stream, ip->fork, 0);
+            launch_ip_apply(a, ip->tile, ip->fxy, ip->lev, ip->delta, blocks, off, bidx, nb, ndev, U, brow, bcol,
+                            ip->stream, ip->list, ip->n, rank);
+            cudaEventRecord(ip->join, ip->stream);
+        }
+        if (nl > 0) {
+            if (lr_ctas >= 8)
+                k_lr_block<8><<<nl, kTile, 0, s>>>(a, blocks, off, bidx, nl, U, V, rank, brow, bcol, ndev, lev, aca_list);
+            else if (lr_ctas >= 6)
+                k_lr_block<6><<<nl, kTile, 0, s>>>(a, blocks, off, bidx, nl, U, V, rank, brow, bcol, ndev, lev, aca_list);
+            else
+                k_lr_block<4><<<nl, kTile, 0, s>>>(a, blocks, off, bidx, nl, U, V, rank, brow, bcol, ndev, lev, aca_list);
+        }
+        if (ip_side)
+            cudaStreamWaitEvent(s, ip->join, 0);
+        else if (ip)
+            launch_ip_apply(a, ip->tile, ip->fxy, ip->lev, ip->delta, blocks, off, bidx, nb, ndev, U, brow, bcol, s,
+                            ip->list, ip->n, rank);
     }
     if (ntiles > 0)
         k_lr_gather<<<ntiles, kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, bidx, yrow, ycol);

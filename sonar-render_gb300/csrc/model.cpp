@@ -182,7 +182,9 @@ struct Compression {
     int nip = 0;                // accepted interpolated blocks
     double mean_rank = 0.0, max_err = 0.0, ip_mean_nodes = 0.0;
     double pairs_cmp = 0.0;     // ordered pairs of the accepted blocks
-    float build_ms = 0.0f, select_ms = 0.0f, aca_ms = 0.0f, ip_ms = 0.0f;
+    // build: whole, selection, cross approximation, interpolation (both on
+    // their own streams), both together
+    float build_ms = 0.0f, select_ms = 0.0f, aca_ms = 0.0f, ip_ms = 0.0f, approx_ms = 0.0f;
     long long ncols = 0;        // factor columns reserved (sum of caps)
     int2 *d_blocks = nullptr;
     uint8_t *d_cls = nullptr;
@@ -200,6 +202,8 @@ struct Compression {
     int *d_kmap = nullptr, *d_acap = nullptr;  // kept block -> candidate, rank caps
     bool interp = false;        // interpolated blocks in this build
     uint8_t *d_lev = nullptr;   // per kept block: 0 cross approximation, 1..3 interpolation level
+    int *d_aca_list = nullptr, *d_ip_list = nullptr;  // kept blocks by kind
+    int naca_kept = 0, nip_kept = 0;
     IpCtx ip;                   // tile frames and box cells of the interpolated blocks
     bool stats_pending = false;     // statistics and timings not read back yet
     bool outputs_ready = false;     // the build also wrote the block outputs of its bounce's inputs
@@ -227,7 +231,8 @@ struct HopRecord {
     // compressed bounce blocks (FACET_SELF with compression on)
     int cmp_cand = 0, cmp_blocks = 0, cmp_accepted = 0, cmp_select = 0, cmp_ip_blocks = 0;
     double cmp_mean_rank = 0.0, cmp_max_err = 0.0, cmp_pairs = 0.0, cmp_ip_nodes = 0.0;
-    float cmp_build_ms = 0.0f, cmp_select_ms = 0.0f, cmp_aca_ms = 0.0f, cmp_ip_ms = 0.0f, lr_ms = 0.0f;
+    float cmp_build_ms = 0.0f, cmp_select_ms = 0.0f, cmp_aca_ms = 0.0f, cmp_ip_ms = 0.0f, cmp_approx_ms = 0.0f;
+    float lr_ms = 0.0f;
 };
 
 struct Model {
@@ -246,10 +251,11 @@ struct Model {
     cudaEvent_t ev6 = nullptr, ev7 = nullptr, ev8 = nullptr;
     // second stream of a compressed bounce: the low-rank apply (HBM-bound)
     // runs there beside the dense remainder (FP32 / SFU-bound)
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    // compression build: start, selected, cross approximation end, end, interpolation end
-    cudaEvent_t evb[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaStream_t side = nullptr, side2 = nullptr;  // low-rank work beside the dense remainder
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_fork2 = nullptr, ev_join2 = nullptr;
+    // compression build: start, selected, cross approximation end, end,
+    // interpolation end, interpolation start (second stream), both joined
+    cudaEvent_t evb[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     float4 *d_src_pos = nullptr, *d_fp_pos = nullptr;
     double2 *d_src_P = nullptr, *d_fp_P = nullptr;
     // field points are kept in Morton (spatial) order on the device so that a
@@ -320,18 +326,20 @@ struct Model {
         pack_cap = partial_cap = limit_cap = colpart_cap = 0;
         sym_tiles = 0;
         for (cudaEvent_t *e : {&ev0, &ev1, &ev2, &ev3, &ev4, &ev5, &ev6, &ev7, &ev8, &evb[0], &evb[1], &evb[2], &evb[3],
-                               &evb[4]})
+                               &evb[4], &evb[5], &evb[6]})
             if (*e) {
                 cudaEventDestroy(*e);
                 *e = nullptr;
             }
-        for (cudaEvent_t *e : {&ev_fork, &ev_join})
+        for (cudaEvent_t *e : {&ev_fork, &ev_join, &ev_fork2, &ev_join2})
             if (*e) {
                 cudaEventDestroy(*e);
                 *e = nullptr;
             }
         if (side) cudaStreamDestroy(side);
         side = nullptr;
+        if (side2) cudaStreamDestroy(side2);
+        side2 = nullptr;
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
         nnodes = ntri = 0;
@@ -563,11 +571,12 @@ void render()
     for (double &v : g.render_ms) v = 0.0;
     CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
     for (cudaEvent_t *e : {&g.ev0, &g.ev1, &g.ev2, &g.ev3, &g.ev4, &g.ev5, &g.ev6, &g.ev7, &g.ev8, &g.evb[0], &g.evb[1],
-                           &g.evb[2], &g.evb[3], &g.evb[4]})
+                           &g.evb[2], &g.evb[3], &g.evb[4], &g.evb[5], &g.evb[6]})
         CK(cudaEventCreate(e));
     CK(cudaStreamCreateWithFlags(&g.side, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&g.ev_fork, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&g.ev_join, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithFlags(&g.side2, cudaStreamNonBlocking));
+    for (cudaEvent_t *e : {&g.ev_fork, &g.ev_join, &g.ev_fork2, &g.ev_join2})
+        CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     g.render_ms[0] = host_ms() - t0;
     for (int t : {OBJ_TARGET, OBJ_SOURCE, OBJ_FIELD})
         for (auto &o : g.obj[t]) render_object(*o);
@@ -895,7 +904,8 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
                        Arena::bytes_of(ngrid, sizeof(int)) + 2 * Arena::bytes_of(M.nsrc, sizeof(double2)) +
                        Arena::bytes_of((size_t)kCmpStats * cmp_stats_parts(), sizeof(double)) +
                        Arena::bytes_of((size_t)kIpTileRec * nt, sizeof(float4)) + Arena::bytes_of(M.nsrc, sizeof(uint16_t)) +
-                       2 * Arena::bytes_of(nmax, 1) + 8192;
+                       2 * Arena::bytes_of(nmax, 1) + 2 * Arena::bytes_of(nmax, sizeof(int)) +
+                       2 * Arena::bytes_of(nb + 1, sizeof(int)) + 8192;
         C.arena.reserve(bytes);
     }
     Arena &ar = C.arena;
@@ -947,14 +957,29 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     const float cut = std::log2(1.0f + g.opt_cmp_rcut);
     launch_keep_lists(nb, d_coff, d_pred, cut, rmax, d_cblocks, d_ccls, d_kcnt, d_ksum, d_koff, d_kcol, C.d_blocks,
                       C.d_cls, C.d_acap, C.d_off, C.d_kmap, st, d_clev, C.d_lev);
+    int *d_ioff = nullptr;
+    C.d_aca_list = C.d_ip_list = nullptr;
+    if (C.interp) {
+        // each kind's kernels get grids of their own blocks only
+        int *d_icnt = ar.take<int>(nb);
+        d_ioff = ar.take<int>(nb + 1);
+        C.d_aca_list = ar.take<int>(nmax);
+        C.d_ip_list = ar.take<int>(nmax);
+        launch_split_kept(nb, d_koff, C.d_lev, d_icnt, d_ioff, C.d_aca_list, C.d_ip_list, st);
+    }
     CK(cudaEventRecord(g.evb[1], st));
-    int hcnt[3] = {0, 0, 0};  // candidates, kept blocks, factor columns
+    int hcnt[4] = {0, 0, 0, 0};  // candidates, kept blocks, factor columns, interpolated kept blocks
     CK(cudaMemcpyAsync(&hcnt[0], d_coff + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&hcnt[1], d_koff + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&hcnt[2], d_kcol + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (d_ioff) CK(cudaMemcpyAsync(&hcnt[3], d_ioff + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     const int n = hcnt[1];
     const long long cols = hcnt[2];
+    C.nip_kept = C.interp ? hcnt[3] : 0;
+    C.naca_kept = n - C.nip_kept;
+    C.ip.list = C.d_ip_list;
+    C.ip.n = C.nip_kept;
     C.select = select;
     C.ncand = hcnt[0];
     C.nblocks = n;
@@ -973,22 +998,39 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     C.d_rank = ar.take<int>(nmax);
     C.d_fro = ar.take<float>(nmax);
     C.d_err = ar.take<float>(nmax);
+    // the interpolated blocks on the second stream beside the cross
+    // approximation (disjoint blocks and output slots; each kernel writes the
+    // rank, error and outputs of its own blocks only)
+    const bool ip_side = C.interp && g.opt_overlap;
+    const cudaStream_t ist = ip_side ? g.side : st;
+    if (ip_side) {
+        CK(cudaEventRecord(g.ev_fork, st));
+        CK(cudaStreamWaitEvent(g.side, g.ev_fork, 0));
+    }
+    CK(cudaEventRecord(g.evb[5], ist));
     // the panel kernels also apply the accepted blocks to this bounce's packed
     // inputs: the first bounce's low-rank apply then only gathers
-    C.outputs_ready = launch_aca(s, C.d_blocks, C.d_cls, C.d_acap, C.d_off, n, g.opt_cmp_tol, C.d_U, C.d_V, C.d_rank,
-                                 C.d_fro, g.opt_cmp_judge, C.d_err, st, g.opt_aca_variant,
-                                 g.opt_fused_apply ? C.d_brow : nullptr, g.opt_fused_apply ? C.d_bcol : nullptr);
+    C.outputs_ready = launch_aca(s, C.d_blocks, C.d_cls, C.d_acap, C.d_off, C.interp ? C.naca_kept : n, g.opt_cmp_tol,
+                                 C.d_U, C.d_V, C.d_rank, C.d_fro, g.opt_cmp_judge, C.d_err, st, g.opt_aca_variant,
+                                 g.opt_fused_apply ? C.d_brow : nullptr, g.opt_fused_apply ? C.d_bcol : nullptr,
+                                 C.d_aca_list);
     CK(cudaGetLastError());
     CK(cudaEventRecord(g.evb[2], st));
     if (C.interp) {
-        // the interpolated blocks: node entries, judge, and the fused apply
-        // when the cross approximation applies its own blocks too
+        // node entries, judge, and the fused apply when the cross
+        // approximation applies its own blocks too
         const bool fused = C.outputs_ready;
-        launch_ip_build(s, C.ip.tile, C.ip.fxy, C.ip.lev, A.delta, C.d_blocks, C.d_off, n, g.opt_cmp_judge, C.d_U,
-                        C.d_rank, C.d_fro, C.d_err, fused ? C.d_brow : nullptr, fused ? C.d_bcol : nullptr, st);
+        launch_ip_build(s, C.ip.tile, C.ip.fxy, C.ip.lev, A.delta, C.d_blocks, C.d_off, C.nip_kept, g.opt_cmp_judge,
+                        C.d_U, C.d_rank, C.d_fro, C.d_err, fused ? C.d_brow : nullptr, fused ? C.d_bcol : nullptr, ist,
+                        C.d_ip_list);
         CK(cudaGetLastError());
     }
-    CK(cudaEventRecord(g.evb[4], st));
+    CK(cudaEventRecord(g.evb[4], ist));
+    if (ip_side) {
+        CK(cudaEventRecord(g.ev_join, g.side));
+        CK(cudaStreamWaitEvent(st, g.ev_join, 0));
+    }
+    CK(cudaEventRecord(g.evb[6], st));
     // ---- accepted blocks: dense flags off, owner lists, statistics
     C.d_flags = ar.take<uint8_t>(ngrid);
     CK(cudaMemcpyAsync(C.d_flags, M.view.flags, ngrid, cudaMemcpyDeviceToDevice, st));
@@ -1034,7 +1076,8 @@ void finish_compression()
     CK(cudaEventElapsedTime(&C.build_ms, g.evb[0], g.evb[3]));
     CK(cudaEventElapsedTime(&C.select_ms, g.evb[0], g.evb[1]));
     CK(cudaEventElapsedTime(&C.aca_ms, g.evb[1], g.evb[2]));
-    CK(cudaEventElapsedTime(&C.ip_ms, g.evb[2], g.evb[4]));
+    CK(cudaEventElapsedTime(&C.ip_ms, g.evb[5], g.evb[4]));
+    CK(cudaEventElapsedTime(&C.approx_ms, g.evb[1], g.evb[6]));
     C.desc.clear();
     C.label.clear();
     if (C.select == 1 && C.nblocks > 0) {
@@ -1173,9 +1216,18 @@ void run_hop(int hop, int a, int b)
                     lst = g.side;
                 }
                 CK(cudaEventRecord(g.ev4, lst));
+                // the interpolated blocks' apply on a third stream beside the
+                // factor stream (compute- and memory-bound work side by side)
+                IpCtx ipc = C.ip;
+                if (g.opt_overlap) {
+                    ipc.stream = g.side2;
+                    ipc.fork = g.ev_fork2;
+                    ipc.join = g.ev_join2;
+                }
                 launch_lr_apply(s, C.d_blocks, C.d_off, C.d_bidx, C.nblocks, C.d_U, C.d_V, C.d_rank, C.d_brow, C.d_bcol,
                                 M.view.ndstblocks, C.d_byJ_off, C.d_byJ, C.d_byI_off, C.d_byI, C.d_yrow, C.d_ycol, lst,
-                                C.d_nacc, built && C.outputs_ready, g.opt_lr_ctas, C.interp ? &C.ip : nullptr);
+                                C.d_nacc, built && C.outputs_ready, g.opt_lr_ctas, C.interp ? &ipc : nullptr,
+                                C.interp ? C.d_aca_list : nullptr, C.naca_kept);
                 CK(cudaEventRecord(g.ev5, lst));
                 if (g.opt_overlap) CK(cudaEventRecord(g.ev_join, lst));
                 yrow = C.d_yrow;
@@ -1260,6 +1312,7 @@ void run_hop(int hop, int a, int b)
             rec.cmp_select_ms = g.cmp.select_ms;
             rec.cmp_aca_ms = g.cmp.aca_ms;
             rec.cmp_ip_ms = g.cmp.ip_ms;
+            rec.cmp_approx_ms = g.cmp.approx_ms;
         }
         CK(cudaEventElapsedTime(&rec.lr_ms, g.ev4, g.ev5));
     }
@@ -1734,10 +1787,11 @@ int sonar_get_stats(char *json, int cap)
                  "\"cmp_accepted\": %d, \"cmp_pairs\": %.0f, \"cmp_mean_rank\": %.3f, \"cmp_max_err\": %.3e, "
                  "\"cmp_ip_blocks\": %d, \"cmp_ip_nodes\": %.3f, "
                  "\"cmp_build_ms\": %.6f, \"cmp_select_ms\": %.6f, \"cmp_aca_ms\": %.6f, \"cmp_ip_ms\": %.6f, "
-                 "\"lr_ms\": %.6f}",
+                 "\"cmp_approx_ms\": %.6f, \"lr_ms\": %.6f}",
                  i ? ", " : "", r.hop, r.pairs, r.mask_ms, r.sum_ms, r.total_ms, r.nsplit, r.launches, r.cmp_select,
                  r.cmp_cand, r.cmp_blocks, r.cmp_accepted, r.cmp_pairs, r.cmp_mean_rank, r.cmp_max_err,
-                 r.cmp_ip_blocks, r.cmp_ip_nodes, r.cmp_build_ms, r.cmp_select_ms, r.cmp_aca_ms, r.cmp_ip_ms, r.lr_ms);
+                 r.cmp_ip_blocks, r.cmp_ip_nodes, r.cmp_build_ms, r.cmp_select_ms, r.cmp_aca_ms, r.cmp_ip_ms,
+                 r.cmp_approx_ms, r.lr_ms);
         s += buf;
     }
     snprintf(buf, sizeof(buf),

@@ -186,6 +186,37 @@ __global__ void __launch_bounds__(kSelThreads) k_keep_fill(const int *coff, cons
     }
 }
 
+// kept blocks of row J by kind: interpolated (level > 0) and cross-approximated
+__global__ void __launch_bounds__(kSelThreads) k_split_count(const int *koff, const uint8_t *alev, int *icnt)
+{
+    __shared__ int sw[kSelThreads / 32];
+    const int J = blockIdx.x, k0 = koff[J], k1 = koff[J + 1];
+    int c = 0;
+    for (int k = k0 + threadIdx.x; k < k1; k += kSelThreads) c += alev[k] ? 1 : 0;
+    int tot;
+    block_scan(c, tot, sw);
+    if (threadIdx.x == 0) icnt[J] = tot;
+}
+
+__global__ void __launch_bounds__(kSelThreads) k_split_fill(const int *koff, const uint8_t *alev, const int *ioff,
+                                                            int *aca_list, int *ip_list)
+{
+    __shared__ int sw[kSelThreads / 32];
+    const int J = blockIdx.x, k0 = koff[J], k1 = koff[J + 1];
+    int ib = ioff[J], ab = k0 - ioff[J];
+    for (int i0 = k0; i0 < k1; i0 += kSelThreads) {
+        const int k = i0 + threadIdx.x;
+        const bool in = k < k1, ip = in && alev[k];
+        int ti, ta;
+        const int pi = block_scan(ip ? 1 : 0, ti, sw);
+        const int pa = block_scan(in && !ip ? 1 : 0, ta, sw);
+        if (ip) ip_list[ib + pi] = k;
+        else if (in) aca_list[ab + pa] = k;
+        ib += ti;
+        ab += ta;
+    }
+}
+
 // accepted blocks (rank > 0) of kept row J: counts, flags of the dense kernel
 // cleared, the (I, J) bitmap for the per-I lists
 __global__ void __launch_bounds__(kSelThreads) k_acc_count(const int *koff, const int2 *ab, const int *rank, int nb,
@@ -320,6 +351,15 @@ void launch_keep_lists(int nb, const int *coff, const float *pred, float cut, in
     k_scan<<<1, kSelThreads, 0, s>>>(ksum, nb, kcoloff);
     k_keep_fill<<<nb, kSelThreads, 0, s>>>(coff, pred, cut, rmax, cblocks, ccls, clev, koff, kcoloff, ab, acls, acap,
                                            aoff, kmap, alev);
+}
+
+void launch_split_kept(int nb, const int *koff, const uint8_t *alev, int *icnt, int *ioff, int *aca_list,
+                       int *ip_list, cudaStream_t s)
+{
+    if (nb <= 0) return;
+    k_split_count<<<nb, kSelThreads, 0, s>>>(koff, alev, icnt);
+    k_scan<<<1, kSelThreads, 0, s>>>(icnt, nb, ioff);
+    k_split_fill<<<nb, kSelThreads, 0, s>>>(koff, alev, ioff, aca_list, ip_list);
 }
 
 void launch_accept_lists(int nt, int nb, const int *koff, const int2 *ab, const int *rank, uint8_t *flags_out,

@@ -162,9 +162,11 @@ void launch_finalize_f2f_sym(const double2 *rowpart, const int *chunk_off, int n
 constexpr int kLrRankLimit = 64;
 // Returns true when the kernel also wrote the low-rank apply's block outputs
 // for the packed inputs of this launch (panel variants given brow, bcol).
+// list (optional): the kept blocks to build (nblocks of them); otherwise blocks 0 .. nblocks - 1
 bool launch_aca(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const int *cap, const long long *off,
                 int nblocks, float tol, float2 *U, float2 *V, int *rank, float *fro, float limit, float *err,
-                cudaStream_t s, int variant = 0, float2 *brow = nullptr, float2 *bcol = nullptr);
+                cudaStream_t s, int variant = 0, float2 *brow = nullptr, float2 *bcol = nullptr,
+                const int *list = nullptr);
 // Full-tile relative RMS error of the sampled accepted blocks (no attenuation)
 void launch_lr_audit(const SumArgs &a, const int2 *blocks, const uint8_t *cls, const long long *off, const int *rank,
                      const int *sample, int ns, const float2 *U, const float2 *V, float *out_err, cudaStream_t s,
@@ -184,8 +186,10 @@ __host__ __device__ constexpr int ip_nodes(int level)
 }
 __host__ __device__ constexpr int ip_columns(int level)
 {
-    // C with rows of odd pitch (P | 1), then the smooth part's 12 x 13
-    return level >= 1 && level <= 3 ? (ip_nodes(level) * (ip_nodes(level) | 1) + 156 + kTile - 1) / kTile : 0;
+    // C with rows of odd pitch (P | 1), then (from an even entry) the smooth part's 12 x 13
+    return level >= 1 && level <= 3
+               ? ((((ip_nodes(level) * (ip_nodes(level) | 1)) + 1) & ~1) + 156 + kTile - 1) / kTile
+               : 0;
 }
 constexpr int kIpTileRec = 6;  // float4 per tile record
 struct IpCtx {
@@ -193,6 +197,13 @@ struct IpCtx {
     const uint16_t *fxy = nullptr;
     const uint8_t *lev = nullptr;
     float delta = 0.0f;
+    // the interpolated kept blocks (n of them)
+    const int *list = nullptr;
+    int n = 0;
+    // optional: the apply runs on this stream beside the factor blocks
+    // (fork / join: events the launcher records to order the two)
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 // facet_grid: per facet (xAxis, nx as int bits), (yAxis, first cell as int bits)
 void launch_ip_tiles(const float4 *pos, const float4 *nrm, const int *act_facet, const int *act_cell,
@@ -201,13 +212,17 @@ void launch_ip_tiles(const float4 *pos, const float4 *nrm, const int *act_facet,
 void launch_ip_level(const int2 *cb, const uint8_t *ccls, const int *ncand, int nmax, const float4 *tile,
                      float delta, float kr, float tol, uint8_t *lev, cudaStream_t s);
 // node entries, judge (rank = node count or -1) and, given brow, the apply to
-// the packed inputs; kept blocks of level 0 are left alone
+// the packed inputs; kept blocks of level 0 are left alone.  list
+// (optional): the interpolated kept blocks, n of them.
 void launch_ip_build(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,
                      const int2 *blocks, const long long *off, int n, float limit, float2 *store, int *rank,
-                     float *fro, float *err, float2 *brow, float2 *bcol, cudaStream_t s);
+                     float *fro, float *err, float2 *brow, float2 *bcol, cudaStream_t s, const int *list = nullptr);
+// the apply of the accepted interpolated blocks: over list (nlist kept
+// blocks, rank > 0) when given, else over the accepted positions bidx
 void launch_ip_apply(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,
                      const int2 *blocks, const long long *off, const int *bidx, int nb, const int *ndev,
-                     const float2 *store, float2 *brow, float2 *bcol, cudaStream_t s);
+                     const float2 *store, float2 *brow, float2 *bcol, cudaStream_t s, const int *list = nullptr,
+                     int nlist = 0, const int *rank = nullptr);
 // full-tile relative RMS error of sampled accepted interpolated blocks (no attenuation)
 void launch_ip_audit(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,
                      const int2 *blocks, const long long *off, const int *sample, int ns, const float2 *store,
@@ -218,7 +233,7 @@ void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off,
                      const float2 *U, const float2 *V, const int *rank, float2 *brow, float2 *bcol, int ntiles,
                      const int *byJ_off, const int *byJ, const int *byI_off, const int *byI, double2 *yrow,
                      double2 *ycol, cudaStream_t s, const int *ndev = nullptr, bool outputs_ready = false,
-                     int lr_ctas = 4, const IpCtx *ip = nullptr);
+                     int lr_ctas = 4, const IpCtx *ip = nullptr, const int *aca_list = nullptr, int naca = 0);
 // select.cu: block lists of the compressed bounce, built on the device
 void launch_cand_lists(const uint8_t *flags, int nt, int nb, int select, float eta, const float4 *cen, int *cnt,
                        int *off, int2 *blocks, uint8_t *cls, cudaStream_t s);
@@ -228,6 +243,10 @@ void launch_keep_lists(int nb, const int *coff, const float *pred, float cut, in
                        const uint8_t *ccls, int *kcnt, int *ksum, int *koff, int *kcoloff, int2 *ab, uint8_t *acls,
                        int *acap, long long *aoff, int *kmap, cudaStream_t s, const uint8_t *clev = nullptr,
                        uint8_t *alev = nullptr);
+// kept blocks by kind, in kept order: the cross-approximated ones
+// (aca_list) and the interpolated ones (ip_list); ioff[nb] = their count
+void launch_split_kept(int nb, const int *koff, const uint8_t *alev, int *icnt, int *ioff, int *aca_list,
+                       int *ip_list, cudaStream_t s);
 void launch_accept_lists(int nt, int nb, const int *koff, const int2 *ab, const int *rank, uint8_t *flags_out,
                          uint8_t *accbm, int *qidx, int *acnt, int *byJ_off, int *bidx, int *byJ, int *icnt,
                          int *byI_off, int *byI, cudaStream_t s);
