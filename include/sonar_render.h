@@ -211,8 +211,11 @@ long long sonar_fragment_triangle(const float *tri9, float delta, int *nx_ny_neg
                                   long long cap);
 
 /* Admissibility network for the low-rank bounce blocks (no counterpart in the
- * reference): a perceptron 8 -> 128 -> 128 -> 128 -> 1 with ReLU, FP32,
- * trained and run by the library's own CUDA kernels.  Input: 8 descriptors
+ * reference): a perceptron 8 -> w -> w -> w -> 1 with ReLU, hidden width w =
+ * 64 (default) or 128, trained in FP32 and run by the library's own CUDA
+ * kernels (width 64: FP32 inference on the CUDA cores; width 128: FP16
+ * hidden layers on the tensor cores with FP32 accumulation, input and
+ * output layers FP32).  Input: 8 descriptors
  * of a block (log2(1 + separation / lambda), log2(1 + radius / lambda) of the
  * source and destination tiles, cosines of both mean normals with the
  * separation direction and with each other, (r_I + r_J) / separation capped
@@ -220,6 +223,9 @@ long long sonar_fragment_triangle(const float *tri9, float delta, int *nx_ny_neg
  * Parameters: per layer the weights (out x in, row-major) then the biases.
  * Every call returns 0 or a negative code (sonar_last_error). */
 int sonar_mlp_param_count(void);
+/* Hidden width 64 or 128; drops the parameters (initialise or load again). */
+int sonar_mlp_set_width(int width);
+int sonar_mlp_width(void);
 int sonar_mlp_init(unsigned seed); /* He-uniform weights, zero biases */
 int sonar_mlp_set_params(const float *params, long long n);
 int sonar_mlp_get_params(float *params, long long n);

@@ -2,8 +2,8 @@
  *
  * TEST INFRASTRUCTURE ONLY: the GPU's forward and backward kernels are
  * checked against these loops.  The reference has no learned component; the
- * network is defined here by its mathematics: layers 8 -> 64 -> 64 -> 64
- * -> 1, y = W x + b, ReLU after every layer but the last, loss = mean over
+ * network is defined here by its mathematics: layers 8 -> w -> w -> w -> 1
+ * (hidden width w = 64 or 128), y = W x + b, ReLU after every layer but the last, loss = mean over
  * the batch of (y_hat - y)^2.  Parameter layout: per layer the weights
  * (out x in, row-major) then the biases.
  */
@@ -11,7 +11,13 @@
 #include <string.h>
 
 #define NL 4
-static const int dims[NL + 1] = {8, 64, 64, 64, 1};
+static int dims[NL + 1] = {8, 64, 64, 64, 1};
+
+/* The hidden width (64 or 128, as the library's network). */
+void orc_mlp_set_width(int w)
+{
+    if (w == 64 || w == 128) dims[1] = dims[2] = dims[3] = w;
+}
 
 int orc_mlp_param_count(void)
 {

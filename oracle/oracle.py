@@ -108,6 +108,7 @@ def lib():
         L.orc_fragment_triangle.argtypes = [_f, C.c_float, _i, _f, _f, C.c_long]
         L.orc_fragment_triangle.restype = C.c_long
         L.orc_segment.argtypes = [_vp, _d, _d, C.c_double, _i]
+        L.orc_mlp_set_width.argtypes = [C.c_int]
         L.orc_mlp_forward.argtypes = [_f, _f, C.c_int, _d]
         L.orc_mlp_grad.argtypes = [_f, _f, _f, C.c_int, _d, _d]
         _lib = L
@@ -140,6 +141,11 @@ def fragment_triangle(tri9, delta):
     L.orc_fragment_triangle(_fp(t), C.c_float(delta), ints.ctypes.data_as(_i), _fp(fl), _fp(areas), n)
     nx, ny, neg = (int(v) for v in ints)
     return (nx, ny, neg), fl, areas[:n].reshape(ny, nx)
+
+
+def mlp_set_width(width):
+    """Hidden width of the network restatement (64 or 128)."""
+    lib().orc_mlp_set_width(int(width))
 
 
 def mlp_param_count() -> int:

@@ -32,6 +32,8 @@ def _lib():
     L = api.lib()
     if not _bound:
         L.sonar_mlp_param_count.restype = C.c_int
+        L.sonar_mlp_set_width.argtypes = [C.c_int]
+        L.sonar_mlp_width.restype = C.c_int
         L.sonar_mlp_init.argtypes = [C.c_uint]
         L.sonar_mlp_set_params.argtypes = [_f, C.c_longlong]
         L.sonar_mlp_get_params.argtypes = [_f, C.c_longlong]
@@ -54,6 +56,16 @@ def _call(r, what):
 
 def _fa(a):
     return a.ctypes.data_as(_f)
+
+
+def set_width(width: int):
+    """Hidden width 64 (FP32 inference) or 128 (FP16 hidden layers on the
+    tensor cores); drops the parameters."""
+    _call(_lib().sonar_mlp_set_width(int(width)), "sonar_mlp_set_width")
+
+
+def width() -> int:
+    return int(_lib().sonar_mlp_width())
 
 
 def param_count() -> int:

@@ -1,5 +1,5 @@
-// mlp.cu -- the learned admissibility model: a 4-layer, width-64 perceptron
-// trained and evaluated by this library's own CUDA kernels.
+// mlp.cu -- the learned admissibility model: a 4-layer perceptron of hidden
+// width 64 or 128, trained and evaluated by this library's own CUDA kernels.
 //
 // It maps the descriptors of a fragment-cluster pair (separation and radii in
 // wavelengths, normal angles, visibility fraction) to the predicted log2 of
@@ -8,25 +8,31 @@
 // attempt; the others are approximated with a rank cap derived from the
 // prediction, and the exact tile still judges every approximation.
 //
-// Layers: 8 -> 64 -> 64 -> 64 -> 1, ReLU between, FP32 weights, activations
-// and gradients.  Training: mean-squared error on log2(rank), Adam.
-// Kernels: a shared-memory tiled dense layer (forward, input gradient, weight
-// gradient), bias/ReLU epilogues, the loss gradient and the Adam update.
+// Layers: 8 -> w -> w -> w -> 1 (w = 64 or 128), ReLU between.  Training in
+// FP32 (weights, activations, gradients): mean-squared error on log2(rank),
+// Adam; kernels: a shared-memory tiled dense layer (forward, input gradient,
+// weight gradient), bias/ReLU epilogues, the loss gradient and the Adam
+// update.  Inference: width 64 in FP32 on the CUDA cores (k_mlp_infer);
+// width 128 with FP16 hidden layers on the tensor cores (k_mlp128_tc:
+// tcgen05.mma, FP32 accumulators in tensor memory), the input and output
+// layers in FP32.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <random>
 #include <vector>
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "sonar_internal.h"
+#include "tc05.cuh"
 
 namespace sonar {
 namespace {
 
-constexpr int kIn = 8, kWidth = 64, kLayers = 4;
-constexpr int kDims[kLayers + 1] = {kIn, kWidth, kWidth, kWidth, 1};
+constexpr int kIn = 8, kWidth = 64, kLayers = 4;  // kWidth: the CUDA-core inference kernel's width
+constexpr int kWide = 128;                        // the tensor-core inference kernel's width
 constexpr int kT = 16;  // tile of the dense-layer kernels
 
 // Y[b, o] = sum_i X[b, i] W[o, i] + bias[o]  (optionally ReLU)
@@ -262,33 +268,231 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_mlp_infer(const float *P, 
     }
 }
 
+
+// ---------------------------------------------------------------- width 128 on the tensor cores
+// One CTA of 128 threads per tile of 128 rows (persistent over the tiles),
+// thread r = row r = tensor-memory lane r.  Layer 1 (8 -> 128, FP32 on the
+// CUDA cores) writes its ReLU output as FP16 into the A operand; each hidden
+// layer is D (128 x 128, FP32 in tensor memory) = A (128 rows x 128, FP16)
+// times W^T (W: 128 out x 128 in, FP16, staged once per CTA): eight
+// tcgen05.mma of K = 16 issued by thread 0, completion on an mbarrier
+// (bounded waits).  The accumulator comes back with tcgen05.ld, 16 columns at
+// a time: bias and ReLU, then either the next layer's FP16 A operand or the
+// output layer's dot product (FP32).  Operands in the no-swizzle K-major
+// canonical layout: element (r, k) at (k / 8) * 2048 + r * 16 + (k % 8) * 2
+// bytes.
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcOpBytes = (uint32_t)kTcRows * kWide * 2;  // one FP16 operand, 32 KB
+constexpr uint32_t kTcLbo = (uint32_t)kTcRows * 16;              // between the K core matrices
+constexpr size_t kTcSmem = 3 * (size_t)kTcOpBytes + sizeof(float) * ((size_t)kIn * kWide + 4 * kWide + 4);
+// instruction descriptor of kind::f16: FP32 accumulator, F16 A and B, both K-major, N = 128, M = 128
+constexpr uint32_t kTcIdescF16 = (1u << 4) | ((uint32_t)(kWide >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+
+__device__ __forceinline__ uint32_t tc_op_off(int r, int k8) { return (uint32_t)k8 * kTcLbo + (uint32_t)r * 16u; }
+
+__device__ __forceinline__ uint4 pack_half8(const float *v)
+{
+    uint4 o;
+    __half2 h;
+    h = __floats2half2_rn(v[0], v[1]);
+    o.x = *reinterpret_cast<uint32_t *>(&h);
+    h = __floats2half2_rn(v[2], v[3]);
+    o.y = *reinterpret_cast<uint32_t *>(&h);
+    h = __floats2half2_rn(v[4], v[5]);
+    o.z = *reinterpret_cast<uint32_t *>(&h);
+    h = __floats2half2_rn(v[6], v[7]);
+    o.w = *reinterpret_cast<uint32_t *>(&h);
+    return o;
+}
+
+__global__ void __launch_bounds__(kTcRows, 1) k_mlp128_tc(const float *P, const float *X, int n, float *Y,
+                                                          int *status)
+{
+    extern __shared__ __align__(1024) uint8_t smt[];
+    uint8_t *sA = smt, *sB2 = smt + kTcOpBytes, *sB3 = smt + 2 * kTcOpBytes;
+    float *W1 = reinterpret_cast<float *>(smt + 3 * kTcOpBytes);  // [kIn][kWide]
+    float *B1 = W1 + kIn * kWide, *B2 = B1 + kWide, *B3 = B2 + kWide, *W4 = B3 + kWide, *B4 = W4 + kWide;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) tmem_alloc(&tmem_base, kWide);
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // parameter vector: per layer W (out x in) then b (out)
+    const float *p1 = P, *pb1 = p1 + kWide * kIn, *p2 = pb1 + kWide, *pb2 = p2 + kWide * kWide,
+                *p3 = pb2 + kWide, *pb3 = p3 + kWide * kWide, *p4 = pb3 + kWide, *pb4 = p4 + kWide;
+    for (int e = tid; e < kWide * kWide / 8; e += kTcRows) {
+        const int o = e / (kWide / 8), k8 = e - o * (kWide / 8);
+        float w[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) w[j] = p2[o * kWide + k8 * 8 + j];
+        *reinterpret_cast<uint4 *>(sB2 + tc_op_off(o, k8)) = pack_half8(w);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) w[j] = p3[o * kWide + k8 * 8 + j];
+        *reinterpret_cast<uint4 *>(sB3 + tc_op_off(o, k8)) = pack_half8(w);
+    }
+    for (int e = tid; e < kWide * kIn; e += kTcRows) {
+        const int o = e / kIn, i = e - o * kIn;
+        W1[i * kWide + o] = p1[e];
+    }
+    for (int e = tid; e < kWide; e += kTcRows) {
+        B1[e] = pb1[e];
+        B2[e] = pb2[e];
+        B3[e] = pb3[e];
+        W4[e] = p4[e];
+    }
+    if (tid == 0) B4[0] = pb4[0];
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base, aA = smem_u32(sA), aB2 = smem_u32(sB2), aB3 = smem_u32(sB3);
+    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    uint32_t commits = 0;
+    bool ok = true;
+    const int ntiles = (n + kTcRows - 1) / kTcRows;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int row = tile * kTcRows + tid;
+        // layer 1: 8 -> 128, ReLU, FP16 into the A operand
+        float x[kIn];
+        if (row < n) {
+            const float4 a = __ldg(reinterpret_cast<const float4 *>(X + (size_t)row * kIn));
+            const float4 b = __ldg(reinterpret_cast<const float4 *>(X + (size_t)row * kIn) + 1);
+            x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w; x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+        } else {
+#pragma unroll
+            for (int i = 0; i < kIn; ++i) x[i] = 0.0f;
+        }
+#pragma unroll 2
+        for (int k8 = 0; k8 < kWide / 8; ++k8) {
+            float h[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int o = k8 * 8 + j;
+                float v = B1[o];
+#pragma unroll
+                for (int i = 0; i < kIn; ++i) v = fmaf(W1[i * kWide + o], x[i], v);
+                h[j] = fmaxf(v, 0.0f);
+            }
+            *reinterpret_cast<uint4 *>(sA + tc_op_off(tid, k8)) = pack_half8(h);
+        }
+        float y = 0.0f;
+        for (int layer = 0; layer < 2; ++layer) {
+            // the A operand written by every thread -> visible to the tensor core
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t aB = layer ? aB3 : aB2;
+#pragma unroll
+                for (int ks = 0; ks < kWide / 16; ++ks)
+                    mma_bf16(tmem, sdesc(aA + ks * 2 * kTcLbo, kTcLbo, 128), sdesc(aB + ks * 2 * kTcLbo, kTcLbo, 128),
+                             kTcIdescF16, ks > 0 ? 1u : 0u);
+                mma_commit(&bar);
+            }
+            ++commits;
+            ok = __syncthreads_and(mbar_wait(&bar, (commits - 1) & 1u));
+            if (!ok) break;
+            tc_fence_after();
+            const float *Bv = layer ? B3 : B2;
+#pragma unroll 1
+            for (int c = 0; c < kWide; c += 16) {
+                float v[16];
+                tmem_ld16(lane_addr + (uint32_t)c, v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + Bv[c + j], 0.0f);
+                if (layer == 0) {
+                    // the MMAs that read the A operand have completed: it becomes the next layer's input
+                    *reinterpret_cast<uint4 *>(sA + tc_op_off(tid, c / 8)) = pack_half8(v);
+                    *reinterpret_cast<uint4 *>(sA + tc_op_off(tid, c / 8 + 1)) = pack_half8(v + 8);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) y = fmaf(W4[c + j], v[j], y);
+                }
+            }
+            tc_fence_before();
+        }
+        if (ok && row < n) Y[row] = y + B4[0];
+    }
+    // a timed-out wait may leave MMAs in flight: wait for the last commit
+    // (bounded again) before the tensor memory is released; if that runs out
+    // too, the tensor memory stays allocated and the status says so (2)
+    bool drained = true;
+    if (!ok && commits > 0) drained = __syncthreads_and(mbar_wait(&bar, (commits - 1) & 1u));
+    if (!ok && tid == 0) atomicExch(status, drained ? 1 : 2);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0 && drained) tmem_dealloc(tmem, kWide);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- host model
 struct Mlp {
+    int width = kWidth;
+    int dims[kLayers + 1] = {kIn, kWidth, kWidth, kWidth, 1};
     // flat parameter vector: for each layer W (out x in) then b (out)
     std::vector<size_t> woff, boff;
     size_t nparam = 0;
     float *d_p = nullptr, *d_g = nullptr, *d_m = nullptr, *d_v = nullptr;
+    int *d_status = nullptr;  // tensor-core inference: 1 (2) when a wait ran out (and the tensor memory was kept)
     int adam_t = 0;
     bool ready = false;
 
     void layout()
     {
+        dims[1] = dims[2] = dims[3] = width;
         woff.assign(kLayers, 0);
         boff.assign(kLayers, 0);
         size_t o = 0;
         for (int l = 0; l < kLayers; ++l) {
             woff[l] = o;
-            o += (size_t)kDims[l + 1] * kDims[l];
+            o += (size_t)dims[l + 1] * dims[l];
             boff[l] = o;
-            o += kDims[l + 1];
+            o += dims[l + 1];
         }
         nparam = o;
+    }
+    void release()
+    {
+        for (float **q : {&d_p, &d_g, &d_m, &d_v})
+            if (*q) {
+                cudaFree(*q);
+                *q = nullptr;
+            }
+        if (d_status) cudaFree(d_status);
+        d_status = nullptr;
+        ready = false;
     }
 };
 
 static Mlp g_mlp;
+
+// Hidden width 64 or 128; the parameters are dropped (initialise or load new ones).
+cudaError_t mlp_set_width(int width)
+{
+    if (width != kWidth && width != kWide) return cudaErrorInvalidValue;
+    if (width == g_mlp.width) return cudaSuccess;
+    g_mlp.release();
+    g_mlp.width = width;
+    g_mlp.layout();
+    return cudaSuccess;
+}
+
+int mlp_width() { return g_mlp.width; }
+
+// Status of the tensor-core inference since the last call (0: fine), reset.
+int mlp_take_status()
+{
+    if (!g_mlp.d_status) return 0;
+    int v = 0;
+    if (cudaMemcpy(&v, g_mlp.d_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    if (v) cudaMemset(g_mlp.d_status, 0, sizeof(int));
+    return v;
+}
 
 static cudaError_t mlp_alloc()
 {
@@ -298,6 +502,8 @@ static cudaError_t mlp_alloc()
     if (e == cudaSuccess) e = cudaMalloc(&g_mlp.d_g, g_mlp.nparam * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&g_mlp.d_m, g_mlp.nparam * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&g_mlp.d_v, g_mlp.nparam * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&g_mlp.d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(g_mlp.d_status, 0, sizeof(int));
     return e;
 }
 
@@ -315,9 +521,9 @@ cudaError_t mlp_init(unsigned seed)
     std::vector<float> p(g_mlp.nparam, 0.0f);
     std::mt19937 rng(seed);
     for (int l = 0; l < kLayers; ++l) {
-        const float lim = std::sqrt(6.0f / (float)kDims[l]);
+        const float lim = std::sqrt(6.0f / (float)g_mlp.dims[l]);
         std::uniform_real_distribution<float> u(-lim, lim);
-        for (size_t k = 0; k < (size_t)kDims[l + 1] * kDims[l]; ++k) p[g_mlp.woff[l] + k] = u(rng);
+        for (size_t k = 0; k < (size_t)g_mlp.dims[l + 1] * g_mlp.dims[l]; ++k) p[g_mlp.woff[l] + k] = u(rng);
     }
     e = cudaMemcpy(g_mlp.d_p, p.data(), p.size() * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(g_mlp.d_m, 0, g_mlp.nparam * sizeof(float));
@@ -358,8 +564,8 @@ struct Acts {
         release();
         B = b;
         for (int l = 0; l <= kLayers; ++l) {
-            cudaError_t e = cudaMalloc(&a[l], (size_t)b * kDims[l] * sizeof(float));
-            if (e == cudaSuccess) e = cudaMalloc(&d[l], (size_t)b * kDims[l] * sizeof(float));
+            cudaError_t e = cudaMalloc(&a[l], (size_t)b * g_mlp.dims[l] * sizeof(float));
+            if (e == cudaSuccess) e = cudaMalloc(&d[l], (size_t)b * g_mlp.dims[l] * sizeof(float));
             if (e != cudaSuccess) return e;
         }
         return cudaSuccess;
@@ -377,7 +583,7 @@ struct Acts {
 static void forward(Acts &A, int B, cudaStream_t s)
 {
     for (int l = 0; l < kLayers; ++l) {
-        const int in = kDims[l], out = kDims[l + 1];
+        const int in = g_mlp.dims[l], out = g_mlp.dims[l + 1];
         k_dense_fwd<<<tiles(out, B), dim3(kT, kT), 0, s>>>(A.a[l], g_mlp.d_p + g_mlp.woff[l], g_mlp.d_p + g_mlp.boff[l],
                                                             A.a[l + 1], B, in, out, l + 1 < kLayers);
     }
@@ -389,7 +595,7 @@ static void backward(Acts &A, const float *y, float *se, int B, cudaStream_t s)
 {
     k_mse<<<(B + 255) / 256, 256, 0, s>>>(A.a[kLayers], y, A.d[kLayers], se, B);
     for (int l = kLayers - 1; l >= 0; --l) {
-        const int in = kDims[l], out = kDims[l + 1];
+        const int in = g_mlp.dims[l], out = g_mlp.dims[l + 1];
         k_dense_bwd_w<<<tiles(in, out), dim3(kT, kT), 0, s>>>(A.d[l + 1], A.a[l], g_mlp.d_g + g_mlp.woff[l], B, in,
                                                               out);
         k_bias_grad<<<out, 256, 0, s>>>(A.d[l + 1], g_mlp.d_g + g_mlp.boff[l], B, out);
@@ -496,12 +702,28 @@ cudaError_t mlp_train(const float *X, const float *y, int n, int epochs, int bat
     return e;
 }
 
-// Predicted log2(1 + rank) of n descriptor rows (device arrays), on stream s,
-// by the fused inference kernel.
+// Predicted log2(1 + rank) of n descriptor rows (device arrays, X 16-byte
+// aligned), on stream s, by the fused inference kernel of the width.
 cudaError_t mlp_infer_dev(const float *dX, int n, float *dY, cudaStream_t s)
 {
     if (!g_mlp.ready) return cudaErrorInvalidValue;
     if (n <= 0) return cudaSuccess;
+    if (g_mlp.width == kWide) {
+        static bool attr_tc = false;
+        if (!attr_tc) {
+            const cudaError_t e =
+                cudaFuncSetAttribute(k_mlp128_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+            if (e != cudaSuccess) return e;
+            attr_tc = true;
+        }
+        int dev = 0, nsm = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        const int ntiles = (n + kTcRows - 1) / kTcRows;
+        k_mlp128_tc<<<std::max(1, std::min(nsm, ntiles)), kTcRows, kTcSmem, s>>>(g_mlp.d_p, dX, n, dY, g_mlp.d_status);
+        return cudaGetLastError();
+    }
     static bool attr = false;
     if (!attr) {
         const cudaError_t e =

@@ -1054,6 +1054,13 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     C.stats_pending = true;
 }
 
+// a failed wait in the tensor-core inference kernel becomes an error
+static void check_mlp_status()
+{
+    const int st = mlp_take_status();
+    if (st) fail(-10, "network inference on the tensor cores timed out (status %d)", st);
+}
+
 // Statistics, timings and (select 1) training samples of the last build,
 // once the stream has passed it.
 void finish_compression()
@@ -1061,6 +1068,7 @@ void finish_compression()
     Compression &C = g.cmp;
     if (!C.stats_pending) return;
     C.stats_pending = false;
+    if (C.select == 2) check_mlp_status();
     std::vector<double> part((size_t)kCmpStats * cmp_stats_parts());
     CK(cudaMemcpy(part.data(), C.d_stats, part.size() * sizeof(double), cudaMemcpyDeviceToHost));
     double st[kCmpStats] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
@@ -2161,6 +2169,17 @@ long long sonar_fragment_triangle(const float *tri9, float delta, int *nx_ny_neg
 // ---- admissibility network
 int sonar_mlp_param_count(void) { return (int)mlp_param_count(); }
 
+int sonar_mlp_set_width(int width)
+{
+    return guarded([&] {
+        if (mlp_set_width(width) != cudaSuccess) fail(-6, "network width %d (64 or 128)", width);
+        g.cmp.release();
+    });
+}
+
+int sonar_mlp_width(void) { return mlp_width(); }
+
+
 int sonar_mlp_init(unsigned seed)
 {
     return guarded([&] {
@@ -2228,6 +2247,7 @@ int sonar_mlp_predict(const float *X, int n, float *out)
         dfree(dX);
         dfree(dY);
         if (e != cudaSuccess) fail(-10, "network inference failed: %s", cudaGetErrorString(e));
+        check_mlp_status();
     });
 }
 

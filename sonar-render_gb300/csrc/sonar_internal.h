@@ -258,9 +258,12 @@ int cmp_stats_parts();
 void launch_cmp_stats(const int *nkeep, const int2 *ab, const int *rank, const float *err, int nsrc, double *out,
                       cudaStream_t s, const uint8_t *lev = nullptr);
 void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s);
-// mlp.cu: the admissibility network (8 -> 128 -> 128 -> 128 -> 1, ReLU, FP32)
+// mlp.cu: the admissibility network (8 -> w -> w -> w -> 1, ReLU; w = 64 or 128)
 size_t mlp_param_count();
 bool mlp_ready();
+cudaError_t mlp_set_width(int width);  // 64 or 128 (drops the parameters)
+int mlp_width();
+int mlp_take_status();                 // tensor-core inference: 0 fine, 1 a wait ran out, 2 and TMEM kept
 cudaError_t mlp_init(unsigned seed);
 cudaError_t mlp_set_params(const float *p, size_t n);
 cudaError_t mlp_get_params(float *p, size_t n);

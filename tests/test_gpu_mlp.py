@@ -49,6 +49,39 @@ def test_forward_and_gradient_match_oracle(adm, oracle_mod):
         off += n
 
 
+def test_width128_tensor_core_inference_and_gradient(adm, oracle_mod):
+    """Width 128: FP16 hidden layers on the tensor cores (tcgen05.mma, FP32
+    accumulation) against the FP64 forward -- the FP16 rounding of
+    activations and weights (2^-11 relative) bounds the error, 5e-3 relative
+    L2 -- over more rows than one 128-row tile and a ragged last tile; the
+    FP32 training kernels' gradient within 1e-4 of the FP64 one."""
+    adm.set_width(128)
+    oracle_mod.mlp_set_width(128)
+    try:
+        assert adm.width() == 128
+        adm.init(7)
+        p = adm.get_params()
+        assert len(p) == oracle_mod.mlp_param_count() == 8 * 128 + 128 + 2 * (128 * 128 + 128) + 128 + 1
+        rng = np.random.default_rng(12)
+        X = rng.uniform(0.0, 4.0, (1000, 8)).astype(np.float32)
+        y = rng.standard_normal(1000).astype(np.float32)
+        pred = adm.predict(X)
+        ref = oracle_mod.mlp_forward(p, X)
+        e_fwd = rel_l2(pred, ref)
+        loss, g = adm.grad(X[:300], y[:300])
+        loss_ref, g_ref = oracle_mod.mlp_grad(p, X[:300], y[:300])
+        e_grad = rel_l2(g, g_ref)
+        print("width 128: tensor-core FP16 forward rel L2 %.2e (max abs %.2e), FP32 gradient rel L2 %.2e"
+              % (e_fwd, np.abs(pred - ref).max(), e_grad))
+        assert e_fwd < 5e-3
+        assert e_grad < 1e-4
+        # a second call gives the same bits (one tile per CTA, fixed order)
+        assert np.array_equal(adm.predict(X), pred)
+    finally:
+        adm.set_width(64)
+        oracle_mod.mlp_set_width(64)
+
+
 def test_training_fits_a_smooth_function(adm):
     rng = np.random.default_rng(2)
     X = rng.uniform(-1, 1, (4096, 8)).astype(np.float32)

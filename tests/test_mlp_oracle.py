@@ -1,13 +1,23 @@
-"""The FP64 oracle of the admissibility network: its backward pass against
-central finite differences of its own forward pass (pins the oracle the GPU
-kernels are checked against)."""
+"""The FP64 oracle of the admissibility network (hidden width 64 and 128):
+its backward pass against central finite differences of its own forward
+pass (pins the oracle the GPU kernels are checked against)."""
 import numpy as np
+import pytest
 
 
-def test_oracle_gradient_matches_finite_differences(oracle_mod):
+@pytest.mark.parametrize("width", [64, 128])
+def test_oracle_gradient_matches_finite_differences(oracle_mod, width):
     rng = np.random.default_rng(5)
+    oracle_mod.mlp_set_width(width)
+    try:
+        _check(oracle_mod, rng, width)
+    finally:
+        oracle_mod.mlp_set_width(64)
+
+
+def _check(oracle_mod, rng, w):
     n = oracle_mod.mlp_param_count()
-    assert n == 8 * 64 + 64 + 2 * (64 * 64 + 64) + 64 + 1
+    assert n == 8 * w + w + 2 * (w * w + w) + w + 1
     p = (rng.standard_normal(n) * 0.2).astype(np.float32)
     X = rng.standard_normal((6, 8)).astype(np.float32)
     y = rng.standard_normal(6).astype(np.float32)
