@@ -28,6 +28,7 @@
 // cross approximation's (gathered by k_lr_gather).
 #include "sonar_internal.h"
 #include "green.cuh"
+#include "tc05.cuh"
 
 namespace sonar {
 namespace {
@@ -252,6 +253,7 @@ struct __align__(16) IpShared {
     float red[2][2];
     float2 eD;  // e^{i k D}
     int si[kIpCols], sj[kIpRows];
+    __align__(8) uint64_t cbar;  // the apply: the node entries' bulk copy
 };
 static_assert(sizeof(IpShared) <= 48 * 1024, "static shared memory");
 // scratch in the weight grids: the node offset tables ((2 x 48 + 2 x 12)
@@ -497,8 +499,16 @@ __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const i
             S.cs[bj * kIpSPitch + ai] = make_float2(val, 0.0f);
             cst[nc + bj * kIpSPitch + ai] = make_float2(val, 0.0f);
         }
-    } else {
-        ip_load_entries(S, cst, P);
+    } else if (t == 0) {
+        // the stored node entries come in by bulk copies while the tables,
+        // weights and projections are computed; waited for at the coupling
+        const uint32_t nb4 = (uint32_t)ip_smooth_at(P) * sizeof(float2);
+        const uint32_t sb4 = (uint32_t)(kIpSmooth * kIpSPitch) * sizeof(float2);
+        mbar_init(&S.cbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_expect_tx(&S.cbar, nb4 + sb4);
+        bulk_g2s(S.c, cst, nb4, &S.cbar);
+        bulk_g2s(S.cs, cst + ip_smooth_at(P), sb4, &S.cbar);
     }
     __syncthreads();
     if (BUILD) {
@@ -650,6 +660,12 @@ __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const i
         float2 acc = make_float2(0.0f, 0.0f);
         for (int y = 0; y < by; ++y) acc = rfma(S.st[s][y][ay], S.ys[s][ax][y], acc);
         S.gs[s][k] = acc;
+    }
+    if (!BUILD && !mbar_wait(&S.cbar, 0)) {
+        // the copy did not arrive in time: wait once more (bounded) so that it
+        // cannot land after the CTA is gone, and report the block
+        if (!mbar_wait(&S.cbar, 0) && t == 0 && ip.status) atomicExch(ip.status, 2);
+        else if (t == 0 && ip.status) atomicExch(ip.status, 1);
     }
     __syncthreads();
     // coupling, two threads per node (even / odd terms, then a lane swap):
@@ -844,7 +860,7 @@ void launch_ip_build(const SumArgs &a, const float4 *tile, const uint16_t *fxy, 
 void launch_ip_apply(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,
                      const int2 *blocks, const long long *off, const int *bidx, int nb, const int *ndev,
                      const float2 *store, float2 *brow, float2 *bcol, cudaStream_t s, const int *list, int nlist,
-                     const int *rank)
+                     const int *rank, int *status)
 {
     if (list) {
         nb = nlist;
@@ -856,6 +872,7 @@ void launch_ip_apply(const SumArgs &a, const float4 *tile, const uint16_t *fxy, 
     ip.fxy = fxy;
     ip.lev = lev;
     ip.delta = delta;
+    ip.status = status;
     float2 *st = const_cast<float2 *>(store);  // read only in the apply
     if (a.ka != 0.0f)
         k_ip<true, false><<<nb, kIpThreads, 0, s>>>(a, ip, blocks, off, bidx, ndev, nb, 0.0f, st,

@@ -3337,7 +3337,7 @@ void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off,
             cudaEventRecord(ip->fork, s);
             cudaStreamWaitEvent(ip->stream, ip->fork, 0);
             launch_ip_apply(a, ip->tile, ip->fxy, ip->lev, ip->delta, blocks, off, bidx, nb, ndev, U, brow, bcol,
-                            ip->stream, ip->list, ip->n, rank);
+                            ip->stream, ip->list, ip->n, rank, ip->status);
             cudaEventRecord(ip->join, ip->stream);
         }
         if (nl > 0) {
@@ -3352,7 +3352,7 @@ void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off,
             cudaStreamWaitEvent(s, ip->join, 0);
         else if (ip)
             launch_ip_apply(a, ip->tile, ip->fxy, ip->lev, ip->delta, blocks, off, bidx, nb, ndev, U, brow, bcol, s,
-                            ip->list, ip->n, rank);
+                            ip->list, ip->n, rank, ip->status);
     }
     if (ntiles > 0)
         k_lr_gather<<<ntiles, kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, bidx, yrow, ycol);

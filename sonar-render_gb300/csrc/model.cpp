@@ -905,7 +905,7 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
                        Arena::bytes_of((size_t)kCmpStats * cmp_stats_parts(), sizeof(double)) +
                        Arena::bytes_of((size_t)kIpTileRec * nt, sizeof(float4)) + Arena::bytes_of(M.nsrc, sizeof(uint16_t)) +
                        2 * Arena::bytes_of(nmax, 1) + 2 * Arena::bytes_of(nmax, sizeof(int)) +
-                       2 * Arena::bytes_of(nb + 1, sizeof(int)) + 8192;
+                       2 * Arena::bytes_of(nb + 1, sizeof(int)) + Arena::bytes_of(1, sizeof(int)) + 8192;
         C.arena.reserve(bytes);
     }
     Arena &ar = C.arena;
@@ -924,6 +924,8 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
                         const_cast<float4 *>(C.ip.tile), fxy, st);
         C.ip.fxy = fxy;
         C.ip.delta = A.delta;
+        C.ip.status = ar.take<int>(1);
+        CK(cudaMemsetAsync(C.ip.status, 0, sizeof(int), st));
     }
     // ---- candidates
     int *d_ccnt = ar.take<int>(nb), *d_coff = ar.take<int>(nb + 1);
@@ -1293,6 +1295,11 @@ void run_hop(int hop, int a, int b)
     CK(cudaGetLastError());
     CK(cudaEventRecord(g.ev1, st));
     CK(cudaEventSynchronize(g.ev1));
+    if (rec_cmp && g.cmp.interp && g.cmp.ip.status) {
+        int ist = 0;
+        CK(cudaMemcpy(&ist, g.cmp.ip.status, sizeof(int), cudaMemcpyDeviceToHost));
+        if (ist) fail(-10, "interpolated blocks: a node-entry copy %s", ist == 2 ? "did not arrive" : "arrived late");
+    }
     if (built) {
         finish_compression();
         rec_cmp_build = g.cmp.build_ms;

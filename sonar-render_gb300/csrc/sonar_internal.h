@@ -200,6 +200,7 @@ struct IpCtx {
     // the interpolated kept blocks (n of them)
     const int *list = nullptr;
     int n = 0;
+    int *status = nullptr;  // apply: 1 when a node-entry copy arrived late, 2 when not at all
     // optional: the apply runs on this stream beside the factor blocks
     // (fork / join: events the launcher records to order the two)
     cudaStream_t stream = nullptr;
@@ -222,7 +223,7 @@ void launch_ip_build(const SumArgs &a, const float4 *tile, const uint16_t *fxy, 
 void launch_ip_apply(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,
                      const int2 *blocks, const long long *off, const int *bidx, int nb, const int *ndev,
                      const float2 *store, float2 *brow, float2 *bcol, cudaStream_t s, const int *list = nullptr,
-                     int nlist = 0, const int *rank = nullptr);
+                     int nlist = 0, const int *rank = nullptr, int *status = nullptr);
 // full-tile relative RMS error of sampled accepted interpolated blocks (no attenuation)
 void launch_ip_audit(const SumArgs &a, const float4 *tile, const uint16_t *fxy, const uint8_t *lev, float delta,
                      const int2 *blocks, const long long *off, const int *sample, int ns, const float2 *store,

@@ -75,6 +75,24 @@ __device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t adesc, uint64_t bd
         : "memory");
 }
 
+// arrive on bar (one of its expected arrivals) and add `bytes` to the
+// transaction count the phase waits for
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// bulk copy global -> this CTA's shared memory, completion counted on bar
+// (both addresses 16-byte aligned, bytes a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 // arrive on bar once every tcgen05 operation issued so far by this thread completed
 __device__ __forceinline__ void mma_commit(uint64_t *bar)
 {
