@@ -317,27 +317,34 @@ def hbm_peak():
 
 
 def lowrank_roofline(stats):
-    """The low-rank apply (k_lr_block + k_lr_gather) is HBM-bound: per
-    accepted block the factors U, V (rank x 256 complex FP32 each) are read
-    once and 2 x 256 complex FP32 outputs written and read back; the gather
-    writes 2 x 16 bytes per fragment."""
+    """The second bounce's apply of the accepted blocks: the factor blocks
+    (k_lr_block) are HBM-bound -- per block U, V (rank x 256 complex FP32
+    each) read once -- the interpolated blocks' (k_ip apply) read their node
+    entries ((P (P | 1) + 156) complex FP32) and are bound by FP32 issue;
+    every block writes 2 x 256 complex FP32 outputs that the gather reads
+    back.  The figure is the HBM rate of these bytes over the whole apply."""
     hops = [h for h in stats["hops"] if h["hop"] == 2 and h.get("lr_ms")]
     if not hops:
         return None
     h = hops[0]
     nacc = h["cmp_accepted"]
-    bytes_launch = nacc * (h["cmp_mean_rank"] * 256 * 8 * 2 + 256 * 8 * 2 * 2)
+    nip = h.get("cmp_ip_blocks", 0)
+    P = h.get("cmp_ip_nodes", 0.0)
+    factor_bytes = (nacc - nip) * h["cmp_mean_rank"] * 256 * 8 * 2
+    node_bytes = nip * (P * (int(P) | 1) + 156) * 8
+    bytes_launch = factor_bytes + node_bytes + nacc * 256 * 8 * 2 * 2
     ms = sum(x["lr_ms"] for x in hops) / len(hops)
     peak, src = hbm_peak()
     ach = bytes_launch / (ms * 1e-3) / 1e9
     # k_lr_block's DRAM bytes were 0.985 x these algorithmic bytes in the ncu
     # capture on the 40 kHz trihedral at tolerance 5e-4 (1.141 GB for 19,502
     # blocks at rank 13.5)
-    return {"kernel": "k_lr_block + k_lr_gather (low-rank apply)", "bound": "hbm", "achieved": round(ach, 1),
+    return {"kernel": "k_lr_block + k_ip apply + k_lr_gather (second bounce's apply of the accepted blocks)",
+            "bound": "hbm for the factor blocks; fp32 issue for the interpolated ones", "achieved": round(ach, 1),
             "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": round(0.985 * bytes_launch),
             "traffic_source": "ncu dram bytes of k_lr_block on the 40 kHz capture, scaled by algorithmic bytes",
             "bytes_per_launch": int(bytes_launch), "launch_ms": round(ms, 4), "peak_source": src,
-            "blocks": nacc, "mean_rank": h["cmp_mean_rank"]}
+            "blocks": nacc, "interpolated_blocks": nip, "mean_rank": h["cmp_mean_rank"]}
 
 
 def aca_roofline(stats, fp32_peak):
@@ -353,7 +360,7 @@ def aca_roofline(stats, fp32_peak):
         return None
     h = hops[0]
     k = h["cmp_mean_rank"]
-    nb = h["cmp_blocks"]
+    nb = h["cmp_blocks"] - h.get("cmp_ip_blocks", 0)  # the interpolated blocks have their own kernel
     flop_block = 48.0 * (2 * 256 * k + 512) + 8.0 * 256 * k * (k - 1) + 8.0 * 512 * k + 8.0 * 4 * 256 * k
     ms = sum(x["cmp_aca_ms"] for x in hops) / len(hops)
     ach = nb * flop_block / (ms * 1e-3) / 1e12
@@ -369,6 +376,41 @@ def aca_roofline(stats, fp32_peak):
             "traffic": round(traffic), "traffic_source": "ncu dram bytes of the 40 kHz capture, scaled by blocks x rank",
             "blocks_per_launch": nb, "mean_rank": k, "flop_per_block": round(flop_block),
             "launch_ms": round(ms, 4), "peak_source": "FP32 FMA rate measured now by sonar_measure_peak"}
+
+
+def ip_roofline(stats, fp32_peak):
+    """Directional interpolation build (k_ip<BUILD>: node entries, judge and
+    the first bounce's apply), FP32 work per launch.  Per interpolated block
+    of P nodes (px x py, px = sqrt(1.4 P) for the mean level) and the 4 x 3
+    smooth nodes: (P^2 + 144) node entries at 45 flop; the judge, 8 P^2 +
+    96 x 12 complex MACs (8 flop) and 64 exact entries at 48 flop; the apply,
+    per side a projection and an expansion over the 16 x 16 occupied cells
+    (16 x 16 x px + P x 16 complex MACs each) and the smooth part's
+    (16 x 16 x 4 + 12 x 16 real x complex, 4 flop), and the couplings 2 P^2
+    complex and 2 x 144 real x complex MACs."""
+    hops = [h for h in stats["hops"] if h["hop"] == 2 and h.get("cmp_ip_ms")]
+    if not hops or not fp32_peak or not hops[0].get("cmp_ip_blocks"):
+        return None
+    h = hops[0]
+    P = h["cmp_ip_nodes"]
+    nb = h["cmp_ip_blocks"]
+    px = (1.4 * P) ** 0.5
+    apply = 8.0 * 4 * (256 * px + 16 * P) + 4.0 * 4 * (256 * 4 + 12 * 16) + 8.0 * 2 * P * P + 4.0 * 2 * 144
+    flop_block = 45.0 * (P * P + 144) + 8.0 * (8 * P * P + 96 * 12) + 48.0 * 64 + apply
+    ms = sum(x["cmp_ip_ms"] for x in hops) / len(hops)
+    ach = nb * flop_block / (ms * 1e-3) / 1e12
+    peak = fp32_peak / 1e12
+    # DRAM: the node entries written once; the ncu capture at 40 kHz wrote
+    # 88.6 MB for 8,158 blocks of mean 39.6 nodes (10.9 KB per block), here
+    # scaled by the stored entries per block
+    traffic = nb * (P * P + 156) * 8.0 * (88.6e6 / (8158 * (39.6 * 39.6 + 156) * 8.0))
+    return {"kernel": "k_ip build (directional interpolation: node entries + 8 x 8 exact-entry judge + first bounce's "
+                      "apply)", "bound": "fp32 issue / barrier latency (seven dependent phases per block)",
+            "achieved": round(ach, 3), "peak": round(peak, 3), "unit": "TFLOP/s", "frac": round(ach / peak, 4),
+            "traffic": round(traffic), "traffic_source": "ncu dram bytes of the 40 kHz capture per stored entry",
+            "blocks_per_launch": nb, "mean_nodes": P, "flop_per_block": round(flop_block),
+            "launch_ms": round(ms, 4), "timed": "its own stream's span, beside the cross approximation on another",
+            "peak_source": "FP32 FMA rate measured now by sonar_measure_peak"}
 
 
 def e2e_path(api, cfg, args, world, pairs_step):
@@ -929,10 +971,15 @@ def run_gb300(args):
     if roof_lr:
         roof_lr["timed"] = "alone (one stream), operator reused; the headline step overlaps it with the dense remainder"
     roof_aca = aca_roofline(st, fp32_peak) if head == "compressed" else None
+    roof_ip = ip_roofline(st, fp32_peak) if head == "compressed" else None
     # the roofline object describes the dominant kernel of the headline step
-    dominant = max(kms, key=kms.get) if kms else None
+    # (not the two approximation kernels' joint span)
+    single = {k: v for k, v in kms.items() if k != "approximation_both"}
+    dominant = max(single, key=single.get) if single else None
     if dominant == "cross_approx" and roof_aca:
         roof_main = roof_aca
+    elif dominant == "interpolation" and roof_ip:
+        roof_main = roof_ip
     elif dominant == "lowrank_apply" and roof_lr:
         roof_main = roof_lr
     else:
@@ -951,7 +998,7 @@ def run_gb300(args):
                            "plain FP32 sums + interaction masks (rebuilt every step)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": roof_main, "roofline_bounce_sum": roof_sym, "roofline_lowrank": roof_lr,
-        "roofline_cross_approx": roof_aca, "dominant_kernel": dominant,
+        "roofline_cross_approx": roof_aca, "roofline_interpolation": roof_ip, "dominant_kernel": dominant,
         "kernel_ms_per_step": kms, "kernel_share": kshare,
         "compression": compression,
         "mask_block_classes": mask_classes,
