@@ -130,3 +130,32 @@ def test_interpolated_audit_full_tiles(api, scenes):
     assert hop["cmp_ip_blocks"] > 0
     assert len(full) == 256 and np.all(np.isfinite(full))
     assert full.max() < 3 * limit
+
+
+def _scene(targets, f, sources):
+    cp = 1480.0
+    return dict(cp=cp, f=f, att=0.0, bounces=2, field_objects=False, sources=np.asarray(sources, np.float32),
+                field_points=np.array([[0.0, 0.0, 5.0]], np.float32), targets=targets, fields=[])
+
+
+def test_interpolation_between_facing_plates(api, oracle_mod, scenes):
+    """Two parallel 1 x 1 m plates facing each other 0.8 m apart at 40 kHz,
+    the source between them: tiles are whole 16 x 16 patches or two half
+    patches of a triangle; the interpolated bounce matches the plain one and
+    the FP64 oracle."""
+    d = scenes.delta_for(40e3)
+    lower = scenes.rectangle(1.0, 1.0, z=0.0, normal_up=True)
+    upper = scenes.rectangle(1.0, 1.0, z=0.8, normal_up=False)
+    sc = _scene([(np.concatenate([lower, upper]), d)], 40e3, [[0.1, -0.05, 0.4]])
+    P0, P_plain, _ = _run(api, sc, 0)
+    _, P_ip, hop = _run(api, sc, 1)
+    e_plain = rel_l2(P_ip - P0, P_plain - P0)
+    print("facing plates: %d interpolated blocks (mean nodes %.1f) of %d accepted; vs plain %.3e"
+          % (hop["cmp_ip_blocks"], hop["cmp_ip_nodes"], hop["cmp_accepted"], e_plain))
+    # the tiles across the rectangles' diagonals (two facets) stay with the cross approximation
+    assert 500 < hop["cmp_ip_blocks"] < hop["cmp_accepted"]
+    assert e_plain < 1e-3
+    Q0, Q1, _ = _run(api, sc, 1, bounces=1)
+    e = _one_bounce_vs_oracle(oracle_mod, sc, Q0, Q1, 93)
+    print("facing plates, one bounce vs FP64 oracle: rel L2 %.3e" % e)
+    assert e < 1e-3
