@@ -391,7 +391,7 @@ __device__ __forceinline__ void ip_load_entries(IpShared &S, const float2 *cst, 
 // packed inputs; otherwise accepted block bidx[blockIdx.x] with the stored
 // entries, apply only.  Blocks of level 0 belong to the cross approximation.
 template <bool ATT, bool BUILD>
-__global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const int2 *blocks, const long long *off,
+__global__ void __launch_bounds__(kIpThreads, 5) k_ip(SumArgs a, IpArgs ip, const int2 *blocks, const long long *off,
                                                    const int *bidx, const int *ndev, int n, float limit,
                                                    float2 *store, int *rank, float *fro, float *err, float2 *brow,
                                                    float2 *bcol, const int *list)
@@ -672,21 +672,35 @@ __global__ void __launch_bounds__(kIpThreads) k_ip(SumArgs a, IpArgs ip, const i
     // into J (forward) from the nodes of I, into I (reciprocal) from those of J
     if (t < 2 * kIpMaxNodes) {
         const int bj = t >> 1, h0 = t & 1;
-        float2 acc = make_float2(0.0f, 0.0f);
+        float2 acc = make_float2(0.0f, 0.0f), acc2 = acc;
         if (bj < P) {
             const float2 *cr = S.c + bj * (P | 1);
-#pragma unroll 4
-            for (int ai = h0; ai < P; ai += 2) acc = cfma(cr[ai], S.g[0][ai], acc);
+            int ai = h0;
+#pragma unroll 2
+            for (; ai + 2 < P; ai += 4) {
+                acc = cfma(cr[ai], S.g[0][ai], acc);
+                acc2 = cfma(cr[ai + 2], S.g[0][ai + 2], acc2);
+            }
+            if (ai < P) acc = cfma(cr[ai], S.g[0][ai], acc);
+            acc.x += acc2.x;
+            acc.y += acc2.y;
         }
         acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 1);
         acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 1);
         if (bj < P && h0 == 0) S.h[1][bj] = cmul(acc, S.eD);
     } else if (t >= 128 && t < 128 + 2 * kIpMaxNodes) {
-        const int ai = (t - 128) >> 1, h0 = t & 1;
-        float2 acc = make_float2(0.0f, 0.0f);
+        const int ai = (t - 128) >> 1, h0 = t & 1, cp = P | 1;
+        float2 acc = make_float2(0.0f, 0.0f), acc2 = acc;
         if (ai < P) {
-#pragma unroll 4
-            for (int bj = h0; bj < P; bj += 2) acc = cfma(S.c[bj * (P | 1) + ai], S.g[1][bj], acc);
+            int bj = h0;
+#pragma unroll 2
+            for (; bj + 2 < P; bj += 4) {
+                acc = cfma(S.c[bj * cp + ai], S.g[1][bj], acc);
+                acc2 = cfma(S.c[(bj + 2) * cp + ai], S.g[1][bj + 2], acc2);
+            }
+            if (bj < P) acc = cfma(S.c[bj * cp + ai], S.g[1][bj], acc);
+            acc.x += acc2.x;
+            acc.y += acc2.y;
         }
         acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 1);
         acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 1);
