@@ -469,6 +469,22 @@ def batch_leg(args, flush, rank):
     st = plan.stats()
     ms = statistics.median(dev)
     pairs = st["pairs"]
+    # the same runs with the centroid-relative phase (FP64 point offsets from
+    # each scene's box centre): its device time and its result
+    plan.set_relative(True)
+    for _ in range(max(args.warmup, 1)):
+        plan.run(copy=False)
+    dev_rel, gemm_rel = [], []
+    for _ in range(max(args.steps, 1)):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        plan.run(copy=False)
+        sr = plan.stats()
+        dev_rel.append(sr["vis_ms"] + sr["gemm_ms"] + sr["reduce_ms"])
+        gemm_rel.append(sr["gemm_ms"])
+    out_rel = plan.run()
+    plan.set_relative(False)
+    ms_rel = statistics.median(dev_rel)
     # e2e through the reused plan, as a sequence of pings at the same scenes:
     # each run uploads its source and receiver positions from host memory,
     # runs the graph and reads the result back
@@ -501,7 +517,7 @@ def batch_leg(args, flush, rank):
     d2h = int(out.size * 16)
     err = None
     if rank == 0:
-        err = batch_error(cfg, out, st)
+        err = batch_error(cfg, out, out_rel, st)
     # tensor-core work of the run: 3 split products x 2 (real embedding)
     # x 2 flop per MAC over the 128 x 64 x (2 K) products
     flops = 3 * 2 * 128 * 64 * 2 * nfrag
@@ -519,7 +535,11 @@ def batch_leg(args, flush, rank):
            "e2e_one_shot": {"value": pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                             "s_per_step": round(e2e_s, 4), "path": "sonar_run_batch: plan, tune (cached), run, free"},
            "generation": gen,
-           "rel_err_vs_fp64": err, "dtype": "split bf16 x3, fp32 accumulate, fp64 reduce",
+           "relative_phase": {"ms_per_run": round(ms_rel, 4), "slowdown": round(ms_rel / ms - 1.0, 4),
+                              "gemm_ms": round(statistics.median(gemm_rel), 4),
+                              "path": "sonar_batch_set_relative(plan, 1): points as FP64 offsets from the scene's "
+                                      "box centre, k R reduced on the host"},
+           "rel_err_vs_fp64": err, "dtype": "split bf16 x3, fp32 accumulate, compensated reduce combined in fp64",
            "l2": "flushed between runs (256 MB write)"}
     plan.close()
     return res
@@ -737,38 +757,56 @@ def config_error(api, cfg, name):
         return {"rel_err_vs_fp64": {"failed": str(ex)}}
 
 
-def batch_error(cfg, out, st):
+def batch_error(cfg, out, out_rel, st):
     """Relative L2 error of sampled (scene, frequency) items, 4 sources each,
-    against the FP64 oracle's per-source runs."""
+    against the FP64 oracle's per-source runs: the default run against the
+    oracle's restatement of the reference's FP32 distances (parity), and
+    both runs (default and centroid-relative phase) against its exact
+    geometry (FP64 distances from the same FP32 positions)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     try:
         nf = len(cfg["freqs"])
         nfr = st["item_fragments"]
         rng = np.random.default_rng(11)
-        # the items with the fewest fragments above 1,000 (the oracle is serial per source)
-        order = [i for i in np.argsort(nfr) if nfr[i] >= 1000][:3]
-        errs = {}
+        # the items with the fewest fragments above 1,000 (the oracle is serial per source),
+        # and at the top frequency, where the phase rounding of FP32 distances is largest,
+        # the smallest item and the smallest plate
+        order = [int(i) for i in np.argsort(nfr) if nfr[i] >= 1000][:3]
+        top = [i for i in np.argsort(nfr) if int(i) % nf == nf - 1]
+        plates = [i for i in top if cfg["kinds"][int(i) // nf] == "plate"]
+        for i in top[:1] + plates[:1]:
+            if int(i) not in order:
+                order.append(int(i))
+        errs, exact_abs, exact_rel = {}, {}, {}
         for it in order:
             s, k = int(it) // nf, int(it) % nf
             f = float(cfg["freqs"][k])
             delta = float(np.float32(cfg["cp"]) / np.float32(f) / np.float32(cfg["per_wavelength"]))
             qs = np.sort(rng.choice(len(cfg["sources"]), 4, replace=False))
-            ref = np.zeros((len(cfg["receivers"]), len(qs)), np.complex128)
-            for c, q in enumerate(qs):
-                o = O.Oracle()
-                o.set_initial_conditions(cfg["cp"], f, cfg["attenuation"])
-                o.load_geometry(cfg["scenes"][s], 0, delta)
-                o.load_source_points(cfg["sources"][q:q + 1])
-                o.load_field_points(cfg["receivers"])
-                o.render()
-                o.project_sources(False)
-                o.project_field_points()
-                ref[:, c] = o.field_points()
-                o.close()
-            got = out[s, k][:, qs]
-            errs["scene%d_%s_%.0fHz_%dfrag" % (s, cfg["kinds"][s], f, nfr[it])] = float(
-                np.linalg.norm(got - ref) / np.linalg.norm(ref))
+            ref = {False: np.zeros((len(cfg["receivers"]), len(qs)), np.complex128)}
+            ref[True] = ref[False].copy()
+            for exact in (False, True):
+                for c, q in enumerate(qs):
+                    o = O.Oracle()
+                    o.set_initial_conditions(cfg["cp"], f, cfg["attenuation"])
+                    o.load_geometry(cfg["scenes"][s], 0, delta)
+                    o.load_source_points(cfg["sources"][q:q + 1])
+                    o.load_field_points(cfg["receivers"])
+                    o.render()
+                    o.set_exact_geometry(exact)
+                    o.project_sources(False)
+                    o.project_field_points()
+                    ref[exact][:, c] = o.field_points()
+                    o.close()
+            key = "scene%d_%s_%.0fHz_%dfrag" % (s, cfg["kinds"][s], f, nfr[it])
+            rl2 = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+            errs[key] = rl2(out[s, k][:, qs], ref[False])
+            exact_abs[key] = rl2(out[s, k][:, qs], ref[True])
+            exact_rel[key] = rl2(out_rel[s, k][:, qs], ref[True])
+        errs["vs_exact_geometry"] = {"absolute": exact_abs, "relative_phase": exact_rel,
+                                     "worst_absolute": max(exact_abs.values()),
+                                     "worst_relative_phase": max(exact_rel.values())}
         return errs
     except Exception as ex:
         return {"failed": str(ex)}

@@ -280,6 +280,16 @@ int sonar_batch_set_points(long long plan, const float *src_xyz, int nsrc, const
  * shared memory holds, at most 4); the run graph is captured again.  Returns
  * 0 or a negative code. */
 int sonar_batch_set_shape(long long plan, int fragments_per_stage, int ctas_per_sm);
+/* Centroid-relative phase for a plan (on != 0), no counterpart in the
+ * reference: the reference forms each distance from absolute FP32 positions
+ * (src/OptiX.cu:45-57, :150-153), which at a 30 m range rounds the phase by
+ * about 2e-4 rad at 40 kHz.  With it on, every point is taken relative to its
+ * scene's box centre c in FP64 on the host (D = point - c, R = |D|, k R
+ * reduced to turns) and the kernel forms the phase distance as
+ * R + (|o|^2 - 2 o.D) / (r + R) with o = fragment - c.  Off by default
+ * (parity with the reference's rounding); the run graph is captured again.
+ * Returns 0 or a negative code. */
+int sonar_batch_set_relative(long long plan, int on);
 int sonar_batch_stream(long long plan, void **stream);
 int sonar_batch_free(long long plan);
 int sonar_run_batch(const float *tris, const int *scene_tri_off, int nscenes, const float *src_xyz, int nsrc,

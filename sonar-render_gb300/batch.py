@@ -41,6 +41,7 @@ def _lib():
         L.sonar_batch_stream.argtypes = [C.c_longlong, C.POINTER(C.c_void_p)]
         L.sonar_batch_set_points.argtypes = [C.c_longlong, _f, C.c_int, _f, C.c_int]
         L.sonar_batch_set_shape.argtypes = [C.c_longlong, C.c_int, C.c_int]
+        L.sonar_batch_set_relative.argtypes = [C.c_longlong, C.c_int]
         L.sonar_batch_free.argtypes = [C.c_longlong]
         L.sonar_run_batch.argtypes = [_f, _i, C.c_int, _f, C.c_int, _f, C.c_int, _f, C.c_int, C.c_float,
                                       C.c_float, C.c_float, _d]
@@ -103,6 +104,13 @@ class Plan:
         r = _lib().sonar_batch_set_shape(self.id, int(fragments_per_stage), int(ctas_per_sm))
         if r != 0:
             raise _err("sonar_batch_set_shape", r)
+
+    def set_relative(self, on=True):
+        """Centroid-relative phase (FP64 point offsets from each scene's box
+        centre) instead of the reference's absolute FP32 distances."""
+        r = _lib().sonar_batch_set_relative(self.id, int(bool(on)))
+        if r != 0:
+            raise _err("sonar_batch_set_relative", r)
 
     def stats(self):
         L = _lib()

@@ -29,7 +29,8 @@
 //   * the accumulator is read back with tcgen05.ld at the end of each
 //     segment (at most kBatchSegChunks chunks, so that an FP32 accumulation
 //     never spans more than a few thousand fragments) into FP32 partials
-//     that k_batch_reduce adds per item in a fixed order in FP64.
+//     that k_batch_reduce adds per item in a fixed order (compensated
+//     FP32 summation, the head and tail combined in FP64).
 // One persistent launch covers every chunk of every item: CTA b processes a
 // contiguous range of the global chunk list (balanced over the grid), cut
 // into segments at item boundaries.
@@ -116,6 +117,92 @@ __device__ __forceinline__ float2 incident_entry(const BatchItem &it, float3 q, 
     return make_float2(amp * cs, amp * sn);
 }
 
+// Centroid-relative forms of the two entries.  The point is given as
+// D = p - c and R = |D| (c: the item's reference point, D rounded from the
+// FP64 difference), the fragment as o = f - c and |o|^2 (formed once per
+// chunk when its data is staged); r = |D - o| for the amplitude and the
+// cosine.  The phase is k r = k R + k (r - R): the entry carries
+// e^{ik (r - R)} with r - R = (|o|^2 - 2 o.D) / (r + R), free of
+// cancellation, and e^{ik R} -- common to the point's row -- is applied in
+// FP64 by the reduction (the host computes it from the FP64 R).  The
+// readout's 1/r^2 term carries no phase, so the entry holds it times
+// e^{-ik R} (the row's factor E, FP32).
+// num = |o|^2 - 2 o.D = r^2 - R^2 (no cancellation); r^2 = R^2 + num is good
+// to FP32's relative accuracy, enough for the amplitude, the cosine and r + R.
+__device__ __forceinline__ float rel_num(float3 o, float oo, float4 D)
+{
+    return fmaf(-2.0f, fmaf(o.x, D.x, fmaf(o.y, D.y, o.z * D.z)), oo);
+}
+
+// the turns of k (r - R), r - R = num / (r + R)
+__device__ __forceinline__ float rel_turns(float r, float R, float num, float k2hi, float k2lo)
+{
+    const float s = r + R;
+    // the quotient from the approximate reciprocal, corrected by one Newton step
+    const float y = __fdividef(1.0f, s);
+    float dr = num * y;
+    dr = fmaf(y, fmaf(-dr, s, num), dr);
+    // |k dr| is at most a few tens of turns: the rounding of dr k2hi (half an
+    // ulp of it, below 1e-6 turns) is kept, the low part of k / 2 pi added
+    const float th = __fmul_rn(dr, k2hi);
+    return fmaf(dr, k2lo, th - rintf(th));
+}
+
+// f: o and area; nf: the facet normal and |o|^2; D: the receiver's offset
+// and R; R2 = R^2; E = e^{-ik R}
+template <bool ATT>
+__device__ __forceinline__ float2 readout_entry_rel(const BatchItem &it, float4 f, float4 nf, float4 D, float R2,
+                                                    float2 E)
+{
+    const float3 o = make_float3(f.x, f.y, f.z);
+    const float num = rel_num(o, nf.w, D);
+    const float rinv = rsqrtf(R2 + num);
+    const float r = (R2 + num) * rinv;
+    const float tu = rel_turns(r, D.w, num, it.k2hi, it.k2lo);
+    float sn, cs;
+    __sincosf(kTwoPiB * tu, &sn, &cs);
+    const float rinv2 = rinv * rinv;
+    float gr, gi;
+    if (ATT) {
+        const float amp = rinv * kInv4PiB * __expf(-it.ka * r);
+        gr = fmaf(amp, fmaf(it.ka, cs, it.kr * sn), rinv2 * E.x);
+        gi = fmaf(amp, fmaf(it.ka, sn, -it.kr * cs), rinv2 * E.y);
+    } else {
+        const float ampk = rinv * it.kr4pi;
+        gr = fmaf(ampk, sn, rinv2 * E.x);
+        gi = fmaf(-ampk, cs, rinv2 * E.y);
+    }
+    // cos_scat: (p - f).n / r
+    const float w = ((D.x - o.x) * nf.x + (D.y - o.y) * nf.y + (D.z - o.z) * nf.z) * rinv * f.w;
+    return make_float2(gr * w, gi * w);
+}
+
+// s: o and |o|^2 of the source-hop centroid; D: the source's offset and R
+template <bool ATT>
+__device__ __forceinline__ float2 incident_entry_rel(const BatchItem &it, float4 D, float R2, float4 s, float4 nf)
+{
+    const float3 o = make_float3(s.x, s.y, s.z);
+    const float num = rel_num(o, s.w, D);
+    const float rinv = rsqrtf(R2 + num);
+    const float r = (R2 + num) * rinv;
+    const float tu = rel_turns(r, D.w, num, it.k2hi, it.k2lo);
+    float sn, cs;
+    __sincosf(kTwoPiB * tu, &sn, &cs);
+    // cos_inc / r: -(s - q).n / r^2
+    float amp = -((o.x - D.x) * nf.x + (o.y - D.y) * nf.y + (o.z - D.z) * nf.z) * rinv * rinv;
+    if (ATT) amp *= __expf(-it.ka * r);
+    return make_float2(amp * cs, amp * sn);
+}
+
+// The points of one thread for the current item: positions, or (relative
+// phase) D, R and the turns of k R.
+struct RowPoints {
+    float3 prx, psrc;
+    float4 Drx, Dsrc;
+    float R2rx, R2src;
+    float2 Erx;
+};
+
 // two FP32 values -> (hi, lo) BF16 pairs packed for a 16-byte row store
 __device__ __forceinline__ void split8(const float *x, uint4 &hi, uint4 &lo)
 {
@@ -155,7 +242,8 @@ struct ChunkFrags {
 
 // Element e (fragment e / 4, field e % 4) of chunk `chunk` of item it, zero
 // past the item's fragments (their visibility words are zero, so padded
-// fragments contribute nothing).
+// fragments contribute nothing).  The relative phase stages it through
+// stage_rel once the load has arrived.
 __device__ __forceinline__ float4 fetch_frag(const BatchArgs &a, const BatchItem &it, int chunk, int kc, int e)
 {
     const int n = chunk * kc + (e >> 2);
@@ -172,9 +260,35 @@ __device__ __forceinline__ float4 fetch_frag(const BatchArgs &a, const BatchItem
     }
 }
 
-template <int KC, bool ATT>
+// Relative phase: the centroids as offsets o from the item's reference
+// point; the source-hop centroid's |o|^2 in its w, the readout centroid's in
+// the normal's w (written by the readout centroid's thread, the normal's
+// thread leaving w alone).
+template <int KC>
+__device__ __forceinline__ void stage_rel(ChunkFrags<KC> &F, const BatchItem &it, int e, float4 v)
+{
+    float4 *d = &F.v[e >> 2][e & 3];
+    const int c = e & 3;
+    if (c == 0 || c == 1) {
+        v.x -= it.cx;
+        v.y -= it.cy;
+        v.z -= it.cz;
+        const float oo = fmaf(v.x, v.x, fmaf(v.y, v.y, v.z * v.z));
+        if (c == 1) v.w = oo;
+        else F.v[e >> 2][2].w = oo;
+        *d = v;
+    } else if (c == 2) {
+        d->x = v.x;
+        d->y = v.y;
+        d->z = v.z;
+    } else {
+        *d = v;
+    }
+}
+
+template <int KC, bool ATT, bool REL>
 __device__ __forceinline__ void generate(uint8_t *st, const ChunkFrags<KC> &F, const BatchItem &it, int tid,
-                                         float3 prx, bool rx_ok, float3 psrc, bool src_ok)
+                                         const RowPoints &pt, bool rx_ok, bool src_ok)
 {
     using S = Stage<KC>;
     uint8_t *Ahi = st, *Alo = st + S::kA, *Bhi = st + 2 * S::kA, *Blo = st + 2 * S::kA + S::kB;
@@ -190,12 +304,14 @@ __device__ __forceinline__ void generate(uint8_t *st, const ChunkFrags<KC> &F, c
             const unsigned wsrc = __float_as_uint(row < 32 ? w4.z : w4.w);
             gr[j] = gi[j] = pr[j] = pi[j] = 0.0f;
             if (rx_ok && ((wrx >> (row & 31)) & 1u)) {
-                const float2 v = readout_entry<ATT>(it, f[0], f[2], prx);
+                const float2 v = REL ? readout_entry_rel<ATT>(it, f[0], f[2], pt.Drx, pt.R2rx, pt.Erx)
+                                     : readout_entry<ATT>(it, f[0], f[2], pt.prx);
                 gr[j] = v.x;
                 gi[j] = v.y;
             }
             if (src_ok && ((wsrc >> (row & 31)) & 1u)) {
-                const float2 v = incident_entry<ATT>(it, psrc, f[1], f[2]);
+                const float2 v = REL ? incident_entry_rel<ATT>(it, pt.Dsrc, pt.R2src, f[1], f[2])
+                                     : incident_entry<ATT>(it, pt.psrc, f[1], f[2]);
                 pr[j] = v.x;
                 pi[j] = v.y;
             }
@@ -225,7 +341,7 @@ __device__ __forceinline__ void generate(uint8_t *st, const ChunkFrags<KC> &F, c
     }
 }
 
-template <int KC, bool ATT>
+template <int KC, bool ATT, bool REL>
 __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
 {
     using S = Stage<KC>;
@@ -244,7 +360,19 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
     const bool rx_ok = row < a.nrx, src_ok = row < a.nsrc;
     const float4 rx4 = rx_ok ? a.rx[row] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float4 sq4 = src_ok ? a.src[row] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    const float3 prx = make_float3(rx4.x, rx4.y, rx4.z), psrc = make_float3(sq4.x, sq4.y, sq4.z);
+    RowPoints pt{};
+    pt.prx = make_float3(rx4.x, rx4.y, rx4.z);
+    pt.psrc = make_float3(sq4.x, sq4.y, sq4.z);
+    // the relative phase's per-item point data of this thread's row
+    auto load_rel = [&](int item) {
+        if (!REL) return;
+        const size_t q = (size_t)item * kBatchMaxPoints + row;
+        pt.Drx = __ldg(a.rel_rx + q);
+        pt.Dsrc = __ldg(a.rel_src + q);
+        pt.Erx = __ldg(a.rel_rx_e + q);
+        pt.R2rx = pt.Drx.w * pt.Drx.w;
+        pt.R2src = pt.Dsrc.w * pt.Dsrc.w;
+    };
     const uint32_t sbase = smem_u32(smem);
     const bool loader = tid < 4 * KC;  // thread tid stages element tid of each chunk's fragment data
     // this CTA's chunks: segments [g0, g1), chunk cc of segment sg
@@ -255,7 +383,12 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
     if (sg < g1) {
         seg = a.segs[sg];
         it = a.items[seg.x];
-        if (loader) sfrag[0].v[tid >> 2][tid & 3] = fetch_frag(a, it, seg.y, KC, tid);
+        load_rel(seg.x);
+        if (loader) {
+            const float4 v = fetch_frag(a, it, seg.y, KC, tid);
+            if (REL) stage_rel(sfrag[0], it, tid, v);
+            else sfrag[0].v[tid >> 2][tid & 3] = v;
+        }
     }
     tc_fence_before();
     __syncthreads();
@@ -288,8 +421,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
             ok = __syncthreads_and(done);
             if (!ok) break;
         }
-        generate<KC, ATT>(smem + st * S::kBytes, sfrag[st], it, tid, prx, rx_ok, psrc, src_ok);
-        if (loader) sfrag[st ^ 1].v[tid >> 2][tid & 3] = nf;
+        generate<KC, ATT, REL>(smem + st * S::kBytes, sfrag[st], it, tid, pt, rx_ok, src_ok);
+        if (loader) {
+            if (REL) stage_rel(sfrag[st ^ 1], nit, tid, nf);
+            else sfrag[st ^ 1].v[tid >> 2][tid & 3] = nf;
+        }
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -331,6 +467,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
             tc_fence_before();
             __syncthreads();
         }
+        if (nsg != sg && nsg < g1 && nseg.x != seg.x) load_rel(nseg.x);
         sg = nsg;
         cc = ncc;
         seg = nseg;
@@ -355,21 +492,47 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs a)
     if (warp == 0 && drained) tmem_dealloc(tmem, kTmemCols);
 }
 
-// out[item][p][q] = sum over the item's segments, fixed order, FP64.  Grid
-// (items, entry chunks of 256): one thread per (receiver, source) entry.
+// Error-free sum of two FP32 values (Knuth's two-sum): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// out[item][p][q] = sum over the item's segments in a fixed order, times
+// the relative phase's row factors e^{ik R} of receiver p and source q when
+// given.  The FP32 partials are added by compensated summation (a head and
+// the sum of the two-sum error terms, all FP32: FP64 arithmetic is scarce on
+// this part), the two words combined in FP64: the sum is exact to about
+// 2^-46 of its terms' magnitude, as an FP64 accumulation would be for this
+// many terms.  Grid (items, entry chunks of 256): one thread per (receiver,
+// source) entry.
 __global__ void __launch_bounds__(256) k_batch_reduce(const float *partial, const int *item_seg_off,
-                                                      const int *item_segs, int nrx, int nsrc, double2 *out)
+                                                      const int *item_segs, int nrx, int nsrc, const double2 *erx,
+                                                      const double2 *esrc, double2 *out)
 {
     const int item = blockIdx.x;
     const int e = blockIdx.y * 256 + threadIdx.x;
     if (e >= nrx * nsrc) return;
     const int s0 = item_seg_off[item], s1 = item_seg_off[item + 1];
     const int p = e / nsrc, q = e - p * nsrc;
-    double re = 0.0, im = 0.0;
+    float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
     for (int s = s0; s < s1; ++s) {
         const float *P = partial + (long long)item_segs[s] * 128 * 64;
-        re += (double)__ldg(P + p * 64 + q);
-        im += (double)__ldg(P + (64 + p) * 64 + q);
+        float e;
+        two_sum(rh, __ldg(P + p * 64 + q), rh, e);
+        rl += e;
+        two_sum(ih, __ldg(P + (64 + p) * 64 + q), ih, e);
+        il += e;
+    }
+    double re = (double)rh + (double)rl, im = (double)ih + (double)il;
+    if (erx) {
+        const double2 a = erx[item * kBatchMaxPoints + p], b = esrc[item * kBatchMaxPoints + q];
+        const double er = a.x * b.x - a.y * b.y, ei = a.x * b.y + a.y * b.x;
+        const double t = re * er - im * ei;
+        im = re * ei + im * er;
+        re = t;
     }
     out[(long long)item * nrx * nsrc + e] = make_double2(re, im);
 }
@@ -382,50 +545,60 @@ size_t batch_smem_bytes(int kc)
                     : kc == 32 ? (size_t)2 * Stage<32>::kBytes : (size_t)2 * Stage<16>::kBytes;
 }
 
-cudaError_t batch_prepare()
+namespace {
+template <int KC>
+cudaError_t prepare_k()
 {
-    cudaError_t e = cudaFuncSetAttribute(k_batch<32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)batch_smem_bytes(32));
+    const int sm = (int)batch_smem_bytes(KC);
+    cudaError_t e = cudaFuncSetAttribute(k_batch<KC, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)batch_smem_bytes(32));
+        e = cudaFuncSetAttribute(k_batch<KC, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch<64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)batch_smem_bytes(64));
+        e = cudaFuncSetAttribute(k_batch<KC, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch<64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)batch_smem_bytes(64));
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)batch_smem_bytes(16));
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)batch_smem_bytes(16));
+        e = cudaFuncSetAttribute(k_batch<KC, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     return e;
 }
+}  // namespace
+
+cudaError_t batch_prepare()
+{
+    cudaError_t e = prepare_k<32>();
+    if (e == cudaSuccess) e = prepare_k<64>();
+    if (e == cudaSuccess) e = prepare_k<16>();
+    return e;
+}
+
+namespace {
+template <int KC>
+void launch_k(const BatchArgs &a, int grid, size_t sm, bool att, bool rel, cudaStream_t s)
+{
+    if (att) {
+        if (rel) k_batch<KC, true, true><<<grid, kBatchThreads, sm, s>>>(a);
+        else k_batch<KC, true, false><<<grid, kBatchThreads, sm, s>>>(a);
+    } else {
+        if (rel) k_batch<KC, false, true><<<grid, kBatchThreads, sm, s>>>(a);
+        else k_batch<KC, false, false><<<grid, kBatchThreads, sm, s>>>(a);
+    }
+}
+}  // namespace
 
 void launch_batch(const BatchArgs &a, int kc, int grid, bool att, cudaStream_t s)
 {
     const size_t sm = batch_smem_bytes(kc);
     if (grid <= 0) return;
-    if (kc == 64) {
-        if (att) k_batch<64, true><<<grid, kBatchThreads, sm, s>>>(a);
-        else k_batch<64, false><<<grid, kBatchThreads, sm, s>>>(a);
-    } else if (kc == 16) {
-        if (att) k_batch<16, true><<<grid, kBatchThreads, sm, s>>>(a);
-        else k_batch<16, false><<<grid, kBatchThreads, sm, s>>>(a);
-    } else {
-        if (att) k_batch<32, true><<<grid, kBatchThreads, sm, s>>>(a);
-        else k_batch<32, false><<<grid, kBatchThreads, sm, s>>>(a);
-    }
+    const bool rel = a.rel_rx != nullptr;
+    if (kc == 64) launch_k<64>(a, grid, sm, att, rel, s);
+    else if (kc == 16) launch_k<16>(a, grid, sm, att, rel, s);
+    else launch_k<32>(a, grid, sm, att, rel, s);
 }
 
 void launch_batch_reduce(const float *partial, const int *item_seg_off, const int *item_segs, int nitems, int nrx,
-                         int nsrc, double2 *out, cudaStream_t s)
+                         int nsrc, const double2 *erx, const double2 *esrc, double2 *out, cudaStream_t s)
 {
     if (nitems > 0)
         k_batch_reduce<<<dim3(nitems, (nrx * nsrc + 255) / 256), 256, 0, s>>>(partial, item_seg_off, item_segs, nrx,
-                                                                            nsrc, out);
+                                                                            nsrc, erx, esrc, out);
 }
 
 }  // namespace sonar

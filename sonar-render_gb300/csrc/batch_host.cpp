@@ -106,12 +106,17 @@ struct Plan {
     std::vector<BatchItem> items;
     std::vector<long long> item_cells;
     std::vector<int> convex;      // per scene
+    std::vector<float> h_src, h_rx;  // the points of the next run (xyz)
+    bool relative = false;           // centroid-relative phase (BatchArgs::rel_*)
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // device
     float4 *d_pos = nullptr, *d_spos = nullptr, *d_nrm = nullptr, *d_facet_n = nullptr;
     int *d_facet = nullptr;
     float4 *d_src = nullptr, *d_rx = nullptr;
+    float4 *d_rel_rx = nullptr, *d_rel_src = nullptr;
+    double2 *d_erx = nullptr, *d_esrc = nullptr;
+    float2 *d_erx_conj = nullptr;
     float4 *d_nodes = nullptr, *d_tris = nullptr;
     BvhView *d_bvh = nullptr;
     uint4 *d_vis = nullptr;
@@ -142,6 +147,8 @@ struct Plan {
         bfree(stream, d_hard_count); bfree(stream, d_items); bfree(stream, d_segs); bfree(stream, d_cta_seg);
         bfree(stream, d_item_seg_off); bfree(stream, d_item_segs); bfree(stream, d_status);
         bfree(stream, d_partial); bfree(stream, d_out);
+        bfree(stream, d_rel_rx); bfree(stream, d_rel_src); bfree(stream, d_erx); bfree(stream, d_esrc);
+        bfree(stream, d_erx_conj);
         for (cudaEvent_t &e : ev)
             if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
@@ -255,7 +262,54 @@ BatchArgs batch_args(const Plan &p)
     a.nsrc = p.nsrc;
     a.partial = p.d_partial;
     a.status = p.d_status;
+    if (p.relative) {
+        a.rel_rx = p.d_rel_rx;
+        a.rel_src = p.d_rel_src;
+        a.rel_rx_e = p.d_erx_conj;
+    }
     return a;
+}
+
+// Per item and point (rows padded to 64): D = point - item centre rounded to
+// FP32 with R = |D|, and the point's phase factor e^{ik R} (FP64; for the
+// receivers also its conjugate in FP32), both from the FP64 difference of
+// the FP32 point and centre (k R reduced in turns).
+void upload_relative(Plan &p)
+{
+    const size_t n = (size_t)p.nitems * kBatchMaxPoints;
+    if (!p.d_rel_rx) {
+        p.d_rel_rx = balloc<float4>(p.stream, n);
+        p.d_rel_src = balloc<float4>(p.stream, n);
+        p.d_erx = balloc<double2>(p.stream, n);
+        p.d_esrc = balloc<double2>(p.stream, n);
+        p.d_erx_conj = balloc<float2>(p.stream, n);
+    }
+    std::vector<float4> Drx(n, make_float4(0.0f, 0.0f, 0.0f, 1.0f)), Dsrc(n, make_float4(0.0f, 0.0f, 0.0f, 1.0f));
+    std::vector<double2> erx(n, make_double2(0.0, 0.0)), esrc(n, make_double2(0.0, 0.0));
+    auto fill = [&](const std::vector<float> &pts, int np, const BatchItem &b, float4 *D, double2 *e) {
+        const double k2 = (double)b.kr / (2.0 * M_PI);
+        for (int i = 0; i < np; i++) {
+            const double dx = (double)pts[3 * i] - (double)b.cx, dy = (double)pts[3 * i + 1] - (double)b.cy,
+                         dz = (double)pts[3 * i + 2] - (double)b.cz;
+            const double R = std::sqrt(dx * dx + dy * dy + dz * dz);
+            const double tu = R * k2, th = 2.0 * M_PI * (tu - std::nearbyint(tu));
+            D[i] = make_float4((float)dx, (float)dy, (float)dz, (float)R);
+            e[i] = make_double2(std::cos(th), std::sin(th));
+        }
+    };
+    for (int it = 0; it < p.nitems; it++) {
+        const size_t o = (size_t)it * kBatchMaxPoints;
+        fill(p.h_rx, p.nrx, p.items[it], Drx.data() + o, erx.data() + o);
+        fill(p.h_src, p.nsrc, p.items[it], Dsrc.data() + o, esrc.data() + o);
+    }
+    BCK(stage_to_device(p.d_rel_rx, Drx.data(), n * sizeof(float4), p.stream));
+    BCK(stage_to_device(p.d_rel_src, Dsrc.data(), n * sizeof(float4), p.stream));
+    BCK(stage_to_device(p.d_erx, erx.data(), n * sizeof(double2), p.stream));
+    BCK(stage_to_device(p.d_esrc, esrc.data(), n * sizeof(double2), p.stream));
+    std::vector<float2> ec(n);
+    for (size_t i = 0; i < n; i++) ec[i] = make_float2((float)erx[i].x, (float)-erx[i].y);
+    BCK(stage_to_device(p.d_erx_conj, ec.data(), n * sizeof(float2), p.stream));
+    BCK(cudaStreamSynchronize(p.stream));
 }
 
 BatchVisArgs vis_args(const Plan &p)
@@ -288,7 +342,8 @@ void enqueue_run(Plan &p)
     BCK(cudaEventRecordWithFlags(p.ev[1], p.stream, cudaEventRecordExternal));
     launch_batch(batch_args(p), p.tune.kc, p.tune.grid, p.att != 0.0f, p.stream);
     BCK(cudaEventRecordWithFlags(p.ev[2], p.stream, cudaEventRecordExternal));
-    launch_batch_reduce(p.d_partial, p.d_item_seg_off, p.d_item_segs, p.nitems, p.nrx, p.nsrc, p.d_out, p.stream);
+    launch_batch_reduce(p.d_partial, p.d_item_seg_off, p.d_item_segs, p.nitems, p.nrx, p.nsrc,
+                        p.relative ? p.d_erx : nullptr, p.relative ? p.d_esrc : nullptr, p.d_out, p.stream);
     BCK(cudaEventRecordWithFlags(p.ev[3], p.stream, cudaEventRecordExternal));
 }
 
@@ -563,6 +618,7 @@ std::unique_ptr<Plan> make_plan(const float *tris, const int *tri_off, int nscen
     for (int i = 0; i < 3 * nsrc; i++) maxp = std::max(maxp, (double)std::fabs(src[i]));
     for (int i = 0; i < 3 * nrx; i++) maxp = std::max(maxp, (double)std::fabs(rx[i]));
     p->convex.assign(nscenes, 0);
+    std::vector<std::array<float, 3>> centre(nscenes);
     for (int s = 0; s < nscenes; s++) {
         std::vector<std::array<float, 9>> t;
         double maxc = maxp, maxv = 0.0;
@@ -576,6 +632,17 @@ std::unique_ptr<Plan> make_plan(const float *tris, const int *tri_off, int nscen
             t.push_back(a);
         }
         p->convex[s] = scene_is_convex(t, 1e-6 * (1.0 + maxv)) ? 1 : 0;
+        {
+            float lo[3] = {t[0][0], t[0][1], t[0][2]}, hi[3] = {lo[0], lo[1], lo[2]};
+            for (const auto &a : t)
+                for (int v = 0; v < 3; v++)
+                    for (int k = 0; k < 3; k++) {
+                        lo[k] = std::min(lo[k], a[3 * v + k]);
+                        hi[k] = std::max(hi[k], a[3 * v + k]);
+                    }
+            centre[s] = {(float)(0.5 * ((double)lo[0] + hi[0])), (float)(0.5 * ((double)lo[1] + hi[1])),
+                         (float)(0.5 * ((double)lo[2] + hi[2]))};
+        }
         // node boxes padded by 1e-5 (1 + largest coordinate of triangles and points):
         // the FP32 slab test and the crossing point of a hit are within a few 1e-7
         // (1 + coordinate) of exact, so every box a hit needs is opened
@@ -592,7 +659,15 @@ std::unique_ptr<Plan> make_plan(const float *tris, const int *tri_off, int nscen
     for (int s = 0; s < nscenes; s++)
         views[s] = BvhView{p->d_nodes + 2 * (size_t)node0[s], p->d_tris + 4 * (size_t)tri0[s],
                            node0[s + 1] - node0[s], tri0[s + 1] - tri0[s]};
-    for (int it = 0; it < p->nitems; it++) p->items[it].convex = p->convex[p->items[it].scene];
+    for (int it = 0; it < p->nitems; it++) {
+        BatchItem &b = p->items[it];
+        b.convex = p->convex[b.scene];
+        b.cx = centre[b.scene][0];
+        b.cy = centre[b.scene][1];
+        b.cz = centre[b.scene][2];
+    }
+    p->h_src.assign(src, src + 3 * (size_t)nsrc);
+    p->h_rx.assign(rx, rx + 3 * (size_t)nrx);
     p->d_bvh = balloc<BvhView>(p->stream, nscenes);
     BCK(stage_to_device(p->d_nodes, nodes.data(), nodes.size() * sizeof(BvhNode), st));
     BCK(stage_to_device(p->d_tris, trec.data(), trec.size() * sizeof(float4), st));
@@ -686,6 +761,22 @@ int sonar_batch_set_points(long long plan, const float *src_xyz, int nsrc, const
         for (int i = 0; i < nrx; i++) r4[i] = make_float4(rx_xyz[3 * i], rx_xyz[3 * i + 1], rx_xyz[3 * i + 2], 0.0f);
         BCK(stage_to_device(p.d_src, s4.data(), nsrc * sizeof(float4), p.stream));
         BCK(stage_to_device(p.d_rx, r4.data(), nrx * sizeof(float4), p.stream));
+        p.h_src.assign(src_xyz, src_xyz + 3 * (size_t)nsrc);
+        p.h_rx.assign(rx_xyz, rx_xyz + 3 * (size_t)nrx);
+        if (p.relative) upload_relative(p);
+        return 0;
+    });
+}
+
+int sonar_batch_set_relative(long long plan, int on)
+{
+    std::lock_guard<std::mutex> lk(g_lock);
+    return (int)bguard([&]() -> long long {
+        Plan &p = find(plan);
+        if ((on != 0) == p.relative) return 0;
+        p.relative = on != 0;
+        if (p.relative) upload_relative(p);
+        capture(p);
         return 0;
     });
 }
@@ -741,10 +832,11 @@ int sonar_batch_stats(long long plan, char *json, int cap)
                  "{\"items\": %d, \"scenes\": %d, \"frequencies\": %d, \"sources\": %d, \"receivers\": %d, "
                  "\"fragments\": %lld, \"cells\": %lld, \"pairs\": %.0f, \"segments\": %d, \"convex_scenes\": %d, "
                  "\"runs\": %d, \"vis_ms\": %.6f, \"gemm_ms\": %.6f, \"reduce_ms\": %.6f, \"shadow_tests\": %u, "
+                 "\"relative\": %s, "
                  "\"tuning\": {\"fragments_per_stage\": %d, \"grid\": %d, \"cached\": %s, \"candidates\": [",
                  p.nitems, p.nscenes, p.nfreq, p.nsrc, p.nrx, p.nfrag, p.ncells, p.pairs, p.nseg,
                  (int)std::count(p.convex.begin(), p.convex.end(), 1),
-                 p.runs, p.vis_ms, p.gemm_ms, p.reduce_ms, hard, p.tune.kc, p.tune.grid,
+                 p.runs, p.vis_ms, p.gemm_ms, p.reduce_ms, hard, p.relative ? "true" : "false", p.tune.kc, p.tune.grid,
                  p.tune_cached ? "true" : "false");
         s += buf;
         for (size_t i = 0; i < p.tried.size(); i++) {

@@ -281,7 +281,7 @@ struct BatchItem {
     int frag0, nfrag;              // the item's fragments [frag0, frag0 + nfrag) of the batch arrays
     int scene, convex;             // scene index (occluders); 1 when the scene is convex
     float kr, ka, k2hi, k2lo, kr4pi;
-    int pad[3];
+    float cx, cy, cz;              // reference point of the centroid-relative phase (the scene's box centre)
 };
 struct BatchArgs {
     const BatchItem *items;
@@ -295,6 +295,12 @@ struct BatchArgs {
     int nrx, nsrc;
     float *partial;                // [segment][128][64] FP32
     int *status;                   // set to 1 when a CTA gave up waiting on the tensor core
+    // centroid-relative phase (null: absolute FP32 distances as the
+    // reference): per item and point (64 rows) D = point - item centre and
+    // R = |D| (float4); the factors e^{ik R} go to the reduction, and the
+    // receivers' e^{-ik R} (FP32) multiplies the readout's 1/r^2 term
+    const float4 *rel_rx = nullptr, *rel_src = nullptr;
+    const float2 *rel_rx_e = nullptr;
 };
 // kernels.cu: interaction bits of both batch hops, one thread per fragment
 struct BatchVisArgs {
@@ -317,7 +323,7 @@ size_t batch_smem_bytes(int kc);
 cudaError_t batch_prepare();        // dynamic shared-memory limits of the batch kernels (outside stream capture)
 void launch_batch(const BatchArgs &a, int kc, int grid, bool att, cudaStream_t s);
 void launch_batch_reduce(const float *partial, const int *item_seg_off, const int *item_segs, int nitems, int nrx,
-                         int nsrc, double2 *out, cudaStream_t s);
+                         int nsrc, const double2 *erx, const double2 *esrc, double2 *out, cudaStream_t s);
 
 // raster.cu: headless rendering of the textured facets (RenderOpenGL)
 struct RasterTri {

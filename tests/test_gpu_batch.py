@@ -31,7 +31,7 @@ def small_batch(scenes):
     return [plate, box, sph], src, rx, np.array([15e3, 25e3], np.float32)
 
 
-def oracle_columns(oracle_mod, tris, src, rx, f, cp=1480.0, att=0.0, per_wl=7.5):
+def oracle_columns(oracle_mod, tris, src, rx, f, cp=1480.0, att=0.0, per_wl=7.5, exact=False):
     delta = float(np.float32(cp) / np.float32(f) / np.float32(per_wl))
     out = np.zeros((len(rx), len(src)), np.complex128)
     for q in range(len(src)):
@@ -41,6 +41,7 @@ def oracle_columns(oracle_mod, tris, src, rx, f, cp=1480.0, att=0.0, per_wl=7.5)
         o.load_source_points(src[q:q + 1])
         o.load_field_points(rx)
         o.render()
+        o.set_exact_geometry(exact)
         o.project_sources(False)
         o.project_field_points()
         out[:, q] = o.field_points()
@@ -180,3 +181,43 @@ def test_every_tuning_shape(api, oracle_mod, scenes):
         e_orc = rel_l2(o[2, 1], ref)
         print("shape %s: vs 32 x 2 %.2e, vs FP64 (sphere, %.0f Hz) %.2e" % (key, e_shape, freqs[1], e_orc))
         assert e_shape < 1e-6 and e_orc < TOL
+
+
+def test_batch_relative_phase_at_30m(api, oracle_mod, scenes):
+    """Sources and receivers on 30 m arcs at 40 kHz: the reference's absolute
+    FP32 distances (src/OptiX.cu:45-57, :150-153) round the phase by about
+    1e-6 m x k.  With the plan's relative phase (points as FP64 offsets from
+    the scene's box centre, k R reduced on the host) every column must move
+    much closer to the oracle's exact-geometry mode (FP64 distances from the
+    same FP32 positions), down to the split-BF16 floor, while the default
+    run keeps the reference's rounding."""
+    from sonar_render_gb300 import batch
+    plate = scenes.rotate(scenes.plate_1x05(), "x", 10.0)
+    box = scenes.translate(scenes.rotate(scenes.box(0.3, 0.2, 0.25), "y", 25.0), [0.4, -0.3, 0.2])
+    src = scenes.arc_xz(30.0, np.linspace(-40.0, 40.0, 8))
+    rx = scenes.arc_xz(29.5, np.linspace(-35.0, 45.0, 6))
+    freqs = np.array([40e3], np.float32)
+    plan = batch.Plan([plate, box], src, rx, freqs)
+    absolute = plan.run()
+    plan.set_relative(True)
+    rel = plan.run()
+    assert plan.stats()["relative"] is True
+    # moved points keep the relative phase
+    plan.set_points(src[::-1].copy(), rx)
+    rel_moved = plan.run()
+    plan.set_points(src, rx)
+    plan.set_relative(False)
+    back = plan.run()
+    plan.close()
+    assert np.array_equal(back, absolute)
+    assert rel_l2(rel_moved[..., ::-1], rel) < 1e-6
+    worst_abs = worst_rel = worst_par = 0.0
+    for s, tris in enumerate((plate, box)):
+        ex = oracle_columns(oracle_mod, tris, src, rx, freqs[0], exact=True)
+        par = oracle_columns(oracle_mod, tris, src, rx, freqs[0], exact=False)
+        e_abs, e_rel, e_par = rel_l2(absolute[s, 0], ex), rel_l2(rel[s, 0], ex), rel_l2(absolute[s, 0], par)
+        print("scene %d at 30 m, 40 kHz vs exact geometry: absolute %.2e -> relative %.2e "
+              "(absolute vs the reference's rounding %.2e)" % (s, e_abs, e_rel, e_par))
+        worst_abs, worst_rel, worst_par = max(worst_abs, e_abs), max(worst_rel, e_rel), max(worst_par, e_par)
+    assert worst_par < TOL
+    assert worst_rel < TOL and worst_rel < 0.5 * worst_abs
