@@ -180,6 +180,7 @@ OVERLAP = [1]      # compressed bounce: low-rank apply on a second stream beside
 LR_CTAS = [4]      # low-rank apply: resident CTAs per SM (register cap)
 FUSED = [1]        # k_aca2: the first bounce's low-rank apply fused into the cross approximation
 INTERP = [1]       # far class-ALL blocks between planar tiles by directional interpolation
+BUILD_OVERLAP = [1]  # interpolation build on a second stream beside the cross approximation
 
 
 def set_path(api, compressed, select):
@@ -193,6 +194,7 @@ def set_path(api, compressed, select):
     api.set_option("lr_block_ctas", LR_CTAS[0])
     api.set_option("overlap_streams", OVERLAP[0])
     api.set_option("compress_interp", INTERP[0])
+    api.set_option("compress_build_overlap", BUILD_OVERLAP[0])
 
 
 def time_path(api, cfg, args, flush, local, world, reuse=False):
@@ -409,7 +411,7 @@ def ip_roofline(stats, fp32_peak):
             "achieved": round(ach, 3), "peak": round(peak, 3), "unit": "TFLOP/s", "frac": round(ach / peak, 4),
             "traffic": round(traffic), "traffic_source": "ncu dram bytes of the 40 kHz capture per stored entry",
             "blocks_per_launch": nb, "mean_nodes": P, "flop_per_block": round(flop_block),
-            "launch_ms": round(ms, 4), "timed": "its own stream's span, beside the cross approximation on another",
+            "launch_ms": round(ms, 4), "timed": "its own stream's span",
             "peak_source": "FP32 FMA rate measured now by sonar_measure_peak"}
 
 
@@ -919,11 +921,17 @@ def run_gb300(args):
     # the low-rank apply timed alone (one stream, reused operator): its
     # roofline; in the steps above it shares the SMs with the dense remainder
     lr_alone = None
+    # and the two approximation kernels of the build (interpolation, cross
+    # approximation) each alone: in the headline steps they share the SMs on
+    # two streams, so neither stream's span is a kernel duration
+    build_alone = None
     if "compressed" in modes:
         set_path(api, True, select)
         api.set_option("overlap_streams", 0)
         load_scene(api, cfg)
         _, lr_alone, _ = time_path(api, cfg, args, flush, local, world, reuse=True)
+        load_scene(api, cfg)
+        _, build_alone, _ = time_path(api, cfg, args, flush, local, world)
         api.set_option("overlap_streams", OVERLAP[0])
     batch_res = batch_leg(args, flush, rank) if args.batch else None
     legs = {}
@@ -1008,11 +1016,20 @@ def run_gb300(args):
     roof_lr = lowrank_roofline(lr_alone) if head == "compressed" and lr_alone else None
     if roof_lr:
         roof_lr["timed"] = "alone (one stream), operator reused; the headline step overlaps it with the dense remainder"
-    roof_aca = aca_roofline(st, fp32_peak) if head == "compressed" else None
-    roof_ip = ip_roofline(st, fp32_peak) if head == "compressed" else None
+    roof_aca = aca_roofline(build_alone or st, fp32_peak) if head == "compressed" else None
+    roof_ip = ip_roofline(build_alone or st, fp32_peak) if head == "compressed" else None
+    for r in (roof_aca, roof_ip):
+        if r and build_alone:
+            r["timed"] = ("alone: the same rebuilt steps with the build on one stream; the headline step runs the "
+                          "interpolation beside the cross approximation on a second stream")
     # the roofline object describes the dominant kernel of the headline step
     # (not the two approximation kernels' joint span)
     single = {k: v for k, v in kms.items() if k != "approximation_both"}
+    alone_ms = None
+    if build_alone:
+        ka = kernel_times(build_alone, args.steps)
+        alone_ms = {k: round(ka[k], 4) for k in ("interpolation", "cross_approx") if k in ka}
+        single.update(alone_ms)
     dominant = max(single, key=single.get) if single else None
     if dominant == "cross_approx" and roof_aca:
         roof_main = roof_aca
@@ -1037,7 +1054,7 @@ def run_gb300(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": roof_main, "roofline_bounce_sum": roof_sym, "roofline_lowrank": roof_lr,
         "roofline_cross_approx": roof_aca, "roofline_interpolation": roof_ip, "dominant_kernel": dominant,
-        "kernel_ms_per_step": kms, "kernel_share": kshare,
+        "kernel_ms_per_step": kms, "kernel_share": kshare, "build_kernels_alone_ms_per_step": alone_ms,
         "compression": compression,
         "mask_block_classes": mask_classes,
         "cpu_baseline": cpu, "e2e": H["e2e"], "clocks": H["clocks"], "gpu_launches": int(H["launches_per_step"] * args.steps),
@@ -1230,6 +1247,8 @@ def main():
                          "(the rest by cross approximation)")
     ap.add_argument("--overlap", type=int, default=1, choices=(0, 1),
                     help="compressed bounce: low-rank apply on a second stream beside the dense remainder")
+    ap.add_argument("--build-overlap", type=int, default=1, choices=(0, 1),
+                    help="compressed build: interpolation on a second stream beside the cross approximation")
     ap.add_argument("--tol", type=float, default=5e-4,
                     help="cross-approximation tolerance of the compressed path (judge limit 3 x tol); the "
                          "default keeps the step's error about 5x below the 1e-3 target")
@@ -1251,6 +1270,7 @@ def main():
     RCUT[0] = args.rcut
     ACA_VARIANT[0] = args.aca_variant
     OVERLAP[0] = args.overlap
+    BUILD_OVERLAP[0] = args.build_overlap
     FUSED[0] = args.fused_apply
     INTERP[0] = args.interp
     LR_CTAS[0] = args.lr_ctas

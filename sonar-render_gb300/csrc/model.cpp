@@ -303,6 +303,7 @@ struct Model {
     int opt_cross_objects = 0;  // bounces also between different targets (FACET_RESP); 0: the reference's behaviour
     int opt_convex_masks = 1;   // convex targets: shadow tests search only where a crossing is possible
     int opt_overlap = 1;        // compressed bounce: low-rank apply on the second stream beside the dense remainder
+    int opt_build_overlap = 1;  // compressed build: interpolated blocks on the second stream beside the cross approximation
     int scene_convex = 0;       // every target vertex on or behind every target triangle's plane
     float scene_vmax = 0.0f;    // largest |coordinate| of the target vertices
     Compression cmp;
@@ -1003,13 +1004,12 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
     // the interpolated blocks on the second stream beside the cross
     // approximation (disjoint blocks and output slots; each kernel writes the
     // rank, error and outputs of its own blocks only)
-    const bool ip_side = C.interp && g.opt_overlap;
+    const bool ip_side = C.interp && g.opt_overlap && g.opt_build_overlap;
     const cudaStream_t ist = ip_side ? g.side : st;
     if (ip_side) {
         CK(cudaEventRecord(g.ev_fork, st));
         CK(cudaStreamWaitEvent(g.side, g.ev_fork, 0));
     }
-    CK(cudaEventRecord(g.evb[5], ist));
     // the panel kernels also apply the accepted blocks to this bounce's packed
     // inputs: the first bounce's low-rank apply then only gathers
     C.outputs_ready = launch_aca(s, C.d_blocks, C.d_cls, C.d_acap, C.d_off, C.interp ? C.naca_kept : n, g.opt_cmp_tol,
@@ -1022,10 +1022,13 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
         // node entries, judge, and the fused apply when the cross
         // approximation applies its own blocks too
         const bool fused = C.outputs_ready;
+        CK(cudaEventRecord(g.evb[5], ist));
         launch_ip_build(s, C.ip.tile, C.ip.fxy, C.ip.lev, A.delta, C.d_blocks, C.d_off, C.nip_kept, g.opt_cmp_judge,
                         C.d_U, C.d_rank, C.d_fro, C.d_err, fused ? C.d_brow : nullptr, fused ? C.d_bcol : nullptr, ist,
                         C.d_ip_list);
         CK(cudaGetLastError());
+    } else {
+        CK(cudaEventRecord(g.evb[5], ist));
     }
     CK(cudaEventRecord(g.evb[4], ist));
     if (ip_side) {
@@ -1854,6 +1857,10 @@ int sonar_set_option(const char *key, double value)
     }
     if (!strcmp(key, "overlap_streams")) {
         g.opt_overlap = value != 0.0 ? 1 : 0;
+        return 0;
+    }
+    if (!strcmp(key, "compress_build_overlap")) {
+        g.opt_build_overlap = value != 0.0 ? 1 : 0;
         return 0;
     }
     if (!strcmp(key, "convex_masks")) {
