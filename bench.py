@@ -1119,7 +1119,7 @@ def check_error(api, cfg):
         e = {}
         graze = {}
         for k in range(nb):
-            q = np.sort(rng.choice(nact, min(32, nact), replace=False))
+            q = np.sort(rng.choice(nact, min(256, nact), replace=False))
             # bounce k+1 input: the pressure after bounce k (P_out <- P)
             v, m = o.hop_subset(2, 0, 0, q, pin=Ps[k], want_mask=(k == 0), nsrc=nact)
             c = o.counters()
@@ -1132,7 +1132,7 @@ def check_error(api, cfg):
                 graze = {"bounce_pairs_checked": c["pairs"], "bounce_grazing": c["grazing"]}
         if npts:
             o.set_pressures(0, 0, Ps[-1])
-            jj = np.sort(rng.choice(npts, min(32, npts), replace=False))
+            jj = np.sort(rng.choice(npts, min(256, npts), replace=False))
             vf, mf = o.hop_subset(1, 0, 0, jj, want_mask=True, nsrc=nact)
             c2 = o.counters()
             gf = (mf & 2).any(axis=1)

@@ -51,6 +51,10 @@ constexpr float kInv4PiB = 0.0795774715459476679f;
 constexpr float kTwoPiB = 6.28318530717958647692f;
 constexpr int kBatchThreads = 256;
 constexpr uint32_t kTmemCols = 64;          // FP32 accumulator: 128 lanes x 64 columns
+#ifndef SONAR_GEN_GROUP
+#define SONAR_GEN_GROUP 4
+#endif
+constexpr int kGenGroup = SONAR_GEN_GROUP;  // fragments whose entries are evaluated together
 
 // Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
 // K-major, N = 64, M = 128.
@@ -296,24 +300,46 @@ __device__ __forceinline__ void generate(uint8_t *st, const ChunkFrags<KC> &F, c
 #pragma unroll 1
     for (int q = tid >> 6; q < KC / 8; q += kBatchThreads / 64) {
         float gr[8], gi[8], pr[8], pi[8];
+        // groups of kGenGroup fragments: a group's entries are evaluated
+        // without branches (independent chains the scheduler interleaves)
+        // when any lane of the warp needs one of them, and selected by the
+        // lane's bits; a group no lane needs is skipped
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const float4 *f = F.v[8 * q + j];
-            const float4 w4 = f[3];
-            const unsigned wrx = __float_as_uint(row < 32 ? w4.x : w4.y);
-            const unsigned wsrc = __float_as_uint(row < 32 ? w4.z : w4.w);
-            gr[j] = gi[j] = pr[j] = pi[j] = 0.0f;
-            if (rx_ok && ((wrx >> (row & 31)) & 1u)) {
-                const float2 v = REL ? readout_entry_rel<ATT>(it, f[0], f[2], pt.Drx, pt.R2rx, pt.Erx)
-                                     : readout_entry<ATT>(it, f[0], f[2], pt.prx);
-                gr[j] = v.x;
-                gi[j] = v.y;
+        for (int j0 = 0; j0 < 8; j0 += kGenGroup) {
+            unsigned mrx = 0u, msrc = 0u;
+#pragma unroll
+            for (int j = j0; j < j0 + kGenGroup; ++j) {
+                const float4 w4 = F.v[8 * q + j][3];
+                const unsigned wrx = __float_as_uint(row < 32 ? w4.x : w4.y);
+                const unsigned wsrc = __float_as_uint(row < 32 ? w4.z : w4.w);
+                mrx |= ((wrx >> (row & 31)) & 1u) << (j - j0);
+                msrc |= ((wsrc >> (row & 31)) & 1u) << (j - j0);
             }
-            if (src_ok && ((wsrc >> (row & 31)) & 1u)) {
-                const float2 v = REL ? incident_entry_rel<ATT>(it, pt.Dsrc, pt.R2src, f[1], f[2])
-                                     : incident_entry<ATT>(it, pt.psrc, f[1], f[2]);
-                pr[j] = v.x;
-                pi[j] = v.y;
+            if (!rx_ok) mrx = 0u;
+            if (!src_ok) msrc = 0u;
+#pragma unroll
+            for (int j = j0; j < j0 + kGenGroup; ++j) gr[j] = gi[j] = pr[j] = pi[j] = 0.0f;
+            if (__any_sync(0xffffffffu, mrx != 0u)) {
+#pragma unroll
+                for (int j = j0; j < j0 + kGenGroup; ++j) {
+                    const float4 *f = F.v[8 * q + j];
+                    const float2 v = REL ? readout_entry_rel<ATT>(it, f[0], f[2], pt.Drx, pt.R2rx, pt.Erx)
+                                         : readout_entry<ATT>(it, f[0], f[2], pt.prx);
+                    const bool on = (mrx >> (j - j0)) & 1u;
+                    gr[j] = on ? v.x : 0.0f;
+                    gi[j] = on ? v.y : 0.0f;
+                }
+            }
+            if (__any_sync(0xffffffffu, msrc != 0u)) {
+#pragma unroll
+                for (int j = j0; j < j0 + kGenGroup; ++j) {
+                    const float4 *f = F.v[8 * q + j];
+                    const float2 v = REL ? incident_entry_rel<ATT>(it, pt.Dsrc, pt.R2src, f[1], f[2])
+                                         : incident_entry<ATT>(it, pt.psrc, f[1], f[2]);
+                    const bool on = (msrc >> (j - j0)) & 1u;
+                    pr[j] = on ? v.x : 0.0f;
+                    pi[j] = on ? v.y : 0.0f;
+                }
             }
         }
         uint4 h, l;
