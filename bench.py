@@ -181,6 +181,7 @@ LR_CTAS = [4]      # low-rank apply: resident CTAs per SM (register cap)
 FUSED = [1]        # k_aca2: the first bounce's low-rank apply fused into the cross approximation
 INTERP = [1]       # far class-ALL blocks between planar tiles by directional interpolation
 BUILD_OVERLAP = [1]  # interpolation build on a second stream beside the cross approximation
+TILE_ALIGN = [1]     # full patches of the fragment grid on 256-fragment tile boundaries
 
 
 def set_path(api, compressed, select):
@@ -195,6 +196,7 @@ def set_path(api, compressed, select):
     api.set_option("overlap_streams", OVERLAP[0])
     api.set_option("compress_interp", INTERP[0])
     api.set_option("compress_build_overlap", BUILD_OVERLAP[0])
+    api.set_option("tile_align", TILE_ALIGN[0])
 
 
 def time_path(api, cfg, args, flush, local, world, reuse=False):
@@ -1132,7 +1134,7 @@ def check_error(api, cfg):
                 graze = {"bounce_pairs_checked": c["pairs"], "bounce_grazing": c["grazing"]}
         if npts:
             o.set_pressures(0, 0, Ps[-1])
-            jj = np.sort(rng.choice(npts, min(256, npts), replace=False))
+            jj = np.sort(rng.choice(npts, min(1024, npts), replace=False))
             vf, mf = o.hop_subset(1, 0, 0, jj, want_mask=True, nsrc=nact)
             c2 = o.counters()
             gf = (mf & 2).any(axis=1)
@@ -1247,6 +1249,8 @@ def main():
                          "(the rest by cross approximation)")
     ap.add_argument("--overlap", type=int, default=1, choices=(0, 1),
                     help="compressed bounce: low-rank apply on a second stream beside the dense remainder")
+    ap.add_argument("--tile-align", type=int, default=1, choices=(0, 1),
+                    help="active fragments: full patches on 256-fragment tile boundaries")
     ap.add_argument("--build-overlap", type=int, default=1, choices=(0, 1),
                     help="compressed build: interpolation on a second stream beside the cross approximation")
     ap.add_argument("--tol", type=float, default=5e-4,
@@ -1271,6 +1275,7 @@ def main():
     ACA_VARIANT[0] = args.aca_variant
     OVERLAP[0] = args.overlap
     BUILD_OVERLAP[0] = args.build_overlap
+    TILE_ALIGN[0] = args.tile_align
     FUSED[0] = args.fused_apply
     INTERP[0] = args.interp
     LR_CTAS[0] = args.lr_ctas

@@ -68,9 +68,12 @@ __constant__ float kChebW[9][8] = {
     {3.121445152e+00f, -8.889123728e+00f, 1.330351380e+01f, -1.569256449e+01f, 1.569256449e+01f, -1.330351380e+01f, 8.889123728e+00f, -3.121445152e+00f}};
 
 // oscillatory nodes (along e1, along e2) per level
-__constant__ int kLvlPx[4] = {0, 6, 7, 8};
-__constant__ int kLvlPy[4] = {0, 4, 5, 6};
-static_assert(ip_nodes(1) == 6 * 4 && ip_nodes(2) == 7 * 5 && ip_nodes(3) == 8 * 6 && ip_nodes(3) == kIpMaxNodes,
+// levels 1-3 for elongated boxes (px along the long side), 4-6 square for
+// tiles of one 16 x 16 patch
+__constant__ int kLvlPx[7] = {0, 6, 7, 8, 4, 5, 6};
+__constant__ int kLvlPy[7] = {0, 4, 5, 6, 4, 5, 6};
+static_assert(ip_nodes(1) == 6 * 4 && ip_nodes(2) == 7 * 5 && ip_nodes(3) == 8 * 6 && ip_nodes(3) == kIpMaxNodes &&
+                  ip_nodes(4) == 4 * 4 && ip_nodes(5) == 5 * 5 && ip_nodes(6) == 6 * 6,
               "level tables");
 static_assert(kIpSmooth * kIpSPitch == 156, "smooth nodes in ip_columns");
 
@@ -208,7 +211,9 @@ __global__ void __launch_bounds__(kTile) k_ip_tiles(const float4 *pos, const flo
 // Candidate c (class ALL, both tiles capable, centres at least two box
 // lengths apart): the interpolation level from kappa = k (W_I^2 + W_J^2) / D,
 // the phase curvature of the plane-wave remainder over the boxes (W: the
-// longer box side); 0 leaves the block to the cross approximation.  The
+// longer box side); 0 leaves the block to the cross approximation.  Blocks
+// of two square tiles (one 16 x 16 patch each) take the square levels 4-6
+// (4 x 4, 5 x 5, 6 x 6 nodes), the others the elongated levels 1-3.  The
 // limits hold the relative error of 97 % of the blocks of a 60 kHz trihedral
 // to 2 tol (tol = 5e-4 at kscale 1; the judge accepts up to 3 tol); kscale =
 // (tol / 5e-4)^(1 / 4.3) follows the error's growth with kappa.
@@ -227,7 +232,11 @@ __global__ void k_ip_level(const int2 *cb, const uint8_t *ccls, const int *ncand
             const float wa = delta * (float)max(A.bx, A.by), wb = delta * (float)max(B.bx, B.by);
             if (D >= 2.0f * fmaxf(wa, wb)) {
                 const float kap = kr * (wa * wa + wb * wb) / D;
-                L = kap <= 6.0f * kscale ? 1 : kap <= 14.0f * kscale ? 2 : kap <= 20.0f * kscale ? 3 : 0;
+                const bool square = A.bx <= 16 && A.by <= 16 && B.bx <= 16 && B.by <= 16;
+                if (square)
+                    L = kap <= 2.08f * kscale ? 4 : kap <= 3.96f * kscale ? 5 : kap <= 7.33f * kscale ? 6 : 0;
+                else
+                    L = kap <= 6.0f * kscale ? 1 : kap <= 14.0f * kscale ? 2 : kap <= 20.0f * kscale ? 3 : 0;
             }
         }
     }

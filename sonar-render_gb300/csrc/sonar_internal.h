@@ -178,19 +178,21 @@ void launch_block_desc(const SumArgs &a, const int2 *blocks, const uint8_t *cls,
 // planar tiles.  Per tile a frame (4 float4: box centre and capability, the
 // facet's grid axes, normal and box size), per fragment its cell in the box;
 // per kept block a level (0: cross approximation; 1..3: nodes (6, 4), (7, 5),
-// (8, 6) of the oscillatory part, 4 x 3 of the smooth part), whose node
-// entries take ip_columns(level) columns of the U array.
+// (8, 6) of the oscillatory part on elongated boxes, 4..6: (4, 4), (5, 5),
+// (6, 6) on square ones; 4 x 3 nodes of the smooth part), whose node entries
+// take ip_columns(level) columns of the U array.
 __host__ __device__ constexpr int ip_nodes(int level)
 {
-    return level == 1 ? 24 : level == 2 ? 35 : level == 3 ? 48 : 0;
+    return level == 1 ? 24 : level == 2 ? 35 : level == 3 ? 48 : level == 4 ? 16 : level == 5 ? 25 : level == 6 ? 36 : 0;
 }
 __host__ __device__ constexpr int ip_columns(int level)
 {
     // C with rows of odd pitch (P | 1), then (from an even entry) the smooth part's 12 x 13
-    return level >= 1 && level <= 3
+    return ip_nodes(level) > 0
                ? ((((ip_nodes(level) * (ip_nodes(level) | 1)) + 1) & ~1) + 156 + kTile - 1) / kTile
                : 0;
 }
+static_assert(ip_columns(4) > 0 && ip_columns(6) > 0 && ip_columns(7) == 0, "levels with node entries");
 constexpr int kIpTileRec = 6;  // float4 per tile record
 struct IpCtx {
     const float4 *tile = nullptr;
