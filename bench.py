@@ -1011,6 +1011,7 @@ def run_gb300(args):
                        "accepted": h["cmp_accepted"], "pair_fraction_compressed": round(h["cmp_pairs"] / h["pairs"], 4),
                        "mean_rank": h["cmp_mean_rank"], "max_judged_block_err": h["cmp_max_err"],
                        "interpolated_blocks": h.get("cmp_ip_blocks", 0), "interpolation_mean_nodes": h.get("cmp_ip_nodes", 0.0),
+                       "interpolation_kept": h.get("cmp_ip_kept", 0),
                        "tolerance": TOL[0], "judge_limit": 3.0 * TOL[0], "network_training": train_info,
                        "judge_audit": audit}
     kms = H["kernels_ms_per_step"]

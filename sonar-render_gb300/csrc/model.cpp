@@ -229,7 +229,7 @@ struct HopRecord {
     int nsplit;
     int launches;    // kernels launched by this hop, mask included
     // compressed bounce blocks (FACET_SELF with compression on)
-    int cmp_cand = 0, cmp_blocks = 0, cmp_accepted = 0, cmp_select = 0, cmp_ip_blocks = 0;
+    int cmp_cand = 0, cmp_blocks = 0, cmp_accepted = 0, cmp_select = 0, cmp_ip_blocks = 0, cmp_ip_kept = 0;
     double cmp_mean_rank = 0.0, cmp_max_err = 0.0, cmp_pairs = 0.0, cmp_ip_nodes = 0.0;
     float cmp_build_ms = 0.0f, cmp_select_ms = 0.0f, cmp_aca_ms = 0.0f, cmp_ip_ms = 0.0f, cmp_approx_ms = 0.0f;
     float lr_ms = 0.0f;
@@ -1397,6 +1397,7 @@ void run_hop(int hop, int a, int b)
         rec.cmp_select = g.cmp.select;
         rec.cmp_mean_rank = g.cmp.mean_rank;
         rec.cmp_ip_blocks = g.cmp.nip;
+        rec.cmp_ip_kept = g.cmp.nip_kept;
         rec.cmp_ip_nodes = g.cmp.ip_mean_nodes;
         rec.cmp_max_err = g.cmp.max_err;
         rec.cmp_pairs = g.cmp.pairs_cmp;
@@ -1878,12 +1879,12 @@ int sonar_get_stats(char *json, int cap)
                  "%s{\"hop\": %d, \"pairs\": %lld, \"mask_ms\": %.6f, \"sum_ms\": %.6f, \"total_ms\": %.6f, "
                  "\"nsplit\": %d, \"launches\": %d, \"cmp_select\": %d, \"cmp_cand\": %d, \"cmp_blocks\": %d, "
                  "\"cmp_accepted\": %d, \"cmp_pairs\": %.0f, \"cmp_mean_rank\": %.3f, \"cmp_max_err\": %.3e, "
-                 "\"cmp_ip_blocks\": %d, \"cmp_ip_nodes\": %.3f, "
+                 "\"cmp_ip_blocks\": %d, \"cmp_ip_kept\": %d, \"cmp_ip_nodes\": %.3f, "
                  "\"cmp_build_ms\": %.6f, \"cmp_select_ms\": %.6f, \"cmp_aca_ms\": %.6f, \"cmp_ip_ms\": %.6f, "
                  "\"cmp_approx_ms\": %.6f, \"lr_ms\": %.6f}",
                  i ? ", " : "", r.hop, r.pairs, r.mask_ms, r.sum_ms, r.total_ms, r.nsplit, r.launches, r.cmp_select,
                  r.cmp_cand, r.cmp_blocks, r.cmp_accepted, r.cmp_pairs, r.cmp_mean_rank, r.cmp_max_err,
-                 r.cmp_ip_blocks, r.cmp_ip_nodes, r.cmp_build_ms, r.cmp_select_ms, r.cmp_aca_ms, r.cmp_ip_ms,
+                 r.cmp_ip_blocks, r.cmp_ip_kept, r.cmp_ip_nodes, r.cmp_build_ms, r.cmp_select_ms, r.cmp_aca_ms, r.cmp_ip_ms,
                  r.cmp_approx_ms, r.lr_ms);
         s += buf;
     }
