@@ -173,7 +173,7 @@ def step_pairs(stats):
     return sum(h["pairs"] for h in stats["hops"])
 
 
-RCUT = [24.0]  # the admissibility network proposes blocks with predicted rank below this
+RCUT = [32.0]  # the admissibility network proposes blocks with predicted rank below this
 TOL = [5e-4]   # cross-approximation tolerance (the judge accepts 3 x this RMS error)
 ACA_VARIANT = [8]  # cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
 OVERLAP = [1]      # compressed bounce: low-rank apply on a second stream beside the dense remainder
@@ -1257,7 +1257,7 @@ def main():
     ap.add_argument("--tol", type=float, default=5e-4,
                     help="cross-approximation tolerance of the compressed path (judge limit 3 x tol); the "
                          "default keeps the step's error about 5x below the 1e-3 target")
-    ap.add_argument("--rcut", type=float, default=24.0,
+    ap.add_argument("--rcut", type=float, default=32.0,
                     help="network: propose blocks whose predicted rank is below this")
     ap.add_argument("--select", type=int, default=2,
                     help="compressed blocks: 0 separation rule, 1 every interacting block, 2 the trained network")

@@ -166,7 +166,7 @@ int sonar_get_stats(char *json, int cap);
  * whose every pair interacts and whose tiles are farther apart than
  * "compress_eta" (1.0) times the sum of their radii; 1 every interacting
  * block; 2 the blocks the admissibility network proposes), "compress_rcut"
- * (the network proposes blocks with predicted rank below this, 24).
+ * (the network proposes blocks with predicted rank below this, 32).
  * Returns 0, or < 0 for an unknown key or a failed action. */
 int sonar_set_option(const char *key, double value);
 /* The library's CUDA stream (a cudaStream_t; NULL before render_cuda), for

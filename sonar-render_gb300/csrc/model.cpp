@@ -292,7 +292,7 @@ struct Model {
     float opt_cmp_tol = 1e-4f, opt_cmp_judge = 3e-4f, opt_cmp_eta = 1.0f;
     int opt_cmp_rmax = 32;
     int opt_cmp_select = 0;     // 0 rule (class ALL, eta-separated), 1 every interacting block, 2 the network
-    float opt_cmp_rcut = 24.0f; // network: propose blocks whose predicted rank is below this
+    float opt_cmp_rcut = 32.0f; // network: propose blocks whose predicted rank is below this
     int opt_aca_variant = 8;    // cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
     int opt_lr_ctas = 4;        // low-rank apply: resident CTAs per SM its register cap allows (4, 6, 8)
     int opt_rel_geom = 0;       // source hop and readout: phase distances relative to FP64 references
@@ -394,9 +394,14 @@ void upload(T *dst, const UploadArray<T> &a, size_t n, cudaStream_t s)
 // to the front are the last ones of the partial patches (in patch order):
 // the tile they share with the previous facet's last cells then joins two
 // far ends of the facets' slanted edges rather than two cells on either side
-// of a shared corner, whose near pairs a sampled judge could miss.  Facets
-// stay contiguous and in order (the zero-input rule's facet ends are
-// unchanged); outputs are mapped through act_cell as before.
+// of a shared corner, whose near pairs a sampled judge could miss.  Edge
+// cells -- whose readout centroid (the cell's left edge, without the x
+// shift) lies on or outside the facet's triangle, so on or behind the plane
+// of a facet that shares the edge -- go last: their pairs are gated or
+// shadowed, and grouped in their own tiles they leave the blocks of the
+// other partial tiles free of per-pair bits.  Facets stay contiguous and in
+// order (the zero-input rule's facet ends are unchanged); outputs are mapped
+// through act_cell as before.
 void align_patches(Object &o, const std::vector<long long> &unit_act, const std::vector<long long> &unit0,
                    float4 *act_pos, int *act_facet)
 {
@@ -426,20 +431,44 @@ void align_patches(Object &o, const std::vector<long long> &unit_act, const std:
             }
         }
         if (full.empty() || part.empty()) continue;
-        long long npart = 0;
-        for (auto &r : part) npart += r.second - r.first;
+        // the facet's triangle: inward normals of its edges (FP64)
+        const double v[3][3] = {{F.v1.x, F.v1.y, F.v1.z}, {F.v2.x, F.v2.y, F.v2.z}, {F.v3.x, F.v3.y, F.v3.z}};
+        double nrm[3], ein[3][3], eoff[3], lmax = 1.0;
+        {
+            const double e1[3] = {v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2]};
+            const double e2[3] = {v[2][0] - v[0][0], v[2][1] - v[0][1], v[2][2] - v[0][2]};
+            nrm[0] = e1[1] * e2[2] - e1[2] * e2[1];
+            nrm[1] = e1[2] * e2[0] - e1[0] * e2[2];
+            nrm[2] = e1[0] * e2[1] - e1[1] * e2[0];
+        }
+        for (int q = 0; q < 3; q++) {
+            const double *a = v[q], *b = v[(q + 1) % 3];
+            const double e[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+            lmax = std::max(lmax, std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]));
+            double n[3] = {nrm[1] * e[2] - nrm[2] * e[1], nrm[2] * e[0] - nrm[0] * e[2], nrm[0] * e[1] - nrm[1] * e[0]};
+            const double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            for (int c = 0; c < 3; c++) ein[q][c] = l > 0.0 ? n[c] / l : 0.0;
+            eoff[q] = ein[q][0] * a[0] + ein[q][1] * a[1] + ein[q][2] * a[2];
+        }
+        auto inside = [&](long long k) {
+            const float4 p = act_pos[k];
+            for (int q = 0; q < 3; q++)
+                if (!(ein[q][0] * p.x + ein[q][1] * p.y + ein[q][2] * p.z - eoff[q] > 1e-6 * lmax)) return false;
+            return true;
+        };
+        std::vector<long long> good, edge;
+        for (auto &r : part)
+            for (long long k = r.first; k < r.second; k++) (inside(k) ? good : edge).push_back(k);
+        const long long ngood = (long long)good.size();
         const long long need = (kTile - a0 % kTile) % kTile;
-        if (need > npart) continue;  // cannot align: keep patch order
+        if (need > ngood) continue;  // cannot align: keep patch order
         order.clear();
         order.reserve((size_t)(a1 - a0));
-        std::vector<long long> partseq;
-        partseq.reserve((size_t)npart);
-        for (auto &r : part)
-            for (long long k = r.first; k < r.second; k++) partseq.push_back(k);
-        for (long long i = npart - need; i < npart; i++) order.push_back((int)partseq[(size_t)i]);
+        for (long long i = ngood - need; i < ngood; i++) order.push_back((int)good[(size_t)i]);
         for (auto &r : full)
             for (long long k = r.first; k < r.second; k++) order.push_back((int)k);
-        for (long long i = 0; i < npart - need; i++) order.push_back((int)partseq[(size_t)i]);
+        for (long long i = 0; i < ngood - need; i++) order.push_back((int)good[(size_t)i]);
+        for (long long k : edge) order.push_back((int)k);
         const size_t n = order.size();
         pos.resize(n);
         fac.resize(n);

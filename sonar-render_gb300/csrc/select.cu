@@ -119,7 +119,9 @@ __device__ __forceinline__ int cap_of(const float *pred, int c, float cut, int r
     return max(4, min(rmax, (int)ceilf(1.5f * r) + 4));
 }
 
-// kept blocks and their caps per candidate row J
+// kept blocks and their caps per candidate row J; a block with an
+// interpolation level is kept whatever the network predicts (its node count
+// does not depend on the cross approximation's rank)
 // factor columns a kept block reserves: its rank cap, or an interpolated
 // block's node entries
 __device__ __forceinline__ int cols_of(const uint8_t *clev, int c, int cap)
@@ -137,6 +139,7 @@ __global__ void __launch_bounds__(kSelThreads) k_keep_count(const int *coff, con
     for (int c = c0 + threadIdx.x; c < c1; c += kSelThreads) {
         bool keep;
         const int cap = cap_of(pred, c, cut, rmax, keep);
+        keep = keep || (clev && clev[c]);
         if (keep) {
             k += 1;
             s += cols_of(clev, c, cap);
@@ -166,6 +169,7 @@ __global__ void __launch_bounds__(kSelThreads) k_keep_fill(const int *coff, cons
         int cap = 0, cols = 0;
         if (c < c1) {
             cap = cap_of(pred, c, cut, rmax, keep);
+            keep = keep || (clev && clev[c]);
             cols = cols_of(clev, c, cap);
         }
         int tk, tc;
