@@ -148,6 +148,11 @@ int sonar_get_stats(char *json, int cap);
  * forward into the higher-index object, reciprocal into the lower, all
  * from the bounce's inputs).
  * "aca_variant" (cross-approximation kernel shape, 0-2; bit-identical).
+ * "tile_align" (1, default: each facet's full 16 x 16-cell patches start on
+ * 256-fragment tile boundaries and its edge cells -- readout centroid on or
+ * outside the triangle -- come last; 0: plain patch order; the order is
+ * internal, outputs are the same up to FP32 summation order; read by
+ * render_cuda).
  * "overlap_streams" (1, default: a compressed bounce runs its low-rank apply
  * on a second stream beside the dense remainder, joined before the
  * finalize; 0: one stream; the same results either way).
