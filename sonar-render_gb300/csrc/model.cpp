@@ -15,6 +15,7 @@
 //   - all work runs on one library stream; each entry point returns after the
 //     stream is idle, as the reference's DoProjection does (OptiX.cpp:163).
 #include <algorithm>
+#include <tuple>
 #include <array>
 #include <chrono>
 #include <cmath>
@@ -390,11 +391,15 @@ void upload(T *dst, const UploadArray<T> &a, size_t n, cudaStream_t s)
 // of 32 x 16 cells, half of it empty).  Within each facet this moves just
 // enough cells of its partial patches in front of its full patches to bring
 // the first full patch onto a tile boundary (all full patches then follow on
-// boundaries), the rest of the partial cells after them.  The cells moved
-// to the front are the last ones of the partial patches (in patch order):
-// the tile they share with the previous facet's last cells then joins two
-// far ends of the facets' slanted edges rather than two cells on either side
-// of a shared corner, whose near pairs a sampled judge could miss.  Edge
+// boundaries), the rest of the partial cells after them.  The partial
+// patches are taken along the facet's boundary -- those left of each patch
+// row's full patches upwards, the rows without full patches, those right of
+// them downwards -- so that consecutive ones are neighbours and the tiles
+// they form stay compact.  The cells moved to the front are the last ones
+// of that sequence: the tile they share with the previous facet's last
+// cells then joins two far ends of the facets' slanted edges rather than two
+// cells on either side of a shared corner, whose near pairs a sampled judge
+// could miss.  Edge
 // cells -- whose readout centroid (the cell's left edge, without the x
 // shift) lies on or outside the facet's triangle, so on or behind the plane
 // of a facet that shares the edge -- go last: their pairs are gated or
@@ -431,6 +436,32 @@ void align_patches(Object &o, const std::vector<long long> &unit_act, const std:
             }
         }
         if (full.empty() || part.empty()) continue;
+        // partial patches along the boundary: left of the full ones (rows
+        // upwards), rows without full patches, right of the full ones (rows downwards)
+        {
+            const int npx = (F.nx + kPatch - 1) / kPatch, npy = (F.ny + kPatch - 1) / kPatch;
+            auto patch_of = [&](long long k) {
+                const long long c = o.act_cell[(size_t)k] - o.cell0[f];
+                return std::make_pair((int)(c / F.nx) / kPatch, (int)(c % F.nx) / kPatch);  // (row, column)
+            };
+            std::vector<int> fmin(npy, INT32_MAX), fmax(npy, -1);
+            for (auto &r : full) {
+                const auto rc = patch_of(r.first);
+                fmin[rc.first] = std::min(fmin[rc.first], rc.second);
+                fmax[rc.first] = std::max(fmax[rc.first], rc.second);
+            }
+            auto key = [&](const std::pair<long long, long long> &r) {
+                const auto rc = patch_of(r.first);
+                const int row = rc.first, col = rc.second;
+                if (fmax[row] < 0) return std::make_tuple(1, row, col);           // no full patch in the row
+                if (col < fmin[row]) return std::make_tuple(0, row, col);         // left, upwards
+                return std::make_tuple(2, -row, col);                             // right, downwards
+            };
+            std::stable_sort(part.begin(), part.end(),
+                             [&](const std::pair<long long, long long> &x, const std::pair<long long, long long> &y) {
+                                 return key(x) < key(y);
+                             });
+        }
         // the facet's triangle: inward normals of its edges (FP64)
         const double v[3][3] = {{F.v1.x, F.v1.y, F.v1.z}, {F.v2.x, F.v2.y, F.v2.z}, {F.v3.x, F.v3.y, F.v3.z}};
         double nrm[3], ein[3][3], eoff[3], lmax = 1.0;
