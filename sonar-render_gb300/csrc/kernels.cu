@@ -1114,6 +1114,11 @@ __global__ void __launch_bounds__(32 * kClsWarps) k_mask_classify_f2f(MaskArgs a
     const int J = (a.upper_only ? I : 0) + (int)blockIdx.x * kClsWarps + warp;
     const int nt = a.mask.ntiles, nb = a.mask.ndstblocks;
     if (J >= nb || I >= nt) return;  // warp-uniform; no block-wide barrier below
+    if (a.src_frange && a.dst_frange) {
+        // both tiles inside one facet: no pair interacts (the flag stays NONE)
+        const int2 fs = __ldg(a.src_frange + I), fd = __ldg(a.dst_frange + J);
+        if (fs.x == fs.y && fd.x == fd.y && fs.x == fd.x) return;
+    }
     const int i0 = I * kTile, j0 = J * kTile;
     const int ni = min(kTile, a.nsrc - i0), nj = min(kTile, a.ndst - j0);
     // this lane's points: q = lane + 32 m, m < 8, of both tiles
@@ -2868,31 +2873,30 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
     s = t;
 }
 
-__global__ void __launch_bounds__(kTile) k_lr_gather(int n, const float2 *brow, const float2 *bcol,
-                                                     const int *byJ_off, const int *byJ, const int *byI_off,
-                                                     const int *byI, const int *bidx, double2 *yrow, double2 *ycol)
+// One CTA of 2 x 256 threads per tile X: the first 256 threads add the row
+// outputs of the blocks (., X) into yrow, the other 256 the column outputs of
+// the blocks (X, .) into ycol, each in list order (compensated FP32, FP64 at
+// the end).  The two lists are independent chains of loads, so splitting them
+// halves the dependent work per thread.
+__global__ void __launch_bounds__(2 * kTile) k_lr_gather(int n, const float2 *brow, const float2 *bcol,
+                                                         const int *byJ_off, const int *byJ, const int *byI_off,
+                                                         const int *byI, const int *bidx, double2 *yrow,
+                                                         double2 *ycol)
 {
-    const int X = blockIdx.x, t = threadIdx.x;
+    const int X = blockIdx.x, t = threadIdx.x & (kTile - 1);
+    const bool cols = threadIdx.x >= kTile;  // warp-uniform
     const int q = X * kTile + t;
-    float fr = 0.0f, fi = 0.0f, cr = 0.0f, ci = 0.0f;
-    float efr = 0.0f, efi = 0.0f, ecr = 0.0f, eci = 0.0f;
-    const int j0 = byJ_off[X], j1 = byJ_off[X + 1], i0 = byI_off[X], i1 = byI_off[X + 1];
+    const int p0 = cols ? byI_off[X] : byJ_off[X], p1 = cols ? byI_off[X + 1] : byJ_off[X + 1];
+    const int *list = cols ? byI : byJ;
+    const float2 *src = cols ? bcol : brow;
+    float fr = 0.0f, fi = 0.0f, efr = 0.0f, efi = 0.0f;
 #pragma unroll 4
-    for (int p = j0; p < j1; ++p) {
-        const float2 v = __ldg(brow + (size_t)bidx[byJ[p]] * kTile + t);
+    for (int p = p0; p < p1; ++p) {
+        const float2 v = __ldg(src + (size_t)bidx[list[p]] * kTile + t);
         kahan_add(fr, efr, v.x);
         kahan_add(fi, efi, v.y);
     }
-#pragma unroll 4
-    for (int p = i0; p < i1; ++p) {
-        const float2 v = __ldg(bcol + (size_t)bidx[byI[p]] * kTile + t);
-        kahan_add(cr, ecr, v.x);
-        kahan_add(ci, eci, v.y);
-    }
-    if (q < n) {
-        yrow[q] = make_double2((double)fr - (double)efr, (double)fi - (double)efi);
-        ycol[q] = make_double2((double)cr - (double)ecr, (double)ci - (double)eci);
-    }
+    if (q < n) (cols ? ycol : yrow)[q] = make_double2((double)fr - (double)efr, (double)fi - (double)efi);
 }
 
 // Per-tile geometry for block descriptors: centroid, radius, mean normal.
@@ -3355,7 +3359,7 @@ void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off,
                             ip->list, ip->n, rank, ip->status);
     }
     if (ntiles > 0)
-        k_lr_gather<<<ntiles, kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, bidx, yrow, ycol);
+        k_lr_gather<<<ntiles, 2 * kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, bidx, yrow, ycol);
 }
 
 void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s)

@@ -109,13 +109,14 @@ struct Object {
     double2 *d_P = nullptr, *d_Pin = nullptr, *d_Pout = nullptr;
     float4 *d_act_pos = nullptr;
     int *d_act_facet = nullptr, *d_act_cell = nullptr, *d_facet_end = nullptr;
+    int2 *d_tile_frange = nullptr;  // per 256-fragment tile: lowest and highest facet index
 
     int nact() const { return (int)act_cell.size(); }
     void free_device()
     {
         dfree(d_cell_pos); dfree(d_cell_facet); dfree(d_facet_n); dfree(d_facet_grid); dfree(d_P); dfree(d_Pin);
         dfree(d_Pout);
-        dfree(d_act_pos); dfree(d_act_facet); dfree(d_act_cell); dfree(d_facet_end);
+        dfree(d_act_pos); dfree(d_act_facet); dfree(d_act_cell); dfree(d_facet_end); dfree(d_tile_frange);
     }
 };
 
@@ -627,6 +628,16 @@ void render_object(Object &o)
         upload(o.d_act_pos, act_pos, na, s);
         upload(o.d_act_facet, act_facet, na, s);
         CK(stage_to_device(o.d_act_cell, o.act_cell.data(), na * sizeof(int), s));
+        const size_t ntl = (na + kTile - 1) / kTile;
+        std::vector<int2> fr(ntl, make_int2(INT32_MAX, -1));
+        for (size_t k = 0; k < na; k++) {
+            int2 &r = fr[k / kTile];
+            r.x = std::min(r.x, act_facet[k]);
+            r.y = std::max(r.y, act_facet[k]);
+        }
+        o.d_tile_frange = dalloc<int2>(ntl);
+        CK(stage_to_device(o.d_tile_frange, fr.data(), ntl * sizeof(int2), s));
+        g.h2d_bytes += (long long)(ntl * sizeof(int2));
     }
     CK(stage_to_device(o.d_facet_end, o.facet_act_end.data(), o.facet_act_end.size() * sizeof(int), s));
     g.h2d_bytes += (long long)(nc * (sizeof(float4) + sizeof(int)) + facet_n.size() * sizeof(float4) +
@@ -815,6 +826,7 @@ HopSets hop_sets(int hop, int a, int b)
         m.src_pos = m.dst_pos = A.d_act_pos;
         m.src_facet = m.dst_facet = A.d_act_facet;
         m.src_facet_n = m.dst_facet_n = A.d_facet_n;
+        m.src_frange = m.dst_frange = A.d_tile_frange;
     } else if (hop == HOP_RESP) {
         // FACET_RESP between two targets: sources of a, destinations of b; the
         // ray starts at the lower-index object's point

@@ -82,6 +82,9 @@ struct MaskArgs {
     int resp_dst_origin = 0;        // FACET_RESP: the ray starts at the destination point
     int convex = 0;                 // every target vertex on or behind every target triangle's plane
     float convex_vmax = 0.0f;       // largest |coordinate| of the target vertices
+    // optional: per source tile / destination block, the lowest and highest
+    // facet index of its fragments (blocks within one facet skip their loads)
+    const int2 *src_frange = nullptr, *dst_frange = nullptr;
 };
 
 struct SumArgs {
