@@ -405,9 +405,9 @@ def ip_roofline(stats, fp32_peak):
     ach = nb * flop_block / (ms * 1e-3) / 1e12
     peak = fp32_peak / 1e12
     # DRAM: the node entries written once; the ncu capture at 40 kHz wrote
-    # 88.6 MB for 8,158 blocks of mean 39.6 nodes (10.9 KB per block), here
+    # 77.7 MB for 11,535 blocks of mean 28.2 nodes (6.7 KB per block), here
     # scaled by the stored entries per block
-    traffic = nb * (P * P + 156) * 8.0 * (88.6e6 / (8158 * (39.6 * 39.6 + 156) * 8.0))
+    traffic = nb * (P * P + 156) * 8.0 * (77.7e6 / (11535 * (28.2 * 28.2 + 156) * 8.0))
     return {"kernel": "k_ip build (directional interpolation: node entries + 8 x 8 exact-entry judge + first bounce's "
                       "apply)", "bound": "fp32 issue / barrier latency (seven dependent phases per block)",
             "achieved": round(ach, 3), "peak": round(peak, 3), "unit": "TFLOP/s", "frac": round(ach / peak, 4),
