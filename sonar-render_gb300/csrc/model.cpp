@@ -409,59 +409,47 @@ void upload(T *dst, const UploadArray<T> &a, size_t n, cudaStream_t s)
 // order (the zero-input rule's facet ends are unchanged); outputs are mapped
 // through act_cell as before.
 void align_patches(Object &o, const std::vector<long long> &unit_act, const std::vector<long long> &unit0,
-                   float4 *act_pos, int *act_facet)
+                   const std::vector<std::vector<int>> &patch_cnt, float4 *act_pos, int *act_facet)
 {
+    struct Run {
+        long long b, e;  // [b, e) in the active order
+        int row, col;    // patch row and column
+    };
     const int nf = (int)o.facets.size();
-    std::vector<int> order;
-    std::vector<float4> pos;
-    std::vector<int> fac, cell;
-    for (int f = 0; f < nf; f++) {
+    parallel_units(nf, [&](long long fl) {
+        const int f = (int)fl;
         const long long a0 = unit_act[(size_t)unit0[f]], a1 = unit_act[(size_t)unit0[f + 1]];
-        if (a1 - a0 < 2 * kTile) continue;
+        if (a1 - a0 < 2 * kTile) return;
         const FacetFrame &F = o.facets[f];
-        // runs of consecutive cells of one patch; full when all 256 cells are active
-        std::vector<std::pair<long long, long long>> full, part;  // [begin, end)
-        long long b = a0;
-        int pid = -1;
-        for (long long k = a0; k <= a1; k++) {
-            int q = -1;
-            if (k < a1) {
-                const long long c = o.act_cell[(size_t)k] - o.cell0[f];
-                const int x = (int)(c % F.nx), y = (int)(c / F.nx);
-                q = (y / kPatch) * ((F.nx + kPatch - 1) / kPatch) + x / kPatch;
-            }
-            if (k == a1 || q != pid) {
-                if (k > b) (k - b == (long long)kPatch * kPatch ? full : part).push_back({b, k});
-                b = k;
-                pid = q;
+        // the patches in patch order, from the counts pass 2 recorded; full
+        // when all 256 cells are active
+        std::vector<Run> full, part;
+        for (long long u = unit0[f]; u < unit0[f + 1]; u++) {
+            long long b = unit_act[(size_t)u];
+            const std::vector<int> &pc = patch_cnt[(size_t)u];
+            for (int c = 0; c < (int)pc.size(); c++) {
+                if (pc[c] == 0) continue;
+                const Run r{b, b + pc[c], (int)(u - unit0[f]), c};
+                (pc[c] == kPatch * kPatch ? full : part).push_back(r);
+                b += pc[c];
             }
         }
-        if (full.empty() || part.empty()) continue;
+        if (full.empty() || part.empty()) return;
         // partial patches along the boundary: left of the full ones (rows
         // upwards), rows without full patches, right of the full ones (rows downwards)
         {
-            const int npx = (F.nx + kPatch - 1) / kPatch, npy = (F.ny + kPatch - 1) / kPatch;
-            auto patch_of = [&](long long k) {
-                const long long c = o.act_cell[(size_t)k] - o.cell0[f];
-                return std::make_pair((int)(c / F.nx) / kPatch, (int)(c % F.nx) / kPatch);  // (row, column)
-            };
+            const int npy = (F.ny + kPatch - 1) / kPatch;
             std::vector<int> fmin(npy, INT32_MAX), fmax(npy, -1);
-            for (auto &r : full) {
-                const auto rc = patch_of(r.first);
-                fmin[rc.first] = std::min(fmin[rc.first], rc.second);
-                fmax[rc.first] = std::max(fmax[rc.first], rc.second);
+            for (const Run &r : full) {
+                fmin[r.row] = std::min(fmin[r.row], r.col);
+                fmax[r.row] = std::max(fmax[r.row], r.col);
             }
-            auto key = [&](const std::pair<long long, long long> &r) {
-                const auto rc = patch_of(r.first);
-                const int row = rc.first, col = rc.second;
-                if (fmax[row] < 0) return std::make_tuple(1, row, col);           // no full patch in the row
-                if (col < fmin[row]) return std::make_tuple(0, row, col);         // left, upwards
-                return std::make_tuple(2, -row, col);                             // right, downwards
+            auto key = [&](const Run &r) {
+                if (fmax[r.row] < 0) return std::make_tuple(1, r.row, r.col);   // no full patch in the row
+                if (r.col < fmin[r.row]) return std::make_tuple(0, r.row, r.col);  // left, upwards
+                return std::make_tuple(2, -r.row, r.col);                          // right, downwards
             };
-            std::stable_sort(part.begin(), part.end(),
-                             [&](const std::pair<long long, long long> &x, const std::pair<long long, long long> &y) {
-                                 return key(x) < key(y);
-                             });
+            std::stable_sort(part.begin(), part.end(), [&](const Run &x, const Run &y) { return key(x) < key(y); });
         }
         // the facet's triangle: inward normals of its edges (FP64)
         const double v[3][3] = {{F.v1.x, F.v1.y, F.v1.z}, {F.v2.x, F.v2.y, F.v2.z}, {F.v3.x, F.v3.y, F.v3.z}};
@@ -488,34 +476,31 @@ void align_patches(Object &o, const std::vector<long long> &unit_act, const std:
                 if (!(ein[q][0] * p.x + ein[q][1] * p.y + ein[q][2] * p.z - eoff[q] > 1e-6 * lmax)) return false;
             return true;
         };
-        std::vector<long long> good, edge;
-        for (auto &r : part)
-            for (long long k = r.first; k < r.second; k++) (inside(k) ? good : edge).push_back(k);
+        std::vector<int> good, edge;
+        for (const Run &r : part)
+            for (long long k = r.b; k < r.e; k++) (inside(k) ? good : edge).push_back((int)k);
         const long long ngood = (long long)good.size();
         const long long need = (kTile - a0 % kTile) % kTile;
-        if (need > ngood) continue;  // cannot align: keep patch order
-        order.clear();
+        if (need > ngood) return;  // cannot align: keep patch order
+        std::vector<int> order;
         order.reserve((size_t)(a1 - a0));
-        for (long long i = ngood - need; i < ngood; i++) order.push_back((int)good[(size_t)i]);
-        for (auto &r : full)
-            for (long long k = r.first; k < r.second; k++) order.push_back((int)k);
-        for (long long i = 0; i < ngood - need; i++) order.push_back((int)good[(size_t)i]);
-        for (long long k : edge) order.push_back((int)k);
+        order.insert(order.end(), good.end() - need, good.end());
+        for (const Run &r : full)
+            for (long long k = r.b; k < r.e; k++) order.push_back((int)k);
+        order.insert(order.end(), good.begin(), good.end() - need);
+        order.insert(order.end(), edge.begin(), edge.end());
         const size_t n = order.size();
-        pos.resize(n);
-        fac.resize(n);
-        cell.resize(n);
+        std::vector<float4> pos(n);
+        std::vector<int> fac(n), cell(n);
         for (size_t i = 0; i < n; i++) {
             pos[i] = act_pos[order[i]];
             fac[i] = act_facet[order[i]];
             cell[i] = o.act_cell[(size_t)order[i]];
         }
-        for (size_t i = 0; i < n; i++) {
-            act_pos[a0 + i] = pos[i];
-            act_facet[a0 + i] = fac[i];
-            o.act_cell[(size_t)(a0 + i)] = cell[i];
-        }
-    }
+        memcpy(act_pos + a0, pos.data(), n * sizeof(float4));
+        memcpy(act_facet + a0, fac.data(), n * sizeof(int));
+        memcpy(o.act_cell.data() + a0, cell.data(), n * sizeof(int));
+    });
 }
 
 void render_object(Object &o)
@@ -574,13 +559,17 @@ void render_object(Object &o)
     UploadArray<float4> act_pos((size_t)na_total);
     UploadArray<int> act_facet((size_t)na_total);
     o.act_cell.resize((size_t)na_total);
+    std::vector<std::vector<int>> patch_cnt((size_t)nunits);  // active cells of each patch of a unit
     parallel_units(nunits, [&](long long u) {
         const int f = unit_facet[(size_t)u];
         const FacetFrame &F = o.facets[f];
         const int py = (int)(u - unit0[f]) * kPatch;
         const float *A = o.area.data() + o.cell0[f];
         size_t k = (size_t)unit_act[(size_t)u];
-        for (int px = 0; px < F.nx; px += kPatch)
+        std::vector<int> &pc = patch_cnt[(size_t)u];
+        pc.reserve((size_t)((F.nx + kPatch - 1) / kPatch));
+        for (int px = 0; px < F.nx; px += kPatch) {
+            const size_t k0 = k;
             for (int y = py; y < std::min(F.ny, py + kPatch); y++)
                 for (int x = px; x < std::min(F.nx, px + kPatch); x++) {
                     const float a = A[(long long)y * F.nx + x];
@@ -591,12 +580,14 @@ void render_object(Object &o)
                     o.act_cell[k] = (int)(o.cell0[f] + (long long)y * F.nx + x);
                     k++;
                 }
+            pc.push_back((int)(k - k0));
+        }
     });
     for (int f = 0; f < nf; f++) {
         o.facet_act_end[f] = (int)unit_act[(size_t)unit0[f + 1]];
         o.facet_nact[f] = unit_act[(size_t)unit0[f + 1]] - unit_act[(size_t)unit0[f]];
     }
-    if (g.opt_tile_align) align_patches(o, unit_act, unit0, act_pos.data(), act_facet.data());
+    if (g.opt_tile_align) align_patches(o, unit_act, unit0, patch_cnt, act_pos.data(), act_facet.data());
     const size_t nc = (size_t)o.ncells, na = o.act_cell.size();
     const double t1 = host_ms();
     g.render_ms[1] += t1 - t0;
