@@ -214,6 +214,15 @@ int sonar_audit_compression(int nsample, unsigned seed, float *full_err, float *
  * count, or < 0 for invalid arguments. */
 long long sonar_fragment_triangle(const float *tri9, float delta, int *nx_ny_neg, float *frame17, float *areas,
                                   long long cap);
+/* Host only (no GPU needed), no counterpart in the reference: the order in
+ * which render_cuda stores one triangle's active fragments when its first
+ * active fragment has index start in the object (option "tile_align", on by
+ * default): xy gets (x, y) grid cells, 2 ints per active fragment, when cap
+ * holds them all.  Full 16 x 16-cell patches start on 256-fragment tile
+ * boundaries; partial patches follow the triangle's boundary; cells whose
+ * readout centroid lies on or outside the triangle come last.  Returns the
+ * number of active fragments, or < 0 for invalid arguments. */
+long long sonar_tile_order(const float *tri9, float delta, long long start, int *xy, long long cap);
 
 /* Admissibility network for the low-rank bounce blocks (no counterpart in the
  * reference): a perceptron 8 -> w -> w -> w -> 1 with ReLU, hidden width w =

@@ -92,6 +92,8 @@ def load_library(path: str | None = None, build: bool = False):
     L.sonar_measure_peak.restype = C.c_double
     L.sonar_fragment_triangle.argtypes = [_f, C.c_float, _i, _f, _f, C.c_longlong]
     L.sonar_fragment_triangle.restype = C.c_longlong
+    L.sonar_tile_order.argtypes = [_f, C.c_float, C.c_longlong, _i, C.c_longlong]
+    L.sonar_tile_order.restype = C.c_longlong
     _lib = L
     return L
 
@@ -332,6 +334,21 @@ def fragment_triangle(tri9, delta):
                               fr.ctypes.data_as(_f), a.ctypes.data_as(_f), n)
     nx, ny, neg = (int(v) for v in ints)
     return (nx, ny, neg), fr, a[:n].reshape(ny, nx)
+
+
+def tile_order(tri9, delta, start=0):
+    """Host-only: the (x, y) grid cells of one triangle's active fragments in
+    the order render_cuda stores them when the first one has index start
+    (see sonar_tile_order); an (n, 2) int32 array."""
+    L = lib()
+    t = np.ascontiguousarray(np.asarray(tri9, dtype=np.float32).reshape(9))
+    n = L.sonar_tile_order(t.ctypes.data_as(_f), C.c_float(delta), C.c_longlong(start), None, 0)
+    if n < 0:
+        raise SonarError("sonar_tile_order failed (%d)" % n)
+    xy = np.zeros((max(n, 1), 2), np.int32)
+    L.sonar_tile_order(t.ctypes.data_as(_f), C.c_float(delta), C.c_longlong(start), xy.ctypes.data_as(_i),
+                       C.c_longlong(n))
+    return xy[:n]
 
 
 def run_scene(cfg, bounces=None, field_objects=True, field_points=True):

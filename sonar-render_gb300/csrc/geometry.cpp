@@ -12,6 +12,7 @@
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <thread>
 
 #include "host.h"
@@ -413,6 +414,73 @@ BvhHost build_bvh(const std::vector<std::array<float, 9>> &tris, double pad)
         }
     }
     return out;
+}
+
+std::vector<int> patch_aligned_order(const FacetFrame &F, const std::vector<PatchRun> &runs, const float4 *readout,
+                                     long long start)
+{
+    std::vector<PatchRun> full, part;
+    for (const PatchRun &r : runs) (r.end - r.begin == (long long)kPatch * kPatch ? full : part).push_back(r);
+    if (full.empty() || part.empty()) return {};
+    // partial patches along the boundary: left of the full ones (rows
+    // upwards), rows without full patches, right of the full ones (rows downwards)
+    {
+        const int npy = (F.ny + kPatch - 1) / kPatch;
+        std::vector<int> fmin(std::max(npy, 1), INT32_MAX), fmax(std::max(npy, 1), -1);
+        for (const PatchRun &r : full) {
+            fmin[r.row] = std::min(fmin[r.row], r.col);
+            fmax[r.row] = std::max(fmax[r.row], r.col);
+        }
+        auto key = [&](const PatchRun &r) {
+            if (fmax[r.row] < 0) return std::make_tuple(1, r.row, r.col);   // no full patch in the row
+            if (r.col < fmin[r.row]) return std::make_tuple(0, r.row, r.col);  // left, upwards
+            return std::make_tuple(2, -r.row, r.col);                          // right, downwards
+        };
+        std::stable_sort(part.begin(), part.end(),
+                         [&](const PatchRun &x, const PatchRun &y) { return key(x) < key(y); });
+    }
+    // the facet's triangle: inward normals of its edges (FP64)
+    const double v[3][3] = {{F.v1.x, F.v1.y, F.v1.z}, {F.v2.x, F.v2.y, F.v2.z}, {F.v3.x, F.v3.y, F.v3.z}};
+    double nrm[3], ein[3][3], eoff[3], lmax = 1.0;
+    {
+        const double e1[3] = {v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2]};
+        const double e2[3] = {v[2][0] - v[0][0], v[2][1] - v[0][1], v[2][2] - v[0][2]};
+        nrm[0] = e1[1] * e2[2] - e1[2] * e2[1];
+        nrm[1] = e1[2] * e2[0] - e1[0] * e2[2];
+        nrm[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    }
+    for (int q = 0; q < 3; q++) {
+        const double *a = v[q], *b = v[(q + 1) % 3];
+        const double e[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+        lmax = std::max(lmax, std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]));
+        const double n[3] = {nrm[1] * e[2] - nrm[2] * e[1], nrm[2] * e[0] - nrm[0] * e[2],
+                             nrm[0] * e[1] - nrm[1] * e[0]};
+        const double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int c = 0; c < 3; c++) ein[q][c] = l > 0.0 ? n[c] / l : 0.0;
+        eoff[q] = ein[q][0] * a[0] + ein[q][1] * a[1] + ein[q][2] * a[2];
+    }
+    auto inside = [&](long long k) {
+        const float4 p = readout[k];
+        for (int q = 0; q < 3; q++)
+            if (!(ein[q][0] * p.x + ein[q][1] * p.y + ein[q][2] * p.z - eoff[q] > 1e-6 * lmax)) return false;
+        return true;
+    };
+    std::vector<int> good, edge;
+    for (const PatchRun &r : part)
+        for (long long k = r.begin; k < r.end; k++) (inside(k) ? good : edge).push_back((int)k);
+    const long long ngood = (long long)good.size();
+    const long long need = (kTile - start % kTile) % kTile;
+    if (need > ngood) return {};
+    long long n = 0;
+    for (const PatchRun &r : runs) n += r.end - r.begin;
+    std::vector<int> order;
+    order.reserve((size_t)n);
+    order.insert(order.end(), good.end() - need, good.end());
+    for (const PatchRun &r : full)
+        for (long long k = r.begin; k < r.end; k++) order.push_back((int)k);
+    order.insert(order.end(), good.begin(), good.end() - need);
+    order.insert(order.end(), edge.begin(), edge.end());
+    return order;
 }
 
 }  // namespace sonar

@@ -41,6 +41,27 @@ void parallel_units(long long n, const std::function<void(long long)> &fn);
 // (src/OptiX.cu:129, :210, :273).
 Vec3 fragment_centroid(const FacetFrame &f, int x, int y, bool source_hop);
 
+// Side, in cells, of the patches that order a facet's active fragments.
+constexpr int kPatch = 16;
+
+// A patch's active cells, consecutive in patch order: [begin, end) counted
+// from the facet's first active cell; its patch row and column.
+struct PatchRun {
+    long long begin, end;
+    int row, col;
+};
+
+// Patch-aligned order of one facet's active cells (given in patch order by
+// their runs and readout centroids, the first of them at global index
+// start): order[i] is the patch-order index of the cell placed at i.  Full
+// patches start on 256-cell tile boundaries, a few cells of the partial
+// patches (taken along the facet's boundary) in front of them and the rest
+// after, the edge cells (readout centroid on or outside the triangle) last.
+// Empty when the facet has no full or no partial patch, or too few partial
+// cells to align: patch order stays.
+std::vector<int> patch_aligned_order(const FacetFrame &F, const std::vector<PatchRun> &runs, const float4 *readout,
+                                     long long start);
+
 struct BvhHost {
     std::vector<BvhNode> nodes;
     std::vector<float4> tris;  // 4 per triangle

@@ -41,7 +41,6 @@ bool write_png(const std::string &path, int width, int height, const unsigned ch
 namespace {
 
 constexpr int OBJ_TARGET = 0, OBJ_SOURCE = 1, OBJ_FIELD = 2;
-constexpr int kPatch = 16;  // side, in cells, of the patches that order active fragments
 
 struct Error : std::runtime_error {
     int code;
@@ -411,91 +410,31 @@ void upload(T *dst, const UploadArray<T> &a, size_t n, cudaStream_t s)
 void align_patches(Object &o, const std::vector<long long> &unit_act, const std::vector<long long> &unit0,
                    const std::vector<std::vector<int>> &patch_cnt, float4 *act_pos, int *act_facet)
 {
-    struct Run {
-        long long b, e;  // [b, e) in the active order
-        int row, col;    // patch row and column
-    };
     const int nf = (int)o.facets.size();
     parallel_units(nf, [&](long long fl) {
         const int f = (int)fl;
         const long long a0 = unit_act[(size_t)unit0[f]], a1 = unit_act[(size_t)unit0[f + 1]];
         if (a1 - a0 < 2 * kTile) return;
-        const FacetFrame &F = o.facets[f];
-        // the patches in patch order, from the counts pass 2 recorded; full
-        // when all 256 cells are active
-        std::vector<Run> full, part;
+        // the patches in patch order, from the counts pass 2 recorded
+        std::vector<PatchRun> runs;
         for (long long u = unit0[f]; u < unit0[f + 1]; u++) {
-            long long b = unit_act[(size_t)u];
+            long long b = unit_act[(size_t)u] - a0;
             const std::vector<int> &pc = patch_cnt[(size_t)u];
             for (int c = 0; c < (int)pc.size(); c++) {
                 if (pc[c] == 0) continue;
-                const Run r{b, b + pc[c], (int)(u - unit0[f]), c};
-                (pc[c] == kPatch * kPatch ? full : part).push_back(r);
+                runs.push_back(PatchRun{b, b + pc[c], (int)(u - unit0[f]), c});
                 b += pc[c];
             }
         }
-        if (full.empty() || part.empty()) return;
-        // partial patches along the boundary: left of the full ones (rows
-        // upwards), rows without full patches, right of the full ones (rows downwards)
-        {
-            const int npy = (F.ny + kPatch - 1) / kPatch;
-            std::vector<int> fmin(npy, INT32_MAX), fmax(npy, -1);
-            for (const Run &r : full) {
-                fmin[r.row] = std::min(fmin[r.row], r.col);
-                fmax[r.row] = std::max(fmax[r.row], r.col);
-            }
-            auto key = [&](const Run &r) {
-                if (fmax[r.row] < 0) return std::make_tuple(1, r.row, r.col);   // no full patch in the row
-                if (r.col < fmin[r.row]) return std::make_tuple(0, r.row, r.col);  // left, upwards
-                return std::make_tuple(2, -r.row, r.col);                          // right, downwards
-            };
-            std::stable_sort(part.begin(), part.end(), [&](const Run &x, const Run &y) { return key(x) < key(y); });
-        }
-        // the facet's triangle: inward normals of its edges (FP64)
-        const double v[3][3] = {{F.v1.x, F.v1.y, F.v1.z}, {F.v2.x, F.v2.y, F.v2.z}, {F.v3.x, F.v3.y, F.v3.z}};
-        double nrm[3], ein[3][3], eoff[3], lmax = 1.0;
-        {
-            const double e1[3] = {v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2]};
-            const double e2[3] = {v[2][0] - v[0][0], v[2][1] - v[0][1], v[2][2] - v[0][2]};
-            nrm[0] = e1[1] * e2[2] - e1[2] * e2[1];
-            nrm[1] = e1[2] * e2[0] - e1[0] * e2[2];
-            nrm[2] = e1[0] * e2[1] - e1[1] * e2[0];
-        }
-        for (int q = 0; q < 3; q++) {
-            const double *a = v[q], *b = v[(q + 1) % 3];
-            const double e[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
-            lmax = std::max(lmax, std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]));
-            double n[3] = {nrm[1] * e[2] - nrm[2] * e[1], nrm[2] * e[0] - nrm[0] * e[2], nrm[0] * e[1] - nrm[1] * e[0]};
-            const double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-            for (int c = 0; c < 3; c++) ein[q][c] = l > 0.0 ? n[c] / l : 0.0;
-            eoff[q] = ein[q][0] * a[0] + ein[q][1] * a[1] + ein[q][2] * a[2];
-        }
-        auto inside = [&](long long k) {
-            const float4 p = act_pos[k];
-            for (int q = 0; q < 3; q++)
-                if (!(ein[q][0] * p.x + ein[q][1] * p.y + ein[q][2] * p.z - eoff[q] > 1e-6 * lmax)) return false;
-            return true;
-        };
-        std::vector<int> good, edge;
-        for (const Run &r : part)
-            for (long long k = r.b; k < r.e; k++) (inside(k) ? good : edge).push_back((int)k);
-        const long long ngood = (long long)good.size();
-        const long long need = (kTile - a0 % kTile) % kTile;
-        if (need > ngood) return;  // cannot align: keep patch order
-        std::vector<int> order;
-        order.reserve((size_t)(a1 - a0));
-        order.insert(order.end(), good.end() - need, good.end());
-        for (const Run &r : full)
-            for (long long k = r.b; k < r.e; k++) order.push_back((int)k);
-        order.insert(order.end(), good.begin(), good.end() - need);
-        order.insert(order.end(), edge.begin(), edge.end());
+        const std::vector<int> order = patch_aligned_order(o.facets[f], runs, act_pos + a0, a0);
+        if (order.empty()) return;
         const size_t n = order.size();
         std::vector<float4> pos(n);
         std::vector<int> fac(n), cell(n);
         for (size_t i = 0; i < n; i++) {
-            pos[i] = act_pos[order[i]];
-            fac[i] = act_facet[order[i]];
-            cell[i] = o.act_cell[(size_t)order[i]];
+            pos[i] = act_pos[a0 + order[i]];
+            fac[i] = act_facet[a0 + order[i]];
+            cell[i] = o.act_cell[(size_t)(a0 + order[i])];
         }
         memcpy(act_pos + a0, pos.data(), n * sizeof(float4));
         memcpy(act_facet + a0, fac.data(), n * sizeof(int));
@@ -2320,6 +2259,47 @@ long long sonar_fragment_triangle(const float *tri9, float delta, int *nx_ny_neg
     }
     const long long n = (long long)F.nx * F.ny;
     if (areas && cap >= n) fragment_areas(F, areas);
+    return n;
+}
+
+long long sonar_tile_order(const float *tri9, float delta, long long start, int *xy, long long cap)
+{
+    if (!tri9 || !(delta > 0.0f) || start < 0) return -6;
+    const FacetFrame F =
+        make_frame({tri9[0], tri9[1], tri9[2]}, {tri9[3], tri9[4], tri9[5]}, {tri9[6], tri9[7], tri9[8]}, delta);
+    std::vector<float> area((size_t)std::max(F.nx * F.ny, 1));
+    fragment_areas(F, area.data());
+    // active cells in patch order (patch row, patch column, row-major inside)
+    std::vector<int> cx, cy;
+    std::vector<float4> pos;
+    std::vector<PatchRun> runs;
+    for (int py = 0; py < F.ny; py += kPatch)
+        for (int px = 0; px < F.nx; px += kPatch) {
+            const long long b = (long long)cx.size();
+            for (int y = py; y < std::min(F.ny, py + kPatch); y++)
+                for (int x = px; x < std::min(F.nx, px + kPatch); x++) {
+                    if (!(area[(size_t)y * F.nx + x] > 1e-6f)) continue;
+                    const Vec3 p = fragment_centroid(F, x, y, false);
+                    cx.push_back(x);
+                    cy.push_back(y);
+                    pos.push_back(make_float4(p.x, p.y, p.z, 0.0f));
+                }
+            if ((long long)cx.size() > b) runs.push_back(PatchRun{b, (long long)cx.size(), py / kPatch, px / kPatch});
+        }
+    const long long n = (long long)cx.size();
+    if (n >= 2 * kTile && xy && cap >= n) {
+        const std::vector<int> order = patch_aligned_order(F, runs, pos.data(), start);
+        for (long long i = 0; i < n; i++) {
+            const int k = order.empty() ? (int)i : order[(size_t)i];
+            xy[2 * i] = cx[(size_t)k];
+            xy[2 * i + 1] = cy[(size_t)k];
+        }
+    } else if (xy && cap >= n) {
+        for (long long i = 0; i < n; i++) {
+            xy[2 * i] = cx[(size_t)i];
+            xy[2 * i + 1] = cy[(size_t)i];
+        }
+    }
     return n;
 }
 
