@@ -182,6 +182,7 @@ FUSED = [1]        # k_aca2: the first bounce's low-rank apply fused into the cr
 INTERP = [1]       # far class-ALL blocks between planar tiles by directional interpolation
 BUILD_OVERLAP = [1]  # interpolation build on a second stream beside the cross approximation
 TILE_ALIGN = [1]     # full patches of the fragment grid on 256-fragment tile boundaries
+IP_TRANSPOSE = [0]   # 1: interpolation tiles taller than wide take the grid's y axis first
 
 
 def set_path(api, compressed, select):
@@ -197,6 +198,7 @@ def set_path(api, compressed, select):
     api.set_option("compress_interp", INTERP[0])
     api.set_option("compress_build_overlap", BUILD_OVERLAP[0])
     api.set_option("tile_align", TILE_ALIGN[0])
+    api.set_option("ip_transpose", IP_TRANSPOSE[0])
 
 
 def time_path(api, cfg, args, flush, local, world, reuse=False):
@@ -1258,6 +1260,8 @@ def main():
                     help="compressed bounce: low-rank apply on a second stream beside the dense remainder")
     ap.add_argument("--tile-align", type=int, default=1, choices=(0, 1),
                     help="active fragments: full patches on 256-fragment tile boundaries")
+    ap.add_argument("--ip-transpose", type=int, default=0, choices=(0, 1),
+                    help="interpolation tiles taller than wide take the fragment grid's y axis as the first axis")
     ap.add_argument("--build-overlap", type=int, default=1, choices=(0, 1),
                     help="compressed build: interpolation on a second stream beside the cross approximation")
     ap.add_argument("--tol", type=float, default=5e-4,
@@ -1283,6 +1287,7 @@ def main():
     OVERLAP[0] = args.overlap
     BUILD_OVERLAP[0] = args.build_overlap
     TILE_ALIGN[0] = args.tile_align
+    IP_TRANSPOSE[0] = args.ip_transpose
     FUSED[0] = args.fused_apply
     INTERP[0] = args.interp
     LR_CTAS[0] = args.lr_ctas

@@ -153,6 +153,11 @@ int sonar_get_stats(char *json, int cap);
  * outside the triangle -- come last; 0: plain patch order; the order is
  * internal, outputs are the same up to FP32 summation order; read by
  * render_cuda).
+ * "ip_transpose" (0, default: an interpolation tile's first axis is the
+ * fragment grid's x axis; 1: a tile whose box is taller than wide takes the
+ * grid's y axis first, so that strips of partial patches along a slanted
+ * facet edge fit the 32 x 16-cell box -- more blocks interpolated, no faster
+ * on the 60 kHz trihedral).
  * "overlap_streams" (1, default: a compressed bounce runs its low-rank apply
  * on a second stream beside the dense remainder, joined before the
  * finalize; 0: one stream; the same results either way).

@@ -146,10 +146,13 @@ __device__ __forceinline__ float dot3(float3 x, float3 y) { return fmaf(x.x, y.x
 // One CTA per tile: the tile is capable when every fragment lies on the first
 // fragment's facet and their cells fit a box of 4..32 x 2..16 cells; the box
 // centre's position follows from the first fragment's (the facet's grid is
-// spaced delta along both axes); fxy = the fragment's cell in the box.
+// spaced delta along both axes); fxy = the fragment's cell in the box.  A
+// box taller than wide is transposed (e1 the grid's y axis, e2 its x axis),
+// so that the longer side lies along e1: the strips of partial patches along
+// a facet's slanted edge (16 x 30 cells) fit the box that way.
 __global__ void __launch_bounds__(kTile) k_ip_tiles(const float4 *pos, const float4 *nrm, const int *act_facet,
                                                     const int *act_cell, const float4 *facet_grid, int n,
-                                                    float delta, float4 *tile, uint16_t *fxy)
+                                                    float delta, bool transpose, float4 *tile, uint16_t *fxy)
 {
     __shared__ int s_f, s_bad, s_min[2], s_max[2], s_rlo[kIpMaxBY], s_rhi[kIpMaxBY];
     const int T = blockIdx.x, t = threadIdx.x, i0 = T * kTile, i = i0 + t;
@@ -179,12 +182,15 @@ __global__ void __launch_bounds__(kTile) k_ip_tiles(const float4 *pos, const flo
         atomicMax(&s_max[1], y);
     }
     __syncthreads();
-    const int x0 = s_min[0], y0 = s_min[1], bx = s_max[0] - x0 + 1, by = s_max[1] - y0 + 1;
+    const int x0 = s_min[0], y0 = s_min[1], gx = s_max[0] - x0 + 1, gy = s_max[1] - y0 + 1;
+    const bool tr = transpose && gy > gx;  // CTA-uniform
+    const int bx = tr ? gy : gx, by = tr ? gx : gy;
     const bool cap = !s_bad && bx >= 4 && by >= 2 && bx <= kIpMaxBX && by <= kIpMaxBY;
-    if (v) fxy[i] = cap ? (uint16_t)((x - x0) | ((y - y0) << 8)) : (uint16_t)0;
+    const int cx = tr ? y - y0 : x - x0, cy = tr ? x - x0 : y - y0;  // the cell in the box
+    if (v) fxy[i] = cap ? (uint16_t)(cx | (cy << 8)) : (uint16_t)0;
     if (v && cap) {
-        atomicMin(&s_rlo[y - y0], x - x0);
-        atomicMax(&s_rhi[y - y0], x - x0);
+        atomicMin(&s_rlo[cy], cx);
+        atomicMax(&s_rhi[cy], cx);
     }
     __syncthreads();
     if (t == 0) {
@@ -197,12 +203,13 @@ __global__ void __launch_bounds__(kTile) k_ip_tiles(const float4 *pos, const flo
         R[5] = make_float4(__uint_as_float(w[4]), __uint_as_float(w[5]), __uint_as_float(w[6]), __uint_as_float(w[7]));
         const float4 g0 = facet_grid[2 * s_f], g1 = facet_grid[2 * s_f + 1];
         const float4 p = pos[i0], q = nrm[i0];
-        const float ox = delta * ((float)x0 + 0.5f * (float)(bx - 1) - (float)x);
-        const float oy = delta * ((float)y0 + 0.5f * (float)(by - 1) - (float)y);
+        const float ox = delta * ((float)x0 + 0.5f * (float)(gx - 1) - (float)x);
+        const float oy = delta * ((float)y0 + 0.5f * (float)(gy - 1) - (float)y);
         R[0] = make_float4(fmaf(g1.x, oy, fmaf(g0.x, ox, p.x)), fmaf(g1.y, oy, fmaf(g0.y, ox, p.y)),
                            fmaf(g1.z, oy, fmaf(g0.z, ox, p.z)), cap ? 1.0f : 0.0f);
-        R[1] = make_float4(g0.x, g0.y, g0.z, 0.0f);
-        R[2] = make_float4(g1.x, g1.y, g1.z, 0.0f);
+        const float4 a1 = tr ? g1 : g0, a2 = tr ? g0 : g1;
+        R[1] = make_float4(a1.x, a1.y, a1.z, 0.0f);
+        R[2] = make_float4(a2.x, a2.y, a2.z, 0.0f);
         R[3] = make_float4(q.x, q.y, q.z, __int_as_float(cap ? (bx | (by << 8)) : 0));
     }
 }
@@ -847,11 +854,12 @@ __global__ void __launch_bounds__(kIpThreads) k_ip_audit(SumArgs a, IpArgs ip, c
 }  // namespace
 
 void launch_ip_tiles(const float4 *pos, const float4 *nrm, const int *act_facet, const int *act_cell,
-                     const float4 *facet_grid, int n, float delta, float4 *tile, uint16_t *fxy, cudaStream_t s)
+                     const float4 *facet_grid, int n, float delta, bool transpose, float4 *tile, uint16_t *fxy,
+                     cudaStream_t s)
 {
     if (n > 0)
-        k_ip_tiles<<<(n + kTile - 1) / kTile, kTile, 0, s>>>(pos, nrm, act_facet, act_cell, facet_grid, n, delta, tile,
-                                                            fxy);
+        k_ip_tiles<<<(n + kTile - 1) / kTile, kTile, 0, s>>>(pos, nrm, act_facet, act_cell, facet_grid, n, delta,
+                                                            transpose, tile, fxy);
 }
 
 void launch_ip_level(const int2 *cb, const uint8_t *ccls, const int *ncand, int nmax, const float4 *tile,

@@ -1036,21 +1036,25 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
                 }
             }
             if (use_queue) {
-                // warp-aggregated slots for this lane's pairs to test
-                const int cnt = __popc(tq);
-                int incl = cnt;
+                // one slot range per warp; the warp's pairs in source-major
+                // order (per source bit, the lanes that test it in lane order),
+                // so that the stores here and the tests' bit clears in sW
+                // after the word touch consecutive entries, not one lane's run
+                int tot = __popc(tq);
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += v;
-                }
+                for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
                 int base = 0;
-                if (lane == 31 && incl > 0) base = atomicAdd(&sQn[w & 1], incl);
-                base = __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
-                while (tq) {
-                    const int b = __ffs(tq) - 1;
-                    tq &= tq - 1u;
-                    sQ[base++] = (unsigned short)(((w * 32 + b) << 8) | tid);
+                if (lane == 0 && tot > 0) base = atomicAdd(&sQn[w & 1], tot);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                const unsigned below = (1u << lane) - 1u;
+                unsigned srcs = __reduce_or_sync(0xffffffffu, tq);
+                while (srcs) {  // warp-uniform
+                    const int b = __ffs(srcs) - 1;
+                    srcs &= srcs - 1u;
+                    const bool mine = (tq >> b) & 1u;
+                    const unsigned m = __ballot_sync(0xffffffffu, mine);
+                    if (mine) sQ[base + __popc(m & below)] = (unsigned short)(((w * 32 + b) << 8) | tid);
+                    base += __popc(m);
                 }
             }
         }

@@ -306,6 +306,7 @@ struct Model {
     int opt_overlap = 1;        // compressed bounce: low-rank apply on the second stream beside the dense remainder
     int opt_build_overlap = 1;  // compressed build: interpolated blocks on the second stream beside the cross approximation
     int opt_tile_align = 1;     // active fragments: full patches on 256-fragment tile boundaries (align_patches)
+    int opt_ip_transpose = 0;   // interpolation tile frames: boxes taller than wide transposed (k_ip_tiles)
     int scene_convex = 0;       // every target vertex on or behind every target triangle's plane
     float scene_vmax = 0.0f;    // largest |coordinate| of the target vertices
     Compression cmp;
@@ -999,7 +1000,7 @@ void build_compression(int a, MaskEntry &M, const SumArgs &s)
         C.ip.tile = ar.take<float4>((size_t)kIpTileRec * nt);
         uint16_t *fxy = ar.take<uint16_t>(M.nsrc);
         launch_ip_tiles(g.d_packA, g.d_packB, A.d_act_facet, A.d_act_cell, A.d_facet_grid, M.nsrc, A.delta,
-                        const_cast<float4 *>(C.ip.tile), fxy, st);
+                        g.opt_ip_transpose != 0, const_cast<float4 *>(C.ip.tile), fxy, st);
         C.ip.fxy = fxy;
         C.ip.delta = A.delta;
         C.ip.status = ar.take<int>(1);
@@ -1939,6 +1940,11 @@ int sonar_set_option(const char *key, double value)
     }
     if (!strcmp(key, "tile_align")) {
         g.opt_tile_align = value != 0.0 ? 1 : 0;
+        return 0;
+    }
+    if (!strcmp(key, "ip_transpose")) {
+        g.opt_ip_transpose = value != 0.0 ? 1 : 0;
+        g.cmp.release();
         return 0;
     }
     if (!strcmp(key, "compress_build_overlap")) {

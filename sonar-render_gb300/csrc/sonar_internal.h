@@ -213,7 +213,8 @@ struct IpCtx {
 };
 // facet_grid: per facet (xAxis, nx as int bits), (yAxis, first cell as int bits)
 void launch_ip_tiles(const float4 *pos, const float4 *nrm, const int *act_facet, const int *act_cell,
-                     const float4 *facet_grid, int n, float delta, float4 *tile, uint16_t *fxy, cudaStream_t s);
+                     const float4 *facet_grid, int n, float delta, bool transpose, float4 *tile, uint16_t *fxy,
+                     cudaStream_t s);
 // levels of the candidates (ncand: their count on the device, nmax bounds the grid)
 void launch_ip_level(const int2 *cb, const uint8_t *ccls, const int *ncand, int nmax, const float4 *tile,
                      float delta, float kr, float tol, uint8_t *lev, cudaStream_t s);
