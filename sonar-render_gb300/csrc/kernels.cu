@@ -1110,7 +1110,7 @@ struct WarpRange {
 };
 
 
-__global__ void __launch_bounds__(32 * kClsWarps) k_mask_classify_f2f(MaskArgs a, int2 *blist, int *count)
+__global__ void __launch_bounds__(32 * kClsWarps, 3) k_mask_classify_f2f(MaskArgs a, int2 *blist, int *count)
 {
     __shared__ int sCand[kClsWarps][kMaxCand];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -2877,30 +2877,53 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
     s = t;
 }
 
-// One CTA of 2 x 256 threads per tile X: the first 256 threads add the row
-// outputs of the blocks (., X) into yrow, the other 256 the column outputs of
-// the blocks (X, .) into ycol, each in list order (compensated FP32, FP64 at
-// the end).  The two lists are independent chains of loads, so splitting them
-// halves the dependent work per thread.
-__global__ void __launch_bounds__(2 * kTile) k_lr_gather(int n, const float2 *brow, const float2 *bcol,
-                                                         const int *byJ_off, const int *byJ, const int *byI_off,
-                                                         const int *byI, const int *bidx, double2 *yrow,
-                                                         double2 *ycol)
+// One CTA of kGatherSeg x 256 threads per tile X.  The tile's two lists --
+// the blocks (., X), whose row outputs add into yrow, then the blocks (X, .),
+// whose column outputs add into ycol -- are read as one sequence cut into
+// kGatherSeg equal segments, one per 256-thread group; thread t of a group
+// adds entry t of its segment's blocks in list order (compensated FP32) and
+// the groups' sums are added in group order in FP64.  With upper-triangular
+// block sets the two lists of tile X hold about X and ntiles - X blocks, so
+// the cut bounds every thread's chain of loads by a quarter of both.
+constexpr int kGatherSeg = 4;
+
+__global__ void __launch_bounds__(kGatherSeg * kTile, 2) k_lr_gather(int n, const float2 *brow, const float2 *bcol,
+                                                                     const int *byJ_off, const int *byJ,
+                                                                     const int *byI_off, const int *byI,
+                                                                     const int *bidx, double2 *yrow, double2 *ycol)
 {
-    const int X = blockIdx.x, t = threadIdx.x & (kTile - 1);
-    const bool cols = threadIdx.x >= kTile;  // warp-uniform
-    const int q = X * kTile + t;
-    const int p0 = cols ? byI_off[X] : byJ_off[X], p1 = cols ? byI_off[X + 1] : byJ_off[X + 1];
-    const int *list = cols ? byI : byJ;
-    const float2 *src = cols ? bcol : brow;
+    __shared__ double2 part[2][kGatherSeg][kTile];  // [rows, columns][group][t]
+    const int X = blockIdx.x, t = threadIdx.x & (kTile - 1), g = threadIdx.x / kTile;  // g warp-uniform
+    const int r0 = byJ_off[X], nr = byJ_off[X + 1] - r0, c0 = byI_off[X], nc = byI_off[X + 1] - c0;
+    const int L = nr + nc, p0 = (int)((long long)L * g / kGatherSeg), p1 = (int)((long long)L * (g + 1) / kGatherSeg);
+    const int pm = min(max(nr, p0), p1);  // [p0, pm): rows, [pm, p1): columns
     float fr = 0.0f, fi = 0.0f, efr = 0.0f, efi = 0.0f;
-#pragma unroll 4
-    for (int p = p0; p < p1; ++p) {
-        const float2 v = __ldg(src + (size_t)bidx[list[p]] * kTile + t);
+#pragma unroll 8
+    for (int p = p0; p < pm; ++p) {
+        const float2 v = __ldg(brow + (size_t)bidx[byJ[r0 + p]] * kTile + t);
         kahan_add(fr, efr, v.x);
         kahan_add(fi, efi, v.y);
     }
-    if (q < n) (cols ? ycol : yrow)[q] = make_double2((double)fr - (double)efr, (double)fi - (double)efi);
+    part[0][g][t] = make_double2((double)fr - (double)efr, (double)fi - (double)efi);
+    fr = fi = efr = efi = 0.0f;
+#pragma unroll 8
+    for (int p = pm; p < p1; ++p) {
+        const float2 v = __ldg(bcol + (size_t)bidx[byI[c0 + p - nr]] * kTile + t);
+        kahan_add(fr, efr, v.x);
+        kahan_add(fi, efi, v.y);
+    }
+    part[1][g][t] = make_double2((double)fr - (double)efr, (double)fi - (double)efi);
+    __syncthreads();
+    const int q = X * kTile + t;
+    if (g < 2 && q < n) {
+        double2 y = part[g][0][t];
+#pragma unroll
+        for (int k = 1; k < kGatherSeg; ++k) {
+            y.x += part[g][k][t].x;
+            y.y += part[g][k][t].y;
+        }
+        (g ? ycol : yrow)[q] = y;
+    }
 }
 
 // Per-tile geometry for block descriptors: centroid, radius, mean normal.
@@ -3363,7 +3386,8 @@ void launch_lr_apply(const SumArgs &a, const int2 *blocks, const long long *off,
                             ip->list, ip->n, rank, ip->status);
     }
     if (ntiles > 0)
-        k_lr_gather<<<ntiles, 2 * kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, bidx, yrow, ycol);
+        k_lr_gather<<<ntiles, kGatherSeg * kTile, 0, s>>>(a.nsrc, brow, bcol, byJ_off, byJ, byI_off, byI, bidx, yrow,
+                                                          ycol);
 }
 
 void launch_tile_stats(const float4 *pos, const float4 *nrm, int n, float4 *cen, float4 *nmean, cudaStream_t s)
