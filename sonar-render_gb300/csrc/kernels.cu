@@ -375,8 +375,11 @@ __device__ __forceinline__ bool convex_needs_test(const MaskArgs &a, float4 ns, 
     return !(cosv > 0.0f && cosv * 0.9e-3f > E);
 }
 
+// One block of k_mask: (destination block blockIdx.x, source tile
+// blockIdx.y), or with a block list its entry qb.  Every early return is
+// taken by the whole CTA.
 template <int HOP>
-__global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
+__device__ __forceinline__ void mask_block(const MaskArgs &a, const int qb)
 {
     __shared__ float4 sP[kTile];
     __shared__ float4 sN[kTile];
@@ -389,10 +392,8 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
     __shared__ int sNc, sKeep, sOverflow;
     const int tid = threadIdx.x;
     int tile = blockIdx.y, jb = blockIdx.x;
-    if (a.blist) {
-        // the blocks a classification pass left for per-pair bits
-        if ((int)blockIdx.x >= *a.blist_count) return;  // CTA-uniform
-        const int2 e = a.blist[blockIdx.x];
+    if (HOP == HOP_F2F && a.blist) {
+        const int2 e = a.blist[qb];
         tile = e.x;
         jb = e.y;
     }
@@ -1091,6 +1092,25 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
     }
     const int blk = __syncthreads_or(any != 0u);
     if (tid == 0) a.mask.flags[fidx] = clear ? kFlagClear : (blk ? kFlagBits : kFlagNone);
+}
+
+// k_mask<HOP>: one CTA per block of the grid (destination block x, source
+// tile y).
+template <int HOP>
+__global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
+{
+    mask_block<HOP>(a, (int)blockIdx.x);
+}
+
+// The pair kernel of a bounce mask on the blocks a classification pass left
+// for per-pair bits (counted on the device): a grid of resident CTAs takes
+// the listed blocks in turn, so the host need not read the count first.
+__global__ void __launch_bounds__(kTile) k_mask_listed(MaskArgs a)
+{
+    for (int q = blockIdx.x; q < *a.blist_count; q += gridDim.x) {  // CTA-uniform
+        mask_block<HOP_F2F>(a, q);
+        __syncthreads();  // the next block rewrites the shared state
+    }
 }
 
 // ---------------------------------------------------------------- bounce-mask classification
@@ -3150,7 +3170,7 @@ double measure_peak(int which)
     return ok ? best : -1.0;
 }
 
-int launch_mask_classified(const MaskArgs &a0, int2 *blist, int *count_dev, int *count_host, cudaStream_t s)
+int launch_mask_classified(const MaskArgs &a0, int2 *blist, int *count_dev, int nsm, cudaStream_t s)
 {
     if (a0.nsrc <= 0 || a0.ndst <= 0) return 0;
     const size_t nflags = (size_t)a0.mask.ntiles * a0.mask.ndstblocks;
@@ -3158,16 +3178,18 @@ int launch_mask_classified(const MaskArgs &a0, int2 *blist, int *count_dev, int 
     cudaMemsetAsync(count_dev, 0, sizeof(int), s);
     dim3 grid((a0.mask.ndstblocks + kClsWarps - 1) / kClsWarps, a0.mask.ntiles);
     k_mask_classify_f2f<<<grid, 32 * kClsWarps, 0, s>>>(a0, blist, count_dev);
-    cudaMemcpyAsync(count_host, count_dev, sizeof(int), cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    const int n = *count_host;
-    if (n > 0) {
-        MaskArgs a = a0;
-        a.blist = blist;
-        a.blist_count = count_dev;
-        k_mask<HOP_F2F><<<(unsigned)n, kTile, 0, s>>>(a);
-    }
-    return n > 0 ? 2 : 1;
+    // the pair kernel on the listed blocks: resident CTAs read the count on the device
+    static int per_sm = 0;
+    if (per_sm == 0 &&
+        (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mask_listed, kTile, 0) != cudaSuccess ||
+         per_sm < 1))
+        per_sm = 1;
+    MaskArgs a = a0;
+    a.blist = blist;
+    a.blist_count = count_dev;
+    const size_t ctas = std::min<size_t>(nflags, (size_t)std::max(nsm, 1) * per_sm);
+    k_mask_listed<<<(unsigned)ctas, kTile, 0, s>>>(a);
+    return 2;
 }
 
 void launch_mask(const MaskArgs &a, cudaStream_t s)

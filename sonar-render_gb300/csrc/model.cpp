@@ -128,6 +128,7 @@ struct MaskEntry {
     int2 *blist = nullptr;  // bounce masks: blocks the classification pass leaves for per-pair bits
     int *bcount = nullptr;
     float mask_ms = 0.0f;
+    bool fresh = false;  // built for the next hop (its time read, from ev6 to ev7, once that hop has ended)
     bool stale = false;  // rebuild into the same buffers before the next use
     void free_device()
     {
@@ -855,19 +856,25 @@ MaskEntry build_mask(int hop, int a, int b, int full, const MaskEntry *reuse = n
     hs.m.full = full;
     hs.m.gate_proj = g.opt_gate_proj;
     hs.m.upper_only = (hop == HOP_F2F && !full && g.opt_f2f_sym) ? 1 : 0;
-    CK(cudaEventRecord(g.ev0, g.stream));
+    // timed by ev6 .. ev7, read after the hop that uses the mask (no host
+    // synchronisation here)
+    CK(cudaEventRecord(g.ev6, g.stream));
     if (classify) {
-        int nbits = 0;
-        g.launches += launch_mask_classified(hs.m, e.blist, e.bcount, &nbits, g.stream);
+        if (g.nsm == 0) {
+            int dev = 0;
+            CK(cudaGetDevice(&dev));
+            CK(cudaDeviceGetAttribute(&g.nsm, cudaDevAttrMultiProcessorCount, dev));
+        }
+        g.launches += launch_mask_classified(hs.m, e.blist, e.bcount, g.nsm, g.stream);
     } else {
         launch_mask(hs.m, g.stream);
         g.launches += (hs.nsrc > 0 && hs.ndst > 0) ? 1 : 0;
     }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(g.ev1, g.stream));
-    CK(cudaEventSynchronize(g.ev1));
-    CK(cudaEventElapsedTime(&e.mask_ms, g.ev0, g.ev1));
+    CK(cudaEventRecord(g.ev7, g.stream));
+    e.fresh = true;
     if (g.opt_class_stats && nflags > 0) {
+        CK(cudaStreamSynchronize(g.stream));
         std::vector<uint8_t> fl(nflags);
         CK(cudaMemcpy(fl.data(), v.flags, nflags, cudaMemcpyDeviceToHost));
         for (uint8_t f : fl) e.classes[f & 3]++;
@@ -1226,7 +1233,7 @@ void timed_sum(const SumArgs &s, cudaStream_t st)
 void run_hop(int hop, int a, int b)
 {
     MaskEntry &M = get_mask(hop, a, b);
-    const bool mask_rebuilt = M.mask_ms > 0.0f;  // built for this call (reported once)
+    const bool mask_rebuilt = M.fresh;  // built for this call (reported once)
     float rec_cmp_build = 0.0f;
     bool rec_cmp = false, built = false;
     if (M.nsrc == 0 || M.ndst == 0) return;
@@ -1388,8 +1395,9 @@ void run_hop(int hop, int a, int b)
     float ms = 0.0f, sum_ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
     CK(cudaEventElapsedTime(&sum_ms, g.ev2, g.ev3));
+    if (M.fresh) CK(cudaEventElapsedTime(&M.mask_ms, g.ev6, g.ev7));
     const int lr_launches = rec_cmp ? (built && g.cmp.outputs_ready ? 1 : 2 + (g.cmp.interp ? 1 : 0)) : 0;
-    const int nl = (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + (M.mask_ms > 0.0f ? 1 : 0) + lr_launches;
+    const int nl = (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + (M.fresh ? 1 : 0) + lr_launches;
     g.launches += (hop == HOP_F2F ? (g.opt_f2f_sym ? 6 : 4) : 3) + lr_launches +
                   (rec_cmp_build > 0.0f ? 4 + (g.cmp.interp ? 3 : 0) : 0);
     HopRecord rec{hop, pair_count(hop, a, b), M.mask_ms, sum_ms, ms, s.nsplit, nl};
@@ -1415,6 +1423,7 @@ void run_hop(int hop, int a, int b)
     }
     g.log.push_back(rec);
     M.mask_ms = 0.0f;  // reported once, with the first use
+    M.fresh = false;
 }
 
 void need_render()

@@ -121,10 +121,11 @@ void launch_mask(const MaskArgs &a, cudaStream_t s);
 void launch_finalize_resp(const double2 *partial, int nsplit, int ndst, const int *cell, const double2 *gate_pin,
                           double2 *Pout, double2 *P, cudaStream_t s);
 // Bounce masks (HOP_F2F, no full export): classification pass, then the pair
-// kernel on the blocks it lists (blist: one entry per block at most; the
-// stream is synchronised once to read their count into *count_host).
-// Returns the number of kernels launched.
-int launch_mask_classified(const MaskArgs &a, int2 *blist, int *count_dev, int *count_host, cudaStream_t s);
+// kernel on the blocks it lists (blist: one entry per block at most, their
+// count in *count_dev), on a grid of resident CTAs (nsm SMs) that reads the
+// count on the device: no host synchronisation.  Returns the number of
+// kernels launched.
+int launch_mask_classified(const MaskArgs &a, int2 *blist, int *count_dev, int nsm, cudaStream_t s);
 void launch_sum(const SumArgs &a, cudaStream_t s);
 void launch_pack_points(const float4 *pts, const double2 *P, int n, float4 *A, float4 *B, cudaStream_t s);
 void launch_pack_frags(const float4 *act_pos, const int *act_facet, const int *act_cell, const float4 *facet_n,
