@@ -174,7 +174,7 @@ def step_pairs(stats):
 
 
 RCUT = [32.0]  # the admissibility network proposes blocks with predicted rank below this
-TOL = [5e-4]   # cross-approximation tolerance (the judge accepts 3 x this RMS error)
+TOL = [7e-4]   # cross-approximation tolerance (the judge accepts 3 x this RMS error)
 ACA_VARIANT = [8]  # cross-approximation kernel shape (k_aca / k_aca2, factor ranks in shared memory, CTAs per SM)
 OVERLAP = [1]      # compressed bounce: low-rank apply on a second stream beside the dense remainder
 LR_CTAS = [4]      # low-rank apply: resident CTAs per SM (register cap)
@@ -1264,9 +1264,9 @@ def main():
                     help="interpolation tiles taller than wide take the fragment grid's y axis as the first axis")
     ap.add_argument("--build-overlap", type=int, default=1, choices=(0, 1),
                     help="compressed build: interpolation on a second stream beside the cross approximation")
-    ap.add_argument("--tol", type=float, default=5e-4,
+    ap.add_argument("--tol", type=float, default=7e-4,
                     help="cross-approximation tolerance of the compressed path (judge limit 3 x tol); the "
-                         "default keeps the step's error about 5x below the 1e-3 target")
+                         "default keeps the step's error about 3x below the 1e-3 target (5e-4: about 4x)")
     ap.add_argument("--rcut", type=float, default=32.0,
                     help="network: propose blocks whose predicted rank is below this")
     ap.add_argument("--select", type=int, default=2,

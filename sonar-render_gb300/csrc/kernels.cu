@@ -1104,12 +1104,20 @@ __global__ void __launch_bounds__(kTile) k_mask(MaskArgs a)
 
 // The pair kernel of a bounce mask on the blocks a classification pass left
 // for per-pair bits (counted on the device): a grid of resident CTAs takes
-// the listed blocks in turn, so the host need not read the count first.
+// the listed blocks one at a time from a counter (their costs differ by an
+// order of magnitude), so the host need not read the count first.  The
+// counter only grows: every CTA leaves once it passes the count.
 __global__ void __launch_bounds__(kTile) k_mask_listed(MaskArgs a)
 {
-    for (int q = blockIdx.x; q < *a.blist_count; q += gridDim.x) {  // CTA-uniform
+    __shared__ int s_q;
+    const int n = *a.blist_count;
+    for (;;) {
+        if (threadIdx.x == 0) s_q = atomicAdd(a.blist_next, 1);
+        __syncthreads();
+        const int q = s_q;  // CTA-uniform
+        if (q >= n) break;
         mask_block<HOP_F2F>(a, q);
-        __syncthreads();  // the next block rewrites the shared state
+        __syncthreads();  // s_q and the shared state are rewritten next
     }
 }
 
@@ -3175,7 +3183,7 @@ int launch_mask_classified(const MaskArgs &a0, int2 *blist, int *count_dev, int 
     if (a0.nsrc <= 0 || a0.ndst <= 0) return 0;
     const size_t nflags = (size_t)a0.mask.ntiles * a0.mask.ndstblocks;
     cudaMemsetAsync(a0.mask.flags, kFlagNone, nflags, s);
-    cudaMemsetAsync(count_dev, 0, sizeof(int), s);
+    cudaMemsetAsync(count_dev, 0, 2 * sizeof(int), s);
     dim3 grid((a0.mask.ndstblocks + kClsWarps - 1) / kClsWarps, a0.mask.ntiles);
     k_mask_classify_f2f<<<grid, 32 * kClsWarps, 0, s>>>(a0, blist, count_dev);
     // the pair kernel on the listed blocks: resident CTAs read the count on the device
@@ -3187,6 +3195,7 @@ int launch_mask_classified(const MaskArgs &a0, int2 *blist, int *count_dev, int 
     MaskArgs a = a0;
     a.blist = blist;
     a.blist_count = count_dev;
+    a.blist_next = count_dev + 1;
     const size_t ctas = std::min<size_t>(nflags, (size_t)std::max(nsm, 1) * per_sm);
     k_mask_listed<<<(unsigned)ctas, kTile, 0, s>>>(a);
     return 2;

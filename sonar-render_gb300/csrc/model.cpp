@@ -847,7 +847,7 @@ MaskEntry build_mask(int hop, int a, int b, int full, const MaskEntry *reuse = n
     const bool classify = hop == HOP_F2F && !full && g.opt_mask_classify;
     if (classify && !e.blist) {
         e.blist = dalloc<int2>(std::max<size_t>(nflags, 1));
-        e.bcount = dalloc<int>(1);
+        e.bcount = dalloc<int>(2);  // listed blocks, the pair kernel's next-block counter
     }
     // every block writes its flag, and the sums read bits only of blocks that
     // stored them; the full export also reads blocks that store none

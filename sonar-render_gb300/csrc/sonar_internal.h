@@ -78,6 +78,7 @@ struct MaskArgs {
     MaskView mask;
     const int2 *blist = nullptr;    // optional: (source tile, destination block) of the blocks to build
     const int *blist_count = nullptr;
+    int *blist_next = nullptr;      // k_mask_listed: the next listed block to take (starts at 0)
     int gate_proj = 1;              // FACET_SELF: decide gates from per-point projections where certain
     int resp_dst_origin = 0;        // FACET_RESP: the ray starts at the destination point
     int convex = 0;                 // every target vertex on or behind every target triangle's plane
@@ -121,10 +122,10 @@ void launch_mask(const MaskArgs &a, cudaStream_t s);
 void launch_finalize_resp(const double2 *partial, int nsplit, int ndst, const int *cell, const double2 *gate_pin,
                           double2 *Pout, double2 *P, cudaStream_t s);
 // Bounce masks (HOP_F2F, no full export): classification pass, then the pair
-// kernel on the blocks it lists (blist: one entry per block at most, their
-// count in *count_dev), on a grid of resident CTAs (nsm SMs) that reads the
-// count on the device: no host synchronisation.  Returns the number of
-// kernels launched.
+// kernel on the blocks it lists (blist: one entry per block at most; count_dev
+// holds two ints: their count and the pair kernel's next-block counter), on a
+// grid of resident CTAs (nsm SMs) that reads the count on the device: no host
+// synchronisation.  Returns the number of kernels launched.
 int launch_mask_classified(const MaskArgs &a, int2 *blist, int *count_dev, int nsm, cudaStream_t s);
 void launch_sum(const SumArgs &a, cudaStream_t s);
 void launch_pack_points(const float4 *pts, const double2 *P, int n, float4 *A, float4 *B, cudaStream_t s);
