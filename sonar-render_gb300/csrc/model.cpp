@@ -857,8 +857,9 @@ MaskEntry build_mask(int hop, int a, int b, int full, const MaskEntry *reuse = n
     hs.m.gate_proj = g.opt_gate_proj;
     hs.m.upper_only = (hop == HOP_F2F && !full && g.opt_f2f_sym) ? 1 : 0;
     // timed by ev6 .. ev7, read after the hop that uses the mask (no host
-    // synchronisation here)
-    CK(cudaEventRecord(g.ev6, g.stream));
+    // synchronisation here); full exports are not timed, so that they leave
+    // the events of a mask built for the next hop alone
+    if (!full) CK(cudaEventRecord(g.ev6, g.stream));
     if (classify) {
         if (g.nsm == 0) {
             int dev = 0;
@@ -871,8 +872,10 @@ MaskEntry build_mask(int hop, int a, int b, int full, const MaskEntry *reuse = n
         g.launches += (hs.nsrc > 0 && hs.ndst > 0) ? 1 : 0;
     }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(g.ev7, g.stream));
-    e.fresh = true;
+    if (!full) {
+        CK(cudaEventRecord(g.ev7, g.stream));
+        e.fresh = true;
+    }
     if (g.opt_class_stats && nflags > 0) {
         CK(cudaStreamSynchronize(g.stream));
         std::vector<uint8_t> fl(nflags);
