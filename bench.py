@@ -422,7 +422,7 @@ def ip_roofline(stats, fp32_peak):
 def e2e_path(api, cfg, args, world, pairs_step):
     import torch
     api.TearDownCuda()
-    e2e_times = []
+    e2e_times, render_ms = [], []
     h2d = d2h = 0
     npts = 0 if cfg.get("field_points") is None else len(cfg["field_points"])
     for k in range(max(1, min(args.steps, 3)) + 1):
@@ -438,10 +438,15 @@ def e2e_path(api, cfg, args, world, pairs_step):
         if k > 0:  # the first one warms the host allocator and the driver
             e2e_times.append(t1 - t0)
             h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+            render_ms.append(st.get("render_host_ms") or {})
         api.TearDownCuda()
     e2e_s = statistics.median(e2e_times)
+    # host time of render_cuda inside the step (facet frames, fragment grids and
+    # areas, tile order, uploads), median over the steps per part
+    parts = sorted({p for r in render_ms for p in r})
+    host = {p: round(statistics.median([float(r.get(p, 0.0)) for r in render_ms]), 4) for p in parts}
     return {"value": pairs_step * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "s_per_step": round(e2e_s, 4)}
+            "d2h_bytes_per_step": int(d2h), "s_per_step": round(e2e_s, 4), "render_host_ms": host}
 
 
 def batch_leg(args, flush, rank):
