@@ -74,3 +74,65 @@ def test_tile_order_edge_cells_last_and_partial_tiles_compact(api, scenes):
     print("partial tiles: %d, boxes %s" % (len(boxes), sorted(set(boxes))))
     assert len(boxes) > 5
     assert all(bx <= 48 and by <= 48 for bx, by in boxes)
+
+
+def _patch_order(nx, area):
+    """The active cells in patch order (patch row, patch column, rows inside)."""
+    ny = area.shape[0]
+    out = []
+    for py in range(0, ny, 16):
+        for px in range(0, nx, 16):
+            for y in range(py, min(ny, py + 16)):
+                for x in range(px, min(nx, px + 16)):
+                    if area[y, x] > 1e-6:
+                        out.append((x, y))
+    return np.array(out, np.int32).reshape(-1, 2)
+
+
+_SHAPES = {
+    "acute": ([0, 0, 0, 1, 0, 0, 0.3, 0.8, 0], 40e3),
+    "tilted": ([0, 0, 0, 0.6, 0.2, 0.5, 0.1, 0.9, 0.3], 40e3),
+    "obtuse": ([0, 0, 0, 1.2, 0, 0, 1.5, 0.4, 0.1], 30e3),
+    "sliver": ([0, 0, 0, 1, 0, 0, 0.5, 0.02, 0], 40e3),
+    "long sliver": ([0, 0, 0, 2.5, 0, 0, 1.2, 0.02, 0], 40e3),
+    "small": ([0, 0, 0, 0.05, 0, 0, 0, 0.05, 0], 40e3),
+}
+
+
+@pytest.mark.parametrize("shape", sorted(_SHAPES))
+@pytest.mark.parametrize("start", [0, 77, 300])
+def test_tile_order_any_triangle(api, scenes, shape, start):
+    """Any triangle: a permutation of the active cells; with a full patch, at
+    least 512 cells and enough partial cells inside the triangle to fill the
+    first tile, every full patch is one tile and the partial cells whose
+    readout centroid is on or outside the triangle come last; otherwise the
+    patch order stays."""
+    tri, f = _SHAPES[shape]
+    d = float(np.float32(scenes.delta_for(f)))
+    (nx, ny, neg), fr, area = api.fragment_triangle(tri, d)
+    xy = api.tile_order(tri, d, start)
+    po = _patch_order(nx, area)
+    assert len(xy) == len(po)
+    assert set(map(tuple, xy)) == set(map(tuple, po))
+    pid = (po[:, 1] // 16) * ((nx + 15) // 16) + po[:, 0] // 16
+    counts = np.bincount(pid) if len(pid) else np.zeros(0, int)
+    full_cell = counts[pid] == 256 if len(pid) else np.zeros(0, bool)
+    inside = _inside(tri, _readout(fr, neg, d, po))
+    need = (256 - start % 256) % 256
+    ngood = int((~full_cell & inside).sum())
+    aligned = full_cell.any() and (~full_cell).any() and len(po) >= 512 and ngood >= need
+    print("%s start %d: %d cells, %d full patches, %d good partial cells, aligned %s"
+          % (shape, start, len(po), int(full_cell.sum()) // 256, ngood, aligned))
+    if not aligned:
+        assert np.array_equal(xy, po)
+        return
+    # every full patch is exactly one tile of the global index space
+    pid_xy = (xy[:, 1] // 16) * ((nx + 15) // 16) + xy[:, 0] // 16
+    for p in np.flatnonzero(counts == 256):
+        at = np.flatnonzero(pid_xy == p)
+        assert len(at) == 256 and at[-1] - at[0] == 255 and (start + at[0]) % 256 == 0
+    # the partial cells on or outside the triangle come last
+    edge = set(map(tuple, po[~full_cell & ~inside]))
+    ne = len(edge)
+    if ne:
+        assert set(map(tuple, xy[len(xy) - ne:])) == edge
